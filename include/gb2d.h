@@ -1,0 +1,234 @@
+/*
+ * gb2d.h -- C ABI of the GB300 world-step library (libgb2d.so).
+ *
+ * The library replaces the body of pypybox2d's World.step(dt, vel_iters,
+ * pos_iters) (pypybox2d/world.py:307-354) for one world or for a batch of
+ * independent worlds.  Everything that step touches -- contact update
+ * (contact_manager.py:174-223), island solve (world.py:475-592,
+ * island.py:65-179), fixture synchronisation and pair finding
+ * (body.py:879-885, fixture.py:287-298, broadphase.py:83-109,
+ * contact_manager.py:102-158) and continuous collision (world.py:594-821) --
+ * runs in sm_103a kernels.  The host side (Python, pypybox2d_gb300) keeps the
+ * reference's World/Body/Fixture API and talks to the library only through
+ * the plain structs and functions below: no PyTorch types, host pointers and
+ * sizes only.
+ *
+ * Conventions
+ *   - every function returns 0 on success, a negative GB_E* code on error;
+ *     gb_last_error() returns a message for the calling thread's last error.
+ *   - all indices inside a world are world-local (body 0 is the first body
+ *     of that world).  Fixtures of one body are contiguous and ordered as the
+ *     body's fixture list; the fixture index is also the broad-phase proxy id.
+ *   - host master copies are float64; GB_PREC_F64 keeps every device
+ *     quantity in float64 (bit-exact with the CPU restatement),
+ *     GB_PREC_F32 keeps body position/angle, sweep, sleep timers and the
+ *     GJK/TOI iteration in float64 and the rest in float32.
+ */
+#ifndef GB2D_H
+#define GB2D_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* shape type ids, as pypybox2d/shapes.py:884-890 */
+#define GB_SHAPE_CIRCLE 0
+#define GB_SHAPE_POLYGON 1
+#define GB_SHAPE_LOOP 2
+#define GB_SHAPE_EDGE 3
+#define GB_MAX_POLY_VERTS 8
+
+/* body types, as pypybox2d/body.py:17-19 */
+#define GB_BODY_STATIC 0
+#define GB_BODY_DYNAMIC 1
+#define GB_BODY_KINEMATIC 2
+
+/* gb_body.flags */
+#define GB_BODY_AWAKE 1u
+#define GB_BODY_ALLOW_SLEEP 2u
+#define GB_BODY_BULLET 4u
+#define GB_BODY_FIXED_ROTATION 8u
+#define GB_BODY_ACTIVE 16u
+
+/* gb_fixture.flags */
+#define GB_FIX_SENSOR 1u
+#define GB_FIX_EDGE_HAS_V0 2u /* edge vertex0 present (vx[2],vy[2]) */
+#define GB_FIX_EDGE_HAS_V3 4u /* edge vertex3 present (vx[3],vy[3]) */
+
+/* gb_contact.flags, as the Contact._*_flag attributes of contact.py:75-87 */
+#define GB_C_TOUCHING 1u
+#define GB_C_ENABLED 2u
+#define GB_C_FILTER 4u
+#define GB_C_ISLAND 8u
+#define GB_C_TOI 16u
+#define GB_C_BULLET_HIT 32u
+
+/* manifold types, as contact_util.py:140-142 */
+#define GB_M_CIRCLES 0
+#define GB_M_FACE_A 1
+#define GB_M_FACE_B 2
+
+/* gb_world_desc.flags, as World attributes of world.py:65-86 */
+#define GB_W_ALLOW_SLEEP 1u
+#define GB_W_WARM_STARTING 2u
+#define GB_W_CONTINUOUS 4u
+#define GB_W_AUTO_CLEAR_FORCES 8u
+#define GB_W_NEW_FIXTURE 16u   /* pair finding over every proxy before the next step */
+#define GB_W_STEP_COMPLETE 32u
+
+/* precision modes */
+#define GB_PREC_F64 0
+#define GB_PREC_F32 1
+
+/* error codes (also OR-ed into the per-world device status word) */
+#define GB_OK 0
+#define GB_E_ARG (-1)
+#define GB_E_CUDA (-2)
+#define GB_E_CONTACT_OVERFLOW (-3)
+#define GB_E_UNSUPPORTED (-4)
+#define GB_E_NONFINITE (-5)
+#define GB_E_ITER_LIMIT (-6)
+#define GB_E_SCRATCH (-7)
+
+/* world status bits reported by gb_batch_status */
+#define GB_ST_CONTACT_OVERFLOW 1u
+#define GB_ST_NONFINITE 2u
+#define GB_ST_ITER_LIMIT 4u
+#define GB_ST_PAIR_OVERFLOW 8u
+#define GB_ST_TOI_ISLAND_CAP 16u
+
+/* One rigid body: the state of pypybox2d.Body (body.py:46-84). */
+typedef struct gb_body {
+    int32_t type;            /* GB_BODY_* */
+    uint32_t flags;          /* GB_BODY_* flags */
+    int32_t fixture_start;   /* world-local index of the first fixture */
+    int32_t fixture_count;
+    double px, py;           /* _xf.position */
+    double qc, qs;           /* _xf rotation: col1 = (qc, qs), col2 = (-qs, qc) */
+    double lcx, lcy;         /* _sweep.local_center */
+    double c0x, c0y, cx, cy; /* _sweep.c0, _sweep.c */
+    double a0, a, alpha0;    /* _sweep.a0, _sweep.a, _sweep.alpha0 */
+    double vx, vy, w;        /* _linear_velocity, _angular_velocity */
+    double fx, fy, torque;   /* _force, _torque */
+    double mass, inv_mass, I, inv_I;
+    double linear_damping, angular_damping, gravity_scale;
+    double sleep_time;
+} gb_body;
+
+/* One fixture with its shape and its single broad-phase proxy
+ * (fixture.py:42-71, shapes.py).  Polygons store vertices and the unit edge
+ * normals computed by the Polygon vertex setter (shapes.py:442-482); a circle
+ * stores its centre in (vx[0], vy[0]); an edge stores vertex1/vertex2 in
+ * slots 0/1 and the optional vertex0/vertex3 in slots 2/3. */
+typedef struct gb_fixture {
+    int32_t body;            /* world-local body index */
+    int32_t shape_type;      /* GB_SHAPE_* */
+    int32_t vertex_count;
+    uint32_t flags;          /* GB_FIX_* */
+    double radius;
+    double friction, restitution, density;
+    uint32_t category_bits, mask_bits;
+    int32_t group_index, _pad0;
+    double vx[GB_MAX_POLY_VERTS], vy[GB_MAX_POLY_VERTS];
+    double nx[GB_MAX_POLY_VERTS], ny[GB_MAX_POLY_VERTS];
+    double aabb[4];          /* fat AABB of the proxy: lower x, lower y, upper x, upper y */
+} gb_fixture;
+
+/* One contact (contact.py:55-87) with its manifold (contact_util.py:120-155).
+ * Contacts of a world are kept in creation order, which is the order of
+ * ContactManager.contacts. */
+typedef struct gb_contact {
+    int32_t fixture_a, fixture_b; /* world-local; A is the primary shape of the pair */
+    int32_t child_a, child_b;
+    uint32_t flags;               /* GB_C_* */
+    int32_t toi_count;
+    double toi;
+    double friction, restitution;
+    int32_t m_type, m_point_count;
+    double m_lnx, m_lny;          /* manifold.local_normal */
+    double m_lpx, m_lpy;          /* manifold.local_point */
+    double p_lx[2], p_ly[2];      /* points[i].local_point */
+    double p_ni[2], p_ti[2];      /* points[i].normal_impulse, tangent_impulse */
+    uint32_t p_id[2];             /* index_a | index_b<<8 | type_a<<16 | type_b<<24 */
+} gb_contact;
+
+/* One world of a batch. */
+typedef struct gb_world_desc {
+    int32_t body_start, body_count;       /* into the batch body array */
+    int32_t fixture_start, fixture_count; /* into the batch fixture array */
+    int32_t contact_start, contact_count; /* initial contacts (into the batch contact array) */
+    int32_t contact_capacity;             /* device contact slots reserved for this world */
+    uint32_t flags;                       /* GB_W_* */
+    double gx, gy;                        /* gravity */
+    double inv_dt0;                       /* World._inv_dt0 */
+} gb_world_desc;
+
+/* A batch of independent worlds described by host arrays. */
+typedef struct gb_scene {
+    int32_t n_worlds;
+    int32_t n_bodies, n_fixtures, n_contacts;
+    const gb_world_desc *worlds;
+    const gb_body *bodies;
+    const gb_fixture *fixtures;
+    const gb_contact *contacts;
+} gb_scene;
+
+typedef struct gb_batch gb_batch; /* opaque device-resident batch of worlds */
+
+/* Step options.  launch_mode: 0 = autotuned, 1 = one CTA per world,
+ * 2 = one warp per world.  block_threads: CTA size for mode 1 (0 = tuned). */
+typedef struct gb_step_opts {
+    double dt;
+    int32_t vel_iters, pos_iters;
+    int32_t n_steps;
+    int32_t launch_mode;
+    int32_t block_threads;
+    int32_t record_order; /* keep the solver constraint order of the last step */
+} gb_step_opts;
+
+/* Library version and build information. */
+const char *gb_version(void);
+/* Message of the calling thread's last error (never NULL). */
+const char *gb_last_error(void);
+/* sizeof of gb_body, gb_fixture, gb_contact, gb_world_desc, gb_scene, gb_step_opts
+ * (6 ints), so bindings can check their record layouts. */
+int gb_struct_sizes(int32_t *sizes);
+
+/* Upload a scene to device memory.  Replaces the host-side construction of
+ * the reference's World (world.py:64-91, 183-233). */
+int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out);
+/* Free every device buffer of the batch. */
+int gb_batch_destroy(gb_batch *batch);
+/* Advance every world by opts->n_steps calls of World.step(dt, vel_iters,
+ * pos_iters) (world.py:307-354) on the given CUDA stream (NULL = default). */
+int gb_batch_step(gb_batch *batch, const gb_step_opts *opts, void *cuda_stream);
+/* Overwrite the device body state of the whole batch from host memory. */
+int gb_batch_set_bodies(gb_batch *batch, const gb_body *bodies, int32_t n_bodies, void *cuda_stream);
+/* Copy the device body state of the whole batch to host memory. */
+int gb_batch_get_bodies(gb_batch *batch, gb_body *bodies, int32_t n_bodies, void *cuda_stream);
+/* Copy the fat AABBs (4 doubles per fixture) to host memory. */
+int gb_batch_get_proxies(gb_batch *batch, double *aabbs, int32_t n_fixtures, void *cuda_stream);
+/* Number of live contacts of every world (n_worlds ints). */
+int gb_batch_get_contact_counts(gb_batch *batch, int32_t *counts, void *cuda_stream);
+/* Copy the live contacts of one world, in creation order, to host memory. */
+int gb_batch_get_contacts(gb_batch *batch, int32_t world, gb_contact *out, int32_t capacity,
+                          int32_t *n_out, void *cuda_stream);
+/* Solver constraint order of the last step of one world (contact indices in
+ * the order the velocity and position passes visited them); only kept when
+ * the step ran with record_order set. */
+int gb_batch_get_solver_order(gb_batch *batch, int32_t world, int32_t *order, int32_t capacity,
+                              int32_t *n_out, void *cuda_stream);
+/* Per-world status words (GB_ST_* bits), n_worlds uint32. */
+int gb_batch_status(gb_batch *batch, uint32_t *status, void *cuda_stream);
+/* Counters of the last gb_batch_step call: kernel launches, colour count of
+ * the last world, step count (3 int64). */
+int gb_batch_counters(gb_batch *batch, int64_t *counters);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB2D_H */

@@ -1,0 +1,53 @@
+/*
+ * oracle.h -- TEST INFRASTRUCTURE: C interface of the CPU restatement of
+ * pypybox2d's World.step (oracle.c).  Loaded by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU baseline only.
+ */
+#ifndef ORACLE_H
+#define ORACLE_H
+
+#include <stdint.h>
+#include "../include/gb2d.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct or_world or_world;
+
+/* Build one world from the batch arrays of a scene (world-local copy). */
+or_world *or_create(const gb_world_desc *wd, const gb_body *bodies, const gb_fixture *fixtures,
+                    const gb_contact *contacts);
+void or_destroy(or_world *w);
+/* World.step(dt, vel_iters, pos_iters) */
+void or_step(or_world *w, double dt, int vel_iters, int pos_iters);
+
+int or_body_count(const or_world *w);
+int or_contact_count(const or_world *w);
+uint32_t or_world_flags(const or_world *w);
+double or_inv_dt0(const or_world *w);
+int or_status(const or_world *w);
+void or_get_bodies(const or_world *w, gb_body *out);
+void or_set_bodies(or_world *w, const gb_body *in);
+void or_get_fixtures(const or_world *w, gb_fixture *out);
+int or_get_contacts(const or_world *w, gb_contact *out, int cap);
+/* Solve the next step's islands in this constraint order (contact-list
+ * positions at the time of the island solve). */
+void or_set_solver_order(or_world *w, const int *order, int n);
+/* Constraint order used by the last step (contact-list positions). */
+int or_get_solver_order(const or_world *w, int *out, int cap);
+long long or_toi_calls(const or_world *w);
+long long or_toi_events(const or_world *w);
+
+/* Step every world of a scene n_steps times with `threads` POSIX threads
+ * (one world at a time per thread, dynamic assignment).  Bodies of all
+ * worlds are written back to `bodies_out` (may be NULL).  Returns the wall
+ * time in seconds. */
+double or_run_scene(const gb_scene *scene, double dt, int vel_iters, int pos_iters, int n_steps, int threads,
+                    gb_body *bodies_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,191 @@
+"""Host-side mirror of ``include/gb2d.h``: numpy record layouts of the C
+structs and the ctypes binding of ``libgb2d.so``.
+
+The record layouts are the plain-data form of the reference's objects:
+``BODY`` is the state of ``pypybox2d.Body`` (body.py:46-84), ``FIXTURE`` a
+fixture with its shape and proxy (fixture.py:42-71, shapes.py), ``CONTACT`` a
+``Contact`` with its ``Manifold`` (contact.py:55-87, contact_util.py:120-155).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+SHAPE_CIRCLE, SHAPE_POLYGON, SHAPE_LOOP, SHAPE_EDGE = 0, 1, 2, 3
+MAX_POLY_VERTS = 8
+BODY_STATIC, BODY_DYNAMIC, BODY_KINEMATIC = 0, 1, 2
+
+BODY_AWAKE = 1
+BODY_ALLOW_SLEEP = 2
+BODY_BULLET = 4
+BODY_FIXED_ROTATION = 8
+BODY_ACTIVE = 16
+
+FIX_SENSOR = 1
+FIX_EDGE_HAS_V0 = 2
+FIX_EDGE_HAS_V3 = 4
+
+C_TOUCHING = 1
+C_ENABLED = 2
+C_FILTER = 4
+C_ISLAND = 8
+C_TOI = 16
+C_BULLET_HIT = 32
+
+M_CIRCLES, M_FACE_A, M_FACE_B = 0, 1, 2
+
+W_ALLOW_SLEEP = 1
+W_WARM_STARTING = 2
+W_CONTINUOUS = 4
+W_AUTO_CLEAR_FORCES = 8
+W_NEW_FIXTURE = 16
+W_STEP_COMPLETE = 32
+
+PREC_F64, PREC_F32 = 0, 1
+
+ST_CONTACT_OVERFLOW = 1
+ST_NONFINITE = 2
+ST_ITER_LIMIT = 4
+ST_PAIR_OVERFLOW = 8
+ST_TOI_ISLAND_CAP = 16
+
+_BODY_FIELDS = [
+    ("type", "<i4"), ("flags", "<u4"), ("fixture_start", "<i4"), ("fixture_count", "<i4"),
+    ("px", "<f8"), ("py", "<f8"), ("qc", "<f8"), ("qs", "<f8"),
+    ("lcx", "<f8"), ("lcy", "<f8"), ("c0x", "<f8"), ("c0y", "<f8"), ("cx", "<f8"), ("cy", "<f8"),
+    ("a0", "<f8"), ("a", "<f8"), ("alpha0", "<f8"),
+    ("vx", "<f8"), ("vy", "<f8"), ("w", "<f8"),
+    ("fx", "<f8"), ("fy", "<f8"), ("torque", "<f8"),
+    ("mass", "<f8"), ("inv_mass", "<f8"), ("I", "<f8"), ("inv_I", "<f8"),
+    ("linear_damping", "<f8"), ("angular_damping", "<f8"), ("gravity_scale", "<f8"),
+    ("sleep_time", "<f8"),
+]
+BODY = np.dtype(_BODY_FIELDS, align=True)
+
+FIXTURE = np.dtype([
+    ("body", "<i4"), ("shape_type", "<i4"), ("vertex_count", "<i4"), ("flags", "<u4"),
+    ("radius", "<f8"), ("friction", "<f8"), ("restitution", "<f8"), ("density", "<f8"),
+    ("category_bits", "<u4"), ("mask_bits", "<u4"), ("group_index", "<i4"), ("_pad0", "<i4"),
+    ("vx", "<f8", (MAX_POLY_VERTS,)), ("vy", "<f8", (MAX_POLY_VERTS,)),
+    ("nx", "<f8", (MAX_POLY_VERTS,)), ("ny", "<f8", (MAX_POLY_VERTS,)),
+    ("aabb", "<f8", (4,)),
+], align=True)
+
+CONTACT = np.dtype([
+    ("fixture_a", "<i4"), ("fixture_b", "<i4"), ("child_a", "<i4"), ("child_b", "<i4"),
+    ("flags", "<u4"), ("toi_count", "<i4"), ("toi", "<f8"),
+    ("friction", "<f8"), ("restitution", "<f8"),
+    ("m_type", "<i4"), ("m_point_count", "<i4"),
+    ("m_lnx", "<f8"), ("m_lny", "<f8"), ("m_lpx", "<f8"), ("m_lpy", "<f8"),
+    ("p_lx", "<f8", (2,)), ("p_ly", "<f8", (2,)), ("p_ni", "<f8", (2,)), ("p_ti", "<f8", (2,)),
+    ("p_id", "<u4", (2,)),
+], align=True)
+
+WORLD = np.dtype([
+    ("body_start", "<i4"), ("body_count", "<i4"), ("fixture_start", "<i4"), ("fixture_count", "<i4"),
+    ("contact_start", "<i4"), ("contact_count", "<i4"), ("contact_capacity", "<i4"), ("flags", "<u4"),
+    ("gx", "<f8"), ("gy", "<f8"), ("inv_dt0", "<f8"),
+], align=True)
+
+
+class Scene(ctypes.Structure):
+    """ctypes form of ``gb_scene``."""
+    _fields_ = [
+        ("n_worlds", ctypes.c_int32), ("n_bodies", ctypes.c_int32),
+        ("n_fixtures", ctypes.c_int32), ("n_contacts", ctypes.c_int32),
+        ("worlds", ctypes.c_void_p), ("bodies", ctypes.c_void_p),
+        ("fixtures", ctypes.c_void_p), ("contacts", ctypes.c_void_p),
+    ]
+
+
+class StepOpts(ctypes.Structure):
+    """ctypes form of ``gb_step_opts``."""
+    _fields_ = [
+        ("dt", ctypes.c_double), ("vel_iters", ctypes.c_int32), ("pos_iters", ctypes.c_int32),
+        ("n_steps", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
+        ("block_threads", ctypes.c_int32), ("record_order", ctypes.c_int32),
+    ]
+
+
+def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,
+               contacts: np.ndarray | None = None) -> tuple[Scene, tuple]:
+    """Pack contiguous record arrays into a ``gb_scene``; the returned tuple
+    keeps the arrays alive as long as the scene is used."""
+    worlds = np.ascontiguousarray(worlds, dtype=WORLD)
+    bodies = np.ascontiguousarray(bodies, dtype=BODY)
+    fixtures = np.ascontiguousarray(fixtures, dtype=FIXTURE)
+    if contacts is None:
+        contacts = np.zeros(0, dtype=CONTACT)
+    contacts = np.ascontiguousarray(contacts, dtype=CONTACT)
+    s = Scene()
+    s.n_worlds = len(worlds)
+    s.n_bodies = len(bodies)
+    s.n_fixtures = len(fixtures)
+    s.n_contacts = len(contacts)
+    s.worlds = worlds.ctypes.data
+    s.bodies = bodies.ctypes.data
+    s.fixtures = fixtures.ctypes.data
+    s.contacts = contacts.ctypes.data if len(contacts) else None
+    return s, (worlds, bodies, fixtures, contacts)
+
+
+_PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG_DIR, "_build", "libgb2d.so")
+
+EXPORTED = (
+    "gb_version", "gb_last_error", "gb_struct_sizes",
+    "gb_batch_create", "gb_batch_destroy", "gb_batch_step",
+    "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_get_proxies",
+    "gb_batch_get_contact_counts", "gb_batch_get_contacts", "gb_batch_get_solver_order",
+    "gb_batch_status", "gb_batch_counters",
+)
+
+_lib = None
+
+
+class GB2DError(RuntimeError):
+    """A C-ABI call returned an error status (message from gb_last_error)."""
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Load ``libgb2d.so`` (built in-tree by ``__graft_entry__.build``).
+
+    There is no fallback: a missing library raises, so nothing silently runs
+    on the CPU."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise GB2DError(f"libgb2d.so not built ({p}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(p)
+    vp, i32, u32p, i32p = ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int32)
+    lib.gb_version.restype = ctypes.c_char_p
+    lib.gb_last_error.restype = ctypes.c_char_p
+    lib.gb_struct_sizes.argtypes = [i32p]
+    lib.gb_batch_create.argtypes = [ctypes.POINTER(Scene), i32, ctypes.POINTER(vp)]
+    lib.gb_batch_destroy.argtypes = [vp]
+    lib.gb_batch_step.argtypes = [vp, ctypes.POINTER(StepOpts), vp]
+    lib.gb_batch_set_bodies.argtypes = [vp, vp, i32, vp]
+    lib.gb_batch_get_bodies.argtypes = [vp, vp, i32, vp]
+    lib.gb_batch_get_proxies.argtypes = [vp, vp, i32, vp]
+    lib.gb_batch_get_contact_counts.argtypes = [vp, i32p, vp]
+    lib.gb_batch_get_contacts.argtypes = [vp, i32, vp, i32, i32p, vp]
+    lib.gb_batch_get_solver_order.argtypes = [vp, i32, i32p, i32, i32p, vp]
+    lib.gb_batch_status.argtypes = [vp, u32p, vp]
+    lib.gb_batch_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    for name in EXPORTED:
+        if name not in ("gb_version", "gb_last_error"):
+            getattr(lib, name).restype = ctypes.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    """Raise GB2DError with the library's message when rc != 0."""
+    if rc != 0:
+        msg = load_library().gb_last_error().decode(errors="replace")
+        raise GB2DError(f"gb2d error {rc}: {msg}")

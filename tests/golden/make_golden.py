@@ -1,0 +1,364 @@
+"""Generate the golden vectors of the World.step path by running the
+reference pypybox2d itself (C-extension math mode) in this container.
+
+Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+
+The reference is imported from its source tree (read only); its C extension
+`_common` must first be compiled by oracle/build_ref.sh into oracle/_ref/.
+Two harness hooks are installed, neither of which touches the physics:
+  * BroadPhase.update_pairs yields the same pair set with the same pair
+    orientation as the reference, in a fixed order (first position of the
+    moved proxy in the move buffer, then the other proxy's index) instead of
+    Python-set order (broadphase.py:83-109);
+  * Island.solve records the contact-list position of each island contact in
+    solver order, so the natural (depth-first) constraint order is pinned too.
+
+Each scene is built through the reference's public API (World,
+create_*_body, Fixture, Polygon/Circle/Edge), exported to the record layouts
+of include/gb2d.h, stepped, and snapshotted at fixed steps.  The result is
+one compressed .npz per scene under tests/golden/.
+"""
+from __future__ import annotations
+
+import argparse
+import glob
+import importlib.util
+import math
+import os
+import random
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+from pypybox2d_gb300 import abi  # noqa: E402
+
+
+def load_reference(ref_root: str):
+    sos = glob.glob(os.path.join(REPO, "oracle", "_ref", "_common*.so"))
+    if not sos:
+        raise SystemExit("build the reference extension first: oracle/build_ref.sh")
+    spec = importlib.util.spec_from_file_location("pypybox2d._common", sos[0])
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    sys.modules["pypybox2d._common"] = mod
+    sys.path.insert(0, ref_root)
+    import pypybox2d as b2  # noqa: F401
+    from pypybox2d import common
+    assert common.Vec2 is mod.Vec2, "reference did not pick up the C extension"
+    return b2
+
+
+def fixture_index(world):
+    idx = {}
+    k = 0
+    for body in world.bodies:
+        for f in body.fixtures:
+            idx[id(f)] = k
+            k += 1
+    return idx
+
+
+def install_hooks(world, b2, order_log):
+    fidx = fixture_index(world)
+    bp = world.contact_manager.broadphase
+
+    def update_pairs(self, callback=None):
+        first = {}
+        for i, node in enumerate(self._move_buffer):
+            if node not in first:
+                first[node] = i
+        pairs = []
+        for node, pos in first.items():
+            for res in self._tree.query(node.aabb):
+                if res is node:
+                    continue
+                if res in first and first[res] < pos:
+                    continue
+                pairs.append((pos, fidx[id(res.user_data.fixture)], node, res))
+        self._move_buffer = []
+        pairs.sort(key=lambda t: (t[0], t[1]))
+        for _, _, a, b in pairs:
+            yield (a.user_data, b.user_data)
+
+    bp.update_pairs = types.MethodType(update_pairs, bp)
+
+    from pypybox2d import island as island_mod
+    orig_solve = island_mod.Island.solve
+
+    def solve(self, step, gravity, allow_sleep):
+        pos = {id(c): i for i, c in enumerate(world.contact_manager.contacts)}
+        order_log.extend(pos[id(c)] for c in self.contacts)
+        return orig_solve(self, step, gravity, allow_sleep)
+
+    island_mod.Island.solve = solve
+    return orig_solve
+
+
+def export_world(world, b2, contacts=True):
+    """Reference world -> (worlds, bodies, fixtures, contacts) record arrays."""
+    fidx = fixture_index(world)
+    nb = len(world.bodies)
+    nf = sum(len(b.fixtures) for b in world.bodies)
+    B = np.zeros(nb, dtype=abi.BODY)
+    F = np.zeros(nf, dtype=abi.FIXTURE)
+    k = 0
+    for i, body in enumerate(world.bodies):
+        r = B[i]
+        r["type"] = body._type
+        fl = 0
+        if body._awake:
+            fl |= abi.BODY_AWAKE
+        if body._allow_sleep:
+            fl |= abi.BODY_ALLOW_SLEEP
+        if body._bullet:
+            fl |= abi.BODY_BULLET
+        if body._fixed_rotation:
+            fl |= abi.BODY_FIXED_ROTATION
+        if body._active:
+            fl |= abi.BODY_ACTIVE
+        r["flags"] = fl
+        r["fixture_start"] = k
+        r["fixture_count"] = len(body.fixtures)
+        xf = body._xf
+        r["px"], r["py"] = xf.position.x, xf.position.y
+        rot = xf.rotation
+        r["qc"], r["qs"] = rot.col1.x, rot.col1.y
+        sw = body._sweep
+        r["lcx"], r["lcy"] = sw.local_center.x, sw.local_center.y
+        r["c0x"], r["c0y"] = sw.c0.x, sw.c0.y
+        r["cx"], r["cy"] = sw.c.x, sw.c.y
+        r["a0"], r["a"], r["alpha0"] = sw.a0, sw.a, sw.alpha0
+        r["vx"], r["vy"] = body._linear_velocity.x, body._linear_velocity.y
+        r["w"] = body._angular_velocity
+        r["fx"], r["fy"] = body._force.x, body._force.y
+        r["torque"] = body._torque
+        r["mass"], r["inv_mass"], r["I"], r["inv_I"] = body._mass, body._inv_mass, body._I, body._invI
+        r["linear_damping"], r["angular_damping"] = body._linear_damping, body._angular_damping
+        r["gravity_scale"] = body._gravity_scale
+        r["sleep_time"] = body._sleep_time
+        for f in body.fixtures:
+            q = F[k]
+            sh = f._shape
+            q["body"] = i
+            q["shape_type"] = sh._type
+            q["radius"] = sh.radius
+            q["friction"], q["restitution"], q["density"] = f._friction, f._restitution, f._density
+            q["category_bits"], q["mask_bits"], q["group_index"] = f._category_bits, f._mask_bits, f._group_index
+            fl = abi.FIX_SENSOR if f._sensor else 0
+            if sh._type == abi.SHAPE_CIRCLE:
+                q["vertex_count"] = 1
+                q["vx"][0], q["vy"][0] = sh.position.x, sh.position.y
+            elif sh._type == abi.SHAPE_POLYGON:
+                q["vertex_count"] = len(sh._vertices)
+                for j, (v, n) in enumerate(zip(sh._vertices, sh._normals)):
+                    q["vx"][j], q["vy"][j] = v.x, v.y
+                    q["nx"][j], q["ny"][j] = n.x, n.y
+            elif sh._type == abi.SHAPE_EDGE:
+                q["vertex_count"] = 2
+                q["vx"][0], q["vy"][0] = sh._vertex1.x, sh._vertex1.y
+                q["vx"][1], q["vy"][1] = sh._vertex2.x, sh._vertex2.y
+                if sh._vertex0 is not None:
+                    fl |= abi.FIX_EDGE_HAS_V0
+                    q["vx"][2], q["vy"][2] = sh._vertex0.x, sh._vertex0.y
+                if sh._vertex3 is not None:
+                    fl |= abi.FIX_EDGE_HAS_V3
+                    q["vx"][3], q["vy"][3] = sh._vertex3.x, sh._vertex3.y
+            else:
+                raise NotImplementedError("loop shapes are not exported")
+            q["flags"] = fl
+            aabb = f._proxies[0].proxy_ref.aabb
+            q["aabb"][:] = (aabb.lower_bound.x, aabb.lower_bound.y, aabb.upper_bound.x, aabb.upper_bound.y)
+            k += 1
+    clist = world.contact_manager.contacts if contacts else []
+    C = np.zeros(len(clist), dtype=abi.CONTACT)
+    for i, c in enumerate(clist):
+        r = C[i]
+        r["fixture_a"], r["fixture_b"] = fidx[id(c._fixture_a)], fidx[id(c._fixture_b)]
+        r["child_a"], r["child_b"] = c._index_a, c._index_b
+        fl = 0
+        for bit, name in ((abi.C_TOUCHING, "_touching_flag"), (abi.C_ENABLED, "_enabled_flag"),
+                          (abi.C_FILTER, "_filter_flag"), (abi.C_ISLAND, "_island_flag"),
+                          (abi.C_TOI, "_toi_flag"), (abi.C_BULLET_HIT, "_bullet_hit_flag")):
+            if getattr(c, name):
+                fl |= bit
+        r["flags"] = fl
+        r["toi_count"], r["toi"] = c._toi_count, c._toi
+        r["friction"], r["restitution"] = c._friction, c._restitution
+        m = c._manifold
+        r["m_type"], r["m_point_count"] = m.type, m.point_count
+        r["m_lnx"], r["m_lny"] = m.local_normal.x, m.local_normal.y
+        r["m_lpx"], r["m_lpy"] = m.local_point.x, m.local_point.y
+        for j in range(2):
+            p = m.points[j]
+            r["p_lx"][j], r["p_ly"][j] = p.local_point.x, p.local_point.y
+            r["p_ni"][j], r["p_ti"][j] = p.normal_impulse, p.tangent_impulse
+            ia, ib, ta, tb = p.id
+            r["p_id"][j] = (ia & 255) | ((ib & 255) << 8) | ((ta & 255) << 16) | ((tb & 255) << 24)
+    W = np.zeros(1, dtype=abi.WORLD)
+    wf = 0
+    if world._allow_sleep:
+        wf |= abi.W_ALLOW_SLEEP
+    if world._warm_starting:
+        wf |= abi.W_WARM_STARTING
+    if world._continuous_physics:
+        wf |= abi.W_CONTINUOUS
+    if world._auto_clear_forces:
+        wf |= abi.W_AUTO_CLEAR_FORCES
+    if world._new_fixture:
+        wf |= abi.W_NEW_FIXTURE
+    if world._step_complete:
+        wf |= abi.W_STEP_COMPLETE
+    W[0] = (0, nb, 0, nf, 0, len(C), max(64, 8 * nf), wf, world._gravity.x, world._gravity.y, world._inv_dt0)
+    return W, B, F, C
+
+
+# ---------------------------------------------------------------- scenes
+def scene_pyramid(b2, rows=20):
+    """Configuration 1: the pyramid of 20 rows of 0.5 m boxes (210 bodies)."""
+    from pypybox2d.common import Vec2
+    from copy import copy
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    world.create_static_body(position=(0, -0.5), shapes=b2.Polygon(box=(40, 0.5)))
+    fixture = b2.Fixture(b2.Polygon(box=(0.5, 0.5)), density=5.0, friction=0.6, restitution=0.0)
+    x = Vec2(-7.0, 0.75)
+    dx, dy = Vec2(0.5625, 1.25), Vec2(1.125, 0.0)
+    for i in range(rows):
+        y = copy(x)
+        for _ in range(i, rows):
+            world.create_dynamic_body(position=y, fixtures=fixture)
+            y = y + dy
+        x = x + dx
+    return world
+
+
+def random_convex(rng, n, rad):
+    """Convex CCW polygon: hull of n random points at radius `rad` (sorted
+    angles on a circle are in convex position)."""
+    angs = sorted(rng.uniform(0, 2 * math.pi) for _ in range(n))
+    pts = [(rad * math.cos(a), rad * math.sin(a)) for a in angs]
+    return pts
+
+
+def scene_mixed(b2, n=40, seed=3, size=12.0):
+    """Configuration-3 style: a static box container of 4 edge shapes with
+    random circles and convex polygons, random velocities."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    h = size / 2
+    ground = world.create_static_body()
+    for v1, v2 in (((-h, -h), (h, -h)), ((h, -h), (h, h)), ((h, h), (-h, h)), ((-h, h), (-h, -h))):
+        ground.create_edge_fixture(v1, v2, friction=0.5)
+    cols = int(math.ceil(math.sqrt(n)))
+    spacing = (size - 2.5) / cols
+    k = 0
+    for gy in range(cols):
+        for gx in range(cols):
+            if k >= n:
+                break
+            px = -h + 1.25 + (gx + 0.5) * spacing
+            py = -h + 1.25 + (gy + 0.5) * spacing
+            body = world.create_dynamic_body(position=(px, py), angle=rng.uniform(-3, 3),
+                                             linear_velocity=(rng.gauss(0, 2), rng.gauss(0, 2)),
+                                             angular_velocity=rng.gauss(0, 1))
+            dens, fr, rest = rng.uniform(0.5, 5), rng.uniform(0.2, 0.8), rng.uniform(0, 0.3)
+            rad = min(rng.uniform(0.25, 1.0), 0.45 * spacing)
+            prad = min(rng.uniform(0.3, 1.0), 0.45 * spacing)
+            if k % 2 == 0:
+                body.create_circle_fixture(radius=rad, density=dens, friction=fr, restitution=rest)
+            else:
+                nv = rng.randint(3, 8)
+                while True:
+                    pts = random_convex(rng, nv, prad)
+                    try:
+                        body.create_polygon_fixture(vertices=pts, density=dens, friction=fr, restitution=rest)
+                        break
+                    except (ValueError, AssertionError):
+                        continue
+            k += 1
+    return world
+
+
+def scene_bullets(b2, seed=5):
+    """Configuration-5 style: a stack of 8 boxes on a ground box plus 2 fast
+    bullet circles (continuous collision)."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    world.create_static_body(position=(0, -0.5), shapes=b2.Polygon(box=(40, 0.5)))
+    for i in range(8):
+        body = world.create_dynamic_body(position=(0.0, 0.5 + 1.0 * i))
+        body.create_polygon_fixture(box=(0.5, 0.5), density=1.0, friction=0.3)
+    for j in range(2):
+        body = world.create_dynamic_body(position=(-30.0, rng.uniform(0.5, 7.0)), bullet=True,
+                                         linear_velocity=(rng.uniform(150, 250), 0.0))
+        body.create_circle_fixture(radius=0.1, density=100.0)
+    return world
+
+
+def scene_sleep(b2):
+    """Small scene whose bodies fall asleep: one isolated box, a two-box
+    stack and a circle on a ground box."""
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    world.create_static_body(position=(0, -0.5), shapes=b2.Polygon(box=(20, 0.5)))
+    world.create_dynamic_body(position=(-5, 0.6)).create_polygon_fixture(box=(0.5, 0.5), density=1.0)
+    world.create_dynamic_body(position=(0, 0.5)).create_polygon_fixture(box=(0.5, 0.5), density=1.0)
+    world.create_dynamic_body(position=(0, 1.5)).create_polygon_fixture(box=(0.5, 0.5), density=1.0)
+    world.create_dynamic_body(position=(5, 0.5)).create_circle_fixture(radius=0.5, density=1.0)
+    return world
+
+
+SCENES = {
+    "pyramid": (scene_pyramid, 300, (1, 2, 3, 5, 10, 30, 100, 200, 300)),
+    "pyramid5": (lambda b2: scene_pyramid(b2, rows=5), 150, (1, 2, 5, 20, 60, 150)),
+    "mixed": (scene_mixed, 200, (1, 2, 5, 20, 60, 120, 200)),
+    "bullets": (scene_bullets, 60, (1, 2, 3, 5, 10, 20, 40, 60)),
+    "sleep": (scene_sleep, 90, (1, 10, 29, 30, 31, 45, 60, 90)),
+}
+
+
+def run_scene(b2, name, builder, n_steps, snaps, vel_iters=8, pos_iters=3, dt=1.0 / 60):
+    from pypybox2d import island as island_mod
+    world = builder(b2)
+    order_log: list[int] = []
+    orig = install_hooks(world, b2, order_log)
+    out = {}
+    W, B, F, C = export_world(world, b2)
+    out["init_world"], out["init_bodies"], out["init_fixtures"] = W, B, F
+    out["iters"] = np.array([vel_iters, pos_iters])
+    try:
+        for s in range(1, n_steps + 1):
+            order_log.clear()
+            world.step(dt, vel_iters, pos_iters)
+            if s in snaps:
+                W2, B2, F2, C2 = export_world(world, b2)
+                out[f"s{s}_bodies"] = B2
+                out[f"s{s}_aabb"] = F2["aabb"].copy()
+                out[f"s{s}_contacts"] = C2
+                out[f"s{s}_world"] = W2
+                out[f"s{s}_order"] = np.array(order_log, dtype=np.int32)
+    finally:
+        island_mod.Island.solve = orig
+    out["snaps"] = np.array(sorted(snaps), dtype=np.int32)
+    out["dt"] = np.array([dt])
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: {len(B)} bodies, {len(F)} fixtures, steps {n_steps} -> {os.path.getsize(path)} bytes")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default=None)
+    args = ap.parse_args()
+    b2 = load_reference(args.ref)
+    for name, (builder, n, snaps) in SCENES.items():
+        if args.only and name != args.only:
+            continue
+        run_scene(b2, name, builder, n, snaps)
+
+
+if __name__ == "__main__":
+    main()

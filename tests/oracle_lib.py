@@ -1,0 +1,117 @@
+"""ctypes binding of the CPU restatement (oracle/) for the tests.
+
+The oracle is test infrastructure: it is the checker of the GPU library and
+is never called by the product.  ``load(libm=True)`` gives the build that
+uses libm cos/sin/pow like CPython (pinned bit for bit against the golden
+vectors of the reference); ``load(libm=False)`` the build with the portable
+sincos and x*x that the float64 GPU kernels reproduce bit for bit.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from pypybox2d_gb300 import abi
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(REPO, "oracle")
+_libs: dict[bool, ctypes.CDLL] = {}
+
+
+def build() -> None:
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
+
+
+def load(libm: bool = False) -> ctypes.CDLL:
+    if libm in _libs:
+        return _libs[libm]
+    name = "liboracle_libm.so" if libm else "liboracle.so"
+    path = os.path.join(ORACLE_DIR, "_build", name)
+    build()
+    lib = ctypes.CDLL(path)
+    vp, i32, dbl = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lib.or_create.restype = vp
+    lib.or_create.argtypes = [vp, vp, vp, vp]
+    lib.or_destroy.argtypes = [vp]
+    lib.or_step.argtypes = [vp, dbl, i32, i32]
+    for n in ("or_body_count", "or_contact_count", "or_status"):
+        getattr(lib, n).argtypes = [vp]
+        getattr(lib, n).restype = i32
+    lib.or_world_flags.argtypes = [vp]
+    lib.or_world_flags.restype = ctypes.c_uint32
+    lib.or_inv_dt0.argtypes = [vp]
+    lib.or_inv_dt0.restype = dbl
+    lib.or_get_bodies.argtypes = [vp, vp]
+    lib.or_set_bodies.argtypes = [vp, vp]
+    lib.or_get_fixtures.argtypes = [vp, vp]
+    lib.or_get_contacts.argtypes = [vp, vp, i32]
+    lib.or_get_contacts.restype = i32
+    lib.or_set_solver_order.argtypes = [vp, vp, i32]
+    lib.or_get_solver_order.argtypes = [vp, vp, i32]
+    lib.or_get_solver_order.restype = i32
+    lib.or_toi_calls.argtypes = [vp]
+    lib.or_toi_calls.restype = ctypes.c_longlong
+    lib.or_toi_events.argtypes = [vp]
+    lib.or_toi_events.restype = ctypes.c_longlong
+    lib.or_run_scene.argtypes = [ctypes.POINTER(abi.Scene), dbl, i32, i32, i32, i32, vp]
+    lib.or_run_scene.restype = dbl
+    _libs[libm] = lib
+    return lib
+
+
+class OracleWorld:
+    """One world of the restatement, built from gb2d record arrays."""
+
+    def __init__(self, world, bodies, fixtures, contacts=None, libm=False, index=0):
+        self.lib = load(libm)
+        self._keep = [np.ascontiguousarray(world, dtype=abi.WORLD),
+                      np.ascontiguousarray(bodies, dtype=abi.BODY),
+                      np.ascontiguousarray(fixtures, dtype=abi.FIXTURE),
+                      np.ascontiguousarray(contacts if contacts is not None else np.zeros(0, abi.CONTACT),
+                                           dtype=abi.CONTACT)]
+        w, b, f, c = self._keep
+        wd = w[index:index + 1]
+        self._wd = np.ascontiguousarray(wd)
+        self.h = self.lib.or_create(self._wd.ctypes.data, b.ctypes.data, f.ctypes.data,
+                                    c.ctypes.data if len(c) else None)
+        self.nb = int(wd["body_count"][0])
+        self.nf = int(wd["fixture_count"][0])
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.or_destroy(self.h)
+            self.h = None
+
+    def step(self, dt, vel_iters=8, pos_iters=3, order=None):
+        if order is not None:
+            o = np.ascontiguousarray(order, dtype=np.int32)
+            self.lib.or_set_solver_order(self.h, o.ctypes.data, len(o))
+        self.lib.or_step(self.h, dt, vel_iters, pos_iters)
+
+    def bodies(self):
+        out = np.zeros(self.nb, dtype=abi.BODY)
+        self.lib.or_get_bodies(self.h, out.ctypes.data)
+        return out
+
+    def fixtures(self):
+        out = np.zeros(self.nf, dtype=abi.FIXTURE)
+        self.lib.or_get_fixtures(self.h, out.ctypes.data)
+        return out
+
+    def contacts(self):
+        n = self.lib.or_contact_count(self.h)
+        out = np.zeros(n, dtype=abi.CONTACT)
+        self.lib.or_get_contacts(self.h, out.ctypes.data, n)
+        return out
+
+    def solver_order(self):
+        cap = max(16, 4 * self.lib.or_contact_count(self.h) + 16)
+        out = np.zeros(cap, dtype=np.int32)
+        n = self.lib.or_get_solver_order(self.h, out.ctypes.data, cap)
+        return out[:n].copy()
+
+    def status(self):
+        return self.lib.or_status(self.h)
