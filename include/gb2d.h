@@ -162,6 +162,9 @@ typedef struct gb_world_desc {
     int32_t contact_start, contact_count; /* initial contacts (into the batch contact array) */
     int32_t contact_capacity;             /* device contact slots reserved for this world */
     uint32_t flags;                       /* GB_W_* */
+    int32_t move_start, move_count;       /* pending broad-phase move buffer (into scene.moves);
+                                             with GB_W_NEW_FIXTURE and move_count == 0 every
+                                             fixture of the world is pending, in index order */
     double gx, gy;                        /* gravity */
     double inv_dt0;                       /* World._inv_dt0 */
 } gb_world_desc;
@@ -174,6 +177,8 @@ typedef struct gb_scene {
     const gb_body *bodies;
     const gb_fixture *fixtures;
     const gb_contact *contacts;
+    int32_t n_moves, _pad0;
+    const int32_t *moves;                 /* world-local fixture indices (BroadPhase._move_buffer) */
 } gb_scene;
 
 typedef struct gb_batch gb_batch; /* opaque device-resident batch of worlds */

@@ -1010,7 +1010,8 @@ void or_step(or_world *w, double dt, int vel_iters, int pos_iters) {
 }
 
 /* ------------------------------------------------------------------ */
-or_world *or_create(const gb_world_desc *wd, const gb_body *bodies, const gb_fixture *fixtures, const gb_contact *contacts) {
+or_world *or_create(const gb_world_desc *wd, const gb_body *bodies, const gb_fixture *fixtures, const gb_contact *contacts,
+                    const int32_t *moves) {
     or_world *w = (or_world *)calloc(1, sizeof(or_world));
     w->nb = wd->body_count;
     w->nf = wd->fixture_count;
@@ -1044,7 +1045,9 @@ or_world *or_create(const gb_world_desc *wd, const gb_body *bodies, const gb_fix
             iv_push(&w->bcon[w->f[c->fb].body], id);
         }
     }
-    if (w->wflags & GB_W_NEW_FIXTURE)
+    if (wd->move_count > 0 && moves)
+        for (int i = 0; i < wd->move_count; ++i) iv_push(&w->move, moves[wd->move_start + i]);
+    else if (w->wflags & GB_W_NEW_FIXTURE)
         for (int i = 0; i < w->nf; ++i) iv_push(&w->move, i);
     return w;
 }
@@ -1127,7 +1130,7 @@ static void *or_worker(void *arg) {
         pthread_mutex_unlock(&j->mu);
         if (wi >= j->scene->n_worlds) break;
         const gb_world_desc *wd = &j->scene->worlds[wi];
-        or_world *w = or_create(wd, j->scene->bodies, j->scene->fixtures, j->scene->contacts);
+        or_world *w = or_create(wd, j->scene->bodies, j->scene->fixtures, j->scene->contacts, j->scene->moves);
         for (int s = 0; s < j->steps; ++s) or_step(w, j->dt, j->vi, j->pi);
         if (j->out) or_get_bodies(w, j->out + wd->body_start);
         or_destroy(w);

@@ -17,7 +17,7 @@ typedef struct or_world or_world;
 
 /* Build one world from the batch arrays of a scene (world-local copy). */
 or_world *or_create(const gb_world_desc *wd, const gb_body *bodies, const gb_fixture *fixtures,
-                    const gb_contact *contacts);
+                    const gb_contact *contacts, const int32_t *moves);
 void or_destroy(or_world *w);
 /* World.step(dt, vel_iters, pos_iters) */
 void or_step(or_world *w, double dt, int vel_iters, int pos_iters);

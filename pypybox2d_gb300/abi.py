@@ -86,6 +86,7 @@ CONTACT = np.dtype([
 WORLD = np.dtype([
     ("body_start", "<i4"), ("body_count", "<i4"), ("fixture_start", "<i4"), ("fixture_count", "<i4"),
     ("contact_start", "<i4"), ("contact_count", "<i4"), ("contact_capacity", "<i4"), ("flags", "<u4"),
+    ("move_start", "<i4"), ("move_count", "<i4"),
     ("gx", "<f8"), ("gy", "<f8"), ("inv_dt0", "<f8"),
 ], align=True)
 
@@ -97,6 +98,7 @@ class Scene(ctypes.Structure):
         ("n_fixtures", ctypes.c_int32), ("n_contacts", ctypes.c_int32),
         ("worlds", ctypes.c_void_p), ("bodies", ctypes.c_void_p),
         ("fixtures", ctypes.c_void_p), ("contacts", ctypes.c_void_p),
+        ("n_moves", ctypes.c_int32), ("_pad0", ctypes.c_int32), ("moves", ctypes.c_void_p),
     ]
 
 
@@ -110,7 +112,7 @@ class StepOpts(ctypes.Structure):
 
 
 def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,
-               contacts: np.ndarray | None = None) -> tuple[Scene, tuple]:
+               contacts: np.ndarray | None = None, moves: np.ndarray | None = None) -> tuple[Scene, tuple]:
     """Pack contiguous record arrays into a ``gb_scene``; the returned tuple
     keeps the arrays alive as long as the scene is used."""
     worlds = np.ascontiguousarray(worlds, dtype=WORLD)
@@ -128,7 +130,10 @@ def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,
     s.bodies = bodies.ctypes.data
     s.fixtures = fixtures.ctypes.data
     s.contacts = contacts.ctypes.data if len(contacts) else None
-    return s, (worlds, bodies, fixtures, contacts)
+    moves = np.ascontiguousarray(moves if moves is not None else np.zeros(0, np.int32), dtype=np.int32)
+    s.n_moves = len(moves)
+    s.moves = moves.ctypes.data if len(moves) else None
+    return s, (worlds, bodies, fixtures, contacts, moves)
 
 
 _PKG_DIR = os.path.dirname(os.path.abspath(__file__))

@@ -1,0 +1,385 @@
+// gb_api.cu -- the C ABI of libgb2d.so (include/gb2d.h).
+//
+// A gb_batch owns one device arena holding every world of the batch in the
+// structure-of-arrays layout of gb_world.cuh plus the per-world scratch of
+// the step.  Host records (gb_body, gb_fixture, gb_contact) cross the bus in
+// their AoS form and are (un)packed on the device.  Errors are reported as
+// negative status codes with a thread-local message; no call falls back to
+// the CPU.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gb_launch.h"
+
+namespace {
+thread_local std::string g_err = "ok";
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char *where) {
+    g_err = std::string(where) + ": " + cudaGetErrorString(e);
+    return GB_E_CUDA;
+}
+#define CK(call)                                             \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+    } while (0)
+
+// Bump allocator over one cudaMalloc'ed arena.
+struct Arena {
+    size_t off = 0;
+    char *base = nullptr;
+    template <class T> T *take(size_t n) {
+        off = (off + 255) & ~size_t(255);
+        T *p = base ? reinterpret_cast<T *>(base + off) : nullptr;
+        off += sizeof(T) * (n ? n : 1);
+        return p;
+    }
+};
+
+template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap) {
+    B.n_worlds = nw;
+    B.hdr = a.take<WorldHdr>(nw);
+    B.b_type = a.take<int>(nb); B.b_flags = a.take<uint32_t>(nb); B.b_fstart = a.take<int>(nb); B.b_fcount = a.take<int>(nb);
+    B.b_xp = a.take<vec2<double>>(nb); B.b_xq = a.take<rot2<double>>(nb);
+    B.b_lc = a.take<vec2<double>>(nb); B.b_c = a.take<vec2<double>>(nb); B.b_c0 = a.take<vec2<double>>(nb);
+    B.b_a = a.take<double>(nb); B.b_a0 = a.take<double>(nb); B.b_alpha0 = a.take<double>(nb);
+    B.b_v = a.take<vec2<R>>(nb); B.b_w = a.take<R>(nb); B.b_f = a.take<vec2<R>>(nb); B.b_torque = a.take<R>(nb);
+    B.b_inv_mass = a.take<R>(nb); B.b_inv_I = a.take<R>(nb); B.b_ldamp = a.take<R>(nb); B.b_adamp = a.take<R>(nb);
+    B.b_gscale = a.take<R>(nb);
+    B.b_mass = a.take<double>(nb); B.b_I = a.take<double>(nb); B.b_sleep = a.take<double>(nb);
+    B.f_body = a.take<int>(nf); B.f_type = a.take<int>(nf); B.f_count = a.take<int>(nf); B.f_flags = a.take<uint32_t>(nf);
+    B.f_radius = a.take<R>(nf); B.f_friction = a.take<R>(nf); B.f_restitution = a.take<R>(nf); B.f_density = a.take<double>(nf);
+    B.f_cat = a.take<uint32_t>(nf); B.f_mask = a.take<uint32_t>(nf); B.f_group = a.take<int>(nf);
+    B.f_v = a.take<vec2<R>>((size_t)nf * GB_MAX_POLY_VERTS); B.f_n = a.take<vec2<R>>((size_t)nf * GB_MAX_POLY_VERTS);
+    B.f_aabb = a.take<dbox>(nf);
+    B.c = a.take<ContactRec<R>>(ncap);
+    B.s_parent = a.take<int>(nb); B.s_wake = a.take<int>(nb); B.s_seed = a.take<int>(nb); B.s_stack = a.take<int>(nb);
+    B.s_adjoff = a.take<int>(nb + nw);
+    B.s_root = a.take<uint32_t>(nb);
+    B.s_claim = a.take<unsigned long long>(nb); B.s_minsep = a.take<unsigned long long>(nb);
+    B.s_minsleep = a.take<unsigned long long>(nb);
+    B.s_bvis = a.take<unsigned char>(nb);
+    B.s_move = a.take<int>(nf); B.s_first = a.take<int>(nf); B.s_cnt = a.take<int>(nf);
+    B.s_proc = a.take<int>(ncap); B.s_pref = a.take<int>(ncap); B.s_adj = a.take<int>(2 * (size_t)ncap);
+    B.s_colour = a.take<int>(ncap); B.s_order = a.take<int>(ncap); B.s_cons_of = a.take<int>(ncap);
+    B.s_cvis = a.take<unsigned char>(ncap);
+    B.s_cons = a.take<Cons<R>>(ncap);
+    B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
+    B.order_out = a.take<int>(ncap);
+}
+}  // namespace
+
+struct gb_batch {
+    int prec = GB_PREC_F64;
+    int nw = 0, nb = 0, nf = 0, ncap = 0;
+    std::vector<WorldHdr> hdr;     // host copy of the headers at creation
+    std::vector<int> launch_order; // worlds sorted by body count, largest first
+    char *arena = nullptr;
+    size_t arena_bytes = 0;
+    Batch<double> bd{};
+    Batch<float> bf{};
+    int *d_worlds = nullptr;
+    gb_body *d_bstage = nullptr;
+    gb_contact *d_cstage = nullptr;
+    int cstage_cap = 0;
+    long long counters[3] = {0, 0, 0};
+};
+
+extern "C" {
+
+const char *gb_version(void) { return "gb2d 0.1 sm_103a"; }
+const char *gb_last_error(void) { return g_err.c_str(); }
+
+int gb_struct_sizes(int32_t *sizes) {
+    if (!sizes) return fail(GB_E_ARG, "sizes is NULL");
+    sizes[0] = (int32_t)sizeof(gb_body);
+    sizes[1] = (int32_t)sizeof(gb_fixture);
+    sizes[2] = (int32_t)sizeof(gb_contact);
+    sizes[3] = (int32_t)sizeof(gb_world_desc);
+    sizes[4] = (int32_t)sizeof(gb_scene);
+    sizes[5] = (int32_t)sizeof(gb_step_opts);
+    return 0;
+}
+
+int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
+    if (!scene || !out) return fail(GB_E_ARG, "scene or out is NULL");
+    if (precision != GB_PREC_F64 && precision != GB_PREC_F32) return fail(GB_E_ARG, "precision must be GB_PREC_F64 or GB_PREC_F32");
+    if (scene->n_worlds <= 0) return fail(GB_E_ARG, "scene has no worlds");
+    gb_batch *b = new gb_batch();
+    b->prec = precision;
+    b->nw = scene->n_worlds;
+    b->nb = scene->n_bodies;
+    b->nf = scene->n_fixtures;
+    b->hdr.resize(b->nw);
+    int cbase = 0;
+    for (int i = 0; i < b->nw; ++i) {
+        const gb_world_desc &d = scene->worlds[i];
+        if (i > 0) {   // worlds lie in order, without overlap (per-world scratch is laid out the same way)
+            const gb_world_desc &p = scene->worlds[i - 1];
+            if (d.body_start < p.body_start + p.body_count || d.fixture_start < p.fixture_start + p.fixture_count) {
+                delete b;
+                return fail(GB_E_ARG, "world " + std::to_string(i) + ": body/fixture ranges must follow the previous world's");
+            }
+        }
+        if (d.body_start < 0 || d.body_count < 0 || d.body_start + d.body_count > scene->n_bodies ||
+            d.fixture_start < 0 || d.fixture_count < 0 || d.fixture_start + d.fixture_count > scene->n_fixtures ||
+            d.contact_count < 0 || (d.contact_count > 0 && (!scene->contacts || d.contact_start < 0 ||
+                                                            d.contact_start + d.contact_count > scene->n_contacts))) {
+            delete b;
+            return fail(GB_E_ARG, "world " + std::to_string(i) + ": ranges outside the scene arrays");
+        }
+        for (int k = 0; k < d.fixture_count; ++k) {
+            const gb_fixture &f = scene->fixtures[d.fixture_start + k];
+            if (f.body < 0 || f.body >= d.body_count || f.vertex_count < 1 || f.vertex_count > GB_MAX_POLY_VERTS ||
+                f.shape_type == GB_SHAPE_LOOP || f.shape_type < 0 || f.shape_type > GB_SHAPE_EDGE) {
+                delete b;
+                return fail(GB_E_UNSUPPORTED, "world " + std::to_string(i) + " fixture " + std::to_string(k) +
+                                                  ": unsupported shape or bad body index");
+            }
+        }
+        if (d.move_count < 0 || d.move_count > d.fixture_count ||
+            (d.move_count > 0 && (!scene->moves || d.move_start < 0 || d.move_start + d.move_count > scene->n_moves))) {
+            delete b;
+            return fail(GB_E_ARG, "world " + std::to_string(i) + ": bad move buffer range");
+        }
+        for (int k = 0; k < d.move_count; ++k) {
+            int m = scene->moves[d.move_start + k];
+            if (m < 0 || m >= d.fixture_count) {
+                delete b;
+                return fail(GB_E_ARG, "world " + std::to_string(i) + ": move buffer entry outside the world");
+            }
+        }
+        int cap = d.contact_capacity > 0 ? d.contact_capacity : 6 * d.fixture_count;
+        cap = std::max(std::max(cap, 64), d.contact_count + 16);
+        WorldHdr &h = b->hdr[i];
+        memset(&h, 0, sizeof(h));
+        h.nb = d.body_count; h.nf = d.fixture_count; h.nc = d.contact_count; h.ccap = cap;
+        h.bbase = d.body_start; h.fbase = d.fixture_start; h.cbase = cbase; h.pcap = d.fixture_count;
+        h.flags = d.flags; h.status = 0;
+        h.gx = d.gx; h.gy = d.gy; h.inv_dt0 = d.inv_dt0;
+        h.nmove0 = d.move_count;
+        cbase += cap;
+    }
+    b->ncap = cbase;
+    b->launch_order.resize(b->nw);
+    for (int i = 0; i < b->nw; ++i) b->launch_order[i] = i;
+    std::stable_sort(b->launch_order.begin(), b->launch_order.end(),
+                     [&](int x, int y) { return b->hdr[x].nb > b->hdr[y].nb; });
+    Arena a;
+    if (precision == GB_PREC_F64) carve(a, b->bd, b->nw, b->nb, b->nf, b->ncap);
+    else carve(a, b->bf, b->nw, b->nb, b->nf, b->ncap);
+    size_t bytes = a.off + 256;
+    cudaError_t e = cudaMalloc((void **)&b->arena, bytes);
+    if (e != cudaSuccess) { delete b; return cuda_fail(e, "cudaMalloc(arena)"); }
+    b->arena_bytes = bytes;
+    CK(cudaMemset(b->arena, 0, bytes));
+    Arena a2;
+    a2.base = b->arena;
+    if (precision == GB_PREC_F64) carve(a2, b->bd, b->nw, b->nb, b->nf, b->ncap);
+    else carve(a2, b->bf, b->nw, b->nb, b->nf, b->ncap);
+    CK(cudaMalloc((void **)&b->d_worlds, sizeof(int) * b->nw));
+    CK(cudaMemcpy(b->d_worlds, b->launch_order.data(), sizeof(int) * b->nw, cudaMemcpyHostToDevice));
+    CK(cudaMalloc((void **)&b->d_bstage, sizeof(gb_body) * std::max(1, b->nb)));
+    WorldHdr *d_hdr = precision == GB_PREC_F64 ? b->bd.hdr : b->bf.hdr;
+    CK(cudaMemcpy(d_hdr, b->hdr.data(), sizeof(WorldHdr) * b->nw, cudaMemcpyHostToDevice));
+    if (b->nb > 0) CK(cudaMemcpy(b->d_bstage, scene->bodies, sizeof(gb_body) * b->nb, cudaMemcpyHostToDevice));
+    gb_fixture *d_fst = nullptr;
+    CK(cudaMalloc((void **)&d_fst, sizeof(gb_fixture) * std::max(1, b->nf)));
+    if (b->nf > 0) CK(cudaMemcpy(d_fst, scene->fixtures, sizeof(gb_fixture) * b->nf, cudaMemcpyHostToDevice));
+    if (precision == GB_PREC_F64) {
+        gb_launch_unpack_bodies<double>(b->bd, b->d_bstage, b->nb, 0);
+        gb_launch_unpack_fixtures<double>(b->bd, d_fst, b->nf, 0);
+    } else {
+        gb_launch_unpack_bodies<float>(b->bf, b->d_bstage, b->nb, 0);
+        gb_launch_unpack_fixtures<float>(b->bf, d_fst, b->nf, 0);
+    }
+    {
+        // pending move buffers go to the front of each world's s_move slice
+        std::vector<int> mv(std::max(1, b->nf), 0);
+        bool any = false;
+        for (int i = 0; i < b->nw; ++i) {
+            const gb_world_desc &d = scene->worlds[i];
+            for (int k = 0; k < d.move_count; ++k) { mv[d.fixture_start + k] = scene->moves[d.move_start + k]; any = true; }
+        }
+        int *d_move = precision == GB_PREC_F64 ? b->bd.s_move : b->bf.s_move;
+        if (any) CK(cudaMemcpy(d_move, mv.data(), sizeof(int) * b->nf, cudaMemcpyHostToDevice));
+    }
+    if (scene->n_contacts > 0 && scene->contacts) {
+        std::vector<gb_contact> hc;
+        std::vector<int> slots;
+        for (int i = 0; i < b->nw; ++i) {
+            const gb_world_desc &d = scene->worlds[i];
+            for (int k = 0; k < d.contact_count; ++k) {
+                hc.push_back(scene->contacts[d.contact_start + k]);
+                slots.push_back(b->hdr[i].cbase + k);
+            }
+        }
+        if (!hc.empty()) {
+            gb_contact *d_c = nullptr;
+            int *d_s = nullptr;
+            CK(cudaMalloc((void **)&d_c, sizeof(gb_contact) * hc.size()));
+            CK(cudaMalloc((void **)&d_s, sizeof(int) * slots.size()));
+            CK(cudaMemcpy(d_c, hc.data(), sizeof(gb_contact) * hc.size(), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(d_s, slots.data(), sizeof(int) * slots.size(), cudaMemcpyHostToDevice));
+            if (precision == GB_PREC_F64) gb_launch_unpack_contacts<double>(b->bd, d_c, d_s, (int)hc.size(), 0);
+            else gb_launch_unpack_contacts<float>(b->bf, d_c, d_s, (int)hc.size(), 0);
+            CK(cudaDeviceSynchronize());
+            cudaFree(d_c);
+            cudaFree(d_s);
+        }
+    }
+    CK(cudaDeviceSynchronize());
+    cudaFree(d_fst);
+    *out = b;
+    return 0;
+}
+
+int gb_batch_destroy(gb_batch *b) {
+    if (!b) return 0;
+    cudaFree(b->arena);
+    cudaFree(b->d_worlds);
+    cudaFree(b->d_bstage);
+    cudaFree(b->d_cstage);
+    delete b;
+    return 0;
+}
+
+int gb_batch_step(gb_batch *b, const gb_step_opts *o, void *stream) {
+    if (!b || !o) return fail(GB_E_ARG, "batch or opts is NULL");
+    if (o->n_steps < 0 || o->vel_iters < 0 || o->pos_iters < 0) return fail(GB_E_ARG, "negative step count or iterations");
+    cudaStream_t st = (cudaStream_t)stream;
+    StepParams sp;
+    sp.dt = o->dt;
+    sp.inv_dt = o->dt > 0.0 ? 1.0 / o->dt : 0.0;
+    sp.dt_ratio = 0.0;
+    sp.vel_iters = o->vel_iters;
+    sp.pos_iters = o->pos_iters;
+    sp.record_order = o->record_order;
+    int mode = o->launch_mode == 2 ? 2 : 1;
+    int threads = o->block_threads > 0 ? o->block_threads : (mode == 2 ? 128 : 128);
+    if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
+    int rc = b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st)
+                                    : gb_launch_step<float>(b->bf, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st);
+    if (rc) return cuda_fail((cudaError_t)rc, "step launch");
+    b->counters[0] += 1;
+    b->counters[2] += o->n_steps;
+    return 0;
+}
+
+int gb_batch_set_bodies(gb_batch *b, const gb_body *bodies, int32_t n, void *stream) {
+    if (!b || !bodies) return fail(GB_E_ARG, "batch or bodies is NULL");
+    if (n != b->nb) return fail(GB_E_ARG, "body count mismatch");
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(b->d_bstage, bodies, sizeof(gb_body) * n, cudaMemcpyHostToDevice, st));
+    if (b->prec == GB_PREC_F64) gb_launch_unpack_bodies<double>(b->bd, b->d_bstage, n, st);
+    else gb_launch_unpack_bodies<float>(b->bf, b->d_bstage, n, st);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int gb_batch_get_bodies(gb_batch *b, gb_body *bodies, int32_t n, void *stream) {
+    if (!b || !bodies) return fail(GB_E_ARG, "batch or bodies is NULL");
+    if (n != b->nb) return fail(GB_E_ARG, "body count mismatch");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (b->prec == GB_PREC_F64) gb_launch_pack_bodies<double>(b->bd, b->d_bstage, n, st);
+    else gb_launch_pack_bodies<float>(b->bf, b->d_bstage, n, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(bodies, b->d_bstage, sizeof(gb_body) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_get_proxies(gb_batch *b, double *aabbs, int32_t n, void *stream) {
+    if (!b || !aabbs) return fail(GB_E_ARG, "batch or aabbs is NULL");
+    if (n != b->nf) return fail(GB_E_ARG, "fixture count mismatch");
+    cudaStream_t st = (cudaStream_t)stream;
+    const dbox *src = b->prec == GB_PREC_F64 ? b->bd.f_aabb : b->bf.f_aabb;
+    CK(cudaMemcpyAsync(aabbs, src, sizeof(dbox) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+static int read_headers(gb_batch *b, std::vector<WorldHdr> &h, cudaStream_t st) {
+    h.resize(b->nw);
+    const WorldHdr *src = b->prec == GB_PREC_F64 ? b->bd.hdr : b->bf.hdr;
+    CK(cudaMemcpyAsync(h.data(), src, sizeof(WorldHdr) * b->nw, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_get_contact_counts(gb_batch *b, int32_t *counts, void *stream) {
+    if (!b || !counts) return fail(GB_E_ARG, "batch or counts is NULL");
+    std::vector<WorldHdr> h;
+    int rc = read_headers(b, h, (cudaStream_t)stream);
+    if (rc) return rc;
+    for (int i = 0; i < b->nw; ++i) counts[i] = h[i].nc;
+    return 0;
+}
+
+int gb_batch_get_contacts(gb_batch *b, int32_t world, gb_contact *out, int32_t capacity, int32_t *n_out, void *stream) {
+    if (!b || !out || !n_out) return fail(GB_E_ARG, "NULL argument");
+    if (world < 0 || world >= b->nw) return fail(GB_E_ARG, "world index out of range");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<WorldHdr> h;
+    int rc = read_headers(b, h, st);
+    if (rc) return rc;
+    int n = h[world].nc;
+    *n_out = n;
+    if (n > capacity) return fail(GB_E_ARG, "capacity too small for the world's contacts");
+    if (n == 0) return 0;
+    if (b->cstage_cap < n) {
+        cudaFree(b->d_cstage);
+        b->d_cstage = nullptr;
+        CK(cudaMalloc((void **)&b->d_cstage, sizeof(gb_contact) * n));
+        b->cstage_cap = n;
+    }
+    if (b->prec == GB_PREC_F64) gb_launch_pack_contacts<double>(b->bd, b->d_cstage, h[world].cbase, n, st);
+    else gb_launch_pack_contacts<float>(b->bf, b->d_cstage, h[world].cbase, n, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, b->d_cstage, sizeof(gb_contact) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_get_solver_order(gb_batch *b, int32_t world, int32_t *order, int32_t capacity, int32_t *n_out, void *stream) {
+    if (!b || !order || !n_out) return fail(GB_E_ARG, "NULL argument");
+    if (world < 0 || world >= b->nw) return fail(GB_E_ARG, "world index out of range");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<WorldHdr> h;
+    int rc = read_headers(b, h, st);
+    if (rc) return rc;
+    int n = h[world].last_ncons;
+    *n_out = n;
+    if (n > capacity) return fail(GB_E_ARG, "capacity too small");
+    const int *src = (b->prec == GB_PREC_F64 ? b->bd.order_out : b->bf.order_out) + h[world].cbase;
+    if (n > 0) CK(cudaMemcpyAsync(order, src, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_status(gb_batch *b, uint32_t *status, void *stream) {
+    if (!b || !status) return fail(GB_E_ARG, "NULL argument");
+    std::vector<WorldHdr> h;
+    int rc = read_headers(b, h, (cudaStream_t)stream);
+    if (rc) return rc;
+    for (int i = 0; i < b->nw; ++i) status[i] = h[i].status;
+    return 0;
+}
+
+int gb_batch_counters(gb_batch *b, int64_t *c) {
+    if (!b || !c) return fail(GB_E_ARG, "NULL argument");
+    c[0] = b->counters[0];
+    c[1] = 0;
+    c[2] = b->counters[2];
+    return 0;
+}
+
+}  // extern "C"

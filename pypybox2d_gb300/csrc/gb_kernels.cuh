@@ -1,0 +1,126 @@
+// gb_kernels.cuh -- host-callable launchers of the step kernel and of the
+// body pack/unpack kernels for one precision.  Included by gb_f64.cu
+// (GB_REAL = double, compiled without FMA contraction so the float64 path
+// reproduces the CPU restatement bit for bit) and gb_f32.cu (GB_REAL = float).
+#pragma once
+#include <cuda_runtime.h>
+#include "gb_toi.cuh"
+#include "gb_launch.h"
+
+namespace {
+
+__global__ void k_unpack_bodies(Batch<GB_REAL> B, const gb_body *src, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const gb_body &s = src[i];
+    B.b_type[i] = s.type; B.b_flags[i] = s.flags; B.b_fstart[i] = s.fixture_start; B.b_fcount[i] = s.fixture_count;
+    B.b_xp[i] = mk<double>(s.px, s.py);
+    rot2<double> q; q.c = s.qc; q.s = s.qs; B.b_xq[i] = q;
+    B.b_lc[i] = mk<double>(s.lcx, s.lcy); B.b_c[i] = mk<double>(s.cx, s.cy); B.b_c0[i] = mk<double>(s.c0x, s.c0y);
+    B.b_a[i] = s.a; B.b_a0[i] = s.a0; B.b_alpha0[i] = s.alpha0;
+    B.b_v[i] = mk<GB_REAL>((GB_REAL)s.vx, (GB_REAL)s.vy); B.b_w[i] = (GB_REAL)s.w;
+    B.b_f[i] = mk<GB_REAL>((GB_REAL)s.fx, (GB_REAL)s.fy); B.b_torque[i] = (GB_REAL)s.torque;
+    B.b_inv_mass[i] = (GB_REAL)s.inv_mass; B.b_inv_I[i] = (GB_REAL)s.inv_I;
+    B.b_ldamp[i] = (GB_REAL)s.linear_damping; B.b_adamp[i] = (GB_REAL)s.angular_damping;
+    B.b_gscale[i] = (GB_REAL)s.gravity_scale;
+    B.b_mass[i] = s.mass; B.b_I[i] = s.I; B.b_sleep[i] = s.sleep_time;
+}
+
+__global__ void k_pack_bodies(Batch<GB_REAL> B, gb_body *dst, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    gb_body s;
+    s.type = B.b_type[i]; s.flags = B.b_flags[i]; s.fixture_start = B.b_fstart[i]; s.fixture_count = B.b_fcount[i];
+    s.px = B.b_xp[i].x; s.py = B.b_xp[i].y; s.qc = B.b_xq[i].c; s.qs = B.b_xq[i].s;
+    s.lcx = B.b_lc[i].x; s.lcy = B.b_lc[i].y; s.c0x = B.b_c0[i].x; s.c0y = B.b_c0[i].y;
+    s.cx = B.b_c[i].x; s.cy = B.b_c[i].y; s.a0 = B.b_a0[i]; s.a = B.b_a[i]; s.alpha0 = B.b_alpha0[i];
+    s.vx = (double)B.b_v[i].x; s.vy = (double)B.b_v[i].y; s.w = (double)B.b_w[i];
+    s.fx = (double)B.b_f[i].x; s.fy = (double)B.b_f[i].y; s.torque = (double)B.b_torque[i];
+    s.mass = B.b_mass[i]; s.inv_mass = (double)B.b_inv_mass[i]; s.I = B.b_I[i]; s.inv_I = (double)B.b_inv_I[i];
+    s.linear_damping = (double)B.b_ldamp[i]; s.angular_damping = (double)B.b_adamp[i];
+    s.gravity_scale = (double)B.b_gscale[i]; s.sleep_time = B.b_sleep[i];
+    dst[i] = s;
+}
+
+__global__ void k_unpack_fixtures(Batch<GB_REAL> B, const gb_fixture *src, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const gb_fixture &f = src[i];
+    B.f_body[i] = f.body; B.f_type[i] = f.shape_type; B.f_count[i] = f.vertex_count; B.f_flags[i] = f.flags;
+    B.f_radius[i] = (GB_REAL)f.radius; B.f_friction[i] = (GB_REAL)f.friction;
+    B.f_restitution[i] = (GB_REAL)f.restitution; B.f_density[i] = f.density;
+    B.f_cat[i] = f.category_bits; B.f_mask[i] = f.mask_bits; B.f_group[i] = f.group_index;
+    for (int k = 0; k < GB_MAX_POLY_VERTS; ++k) {
+        B.f_v[(size_t)i * GB_MAX_POLY_VERTS + k] = mk<GB_REAL>((GB_REAL)f.vx[k], (GB_REAL)f.vy[k]);
+        B.f_n[(size_t)i * GB_MAX_POLY_VERTS + k] = mk<GB_REAL>((GB_REAL)f.nx[k], (GB_REAL)f.ny[k]);
+    }
+    B.f_aabb[i] = mkbox(f.aabb[0], f.aabb[1], f.aabb[2], f.aabb[3]);
+}
+
+// contacts: host records (one world per launch range) <-> device ContactRec
+__global__ void k_unpack_contacts(Batch<GB_REAL> B, const gb_contact *src, const int *dst_slot, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const gb_contact &g = src[i];
+    ContactRec<GB_REAL> c;
+    c.fa = g.fixture_a; c.fb = g.fixture_b; c.flags = g.flags; c.toi_count = g.toi_count; c.toi = g.toi;
+    c.friction = (GB_REAL)g.friction; c.restitution = (GB_REAL)g.restitution;
+    c.m.type = g.m_type; c.m.count = g.m_point_count;
+    c.m.ln = mk<GB_REAL>((GB_REAL)g.m_lnx, (GB_REAL)g.m_lny); c.m.lp = mk<GB_REAL>((GB_REAL)g.m_lpx, (GB_REAL)g.m_lpy);
+    for (int k = 0; k < 2; ++k) {
+        c.m.plp[k] = mk<GB_REAL>((GB_REAL)g.p_lx[k], (GB_REAL)g.p_ly[k]);
+        c.m.ni[k] = (GB_REAL)g.p_ni[k]; c.m.ti[k] = (GB_REAL)g.p_ti[k]; c.m.id[k] = g.p_id[k];
+    }
+    B.c[dst_slot[i]] = c;
+}
+
+__global__ void k_pack_contacts(Batch<GB_REAL> B, gb_contact *dst, int base, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ContactRec<GB_REAL> &c = B.c[base + i];
+    gb_contact g;
+    g.fixture_a = c.fa; g.fixture_b = c.fb; g.child_a = 0; g.child_b = 0;
+    g.flags = c.flags; g.toi_count = c.toi_count; g.toi = c.toi;
+    g.friction = (double)c.friction; g.restitution = (double)c.restitution;
+    g.m_type = c.m.type; g.m_point_count = c.m.count;
+    g.m_lnx = (double)c.m.ln.x; g.m_lny = (double)c.m.ln.y; g.m_lpx = (double)c.m.lp.x; g.m_lpy = (double)c.m.lp.y;
+    for (int k = 0; k < 2; ++k) {
+        g.p_lx[k] = (double)c.m.plp[k].x; g.p_ly[k] = (double)c.m.plp[k].y;
+        g.p_ni[k] = (double)c.m.ni[k]; g.p_ti[k] = (double)c.m.ti[k]; g.p_id[k] = c.m.id[k];
+    }
+    dst[i] = g;
+}
+
+}  // namespace
+
+template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *d_worlds,
+                                        int n_list, int mode, int threads, cudaStream_t st) {
+    if (n_list <= 0) return 0;
+    // the step kernels use ~220 registers per thread: at most 256 threads per CTA
+    if (threads > 256) threads = 256;
+    if (mode == 2) {
+        int wpc = threads / 32;
+        if (wpc < 1) wpc = 1;
+        int blocks = (n_list + wpc - 1) / wpc;
+        k_step_warp<GB_REAL><<<blocks, wpc * 32, 0, st>>>(B, sp, n_steps, d_worlds, n_list);
+    } else {
+        k_step_cta<GB_REAL><<<n_list, threads, 0, st>>>(B, sp, n_steps, d_worlds);
+    }
+    return (int)cudaGetLastError();
+}
+
+template <> void gb_launch_unpack_bodies<GB_REAL>(const Batch<GB_REAL> &B, const gb_body *d, int n, cudaStream_t st) {
+    if (n > 0) k_unpack_bodies<<<(n + 255) / 256, 256, 0, st>>>(B, d, n);
+}
+template <> void gb_launch_pack_bodies<GB_REAL>(const Batch<GB_REAL> &B, gb_body *d, int n, cudaStream_t st) {
+    if (n > 0) k_pack_bodies<<<(n + 255) / 256, 256, 0, st>>>(B, d, n);
+}
+template <> void gb_launch_unpack_fixtures<GB_REAL>(const Batch<GB_REAL> &B, const gb_fixture *d, int n, cudaStream_t st) {
+    if (n > 0) k_unpack_fixtures<<<(n + 255) / 256, 256, 0, st>>>(B, d, n);
+}
+template <> void gb_launch_unpack_contacts<GB_REAL>(const Batch<GB_REAL> &B, const gb_contact *d, const int *slots, int n, cudaStream_t st) {
+    if (n > 0) k_unpack_contacts<<<(n + 255) / 256, 256, 0, st>>>(B, d, slots, n);
+}
+template <> void gb_launch_pack_contacts<GB_REAL>(const Batch<GB_REAL> &B, gb_contact *d, int base, int n, cudaStream_t st) {
+    if (n > 0) k_pack_contacts<<<(n + 255) / 256, 256, 0, st>>>(B, d, base, n);
+}

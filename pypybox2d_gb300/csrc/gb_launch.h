@@ -1,0 +1,26 @@
+// gb_launch.h -- launchers shared by the precision translation units
+// (gb_f64.cu, gb_f32.cu) and the C ABI (gb_api.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include "gb_world.cuh"
+
+template <class R> int gb_launch_step(const Batch<R> &B, const StepParams &sp, int n_steps, const int *d_worlds, int n_list,
+                                      int mode, int threads, cudaStream_t st);
+template <class R> void gb_launch_unpack_bodies(const Batch<R> &B, const gb_body *d, int n, cudaStream_t st);
+template <class R> void gb_launch_pack_bodies(const Batch<R> &B, gb_body *d, int n, cudaStream_t st);
+template <class R> void gb_launch_unpack_fixtures(const Batch<R> &B, const gb_fixture *d, int n, cudaStream_t st);
+template <class R> void gb_launch_unpack_contacts(const Batch<R> &B, const gb_contact *d, const int *slots, int n, cudaStream_t st);
+template <class R> void gb_launch_pack_contacts(const Batch<R> &B, gb_contact *d, int base, int n, cudaStream_t st);
+
+template <> int gb_launch_step<double>(const Batch<double> &, const StepParams &, int, const int *, int, int, int, cudaStream_t);
+template <> int gb_launch_step<float>(const Batch<float> &, const StepParams &, int, const int *, int, int, int, cudaStream_t);
+template <> void gb_launch_unpack_bodies<double>(const Batch<double> &, const gb_body *, int, cudaStream_t);
+template <> void gb_launch_unpack_bodies<float>(const Batch<float> &, const gb_body *, int, cudaStream_t);
+template <> void gb_launch_pack_bodies<double>(const Batch<double> &, gb_body *, int, cudaStream_t);
+template <> void gb_launch_pack_bodies<float>(const Batch<float> &, gb_body *, int, cudaStream_t);
+template <> void gb_launch_unpack_fixtures<double>(const Batch<double> &, const gb_fixture *, int, cudaStream_t);
+template <> void gb_launch_unpack_fixtures<float>(const Batch<float> &, const gb_fixture *, int, cudaStream_t);
+template <> void gb_launch_unpack_contacts<double>(const Batch<double> &, const gb_contact *, const int *, int, cudaStream_t);
+template <> void gb_launch_unpack_contacts<float>(const Batch<float> &, const gb_contact *, const int *, int, cudaStream_t);
+template <> void gb_launch_pack_contacts<double>(const Batch<double> &, gb_contact *, int, int, cudaStream_t);
+template <> void gb_launch_pack_contacts<float>(const Batch<float> &, gb_contact *, int, int, cudaStream_t);

@@ -1,0 +1,978 @@
+// gb_step.cuh -- World.step (pypybox2d/world.py:307-354) for one world,
+// executed by one group of threads (see gb_world.cuh).
+//
+// Phases and the reference code each one replaces:
+//   pair finding ..... broadphase.py:83-109 + contact_manager.py:102-158
+//   collide .......... contact_manager.py:174-223 + contact.py:210-268
+//   islands .......... world.py:475-573 (union-find; depth-first order only
+//                      where the reference's result depends on it)
+//   contact solver ... island.py:65-179 + contact.py:375-864, Gauss-Seidel
+//                      over graph-coloured constraint batches
+//   fixture sync ..... world.py:582-589, body.py:879-885, fixture.py:287-298,
+//                      dynamictree.py:152-188
+//   continuous ....... world.py:594-821, island.py:181-243, contact.py:866-933
+#pragma once
+#include "gb_world.cuh"
+
+#define GB_MAX_TRANSLATION 2.0
+#define GB_MAX_TRANSLATION_SQR 4.0
+#define GB_MAX_ROTATION (0.5 * 3.141592653589793)
+#define GB_MAX_ROTATION_SQR 2.4674011002723395
+#define GB_BAUMGARTE 0.2
+#define GB_TOI_BAUMGARTE 0.75
+#define GB_MAX_LINEAR_CORRECTION 0.2
+#define GB_VELOCITY_THRESHOLD 1.0
+#define GB_TIME_TO_SLEEP 0.5
+#define GB_LINEAR_SLEEP_TOL_SQR 0.0001
+#define GB_ANGULAR_SLEEP_TOL_SQR 0.0012184696791468343
+#define GB_AABB_EXTENSION 0.1
+#define GB_AABB_MULTIPLIER 2.0
+#define GB_MAX_SUB_STEPS 8
+#define GB_MAX_TOI_CONTACTS 32
+#define GB_INF_IDX 0x7fffffff
+
+#define R_SIM 1u      // island is simulated this step
+#define R_DONE 2u     // position iterations finished (early exit)
+#define R_SOLVED 4u   // position_solved
+#define R_DFS 8u      // needs the depth-first body order
+#define R_STATIC_IN 16u  // (bodies) static body attached to a simulated island
+
+
+// Group-shared scratch scalars of one world.
+struct WShared {
+    unsigned long long red;
+    int nmove;
+    int min_contact;
+    double min_alpha;
+    int any_dfs;
+    int ncons, ncolours;
+    int pass;
+    int all_allow_sleep;
+};
+
+// body.py:781-793 awake setter
+template <class R> __device__ __forceinline__ void wake_body(const WView<R> &w, int b) {
+    uint32_t f = w.B.b_flags[w.bb + b];
+    if (!(f & GB_BODY_AWAKE)) { w.B.b_sleep[w.bb + b] = 0.0; w.B.b_flags[w.bb + b] = f | GB_BODY_AWAKE; }
+}
+template <class R> __device__ __forceinline__ void sleep_body(const WView<R> &w, int b) {
+    int g = w.bb + b;
+    w.B.b_sleep[g] = 0.0;
+    w.B.b_v[g] = mk<R>(0, 0); w.B.b_w[g] = (R)0;
+    w.B.b_f[g] = mk<R>(0, 0); w.B.b_torque[g] = (R)0;
+    w.B.b_flags[g] &= ~GB_BODY_AWAKE;
+}
+// body.py:887-889
+template <class R> __device__ __forceinline__ void sync_transform(const WView<R> &w, int b) {
+    int g = w.bb + b;
+    rot2<double> q = rot_of(w.B.b_a[g]);
+    vec2<double> p = w.B.b_c[g] - rmul(q, w.B.b_lc[g]);
+    w.B.b_xp[g] = p; w.B.b_xq[g] = q;
+}
+// body.py:911-918
+template <class R> __device__ void body_advance(const WView<R> &w, int b, double alpha) {
+    Sweep s = w.sweep(b);
+    sweep_advance(s, alpha);
+    s.c = s.c0; s.a = s.a0;
+    w.put_sweep(b, s);
+    rot2<double> q = rot_of(s.a);
+    w.B.b_xq[w.bb + b] = q;
+    w.B.b_xp[w.bb + b] = s.c - rmul(q, s.lc);
+}
+
+// aabbmodule.c AABB_test_overlap
+static __device__ __forceinline__ bool aabb_overlap(dbox a, dbox b) {
+    return !((b.x - a.z) > 0.0 || (b.y - a.w) > 0.0 || (a.x - b.z) > 0.0 || (a.y - b.w) > 0.0);
+}
+
+// world.py:958-970
+template <class R> __device__ __forceinline__ bool default_filter(const WView<R> &w, int fa, int fb) {
+    int ga = w.B.f_group[w.fb + fa], gb = w.B.f_group[w.fb + fb];
+    if (ga == gb && ga != 0) return ga > 0;
+    return ((w.B.f_mask[w.fb + fa] & w.B.f_cat[w.fb + fb]) != 0) && ((w.B.f_cat[w.fb + fa] & w.B.f_mask[w.fb + fb]) != 0);
+}
+template <class R> __device__ __forceinline__ bool should_collide(const WView<R> &w, int ba, int bb) {
+    return w.btype(ba) == GB_BODY_DYNAMIC || w.btype(bb) == GB_BODY_DYNAMIC;
+}
+template <class R> __device__ __forceinline__ bool fx_sensor(const WView<R> &w, int f) {
+    return (w.B.f_flags[w.fb + f] & GB_FIX_SENSOR) != 0;
+}
+
+// contact.py:210-268 Contact.update; returns whether touching changed.
+template <class R> __device__ bool contact_update(const WView<R> &w, int i) {
+    ContactRec<R> &c = w.con(i);
+    Manifold<R> old = c.m;
+    c.flags |= GB_C_ENABLED;
+    bool was = (c.flags & GB_C_TOUCHING) != 0;
+    int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+    Shape<R> sa = w.shape(c.fa), sb = w.shape(c.fb);
+    bool touching;
+    bool changed = false;
+    if (fx_sensor(w, c.fa) || fx_sensor(w, c.fb)) {
+        DProxy pa, pb;
+        dproxy_init(pa, sa); dproxy_init(pb, sb);
+        SCache cache; cache.metric = 0; cache.count = 0;
+        for (int k = 0; k < 3; ++k) { cache.ia[k] = 0; cache.ib[k] = 0; }
+        double d = shape_distance(pa, pb, w.xfd(ba), w.xfd(bb), true, cache);
+        touching = d < 10.0 * GB_EPSILON;
+        c.m.count = 0;
+    } else {
+        evaluate_manifold(c.m, sa, w.xf(ba), sb, w.xf(bb));
+        touching = c.m.count > 0;
+        for (int k = 0; k < c.m.count; ++k) {
+            int found = -1;
+            for (int j = old.count - 1; j >= 0; --j)
+                if (old.id[j] == c.m.id[k]) { found = j; break; }
+            if (found >= 0) { c.m.ni[k] = old.ni[found]; c.m.ti[k] = old.ti[found]; }
+            else { c.m.ni[k] = (R)0; c.m.ti[k] = (R)0; }
+        }
+        changed = touching != was;
+    }
+    if (touching) c.flags |= GB_C_TOUCHING; else c.flags &= ~GB_C_TOUCHING;
+    return changed;
+}
+
+// shapes.py compute_aabb (child 0), float64
+template <class R> __device__ dbox shape_aabb(const WView<R> &w, int f, xform2<double> x) {
+    Shape<R> s = w.shape(f);
+    double r = (double)s.radius;
+    if (s.type == GB_SHAPE_CIRCLE) {
+        vec2<double> p = x.p + rmul(x.q, cvt<double>(s.v[0]));
+        return mkbox(p.x - r, p.y - r, p.x + r, p.y + r);
+    }
+    int n = (s.type == GB_SHAPE_POLYGON) ? s.count : 2;
+    vec2<double> lo = xmul(x, cvt<double>(s.v[0])), hi = lo;
+    for (int i = (s.type == GB_SHAPE_POLYGON ? 0 : 1); i < n; ++i) {
+        vec2<double> v = xmul(x, cvt<double>(s.v[i]));
+        lo = mk<double>(cmin(lo.x, v.x), cmin(lo.y, v.y));
+        hi = mk<double>(cmax(hi.x, v.x), cmax(hi.y, v.y));
+    }
+    return mkbox(lo.x - r, lo.y - r, hi.x + r, hi.y + r);
+}
+
+// body.py:879-885 + fixture.py:287-298 + dynamictree.py:152-188 for one
+// fixture; returns whether the proxy was re-fattened (enters the move buffer).
+template <class R> __device__ bool sync_fixture(const WView<R> &w, int f) {
+    int b = w.fbody(f);
+    int gbi = w.bb + b;
+    xform2<double> x1;
+    x1.q = rot_of(w.B.b_a0[gbi]);
+    x1.p = w.B.b_c0[gbi] - rmul(x1.q, w.B.b_lc[gbi]);
+    xform2<double> x2 = w.xfd(b);
+    dbox a1 = shape_aabb(w, f, x1), a2 = shape_aabb(w, f, x2);
+    dbox ab = mkbox(cmin(a1.x, a2.x), cmin(a1.y, a2.y), cmax(a1.z, a2.z), cmax(a1.w, a2.w));
+    vec2<double> disp = x2.p - x1.p;
+    dbox fat = w.B.f_aabb[w.fb + f];
+    if (fat.x <= ab.x && fat.y <= ab.y && ab.z <= fat.z && ab.w <= fat.w) return false;
+    dbox nb = mkbox(ab.x - GB_AABB_EXTENSION, ab.y - GB_AABB_EXTENSION, ab.z + GB_AABB_EXTENSION, ab.w + GB_AABB_EXTENSION);
+    vec2<double> d = GB_AABB_MULTIPLIER * disp;
+    if (d.x < 0.0) { nb.x = nb.x + d.x; nb.y = nb.y + 0.0; } else { nb.z = nb.z + d.x; nb.w = nb.w + 0.0; }
+    if (d.y < 0.0) { nb.x = nb.x + 0.0; nb.y = nb.y + d.y; } else { nb.z = nb.z + 0.0; nb.w = nb.w + d.y; }
+    w.B.f_aabb[w.fb + f] = nb;
+    return true;
+}
+
+// ------------------------------------------------------------ pair finding
+// broadphase.py:83-109 with the fixed pair order (first move-buffer position
+// of the moved proxy, then the other proxy's index) followed by
+// contact_manager.py:102-158.  The move buffer is s_move[0..nmove).
+template <class R> __device__ __forceinline__ bool pair_candidate(const WView<R> &w, int i, int p, int q, int *first,
+                                                                  unsigned long long *hash, int hmask) {
+    if (q == p) return false;
+    int fq = first[q];
+    if (fq < i) return false;  // emitted when q was processed
+    if (!aabb_overlap(w.B.f_aabb[w.fb + q], w.B.f_aabb[w.fb + p])) return false;
+    int ba = w.fbody(p), bb = w.fbody(q);
+    if (ba == bb) return false;
+    // does a contact already exist?
+    unsigned long long key = ((unsigned long long)(unsigned)min(p, q) << 32) | (unsigned)max(p, q);
+    key += 1ull;
+    unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 32) & hmask;
+    for (int probe = 0; probe <= hmask; ++probe) {
+        unsigned long long k = hash[h];
+        if (k == key) return false;
+        if (k == 0ull) break;
+        h = (h + 1) & hmask;
+    }
+    if (!should_collide(w, bb, ba)) return false;
+    if (!default_filter(w, p, q)) return false;
+    bool prim;
+    if (!pair_registered(w.B.f_type[w.fb + p], w.B.f_type[w.fb + q], &prim)) return false;
+    return true;
+}
+
+template <class R, class G> __device__ void find_new_contacts(const G &g, const WView<R> &w, WShared *sh) {
+    int nmove = sh->nmove;
+    int nf = w.H->nf;
+    int *first = w.B.s_first + w.fb;
+    int *mv = w.B.s_move + w.fb;
+    int *cnt = w.B.s_cnt + w.fb;
+    unsigned long long *hash = w.B.s_hash + 4 * (size_t)w.cb;
+    int hcap = 1;
+    while (hcap < 2 * w.H->ccap) hcap <<= 1;
+    int hmask = hcap - 1;
+    if (nmove == 0) return;
+    for (int f = g.rank(); f < nf; f += g.size()) first[f] = GB_INF_IDX;
+    for (int k = g.rank(); k < hcap; k += g.size()) hash[k] = 0ull;
+    g.sync();
+    for (int i = g.rank(); i < nmove; i += g.size()) atomicMin(&first[mv[i]], i);
+    int nc = w.H->nc;
+    for (int i = g.rank(); i < nc; i += g.size()) {
+        const ContactRec<R> &c = w.con(i);
+        unsigned long long key = ((unsigned long long)(unsigned)min(c.fa, c.fb) << 32) | (unsigned)max(c.fa, c.fb);
+        key += 1ull;
+        unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 32) & hmask;
+        for (int probe = 0; probe <= hmask; ++probe) {
+            unsigned long long prev = atomicCAS(&hash[h], 0ull, key);
+            if (prev == 0ull || prev == key) break;
+            h = (h + 1) & hmask;
+        }
+    }
+    g.sync();
+    // pass 1: count survivors per move-buffer entry
+    for (int i = g.rank(); i < nmove; i += g.size()) {
+        int p = mv[i];
+        int n = 0;
+        if (first[p] == i)
+            for (int q = 0; q < nf; ++q) n += pair_candidate(w, i, p, q, first, hash, hmask) ? 1 : 0;
+        cnt[i] = n;
+    }
+    g.sync();
+    int total = group_scan(g, nmove, [&](int i) { return cnt[i]; }, cnt);
+    g.sync();
+    int ccap = w.H->ccap;
+    // pass 2: create the contacts in order (contact.py:313-326 _create)
+    for (int i = g.rank(); i < nmove; i += g.size()) {
+        int p = mv[i];
+        if (first[p] != i) continue;
+        int pos = nc + cnt[i];
+        for (int q = 0; q < nf; ++q) {
+            if (!pair_candidate(w, i, p, q, first, hash, hmask)) continue;
+            if (pos < ccap) {
+                int fa = p, fb = q;
+                bool prim;
+                pair_registered(w.B.f_type[w.fb + p], w.B.f_type[w.fb + q], &prim);
+                if (!prim) { fa = q; fb = p; }
+                ContactRec<R> &c = w.con(pos);
+                c.fa = fa; c.fb = fb;
+                c.flags = 0; c.toi_count = 0; c.toi = 0.0;
+                R fra = w.B.f_friction[w.fb + fa], frb = w.B.f_friction[w.fb + fb];
+                c.friction = sqrt(fra * frb);
+                c.restitution = pymax(w.B.f_restitution[w.fb + fa], w.B.f_restitution[w.fb + fb]);
+                Manifold<R> &m = c.m;
+                m.type = GB_M_CIRCLES; m.count = 0;
+                m.ln = mk<R>(0, 0); m.lp = mk<R>(0, 0);
+                for (int k = 0; k < 2; ++k) { m.plp[k] = mk<R>(0, 0); m.ni[k] = (R)0; m.ti[k] = (R)0; m.id[k] = 0; }
+            }
+            ++pos;
+        }
+    }
+    g.sync();
+    if (g.rank() == 0) {
+        int nn = nc + total;
+        if (nn > ccap) { w.H->status |= GB_ST_CONTACT_OVERFLOW; nn = ccap; }
+        w.H->nc = nn;
+        sh->nmove = 0;
+    }
+    g.sync();
+}
+
+// ------------------------------------------------------------ collide
+template <class R, class G> __device__ void collide(const G &g, const WView<R> &w) {
+    int nb = w.H->nb, nc = w.H->nc;
+    int *wake = w.B.s_wake + w.bb;
+    int *proc = w.B.s_proc + w.cb;     // 0 = not processed, 1 = processed, 2 = destroy
+    for (int b = g.rank(); b < nb; b += g.size())
+        wake[b] = (w.awake(b) && w.btype(b) != GB_BODY_STATIC) ? -1 : GB_INF_IDX;
+    for (int i = g.rank(); i < nc; i += g.size()) proc[i] = 0;
+    g.sync();
+    // Least fixed point of the sequential rule "contact i is updated iff one
+    // of its bodies is non-static and awake when the loop reaches i"; a body
+    // woken by contact j counts as awake for contacts after j.
+    for (int round = 0; round <= nc + 1; ++round) {
+        bool changed = false;
+        for (int i = g.rank(); i < nc; i += g.size()) {
+            if (proc[i]) continue;
+            ContactRec<R> &c = w.con(i);
+            int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+            bool act_a = w.btype(ba) != GB_BODY_STATIC && wake[ba] < i;
+            bool act_b = w.btype(bb) != GB_BODY_STATIC && wake[bb] < i;
+            if (!act_a && !act_b) continue;
+            proc[i] = 1;
+            if (c.flags & GB_C_FILTER) {
+                if (!should_collide(w, bb, ba) || !default_filter(w, c.fa, c.fb)) { proc[i] = 2; continue; }
+                c.flags &= ~GB_C_FILTER;
+            }
+            if (!aabb_overlap(w.B.f_aabb[w.fb + c.fa], w.B.f_aabb[w.fb + c.fb])) { proc[i] = 2; continue; }
+            if (contact_update(w, i)) {
+                int oa = atomicMin(&wake[ba], i);
+                int ob = atomicMin(&wake[bb], i);
+                if (oa > i || ob > i) changed = true;
+            }
+        }
+        if (!g.any(changed)) break;
+    }
+    g.sync();
+    for (int b = g.rank(); b < nb; b += g.size())
+        if (wake[b] >= 0 && wake[b] != GB_INF_IDX) wake_body(w, b);
+    // destroy (contact_manager.py:160-172), keeping creation order
+    int *pref = w.B.s_pref + w.cb;
+    int alive = group_scan(g, nc, [&](int i) { return proc[i] == 2 ? 0 : 1; }, pref);
+    g.sync();
+    if (alive != nc) {
+        for (int base = 0; base < nc; base += g.size()) {
+            int i = base + g.rank();
+            ContactRec<R> rec;
+            bool keep = i < nc && proc[i] != 2;
+            if (keep) rec = w.con(i);
+            g.sync();
+            if (keep) w.con(pref[i]) = rec;
+            g.sync();
+        }
+        if (g.rank() == 0) w.H->nc = alive;
+    }
+    g.sync();
+}
+
+// ------------------------------------------------------------ contact solver
+// contact.py:375-412 + 414-496
+template <class R> __device__ void build_cons(const WView<R> &w, Cons<R> &k, int ci, bool warm, double dt_ratio) {
+    const ContactRec<R> &c = w.con(ci);
+    int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+    k.cidx = ci; k.ia = ba; k.ib = bb;
+    k.ma = w.B.b_inv_mass[w.bb + ba]; k.mb = w.B.b_inv_mass[w.bb + bb];
+    k.iA = w.B.b_inv_I[w.bb + ba]; k.iB = w.B.b_inv_I[w.bb + bb];
+    k.lca = cvt<R>(w.B.b_lc[w.bb + ba]); k.lcb = cvt<R>(w.B.b_lc[w.bb + bb]);
+    k.ra = w.B.f_radius[w.fb + c.fa]; k.rb = w.B.f_radius[w.fb + c.fb];
+    k.friction = c.friction; k.restitution = c.restitution;
+    k.mcount = c.m.count; k.npts = c.m.count; k.mtype = c.m.type;
+    k.ln = c.m.ln; k.lp = c.m.lp;
+    for (int j = 0; j < c.m.count; ++j) {
+        k.lpts[j] = c.m.plp[j];
+        if (warm) { k.ni[j] = (R)dt_ratio * c.m.ni[j]; k.ti[j] = (R)dt_ratio * c.m.ti[j]; }
+        else { k.ni[j] = c.m.ni[j]; k.ti[j] = c.m.ti[j]; }
+    }
+}
+
+template <class R> __device__ __forceinline__ xform2<R> pose_xf(vec2<double> c, double a, vec2<R> lc) {
+    xform2<R> x;
+    x.q = Rot<R>::of(a);
+    x.p = cvt<R>(c) - rmul(x.q, lc);
+    return x;
+}
+
+// contact.py:414-496 initialize_velocity_constraints + contact_util.py:195-245
+template <class R> __device__ void init_velocity(Cons<R> &k, vec2<double> ca, double aa, vec2<double> cb, double ab,
+                                                 vec2<R> va, R wa, vec2<R> vb, R wb) {
+    xform2<R> xa = pose_xf<R>(ca, aa, k.lca), xb = pose_xf<R>(cb, ab, k.lcb);
+    vec2<R> normal, pts[2];
+    if (k.mtype == GB_M_CIRCLES) {
+        normal = mk<R>(1, 0);
+        vec2<R> pA = xmul(xa, k.lp), pB = xmul(xb, k.lpts[0]);
+        vec2<R> dd = pA - pB;
+        if (dot(dd, dd) > (R)GB_EPSILON_SQR) normal = normalized(pB - pA);
+        vec2<R> cA = pA + k.ra * normal, cB = pB - k.rb * normal;
+        pts[0] = (R)0.5 * (cA + cB);
+    } else if (k.mtype == GB_M_FACE_A) {
+        normal = rmul(xa.q, k.ln);
+        vec2<R> plane = xmul(xa, k.lp);
+        for (int i = 0; i < k.mcount; ++i) {
+            vec2<R> clip = xmul(xb, k.lpts[i]);
+            vec2<R> cA = clip + (k.ra - dot(clip - plane, normal)) * normal;
+            vec2<R> cB = clip - k.rb * normal;
+            pts[i] = (R)0.5 * (cA + cB);
+        }
+    } else {
+        normal = rmul(xb.q, k.ln);
+        vec2<R> plane = xmul(xb, k.lp);
+        for (int i = 0; i < k.mcount; ++i) {
+            vec2<R> clip = xmul(xa, k.lpts[i]);
+            vec2<R> cB = clip + (k.rb - dot(clip - plane, normal)) * normal;
+            vec2<R> cA = clip - k.ra * normal;
+            pts[i] = (R)0.5 * (cA + cB);
+        }
+        normal = -normal;
+    }
+    k.normal = normal;
+    vec2<R> tangent = cross(normal, (R)1);
+    vec2<R> car = cvt<R>(ca), cbr = cvt<R>(cb);
+    for (int i = 0; i < k.npts; ++i) {
+        vec2<R> ra = pts[i] - car, rb = pts[i] - cbr;
+        k.rA[i] = ra; k.rB[i] = rb;
+        R rna = sq(cross(ra, normal)), rnb = sq(cross(rb, normal));
+        R kn = k.ma + k.mb + k.iA * rna + k.iB * rnb;
+        k.nm[i] = kn > (R)0 ? (R)1 / kn : (R)0;
+        R rta = sq(cross(ra, tangent)), rtb = sq(cross(rb, tangent));
+        R kt = k.ma + k.mb + k.iA * rta + k.iB * rtb;
+        k.tm[i] = kt > (R)0 ? (R)1 / kt : (R)0;
+        k.bias[i] = (R)0;
+        R vrel = dot(normal, ((vb + cross(wb, rb)) - va) - cross(wa, ra));
+        if (vrel < (R)-GB_VELOCITY_THRESHOLD) k.bias[i] = -k.restitution * vrel;
+    }
+    if (k.npts == 2) {
+        R rn1a = cross(k.rA[0], normal), rn1b = cross(k.rB[0], normal);
+        R rn2a = cross(k.rA[1], normal), rn2b = cross(k.rB[1], normal);
+        R k11 = k.ma + k.mb + k.iA * rn1a * rn1a + k.iB * rn1b * rn1b;
+        R k22 = k.ma + k.mb + k.iA * rn2a * rn2a + k.iB * rn2b * rn2b;
+        R k12 = k.ma + k.mb + k.iA * rn1a * rn2a + k.iB * rn1b * rn2b;
+        if (sq(k11) < (R)1000 * (k11 * k22 - sq(k12))) {
+            k.k11 = k11; k.k12 = k12; k.k22 = k22;
+            R det = k11 * k22 - k12 * k12;
+            if (det != (R)0) det = (R)1 / det;
+            k.nm11 = det * k22; k.nm12 = -det * k12; k.nm21 = -det * k12; k.nm22 = det * k11;
+        } else {
+            k.npts = 1;
+        }
+    }
+}
+
+// contact.py:498-525
+template <class R> __device__ __forceinline__ void warm_start(const Cons<R> &k, vec2<R> &va, R &wa, vec2<R> &vb, R &wb) {
+    vec2<R> normal = k.normal, tangent = cross(normal, (R)1);
+    for (int i = 0; i < k.npts; ++i) {
+        vec2<R> P = k.ni[i] * normal + k.ti[i] * tangent;
+        wa = wa - k.iA * cross(k.rA[i], P);
+        va = va - k.ma * P;
+        wb = wb + k.iB * cross(k.rB[i], P);
+        vb = vb + k.mb * P;
+    }
+}
+
+// contact.py:527-799
+template <class R> __device__ __forceinline__ void solve_velocity(Cons<R> &k, vec2<R> &va, R &wa, vec2<R> &vb, R &wb) {
+    const R ma = k.ma, mb = k.mb, iA = k.iA, iB = k.iB;
+    vec2<R> normal = k.normal, tangent = cross(normal, (R)1);
+    R friction = k.friction;
+    for (int i = 0; i < k.npts; ++i) {
+        vec2<R> ra = k.rA[i], rb = k.rB[i];
+        vec2<R> dv = ((vb + cross(wb, rb)) - va) - cross(wa, ra);
+        R vt = dot(dv, tangent);
+        R lambda = k.tm[i] * (-vt);
+        R maxf = friction * k.ni[i];
+        R ni = cclamp(k.ti[i] + lambda, -maxf, maxf);
+        lambda = ni - k.ti[i];
+        vec2<R> P = lambda * tangent;
+        va = va - ma * P;
+        wa = wa - iA * cross(ra, P);
+        vb = vb + mb * P;
+        wb = wb + iB * cross(rb, P);
+        k.ti[i] = ni;
+    }
+    if (k.npts == 1) {
+        vec2<R> ra = k.rA[0], rb = k.rB[0];
+        vec2<R> dv = ((vb + cross(wb, rb)) - va) - cross(wa, ra);
+        R vn = dot(dv, normal);
+        R lambda = -k.nm[0] * (vn - k.bias[0]);
+        R ni = pymax(k.ni[0] + lambda, (R)0);
+        lambda = ni - k.ni[0];
+        vec2<R> P = lambda * normal;
+        va = va - ma * P;
+        wa = wa - iA * cross(ra, P);
+        vb = vb + mb * P;
+        wb = wb + iB * cross(rb, P);
+        k.ni[0] = ni;
+    } else {
+        vec2<R> a = mk<R>(k.ni[0], k.ni[1]);
+        vec2<R> ra1 = k.rA[0], rb1 = k.rB[0], ra2 = k.rA[1], rb2 = k.rB[1];
+        vec2<R> dv1 = ((vb + cross(wb, rb1)) - va) - cross(wa, ra1);
+        vec2<R> dv2 = ((vb + cross(wb, rb2)) - va) - cross(wa, ra2);
+        R vn1 = dot(dv1, normal), vn2 = dot(dv2, normal);
+        vec2<R> b = mk<R>(vn1 - k.bias[0], vn2 - k.bias[1]);
+        b = b - mk<R>(k.k11 * a.x + k.k12 * a.y, k.k12 * a.x + k.k22 * a.y);
+        vec2<R> x;
+        bool solved = false;
+        x = mk<R>(-(k.nm11 * b.x + k.nm12 * b.y), -(k.nm21 * b.x + k.nm22 * b.y));
+        if (x.x >= (R)0 && x.y >= (R)0) solved = true;
+        if (!solved) {
+            x = mk<R>(-k.nm[0] * b.x, (R)0);
+            vn2 = k.k12 * x.x + b.y;
+            if (x.x >= (R)0 && vn2 >= (R)0) solved = true;
+        }
+        if (!solved) {
+            x = mk<R>((R)0, -k.nm[1] * b.y);
+            vn1 = k.k12 * x.y + b.x;
+            if (x.y >= (R)0 && vn1 >= (R)0) solved = true;
+        }
+        if (!solved) {
+            x = mk<R>(0, 0);
+            vn1 = b.x; vn2 = b.y;
+            if (vn1 >= (R)0 && vn2 >= (R)0) solved = true;
+        }
+        if (solved) {
+            vec2<R> d = x - a;
+            vec2<R> p1 = d.x * normal, p2 = d.y * normal;
+            va = va - ma * (p1 + p2);
+            wa = wa - iA * (cross(ra1, p1) + cross(ra2, p2));
+            vb = vb + mb * (p1 + p2);
+            wb = wb + iB * (cross(rb1, p1) + cross(rb2, p2));
+            k.ni[0] = x.x; k.ni[1] = x.y;
+        }
+    }
+}
+
+// contact_util.py:323-360 + contact.py:809-864 / 866-933 for one
+// constraint; returns the constraint's running minimum separation.
+template <class R> __device__ double solve_position(const Cons<R> &k, vec2<double> &ca, double &aa, vec2<double> &cb,
+                                                   double &ab, double minsep, bool toi, bool toi_a, bool toi_b) {
+    R ma = k.ma, mb = k.mb, iA = k.iA, iB = k.iB;
+    R baum = (R)GB_BAUMGARTE;
+    if (toi) {
+        baum = (R)GB_TOI_BAUMGARTE;
+        if (!toi_a) { ma = (R)0; iA = (R)0; }
+        if (!toi_b) { mb = (R)0; iB = (R)0; }
+    }
+    for (int j = 0; j < k.mcount; ++j) {
+        xform2<R> xa = pose_xf<R>(ca, aa, k.lca), xb = pose_xf<R>(cb, ab, k.lcb);
+        vec2<R> normal, point;
+        R sep;
+        if (k.mtype == GB_M_CIRCLES) {
+            vec2<R> pA = xmul(xa, k.lp), pB = xmul(xb, k.lpts[0]);
+            normal = normalized(pB - pA);
+            point = (R)0.5 * (pA + pB);
+            sep = dot(pB - pA, normal) - k.ra - k.rb;
+        } else if (k.mtype == GB_M_FACE_A) {
+            normal = rmul(xa.q, k.ln);
+            vec2<R> plane = xmul(xa, k.lp);
+            vec2<R> clip = xmul(xb, k.lpts[j]);
+            sep = dot(clip - plane, normal) - k.ra - k.rb;
+            point = clip;
+        } else {
+            normal = rmul(xb.q, k.ln);
+            vec2<R> plane = xmul(xb, k.lp);
+            vec2<R> clip = xmul(xa, k.lpts[j]);
+            sep = dot(clip - plane, normal) - k.ra - k.rb;
+            point = clip;
+            normal = -normal;
+        }
+        vec2<R> ra = point - cvt<R>(ca), rb = point - cvt<R>(cb);
+        minsep = pymin(minsep, (double)sep);
+        R C = cclamp(baum * (sep + (R)GB_LINEAR_SLOP), (R)-GB_MAX_LINEAR_CORRECTION, (R)0);
+        R rna = sq(cross(ra, normal)), rnb = sq(cross(rb, normal));
+        R K = ma + mb + (iA * rna) + (iB * rnb);
+        R impulse = K > (R)0 ? -C / K : (R)0;
+        vec2<R> P = impulse * normal;
+        ca = ca - cvt<double>(ma * P);
+        aa = aa - (double)(iA * cross(ra, P));
+        cb = cb + cvt<double>(mb * P);
+        ab = ab + (double)(iB * cross(rb, P));
+    }
+    return minsep;
+}
+
+// ------------------------------------------------------------ islands + solve
+template <class R> __device__ __forceinline__ bool qualifies(const WView<R> &w, const ContactRec<R> &c) {
+    return (c.flags & GB_C_ENABLED) && (c.flags & GB_C_TOUCHING) && !fx_sensor(w, c.fa) && !fx_sensor(w, c.fb);
+}
+static __device__ __forceinline__ int uf_find(int *parent, int x) {
+    int p = parent[x];
+    while (p != x) { x = p; p = parent[x]; }
+    return x;
+}
+static __device__ __forceinline__ void uf_union(int *parent, int a, int b) {
+    for (int guard = 0; guard < 1 << 20; ++guard) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b) return;
+        if (a < b) { int t = a; a = b; b = t; }
+        // hook the larger root under the smaller one: the final root of a
+        // component is its smallest body index, whatever the schedule.
+        if (atomicCAS(&parent[a], a, b) == a) return;
+    }
+}
+
+// Depth-first island search of world.py:495-573 for one island, used only
+// where the reference's result depends on the visit order (island.py:163-179
+// reads the last visited body and puts the last non-static one to sleep).
+template <class R> __device__ void island_dfs(const WView<R> &w, int seed, int *last, int *last_ns) {
+    int *stack = w.B.s_stack + w.bb;
+    unsigned char *bvis = w.B.s_bvis + w.bb;
+    unsigned char *cvis = w.B.s_cvis + w.cb;
+    const int *off = w.B.s_adjoff + w.bb + w.wi;
+    const int *adj = w.B.s_adj + 2 * w.cb;
+    int sp = 0;
+    stack[sp++] = seed;
+    bvis[seed] = 1;
+    int lb = -1, lns = -1;
+    while (sp > 0) {
+        int b = stack[--sp];
+        lb = b;
+        if (w.btype(b) == GB_BODY_STATIC) continue;
+        lns = b;
+        for (int e = off[b]; e < off[b + 1]; ++e) {
+            int ci = adj[e];
+            if (cvis[ci]) continue;
+            cvis[ci] = 1;
+            const ContactRec<R> &c = w.con(ci);
+            int fa = w.fbody(c.fa), fbb = w.fbody(c.fb);
+            int other = (fa == b) ? fbb : fa;
+            if (bvis[other]) continue;
+            stack[sp++] = other;
+            bvis[other] = 1;
+        }
+    }
+    *last = lb;
+    *last_ns = lns;
+}
+
+template <class R, class G> __device__ void world_solve(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh) {
+    const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
+    int *parent = w.B.s_parent + w.bb;
+    uint32_t *rootf = w.B.s_root + w.bb;
+    int *seed = w.B.s_seed + w.bb;
+    unsigned long long *minsep = w.B.s_minsep + w.bb;
+    unsigned long long *minsleep = w.B.s_minsleep + w.bb;
+    unsigned long long *claim = w.B.s_claim + w.bb;
+    int *cons_of = w.B.s_cons_of + w.cb;
+    int *colour = w.B.s_colour + w.cb;
+    int *order = w.B.s_order + w.cb;
+    int *pref = w.B.s_pref + w.cb;
+    Cons<R> *cons = w.B.s_cons + w.cb;
+    const double dt = sp.dt;
+    const bool warm = (w.H->flags & GB_W_WARM_STARTING) != 0;
+
+    // 1. components of the constraint graph (static bodies do not link)
+    for (int b = g.rank(); b < nb; b += g.size()) {
+        parent[b] = b; rootf[b] = 0; seed[b] = GB_INF_IDX;
+        minsleep[b] = ~0ull;
+    }
+    g.sync();
+    for (int i = g.rank(); i < nc; i += g.size()) {
+        const ContactRec<R> &c = w.con(i);
+        if (!qualifies(w, c)) continue;
+        int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+        if (w.btype(ba) != GB_BODY_STATIC && w.btype(bb) != GB_BODY_STATIC) uf_union(parent, ba, bb);
+    }
+    g.sync();
+    for (int b = g.rank(); b < nb; b += g.size()) parent[b] = uf_find(parent, b);
+    g.sync();
+    bool all_allow = true;
+    for (int b = g.rank(); b < nb; b += g.size()) {
+        uint32_t f = w.B.b_flags[w.bb + b];
+        if (!(f & GB_BODY_ALLOW_SLEEP)) all_allow = false;
+        if (w.btype(b) != GB_BODY_STATIC && (f & GB_BODY_AWAKE) && (f & GB_BODY_ACTIVE)) {
+            atomicOr(&rootf[parent[b]], R_SIM);
+            atomicMin(&seed[parent[b]], b);
+        }
+    }
+    all_allow = !g.any(!all_allow);
+    g.sync();
+    // 2. island membership: wake the members of simulated islands (DFS sets
+    //    body.awake = True, world.py:520), constraints = qualifying contacts
+    //    of simulated islands in contact-list order.
+    for (int b = g.rank(); b < nb; b += g.size())
+        if (w.btype(b) != GB_BODY_STATIC && (rootf[parent[b]] & R_SIM)) wake_body(w, b);
+    int ncons = group_scan(g, nc, [&](int i) {
+        const ContactRec<R> &c = w.con(i);
+        if (!qualifies(w, c)) return 0;
+        int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+        int dyn = (w.btype(ba) != GB_BODY_STATIC) ? ba : bb;
+        return (rootf[parent[dyn]] & R_SIM) ? 1 : 0;
+    }, pref);
+    g.sync();
+    for (int i = g.rank(); i < nc; i += g.size()) {
+        const ContactRec<R> &c = w.con(i);
+        cons_of[i] = -1;
+        if (!qualifies(w, c)) continue;
+        int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+        int dyn = (w.btype(ba) != GB_BODY_STATIC) ? ba : bb;
+        int stat = (dyn == ba) ? bb : ba;
+        if (!(rootf[parent[dyn]] & R_SIM)) continue;
+        int k = pref[i];
+        cons_of[i] = k;
+        cons[k].cidx = i;
+        cons[k].root = parent[dyn];
+        colour[k] = -1;
+        if (w.btype(stat) == GB_BODY_STATIC) wake_body(w, stat);
+    }
+    g.sync();
+    // 3. graph colouring: Jones-Plassmann rounds with fixed hash priorities;
+    //    a constraint is coloured when it holds the highest key on each of its
+    //    non-static bodies.  Colour classes share no non-static body, so each
+    //    class is solved in parallel exactly as a sequential pass would.
+    int ncol = 0;
+    for (int round = 0; round <= ncons; ++round) {   // >= 1 constraint is coloured per round
+        for (int b = g.rank(); b < nb; b += g.size()) claim[b] = 0ull;
+        g.sync();
+        bool left = false;
+        for (int k = g.rank(); k < ncons; k += g.size()) {
+            if (colour[k] >= 0) continue;
+            left = true;
+            const ContactRec<R> &c = w.con(cons[k].cidx);
+            int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+            unsigned h = (unsigned)k * 2654435761u;
+            h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
+            unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
+            if (w.btype(ba) != GB_BODY_STATIC) atomicMax(&claim[ba], key);
+            if (w.btype(bb) != GB_BODY_STATIC) atomicMax(&claim[bb], key);
+        }
+        if (!g.any(left)) break;
+        for (int k = g.rank(); k < ncons; k += g.size()) {
+            if (colour[k] >= 0) continue;
+            const ContactRec<R> &c = w.con(cons[k].cidx);
+            int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+            unsigned h = (unsigned)k * 2654435761u;
+            h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
+            unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
+            bool win = (w.btype(ba) == GB_BODY_STATIC || claim[ba] == key) && (w.btype(bb) == GB_BODY_STATIC || claim[bb] == key);
+            if (win) colour[k] = round;
+        }
+        ncol = round + 1;
+        g.sync();
+    }
+    g.sync();
+    // order = constraints sorted by (colour, index); colour offsets live in
+    // the collide scratch (free during the solve); ncol < ccap always holds
+    // because every colour holds at least one constraint and ncons <= nc.
+    int *coff = w.B.s_proc + w.cb;
+    if (ncol + 1 > w.H->ccap) {   // cannot happen while ncons < ccap; never index past the world's slots
+        if (g.rank() == 0) w.H->status |= GB_ST_ITER_LIMIT;
+        ncol = w.H->ccap - 1;
+    }
+    {
+        // counting sort, one scan per colour (colours are few)
+        int start = 0;
+        for (int cc = 0; cc < ncol; ++cc) {
+            int n = group_scan(g, ncons, [&](int k) { return colour[k] == cc ? 1 : 0; }, pref);
+            g.sync();
+            for (int k = g.rank(); k < ncons; k += g.size())
+                if (colour[k] == cc) order[start + pref[k]] = k;
+            if (g.rank() == 0) coff[cc] = start;
+            start += n;
+            g.sync();
+        }
+        if (g.rank() == 0) coff[ncol] = start;
+    }
+    if (g.rank() == 0) { sh->ncons = ncons; sh->ncolours = ncol; w.H->last_ncons = ncons; w.H->last_ncolours = ncol; }
+    g.sync();
+    if (sp.record_order) {
+        int *out = w.B.order_out + w.cb;
+        for (int k = g.rank(); k < ncons; k += g.size()) out[k] = cons[order[k]].cidx;
+    }
+    // 4. integrate velocities (island.py:71-95)
+    const vec2<R> grav = mk<R>((R)w.H->gx, (R)w.H->gy);
+    for (int b = g.rank(); b < nb; b += g.size()) {
+        if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
+        int gb = w.bb + b;
+        w.B.b_c0[gb] = w.B.b_c[gb];
+        w.B.b_a0[gb] = w.B.b_a[gb];
+        if (w.btype(b) == GB_BODY_DYNAMIC) {
+            vec2<R> v = w.B.b_v[gb];
+            R om = w.B.b_w[gb];
+            const R dtr = (R)dt;
+            v = v + dtr * (w.B.b_gscale[gb] * grav + w.B.b_inv_mass[gb] * w.B.b_f[gb]);
+            om = om + dtr * w.B.b_inv_I[gb] * w.B.b_torque[gb];
+            v = cclamp((R)1 - dtr * w.B.b_ldamp[gb], (R)0, (R)1) * v;
+            om = om * cclamp((R)1 - dtr * w.B.b_adamp[gb], (R)0, (R)1);
+            w.B.b_v[gb] = v; w.B.b_w[gb] = om;
+        }
+    }
+    g.sync();
+    // 5. constraint set-up (positions before integration, velocities after)
+    for (int k = g.rank(); k < ncons; k += g.size()) {
+        Cons<R> &q = cons[k];
+        int root = q.root;
+        build_cons(w, q, q.cidx, warm, sp.dt_ratio);
+        q.root = root;
+        int ga = w.bb + q.ia, gbb = w.bb + q.ib;
+        init_velocity(q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], w.B.b_v[ga], w.B.b_w[ga], w.B.b_v[gbb], w.B.b_w[gbb]);
+    }
+    g.sync();
+    // 6. warm start and velocity iterations, colour by colour
+    for (int it = (warm ? -1 : 0); it < sp.vel_iters; ++it) {
+        for (int cc = 0; cc < ncol; ++cc) {
+            int s0 = coff[cc], s1 = coff[cc + 1];
+            for (int j = s0 + g.rank(); j < s1; j += g.size()) {
+                Cons<R> &q = cons[order[j]];
+                int ga = w.bb + q.ia, gbb = w.bb + q.ib;
+                vec2<R> va = w.B.b_v[ga], vb = w.B.b_v[gbb];
+                R wa = w.B.b_w[ga], wb = w.B.b_w[gbb];
+                if (it < 0) warm_start(q, va, wa, vb, wb);
+                else solve_velocity(q, va, wa, vb, wb);
+                // colour classes share no non-static body; static bodies keep v = 0
+                if (w.btype(q.ia) != GB_BODY_STATIC) { w.B.b_v[ga] = va; w.B.b_w[ga] = wa; }
+                if (w.btype(q.ib) != GB_BODY_STATIC) { w.B.b_v[gbb] = vb; w.B.b_w[gbb] = wb; }
+            }
+            g.sync();
+        }
+    }
+    // 7. store impulses (contact.py:801-806)
+    for (int k = g.rank(); k < ncons; k += g.size()) {
+        const Cons<R> &q = cons[k];
+        ContactRec<R> &c = w.con(q.cidx);
+        for (int j = 0; j < q.npts && j < c.m.count; ++j) { c.m.ni[j] = q.ni[j]; c.m.ti[j] = q.ti[j]; }
+    }
+    // 8. integrate positions (island.py:120-138)
+    for (int b = g.rank(); b < nb; b += g.size()) {
+        if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
+        int gb = w.bb + b;
+        vec2<R> v = w.B.b_v[gb];
+        R om = w.B.b_w[gb];
+        const R dtr = (R)dt;
+        vec2<R> tr = dtr * v;
+        if (dot(tr, tr) > (R)GB_MAX_TRANSLATION_SQR) {
+            R ratio = (R)GB_MAX_TRANSLATION / len(tr);
+            v = ratio * v;
+        }
+        R rotation = dtr * om;
+        if (sq(rotation) > (R)GB_MAX_ROTATION_SQR) {
+            R ratio = (R)GB_MAX_ROTATION / fabs(rotation);
+            om = om * ratio;
+        }
+        w.B.b_c[gb] = w.B.b_c[gb] + cvt<double>(dtr * v);
+        w.B.b_a[gb] = w.B.b_a[gb] + (double)(dtr * om);
+        w.B.b_v[gb] = v; w.B.b_w[gb] = om;
+    }
+    g.sync();
+    // 9. position iterations with the per-island early exit (island.py:141-153)
+    for (int it = 0; it < sp.pos_iters; ++it) {
+        for (int b = g.rank(); b < nb; b += g.size()) minsep[b] = dkey(0.0);
+        g.sync();
+        for (int cc = 0; cc < ncol; ++cc) {
+            int s0 = coff[cc], s1 = coff[cc + 1];
+            for (int j = s0 + g.rank(); j < s1; j += g.size()) {
+                const Cons<R> &q = cons[order[j]];
+                if (rootf[q.root] & R_DONE) continue;
+                int ga = w.bb + q.ia, gbb = w.bb + q.ib;
+                vec2<double> ca = w.B.b_c[ga], cb = w.B.b_c[gbb];
+                double aa = w.B.b_a[ga], ab = w.B.b_a[gbb];
+                double ms = solve_position(q, ca, aa, cb, ab, 0.0, false, false, false);
+                atomicMin(&minsep[q.root], dkey(ms));
+                if (w.btype(q.ia) != GB_BODY_STATIC) { w.B.b_c[ga] = ca; w.B.b_a[ga] = aa; }
+                if (w.btype(q.ib) != GB_BODY_STATIC) { w.B.b_c[gbb] = cb; w.B.b_a[gbb] = ab; }
+            }
+            g.sync();
+        }
+        bool pending = false;
+        for (int b = g.rank(); b < nb; b += g.size()) {
+            if (parent[b] != b || !(rootf[b] & R_SIM) || (rootf[b] & R_DONE)) continue;
+            if (w.btype(b) == GB_BODY_STATIC) continue;
+            if (dkey_inv(minsep[b]) >= -3.0 * GB_LINEAR_SLOP) rootf[b] |= R_DONE | R_SOLVED;
+            else pending = true;
+        }
+        if (!g.any(pending)) break;
+    }
+    g.sync();
+    // 10. write back the transforms of the island bodies (island.py:156-159)
+    for (int b = g.rank(); b < nb; b += g.size()) {
+        if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
+        sync_transform(w, b);
+    }
+    g.sync();
+    // 11. sleep (island.py:163-179)
+    if (w.H->flags & GB_W_ALLOW_SLEEP) {
+        bool need_dfs_all = !all_allow;
+        if (need_dfs_all) {
+            // the sleep test of every island reads the last visited body
+            if (g.rank() == 0) sh->any_dfs = 1;
+        }
+        for (int b = g.rank(); b < nb; b += g.size()) {
+            if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
+            int gb = w.bb + b;
+            R om = w.B.b_w[gb];
+            vec2<R> v = w.B.b_v[gb];
+            bool moving = sq(om) > (R)GB_ANGULAR_SLEEP_TOL_SQR || len2(v) > (R)GB_LINEAR_SLEEP_TOL_SQR;
+            if (!need_dfs_all) {
+                if (moving) { w.B.b_sleep[gb] = 0.0; atomicMin(&minsleep[parent[b]], 0ull); }
+                else {
+                    double st = w.B.b_sleep[gb] + dt;
+                    w.B.b_sleep[gb] = st;
+                    atomicMin(&minsleep[parent[b]], (unsigned long long)__double_as_longlong(st));
+                }
+            }
+        }
+        g.sync();
+        // islands that may fall asleep need the depth-first order
+        bool want = false;
+        for (int b = g.rank(); b < nb; b += g.size()) {
+            if (parent[b] != b || w.btype(b) == GB_BODY_STATIC || !(rootf[b] & R_SIM)) continue;
+            bool cand = need_dfs_all || (__longlong_as_double((long long)minsleep[b]) >= GB_TIME_TO_SLEEP && (rootf[b] & R_SOLVED));
+            if (cand) { rootf[b] |= R_DFS; want = true; }
+        }
+        want = g.any(want);
+        if (want) {
+            // adjacency of every body in contact-list order (Body._contacts)
+            int *off = w.B.s_adjoff + w.bb + w.wi;
+            int *adj = w.B.s_adj + 2 * w.cb;
+            int *deg = w.B.s_stack + w.bb;
+            for (int b = g.rank(); b < nb; b += g.size()) deg[b] = 0;
+            g.sync();
+            for (int i = g.rank(); i < nc; i += g.size()) {
+                const ContactRec<R> &c = w.con(i);
+                if (!qualifies(w, c)) continue;
+                atomicAdd(&deg[w.fbody(c.fa)], 1);
+                atomicAdd(&deg[w.fbody(c.fb)], 1);
+            }
+            g.sync();
+            int tot = group_scan(g, nb, [&](int b) { return deg[b]; }, off);
+            if (g.rank() == 0) off[nb] = tot;
+            g.sync();
+            for (int b = g.rank(); b < nb; b += g.size()) deg[b] = off[b];
+            g.sync();
+            for (int i = g.rank(); i < nc; i += g.size()) {
+                const ContactRec<R> &c = w.con(i);
+                if (!qualifies(w, c)) continue;
+                adj[atomicAdd(&deg[w.fbody(c.fa)], 1)] = i;
+                adj[atomicAdd(&deg[w.fbody(c.fb)], 1)] = i;
+            }
+            g.sync();
+            for (int b = g.rank(); b < nb; b += g.size()) {
+                for (int e = off[b] + 1; e < off[b + 1]; ++e) {   // insertion sort by contact index
+                    int v = adj[e], j = e - 1;
+                    while (j >= off[b] && adj[j] > v) { adj[j + 1] = adj[j]; --j; }
+                    adj[j + 1] = v;
+                }
+                w.B.s_bvis[w.bb + b] = 0;
+            }
+            for (int i = g.rank(); i < nc; i += g.size()) w.B.s_cvis[w.cb + i] = 0;
+            g.sync();
+            if (g.rank() == 0) {
+                unsigned char *bvis = w.B.s_bvis + w.bb;
+                for (int r = 0; r < nb; ++r) {
+                    if (parent[r] != r || !(rootf[r] & R_DFS)) continue;
+                    int last, last_ns;
+                    island_dfs(w, seed[r], &last, &last_ns);
+                    // static bodies may belong to several islands: clear all marks
+                    for (int b = 0; b < nb; ++b) if (w.btype(b) == GB_BODY_STATIC) bvis[b] = 0;
+                    if (need_dfs_all) {
+                        bool allow_last = (w.B.b_flags[w.bb + last] & GB_BODY_ALLOW_SLEEP) != 0;
+                        unsigned long long ms = ~0ull;
+                        for (int b = 0; b < nb; ++b) {
+                            if (parent[b] != r || w.btype(b) == GB_BODY_STATIC) continue;
+                            int gb = w.bb + b;
+                            bool moving = sq(w.B.b_w[gb]) > (R)GB_ANGULAR_SLEEP_TOL_SQR || len2(w.B.b_v[gb]) > (R)GB_LINEAR_SLEEP_TOL_SQR;
+                            if (!allow_last || moving) { w.B.b_sleep[gb] = 0.0; ms = 0ull; }
+                            else {
+                                double st = w.B.b_sleep[gb] + dt;
+                                w.B.b_sleep[gb] = st;
+                                unsigned long long k = (unsigned long long)__double_as_longlong(st);
+                                if (k < ms) ms = k;
+                            }
+                        }
+                        minsleep[r] = ms;
+                    }
+                    if (__longlong_as_double((long long)minsleep[r]) >= GB_TIME_TO_SLEEP && (rootf[r] & R_SOLVED) && last_ns >= 0)
+                        sleep_body(w, last_ns);
+                }
+            }
+            g.sync();
+        }
+    }
+    // 12. synchronise fixtures of island bodies; the move buffer is the
+    //     re-fattened proxies in body order = fixture order (world.py:584-589)
+    int *mv = w.B.s_move + w.fb;
+    int *mflag = w.B.s_first + w.fb;
+    for (int f = g.rank(); f < nf; f += g.size()) {
+        int b = w.fbody(f);
+        bool moved = false;
+        if (w.btype(b) != GB_BODY_STATIC && (rootf[parent[b]] & R_SIM)) moved = sync_fixture(w, f);
+        mflag[f] = moved ? 1 : 0;
+    }
+    g.sync();
+    int nmove = group_scan(g, nf, [&](int f) { return mflag[f]; }, w.B.s_cnt + w.fb);
+    g.sync();
+    for (int f = g.rank(); f < nf; f += g.size())
+        if (mflag[f]) mv[w.B.s_cnt[w.fb + f]] = f;
+    if (g.rank() == 0) sh->nmove = nmove;
+    g.sync();
+    find_new_contacts(g, w, sh);
+}

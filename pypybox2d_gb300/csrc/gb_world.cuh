@@ -1,0 +1,203 @@
+// gb_world.cuh -- device layout of a batch of worlds and the "group"
+// abstraction the step is written against.
+//
+// A world is advanced by one group of threads: a whole CTA (launch mode 1)
+// or one warp (launch mode 2).  Every phase of World.step is a loop over the
+// world's bodies / fixtures / contacts / constraints strided by the group
+// size, separated by group barriers; the few phases whose result depends on
+// the reference's sequential order (the time-of-impact event loop, the
+// island depth-first search that picks which body may sleep) run on the
+// group's rank 0.  All group algorithms (scans, union-find, colouring) give
+// results independent of the group size, so the CTA and warp mappings are
+// bit-identical.
+#pragma once
+#include "gb_collide.cuh"
+
+// ---------------------------------------------------------------- layout
+// Batch-global structure of arrays.  Body / fixture arrays are indexed by
+// the batch-global index (world base + world-local index); contact slots by
+// world contact base + list position (contacts are kept dense, in creation
+// order = ContactManager.contacts order).
+template <class R> struct ContactRec {
+    int fa, fb;          // world-local fixtures, fa is the primary shape
+    uint32_t flags;      // GB_C_*
+    int toi_count;
+    double toi;
+    R friction, restitution;
+    Manifold<R> m;
+};
+
+template <class R> struct Cons {
+    int cidx;            // contact list position
+    int ia, ib;          // world-local bodies
+    int root;            // island (union-find root, world-local body)
+    R ma, mb, iA, iB;
+    vec2<R> lca, lcb;
+    R ra, rb, friction, restitution;
+    int npts, mcount, mtype;
+    vec2<R> normal;
+    vec2<R> rA[2], rB[2];
+    R ni[2], ti[2], nm[2], tm[2], bias[2];
+    R k11, k12, k22, nm11, nm12, nm21, nm22;
+    vec2<R> ln, lp, lpts[2];
+};
+
+struct WorldHdr {              // per-world scalars (device)
+    int nb, nf, nc, ccap;      // counts, contact capacity
+    int bbase, fbase, cbase;   // batch bases
+    int pcap;                  // move-buffer capacity (fixtures)
+    uint32_t flags;            // GB_W_*
+    uint32_t status;           // GB_ST_*
+    double gx, gy, inv_dt0;
+    int last_ncons, last_ncolours;
+    int nmove0;                // pending move buffer given at creation (in s_move)
+    int _pad;
+};
+
+template <class R> struct Batch {
+    int n_worlds;
+    WorldHdr *hdr;
+    // bodies
+    int *b_type; uint32_t *b_flags; int *b_fstart; int *b_fcount;
+    vec2<double> *b_xp; rot2<double> *b_xq;
+    vec2<double> *b_lc, *b_c, *b_c0; double *b_a, *b_a0, *b_alpha0;
+    vec2<R> *b_v; R *b_w; vec2<R> *b_f; R *b_torque;
+    R *b_inv_mass, *b_inv_I, *b_ldamp, *b_adamp, *b_gscale;
+    double *b_mass, *b_I, *b_sleep;
+    // fixtures
+    int *f_body, *f_type, *f_count; uint32_t *f_flags;
+    R *f_radius, *f_friction, *f_restitution; double *f_density;
+    uint32_t *f_cat, *f_mask; int *f_group;
+    vec2<R> *f_v, *f_n;       // 8 slots per fixture
+    dbox *f_aabb;          // fat AABB
+    // contacts
+    ContactRec<R> *c;
+    // scratch (body-indexed)
+    int *s_parent, *s_wake, *s_seed, *s_stack, *s_adjoff;
+    uint32_t *s_root;         // per-root bits
+    unsigned long long *s_claim, *s_minsep, *s_minsleep;
+    unsigned char *s_bvis;
+    // scratch (fixture-indexed)
+    int *s_move, *s_first, *s_cnt;
+    // scratch (contact-slot-indexed)
+    int *s_proc, *s_pref, *s_adj, *s_colour, *s_order, *s_cons_of;
+    unsigned char *s_cvis;
+    Cons<R> *s_cons;
+    unsigned long long *s_hash;  // 4 * ccap slots per world (a power of two >= 2*ccap fits)
+    int *order_out;              // recorded solver order (contact positions), ccap per world
+};
+
+struct StepParams {
+    double dt, inv_dt, dt_ratio;
+    int vel_iters, pos_iters;
+    int record_order;
+};
+
+// ---------------------------------------------------------------- groups
+struct GroupCta {
+    int *sm;   // >= 64 ints of shared memory owned by the group
+    __device__ __forceinline__ int rank() const { return threadIdx.x; }
+    __device__ __forceinline__ int size() const { return blockDim.x; }
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+    __device__ __forceinline__ bool any(bool p) const { return __syncthreads_or(p) != 0; }
+    // exclusive scan of v over the group; *total = sum.  Contains barriers.
+    __device__ int exscan(int v, int *total) const {
+        int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) sm[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int s = (lane < nw) ? sm[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            if (lane < nw) sm[32 + lane] = s;
+        }
+        __syncthreads();
+        int base = warp ? sm[32 + warp - 1] : 0;
+        *total = sm[32 + nw - 1];
+        __syncthreads();
+        return base + x - v;
+    }
+};
+
+struct GroupWarp {
+    int *sm;
+    __device__ __forceinline__ int rank() const { return threadIdx.x & 31; }
+    __device__ __forceinline__ int size() const { return 32; }
+    __device__ __forceinline__ void sync() const { __syncwarp(); }
+    __device__ __forceinline__ bool any(bool p) const { __syncwarp(); return __any_sync(0xffffffffu, p) != 0; }
+    __device__ int exscan(int v, int *total) const {
+        int lane = threadIdx.x & 31;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        *total = __shfl_sync(0xffffffffu, x, 31);
+        __syncwarp();
+        return x - v;
+    }
+};
+
+// Chunked exclusive scan of flag(i) for i < n into out[i]; returns the total.
+template <class G, class F> __device__ int group_scan(const G &g, int n, F flag, int *out) {
+    int carry = 0;
+    for (int base = 0; base < n; base += g.size()) {
+        int i = base + g.rank();
+        int v = (i < n) ? flag(i) : 0;
+        int tot;
+        int ex = g.exscan(v, &tot);
+        if (i < n) out[i] = carry + ex;
+        carry += tot;
+    }
+    return carry;
+}
+
+// Per-world view: world-local indexing helpers over the batch arrays.
+template <class R> struct WView {
+    Batch<R> B;
+    WorldHdr *H;   // group-shared copy
+    int bb, fb, cb, wi;
+    __device__ __forceinline__ Shape<R> shape(int f) const {
+        int gf = fb + f;
+        Shape<R> s;
+        s.type = B.f_type[gf]; s.count = B.f_count[gf]; s.flags = B.f_flags[gf]; s.radius = B.f_radius[gf];
+        s.v = B.f_v + (size_t)gf * GB_MAX_POLY_VERTS;
+        s.n = B.f_n + (size_t)gf * GB_MAX_POLY_VERTS;
+        return s;
+    }
+    __device__ __forceinline__ int fbody(int f) const { return B.f_body[fb + f]; }
+    __device__ __forceinline__ xform2<R> xf(int b) const {
+        xform2<R> x;
+        vec2<double> p = B.b_xp[bb + b];
+        rot2<double> q = B.b_xq[bb + b];
+        x.p = mk<R>((R)p.x, (R)p.y);
+        x.q.c = (R)q.c; x.q.s = (R)q.s;
+        return x;
+    }
+    __device__ __forceinline__ xform2<double> xfd(int b) const {
+        xform2<double> x;
+        x.p = B.b_xp[bb + b];
+        x.q = B.b_xq[bb + b];
+        return x;
+    }
+    __device__ __forceinline__ bool awake(int b) const { return (B.b_flags[bb + b] & GB_BODY_AWAKE) != 0; }
+    __device__ __forceinline__ int btype(int b) const { return B.b_type[bb + b]; }
+    __device__ __forceinline__ ContactRec<R> &con(int i) const { return B.c[cb + i]; }
+    __device__ __forceinline__ Sweep sweep(int b) const {
+        Sweep s;
+        s.lc = B.b_lc[bb + b]; s.c0 = B.b_c0[bb + b]; s.c = B.b_c[bb + b];
+        s.a0 = B.b_a0[bb + b]; s.a = B.b_a[bb + b]; s.alpha0 = B.b_alpha0[bb + b];
+        return s;
+    }
+    __device__ __forceinline__ void put_sweep(int b, const Sweep &s) const {
+        B.b_lc[bb + b] = s.lc; B.b_c0[bb + b] = s.c0; B.b_c[bb + b] = s.c;
+        B.b_a0[bb + b] = s.a0; B.b_a[bb + b] = s.a; B.b_alpha0[bb + b] = s.alpha0;
+    }
+};

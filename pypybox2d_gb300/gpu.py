@@ -1,0 +1,83 @@
+"""Thin host wrapper of the C ABI: a device-resident batch of worlds.
+
+``GpuBatch`` is the plumbing under ``World`` / ``WorldBatch``: it uploads
+record arrays (``abi.BODY``, ``abi.FIXTURE``, ``abi.CONTACT``, ``abi.WORLD``)
+through ``gb_batch_create`` and advances them with ``gb_batch_step``.  Every
+call goes to libgb2d.so; a missing library or a CUDA error raises.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import abi
+
+
+class GpuBatch:
+    """A batch of independent worlds resident in device memory."""
+
+    def __init__(self, worlds, bodies, fixtures, contacts=None, precision: str = "f64"):
+        self.lib = abi.load_library()
+        self.prec = abi.PREC_F64 if precision in ("f64", "float64", abi.PREC_F64) else abi.PREC_F32
+        scene, keep = abi.make_scene(worlds, bodies, fixtures, contacts)
+        self.worlds, self.n_bodies, self.n_fixtures = keep[0], len(keep[1]), len(keep[2])
+        h = ctypes.c_void_p()
+        abi.check(self.lib.gb_batch_create(ctypes.byref(scene), self.prec, ctypes.byref(h)))
+        self.h = h
+        self.n_worlds = len(self.worlds)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.gb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, dt: float, vel_iters: int = 8, pos_iters: int = 3, n_steps: int = 1, launch_mode: int = 1,
+             block_threads: int = 0, record_order: bool = False, stream: int | None = None) -> None:
+        o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, 1 if record_order else 0)
+        abi.check(self.lib.gb_batch_step(self.h, ctypes.byref(o), ctypes.c_void_p(stream or 0)))
+
+    def bodies(self, stream: int | None = None) -> np.ndarray:
+        out = np.zeros(self.n_bodies, dtype=abi.BODY)
+        abi.check(self.lib.gb_batch_get_bodies(self.h, out.ctypes.data, self.n_bodies, ctypes.c_void_p(stream or 0)))
+        return out
+
+    def set_bodies(self, bodies: np.ndarray, stream: int | None = None) -> None:
+        b = np.ascontiguousarray(bodies, dtype=abi.BODY)
+        abi.check(self.lib.gb_batch_set_bodies(self.h, b.ctypes.data, len(b), ctypes.c_void_p(stream or 0)))
+
+    def proxies(self) -> np.ndarray:
+        out = np.zeros((self.n_fixtures, 4), dtype=np.float64)
+        abi.check(self.lib.gb_batch_get_proxies(self.h, out.ctypes.data, self.n_fixtures, None))
+        return out
+
+    def contact_counts(self) -> np.ndarray:
+        out = np.zeros(self.n_worlds, dtype=np.int32)
+        abi.check(self.lib.gb_batch_get_contact_counts(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), None))
+        return out
+
+    def contacts(self, world: int = 0) -> np.ndarray:
+        cap = int(self.contact_counts()[world])
+        out = np.zeros(max(cap, 1), dtype=abi.CONTACT)
+        n = ctypes.c_int32()
+        abi.check(self.lib.gb_batch_get_contacts(self.h, world, out.ctypes.data, len(out), ctypes.byref(n), None))
+        return out[:n.value].copy()
+
+    def solver_order(self, world: int = 0) -> np.ndarray:
+        cap = max(16, int(self.contact_counts()[world]) + 16)
+        out = np.zeros(cap, dtype=np.int32)
+        n = ctypes.c_int32()
+        abi.check(self.lib.gb_batch_get_solver_order(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                     cap, ctypes.byref(n), None))
+        return out[:n.value].copy()
+
+    def status(self) -> np.ndarray:
+        out = np.zeros(self.n_worlds, dtype=np.uint32)
+        abi.check(self.lib.gb_batch_status(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), None))
+        return out

@@ -212,7 +212,7 @@ def export_world(world, b2, contacts=True):
         wf |= abi.W_NEW_FIXTURE
     if world._step_complete:
         wf |= abi.W_STEP_COMPLETE
-    W[0] = (0, nb, 0, nf, 0, len(C), max(64, 8 * nf), wf, world._gravity.x, world._gravity.y, world._inv_dt0)
+    W[0] = (0, nb, 0, nf, 0, len(C), max(64, 8 * nf), wf, 0, 0, world._gravity.x, world._gravity.y, world._inv_dt0)
     return W, B, F, C
 
 

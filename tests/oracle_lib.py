@@ -34,7 +34,7 @@ def load(libm: bool = False) -> ctypes.CDLL:
     lib = ctypes.CDLL(path)
     vp, i32, dbl = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
     lib.or_create.restype = vp
-    lib.or_create.argtypes = [vp, vp, vp, vp]
+    lib.or_create.argtypes = [vp, vp, vp, vp, vp]
     lib.or_destroy.argtypes = [vp]
     lib.or_step.argtypes = [vp, dbl, i32, i32]
     for n in ("or_body_count", "or_contact_count", "or_status"):
@@ -65,18 +65,19 @@ def load(libm: bool = False) -> ctypes.CDLL:
 class OracleWorld:
     """One world of the restatement, built from gb2d record arrays."""
 
-    def __init__(self, world, bodies, fixtures, contacts=None, libm=False, index=0):
+    def __init__(self, world, bodies, fixtures, contacts=None, libm=False, index=0, moves=None):
         self.lib = load(libm)
         self._keep = [np.ascontiguousarray(world, dtype=abi.WORLD),
                       np.ascontiguousarray(bodies, dtype=abi.BODY),
                       np.ascontiguousarray(fixtures, dtype=abi.FIXTURE),
                       np.ascontiguousarray(contacts if contacts is not None else np.zeros(0, abi.CONTACT),
                                            dtype=abi.CONTACT)]
-        w, b, f, c = self._keep
+        self._keep.append(np.ascontiguousarray(moves if moves is not None else np.zeros(0, np.int32), dtype=np.int32))
+        w, b, f, c, mv = self._keep
         wd = w[index:index + 1]
         self._wd = np.ascontiguousarray(wd)
         self.h = self.lib.or_create(self._wd.ctypes.data, b.ctypes.data, f.ctypes.data,
-                                    c.ctypes.data if len(c) else None)
+                                    c.ctypes.data if len(c) else None, mv.ctypes.data if len(mv) else None)
         self.nb = int(wd["body_count"][0])
         self.nf = int(wd["fixture_count"][0])
 
