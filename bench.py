@@ -1,0 +1,384 @@
+"""Benchmark of the World.step hot path on GB300.
+
+Workload (the batched configuration): 4096 copies of the pyramid world
+(20 rows of 0.5 m boxes on a 40 x 0.5 m ground box, 210 dynamic bodies per
+world), every box position jittered by a seeded U(-0.01, 0.01) m, dt = 1/60,
+8 velocity and 3 position iterations, float32 bulk arithmetic with float64
+positions, advanced by one persistent launch (one CTA per world) per timed
+region.  A "step" is one World.step of every world of the batch.
+
+Reported (one JSON line on rank 0):
+  value    dynamic body-steps/s with the batch resident in HBM (device time,
+           CUDA events on the launching stream, max over ranks)
+  e2e      the same metric through the C ABI with host buffers: every step
+           uploads the body records from pinned host memory
+           (gb_batch_set_bodies), steps, and reads them back (gb_batch_get_bodies)
+  roofline HBM roofline of the step kernel from the algorithmic bytes per
+           world-step (152 B per body + 96 B per box fixture + 128 B per
+           contact, from live counts) over the kernel's event-timed duration
+  cpu_baseline  the CPU restatement (oracle/, C, float64) on the host cores
+           stepping a bounded sample of the same worlds
+  plain    the float64 path launched per world, one step per launch
+  error    float32 position error after one step against the float64
+           restatement from identical state, solved in the same order
+
+--impl reference runs the CPU restatement of the reference (oracle/) with
+all host threads on a bounded sample of the same workload instead.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(HERE, "tests"))
+
+METRIC = "body-steps/s on 1 GB300: batched FP32 vs plain FP64 GPU path at stated step error"
+BODIES_PER_WORLD = 210
+DT = 1.0 / 60.0
+VI, PI = 8, 3
+
+
+def _peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes_per_world_step(n_bodies, fixtures, n_contacts):
+    """152 B per body (read c, a, v, w, mass constants, flags, sleep timer;
+    write c, a, c0, a0, v, w, sleep timer, flags) + per fixture its shape
+    (polygon: 16 B per vertex for vertex + normal in float32, circle 12 B)
+    and its fat AABB read and write (32 B) + 128 B per contact (pair
+    indices, manifold read and write, flags)."""
+    shape = np.where(fixtures["shape_type"] == 0, 12, fixtures["vertex_count"] * 16)
+    return 152.0 * n_bodies + float(np.sum(shape + 32)) + 128.0 * n_contacts
+
+
+def cpu_oracle_rate(W, B, F, M, steps, threads, target_s=8.0, max_worlds=None):
+    """Body-steps/s of the CPU restatement stepping a sample of the worlds."""
+    import oracle_lib
+    from pypybox2d_gb300 import abi
+    lib = oracle_lib.load(False)
+    nw = len(W)
+    # calibrate on one world-step per thread
+    probe = min(nw, threads)
+    s, keep = abi.make_scene(W[:probe], B, F, None, M)
+    h = lib.or_batch_create(ctypes.byref(s))
+    t = lib.or_batch_step(h, DT, VI, PI, 2, threads)
+    lib.or_batch_destroy(h)
+    per_world_step = max(t / 2.0, 1e-6)          # wall seconds for `probe` worlds on `threads` threads
+    want = int(target_s / (per_world_step * steps) * probe)
+    n = int(max(threads, min(nw, want, max_worlds or nw)))
+    s, keep = abi.make_scene(W[:n], B, F, None, M)
+    h = lib.or_batch_create(ctypes.byref(s))
+    t = lib.or_batch_step(h, DT, VI, PI, steps, threads)
+    lib.or_batch_destroy(h)
+    return n * BODIES_PER_WORLD * steps / t, n, t
+
+
+def run_reference(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from pypybox2d_gb300 import scenes
+    threads = os.cpu_count() or 1
+    n = max(threads, 2 * threads)
+    W, B, F, M = scenes.pyramid_batch(min(n, args.worlds), rows=20, jitter=0.01, seed=0)
+    import oracle_lib
+    from pypybox2d_gb300 import abi
+    lib = oracle_lib.load(False)
+    s, keep = abi.make_scene(W, B, F, None, M)
+    h = lib.or_batch_create(ctypes.byref(s))
+    for _ in range(args.warmup):
+        lib.or_batch_step(h, DT, VI, PI, 1, threads)
+    t = 0.0
+    for _ in range(args.steps):
+        t += lib.or_batch_step(h, DT, VI, PI, 1, threads)
+    lib.or_batch_destroy(h)
+    nwd = len(W)
+    value = nwd * BODIES_PER_WORLD * args.steps / t
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"pyramid x{nwd} (sample of the {args.worlds}-world batch), 210 boxes/world, "
+                               f"jitter U(-0.01,0.01) m, dt=1/60, 8 vel / 3 pos iters",
+                   "worlds": nwd},
+        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{nwd} worlds x {args.steps} steps, one world per thread task, {threads} threads"},
+        "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of pypybox2d World.step (oracle/, float64 C, pinned bit-exact to the reference's "
+                "golden vectors); the reference itself is CPython and does not run on the GPU box",
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--worlds", type=int, default=4096)
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--mode", type=int, default=1, help="1 = CTA per world, 2 = warp per world")
+    ap.add_argument("--threads", type=int, default=128)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--no-extras", action="store_true", help="skip cpu baseline, plain path and error legs")
+    args = ap.parse_args()
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    ws, rank, local = _dist()
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    from pypybox2d_gb300 import abi, scenes
+    from pypybox2d_gb300.gpu import GpuBatch
+
+    W, B, F, M = scenes.pyramid_batch(args.worlds, rows=20, jitter=0.01, seed=rank * args.worlds)
+    batch = GpuBatch(W, B, F, precision=args.precision, moves=M)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # warm-up (also finds the initial contacts)
+    batch.step(DT, VI, PI, args.warmup, launch_mode=args.mode, block_threads=args.threads, stream=sh)
+    torch.cuda.synchronize()
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        batch.step(DT, VI, PI, args.steps, launch_mode=args.mode, block_threads=args.threads, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    t = e0.elapsed_time(e1) / 1e3
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    status = batch.status()
+    counts = batch.contact_counts()
+    print(f"[bench] {args.steps} steps of {args.worlds} worlds: {t:.3f} s", file=sys.stderr, flush=True)
+    total_bodies = args.worlds * BODIES_PER_WORLD * ws
+    value = total_bodies * args.steps / t
+
+    # roofline of the step kernel (one launch = args.steps world-steps of every world)
+    nb_world = len(B) // args.worlds
+    nf_world = len(F) // args.worlds
+    bytes_ws = algorithmic_bytes_per_world_step(nb_world, F[:nf_world], float(np.mean(counts)))
+    achieved = bytes_ws * args.worlds * args.steps / t / 1e9
+    peak, peak_kind = _peaks()
+    traffic = None
+    tp = os.path.join(HERE, "profiles", "traffic_step_kernel.txt")
+    if os.path.exists(tp):
+        for ln in open(tp):
+            if ln.startswith("dram_bytes_per_world_step_f32:") and args.precision == "f32":
+                traffic = float(ln.split(":")[1]) * args.worlds * args.steps
+
+    # e2e through the C ABI with pinned host buffers
+    n_b = len(B)
+    pinned = torch.empty(n_b * abi.BODY.itemsize, dtype=torch.uint8, pin_memory=True)
+    host = np.frombuffer(pinned.numpy(), dtype=abi.BODY)
+    lib = batch.lib
+    host[:] = batch.bodies(stream=sh)
+    ptr = pinned.data_ptr()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    opts = abi.StepOpts(DT, VI, PI, 1, args.mode, args.threads, 0)
+    barrier()
+    torch.cuda.synchronize()
+    e2.record(stream)
+    for _ in range(args.e2e_steps):
+        abi.check(lib.gb_batch_set_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh)))
+        abi.check(lib.gb_batch_step(batch.h, ctypes.byref(opts), ctypes.c_void_p(sh)))
+        abi.check(lib.gb_batch_get_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh)))
+    e3.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    te = e2.elapsed_time(e3) / 1e3
+    e2e_value = total_bodies * args.e2e_steps / te
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
+        "config": {"workload": f"pyramid x{args.worlds} per GPU, 210 boxes/world, jitter U(-0.01,0.01) m, "
+                               f"dt=1/60, 8 vel / 3 pos iters, {args.precision} bulk / f64 positions",
+                   "worlds_per_gpu": args.worlds, "bodies_per_world": BODIES_PER_WORLD,
+                   "launch": "one persistent launch per timed region, " + ("one CTA per world" if args.mode == 1 else "one warp per world"),
+                   "block_threads": args.threads,
+                   "l2": f"inputs larger than L2: {batch.arena_bytes() / 2**30:.2f} GiB resident per GPU",
+                   "mean_contacts_per_world": float(np.mean(counts))},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_world_step": bytes_ws},
+        "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY.itemsize,
+                "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": args.e2e_steps},
+        "gpu_launches": 1,
+        "clocks": clocks.summary(),
+        "status_nonzero_worlds": int(np.count_nonzero(status)),
+    }
+
+    if rank == 0 and not args.no_extras:
+        threads = os.cpu_count() or 1
+        cpu_steps = max(10, min(args.steps, 50))
+        rate, n, tcpu = cpu_oracle_rate(W, B, F, M, cpu_steps, threads, target_s=8.0)
+        out["cpu_baseline"] = {"value": rate, "unit": "body-steps/s", "cores": threads, "kind": "port",
+                               "sample": f"{n} of the {args.worlds} worlds x {cpu_steps} steps from the initial state "
+                                         f"({tcpu:.1f} s, {threads} threads, float64 C restatement)"}
+        # plain float64 path: one world per batch, one launch per world-step
+        n_plain, plain_steps = 16, 5
+        plain = [GpuBatch(*world_slice(W, B, F, M, w, args.worlds)[:3], precision="f64",
+                          moves=world_slice(W, B, F, M, w, args.worlds)[3]) for w in range(n_plain)]
+        for p in plain:
+            p.step(DT, VI, PI, 1, stream=sh)
+        torch.cuda.synchronize()
+        e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e4.record(stream)
+        for _ in range(plain_steps):
+            for p in plain:
+                p.step(DT, VI, PI, 1, stream=sh)
+        e5.record(stream)
+        torch.cuda.synchronize()
+        tp_ = e4.elapsed_time(e5) / 1e3
+        plain_rate = n_plain * BODIES_PER_WORLD * plain_steps / tp_
+        out["plain_f64_per_world"] = {"value": plain_rate, "unit": "body-steps/s",
+                                      "sample": f"{n_plain} worlds x {plain_steps} steps, one launch per world-step",
+                                      "batched_over_plain": value / plain_rate}
+        out["error"] = f32_step_error(W, B, F, M, args.worlds)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def world_slice(W, B, F, M, w, n_worlds):
+    """Records of world w of a batch, as a one-world batch."""
+    nb, nf, nm = len(B) // n_worlds, len(F) // n_worlds, len(M) // n_worlds
+    Wi = W[w:w + 1].copy()
+    Wi["body_start"] = 0
+    Wi["fixture_start"] = 0
+    Wi["move_start"] = 0
+    return Wi, B[w * nb:(w + 1) * nb].copy(), F[w * nf:(w + 1) * nf].copy(), M[w * nm:(w + 1) * nm].copy()
+
+
+def f32_step_error(W, B, F, M, n_worlds, settle_steps=60):
+    """Position/angle error of one float32 step against the float64
+    restatement, both started from the float64 state of world 0 after
+    `settle_steps` steps (bodies, fat AABBs and contacts) and solving in the
+    same constraint order."""
+    import oracle_lib
+    from pypybox2d_gb300 import abi
+    from pypybox2d_gb300.gpu import GpuBatch
+    Wi, Bi, Fi, Mi = world_slice(W, B, F, M, 0, n_worlds)
+    g64 = GpuBatch(Wi, Bi, Fi, precision="f64", moves=Mi)
+    g64.step(DT, VI, PI, settle_steps)
+    st, C = g64.bodies(), g64.contacts(0)
+    F2 = Fi.copy()
+    F2["aabb"] = g64.proxies()
+    W2 = Wi.copy()
+    W2["flags"] = W2["flags"] & np.uint32(0xFFFFFFFF ^ abi.W_NEW_FIXTURE)
+    W2["move_count"] = 0
+    W2["contact_count"] = len(C)
+    W2["inv_dt0"] = 1.0 / DT
+    g32 = GpuBatch(W2, st, F2, contacts=C, precision="f32")
+    g32.step(DT, VI, PI, 1, record_order=True)
+    orc = oracle_lib.OracleWorld(W2, st, F2, contacts=C, libm=False)
+    orc.step(DT, VI, PI, order=g32.solver_order(0))
+    a, b = g32.bodies(), orc.bodies()
+    return {"f32_one_step_max_position_error_m": float(np.hypot(a["cx"] - b["cx"], a["cy"] - b["cy"]).max()),
+            "f32_one_step_max_angle_error_rad": float(np.abs(a["a"] - b["a"]).max()),
+            "f32_one_step_max_velocity_error_mps": float(np.hypot(a["vx"] - b["vx"], a["vy"] - b["vy"]).max()),
+            "state": f"world 0 after {settle_steps} float64 steps; one step each from identical state, same constraint order"}
+
+
+if __name__ == "__main__":
+    main()

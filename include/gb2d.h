@@ -228,8 +228,8 @@ int gb_batch_get_solver_order(gb_batch *batch, int32_t world, int32_t *order, in
                               int32_t *n_out, void *cuda_stream);
 /* Per-world status words (GB_ST_* bits), n_worlds uint32. */
 int gb_batch_status(gb_batch *batch, uint32_t *status, void *cuda_stream);
-/* Counters of the last gb_batch_step call: kernel launches, colour count of
- * the last world, step count (3 int64). */
+/* Counters: step launches so far, bytes of device memory held by the
+ * batch, world-steps requested so far (3 int64). */
 int gb_batch_counters(gb_batch *batch, int64_t *counters);
 
 #ifdef __cplusplus

@@ -1155,3 +1155,67 @@ double or_run_scene(const gb_scene *scene, double dt, int vel_iters, int pos_ite
     pthread_mutex_destroy(&j.mu);
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }
+
+/* Persistent batch of worlds stepped by a pool of POSIX threads (the CPU
+ * baseline steps the same worlds repeatedly, as a simulation loop does). */
+struct or_batch {
+    int n;
+    or_world **w;
+};
+
+or_batch *or_batch_create(const gb_scene *scene) {
+    or_batch *b = (or_batch *)calloc(1, sizeof(or_batch));
+    b->n = scene->n_worlds;
+    b->w = (or_world **)calloc(b->n ? b->n : 1, sizeof(or_world *));
+    for (int i = 0; i < b->n; ++i)
+        b->w[i] = or_create(&scene->worlds[i], scene->bodies, scene->fixtures, scene->contacts, scene->moves);
+    return b;
+}
+
+void or_batch_destroy(or_batch *b) {
+    if (!b) return;
+    for (int i = 0; i < b->n; ++i) or_destroy(b->w[i]);
+    free(b->w);
+    free(b);
+}
+
+typedef struct {
+    or_batch *b;
+    double dt;
+    int vi, pi, steps, next;
+    pthread_mutex_t mu;
+} or_bjob;
+
+static void *or_bworker(void *arg) {
+    or_bjob *j = (or_bjob *)arg;
+    for (;;) {
+        pthread_mutex_lock(&j->mu);
+        int wi = j->next++;
+        pthread_mutex_unlock(&j->mu);
+        if (wi >= j->b->n) break;
+        for (int s = 0; s < j->steps; ++s) or_step(j->b->w[wi], j->dt, j->vi, j->pi);
+    }
+    return NULL;
+}
+
+double or_batch_step(or_batch *b, double dt, int vel_iters, int pos_iters, int n_steps, int threads) {
+    or_bjob j;
+    j.b = b; j.dt = dt; j.vi = vel_iters; j.pi = pos_iters; j.steps = n_steps; j.next = 0;
+    pthread_mutex_init(&j.mu, NULL);
+    if (threads < 1) threads = 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * threads);
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (int i = 0; i < threads; ++i) pthread_create(&th[i], NULL, or_bworker, &j);
+    for (int i = 0; i < threads; ++i) pthread_join(th[i], NULL);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    free(th);
+    pthread_mutex_destroy(&j.mu);
+    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+int or_batch_get_bodies(const or_batch *b, int wi, gb_body *out) {
+    if (wi < 0 || wi >= b->n) return -1;
+    or_get_bodies(b->w[wi], out);
+    return b->w[wi]->nb;
+}

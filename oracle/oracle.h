@@ -46,6 +46,14 @@ long long or_toi_events(const or_world *w);
 double or_run_scene(const gb_scene *scene, double dt, int vel_iters, int pos_iters, int n_steps, int threads,
                     gb_body *bodies_out);
 
+/* A persistent batch of worlds for the CPU baseline. */
+typedef struct or_batch or_batch;
+or_batch *or_batch_create(const gb_scene *scene);
+void or_batch_destroy(or_batch *b);
+/* n_steps World.step calls on every world, `threads` POSIX threads; wall seconds. */
+double or_batch_step(or_batch *b, double dt, int vel_iters, int pos_iters, int n_steps, int threads);
+int or_batch_get_bodies(const or_batch *b, int world, gb_body *out);
+
 #ifdef __cplusplus
 }
 #endif

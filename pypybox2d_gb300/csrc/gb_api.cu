@@ -377,7 +377,7 @@ int gb_batch_status(gb_batch *b, uint32_t *status, void *stream) {
 int gb_batch_counters(gb_batch *b, int64_t *c) {
     if (!b || !c) return fail(GB_E_ARG, "NULL argument");
     c[0] = b->counters[0];
-    c[1] = 0;
+    c[1] = (int64_t)b->arena_bytes;
     c[2] = b->counters[2];
     return 0;
 }

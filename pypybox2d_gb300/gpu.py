@@ -17,10 +17,10 @@ from . import abi
 class GpuBatch:
     """A batch of independent worlds resident in device memory."""
 
-    def __init__(self, worlds, bodies, fixtures, contacts=None, precision: str = "f64"):
+    def __init__(self, worlds, bodies, fixtures, contacts=None, precision: str = "f64", moves=None):
         self.lib = abi.load_library()
         self.prec = abi.PREC_F64 if precision in ("f64", "float64", abi.PREC_F64) else abi.PREC_F32
-        scene, keep = abi.make_scene(worlds, bodies, fixtures, contacts)
+        scene, keep = abi.make_scene(worlds, bodies, fixtures, contacts, moves)
         self.worlds, self.n_bodies, self.n_fixtures = keep[0], len(keep[1]), len(keep[2])
         h = ctypes.c_void_p()
         abi.check(self.lib.gb_batch_create(ctypes.byref(scene), self.prec, ctypes.byref(h)))
@@ -76,6 +76,11 @@ class GpuBatch:
         abi.check(self.lib.gb_batch_get_solver_order(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                                                      cap, ctypes.byref(n), None))
         return out[:n.value].copy()
+
+    def arena_bytes(self) -> int:
+        c = (ctypes.c_int64 * 3)()
+        abi.check(self.lib.gb_batch_counters(self.h, c))
+        return int(c[1])
 
     def status(self) -> np.ndarray:
         out = np.zeros(self.n_worlds, dtype=np.uint32)

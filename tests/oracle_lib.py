@@ -58,6 +58,13 @@ def load(libm: bool = False) -> ctypes.CDLL:
     lib.or_toi_events.restype = ctypes.c_longlong
     lib.or_run_scene.argtypes = [ctypes.POINTER(abi.Scene), dbl, i32, i32, i32, i32, vp]
     lib.or_run_scene.restype = dbl
+    lib.or_batch_create.argtypes = [ctypes.POINTER(abi.Scene)]
+    lib.or_batch_create.restype = vp
+    lib.or_batch_destroy.argtypes = [vp]
+    lib.or_batch_step.argtypes = [vp, dbl, i32, i32, i32, i32]
+    lib.or_batch_step.restype = dbl
+    lib.or_batch_get_bodies.argtypes = [vp, i32, vp]
+    lib.or_batch_get_bodies.restype = i32
     _libs[libm] = lib
     return lib
 
