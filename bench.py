@@ -192,7 +192,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--worlds", type=int, default=4096)
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
-    ap.add_argument("--mode", type=int, default=1, help="1 = CTA per world, 2 = warp per world")
+    ap.add_argument("--mode", type=int, default=3, help="1 = one CTA per world (monolithic), 2 = one warp per world, "
+                                                        "3 = phase kernels over the whole batch")
     ap.add_argument("--threads", type=int, default=128)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="skip cpu baseline, plain path and error legs")
@@ -292,7 +293,9 @@ def main():
         "config": {"workload": f"pyramid x{args.worlds} per GPU, 210 boxes/world, jitter U(-0.01,0.01) m, "
                                f"dt=1/60, 8 vel / 3 pos iters, {args.precision} bulk / f64 positions",
                    "worlds_per_gpu": args.worlds, "bodies_per_world": BODIES_PER_WORLD,
-                   "launch": "one persistent launch per timed region, " + ("one CTA per world" if args.mode == 1 else "one warp per world"),
+                   "launch": {1: "one persistent launch per timed region, one CTA per world",
+                              2: "one persistent launch per timed region, one warp per world",
+                              3: "11 phase kernels per step (batch-wide + per-world)"}[args.mode],
                    "block_threads": args.threads,
                    "l2": f"inputs larger than L2: {batch.arena_bytes() / 2**30:.2f} GiB resident per GPU",
                    "mean_contacts_per_world": float(np.mean(counts))},
@@ -301,7 +304,7 @@ def main():
                      "algorithmic_bytes_per_world_step": bytes_ws},
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY.itemsize,
                 "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": args.e2e_steps},
-        "gpu_launches": 1,
+        "gpu_launches": 1 if args.mode != 3 else 11 * args.steps,
         "clocks": clocks.summary(),
         "status_nonzero_worlds": int(np.count_nonzero(status)),
     }

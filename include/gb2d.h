@@ -191,7 +191,8 @@ typedef struct gb_step_opts {
     int32_t n_steps;
     int32_t launch_mode;
     int32_t block_threads;
-    int32_t record_order; /* keep the solver constraint order of the last step */
+    int32_t record_order; /* bit 0: keep the solver constraint order of the last step;
+                             bit 1: accumulate per-phase SM clocks (gb_batch_phase_clocks) */
 } gb_step_opts;
 
 /* Library version and build information. */
@@ -228,6 +229,11 @@ int gb_batch_get_solver_order(gb_batch *batch, int32_t world, int32_t *order, in
                               int32_t *n_out, void *cuda_stream);
 /* Per-world status words (GB_ST_* bits), n_worlds uint32. */
 int gb_batch_status(gb_batch *batch, uint32_t *status, void *cuda_stream);
+/* Accumulated SM clock cycles per step phase, 16 int64 per world
+ * (0 pairing of new fixtures, 1 contact update, 2 islands, 3 colouring,
+ * 4 velocity set-up, 5 velocity iterations, 6 position iterations, 7 sleep,
+ * 8 fixture sync + pair finding, 9 continuous collision, 10 force clear). */
+int gb_batch_phase_clocks(gb_batch *batch, int64_t *clocks, void *cuda_stream);
 /* Counters: step launches so far, bytes of device memory held by the
  * batch, world-steps requested so far (3 int64). */
 int gb_batch_counters(gb_batch *batch, int64_t *counters);

@@ -144,7 +144,7 @@ EXPORTED = (
     "gb_batch_create", "gb_batch_destroy", "gb_batch_step",
     "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_get_proxies",
     "gb_batch_get_contact_counts", "gb_batch_get_contacts", "gb_batch_get_solver_order",
-    "gb_batch_status", "gb_batch_counters",
+    "gb_batch_status", "gb_batch_counters", "gb_batch_phase_clocks",
 )
 
 _lib = None
@@ -181,6 +181,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_get_solver_order.argtypes = [vp, i32, i32p, i32, i32p, vp]
     lib.gb_batch_status.argtypes = [vp, u32p, vp]
     lib.gb_batch_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    lib.gb_batch_phase_clocks.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

@@ -46,7 +46,11 @@ struct Arena {
 
 template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap) {
     B.n_worlds = nw;
+    B.n_bodies = nb;
+    B.n_slots = ncap;
     B.hdr = a.take<WorldHdr>(nw);
+    B.b_world = a.take<int>(nb);
+    B.c_world = a.take<int>(ncap);
     B.b_type = a.take<int>(nb); B.b_flags = a.take<uint32_t>(nb); B.b_fstart = a.take<int>(nb); B.b_fcount = a.take<int>(nb);
     B.b_xp = a.take<vec2<double>>(nb); B.b_xq = a.take<rot2<double>>(nb);
     B.b_lc = a.take<vec2<double>>(nb); B.b_c = a.take<vec2<double>>(nb); B.b_c0 = a.take<vec2<double>>(nb);
@@ -74,6 +78,8 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_cons = a.take<Cons<R>>(ncap);
     B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
     B.order_out = a.take<int>(ncap);
+    B.prof = a.take<long long>((size_t)nw * GB_NPROF);
+    B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
 }
 }  // namespace
 
@@ -185,6 +191,18 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
     a2.base = b->arena;
     if (precision == GB_PREC_F64) carve(a2, b->bd, b->nw, b->nb, b->nf, b->ncap);
     else carve(a2, b->bf, b->nw, b->nb, b->nf, b->ncap);
+    {
+        std::vector<int> bw(std::max(1, b->nb), 0), cw(std::max(1, b->ncap), 0);
+        for (int i = 0; i < b->nw; ++i) {
+            for (int k = 0; k < b->hdr[i].nb; ++k) bw[b->hdr[i].bbase + k] = i;
+            for (int k = 0; k < b->hdr[i].ccap; ++k) cw[b->hdr[i].cbase + k] = i;
+        }
+        // bodies outside every world keep world 0 but are never stepped
+        int *d_bw = precision == GB_PREC_F64 ? b->bd.b_world : b->bf.b_world;
+        int *d_cw = precision == GB_PREC_F64 ? b->bd.c_world : b->bf.c_world;
+        if (b->nb > 0) CK(cudaMemcpy(d_bw, bw.data(), sizeof(int) * b->nb, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(d_cw, cw.data(), sizeof(int) * b->ncap, cudaMemcpyHostToDevice));
+    }
     CK(cudaMalloc((void **)&b->d_worlds, sizeof(int) * b->nw));
     CK(cudaMemcpy(b->d_worlds, b->launch_order.data(), sizeof(int) * b->nw, cudaMemcpyHostToDevice));
     CK(cudaMalloc((void **)&b->d_bstage, sizeof(gb_body) * std::max(1, b->nb)));
@@ -262,8 +280,9 @@ int gb_batch_step(gb_batch *b, const gb_step_opts *o, void *stream) {
     sp.dt_ratio = 0.0;
     sp.vel_iters = o->vel_iters;
     sp.pos_iters = o->pos_iters;
-    sp.record_order = o->record_order;
-    int mode = o->launch_mode == 2 ? 2 : 1;
+    sp.record_order = o->record_order & 1;
+    sp.profile = (o->record_order >> 1) & 1;
+    int mode = (o->launch_mode == 2 || o->launch_mode == 3) ? o->launch_mode : (o->launch_mode == 0 ? 3 : 1);
     int threads = o->block_threads > 0 ? o->block_threads : (mode == 2 ? 128 : 128);
     if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
     int rc = b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st)
@@ -371,6 +390,14 @@ int gb_batch_status(gb_batch *b, uint32_t *status, void *stream) {
     int rc = read_headers(b, h, (cudaStream_t)stream);
     if (rc) return rc;
     for (int i = 0; i < b->nw; ++i) status[i] = h[i].status;
+    return 0;
+}
+
+int gb_batch_phase_clocks(gb_batch *b, int64_t *clocks, void *stream) {
+    if (!b || !clocks) return fail(GB_E_ARG, "NULL argument");
+    const long long *src = b->prec == GB_PREC_F64 ? b->bd.prof : b->bf.prof;
+    CK(cudaMemcpyAsync(clocks, src, sizeof(long long) * (size_t)b->nw * GB_NPROF, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
     return 0;
 }
 

@@ -4,7 +4,7 @@
 // reproduces the CPU restatement bit for bit) and gb_f32.cu (GB_REAL = float).
 #pragma once
 #include <cuda_runtime.h>
-#include "gb_toi.cuh"
+#include "gb_phases.cuh"
 #include "gb_launch.h"
 
 namespace {
@@ -98,6 +98,26 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
     if (n_list <= 0) return 0;
     // the step kernels use ~220 registers per thread: at most 256 threads per CTA
     if (threads > 256) threads = 256;
+    if (mode == 3) {
+        // phased: batch-wide kernels for the per-element work, per-world CTAs
+        // for the ordered parts (see gb_phases.cuh)
+        const int nb = B.n_bodies, ns = B.n_slots, T = 256;
+        const int gb = (nb + T - 1) / T, gs = (ns + T - 1) / T;
+        for (int s = 0; s < n_steps; ++s) {
+            k_world<GB_REAL, PH_PAIRS0><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            if (nb) k_pre<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
+            if (ns) k_collide<GB_REAL><<<gs, T, 0, st>>>(B, ns);
+            k_world<GB_REAL, PH_COLLIDE2><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            k_world<GB_REAL, PH_ISLANDS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            if (nb) k_vinit<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
+            if (ns) k_cinit<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
+            k_world<GB_REAL, PH_SOLVE><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            k_world<GB_REAL, PH_PAIRS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            if (ns) k_toi1<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
+            k_world<GB_REAL, PH_TOI2><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+        }
+        return (int)cudaGetLastError();
+    }
     if (mode == 2) {
         int wpc = threads / 32;
         if (wpc < 1) wpc = 1;

@@ -1,0 +1,193 @@
+// gb_phases.cuh -- the batched step as a sequence of phase kernels.
+//
+// One World.step of every world of the batch is 11 launches (captured once
+// into a CUDA graph and replayed per step):
+//
+//   k_pairs0    per world   pair finding over the pending move buffer (new fixtures)
+//   k_pre       per body    collide wake marks, TOI state reset
+//   k_collide   per contact narrow phase + warm-start matching of every contact with
+//                           an awake non-static body (contact_manager.py:174-223)
+//   k_collide2  per world   the same loop for contacts whose bodies were asleep (in
+//                           list order, on one thread: wakes propagate forward), wakes,
+//                           destruction of non-overlapping contacts
+//   k_islands   per world   union-find islands, constraint list, graph colouring
+//   k_vinit     per body    velocity integration (island.py:71-95)
+//   k_cinit     per constraint  solver set-up (contact.py:375-496)
+//   k_solve     per world   warm start, velocity and position iterations, sleep
+//   k_pairs     per world   fixture sync and pair finding (world.py:582-592)
+//   k_toi1      per contact first pass of the time-of-impact loop (float64)
+//   k_toi2      per world   the rest of the event loop, force clear
+//
+// "per body / contact / constraint" kernels run one thread per element of
+// every world (the 4096-world batch gives ~2.4 M contact threads), "per
+// world" kernels one CTA per world.  The order inside each world is the
+// monolithic step's, so both give the same doubles.
+#pragma once
+#include "gb_toi.cuh"
+
+#define P_DEFERRED 1u   // some contact was skipped by k_collide (both bodies asleep)
+#define P_WOKE 2u       // k_collide woke a body that was asleep
+#define P_DESTROY 4u    // some contact is to be destroyed
+#define P_SOLVING 8u    // the island solve runs this step
+
+template <class R> __device__ __forceinline__ WView<R> view_global(const Batch<R> &B, int wi) {
+    WorldHdr *H = &B.hdr[wi];
+    WView<R> w{B, H, H->bbase, H->fbase, H->cbase, wi};
+    return w;
+}
+
+template <class R> __global__ void k_pre(Batch<R> B, int n_bodies, StepParams sp) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_bodies) return;
+    const WorldHdr *H = &B.hdr[B.b_world[b]];
+    uint32_t f = B.b_flags[b];
+    B.s_wake[b] = ((f & GB_BODY_AWAKE) && B.b_type[b] != GB_BODY_STATIC) ? -1 : GB_INF_IDX;
+    // world.py:599-602 (alpha0 is read by nothing before the TOI loop)
+    if ((H->flags & GB_W_CONTINUOUS) && (H->flags & GB_W_STEP_COMPLETE) && sp.dt > 0.0) B.b_alpha0[b] = 0.0;
+}
+
+template <class R> __global__ void k_collide(Batch<R> B, int n_slots) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_slots) return;
+    int wi = B.c_world[s];
+    WView<R> w = view_global(B, wi);
+    int i = s - w.cb;
+    if (i >= w.H->nc) return;
+    int *wake = B.s_wake + w.bb;
+    bool woke;
+    int r = collide_one(w, i, wake, &woke);
+    B.s_proc[s] = r;
+    if (r == 0) { atomicOr(&w.H->pflags, P_DEFERRED); return; }
+    if (r == 2) { atomicOr(&w.H->pflags, P_DESTROY); return; }
+    if (woke) {
+        const ContactRec<R> &c = w.con(i);
+        int oa = atomicMin(&wake[w.fbody(c.fa)], i);
+        int ob = atomicMin(&wake[w.fbody(c.fb)], i);
+        if (oa == GB_INF_IDX || ob == GB_INF_IDX) atomicOr(&w.H->pflags, P_WOKE);
+    }
+}
+
+template <class R> __global__ void k_vinit(Batch<R> B, int n_bodies, StepParams sp) {
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= n_bodies) return;
+    WView<R> w = view_global(B, B.b_world[b]);
+    if (!(w.H->pflags & P_SOLVING)) return;
+    integrate_velocity_body(w, b - w.bb, sp.dt);
+}
+
+template <class R> __global__ void k_cinit(Batch<R> B, int n_slots, StepParams sp) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_slots) return;
+    WView<R> w = view_global(B, B.c_world[s]);
+    int k = s - w.cb;
+    if (!(w.H->pflags & P_SOLVING) || k >= w.H->last_ncons) return;
+    init_constraint(w, k, sp);
+}
+
+template <class R> __global__ void k_toi1(Batch<R> B, int n_slots, StepParams sp) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_slots) return;
+    WView<R> w = view_global(B, B.c_world[s]);
+    int i = s - w.cb;
+    if (i >= w.H->nc) return;
+    if (!((w.H->flags & GB_W_CONTINUOUS) && sp.dt > 0.0)) return;
+    if (!(w.H->flags & GB_W_STEP_COMPLETE)) return;   // k_toi2 then runs the whole loop in order
+    toi_reset_contact(w, i);
+    toi_first_pass_contact(w, i, B.s_proc + w.cb);
+}
+
+// Per-world phases ---------------------------------------------------------
+#define PH_PAIRS0 0
+#define PH_COLLIDE2 1
+#define PH_ISLANDS 2
+#define PH_SOLVE 3
+#define PH_PAIRS 4
+#define PH_TOI2 5
+
+template <class R, int PH> __global__ void __launch_bounds__(256) k_world(Batch<R> B, StepParams sp, const int *worlds) {
+    __shared__ int sm[96];
+    __shared__ WorldHdr H;
+    __shared__ WShared sh;
+    const int wi = worlds[blockIdx.x];
+    if (threadIdx.x == 0) { H = B.hdr[wi]; sh.nmove = 0; }
+    __syncthreads();
+    GroupCta g{sm};
+    WView<R> w{B, &H, H.bbase, H.fbase, H.cbase, wi};
+    const bool solving = (H.flags & GB_W_STEP_COMPLETE) && sp.dt > 0.0;
+    if (PH == PH_PAIRS0) {
+        if (threadIdx.x == 0) H.pflags = 0;
+        if (H.flags & GB_W_NEW_FIXTURE) {
+            int nf = H.nf;
+            int n0 = H.nmove0;
+            if (n0 == 0)
+                for (int f = g.rank(); f < nf; f += g.size()) B.s_move[w.fb + f] = f;
+            g.sync();
+            if (g.rank() == 0) { sh.nmove = n0 ? n0 : nf; H.nmove0 = 0; }
+            g.sync();
+            find_new_contacts(g, w, &sh);
+            if (g.rank() == 0) H.flags &= ~GB_W_NEW_FIXTURE;
+        }
+    } else if (PH == PH_COLLIDE2) {
+        int *wake = B.s_wake + w.bb;
+        int *proc = B.s_proc + w.cb;
+        uint32_t pf = H.pflags;
+        bool woke_any = (pf & P_WOKE) != 0;
+        if ((pf & P_DEFERRED) && (pf & P_WOKE)) {
+            // contacts between sleeping bodies, in list order: a body woken at
+            // position j makes the contacts after j active (sequential rule)
+            if (g.rank() == 0) {
+                for (int i = 0; i < H.nc; ++i) {
+                    if (proc[i] != 0) continue;
+                    bool woke;
+                    int r = collide_one(w, i, wake, &woke);
+                    proc[i] = r;
+                    if (r == 2) H.pflags |= P_DESTROY;
+                    if (woke) {
+                        const ContactRec<R> &c = w.con(i);
+                        int a = w.fbody(c.fa), b = w.fbody(c.fb);
+                        if (wake[a] > i) wake[a] = i;
+                        if (wake[b] > i) wake[b] = i;
+                    }
+                }
+            }
+            g.sync();
+        }
+        if (woke_any)
+            for (int b = g.rank(); b < H.nb; b += g.size())
+                if (wake[b] >= 0 && wake[b] != GB_INF_IDX) wake_body(w, b);
+        g.sync();
+        if (H.pflags & P_DESTROY) compact_contacts(g, w, proc);
+    } else if (PH == PH_ISLANDS) {
+        if (solving) {
+            if (g.rank() == 0) H.pflags |= P_SOLVING;
+            islands_group(g, w, sp);
+            constraints_group(g, w, sp);
+        } else if (g.rank() == 0) {
+            H.last_ncons = 0;
+        }
+    } else if (PH == PH_SOLVE) {
+        if (H.pflags & P_SOLVING) {
+            solve_group(g, w, sp);
+            sleep_group(g, w, sp);
+        }
+    } else if (PH == PH_PAIRS) {
+        if (H.pflags & P_SOLVING) sync_pairs_group(g, w, sp, &sh);
+    } else if (PH == PH_TOI2) {
+        if ((H.flags & GB_W_CONTINUOUS) && sp.dt > 0.0) {
+            const bool par_first = (H.flags & GB_W_STEP_COMPLETE) != 0;
+            if (par_first)   // island flags of the bodies (world.py:600-601)
+                for (int b = g.rank(); b < H.nb; b += g.size()) B.s_bvis[w.bb + b] = 0;
+            g.sync();
+            toi_loop(g, w, sp, &sh, par_first, par_first);
+        }
+        g.sync();
+        if (g.rank() == 0 && sp.dt > 0.0) H.inv_dt0 = sp.inv_dt;
+        if (H.flags & GB_W_AUTO_CLEAR_FORCES)
+            for (int b = g.rank(); b < H.nb; b += g.size()) {
+                B.b_f[w.bb + b] = mk<R>(0, 0);
+                B.b_torque[w.bb + b] = (R)0;
+            }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) B.hdr[wi] = H;
+}

@@ -42,6 +42,7 @@
 struct WShared {
     unsigned long long red;
     int nmove;
+    int nisland;
     int min_contact;
     double min_alpha;
     int any_dfs;
@@ -278,44 +279,32 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
 }
 
 // ------------------------------------------------------------ collide
-template <class R, class G> __device__ void collide(const G &g, const WView<R> &w) {
-    int nb = w.H->nb, nc = w.H->nc;
-    int *wake = w.B.s_wake + w.bb;
-    int *proc = w.B.s_proc + w.cb;     // 0 = not processed, 1 = processed, 2 = destroy
-    for (int b = g.rank(); b < nb; b += g.size())
-        wake[b] = (w.awake(b) && w.btype(b) != GB_BODY_STATIC) ? -1 : GB_INF_IDX;
-    for (int i = g.rank(); i < nc; i += g.size()) proc[i] = 0;
-    g.sync();
-    // Least fixed point of the sequential rule "contact i is updated iff one
-    // of its bodies is non-static and awake when the loop reaches i"; a body
-    // woken by contact j counts as awake for contacts after j.
-    for (int round = 0; round <= nc + 1; ++round) {
-        bool changed = false;
-        for (int i = g.rank(); i < nc; i += g.size()) {
-            if (proc[i]) continue;
-            ContactRec<R> &c = w.con(i);
-            int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
-            bool act_a = w.btype(ba) != GB_BODY_STATIC && wake[ba] < i;
-            bool act_b = w.btype(bb) != GB_BODY_STATIC && wake[bb] < i;
-            if (!act_a && !act_b) continue;
-            proc[i] = 1;
-            if (c.flags & GB_C_FILTER) {
-                if (!should_collide(w, bb, ba) || !default_filter(w, c.fa, c.fb)) { proc[i] = 2; continue; }
-                c.flags &= ~GB_C_FILTER;
-            }
-            if (!aabb_overlap(w.B.f_aabb[w.fb + c.fa], w.B.f_aabb[w.fb + c.fb])) { proc[i] = 2; continue; }
-            if (contact_update(w, i)) {
-                int oa = atomicMin(&wake[ba], i);
-                int ob = atomicMin(&wake[bb], i);
-                if (oa > i || ob > i) changed = true;
-            }
-        }
-        if (!g.any(changed)) break;
+// One iteration of ContactManager.collide's loop (contact_manager.py:174-223)
+// for contact i, where wake[] gives for every body of the world the list
+// position from which it counts as awake (-1: awake and non-static when the
+// loop starts).  Returns 0 when both bodies are inactive at that point,
+// 1 after Contact.update (*woke: touching changed, both bodies woken), 2 when
+// the contact is to be destroyed.
+template <class R> __device__ int collide_one(const WView<R> &w, int i, const int *wake, bool *woke) {
+    ContactRec<R> &c = w.con(i);
+    int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+    bool act_a = w.btype(ba) != GB_BODY_STATIC && wake[ba] < i;
+    bool act_b = w.btype(bb) != GB_BODY_STATIC && wake[bb] < i;
+    *woke = false;
+    if (!act_a && !act_b) return 0;
+    if (c.flags & GB_C_FILTER) {
+        if (!should_collide(w, bb, ba) || !default_filter(w, c.fa, c.fb)) return 2;
+        c.flags &= ~GB_C_FILTER;
     }
-    g.sync();
-    for (int b = g.rank(); b < nb; b += g.size())
-        if (wake[b] >= 0 && wake[b] != GB_INF_IDX) wake_body(w, b);
-    // destroy (contact_manager.py:160-172), keeping creation order
+    if (!aabb_overlap(w.B.f_aabb[w.fb + c.fa], w.B.f_aabb[w.fb + c.fb])) return 2;
+    *woke = contact_update(w, i);
+    return 1;
+}
+
+// contact_manager.py:160-172 destroy of every contact with proc[i] == 2,
+// keeping creation order.
+template <class R, class G> __device__ void compact_contacts(const G &g, const WView<R> &w, const int *proc) {
+    const int nc = w.H->nc;
     int *pref = w.B.s_pref + w.cb;
     int alive = group_scan(g, nc, [&](int i) { return proc[i] == 2 ? 0 : 1; }, pref);
     g.sync();
@@ -332,6 +321,40 @@ template <class R, class G> __device__ void collide(const G &g, const WView<R> &
         if (g.rank() == 0) w.H->nc = alive;
     }
     g.sync();
+}
+
+template <class R, class G> __device__ void collide(const G &g, const WView<R> &w) {
+    int nb = w.H->nb, nc = w.H->nc;
+    int *wake = w.B.s_wake + w.bb;
+    int *proc = w.B.s_proc + w.cb;     // 0 = not updated, 1 = updated, 2 = destroy
+    for (int b = g.rank(); b < nb; b += g.size())
+        wake[b] = (w.awake(b) && w.btype(b) != GB_BODY_STATIC) ? -1 : GB_INF_IDX;
+    for (int i = g.rank(); i < nc; i += g.size()) proc[i] = 0;
+    g.sync();
+    // Least fixed point of the sequential rule "contact i is updated iff one
+    // of its bodies is non-static and awake when the loop reaches i"; a body
+    // woken by contact j counts as awake for contacts after j.
+    for (int round = 0; round <= nc + 1; ++round) {
+        bool changed = false;
+        for (int i = g.rank(); i < nc; i += g.size()) {
+            if (proc[i]) continue;
+            bool woke;
+            int r = collide_one(w, i, wake, &woke);
+            if (r == 0) continue;
+            proc[i] = r;
+            if (woke) {
+                const ContactRec<R> &c = w.con(i);
+                int oa = atomicMin(&wake[w.fbody(c.fa)], i);
+                int ob = atomicMin(&wake[w.fbody(c.fb)], i);
+                if (oa > i || ob > i) changed = true;
+            }
+        }
+        if (!g.any(changed)) break;
+    }
+    g.sync();
+    for (int b = g.rank(); b < nb; b += g.size())
+        if (wake[b] >= 0 && wake[b] != GB_INF_IDX) wake_body(w, b);
+    compact_contacts(g, w, proc);
 }
 
 // ------------------------------------------------------------ contact solver
@@ -614,7 +637,10 @@ template <class R> __device__ void island_dfs(const WView<R> &w, int seed, int *
     *last_ns = lns;
 }
 
-template <class R, class G> __device__ void world_solve(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh) {
+// Island search by union-find (world.py:495-573 without the visit order):
+// components over qualifying contacts between non-static bodies, the
+// simulated flag of each component and its depth-first seed.
+template <class R, class G> __device__ void islands_group(const G &g, const WView<R> &w, const StepParams &sp) {
     const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
     int *parent = w.B.s_parent + w.bb;
     uint32_t *rootf = w.B.s_root + w.bb;
@@ -627,9 +653,11 @@ template <class R, class G> __device__ void world_solve(const G &g, const WView<
     int *order = w.B.s_order + w.cb;
     int *pref = w.B.s_pref + w.cb;
     Cons<R> *cons = w.B.s_cons + w.cb;
+    int *coff = w.B.s_proc + w.cb;
     const double dt = sp.dt;
     const bool warm = (w.H->flags & GB_W_WARM_STARTING) != 0;
-
+    (void)nb; (void)nc; (void)nf; (void)parent; (void)rootf; (void)seed; (void)minsep; (void)minsleep; (void)claim;
+    (void)cons_of; (void)colour; (void)order; (void)pref; (void)cons; (void)coff; (void)dt; (void)warm;
     // 1. components of the constraint graph (static bodies do not link)
     for (int b = g.rank(); b < nb; b += g.size()) {
         parent[b] = b; rootf[b] = 0; seed[b] = GB_INF_IDX;
@@ -655,7 +683,30 @@ template <class R, class G> __device__ void world_solve(const G &g, const WView<
         }
     }
     all_allow = !g.any(!all_allow);
+    if (g.rank() == 0) w.H->all_allow = all_allow ? 1 : 0;
     g.sync();
+}
+
+// Constraint list of the simulated islands in contact-list order, graph
+// colouring and the colour-major solver order.
+template <class R, class G> __device__ void constraints_group(const G &g, const WView<R> &w, const StepParams &sp) {
+    const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
+    int *parent = w.B.s_parent + w.bb;
+    uint32_t *rootf = w.B.s_root + w.bb;
+    int *seed = w.B.s_seed + w.bb;
+    unsigned long long *minsep = w.B.s_minsep + w.bb;
+    unsigned long long *minsleep = w.B.s_minsleep + w.bb;
+    unsigned long long *claim = w.B.s_claim + w.bb;
+    int *cons_of = w.B.s_cons_of + w.cb;
+    int *colour = w.B.s_colour + w.cb;
+    int *order = w.B.s_order + w.cb;
+    int *pref = w.B.s_pref + w.cb;
+    Cons<R> *cons = w.B.s_cons + w.cb;
+    int *coff = w.B.s_proc + w.cb;
+    const double dt = sp.dt;
+    const bool warm = (w.H->flags & GB_W_WARM_STARTING) != 0;
+    (void)nb; (void)nc; (void)nf; (void)parent; (void)rootf; (void)seed; (void)minsep; (void)minsleep; (void)claim;
+    (void)cons_of; (void)colour; (void)order; (void)pref; (void)cons; (void)coff; (void)dt; (void)warm;
     // 2. island membership: wake the members of simulated islands (DFS sets
     //    body.awake = True, world.py:520), constraints = qualifying contacts
     //    of simulated islands in contact-list order.
@@ -723,7 +774,6 @@ template <class R, class G> __device__ void world_solve(const G &g, const WView<
     // order = constraints sorted by (colour, index); colour offsets live in
     // the collide scratch (free during the solve); ncol < ccap always holds
     // because every colour holds at least one constraint and ncons <= nc.
-    int *coff = w.B.s_proc + w.cb;
     if (ncol + 1 > w.H->ccap) {   // cannot happen while ncons < ccap; never index past the world's slots
         if (g.rank() == 0) w.H->status |= GB_ST_ITER_LIMIT;
         ncol = w.H->ccap - 1;
@@ -742,42 +792,69 @@ template <class R, class G> __device__ void world_solve(const G &g, const WView<
         }
         if (g.rank() == 0) coff[ncol] = start;
     }
-    if (g.rank() == 0) { sh->ncons = ncons; sh->ncolours = ncol; w.H->last_ncons = ncons; w.H->last_ncolours = ncol; }
+    if (g.rank() == 0) { w.H->last_ncons = ncons; w.H->last_ncolours = ncol; }
     g.sync();
     if (sp.record_order) {
         int *out = w.B.order_out + w.cb;
         for (int k = g.rank(); k < ncons; k += g.size()) out[k] = cons[order[k]].cidx;
     }
-    // 4. integrate velocities (island.py:71-95)
+}
+
+// island.py:71-95 for one body of a simulated island
+template <class R> __device__ __forceinline__ void integrate_velocity_body(const WView<R> &w, int b, double dt) {
+    const uint32_t *rootf = w.B.s_root + w.bb;
+    const int *parent = w.B.s_parent + w.bb;
+    if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) return;
     const vec2<R> grav = mk<R>((R)w.H->gx, (R)w.H->gy);
-    for (int b = g.rank(); b < nb; b += g.size()) {
-        if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
-        int gb = w.bb + b;
-        w.B.b_c0[gb] = w.B.b_c[gb];
-        w.B.b_a0[gb] = w.B.b_a[gb];
-        if (w.btype(b) == GB_BODY_DYNAMIC) {
-            vec2<R> v = w.B.b_v[gb];
-            R om = w.B.b_w[gb];
-            const R dtr = (R)dt;
-            v = v + dtr * (w.B.b_gscale[gb] * grav + w.B.b_inv_mass[gb] * w.B.b_f[gb]);
-            om = om + dtr * w.B.b_inv_I[gb] * w.B.b_torque[gb];
-            v = cclamp((R)1 - dtr * w.B.b_ldamp[gb], (R)0, (R)1) * v;
-            om = om * cclamp((R)1 - dtr * w.B.b_adamp[gb], (R)0, (R)1);
-            w.B.b_v[gb] = v; w.B.b_w[gb] = om;
-        }
+    int gb = w.bb + b;
+    w.B.b_c0[gb] = w.B.b_c[gb];
+    w.B.b_a0[gb] = w.B.b_a[gb];
+    if (w.btype(b) == GB_BODY_DYNAMIC) {
+        vec2<R> v = w.B.b_v[gb];
+        R om = w.B.b_w[gb];
+        const R dtr = (R)dt;
+        v = v + dtr * (w.B.b_gscale[gb] * grav + w.B.b_inv_mass[gb] * w.B.b_f[gb]);
+        om = om + dtr * w.B.b_inv_I[gb] * w.B.b_torque[gb];
+        v = cclamp((R)1 - dtr * w.B.b_ldamp[gb], (R)0, (R)1) * v;
+        om = om * cclamp((R)1 - dtr * w.B.b_adamp[gb], (R)0, (R)1);
+        w.B.b_v[gb] = v; w.B.b_w[gb] = om;
     }
-    g.sync();
-    // 5. constraint set-up (positions before integration, velocities after)
-    for (int k = g.rank(); k < ncons; k += g.size()) {
-        Cons<R> &q = cons[k];
-        int root = q.root;
-        build_cons(w, q, q.cidx, warm, sp.dt_ratio);
-        q.root = root;
-        int ga = w.bb + q.ia, gbb = w.bb + q.ib;
-        init_velocity(q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], w.B.b_v[ga], w.B.b_w[ga], w.B.b_v[gbb], w.B.b_w[gbb]);
-    }
-    g.sync();
+}
+
+// contact.py:375-496 for constraint k (positions before integration,
+// velocities after)
+template <class R> __device__ __forceinline__ void init_constraint(const WView<R> &w, int k, const StepParams &sp) {
+    Cons<R> &q = w.B.s_cons[w.cb + k];
+    int root = q.root;
+    build_cons(w, q, q.cidx, (w.H->flags & GB_W_WARM_STARTING) != 0, w.H->inv_dt0 * sp.dt);
+    q.root = root;
+    int ga = w.bb + q.ia, gbb = w.bb + q.ib;
+    init_velocity(q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], w.B.b_v[ga], w.B.b_w[ga], w.B.b_v[gbb], w.B.b_w[gbb]);
+}
+
+// Warm start, velocity iterations, impulse store, position integration,
+// position iterations and transform write-back (island.py:98-159).
+template <class R, class G> __device__ void solve_group(const G &g, const WView<R> &w, const StepParams &sp) {
+    const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
+    int *parent = w.B.s_parent + w.bb;
+    uint32_t *rootf = w.B.s_root + w.bb;
+    int *seed = w.B.s_seed + w.bb;
+    unsigned long long *minsep = w.B.s_minsep + w.bb;
+    unsigned long long *minsleep = w.B.s_minsleep + w.bb;
+    unsigned long long *claim = w.B.s_claim + w.bb;
+    int *cons_of = w.B.s_cons_of + w.cb;
+    int *colour = w.B.s_colour + w.cb;
+    int *order = w.B.s_order + w.cb;
+    int *pref = w.B.s_pref + w.cb;
+    Cons<R> *cons = w.B.s_cons + w.cb;
+    int *coff = w.B.s_proc + w.cb;
+    const double dt = sp.dt;
+    const bool warm = (w.H->flags & GB_W_WARM_STARTING) != 0;
+    (void)nb; (void)nc; (void)nf; (void)parent; (void)rootf; (void)seed; (void)minsep; (void)minsleep; (void)claim;
+    (void)cons_of; (void)colour; (void)order; (void)pref; (void)cons; (void)coff; (void)dt; (void)warm;
     // 6. warm start and velocity iterations, colour by colour
+    const int ncol = w.H->last_ncolours;
+    const int ncons = w.H->last_ncons;
     for (int it = (warm ? -1 : 0); it < sp.vel_iters; ++it) {
         for (int cc = 0; cc < ncol; ++cc) {
             int s0 = coff[cc], s1 = coff[cc + 1];
@@ -858,13 +935,31 @@ template <class R, class G> __device__ void world_solve(const G &g, const WView<
         sync_transform(w, b);
     }
     g.sync();
+}
+
+// island.py:163-179 sleep, including the depth-first order where the
+// reference's result depends on it.
+template <class R, class G> __device__ void sleep_group(const G &g, const WView<R> &w, const StepParams &sp) {
+    const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
+    int *parent = w.B.s_parent + w.bb;
+    uint32_t *rootf = w.B.s_root + w.bb;
+    int *seed = w.B.s_seed + w.bb;
+    unsigned long long *minsep = w.B.s_minsep + w.bb;
+    unsigned long long *minsleep = w.B.s_minsleep + w.bb;
+    unsigned long long *claim = w.B.s_claim + w.bb;
+    int *cons_of = w.B.s_cons_of + w.cb;
+    int *colour = w.B.s_colour + w.cb;
+    int *order = w.B.s_order + w.cb;
+    int *pref = w.B.s_pref + w.cb;
+    Cons<R> *cons = w.B.s_cons + w.cb;
+    int *coff = w.B.s_proc + w.cb;
+    const double dt = sp.dt;
+    const bool warm = (w.H->flags & GB_W_WARM_STARTING) != 0;
+    (void)nb; (void)nc; (void)nf; (void)parent; (void)rootf; (void)seed; (void)minsep; (void)minsleep; (void)claim;
+    (void)cons_of; (void)colour; (void)order; (void)pref; (void)cons; (void)coff; (void)dt; (void)warm;
     // 11. sleep (island.py:163-179)
     if (w.H->flags & GB_W_ALLOW_SLEEP) {
-        bool need_dfs_all = !all_allow;
-        if (need_dfs_all) {
-            // the sleep test of every island reads the last visited body
-            if (g.rank() == 0) sh->any_dfs = 1;
-        }
+        bool need_dfs_all = !w.H->all_allow;
         for (int b = g.rank(); b < nb; b += g.size()) {
             if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
             int gb = w.bb + b;
@@ -957,6 +1052,28 @@ template <class R, class G> __device__ void world_solve(const G &g, const WView<
             g.sync();
         }
     }
+}
+
+// world.py:582-592: fixture sync of island bodies, move buffer in fixture
+// order, pair finding.
+template <class R, class G> __device__ void sync_pairs_group(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh) {
+    const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
+    int *parent = w.B.s_parent + w.bb;
+    uint32_t *rootf = w.B.s_root + w.bb;
+    int *seed = w.B.s_seed + w.bb;
+    unsigned long long *minsep = w.B.s_minsep + w.bb;
+    unsigned long long *minsleep = w.B.s_minsleep + w.bb;
+    unsigned long long *claim = w.B.s_claim + w.bb;
+    int *cons_of = w.B.s_cons_of + w.cb;
+    int *colour = w.B.s_colour + w.cb;
+    int *order = w.B.s_order + w.cb;
+    int *pref = w.B.s_pref + w.cb;
+    Cons<R> *cons = w.B.s_cons + w.cb;
+    int *coff = w.B.s_proc + w.cb;
+    const double dt = sp.dt;
+    const bool warm = (w.H->flags & GB_W_WARM_STARTING) != 0;
+    (void)nb; (void)nc; (void)nf; (void)parent; (void)rootf; (void)seed; (void)minsep; (void)minsleep; (void)claim;
+    (void)cons_of; (void)colour; (void)order; (void)pref; (void)cons; (void)coff; (void)dt; (void)warm;
     // 12. synchronise fixtures of island bodies; the move buffer is the
     //     re-fattened proxies in body order = fixture order (world.py:584-589)
     int *mv = w.B.s_move + w.fb;
@@ -975,4 +1092,23 @@ template <class R, class G> __device__ void world_solve(const G &g, const WView<
     if (g.rank() == 0) sh->nmove = nmove;
     g.sync();
     find_new_contacts(g, w, sh);
+}
+
+template <class R, class G> __device__ void world_solve(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh,
+                                                        PhaseClock &pc) {
+    islands_group(g, w, sp);
+    if (g.rank() == 0) pc.mark(2);
+    constraints_group(g, w, sp);
+    if (g.rank() == 0) pc.mark(3);
+    for (int b = g.rank(); b < w.H->nb; b += g.size()) integrate_velocity_body(w, b, sp.dt);
+    g.sync();
+    for (int k = g.rank(); k < w.H->last_ncons; k += g.size()) init_constraint(w, k, sp);
+    g.sync();
+    if (g.rank() == 0) pc.mark(4);
+    solve_group(g, w, sp);
+    if (g.rank() == 0) pc.mark(6);
+    sleep_group(g, w, sp);
+    if (g.rank() == 0) pc.mark(7);
+    sync_pairs_group(g, w, sp, sh);
+    if (g.rank() == 0) pc.mark(8);
 }

@@ -12,20 +12,30 @@
 #pragma once
 #include "gb_step.cuh"
 
-// world.py:617-686 for one contact: its cached or freshly computed TOI.
-// Returns false when the contact is skipped (sensor, inactive, no bullet).
-template <class R> __device__ bool toi_of_contact(const WView<R> &w, int i, double *alpha_out) {
-    ContactRec<R> &c = w.con(i);
-    if (c.flags & GB_C_TOI) { *alpha_out = c.toi; return true; }
-    if (fx_sensor(w, c.fa) || fx_sensor(w, c.fb)) return false;
+// world.py:617-653 for contact i at the start of a TOI pass: 0 = skipped
+// (disabled, sub-stepped too often, sensor, inactive, no bullet or
+// non-dynamic body), 1 = cached time of impact, 2 = needs a fresh one.
+template <class R> __device__ int toi_status(const WView<R> &w, int i) {
+    const ContactRec<R> &c = w.con(i);
+    if (!(c.flags & GB_C_ENABLED) || c.toi_count > GB_MAX_SUB_STEPS) return 0;
+    if (c.flags & GB_C_TOI) return 1;
+    if (fx_sensor(w, c.fa) || fx_sensor(w, c.fb)) return 0;
     int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
     int ta = w.btype(ba), tb = w.btype(bb);
     bool act_a = w.awake(ba) && ta != GB_BODY_STATIC;
     bool act_b = w.awake(bb) && tb != GB_BODY_STATIC;
-    if (!act_a && !act_b) return false;
+    if (!act_a && !act_b) return 0;
     bool col_a = (w.B.b_flags[w.bb + ba] & GB_BODY_BULLET) || ta != GB_BODY_DYNAMIC;
     bool col_b = (w.B.b_flags[w.bb + bb] & GB_BODY_BULLET) || tb != GB_BODY_DYNAMIC;
-    if (!col_a && !col_b) return false;
+    if (!col_a && !col_b) return 0;
+    return 2;
+}
+
+// world.py:656-661: put both sweeps on the same time interval, advancing
+// the lagging body's sweep in place; returns alpha0 and the two sweeps.
+template <class R> __device__ double toi_align(const WView<R> &w, int i, Sweep *sa, Sweep *sb) {
+    const ContactRec<R> &c = w.con(i);
+    int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
     double al_a = w.B.b_alpha0[w.bb + ba], al_b = w.B.b_alpha0[w.bb + bb];
     double alpha0 = al_a;
     if (al_a < al_b) {
@@ -34,18 +44,36 @@ template <class R> __device__ bool toi_of_contact(const WView<R> &w, int i, doub
     } else if (al_b < al_a) {
         Sweep s = w.sweep(bb); sweep_advance(s, alpha0); w.put_sweep(bb, s);
     }
+    *sa = w.sweep(ba);
+    *sb = w.sweep(bb);
+    return alpha0;
+}
+
+// world.py:669-681: the time of impact from the aligned sweeps (float64)
+template <class R> __device__ void toi_compute(const WView<R> &w, int i, double alpha0, const Sweep &sa, const Sweep &sb) {
+    ContactRec<R> &c = w.con(i);
     DProxy pa, pb;
     dproxy_init(pa, w.shape(c.fa));
     dproxy_init(pb, w.shape(c.fb));
-    Sweep sa = w.sweep(ba), sb = w.sweep(bb);
     double beta;
     bool lim = false;
     int state = time_of_impact(pa, pb, sa, sb, 1.0, &beta, &lim);
-    if (lim) w.H->status |= GB_ST_ITER_LIMIT;
+    if (lim) atomicOr(&w.H->status, GB_ST_ITER_LIMIT);
     double alpha = (state == TOI_TOUCHING) ? pymin(alpha0 + (1.0 - alpha0) * beta, 1.0) : 1.0;
     c.toi = alpha;
     c.flags |= GB_C_TOI;
-    *alpha_out = alpha;
+}
+
+// One contact of a TOI pass (status, alignment, computation); false when
+// the contact does not take part.
+template <class R> __device__ bool toi_of_contact(const WView<R> &w, int i) {
+    int st = toi_status(w, i);
+    if (st == 0) return false;
+    if (st == 2) {
+        Sweep sa, sb;
+        double a0 = toi_align(w, i, &sa, &sb);
+        toi_compute(w, i, a0, sa, sb);
+    }
     return true;
 }
 
@@ -123,7 +151,11 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
 
 // One TOI event (world.py:693-817) on rank 0.  Appends the re-fattened
 // proxies to the move buffer (sh->nmove).
-template <class R> __device__ void toi_event(const WView<R> &w, int mi, double min_alpha, double dt, int vel_iters, WShared *sh) {
+// la/lb: the contacts of the TOI contact's bodies A and B in list order
+// (Body._contacts).  The island bodies are left in s_stack[0..sh->nisland)
+// with their s_bvis marks set; the caller invalidates and clears them.
+template <class R> __device__ void toi_event(const WView<R> &w, int mi, double min_alpha, double dt, int vel_iters, WShared *sh,
+                                             const int *la, int na, const int *lb, int nlb) {
     ContactRec<R> &mc = w.con(mi);
     unsigned char *bflag = w.B.s_bvis + w.bb;
     int bia = w.fbody(mc.fa), bib = w.fbody(mc.fb);
@@ -133,6 +165,7 @@ template <class R> __device__ void toi_event(const WView<R> &w, int mi, double m
     contact_update(w, mi);
     mc.flags &= ~GB_C_TOI;
     mc.toi_count += 1;
+    sh->nisland = 0;
     if (!(mc.flags & GB_C_ENABLED) || !(mc.flags & GB_C_TOUCHING)) {
         mc.flags &= ~GB_C_ENABLED;
         w.put_sweep(bia, back_a); w.put_sweep(bib, back_b);
@@ -149,14 +182,15 @@ template <class R> __device__ void toi_event(const WView<R> &w, int mi, double m
     int dyn[2], nd = 0;
     if (w.btype(bia) == GB_BODY_DYNAMIC) dyn[nd++] = bia;
     if (w.btype(bib) == GB_BODY_DYNAMIC) dyn[nd++] = bib;
-    const int nc = w.H->nc;
     for (int di = 0; di < nd; ++di) {
         int bi = dyn[di];
         bool bullet = (w.B.b_flags[w.bb + bi] & GB_BODY_BULLET) != 0;
-        for (int ci = 0; ci < nc; ++ci) {   // Body._contacts in contact-list order
+        const int *lst = (bi == bia) ? la : lb;
+        const int nl = (bi == bia) ? na : nlb;
+        for (int li = 0; li < nl; ++li) {   // Body._contacts in contact-list order
+            int ci = lst[li];
             ContactRec<R> &c = w.con(ci);
             int fa = w.fbody(c.fa), fbb = w.fbody(c.fb);
-            if (fa != bi && fbb != bi) continue;
             if (nbi == 2 * GB_MAX_TOI_CONTACTS || nci == GB_MAX_TOI_CONTACTS) { w.H->status |= GB_ST_TOI_ISLAND_CAP; break; }
             if (c.flags & GB_C_ISLAND) continue;
             int oi = (fa == bi) ? fbb : fa;
@@ -192,48 +226,67 @@ template <class R> __device__ void toi_event(const WView<R> &w, int mi, double m
                 }
         }
     }
-    // invalidate the TOIs of every contact of a displaced dynamic body
-    for (int ci = 0; ci < nc; ++ci) {
-        ContactRec<R> &c = w.con(ci);
-        int fa = w.fbody(c.fa), fbb = w.fbody(c.fb);
-        bool hit = (bflag[fa] && w.btype(fa) == GB_BODY_DYNAMIC) || (bflag[fbb] && w.btype(fbb) == GB_BODY_DYNAMIC);
-        if (hit) c.flags &= ~(GB_C_TOI | GB_C_ISLAND);
-    }
-    for (int i = 0; i < nbi; ++i) bflag[ib[i]] = 0;
+    int *isl = w.B.s_stack + w.bb;
+    for (int i = 0; i < nbi; ++i) isl[i] = ib[i];
+    sh->nisland = nbi;
 }
 
-template <class R, class G> __device__ void world_solve_toi(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh) {
-    const int nb = w.H->nb;
+// world.py:599-609 reset of the TOI state of one contact
+template <class R> __device__ __forceinline__ void toi_reset_contact(const WView<R> &w, int i) {
+    ContactRec<R> &c = w.con(i);
+    c.flags &= ~(GB_C_TOI | GB_C_ISLAND);
+    c.toi_count = 0;
+    c.toi = 1.0;
+}
+
+// First pass of the TOI loop for contact i (every sweep at alpha0 = 0, so
+// contacts are independent): proc = whether the contact takes part.
+template <class R> __device__ __forceinline__ void toi_first_pass_contact(const WView<R> &w, int i, int *proc) {
+    proc[i] = toi_of_contact(w, i) ? 1 : 0;
+}
+
+// The event loop of world.py:612-821; `first_done` means pass 0 already ran
+// (in the batch-wide kernel).
+template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh,
+                                                     bool par_first, bool first_done) {
     int *proc = w.B.s_proc + w.cb;
-    // every sweep starts at alpha0 = 0 after a complete step, so the first
-    // pass advances no sweep and may run in parallel
-    const bool par_first = (w.H->flags & GB_W_STEP_COMPLETE) != 0;
-    if (w.H->flags & GB_W_STEP_COMPLETE) {
-        for (int b = g.rank(); b < nb; b += g.size()) { w.B.b_alpha0[w.bb + b] = 0.0; w.B.s_bvis[w.bb + b] = 0; }
-        for (int i = g.rank(); i < w.H->nc; i += g.size()) {
-            ContactRec<R> &c = w.con(i);
-            c.flags &= ~(GB_C_TOI | GB_C_ISLAND);
-            c.toi_count = 0;
-            c.toi = 1.0;
-        }
-    }
-    g.sync();
+    int *ids = w.B.s_pref + w.cb;
     unsigned long long *red = &sh->red;
+    TPlan *plan = w.B.s_plan + (size_t)w.wi * GB_TOI_PLAN_CAP;
+    unsigned char *bflag = w.B.s_bvis + w.bb;
     for (int pass = 0; pass < (1 << 20); ++pass) {
         const int nc = w.H->nc;
-        if (pass == 0 && par_first) {
-            for (int i = g.rank(); i < nc; i += g.size()) {
-                const ContactRec<R> &c = w.con(i);
-                double a;
-                bool ok = (c.flags & GB_C_ENABLED) && c.toi_count <= GB_MAX_SUB_STEPS && toi_of_contact(w, i, &a);
-                proc[i] = ok ? 1 : 0;
-            }
-        } else if (g.rank() == 0) {
-            for (int i = 0; i < nc; ++i) {
-                const ContactRec<R> &c = w.con(i);
-                double a;
-                bool ok = (c.flags & GB_C_ENABLED) && c.toi_count <= GB_MAX_SUB_STEPS && toi_of_contact(w, i, &a);
-                proc[i] = ok ? 1 : 0;
+        if (pass == 0 && first_done) {
+            // computed by the batch-wide first pass
+        } else if (pass == 0 && par_first) {
+            for (int i = g.rank(); i < nc; i += g.size()) proc[i] = toi_of_contact(w, i) ? 1 : 0;
+        } else {
+            // statuses in parallel; the contacts needing a fresh TOI in list order
+            int nfresh = group_scan(g, nc, [&](int i) {
+                int st = toi_status(w, i);
+                proc[i] = st != 0 ? 1 : 0;
+                return st == 2 ? 1 : 0;
+            }, ids);
+            g.sync();
+            if (nfresh > 0) {
+                int *fresh = w.B.s_adj + 2 * (size_t)w.cb;   // free during the TOI loop
+                for (int i = g.rank(); i < nc; i += g.size())
+                    if (proc[i] && !(w.con(i).flags & GB_C_TOI)) fresh[ids[i]] = i;
+                g.sync();
+                if (nfresh <= GB_TOI_PLAN_CAP) {
+                    // the sweep alignment is order dependent and cheap: rank 0 replays
+                    // it in list order; the float64 TOIs then run in parallel
+                    if (g.rank() == 0)
+                        for (int k = 0; k < nfresh; ++k) plan[k].alpha0 = toi_align(w, fresh[k], &plan[k].sa, &plan[k].sb);
+                    g.sync();
+                    for (int k = g.rank(); k < nfresh; k += g.size()) toi_compute(w, fresh[k], plan[k].alpha0, plan[k].sa, plan[k].sb);
+                } else if (g.rank() == 0) {
+                    for (int k = 0; k < nfresh; ++k) {
+                        Sweep sa, sb;
+                        double a0 = toi_align(w, fresh[k], &sa, &sb);
+                        toi_compute(w, fresh[k], a0, sa, sb);
+                    }
+                }
             }
         }
         if (g.rank() == 0) { red[0] = dkey(1.0); sh->min_contact = GB_INF_IDX; }
@@ -251,16 +304,70 @@ template <class R, class G> __device__ void world_solve_toi(const G &g, const WV
             g.sync();
             break;
         }
+        // contact lists of the event's two bodies (Body._contacts), in parallel
+        const ContactRec<R> &mc = w.con(mi);
+        const int bia = w.fbody(mc.fa), bib = w.fbody(mc.fb);
+        int *la = w.B.s_adj + 2 * (size_t)w.cb;
+        int *lb = la + w.H->ccap;
+        int *pa_ = ids;
+        int na = group_scan(g, nc, [&](int i) {
+            const ContactRec<R> &c = w.con(i);
+            return (w.fbody(c.fa) == bia || w.fbody(c.fb) == bia) ? 1 : 0;
+        }, pa_);
+        g.sync();
+        for (int i = g.rank(); i < nc; i += g.size()) {
+            const ContactRec<R> &c = w.con(i);
+            if (w.fbody(c.fa) == bia || w.fbody(c.fb) == bia) la[pa_[i]] = i;
+        }
+        g.sync();
+        int nlb = group_scan(g, nc, [&](int i) {
+            const ContactRec<R> &c = w.con(i);
+            return (w.fbody(c.fa) == bib || w.fbody(c.fb) == bib) ? 1 : 0;
+        }, pa_);
+        g.sync();
+        for (int i = g.rank(); i < nc; i += g.size()) {
+            const ContactRec<R> &c = w.con(i);
+            if (w.fbody(c.fa) == bib || w.fbody(c.fb) == bib) lb[pa_[i]] = i;
+        }
+        g.sync();
         if (g.rank() == 0) {
             sh->nmove = 0;
-            toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh);
+            toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh, la, na, lb, nlb);
         }
+        g.sync();
+        // invalidate the TOIs of every contact of a displaced dynamic body and
+        // clear the island marks (world.py:804-813)
+        const int nisl = sh->nisland;
+        for (int i = g.rank(); i < nc; i += g.size()) {
+            ContactRec<R> &c = w.con(i);
+            int fa = w.fbody(c.fa), fbb = w.fbody(c.fb);
+            bool hit = (bflag[fa] && w.btype(fa) == GB_BODY_DYNAMIC) || (bflag[fbb] && w.btype(fbb) == GB_BODY_DYNAMIC);
+            if (hit) c.flags &= ~(GB_C_TOI | GB_C_ISLAND);
+        }
+        g.sync();
+        for (int k = g.rank(); k < nisl; k += g.size()) bflag[w.B.s_stack[w.bb + k]] = 0;
         g.sync();
         find_new_contacts(g, w, sh);
     }
 }
 
+template <class R, class G> __device__ void world_solve_toi(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh) {
+    const int nb = w.H->nb;
+    // every sweep starts at alpha0 = 0 after a complete step, so the first
+    // pass advances no sweep and may run in parallel
+    const bool par_first = (w.H->flags & GB_W_STEP_COMPLETE) != 0;
+    if (w.H->flags & GB_W_STEP_COMPLETE) {
+        for (int b = g.rank(); b < nb; b += g.size()) { w.B.b_alpha0[w.bb + b] = 0.0; w.B.s_bvis[w.bb + b] = 0; }
+        for (int i = g.rank(); i < w.H->nc; i += g.size()) toi_reset_contact(w, i);
+    }
+    g.sync();
+    toi_loop(g, w, sp, sh, par_first, false);
+}
+
 template <class R, class G> __device__ void world_step(const G &g, const WView<R> &w, StepParams sp, WShared *sh) {
+    PhaseClock pc;
+    pc.acc = (sp.profile && g.rank() == 0) ? w.B.prof + (size_t)w.wi * GB_NPROF : nullptr;
+    pc.start();
     if (w.H->flags & GB_W_NEW_FIXTURE) {
         int nf = w.H->nf;
         int n0 = w.H->nmove0;
@@ -274,10 +381,13 @@ template <class R, class G> __device__ void world_step(const G &g, const WView<R
         g.sync();
     }
     sp.dt_ratio = w.H->inv_dt0 * sp.dt;
+    pc.mark(0);
     collide(g, w);
-    if ((w.H->flags & GB_W_STEP_COMPLETE) && sp.dt > 0.0) world_solve(g, w, sp, sh);
+    pc.mark(1);
+    if ((w.H->flags & GB_W_STEP_COMPLETE) && sp.dt > 0.0) world_solve(g, w, sp, sh, pc);
     if ((w.H->flags & GB_W_CONTINUOUS) && sp.dt > 0.0) world_solve_toi(g, w, sp, sh);
     g.sync();
+    pc.mark(9);
     if (g.rank() == 0 && sp.dt > 0.0) w.H->inv_dt0 = sp.inv_dt;
     if (w.H->flags & GB_W_AUTO_CLEAR_FORCES)
         for (int b = g.rank(); b < w.H->nb; b += g.size()) {
@@ -285,6 +395,7 @@ template <class R, class G> __device__ void world_step(const G &g, const WView<R
             w.B.b_torque[w.bb + b] = (R)0;
         }
     g.sync();
+    pc.mark(10);
 }
 
 // ---------------------------------------------------------------- kernels

@@ -51,12 +51,16 @@ struct WorldHdr {              // per-world scalars (device)
     double gx, gy, inv_dt0;
     int last_ncons, last_ncolours;
     int nmove0;                // pending move buffer given at creation (in s_move)
+    int all_allow;             // every body allows sleep (island.py:168 reads one body's flag)
+    uint32_t pflags;           // phase flags of the current step (P_*)
     int _pad;
 };
 
 template <class R> struct Batch {
-    int n_worlds;
+    int n_worlds, n_bodies, n_slots;
     WorldHdr *hdr;
+    int *b_world;             // world of each body
+    int *c_world;             // world of each contact slot
     // bodies
     int *b_type; uint32_t *b_flags; int *b_fstart; int *b_fcount;
     vec2<double> *b_xp; rot2<double> *b_xq;
@@ -85,12 +89,29 @@ template <class R> struct Batch {
     Cons<R> *s_cons;
     unsigned long long *s_hash;  // 4 * ccap slots per world (a power of two >= 2*ccap fits)
     int *order_out;              // recorded solver order (contact positions), ccap per world
+    long long *prof;             // per-world phase clocks (GB_NPROF per world), when profiling
+    struct TPlan *s_plan;        // GB_TOI_PLAN_CAP planned TOI sweeps per world
 };
+#define GB_NPROF 16
+#define GB_TOI_PLAN_CAP 64
+// A TOI computation prepared by the order-dependent sweep alignment.
+struct TPlan { double alpha0; Sweep sa, sb; };
 
 struct StepParams {
     double dt, inv_dt, dt_ratio;
     int vel_iters, pos_iters;
     int record_order;
+    int profile;
+};
+
+// Phase clocks: rank 0 adds the SM clock delta since the last mark.
+struct PhaseClock {
+    long long *acc;
+    long long t;
+    __device__ __forceinline__ void start() { if (acc) t = clock64(); }
+    __device__ __forceinline__ void mark(int k) {
+        if (acc) { long long n = clock64(); acc[k] += n - t; t = n; }
+    }
 };
 
 // ---------------------------------------------------------------- groups

@@ -39,8 +39,10 @@ class GpuBatch:
             pass
 
     def step(self, dt: float, vel_iters: int = 8, pos_iters: int = 3, n_steps: int = 1, launch_mode: int = 1,
-             block_threads: int = 0, record_order: bool = False, stream: int | None = None) -> None:
-        o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, 1 if record_order else 0)
+             block_threads: int = 0, record_order: bool = False, stream: int | None = None,
+             profile: bool = False) -> None:
+        flags = (1 if record_order else 0) | (2 if profile else 0)
+        o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, flags)
         abi.check(self.lib.gb_batch_step(self.h, ctypes.byref(o), ctypes.c_void_p(stream or 0)))
 
     def bodies(self, stream: int | None = None) -> np.ndarray:
@@ -76,6 +78,12 @@ class GpuBatch:
         abi.check(self.lib.gb_batch_get_solver_order(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                                                      cap, ctypes.byref(n), None))
         return out[:n.value].copy()
+
+    def phase_clocks(self) -> np.ndarray:
+        """Accumulated SM clocks per step phase and world (n_worlds x 16)."""
+        out = np.zeros((self.n_worlds, 16), dtype=np.int64)
+        abi.check(self.lib.gb_batch_phase_clocks(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), None))
+        return out
 
     def arena_bytes(self) -> int:
         c = (ctypes.c_int64 * 3)()

@@ -68,9 +68,10 @@ def run_lockstep(scene, steps, launch_mode=1, block_threads=0):
     return gpu, orc
 
 
+@pytest.mark.parametrize("mode", [1, 3], ids=["monolithic", "phased"])
 @pytest.mark.parametrize("scene", sorted(STEPS))
-def test_f64_bit_exact_with_oracle(scene):
-    run_lockstep(scene, STEPS[scene])
+def test_f64_bit_exact_with_oracle(scene, mode):
+    run_lockstep(scene, STEPS[scene], launch_mode=mode)
 
 
 def test_warp_mapping_matches_cta_mapping():
@@ -79,7 +80,7 @@ def test_warp_mapping_matches_cta_mapping():
     d = np.load(os.path.join(GOLDEN, "mixed.npz"))
     W, B, F = d["init_world"], d["init_bodies"], d["init_fixtures"]
     out = []
-    for mode, threads in ((1, 128), (1, 256), (2, 64)):
+    for mode, threads in ((1, 128), (1, 256), (2, 64), (3, 128), (3, 64)):
         g = GpuBatch(W, B, F, precision="f64")
         g.step(1 / 60, 8, 3, 50, launch_mode=mode, block_threads=threads)
         out.append(g.bodies())
