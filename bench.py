@@ -187,14 +187,14 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--worlds", type=int, default=4096)
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--mode", type=int, default=3, help="1 = one CTA per world (monolithic), 2 = one warp per world, "
                                                         "3 = phase kernels over the whole batch")
-    ap.add_argument("--threads", type=int, default=128)
+    ap.add_argument("--threads", type=int, default=64)
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-extras", action="store_true", help="skip cpu baseline, plain path and error legs")
     args = ap.parse_args()

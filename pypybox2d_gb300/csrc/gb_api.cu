@@ -80,6 +80,8 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.order_out = a.take<int>(ncap);
     B.prof = a.take<long long>((size_t)nw * GB_NPROF);
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
+    B.toi_list = a.take<int>(ncap);
+    B.toi_n = a.take<int>(1);
 }
 }  // namespace
 

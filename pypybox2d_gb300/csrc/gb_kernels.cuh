@@ -114,7 +114,8 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
             k_world<GB_REAL, PH_SOLVE><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
             k_world<GB_REAL, PH_PAIRS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
             if (ns) k_toi1<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
-            k_world<GB_REAL, PH_TOI2><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            if (ns) k_toi1b<GB_REAL><<<152 * 4, 128, 0, st>>>(B);
+            k_world_toi2<GB_REAL><<<n_list, 32, 0, st>>>(B, sp, d_worlds);
         }
         return (int)cudaGetLastError();
     }

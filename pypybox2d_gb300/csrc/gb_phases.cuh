@@ -38,6 +38,7 @@ template <class R> __device__ __forceinline__ WView<R> view_global(const Batch<R
 
 template <class R> __global__ void k_pre(Batch<R> B, int n_bodies, StepParams sp) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b == 0) *B.toi_n = 0;
     if (b >= n_bodies) return;
     const WorldHdr *H = &B.hdr[B.b_world[b]];
     uint32_t f = B.b_flags[b];
@@ -84,6 +85,9 @@ template <class R> __global__ void k_cinit(Batch<R> B, int n_slots, StepParams s
     init_constraint(w, k, sp);
 }
 
+// First TOI pass, part 1: reset every contact's TOI state (world.py:604-609)
+// and list the contacts that need a time of impact.  All sweeps start at
+// alpha0 = 0, so the listed computations are independent of each other.
 template <class R> __global__ void k_toi1(Batch<R> B, int n_slots, StepParams sp) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n_slots) return;
@@ -93,7 +97,23 @@ template <class R> __global__ void k_toi1(Batch<R> B, int n_slots, StepParams sp
     if (!((w.H->flags & GB_W_CONTINUOUS) && sp.dt > 0.0)) return;
     if (!(w.H->flags & GB_W_STEP_COMPLETE)) return;   // k_toi2 then runs the whole loop in order
     toi_reset_contact(w, i);
-    toi_first_pass_contact(w, i, B.s_proc + w.cb);
+    int st = toi_status(w, i);
+    B.s_proc[s] = st != 0 ? 1 : 0;
+    if (st == 2) B.toi_list[atomicAdd(B.toi_n, 1)] = s;
+}
+
+// First TOI pass, part 2: the float64 times of impact of the listed
+// contacts, one per thread (dense warps; the list order does not matter).
+template <class R> __global__ void k_toi1b(Batch<R> B) {
+    const int n = *B.toi_n;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        int s = B.toi_list[t];
+        WView<R> w = view_global(B, B.c_world[s]);
+        int i = s - w.cb;
+        const ContactRec<R> &c = w.con(i);
+        int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+        toi_compute(w, i, 0.0, w.sweep(ba), w.sweep(bb));
+    }
 }
 
 // Per-world phases ---------------------------------------------------------
@@ -104,11 +124,22 @@ template <class R> __global__ void k_toi1(Batch<R> B, int n_slots, StepParams sp
 #define PH_PAIRS 4
 #define PH_TOI2 5
 
+template <class R, int PH> __device__ __forceinline__ void world_phase(const Batch<R> &B, const StepParams &sp, const int wi);
+
 template <class R, int PH> __global__ void __launch_bounds__(256) k_world(Batch<R> B, StepParams sp, const int *worlds) {
+    world_phase<R, PH>(B, sp, worlds[blockIdx.x]);
+}
+
+// The TOI event loop is latency bound (float64, mostly one thread): one warp
+// per world with a register cap keeps many worlds in flight per SM.
+template <class R> __global__ void __launch_bounds__(32, 24) k_world_toi2(Batch<R> B, StepParams sp, const int *worlds) {
+    world_phase<R, PH_TOI2>(B, sp, worlds[blockIdx.x]);
+}
+
+template <class R, int PH> __device__ __forceinline__ void world_phase(const Batch<R> &B, const StepParams &sp, const int wi) {
     __shared__ int sm[96];
     __shared__ WorldHdr H;
     __shared__ WShared sh;
-    const int wi = worlds[blockIdx.x];
     if (threadIdx.x == 0) { H = B.hdr[wi]; sh.nmove = 0; }
     __syncthreads();
     GroupCta g{sm};
@@ -178,7 +209,10 @@ template <class R, int PH> __global__ void __launch_bounds__(256) k_world(Batch<
             if (par_first)   // island flags of the bodies (world.py:600-601)
                 for (int b = g.rank(); b < H.nb; b += g.size()) B.s_bvis[w.bb + b] = 0;
             g.sync();
-            toi_loop(g, w, sp, &sh, par_first, par_first);
+            PhaseClock pc;
+            pc.acc = (sp.profile && g.rank() == 0) ? B.prof + (size_t)wi * GB_NPROF : nullptr;
+            pc.start();
+            toi_loop(g, w, sp, &sh, par_first, par_first, &pc);
         }
         g.sync();
         if (g.rank() == 0 && sp.dt > 0.0) H.inv_dt0 = sp.inv_dt;

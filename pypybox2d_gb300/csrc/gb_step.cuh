@@ -209,16 +209,26 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
     int *mv = w.B.s_move + w.fb;
     int *cnt = w.B.s_cnt + w.fb;
     unsigned long long *hash = w.B.s_hash + 4 * (size_t)w.cb;
-    int hcap = 1;
-    while (hcap < 2 * w.H->ccap) hcap <<= 1;
-    int hmask = hcap - 1;
     if (nmove == 0) return;
     for (int f = g.rank(); f < nf; f += g.size()) first[f] = GB_INF_IDX;
-    for (int k = g.rank(); k < hcap; k += g.size()) hash[k] = 0ull;
     g.sync();
     for (int i = g.rank(); i < nmove; i += g.size()) atomicMin(&first[mv[i]], i);
+    g.sync();
     int nc = w.H->nc;
+    // only contacts of moved proxies can match a candidate pair: size the
+    // existence hash for those (after a TOI event a handful, not the world)
+    auto involved = [&](int i) {
+        const ContactRec<R> &c = w.con(i);
+        return (first[c.fa] != GB_INF_IDX || first[c.fb] != GB_INF_IDX) ? 1 : 0;
+    };
+    int m = group_count(g, nc, involved);
+    int hcap = 16;
+    while (hcap < 2 * m) hcap <<= 1;
+    int hmask = hcap - 1;
+    for (int k = g.rank(); k < hcap; k += g.size()) hash[k] = 0ull;
+    g.sync();
     for (int i = g.rank(); i < nc; i += g.size()) {
+        if (!involved(i)) continue;
         const ContactRec<R> &c = w.con(i);
         unsigned long long key = ((unsigned long long)(unsigned)min(c.fa, c.fb) << 32) | (unsigned)max(c.fa, c.fb);
         key += 1ull;

@@ -248,7 +248,10 @@ template <class R> __device__ __forceinline__ void toi_first_pass_contact(const 
 // The event loop of world.py:612-821; `first_done` means pass 0 already ran
 // (in the batch-wide kernel).
 template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh,
-                                                     bool par_first, bool first_done) {
+                                                     bool par_first, bool first_done, PhaseClock *pc = nullptr) {
+    PhaseClock dummy;
+    dummy.acc = nullptr;
+    PhaseClock &ck = pc ? *pc : dummy;
     int *proc = w.B.s_proc + w.cb;
     int *ids = w.B.s_pref + w.cb;
     unsigned long long *red = &sh->red;
@@ -289,7 +292,8 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
                 }
             }
         }
-        if (g.rank() == 0) { red[0] = dkey(1.0); sh->min_contact = GB_INF_IDX; }
+        g.sync();
+        if (g.rank() == 0) { ck.mark(11); red[0] = dkey(1.0); sh->min_contact = GB_INF_IDX; }
         g.sync();
         for (int i = g.rank(); i < nc; i += g.size())
             if (proc[i] && w.con(i).toi < 1.0) atomicMin(&red[0], dkey(w.con(i).toi));
@@ -331,8 +335,10 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
         }
         g.sync();
         if (g.rank() == 0) {
+            ck.mark(12);
             sh->nmove = 0;
             toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh, la, na, lb, nlb);
+            ck.mark(13);
         }
         g.sync();
         // invalidate the TOIs of every contact of a displaced dynamic body and
@@ -348,6 +354,7 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
         for (int k = g.rank(); k < nisl; k += g.size()) bflag[w.B.s_stack[w.bb + k]] = 0;
         g.sync();
         find_new_contacts(g, w, sh);
+        if (g.rank() == 0) { ck.mark(14); if (ck.acc) ck.acc[15] += 1; }
     }
 }
 

@@ -91,6 +91,8 @@ template <class R> struct Batch {
     int *order_out;              // recorded solver order (contact positions), ccap per world
     long long *prof;             // per-world phase clocks (GB_NPROF per world), when profiling
     struct TPlan *s_plan;        // GB_TOI_PLAN_CAP planned TOI sweeps per world
+    int *toi_list;               // contact slots needing a first-pass TOI (batch-wide)
+    int *toi_n;                  // their count
 };
 #define GB_NPROF 16
 #define GB_TOI_PLAN_CAP 64
@@ -165,6 +167,15 @@ struct GroupWarp {
         return x - v;
     }
 };
+
+// Number of i < n with pred(i) over the group (contains barriers).
+template <class G, class F> __device__ int group_count(const G &g, int n, F pred) {
+    int local = 0;
+    for (int i = g.rank(); i < n; i += g.size()) local += pred(i);
+    int tot;
+    g.exscan(local, &tot);
+    return tot;
+}
 
 // Chunked exclusive scan of flag(i) for i < n into out[i]; returns the total.
 template <class G, class F> __device__ int group_scan(const G &g, int n, F flag, int *out) {
