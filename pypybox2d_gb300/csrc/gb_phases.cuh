@@ -198,8 +198,12 @@ template <class R, int PH> __device__ __forceinline__ void world_phase(const Bat
         }
     } else if (PH == PH_SOLVE) {
         if (H.pflags & P_SOLVING) {
-            solve_group(g, w, sp);
+            PhaseClock pc;
+            pc.acc = (sp.profile && g.rank() == 0) ? B.prof + (size_t)wi * GB_NPROF : nullptr;
+            pc.start();
+            solve_group(g, w, sp, &pc);
             sleep_group(g, w, sp);
+            if (g.rank() == 0) pc.mark(7);
         }
     } else if (PH == PH_PAIRS) {
         if (H.pflags & P_SOLVING) sync_pairs_group(g, w, sp, &sh);

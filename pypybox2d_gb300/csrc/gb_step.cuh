@@ -700,23 +700,18 @@ template <class R, class G> __device__ void islands_group(const G &g, const WVie
 // Constraint list of the simulated islands in contact-list order, graph
 // colouring and the colour-major solver order.
 template <class R, class G> __device__ void constraints_group(const G &g, const WView<R> &w, const StepParams &sp) {
-    const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
-    int *parent = w.B.s_parent + w.bb;
-    uint32_t *rootf = w.B.s_root + w.bb;
-    int *seed = w.B.s_seed + w.bb;
-    unsigned long long *minsep = w.B.s_minsep + w.bb;
-    unsigned long long *minsleep = w.B.s_minsleep + w.bb;
+    const int nb = w.H->nb, nc = w.H->nc;
+    const int *parent = w.B.s_parent + w.bb;
+    const uint32_t *rootf = w.B.s_root + w.bb;
     unsigned long long *claim = w.B.s_claim + w.bb;
-    int *cons_of = w.B.s_cons_of + w.cb;
     int *colour = w.B.s_colour + w.cb;
-    int *order = w.B.s_order + w.cb;
     int *pref = w.B.s_pref + w.cb;
     Cons<R> *cons = w.B.s_cons + w.cb;
     int *coff = w.B.s_proc + w.cb;
-    const double dt = sp.dt;
-    const bool warm = (w.H->flags & GB_W_WARM_STARTING) != 0;
-    (void)nb; (void)nc; (void)nf; (void)parent; (void)rootf; (void)seed; (void)minsep; (void)minsleep; (void)claim;
-    (void)cons_of; (void)colour; (void)order; (void)pref; (void)cons; (void)coff; (void)dt; (void)warm;
+    int *kc = w.B.s_cons_of + w.cb;                 // contact of constraint k
+    int2 *kb = w.B.s_kb + w.cb;                     // its non-static bodies (-1: static)
+    int *kroot = w.B.s_adj + 2 * (size_t)w.cb;      // its island
+    (void)sp;
     // 2. island membership: wake the members of simulated islands (DFS sets
     //    body.awake = True, world.py:520), constraints = qualifying contacts
     //    of simulated islands in contact-list order.
@@ -732,18 +727,18 @@ template <class R, class G> __device__ void constraints_group(const G &g, const 
     g.sync();
     for (int i = g.rank(); i < nc; i += g.size()) {
         const ContactRec<R> &c = w.con(i);
-        cons_of[i] = -1;
         if (!qualifies(w, c)) continue;
         int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
-        int dyn = (w.btype(ba) != GB_BODY_STATIC) ? ba : bb;
-        int stat = (dyn == ba) ? bb : ba;
+        bool sa = w.btype(ba) == GB_BODY_STATIC, sb = w.btype(bb) == GB_BODY_STATIC;
+        int dyn = sa ? bb : ba;
         if (!(rootf[parent[dyn]] & R_SIM)) continue;
         int k = pref[i];
-        cons_of[i] = k;
-        cons[k].cidx = i;
-        cons[k].root = parent[dyn];
+        kc[k] = i;
+        kroot[k] = parent[dyn];
+        kb[k] = make_int2(sa ? -1 : ba, sb ? -1 : bb);
         colour[k] = -1;
-        if (w.btype(stat) == GB_BODY_STATIC) wake_body(w, stat);
+        if (sa) wake_body(w, ba);
+        if (sb) wake_body(w, bb);
     }
     g.sync();
     // 3. graph colouring: Jones-Plassmann rounds with fixed hash priorities;
@@ -758,55 +753,57 @@ template <class R, class G> __device__ void constraints_group(const G &g, const 
         for (int k = g.rank(); k < ncons; k += g.size()) {
             if (colour[k] >= 0) continue;
             left = true;
-            const ContactRec<R> &c = w.con(cons[k].cidx);
-            int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+            int2 q = kb[k];
             unsigned h = (unsigned)k * 2654435761u;
             h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
             unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
-            if (w.btype(ba) != GB_BODY_STATIC) atomicMax(&claim[ba], key);
-            if (w.btype(bb) != GB_BODY_STATIC) atomicMax(&claim[bb], key);
+            if (q.x >= 0) atomicMax(&claim[q.x], key);
+            if (q.y >= 0) atomicMax(&claim[q.y], key);
         }
         if (!g.any(left)) break;
         for (int k = g.rank(); k < ncons; k += g.size()) {
             if (colour[k] >= 0) continue;
-            const ContactRec<R> &c = w.con(cons[k].cidx);
-            int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+            int2 q = kb[k];
             unsigned h = (unsigned)k * 2654435761u;
             h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
             unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
-            bool win = (w.btype(ba) == GB_BODY_STATIC || claim[ba] == key) && (w.btype(bb) == GB_BODY_STATIC || claim[bb] == key);
+            bool win = (q.x < 0 || claim[q.x] == key) && (q.y < 0 || claim[q.y] == key);
             if (win) colour[k] = round;
         }
         ncol = round + 1;
         g.sync();
     }
     g.sync();
-    // order = constraints sorted by (colour, index); colour offsets live in
-    // the collide scratch (free during the solve); ncol < ccap always holds
-    // because every colour holds at least one constraint and ncons <= nc.
+    // The constraints are stored colour-major: constraint slots [coff[c],
+    // coff[c+1]) hold colour c.  Positions inside a colour come from atomics:
+    // a colour's constraints share no non-static body, so their order there
+    // changes no result.  coff lives in the collide scratch (free during the
+    // solve); ncol < ccap because every colour holds a constraint.
     if (ncol + 1 > w.H->ccap) {   // cannot happen while ncons < ccap; never index past the world's slots
         if (g.rank() == 0) w.H->status |= GB_ST_ITER_LIMIT;
         ncol = w.H->ccap - 1;
     }
-    {
-        // counting sort, one scan per colour (colours are few)
-        int start = 0;
-        for (int cc = 0; cc < ncol; ++cc) {
-            int n = group_scan(g, ncons, [&](int k) { return colour[k] == cc ? 1 : 0; }, pref);
-            g.sync();
-            for (int k = g.rank(); k < ncons; k += g.size())
-                if (colour[k] == cc) order[start + pref[k]] = k;
-            if (g.rank() == 0) coff[cc] = start;
-            start += n;
-            g.sync();
-        }
-        if (g.rank() == 0) coff[ncol] = start;
+    for (int cc = g.rank(); cc <= ncol; cc += g.size()) coff[cc] = 0;
+    g.sync();
+    for (int k = g.rank(); k < ncons; k += g.size())
+        if (colour[k] >= 0 && colour[k] < ncol) atomicAdd(&coff[colour[k] + 1], 1);
+    g.sync();
+    if (g.rank() == 0)
+        for (int cc = 1; cc <= ncol; ++cc) coff[cc] += coff[cc - 1];
+    g.sync();
+    for (int cc = g.rank(); cc < ncol; cc += g.size()) pref[cc] = coff[cc];
+    g.sync();
+    for (int k = g.rank(); k < ncons; k += g.size()) {
+        if (colour[k] < 0 || colour[k] >= ncol) continue;
+        int pos = atomicAdd(&pref[colour[k]], 1);
+        cons[pos].cidx = kc[k];
+        cons[pos].root = kroot[k];
     }
-    if (g.rank() == 0) { w.H->last_ncons = ncons; w.H->last_ncolours = ncol; }
+    if (g.rank() == 0) { w.H->last_ncons = coff[ncol]; w.H->last_ncolours = ncol; }
     g.sync();
     if (sp.record_order) {
         int *out = w.B.order_out + w.cb;
-        for (int k = g.rank(); k < ncons; k += g.size()) out[k] = cons[order[k]].cidx;
+        for (int k = g.rank(); k < w.H->last_ncons; k += g.size()) out[k] = cons[k].cidx;
     }
 }
 
@@ -844,7 +841,10 @@ template <class R> __device__ __forceinline__ void init_constraint(const WView<R
 
 // Warm start, velocity iterations, impulse store, position integration,
 // position iterations and transform write-back (island.py:98-159).
-template <class R, class G> __device__ void solve_group(const G &g, const WView<R> &w, const StepParams &sp) {
+template <class R, class G> __device__ void solve_group(const G &g, const WView<R> &w, const StepParams &sp, PhaseClock *pcp = nullptr) {
+    PhaseClock dummy;
+    dummy.acc = nullptr;
+    PhaseClock &ck = pcp ? *pcp : dummy;
     const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
     int *parent = w.B.s_parent + w.bb;
     uint32_t *rootf = w.B.s_root + w.bb;
@@ -869,12 +869,16 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         for (int cc = 0; cc < ncol; ++cc) {
             int s0 = coff[cc], s1 = coff[cc + 1];
             for (int j = s0 + g.rank(); j < s1; j += g.size()) {
-                Cons<R> &q = cons[order[j]];
+                Cons<R> q = cons[j];   // by value: independent loads, no aliasing reloads
                 int ga = w.bb + q.ia, gbb = w.bb + q.ib;
                 vec2<R> va = w.B.b_v[ga], vb = w.B.b_v[gbb];
                 R wa = w.B.b_w[ga], wb = w.B.b_w[gbb];
                 if (it < 0) warm_start(q, va, wa, vb, wb);
-                else solve_velocity(q, va, wa, vb, wb);
+                else {
+                    solve_velocity(q, va, wa, vb, wb);
+                    cons[j].ni[0] = q.ni[0]; cons[j].ni[1] = q.ni[1];
+                    cons[j].ti[0] = q.ti[0]; cons[j].ti[1] = q.ti[1];
+                }
                 // colour classes share no non-static body; static bodies keep v = 0
                 if (w.btype(q.ia) != GB_BODY_STATIC) { w.B.b_v[ga] = va; w.B.b_w[ga] = wa; }
                 if (w.btype(q.ib) != GB_BODY_STATIC) { w.B.b_v[gbb] = vb; w.B.b_w[gbb] = wb; }
@@ -882,6 +886,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             g.sync();
         }
     }
+    if (g.rank() == 0) { ck.mark(4); if (ck.acc) ck.acc[10] += ncol; }
     // 7. store impulses (contact.py:801-806)
     for (int k = g.rank(); k < ncons; k += g.size()) {
         const Cons<R> &q = cons[k];
@@ -910,6 +915,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         w.B.b_v[gb] = v; w.B.b_w[gb] = om;
     }
     g.sync();
+    if (g.rank() == 0) ck.mark(5);
     // 9. position iterations with the per-island early exit (island.py:141-153)
     for (int it = 0; it < sp.pos_iters; ++it) {
         for (int b = g.rank(); b < nb; b += g.size()) minsep[b] = dkey(0.0);
@@ -917,7 +923,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         for (int cc = 0; cc < ncol; ++cc) {
             int s0 = coff[cc], s1 = coff[cc + 1];
             for (int j = s0 + g.rank(); j < s1; j += g.size()) {
-                const Cons<R> &q = cons[order[j]];
+                const Cons<R> q = cons[j];
                 if (rootf[q.root] & R_DONE) continue;
                 int ga = w.bb + q.ia, gbb = w.bb + q.ib;
                 vec2<double> ca = w.B.b_c[ga], cb = w.B.b_c[gbb];
@@ -939,6 +945,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         if (!g.any(pending)) break;
     }
     g.sync();
+    if (g.rank() == 0) ck.mark(6);
     // 10. write back the transforms of the island bodies (island.py:156-159)
     for (int b = g.rank(); b < nb; b += g.size()) {
         if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;

@@ -85,6 +85,7 @@ template <class R> struct Batch {
     int *s_move, *s_first, *s_cnt;
     // scratch (contact-slot-indexed)
     int *s_proc, *s_pref, *s_adj, *s_colour, *s_order, *s_cons_of;
+    int2 *s_kb;
     unsigned char *s_cvis;
     Cons<R> *s_cons;
     unsigned long long *s_hash;  // 4 * ccap slots per world (a power of two >= 2*ccap fits)
