@@ -238,6 +238,18 @@ int gb_batch_phase_clocks(gb_batch *batch, int64_t *clocks, void *cuda_stream);
  * batch, world-steps requested so far (3 int64). */
 int gb_batch_counters(gb_batch *batch, int64_t *counters);
 
+/* Size of the static device scratch of gb_batch_step_static_scratch (32 MiB). */
+#define GB_STATIC_SCRATCH_BYTES (32u << 20)
+/* gb_batch_step with the step's scratch arrays placed in one static device
+ * array of GB_STATIC_SCRATCH_BYTES instead of the batch arena; the call
+ * allocates no device memory.  No counterpart in the reference (its step
+ * allocates Python objects per call).  The first call on a device looks up
+ * the array's address (loading the module), so make one call before any
+ * stream capture.  A batch whose scratch exceeds the array is rejected with
+ * GB_E_SCRATCH before any launch.  All calls on a device share the array:
+ * calls whose work may overlap (other streams or host threads) race. */
+int gb_batch_step_static_scratch(gb_batch *batch, const gb_step_opts *opts, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

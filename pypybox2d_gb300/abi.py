@@ -145,7 +145,12 @@ EXPORTED = (
     "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_get_proxies",
     "gb_batch_get_contact_counts", "gb_batch_get_contacts", "gb_batch_get_solver_order",
     "gb_batch_status", "gb_batch_counters", "gb_batch_phase_clocks",
+    "gb_batch_step_static_scratch",
 )
+
+#: bytes of the static device scratch behind gb_batch_step_static_scratch
+STATIC_SCRATCH_BYTES = 32 << 20
+E_SCRATCH = -7
 
 _lib = None
 
@@ -182,6 +187,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_status.argtypes = [vp, u32p, vp]
     lib.gb_batch_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     lib.gb_batch_phase_clocks.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), vp]
+    lib.gb_batch_step_static_scratch.argtypes = [vp, ctypes.POINTER(StepOpts), vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -80,6 +81,28 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
     B.order_out = a.take<int>(ncap);
     B.prof = a.take<long long>((size_t)nw * GB_NPROF);
+    B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
+    B.toi_list = a.take<int>(ncap);
+    B.toi_n = a.take<int>(1);
+}
+// Re-points the per-step scratch arrays of a batch into one region laid out
+// by `a` (a.base == nullptr only measures it).  The state that outlives a step
+// stays in the batch arena: the pending move buffer (s_move, read by the
+// first step), the recorded solver order and the phase clocks.
+template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap) {
+    B.s_parent = a.take<int>(nb); B.s_wake = a.take<int>(nb); B.s_seed = a.take<int>(nb); B.s_stack = a.take<int>(nb);
+    B.s_adjoff = a.take<int>(nb + nw);
+    B.s_root = a.take<uint32_t>(nb);
+    B.s_claim = a.take<unsigned long long>(nb); B.s_minsep = a.take<unsigned long long>(nb);
+    B.s_minsleep = a.take<unsigned long long>(nb);
+    B.s_bvis = a.take<unsigned char>(nb);
+    B.s_first = a.take<int>(nf); B.s_cnt = a.take<int>(nf);
+    B.s_proc = a.take<int>(ncap); B.s_pref = a.take<int>(ncap); B.s_adj = a.take<int>(2 * (size_t)ncap);
+    B.s_colour = a.take<int>(ncap); B.s_order = a.take<int>(ncap); B.s_cons_of = a.take<int>(ncap);
+    B.s_cvis = a.take<unsigned char>(ncap);
+    B.s_kb = a.take<int2>(ncap);
+    B.s_cons = a.take<Cons<R>>(ncap);
+    B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
     B.toi_n = a.take<int>(1);
@@ -413,3 +436,78 @@ int gb_batch_counters(gb_batch *b, int64_t *c) {
 }
 
 }  // extern "C"
+
+// Step scratch in static device memory, for gb_batch_step_static_scratch:
+// the call itself allocates no device memory.  Every call on a device shares
+// this one region, so calls whose launches may overlap (other streams, other
+// host threads) race on it.
+static __device__ __align__(256) unsigned char g_step_scratch[GB_STATIC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_step_scratch on the current device, looked up once per
+// device (the lookup loads the module; a later call only reads the table).
+int static_scratch_base(void **out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(GB_E_ARG, "device ordinal beyond the static scratch table");
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_step_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_step_scratch)");
+        if (!p) return fail(GB_E_CUDA, "cudaGetSymbolAddress(g_step_scratch) returned NULL");
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return 0;
+}
+
+template <class R> int step_static(gb_batch *b, const Batch<R> &arena_view, const StepParams &sp, int n_steps, int mode,
+                                   int threads, cudaStream_t st) {
+    Batch<R> B = arena_view;
+    Arena need;
+    carve_step_scratch(need, B, b->nw, b->nb, b->nf, b->ncap);
+    if (need.off > (size_t)GB_STATIC_SCRATCH_BYTES)
+        return fail(GB_E_SCRATCH, "batch needs " + std::to_string(need.off) + " bytes of step scratch; the static scratch holds " +
+                                      std::to_string((size_t)GB_STATIC_SCRATCH_BYTES) + " (use gb_batch_step)");
+    void *base = nullptr;
+    int rc = static_scratch_base(&base);
+    if (rc) return rc;
+    Arena a;
+    a.base = static_cast<char *>(base);
+    carve_step_scratch(a, B, b->nw, b->nb, b->nf, b->ncap);
+    // every scratch array is written before it is read inside a step, except
+    // the first-pass TOI list counter
+    CK(cudaMemsetAsync(B.toi_n, 0, sizeof(int), st));
+    rc = gb_launch_step<R>(B, sp, n_steps, b->d_worlds, b->nw, mode, threads, st);
+    if (rc) return cuda_fail((cudaError_t)rc, "step launch (static scratch)");
+    return 0;
+}
+}  // namespace
+
+extern "C" int gb_batch_step_static_scratch(gb_batch *b, const gb_step_opts *o, void *stream) {
+    if (!b || !o) return fail(GB_E_ARG, "batch or opts is NULL");
+    if (o->n_steps < 0 || o->vel_iters < 0 || o->pos_iters < 0) return fail(GB_E_ARG, "negative step count or iterations");
+    StepParams sp;
+    sp.dt = o->dt;
+    sp.inv_dt = o->dt > 0.0 ? 1.0 / o->dt : 0.0;
+    sp.dt_ratio = 0.0;
+    sp.vel_iters = o->vel_iters;
+    sp.pos_iters = o->pos_iters;
+    sp.record_order = o->record_order & 1;
+    sp.profile = (o->record_order >> 1) & 1;
+    int mode = (o->launch_mode == 2 || o->launch_mode == 3) ? o->launch_mode : (o->launch_mode == 0 ? 3 : 1);
+    int threads = o->block_threads > 0 ? o->block_threads : 128;
+    if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = b->prec == GB_PREC_F64 ? step_static<double>(b, b->bd, sp, o->n_steps, mode, threads, st)
+                                    : step_static<float>(b, b->bf, sp, o->n_steps, mode, threads, st);
+    if (rc) return rc;
+    b->counters[0] += 1;
+    b->counters[2] += o->n_steps;
+    return 0;
+}

@@ -45,6 +45,14 @@ class GpuBatch:
         o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, flags)
         abi.check(self.lib.gb_batch_step(self.h, ctypes.byref(o), ctypes.c_void_p(stream or 0)))
 
+    def step_static_scratch(self, dt: float, vel_iters: int = 8, pos_iters: int = 3, n_steps: int = 1,
+                            launch_mode: int = 1, block_threads: int = 0, stream: int | None = None) -> None:
+        """``step`` with the step scratch in the library's static device array
+        (gb_batch_step_static_scratch): no device allocation in the call; the
+        batch's scratch must fit ``abi.STATIC_SCRATCH_BYTES``."""
+        o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, 0)
+        abi.check(self.lib.gb_batch_step_static_scratch(self.h, ctypes.byref(o), ctypes.c_void_p(stream or 0)))
+
     def bodies(self, stream: int | None = None) -> np.ndarray:
         out = np.zeros(self.n_bodies, dtype=abi.BODY)
         abi.check(self.lib.gb_batch_get_bodies(self.h, out.ctypes.data, self.n_bodies, ctypes.c_void_p(stream or 0)))
