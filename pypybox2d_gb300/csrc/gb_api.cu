@@ -229,6 +229,14 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         if (b->nb > 0) CK(cudaMemcpy(d_bw, bw.data(), sizeof(int) * b->nb, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(d_cw, cw.data(), sizeof(int) * b->ncap, cudaMemcpyHostToDevice));
     }
+    {
+        // solver body cache: sized for the largest world, up to 2048 bodies (48 KiB)
+        int max_nb = 0;
+        for (int i = 0; i < b->nw; ++i) max_nb = std::max(max_nb, b->hdr[i].nb);
+        int cache = max_nb <= 2048 ? max_nb : 0;
+        b->bd.cache_bodies = cache;
+        b->bf.cache_bodies = cache;
+    }
     CK(cudaMalloc((void **)&b->d_worlds, sizeof(int) * b->nw));
     CK(cudaMemcpy(b->d_worlds, b->launch_order.data(), sizeof(int) * b->nw, cudaMemcpyHostToDevice));
     CK(cudaMalloc((void **)&b->d_bstage, sizeof(gb_body) * std::max(1, b->nb)));

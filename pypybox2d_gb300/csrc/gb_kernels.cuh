@@ -103,6 +103,13 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
         // for the ordered parts (see gb_phases.cuh)
         const int nb = B.n_bodies, ns = B.n_slots, T = 256;
         const int gb = (nb + T - 1) / T, gs = (ns + T - 1) / T;
+        // the solve kernel stages each world's bodies in shared memory
+        const size_t solve_smem = (size_t)B.cache_bodies * GB_CACHE_BYTES_PER_BODY;
+        if (solve_smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k_world<GB_REAL, PH_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)solve_smem);
+            if (e != cudaSuccess) return (int)e;
+        }
         for (int s = 0; s < n_steps; ++s) {
             k_world<GB_REAL, PH_PAIRS0><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
             if (nb) k_pre<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
@@ -111,7 +118,7 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
             k_world<GB_REAL, PH_ISLANDS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
             if (nb) k_vinit<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
             if (ns) k_cinit<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
-            k_world<GB_REAL, PH_SOLVE><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            k_world<GB_REAL, PH_SOLVE><<<n_list, threads, solve_smem, st>>>(B, sp, d_worlds);
             k_world<GB_REAL, PH_PAIRS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
             if (ns) k_toi1<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
             if (ns) k_toi1b<GB_REAL><<<152 * 4, 128, 0, st>>>(B);

@@ -462,7 +462,9 @@ template <class R> __device__ void init_velocity(Cons<R> &k, vec2<double> ca, do
 // contact.py:498-525
 template <class R> __device__ __forceinline__ void warm_start(const Cons<R> &k, vec2<R> &va, R &wa, vec2<R> &vb, R &wb) {
     vec2<R> normal = k.normal, tangent = cross(normal, (R)1);
-    for (int i = 0; i < k.npts; ++i) {
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {   // i < npts; constant indices keep the constraint in registers
+        if (i >= k.npts) break;
         vec2<R> P = k.ni[i] * normal + k.ti[i] * tangent;
         wa = wa - k.iA * cross(k.rA[i], P);
         va = va - k.ma * P;
@@ -476,7 +478,9 @@ template <class R> __device__ __forceinline__ void solve_velocity(Cons<R> &k, ve
     const R ma = k.ma, mb = k.mb, iA = k.iA, iB = k.iB;
     vec2<R> normal = k.normal, tangent = cross(normal, (R)1);
     R friction = k.friction;
-    for (int i = 0; i < k.npts; ++i) {
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        if (i >= k.npts) break;
         vec2<R> ra = k.rA[i], rb = k.rB[i];
         vec2<R> dv = ((vb + cross(wb, rb)) - va) - cross(wa, ra);
         R vt = dot(dv, tangent);
@@ -554,7 +558,9 @@ template <class R> __device__ double solve_position(const Cons<R> &k, vec2<doubl
         if (!toi_a) { ma = (R)0; iA = (R)0; }
         if (!toi_b) { mb = (R)0; iB = (R)0; }
     }
-    for (int j = 0; j < k.mcount; ++j) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {   // j < point count
+        if (j >= k.mcount) break;
         xform2<R> xa = pose_xf<R>(ca, aa, k.lca), xb = pose_xf<R>(cb, ab, k.lcb);
         vec2<R> normal, point;
         R sep;
@@ -841,7 +847,16 @@ template <class R> __device__ __forceinline__ void init_constraint(const WView<R
 
 // Warm start, velocity iterations, impulse store, position integration,
 // position iterations and transform write-back (island.py:98-159).
-template <class R, class G> __device__ void solve_group(const G &g, const WView<R> &w, const StepParams &sp, PhaseClock *pcp = nullptr) {
+// Bodies of one world staged in shared memory for the solver passes:
+// velocities during the velocity iterations, then positions during the
+// position iterations (the same bytes, 24 per body).
+struct BodyCache {
+    unsigned char *mem;   // nullptr: the passes read and write global memory
+};
+#define GB_CACHE_BYTES_PER_BODY 24
+
+template <class R, class G> __device__ void solve_group(const G &g, const WView<R> &w, const StepParams &sp, PhaseClock *pcp = nullptr,
+                                                        BodyCache cache = BodyCache{nullptr}) {
     PhaseClock dummy;
     dummy.acc = nullptr;
     PhaseClock &ck = pcp ? *pcp : dummy;
@@ -865,14 +880,22 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     // 6. warm start and velocity iterations, colour by colour
     const int ncol = w.H->last_ncolours;
     const int ncons = w.H->last_ncons;
+    // velocities: shared-memory copy (world-local index) or the batch arrays
+    vec2<R> *vel = w.B.b_v + w.bb;
+    R *om = w.B.b_w + w.bb;
+    if (cache.mem) {
+        vel = reinterpret_cast<vec2<R> *>(cache.mem);
+        om = reinterpret_cast<R *>(cache.mem + sizeof(vec2<R>) * (size_t)nb);
+        for (int b = g.rank(); b < nb; b += g.size()) { vel[b] = w.B.b_v[w.bb + b]; om[b] = w.B.b_w[w.bb + b]; }
+        g.sync();
+    }
     for (int it = (warm ? -1 : 0); it < sp.vel_iters; ++it) {
         for (int cc = 0; cc < ncol; ++cc) {
             int s0 = coff[cc], s1 = coff[cc + 1];
             for (int j = s0 + g.rank(); j < s1; j += g.size()) {
                 Cons<R> q = cons[j];   // by value: independent loads, no aliasing reloads
-                int ga = w.bb + q.ia, gbb = w.bb + q.ib;
-                vec2<R> va = w.B.b_v[ga], vb = w.B.b_v[gbb];
-                R wa = w.B.b_w[ga], wb = w.B.b_w[gbb];
+                vec2<R> va = vel[q.ia], vb = vel[q.ib];
+                R wa = om[q.ia], wb = om[q.ib];
                 if (it < 0) warm_start(q, va, wa, vb, wb);
                 else {
                     solve_velocity(q, va, wa, vb, wb);
@@ -880,11 +903,15 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
                     cons[j].ti[0] = q.ti[0]; cons[j].ti[1] = q.ti[1];
                 }
                 // colour classes share no non-static body; static bodies keep v = 0
-                if (w.btype(q.ia) != GB_BODY_STATIC) { w.B.b_v[ga] = va; w.B.b_w[ga] = wa; }
-                if (w.btype(q.ib) != GB_BODY_STATIC) { w.B.b_v[gbb] = vb; w.B.b_w[gbb] = wb; }
+                if (w.btype(q.ia) != GB_BODY_STATIC) { vel[q.ia] = va; om[q.ia] = wa; }
+                if (w.btype(q.ib) != GB_BODY_STATIC) { vel[q.ib] = vb; om[q.ib] = wb; }
             }
             g.sync();
         }
+    }
+    if (cache.mem) {
+        for (int b = g.rank(); b < nb; b += g.size()) { w.B.b_v[w.bb + b] = vel[b]; w.B.b_w[w.bb + b] = om[b]; }
+        g.sync();
     }
     if (g.rank() == 0) { ck.mark(4); if (ck.acc) ck.acc[10] += ncol; }
     // 7. store impulses (contact.py:801-806)
@@ -917,6 +944,14 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     g.sync();
     if (g.rank() == 0) ck.mark(5);
     // 9. position iterations with the per-island early exit (island.py:141-153)
+    vec2<double> *pc = w.B.b_c + w.bb;
+    double *pa = w.B.b_a + w.bb;
+    if (cache.mem) {
+        pc = reinterpret_cast<vec2<double> *>(cache.mem);
+        pa = reinterpret_cast<double *>(cache.mem + sizeof(vec2<double>) * (size_t)nb);
+        for (int b = g.rank(); b < nb; b += g.size()) { pc[b] = w.B.b_c[w.bb + b]; pa[b] = w.B.b_a[w.bb + b]; }
+        g.sync();
+    }
     for (int it = 0; it < sp.pos_iters; ++it) {
         for (int b = g.rank(); b < nb; b += g.size()) minsep[b] = dkey(0.0);
         g.sync();
@@ -925,13 +960,12 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             for (int j = s0 + g.rank(); j < s1; j += g.size()) {
                 const Cons<R> q = cons[j];
                 if (rootf[q.root] & R_DONE) continue;
-                int ga = w.bb + q.ia, gbb = w.bb + q.ib;
-                vec2<double> ca = w.B.b_c[ga], cb = w.B.b_c[gbb];
-                double aa = w.B.b_a[ga], ab = w.B.b_a[gbb];
+                vec2<double> ca = pc[q.ia], cb = pc[q.ib];
+                double aa = pa[q.ia], ab = pa[q.ib];
                 double ms = solve_position(q, ca, aa, cb, ab, 0.0, false, false, false);
                 atomicMin(&minsep[q.root], dkey(ms));
-                if (w.btype(q.ia) != GB_BODY_STATIC) { w.B.b_c[ga] = ca; w.B.b_a[ga] = aa; }
-                if (w.btype(q.ib) != GB_BODY_STATIC) { w.B.b_c[gbb] = cb; w.B.b_a[gbb] = ab; }
+                if (w.btype(q.ia) != GB_BODY_STATIC) { pc[q.ia] = ca; pa[q.ia] = aa; }
+                if (w.btype(q.ib) != GB_BODY_STATIC) { pc[q.ib] = cb; pa[q.ib] = ab; }
             }
             g.sync();
         }
@@ -945,6 +979,10 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         if (!g.any(pending)) break;
     }
     g.sync();
+    if (cache.mem) {
+        for (int b = g.rank(); b < nb; b += g.size()) { w.B.b_c[w.bb + b] = pc[b]; w.B.b_a[w.bb + b] = pa[b]; }
+        g.sync();
+    }
     if (g.rank() == 0) ck.mark(6);
     // 10. write back the transforms of the island bodies (island.py:156-159)
     for (int b = g.rank(); b < nb; b += g.size()) {

@@ -58,6 +58,7 @@ struct WorldHdr {              // per-world scalars (device)
 
 template <class R> struct Batch {
     int n_worlds, n_bodies, n_slots;
+    int cache_bodies;         // worlds of at most this many bodies are solved from shared memory
     WorldHdr *hdr;
     int *b_world;             // world of each body
     int *c_world;             // world of each contact slot

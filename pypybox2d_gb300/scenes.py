@@ -20,7 +20,7 @@ import math
 import numpy as np
 
 from . import abi
-from .shapes import Circle, Edge, Polygon, _xmul
+from .shapes import FLT_EPSILON, POLYGON_RADIUS, Circle, Edge, Polygon, _xmul
 
 AABB_EXTENSION = 0.1
 
@@ -306,3 +306,250 @@ def pyramid_batch(n_worlds: int, rows: int = 20, jitter: float = 0.01, seed: int
         Bs = Bv.reshape(-1)
         Fs = Fv.reshape(-1)
     return Ws, Bs, Fs, Ms
+
+
+# ------------------------------------------------------------ uneven batch
+# Worlds of log-uniform size in [10, 2000] bodies: a static 100 x 100 m
+# container of four edges, half circles (radius U(0.25, 1)) and half convex
+# polygons of 3-8 vertices on a circle of radius U(0.3, 1); density U(0.5, 5),
+# friction U(0.2, 0.8), restitution U(0, 0.3); bodies start on distinct
+# cells of a 2.1 m grid (so they do not overlap) with velocity N(0, 2) m/s,
+# angular velocity N(0, 1) rad/s and angle U(-pi, pi); gravity (0, -10).
+CONTAINER_HALF = 50.0
+GRID_CELL = 2.1
+GRID_N = 45                                   # 45 x 45 cells span +-47.25 m
+UNEVEN_MIN, UNEVEN_MAX = 10, 2000
+
+
+def uneven_count(seed: int) -> int:
+    r = np.random.default_rng(seed)
+    return int(math.floor(math.exp(r.uniform(math.log(UNEVEN_MIN), math.log(UNEVEN_MAX)))))
+
+
+def _uneven_draws(seed: int, n: int | None = None) -> dict:
+    """Every random draw of one uneven world, in a fixed order (shared by the
+    SceneBuilder form and the vectorised batch, so both see the same numbers)."""
+    if n is None:
+        n = uneven_count(seed)
+    r = np.random.default_rng((seed, 1))
+    cells = r.choice(GRID_N * GRID_N, size=n, replace=False)
+    jit = r.uniform(-0.04, 0.04, size=(n, 2))
+    x0 = -0.5 * GRID_N * GRID_CELL + 0.5 * GRID_CELL
+    px = x0 + (cells % GRID_N) * GRID_CELL + jit[:, 0]
+    py = x0 + (cells // GRID_N) * GRID_CELL + jit[:, 1]
+    circle = r.random(n) < 0.5
+    crad = r.uniform(0.25, 1.0, n)
+    prad = r.uniform(0.3, 1.0, n)
+    nv = r.integers(3, abi.MAX_POLY_VERTS + 1, n)
+    # polygon vertices: nv angles in CCW order on the circle (points on a
+    # circle are in strictly convex position); the gaps are 0.2 rad plus a
+    # Dirichlet(4) share of the rest (no short edges), redrawn while one
+    # exceeds 3 rad (the polygon holds its origin)
+    theta = np.zeros((n, abi.MAX_POLY_VERTS))
+    cols = np.arange(abi.MAX_POLY_VERTS)[None, :]
+    todo = np.arange(n)
+    while len(todo):
+        k = nv[todo][:, None]
+        e = np.where(cols < k, r.gamma(4.0, 1.0, (len(todo), abi.MAX_POLY_VERTS)), 0.0)
+        gaps = 0.2 + (2.0 * math.pi - 0.2 * k) * (e / e.sum(axis=1, keepdims=True))
+        gaps = np.where(cols < k, gaps, 0.0)
+        ok = gaps.max(axis=1) <= 3.0
+        start = r.uniform(0.0, 2.0 * math.pi, len(todo))
+        ang = start[:, None] + np.concatenate([np.zeros((len(todo), 1)), np.cumsum(gaps, axis=1)[:, :-1]], axis=1)
+        theta[todo[ok]] = np.where(cols < k, ang, 0.0)[ok]
+        todo = todo[~ok]
+    vx = prad[:, None] * np.cos(theta)
+    vy = prad[:, None] * np.sin(theta)
+    return dict(n=n, px=px, py=py, circle=circle, crad=crad, nv=nv, vx=vx, vy=vy,
+                density=r.uniform(0.5, 5.0, n), friction=r.uniform(0.2, 0.8, n),
+                restitution=r.uniform(0.0, 0.3, n), v=r.normal(0.0, 2.0, (n, 2)),
+                w=r.normal(0.0, 1.0, n), angle=r.uniform(-math.pi, math.pi, n))
+
+
+def _container_edges():
+    h = CONTAINER_HALF
+    return [Edge((-h, -h), (h, -h)), Edge((h, -h), (h, h)), Edge((h, h), (-h, h)), Edge((-h, h), (-h, -h))]
+
+
+def uneven_builder(seed: int, n: int | None = None) -> SceneBuilder:
+    """One uneven world built body by body through SceneBuilder."""
+    d = _uneven_draws(seed, n)
+    s = SceneBuilder(gravity=(0.0, -10.0), do_sleep=True)
+    s.create_body(abi.BODY_STATIC, position=(0, 0), fixtures=[(e, {}) for e in _container_edges()])
+    for i in range(d["n"]):
+        if d["circle"][i]:
+            shape = Circle(radius=float(d["crad"][i]))
+        else:
+            k = int(d["nv"][i])
+            shape = Polygon(vertices=list(zip(d["vx"][i, :k].tolist(), d["vy"][i, :k].tolist())))
+        fk = dict(density=float(d["density"][i]), friction=float(d["friction"][i]),
+                  restitution=float(d["restitution"][i]))
+        s.create_body(abi.BODY_DYNAMIC, position=(float(d["px"][i]), float(d["py"][i])), angle=float(d["angle"][i]),
+                      linear_velocity=(float(d["v"][i, 0]), float(d["v"][i, 1])), angular_velocity=float(d["w"][i]),
+                      fixtures=[(shape, fk)])
+    return s
+
+
+def uneven_world(seed: int, n: int | None = None):
+    return uneven_builder(seed, n).records()
+
+
+def uneven_batch(n_worlds: int = 8192, seed: int = 0, counts=None):
+    """The uneven batch, world w drawn from seed + w.  Records are assembled
+    with numpy in the same float64 operation order as SceneBuilder (circle and
+    polygon mass data, centre of mass, the velocity shift of reset_mass_data,
+    edge normals and fat AABBs), so world w equals uneven_world(seed + w)."""
+    draws = [_uneven_draws(seed + w, None if counts is None else int(counts[w])) for w in range(n_worlds)]
+    ns = np.array([d["n"] for d in draws])
+    cat = {k: np.concatenate([d[k] for d in draws]) for k in draws[0] if k != "n"}
+    nbody = int(ns.sum())
+    nb_w = ns + 1
+    nf_w = ns + 4
+    b_start = np.concatenate([[0], np.cumsum(nb_w)[:-1]])
+    f_start = np.concatenate([[0], np.cumsum(nf_w)[:-1]])
+    # container (static body 0 of every world, four edge fixtures)
+    cs = SceneBuilder(gravity=(0.0, -10.0), do_sleep=True)
+    cs.create_body(abi.BODY_STATIC, position=(0, 0), fixtures=[(e, {}) for e in _container_edges()])
+    Wc, Bc, Fc, _ = cs.records()
+    B = np.zeros(int(nb_w.sum()), dtype=abi.BODY)
+    F = np.zeros(int(nf_w.sum()), dtype=abi.FIXTURE)
+    B[b_start] = Bc[0]
+    for k in range(4):
+        F[f_start + k] = Fc[k]
+    # dynamic bodies: index of body i of world w = b_start[w] + 1 + i
+    widx = np.repeat(np.arange(n_worlds), ns)
+    local = np.arange(nbody) - np.repeat(np.concatenate([[0], np.cumsum(ns)[:-1]]), ns)
+    bi = b_start[widx] + 1 + local
+    fi = f_start[widx] + 4 + local
+    angle = cat["angle"]
+    qc = np.fromiter((math.cos(a) for a in angle.tolist()), float, nbody)
+    qs = np.fromiter((math.sin(a) for a in angle.tolist()), float, nbody)
+    px, py = cat["px"], cat["py"]
+    circ = cat["circle"]
+    dens = cat["density"]
+    # mass data (Circle.compute_mass, Polygon.compute_mass)
+    r = cat["crad"]
+    r2 = np.fromiter((x ** 2 for x in r.tolist()), float, nbody)   # CPython float pow, as Circle.compute_mass
+    cm = dens * math.pi * r2
+    cI = cm * (0.5 * r2 + (0.0 * 0.0 + 0.0 * 0.0))
+    nv = cat["nv"]
+    vx, vy = cat["vx"], cat["vy"]
+    sx, sy = vx[:, 0].copy(), vy[:, 0].copy()
+    for m in range(1, abi.MAX_POLY_VERTS):
+        use = m < nv
+        sx = np.where(use, sx + vx[:, m], sx)
+        sy = np.where(use, sy + vy[:, m], sy)
+    fn = nv.astype(float)
+    sx, sy = sx / fn, sy / fn
+    ccx = np.zeros(nbody); ccy = np.zeros(nbody); area = np.zeros(nbody); pI = np.zeros(nbody)
+    inv3 = 1.0 / 3.0
+    for m in range(abi.MAX_POLY_VERTS):
+        use = m < nv
+        j = np.where(m + 1 < nv, m + 1, 0)
+        e1x, e1y = vx[:, m] - sx, vy[:, m] - sy
+        e2x = np.take_along_axis(vx, j[:, None], axis=1)[:, 0] - sx
+        e2y = np.take_along_axis(vy, j[:, None], axis=1)[:, 0] - sy
+        D = e1x * e2y - e1y * e2x
+        tri = 0.5 * D
+        area = np.where(use, area + tri, area)
+        kk = tri * inv3
+        ccx = np.where(use, ccx + kk * (e1x + e2x), ccx)
+        ccy = np.where(use, ccy + kk * (e1y + e2y), ccy)
+        intx2 = e1x * e1x + e2x * e1x + e2x * e2x
+        inty2 = e1y * e1y + e2y * e1y + e2y * e2y
+        pI = np.where(use, pI + (0.25 * inv3 * D) * (intx2 + inty2), pI)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        pm = dens * area
+        ccx, ccy = ccx / area, ccy / area
+        mcx, mcy = ccx + sx, ccy + sy
+        pIm = dens * pI
+        pIm = pIm + pm * ((mcx * mcx + mcy * mcy) - (ccx * ccx + ccy * ccy))
+    md_mass = np.where(circ, cm, pm)
+    md_cx = np.where(circ, 0.0, mcx)
+    md_cy = np.where(circ, 0.0, mcy)
+    md_I = np.where(circ, cI, pIm)
+    # Body.reset_mass_data (twice: once when the fixture is attached, once when
+    # the body joins the world; the second leaves the state unchanged but its
+    # velocity shift is by a zero vector)
+    mass = 0.0 + md_mass
+    cx = 0.0 + mass * md_cx
+    cy = 0.0 + mass * md_cy
+    I = 0.0 + md_I
+    inv_mass = 1.0 / mass
+    cx, cy = cx * inv_mass, cy * inv_mass
+    I = I - mass * (cx * cx + cy * cy)
+    invI = 1.0 / I
+    c0x = px + qc * 0.0 + (-qs) * 0.0
+    c0y = py + qs * 0.0 + qc * 0.0
+    ncx = px + qc * cx + (-qs) * cy
+    ncy = py + qs * cx + qc * cy
+    w = cat["w"]
+    v0, v1 = cat["v"][:, 0], cat["v"][:, 1]
+    v0, v1 = v0 + (-w * (ncy - c0y)), v1 + w * (ncx - c0x)
+    v0, v1 = v0 + (-w * (ncy - ncy)), v1 + w * (ncx - ncx)
+    Bd = B[bi]
+    Bd["type"] = abi.BODY_DYNAMIC
+    Bd["flags"] = abi.BODY_AWAKE | abi.BODY_ALLOW_SLEEP | abi.BODY_ACTIVE
+    Bd["fixture_start"] = 4 + local
+    Bd["fixture_count"] = 1
+    Bd["px"], Bd["py"], Bd["qc"], Bd["qs"] = px, py, qc, qs
+    Bd["lcx"], Bd["lcy"] = cx, cy
+    Bd["c0x"], Bd["c0y"], Bd["cx"], Bd["cy"] = ncx, ncy, ncx, ncy
+    Bd["a0"], Bd["a"] = angle, angle
+    Bd["vx"], Bd["vy"], Bd["w"] = v0, v1, w
+    Bd["mass"], Bd["inv_mass"], Bd["I"], Bd["inv_I"] = mass, inv_mass, I, invI
+    Bd["gravity_scale"] = 1.0
+    B[bi] = Bd
+    # fixtures
+    Fd = F[fi]
+    Fd["body"] = 1 + local
+    Fd["shape_type"] = np.where(circ, abi.SHAPE_CIRCLE, abi.SHAPE_POLYGON)
+    Fd["vertex_count"] = np.where(circ, 1, nv)
+    Fd["radius"] = np.where(circ, r, POLYGON_RADIUS)
+    Fd["friction"], Fd["restitution"], Fd["density"] = cat["friction"], cat["restitution"], dens
+    Fd["category_bits"], Fd["mask_bits"] = 0x0001, 0xFFFF
+    used = np.arange(abi.MAX_POLY_VERTS)[None, :] < nv[:, None]
+    pvx = np.where(used, vx, 0.0)
+    pvy = np.where(used, vy, 0.0)
+    # edge normals (Polygon.vertices setter)
+    nxs = np.zeros_like(pvx); nys = np.zeros_like(pvy)
+    for m in range(abi.MAX_POLY_VERTS):
+        j = np.where(m + 1 < nv, m + 1, 0)
+        ex = np.take_along_axis(pvx, j[:, None], axis=1)[:, 0] - pvx[:, m]
+        ey = np.take_along_axis(pvy, j[:, None], axis=1)[:, 0] - pvy[:, m]
+        nx, ny = 1.0 * ey, -1.0 * ex
+        ln = np.sqrt(nx * nx + ny * ny)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            inv = 1.0 / ln
+        small = ln < FLT_EPSILON
+        nxs[:, m] = np.where(used[:, m], np.where(small, nx, nx * inv), 0.0)
+        nys[:, m] = np.where(used[:, m], np.where(small, ny, ny * inv), 0.0)
+    Fd["vx"] = np.where(circ[:, None], 0.0, pvx)
+    Fd["vy"] = np.where(circ[:, None], 0.0, pvy)
+    Fd["nx"] = np.where(circ[:, None], 0.0, nxs)
+    Fd["ny"] = np.where(circ[:, None], 0.0, nys)
+    # fat AABBs (compute_aabb at the body transform, then +-0.1)
+    X = px[:, None] + qc[:, None] * pvx + (-qs[:, None]) * pvy
+    Y = py[:, None] + qs[:, None] * pvx + qc[:, None] * pvy
+    lx, ly, ux, uy = X[:, 0].copy(), Y[:, 0].copy(), X[:, 0].copy(), Y[:, 0].copy()
+    for m in range(abi.MAX_POLY_VERTS):
+        use = m < nv
+        lx = np.where(use & ~(lx < X[:, m]), X[:, m], lx)
+        ly = np.where(use & ~(ly < Y[:, m]), Y[:, m], ly)
+        ux = np.where(use & ~(ux > X[:, m]), X[:, m], ux)
+        uy = np.where(use & ~(uy > Y[:, m]), Y[:, m], uy)
+    pr = POLYGON_RADIUS
+    paabb = np.stack([(lx - pr) - AABB_EXTENSION, (ly - pr) - AABB_EXTENSION,
+                      (ux + pr) + AABB_EXTENSION, (uy + pr) + AABB_EXTENSION], axis=-1)
+    ccx_, ccy_ = px + (qc * 0.0 + (-qs) * 0.0), py + (qs * 0.0 + qc * 0.0)
+    caabb = np.stack([(ccx_ - r) - AABB_EXTENSION, (ccy_ - r) - AABB_EXTENSION,
+                      (ccx_ + r) + AABB_EXTENSION, (ccy_ + r) + AABB_EXTENSION], axis=-1)
+    Fd["aabb"] = np.where(circ[:, None], caabb, paabb)
+    F[fi] = Fd
+    Wv = np.zeros(n_worlds, dtype=abi.WORLD)
+    Wv[:] = Wc[0]
+    Wv["body_start"], Wv["body_count"] = b_start, nb_w
+    Wv["fixture_start"], Wv["fixture_count"] = f_start, nf_w
+    Wv["move_start"], Wv["move_count"] = f_start, nf_w
+    M = np.concatenate([np.arange(k, dtype=np.int32) for k in nf_w]) if n_worlds else np.zeros(0, np.int32)
+    return Wv, B, F, M

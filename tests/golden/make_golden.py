@@ -310,12 +310,37 @@ def scene_sleep(b2):
     return world
 
 
+def scene_uneven(b2, seed=11, n=250):
+    """One world of the uneven-batch workload (pypybox2d_gb300.scenes draws:
+    100 m container of 4 edges, circles and convex polygons on a 2.1 m grid,
+    random velocities), built through the reference's API."""
+    from pypybox2d_gb300 import scenes
+    d = scenes._uneven_draws(seed, n)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    h = scenes.CONTAINER_HALF
+    edges = [((-h, -h), (h, -h)), ((h, -h), (h, h)), ((h, h), (-h, h)), ((-h, h), (-h, -h))]
+    world.create_static_body(position=(0, 0), fixtures=[b2.Fixture(b2.Edge(v1, v2)) for v1, v2 in edges])
+    for i in range(d["n"]):
+        if d["circle"][i]:
+            shape = b2.Circle(radius=float(d["crad"][i]))
+        else:
+            k = int(d["nv"][i])
+            shape = b2.Polygon(vertices=list(zip(d["vx"][i, :k].tolist(), d["vy"][i, :k].tolist())))
+        fx = b2.Fixture(shape, density=float(d["density"][i]), friction=float(d["friction"][i]),
+                        restitution=float(d["restitution"][i]))
+        world.create_dynamic_body(position=(float(d["px"][i]), float(d["py"][i])), angle=float(d["angle"][i]),
+                                  linear_velocity=(float(d["v"][i, 0]), float(d["v"][i, 1])),
+                                  angular_velocity=float(d["w"][i]), fixtures=fx)
+    return world
+
+
 SCENES = {
     "pyramid": (scene_pyramid, 300, (1, 2, 3, 5, 10, 30, 100, 200, 300)),
     "pyramid5": (lambda b2: scene_pyramid(b2, rows=5), 150, (1, 2, 5, 20, 60, 150)),
     "mixed": (scene_mixed, 200, (1, 2, 5, 20, 60, 120, 200)),
     "bullets": (scene_bullets, 60, (1, 2, 3, 5, 10, 20, 40, 60)),
     "sleep": (scene_sleep, 90, (1, 10, 29, 30, 31, 45, 60, 90)),
+    "uneven": (scene_uneven, 240, (1, 2, 5, 30, 60, 120, 180, 240)),
 }
 
 

@@ -56,3 +56,22 @@ def test_pyramid_batch_first_world_and_jitter():
     Wb, Bb, Fb, _ = scenes.pyramid_builder(5, jitter=lambda k: (jit[k, 0], jit[k, 1])).records()
     same(B[nb:2 * nb], Bb, "jittered bodies")
     same(F[len(Fb):2 * len(Fb)], Fb, "jittered fixtures")
+
+
+def test_uneven_world_records_match_reference():
+    d = np.load(os.path.join(GOLDEN, "uneven.npz"))
+    W, B, F, M = scenes.uneven_world(11, 250)
+    same(B, d["init_bodies"], "bodies")
+    same(F, d["init_fixtures"], "fixtures")
+    assert np.array_equal(M, np.arange(len(F)))
+
+
+def test_uneven_batch_equals_worlds_built_one_body_at_a_time():
+    W, B, F, M = scenes.uneven_batch(5, seed=40)
+    W2, B2, F2, M2 = scenes.concat([scenes.uneven_world(40 + w) for w in range(5)])
+    same(W, W2, "worlds")
+    same(B, B2, "bodies")
+    same(F, F2, "fixtures")
+    assert np.array_equal(M, M2)
+    n = W["body_count"] - 1
+    assert ((n >= scenes.UNEVEN_MIN) & (n <= scenes.UNEVEN_MAX)).all()
