@@ -49,6 +49,11 @@ struct WShared {
     int ncons, ncolours;
     int pass;
     int all_allow_sleep;
+    // pair-finding grid of the world (find_new_contacts)
+    unsigned long long gred[6];
+    float gsum;
+    int gx, gy, nsmall, nbig;
+    double x0, y0, inv_h, maxw, maxh, cut;
 };
 
 // body.py:781-793 awake setter
@@ -202,6 +207,98 @@ template <class R> __device__ __forceinline__ bool pair_candidate(const WView<R>
     return true;
 }
 
+// Uniform grid over the lower corners of the world's fat AABBs, rebuilt for
+// each pair-finding pass.  Proxies larger than four times the mean extent
+// (ground boxes, container edges) are "big": they stay out of the grid and
+// are tested against every moved proxy, and a moved big proxy tests every
+// proxy.  The grid only prunes candidates: every pair is still decided by
+// the exact float64 overlap test, and the pairs of a moved proxy are sorted
+// by the other proxy's index, so the result does not depend on the grid.
+#define GB_GRID_MIN_MOVES 8
+static __device__ __forceinline__ int grid_cell(double x, double x0, double inv_h, int n) {
+    double t = floor((x - x0) * inv_h);
+    t = fmin(fmax(t, 0.0), (double)(n - 1));
+    return (int)t;
+}
+static __device__ __forceinline__ bool grid_big(const dbox &b, double cut) {
+    return (b.z - b.x) > cut || (b.w - b.y) > cut;
+}
+
+template <class R, class G> __device__ void build_pair_grid(const G &g, const WView<R> &w, WShared *sh, int *goff, int *gitem) {
+    const int nf = w.H->nf;
+    const dbox *aabb = w.B.f_aabb + w.fb;
+    if (g.rank() == 0) {
+        sh->gsum = 0.0f;
+        sh->gred[0] = sh->gred[1] = ~0ull;
+        sh->gred[2] = sh->gred[3] = sh->gred[4] = sh->gred[5] = 0ull;
+        sh->nbig = 0;
+    }
+    g.sync();
+    for (int f = g.rank(); f < nf; f += g.size()) {
+        dbox b = aabb[f];
+        atomicAdd(&sh->gsum, (float)fmax(b.z - b.x, b.w - b.y));
+    }
+    g.sync();
+    if (g.rank() == 0) sh->cut = 4.0 * (double)sh->gsum / (double)nf;
+    g.sync();
+    const double cut = sh->cut;
+    for (int f = g.rank(); f < nf; f += g.size()) {
+        dbox b = aabb[f];
+        if (grid_big(b, cut)) continue;
+        atomicMin(&sh->gred[0], dkey(b.x));
+        atomicMin(&sh->gred[1], dkey(b.y));
+        atomicMax(&sh->gred[2], dkey(b.x));
+        atomicMax(&sh->gred[3], dkey(b.y));
+        atomicMax(&sh->gred[4], dkey(b.z - b.x));
+        atomicMax(&sh->gred[5], dkey(b.w - b.y));
+    }
+    g.sync();
+    if (g.rank() == 0) {
+        int gx = 1, gy = 1;
+        double x0 = 0.0, y0 = 0.0, h = 1.0, mw = 0.0, mh = 0.0;
+        if (sh->gred[0] != ~0ull) {
+            x0 = dkey_inv(sh->gred[0]); y0 = dkey_inv(sh->gred[1]);
+            double sx = dkey_inv(sh->gred[2]) - x0, sy = dkey_inv(sh->gred[3]) - y0;
+            mw = dkey_inv(sh->gred[4]); mh = dkey_inv(sh->gred[5]);
+            h = fmax(fmax(mw, mh), 1e-6);
+            const double cap = 2.0 * nf;
+            for (int k = 0; k < 64; ++k) {   // at most 2 nf cells
+                double cx = floor(sx / h) + 1.0, cy = floor(sy / h) + 1.0;
+                if (cx * cy <= cap) { gx = (int)cx; gy = (int)cy; break; }
+                h *= 1.5;
+            }
+        }
+        sh->x0 = x0; sh->y0 = y0; sh->inv_h = 1.0 / h; sh->maxw = mw; sh->maxh = mh;
+        sh->gx = gx; sh->gy = gy;
+    }
+    g.sync();
+    const int ncell = sh->gx * sh->gy;
+    const double x0 = sh->x0, y0 = sh->y0, ih = sh->inv_h;
+    const int gx = sh->gx, gy = sh->gy;
+    for (int c = g.rank(); c < ncell; c += g.size()) goff[c] = 0;
+    g.sync();
+    for (int f = g.rank(); f < nf; f += g.size()) {
+        dbox b = aabb[f];
+        if (grid_big(b, cut)) continue;
+        atomicAdd(&goff[grid_cell(b.y, y0, ih, gy) * gx + grid_cell(b.x, x0, ih, gx)], 1);
+    }
+    g.sync();
+    int nsmall = group_scan(g, ncell, [&](int c) { return goff[c]; }, goff);
+    g.sync();
+    if (g.rank() == 0) sh->nsmall = nsmall;
+    // scatter: afterwards goff[c] is the end of cell c (its start is goff[c - 1])
+    for (int f = g.rank(); f < nf; f += g.size()) {
+        dbox b = aabb[f];
+        if (grid_big(b, cut)) {
+            gitem[nsmall + atomicAdd(&sh->nbig, 1)] = f;
+        } else {
+            int c = grid_cell(b.y, y0, ih, gy) * gx + grid_cell(b.x, x0, ih, gx);
+            gitem[atomicAdd(&goff[c], 1)] = f;
+        }
+    }
+    g.sync();
+}
+
 template <class R, class G> __device__ void find_new_contacts(const G &g, const WView<R> &w, WShared *sh) {
     int nmove = sh->nmove;
     int nf = w.H->nf;
@@ -240,43 +337,94 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
         }
     }
     g.sync();
-    // pass 1: count survivors per move-buffer entry
+    // candidate proxies of a moved proxy: the grid cells its fat AABB can
+    // reach plus the big proxies, or every proxy (in index order)
+    const bool use_grid = nmove >= GB_GRID_MIN_MOVES;
+    int *goff = w.B.s_grid + 3 * (size_t)w.fb + 2 * (size_t)w.wi;
+    int *gitem = goff + 2 * (size_t)nf + 2;
+    if (use_grid) build_pair_grid(g, w, sh, goff, gitem);
+    const dbox *aabb = w.B.f_aabb + w.fb;
+    auto gridded = [&](int p) { return use_grid && !grid_big(aabb[p], sh->cut); };
+    auto each_candidate = [&](int i, int p, auto &&emit) {
+        if (!gridded(p)) {
+            for (int q = 0; q < nf; ++q)
+                if (pair_candidate(w, i, p, q, first, hash, hmask)) emit(q);
+            return;
+        }
+        const dbox b = aabb[p];
+        const double x0 = sh->x0, y0 = sh->y0, ih = sh->inv_h;
+        const int gx = sh->gx, gy = sh->gy;
+        // a proxy overlapping b has its lower corner within the largest
+        // gridded extent below b's lower corner (with a rounding margin)
+        const double lx = b.x - (sh->maxw + (fabs(b.x) + sh->maxw) * 1e-12);
+        const double ly = b.y - (sh->maxh + (fabs(b.y) + sh->maxh) * 1e-12);
+        const int cx0 = grid_cell(lx, x0, ih, gx), cx1 = grid_cell(b.z, x0, ih, gx);
+        const int cy0 = grid_cell(ly, y0, ih, gy), cy1 = grid_cell(b.w, y0, ih, gy);
+        for (int cy = cy0; cy <= cy1; ++cy)
+            for (int cx = cx0; cx <= cx1; ++cx) {
+                int c = cy * gx + cx;
+                for (int k = c ? goff[c - 1] : 0; k < goff[c]; ++k) {
+                    int q = gitem[k];
+                    if (pair_candidate(w, i, p, q, first, hash, hmask)) emit(q);
+                }
+            }
+        for (int k = sh->nsmall; k < sh->nsmall + sh->nbig; ++k) {
+            int q = gitem[k];
+            if (pair_candidate(w, i, p, q, first, hash, hmask)) emit(q);
+        }
+    };
+    // pass 1: count the new pairs of every move-buffer entry
     for (int i = g.rank(); i < nmove; i += g.size()) {
         int p = mv[i];
         int n = 0;
-        if (first[p] == i)
-            for (int q = 0; q < nf; ++q) n += pair_candidate(w, i, p, q, first, hash, hmask) ? 1 : 0;
+        if (first[p] == i) each_candidate(i, p, [&](int) { ++n; });
         cnt[i] = n;
     }
     g.sync();
     int total = group_scan(g, nmove, [&](int i) { return cnt[i]; }, cnt);
     g.sync();
-    int ccap = w.H->ccap;
-    // pass 2: create the contacts in order (contact.py:313-326 _create)
+    const int ccap = w.H->ccap;
+    const int room = ccap - nc;
+    // pass 2: the other proxy of each new pair, in index order per entry
+    int *pq = w.B.s_colour + w.cb;   // other proxy of new pair t (free outside the island phase)
+    int *pp = w.B.s_order + w.cb;    // moved proxy of new pair t
     for (int i = g.rank(); i < nmove; i += g.size()) {
         int p = mv[i];
         if (first[p] != i) continue;
-        int pos = nc + cnt[i];
-        for (int q = 0; q < nf; ++q) {
-            if (!pair_candidate(w, i, p, q, first, hash, hmask)) continue;
-            if (pos < ccap) {
-                int fa = p, fb = q;
-                bool prim;
-                pair_registered(w.B.f_type[w.fb + p], w.B.f_type[w.fb + q], &prim);
-                if (!prim) { fa = q; fb = p; }
-                ContactRec<R> &c = w.con(pos);
-                c.fa = fa; c.fb = fb;
-                c.flags = 0; c.toi_count = 0; c.toi = 0.0;
-                R fra = w.B.f_friction[w.fb + fa], frb = w.B.f_friction[w.fb + fb];
-                c.friction = sqrt(fra * frb);
-                c.restitution = pymax(w.B.f_restitution[w.fb + fa], w.B.f_restitution[w.fb + fb]);
-                Manifold<R> &m = c.m;
-                m.type = GB_M_CIRCLES; m.count = 0;
-                m.ln = mk<R>(0, 0); m.lp = mk<R>(0, 0);
-                for (int k = 0; k < 2; ++k) { m.plp[k] = mk<R>(0, 0); m.ni[k] = (R)0; m.ti[k] = (R)0; m.id[k] = 0; }
+        const int base = cnt[i];
+        int k = base;
+        each_candidate(i, p, [&](int q) {
+            if (k < room) { pq[k] = q; pp[k] = p; }
+            ++k;
+        });
+        if (gridded(p)) {
+            const int end = k < room ? k : room;
+            for (int a = base + 1; a < end; ++a) {   // insertion sort by proxy index
+                int v = pq[a], b = a - 1;
+                while (b >= base && pq[b] > v) { pq[b + 1] = pq[b]; --b; }
+                pq[b + 1] = v;
             }
-            ++pos;
         }
+    }
+    g.sync();
+    // create the contacts in that order (contact.py:313-326 _create)
+    const int ncreate = total < room ? total : room;
+    for (int t = g.rank(); t < ncreate; t += g.size()) {
+        int p = pp[t], q = pq[t];
+        int fa = p, fb = q;
+        bool prim;
+        pair_registered(w.B.f_type[w.fb + p], w.B.f_type[w.fb + q], &prim);
+        if (!prim) { fa = q; fb = p; }
+        ContactRec<R> &c = w.con(nc + t);
+        c.fa = fa; c.fb = fb;
+        c.flags = 0; c.toi_count = 0; c.toi = 0.0;
+        R fra = w.B.f_friction[w.fb + fa], frb = w.B.f_friction[w.fb + fb];
+        c.friction = sqrt(fra * frb);
+        c.restitution = pymax(w.B.f_restitution[w.fb + fa], w.B.f_restitution[w.fb + fb]);
+        Manifold<R> &m = c.m;
+        m.type = GB_M_CIRCLES; m.count = 0;
+        m.ln = mk<R>(0, 0); m.lp = mk<R>(0, 0);
+        for (int k = 0; k < 2; ++k) { m.plp[k] = mk<R>(0, 0); m.ni[k] = (R)0; m.ti[k] = (R)0; m.id[k] = 0; }
     }
     g.sync();
     if (g.rank() == 0) {

@@ -152,6 +152,52 @@ class SceneBuilder:
         b.aabbs[k] = (lx - AABB_EXTENSION, ly - AABB_EXTENSION, ux + AABB_EXTENSION, uy + AABB_EXTENSION)
         self.moves.append((bi, k))
 
+    def body_records(self, bi: int, body_index: int | None = None):
+        """Record of body bi and the records of its fixtures (``body`` field =
+        body_index, default bi)."""
+        b = self.bodies[bi]
+        B = np.zeros(1, dtype=abi.BODY)
+        F = np.zeros(len(b.fixtures), dtype=abi.FIXTURE)
+        fl = ((abi.BODY_AWAKE if b.awake else 0) | (abi.BODY_ALLOW_SLEEP if b.allow_sleep else 0) |
+              (abi.BODY_BULLET if b.bullet else 0) | (abi.BODY_FIXED_ROTATION if b.fixed_rotation else 0) |
+              (abi.BODY_ACTIVE if b.active else 0))
+        B[0] = (b.type, fl, 0, len(b.fixtures), b.p[0], b.p[1], b.q[0], b.q[1], b.lc[0], b.lc[1],
+                b.c0[0], b.c0[1], b.c[0], b.c[1], b.a0, b.a, b.alpha0, b.v[0], b.v[1], b.w,
+                b.force[0], b.force[1], b.torque, b.mass, b.inv_mass, b.I, b.invI, b.ld, b.ad, b.gs, b.sleep_time)
+        for j, f in enumerate(b.fixtures):
+            r = F[j]
+            sh = f.shape
+            r["body"], r["shape_type"], r["radius"] = bi if body_index is None else body_index, sh.type, sh.radius
+            r["friction"], r["restitution"], r["density"] = f.friction, f.restitution, f.density
+            r["category_bits"], r["mask_bits"], r["group_index"] = f.category, f.mask, f.group
+            ffl = abi.FIX_SENSOR if f.sensor else 0
+            if isinstance(sh, Circle):
+                r["vertex_count"] = 1
+                r["vx"][0], r["vy"][0] = sh.position
+            elif isinstance(sh, Polygon):
+                r["vertex_count"] = len(sh._vertices)
+                for m, ((vx, vy), (nx, ny)) in enumerate(zip(sh._vertices, sh._normals)):
+                    r["vx"][m], r["vy"][m], r["nx"][m], r["ny"][m] = vx, vy, nx, ny
+            elif isinstance(sh, Edge):
+                r["vertex_count"] = 2
+                r["vx"][0], r["vy"][0] = sh.vertex1
+                r["vx"][1], r["vy"][1] = sh.vertex2
+                if sh.vertex0 is not None:
+                    ffl |= abi.FIX_EDGE_HAS_V0
+                    r["vx"][2], r["vy"][2] = sh.vertex0
+                if sh.vertex3 is not None:
+                    ffl |= abi.FIX_EDGE_HAS_V3
+                    r["vx"][3], r["vy"][3] = sh.vertex3
+            r["flags"] = ffl
+            r["aabb"][:] = b.aabbs[j] if j < len(b.aabbs) and b.aabbs[j] is not None else (0, 0, 0, 0)
+        return B[0], F
+
+    def world_record(self, nb: int, nf: int, n_moves: int):
+        W = np.zeros(1, dtype=abi.WORLD)
+        flags = self.flags | (abi.W_NEW_FIXTURE if n_moves else 0)
+        W[0] = (0, nb, 0, nf, 0, 0, 0, flags, 0, n_moves, self.gravity[0], self.gravity[1], 0.0)
+        return W
+
     def records(self):
         """(worlds[1], bodies, fixtures, moves) record arrays of this world."""
         nb = len(self.bodies)
@@ -160,46 +206,14 @@ class SceneBuilder:
         F = np.zeros(nf, dtype=abi.FIXTURE)
         start = []
         k = 0
-        for i, b in enumerate(self.bodies):
+        for i in range(nb):
             start.append(k)
-            fl = ((abi.BODY_AWAKE if b.awake else 0) | (abi.BODY_ALLOW_SLEEP if b.allow_sleep else 0) |
-                  (abi.BODY_BULLET if b.bullet else 0) | (abi.BODY_FIXED_ROTATION if b.fixed_rotation else 0) |
-                  (abi.BODY_ACTIVE if b.active else 0))
-            B[i] = (b.type, fl, k, len(b.fixtures), b.p[0], b.p[1], b.q[0], b.q[1], b.lc[0], b.lc[1],
-                    b.c0[0], b.c0[1], b.c[0], b.c[1], b.a0, b.a, b.alpha0, b.v[0], b.v[1], b.w,
-                    b.force[0], b.force[1], b.torque, b.mass, b.inv_mass, b.I, b.invI, b.ld, b.ad, b.gs, b.sleep_time)
-            for j, f in enumerate(b.fixtures):
-                r = F[k]
-                sh = f.shape
-                r["body"], r["shape_type"], r["radius"] = i, sh.type, sh.radius
-                r["friction"], r["restitution"], r["density"] = f.friction, f.restitution, f.density
-                r["category_bits"], r["mask_bits"], r["group_index"] = f.category, f.mask, f.group
-                fl = abi.FIX_SENSOR if f.sensor else 0
-                if isinstance(sh, Circle):
-                    r["vertex_count"] = 1
-                    r["vx"][0], r["vy"][0] = sh.position
-                elif isinstance(sh, Polygon):
-                    r["vertex_count"] = len(sh._vertices)
-                    for m, ((vx, vy), (nx, ny)) in enumerate(zip(sh._vertices, sh._normals)):
-                        r["vx"][m], r["vy"][m], r["nx"][m], r["ny"][m] = vx, vy, nx, ny
-                elif isinstance(sh, Edge):
-                    r["vertex_count"] = 2
-                    r["vx"][0], r["vy"][0] = sh.vertex1
-                    r["vx"][1], r["vy"][1] = sh.vertex2
-                    if sh.vertex0 is not None:
-                        fl |= abi.FIX_EDGE_HAS_V0
-                        r["vx"][2], r["vy"][2] = sh.vertex0
-                    if sh.vertex3 is not None:
-                        fl |= abi.FIX_EDGE_HAS_V3
-                        r["vx"][3], r["vy"][3] = sh.vertex3
-                r["flags"] = fl
-                r["aabb"][:] = b.aabbs[j] if j < len(b.aabbs) and b.aabbs[j] is not None else (0, 0, 0, 0)
-                k += 1
+            B[i], Fi = self.body_records(i)
+            B[i]["fixture_start"] = k
+            F[k:k + len(Fi)] = Fi
+            k += len(Fi)
         moves = np.array([start[bi] + k for bi, k in self.moves], dtype=np.int32)
-        W = np.zeros(1, dtype=abi.WORLD)
-        flags = self.flags | (abi.W_NEW_FIXTURE if len(moves) else 0)
-        W[0] = (0, nb, 0, nf, 0, 0, 0, flags, 0, len(moves), self.gravity[0], self.gravity[1], 0.0)
-        return W, B, F, moves
+        return self.world_record(nb, nf, len(moves)), B, F, moves
 
 
 def concat(worlds: list) -> tuple:

@@ -1,0 +1,709 @@
+"""The reference's World / Body / Fixture API over the GPU step.
+
+``World`` mirrors pypybox2d's ``World`` (pypybox2d/world.py:64-473),
+``Body`` its ``Body`` (body.py) and ``Fixture`` its ``Fixture``
+(fixture.py:43-): the same constructor arguments, properties and methods
+for the parts the step uses, so a script written for pypybox2d runs with
+
+    import pypybox2d_gb300 as b2
+
+The host keeps the construction-time records (built with the reference's
+float64 arithmetic by ``scenes.SceneBuilder``); the first ``step`` uploads
+them (``gb_batch_create``) and from then on the device owns the state:
+
+* ``World.step`` is one ``gb_batch_step`` call;
+* reading a body property downloads all bodies once per step
+  (``gb_batch_get_bodies``); changing a velocity, a force or the awake flag
+  edits the host record and re-uploads the bodies before the next step
+  (``gb_batch_set_bodies``);
+* structural changes (a new body or fixture, a transform set by hand,
+  gravity, a destroyed body) download the whole world -- bodies, fat AABBs,
+  contacts with their manifolds and impulses -- edit it on the host with the
+  reference's arithmetic and upload it again, with the moved proxies in the
+  move buffer; pair finding for them runs on the device at the start of the
+  next step, as the reference's ``find_new_contacts`` would before it.
+
+What the GPU step does not support raises instead of running elsewhere:
+loop shapes, joints, sub-stepping, custom contact filters and
+``pre_solve`` callbacks that run mid-step.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import abi
+from .scenes import AABB_EXTENSION, SceneBuilder, _Body
+from .shapes import Circle, Edge, Loop, Polygon, Shape
+
+
+class LockedError(RuntimeError):
+    """A world was changed during a step (common.py:84-86)."""
+
+
+class Vec2(tuple):
+    """A 2-vector returned by the getters (x, y, arithmetic, length)."""
+
+    def __new__(cls, x=0.0, y=0.0):
+        return tuple.__new__(cls, (float(x), float(y)))
+
+    x = property(lambda self: self[0])
+    y = property(lambda self: self[1])
+
+    def __add__(self, o):
+        return Vec2(self[0] + o[0], self[1] + o[1])
+
+    def __sub__(self, o):
+        return Vec2(self[0] - o[0], self[1] - o[1])
+
+    def __mul__(self, k):
+        return Vec2(self[0] * k, self[1] * k)
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return Vec2(-self[0], -self[1])
+
+    def dot(self, o):
+        return self[0] * o[0] + self[1] * o[1]
+
+    def cross(self, o):
+        return self[0] * o[1] - self[1] * o[0]
+
+    @property
+    def length(self):
+        return math.sqrt(self[0] * self[0] + self[1] * self[1])
+
+    @property
+    def length_squared(self):
+        return self[0] * self[0] + self[1] * self[1]
+
+    def __repr__(self):
+        return f"Vec2({self[0]:g}, {self[1]:g})"
+
+
+class Fixture:
+    """fixture.py:43-71: a shape with its material and filter data."""
+
+    def __init__(self, shape=None, friction=0.2, restitution=0.0, density=0.0, category_bits=0x0001,
+                 mask_bits=0xFFFF, group_index=0, sensor=False, user_data=None, body=None):
+        if isinstance(shape, Loop):
+            raise NotImplementedError("Loop shapes are not supported by the GPU world step")
+        self._shape = shape
+        self.friction, self.restitution, self.density = float(friction), float(restitution), float(density)
+        self.category_bits, self.mask_bits, self.group_index = category_bits, mask_bits, group_index
+        self.sensor = bool(sensor)
+        self.user_data = user_data
+        self._body = None
+        self._slot = -1
+
+    def __copy__(self):
+        return Fixture(self._shape, self.friction, self.restitution, self.density, self.category_bits,
+                       self.mask_bits, self.group_index, self.sensor, self.user_data)
+
+    @property
+    def shape(self):
+        return self._shape
+
+    @property
+    def body(self):
+        return self._body
+
+    def _kwargs(self):
+        return dict(friction=self.friction, restitution=self.restitution, density=self.density,
+                    category=self.category_bits, mask=self.mask_bits, group=self.group_index, sensor=self.sensor)
+
+
+class Body:
+    """body.py: a rigid body of a World.  Properties read the device state."""
+
+    STATIC, DYNAMIC, KINEMATIC = abi.BODY_STATIC, abi.BODY_DYNAMIC, abi.BODY_KINEMATIC
+
+    def __init__(self, world, index, fixtures, user_data=None):
+        self._world = world
+        self._index = index
+        self.fixtures = fixtures
+        self.user_data = user_data
+
+    # -- record access
+    def _rec(self):
+        return self._world._body_record(self._index)
+
+    def _edit(self):
+        return self._world._body_record(self._index, write=True)
+
+    # -- read-only state
+    @property
+    def world(self):
+        return self._world
+
+    @property
+    def type(self):
+        return int(self._rec()["type"])
+
+    @property
+    def static(self):
+        return self.type == Body.STATIC
+
+    @property
+    def dynamic(self):
+        return self.type == Body.DYNAMIC
+
+    @property
+    def kinematic(self):
+        return self.type == Body.KINEMATIC
+
+    @property
+    def position(self):
+        r = self._rec()
+        return Vec2(r["px"], r["py"])
+
+    @position.setter
+    def position(self, pos):
+        self.transform = (pos, self.angle)
+
+    @property
+    def angle(self):
+        return float(self._rec()["a"])
+
+    @angle.setter
+    def angle(self, angle):
+        self.transform = (self.position, angle)
+
+    @property
+    def transform(self):
+        r = self._rec()
+        return (Vec2(r["px"], r["py"]), (float(r["qc"]), float(r["qs"])))
+
+    @transform.setter
+    def transform(self, position_angle):
+        self._world._check_unlocked()
+        pos, angle = position_angle
+        self._world._set_transform(self._index, (float(pos[0]), float(pos[1])), float(angle))
+
+    @property
+    def world_center(self):
+        r = self._rec()
+        return Vec2(r["cx"], r["cy"])
+
+    @property
+    def local_center(self):
+        r = self._rec()
+        return Vec2(r["lcx"], r["lcy"])
+
+    @property
+    def mass(self):
+        return float(self._rec()["mass"])
+
+    @property
+    def inertia(self):
+        """body.py: rotational inertia about the local origin."""
+        r = self._rec()
+        return float(r["I"]) + float(r["mass"]) * (float(r["lcx"]) ** 2 + float(r["lcy"]) ** 2)
+
+    @property
+    def linear_velocity(self):
+        r = self._rec()
+        return Vec2(r["vx"], r["vy"])
+
+    @linear_velocity.setter
+    def linear_velocity(self, v):
+        """body.py: static bodies ignore it; a non-zero velocity wakes the body."""
+        if self.type == Body.STATIC:
+            return
+        vx, vy = float(v[0]), float(v[1])
+        if vx * vx + vy * vy > 0.0:
+            self.awake = True
+        r = self._edit()
+        r["vx"], r["vy"] = vx, vy
+
+    @property
+    def angular_velocity(self):
+        return float(self._rec()["w"])
+
+    @angular_velocity.setter
+    def angular_velocity(self, w):
+        if self.type == Body.STATIC:
+            return
+        w = float(w)
+        if w * w > 0.0:
+            self.awake = True
+        self._edit()["w"] = w
+
+    @property
+    def awake(self):
+        return bool(self._rec()["flags"] & abi.BODY_AWAKE)
+
+    @awake.setter
+    def awake(self, awake):
+        """body.py:800-812"""
+        r = self._edit()
+        was = bool(r["flags"] & abi.BODY_AWAKE)
+        if awake:
+            if not was:
+                r["sleep_time"] = 0.0
+            r["flags"] |= abi.BODY_AWAKE
+        else:
+            r["sleep_time"] = 0.0
+            r["vx"] = r["vy"] = r["w"] = 0.0
+            r["fx"] = r["fy"] = r["torque"] = 0.0
+            r["flags"] &= np.uint32(0xFFFFFFFF ^ abi.BODY_AWAKE)
+
+    @property
+    def sleeping(self):
+        return not self.awake
+
+    @property
+    def bullet(self):
+        return bool(self._rec()["flags"] & abi.BODY_BULLET)
+
+    @bullet.setter
+    def bullet(self, flag):
+        r = self._edit()
+        r["flags"] = (r["flags"] | abi.BODY_BULLET) if flag else (r["flags"] & np.uint32(0xFFFFFFFF ^ abi.BODY_BULLET))
+
+    @property
+    def sleeping_allowed(self):
+        return bool(self._rec()["flags"] & abi.BODY_ALLOW_SLEEP)
+
+    @sleeping_allowed.setter
+    def sleeping_allowed(self, flag):
+        r = self._edit()
+        if flag:
+            r["flags"] |= abi.BODY_ALLOW_SLEEP
+        else:
+            r["flags"] &= np.uint32(0xFFFFFFFF ^ abi.BODY_ALLOW_SLEEP)
+            self.awake = True
+
+    @property
+    def active(self):
+        return bool(self._rec()["flags"] & abi.BODY_ACTIVE)
+
+    @property
+    def fixed_rotation(self):
+        return bool(self._rec()["flags"] & abi.BODY_FIXED_ROTATION)
+
+    @property
+    def linear_damping(self):
+        return float(self._rec()["linear_damping"])
+
+    @linear_damping.setter
+    def linear_damping(self, v):
+        self._edit()["linear_damping"] = float(v)
+
+    @property
+    def angular_damping(self):
+        return float(self._rec()["angular_damping"])
+
+    @angular_damping.setter
+    def angular_damping(self, v):
+        self._edit()["angular_damping"] = float(v)
+
+    @property
+    def gravity_scale(self):
+        return float(self._rec()["gravity_scale"])
+
+    @gravity_scale.setter
+    def gravity_scale(self, v):
+        self._edit()["gravity_scale"] = float(v)
+
+    @property
+    def force(self):
+        r = self._rec()
+        return Vec2(r["fx"], r["fy"])
+
+    @property
+    def torque(self):
+        return float(self._rec()["torque"])
+
+    # -- forces and impulses (body.py:477-545): dynamic bodies only, wake
+    def _wake_for_force(self):
+        if self.type != Body.DYNAMIC:
+            return False
+        if not self.awake:
+            self.awake = True
+        return True
+
+    def apply_force(self, force, point):
+        if not self._wake_for_force():
+            return
+        r = self._edit()
+        fx, fy = float(force[0]), float(force[1])
+        r["fx"], r["fy"] = r["fx"] + fx, r["fy"] + fy
+        dx, dy = float(point[0]) - float(r["cx"]), float(point[1]) - float(r["cy"])
+        r["torque"] = r["torque"] + (dx * fy - dy * fx)
+
+    def apply_force_to_center(self, force):
+        if not self._wake_for_force():
+            return
+        r = self._edit()
+        r["fx"], r["fy"] = r["fx"] + float(force[0]), r["fy"] + float(force[1])
+
+    def apply_torque(self, torque):
+        if not self._wake_for_force():
+            return
+        r = self._edit()
+        r["torque"] = r["torque"] + float(torque)
+
+    def apply_linear_impulse(self, impulse, point):
+        if not self._wake_for_force():
+            return
+        r = self._edit()
+        ix, iy = float(impulse[0]), float(impulse[1])
+        im = float(r["inv_mass"])
+        r["vx"], r["vy"] = r["vx"] + im * ix, r["vy"] + im * iy
+        dx, dy = float(point[0]) - float(r["cx"]), float(point[1]) - float(r["cy"])
+        r["w"] = r["w"] + float(r["inv_I"]) * (dx * iy - dy * ix)
+
+    def apply_angular_impulse(self, impulse):
+        if not self._wake_for_force():
+            return
+        r = self._edit()
+        r["w"] = r["w"] + float(r["inv_I"]) * float(impulse)
+
+    # -- fixtures (body.py:164-234)
+    def create_fixture(self, shape, friction=0.2, restitution=0.0, density=0.0, category_bits=0x0001,
+                       mask_bits=0xFFFF, group_index=0, sensor=False, user_data=None):
+        fx = Fixture(shape, friction, restitution, density, category_bits, mask_bits, group_index, sensor, user_data)
+        return self.attach_fixture(fx)
+
+    def attach_fixture(self, fixture):
+        self._world._check_unlocked()
+        if fixture._body is not None:
+            raise ValueError("Fixture is already attached to a body")
+        self._world._add_fixture(self, fixture)
+        return fixture
+
+    def create_circle_fixture(self, radius=0.2, position=(0, 0), **kwargs):
+        return self.create_fixture(Circle(radius, position), **kwargs)
+
+    def create_polygon_fixture(self, vertices=None, box=None, **kwargs):
+        return self.create_fixture(Polygon(vertices, box), **kwargs)
+
+    def create_edge_fixture(self, v1=None, v2=None, v0=None, v3=None, **kwargs):
+        return self.create_fixture(Edge(v1, v2, v0, v3), **kwargs)
+
+    def create_loop_fixture(self, vertices, *args, **kwargs):
+        raise NotImplementedError("Loop shapes are not supported by the GPU world step")
+
+    def __repr__(self):
+        return f"Body(index={self._index}, position={self.position}, angle={self.angle:g})"
+
+
+class Contact:
+    """A read-only view of one contact after a step (contact.py:55-87)."""
+
+    def __init__(self, world, rec):
+        self._rec = rec
+        self.fixture_a = world._fixture_at(int(rec["fixture_a"]))
+        self.fixture_b = world._fixture_at(int(rec["fixture_b"]))
+
+    touching = property(lambda self: bool(self._rec["flags"] & abi.C_TOUCHING))
+    enabled = property(lambda self: bool(self._rec["flags"] & abi.C_ENABLED))
+    point_count = property(lambda self: int(self._rec["m_point_count"]))
+    friction = property(lambda self: float(self._rec["friction"]))
+    restitution = property(lambda self: float(self._rec["restitution"]))
+
+    @property
+    def normal_impulses(self):
+        return [float(self._rec["p_ni"][k]) for k in range(self.point_count)]
+
+    @property
+    def tangent_impulses(self):
+        return [float(self._rec["p_ti"][k]) for k in range(self.point_count)]
+
+    @property
+    def local_normal(self):
+        return Vec2(self._rec["m_lnx"], self._rec["m_lny"])
+
+    @property
+    def local_point(self):
+        return Vec2(self._rec["m_lpx"], self._rec["m_lpy"])
+
+
+def _fixture_list(shapes, fixtures, shape_fixture):
+    """Body(shapes=..., fixtures=..., shape_fixture=...) of body.py:20-115."""
+    out = []
+    if shapes is not None:
+        if isinstance(shapes, Shape):
+            shapes = [shapes]
+        base = shape_fixture if shape_fixture is not None else Fixture()
+        for sh in shapes:
+            f = base.__copy__()
+            f._shape = sh
+            out.append(f)
+    if fixtures is not None:
+        if not isinstance(fixtures, (list, tuple)):
+            fixtures = [fixtures]
+        out.extend(f.__copy__() for f in fixtures)
+    return out
+
+
+class World:
+    """world.py:64-473 for the step path, advanced by the GPU library.
+
+    The host records (``abi.WORLD``/``BODY``/``FIXTURE``/``CONTACT`` arrays and
+    the pending move buffer) are the state between device round trips;
+    ``scenes.SceneBuilder`` supplies the reference's construction
+    arithmetic for new bodies and fixtures."""
+
+    def __init__(self, gravity=(0, -10), do_sleep=True, warm_starting=True, continuous_physics=True,
+                 sub_stepping=False, auto_clear_forces=True, contact_filter=None, precision="f64"):
+        if sub_stepping:
+            raise NotImplementedError("sub_stepping is not supported by the GPU world step")
+        if contact_filter is not None:
+            raise NotImplementedError("a custom contact filter cannot run inside the GPU step")
+        self._sb = SceneBuilder(gravity=gravity, do_sleep=do_sleep, warm_starting=warm_starting,
+                                continuous_physics=continuous_physics, auto_clear_forces=auto_clear_forces)
+        self._precision = precision
+        self._bodies: list[Body] = []
+        self._W = self._sb.world_record(0, 0, 0)
+        self._B = np.zeros(0, dtype=abi.BODY)
+        self._F = np.zeros(0, dtype=abi.FIXTURE)
+        self._C = np.zeros(0, dtype=abi.CONTACT)
+        self._M = np.zeros(0, dtype=np.int32)
+        self._gpu = None
+        self._host_fresh = True     # host records equal the device state
+        self._upload_bodies = False
+        self._locked = False
+        self._inv_dt0 = 0.0
+
+    # -- properties
+    @property
+    def gravity(self):
+        return Vec2(*self._sb.gravity)
+
+    @gravity.setter
+    def gravity(self, g):
+        self._check_unlocked()
+        self._structural()
+        self._sb.gravity = (float(g[0]), float(g[1]))
+
+    @property
+    def locked(self):
+        return self._locked
+
+    @property
+    def bodies(self):
+        return list(self._bodies)
+
+    @property
+    def body_count(self):
+        return len(self._bodies)
+
+    @property
+    def contacts(self):
+        self._materialise()
+        return [Contact(self, self._C[i]) for i in range(len(self._C))]
+
+    @property
+    def contact_count(self):
+        self._materialise()
+        return len(self._C)
+
+    def _check_unlocked(self):
+        if self._locked:
+            raise LockedError("the world is locked during a step")
+
+    # -- bodies
+    def create_body(self, body=None, **kwargs):
+        """world.py:208-224"""
+        self._check_unlocked()
+        if body is not None:
+            raise NotImplementedError("copying an existing Body is not supported; pass keyword arguments")
+        fixtures = _fixture_list(kwargs.pop("shapes", None), kwargs.pop("fixtures", None), kwargs.pop("shape_fixture", None))
+        user_data = kwargs.pop("user_data", None)
+        kwargs.pop("world", None)
+        btype = kwargs.pop("type", Body.STATIC)
+        self._structural()
+        n_moves0 = len(self._sb.moves)
+        bi = self._sb.create_body(btype, fixtures=[(f.shape, f._kwargs()) for f in fixtures], **kwargs)
+        rb, rf = self._sb.body_records(bi)
+        f0 = len(self._F)
+        rb["fixture_start"] = f0
+        self._B = np.concatenate([self._B, rb[None]])
+        self._F = np.concatenate([self._F, rf])
+        new_moves = [f0 + k for (b, k) in self._sb.moves[n_moves0:] if b == bi]
+        self._M = np.concatenate([self._M, np.array(new_moves, np.int32)]).astype(np.int32)
+        body = Body(self, bi, fixtures, user_data)
+        for k, f in enumerate(fixtures):
+            f._body, f._slot = body, k
+        self._bodies.append(body)
+        return body
+
+    def create_dynamic_body(self, body=None, **kwargs):
+        return self.create_body(body, type=Body.DYNAMIC, **kwargs)
+
+    def create_static_body(self, body=None, **kwargs):
+        return self.create_body(body, type=Body.STATIC, **kwargs)
+
+    def create_kinematic_body(self, body=None, **kwargs):
+        return self.create_body(body, type=Body.KINEMATIC, **kwargs)
+
+    def destroy_body(self, body):
+        """world.py:235-270: the body, its fixtures and their contacts leave the world."""
+        self._check_unlocked()
+        self._structural()
+        bi = body._index
+        B, F, C, M = self._B, self._F, self._C, self._M
+        f0, nfix = int(B[bi]["fixture_start"]), int(B[bi]["fixture_count"])
+        gone = lambda x: (x >= f0) & (x < f0 + nfix)   # noqa: E731
+        C = C[~(gone(C["fixture_a"]) | gone(C["fixture_b"]))].copy()
+        for key in ("fixture_a", "fixture_b"):
+            C[key] = np.where(C[key] >= f0 + nfix, C[key] - nfix, C[key])
+        M = M[~gone(M)]
+        M = np.where(M >= f0 + nfix, M - nfix, M).astype(np.int32)
+        F = np.delete(F, np.arange(f0, f0 + nfix))
+        F["body"] = np.where(F["body"] > bi, F["body"] - 1, F["body"])
+        B = np.delete(B, bi)
+        B["fixture_start"] = np.where(B["fixture_start"] > f0, B["fixture_start"] - nfix, B["fixture_start"])
+        self._B, self._F, self._C, self._M = B, F, C, M
+        self._sb.bodies.pop(bi)
+        self._sb.moves = [(b if b < bi else b - 1, k) for (b, k) in self._sb.moves if b != bi]
+        self._bodies.pop(bi)
+        for b in self._bodies[bi:]:
+            b._index -= 1
+        body._world = None
+
+    def clear_forces(self):
+        """world.py:356-369"""
+        self._check_unlocked()
+        self._materialise()
+        self._B["fx"] = self._B["fy"] = self._B["torque"] = 0.0
+        self._mark_bodies_edited()
+
+    # -- the step
+    def step(self, dt, vel_iters, pos_iters):
+        """world.py:307-354: one gb_batch_step of this world."""
+        self._check_unlocked()
+        self._sync_device()
+        self._locked = True
+        try:
+            self._gpu.step(float(dt), int(vel_iters), int(pos_iters), 1, launch_mode=1)
+        finally:
+            self._locked = False
+        if dt > 0.0:
+            self._inv_dt0 = 1.0 / dt
+        self._host_fresh = False
+        st = self._gpu.status()
+        if st[0]:
+            raise RuntimeError(f"GPU world step failed: status bits {int(st[0]):#x}")
+
+    # ---------------------------------------------------------------- internals
+    def _materialise(self):
+        """Download the device state into the host records (once per step)."""
+        if self._gpu is None or self._host_fresh:
+            return
+        self._B = self._gpu.bodies()
+        self._F["aabb"] = self._gpu.proxies()
+        self._C = self._gpu.contacts(0)
+        self._M = np.zeros(0, np.int32)
+        self._host_fresh = True
+
+    def _structural(self):
+        """The next step re-uploads the whole world from the host records."""
+        self._materialise()
+        if self._gpu is not None:
+            self._gpu.close()
+            self._gpu = None
+        self._upload_bodies = False
+
+    def _body_record(self, i, write=False):
+        self._materialise()
+        if write:
+            self._mark_bodies_edited()
+        return self._B[i]
+
+    def _mark_bodies_edited(self):
+        if self._gpu is not None:
+            self._upload_bodies = True
+
+    def _fixture_at(self, f):
+        bi = int(self._F[f]["body"])
+        return self._bodies[bi].fixtures[f - int(self._B[bi]["fixture_start"])]
+
+    def _sync_device(self):
+        if self._gpu is None:
+            W = self._sb.world_record(len(self._B), len(self._F), len(self._M))
+            W["contact_count"] = len(self._C)
+            W["inv_dt0"] = self._inv_dt0
+            self._gpu = self._make_batch(W, self._B, self._F, self._C, self._M)
+            self._host_fresh = True
+            self._upload_bodies = False
+        elif self._upload_bodies:
+            self._gpu.set_bodies(self._B)
+            self._upload_bodies = False
+
+    def _make_batch(self, W, B, F, C, M):
+        """The device batch holding this world (gb_batch_create)."""
+        from .gpu import GpuBatch
+        return GpuBatch(W, B, F, contacts=C if len(C) else None, precision=self._precision, moves=M)
+
+    def _add_fixture(self, body, fixture):
+        """body.py:185-214: the fixture joins the body, its proxy the move
+        buffer; a positive density resets the body's mass data."""
+        self._structural()
+        bi = body._index
+        b = self._sb.bodies[bi]
+        _load_body_state(b, self._B[bi])
+        self._sb.add_fixture(bi, fixture.shape, **fixture._kwargs())
+        rb, rf = self._sb.body_records(bi)
+        r = self._B[bi]
+        for key in ("lcx", "lcy", "c0x", "c0y", "cx", "cy", "vx", "vy", "mass", "inv_mass", "I", "inv_I"):
+            r[key] = rb[key]
+        pos = int(r["fixture_start"]) + len(body.fixtures)
+        self._F = np.insert(self._F, pos, rf[-1])
+        self._B["fixture_count"][bi] += 1
+        self._B["fixture_start"] = np.where(np.arange(len(self._B)) > bi, self._B["fixture_start"] + 1,
+                                            self._B["fixture_start"])
+        for key in ("fixture_a", "fixture_b"):
+            self._C[key] = np.where(self._C[key] >= pos, self._C[key] + 1, self._C[key])
+        M = np.where(self._M >= pos, self._M + 1, self._M)
+        self._M = np.concatenate([M, np.array([pos], np.int32)]).astype(np.int32)
+        fixture._body, fixture._slot = body, len(body.fixtures)
+        body.fixtures.append(fixture)
+
+    def _set_transform(self, bi, pos, angle):
+        """body.py:_transform_updated: new transform and sweep; the fixtures
+        are synchronised with zero displacement (fixture.py:287-298,
+        dynamictree.py:152-188) and re-fattened ones enter the move buffer."""
+        self._structural()
+        r = self._B[bi]
+        q = (math.cos(angle), math.sin(angle))
+        r["px"], r["py"], r["qc"], r["qs"] = pos[0], pos[1], q[0], q[1]
+        lcx, lcy = float(r["lcx"]), float(r["lcy"])
+        cx = pos[0] + q[0] * lcx + (-q[1]) * lcy
+        cy = pos[1] + q[1] * lcx + q[0] * lcy
+        r["c0x"], r["c0y"], r["cx"], r["cy"] = cx, cy, cx, cy
+        r["a0"] = r["a"] = angle
+        start = int(r["fixture_start"])
+        moved = []
+        for k, f in enumerate(self._sb.bodies[bi].fixtures):
+            tight = f.shape.compute_aabb(pos, q)
+            fat = tuple(float(x) for x in self._F[start + k]["aabb"])
+            if not _contains(fat, tight):
+                self._F[start + k]["aabb"] = (tight[0] - AABB_EXTENSION, tight[1] - AABB_EXTENSION,
+                                              tight[2] + AABB_EXTENSION, tight[3] + AABB_EXTENSION)
+                moved.append(start + k)
+        if moved:
+            self._M = np.concatenate([self._M, np.array(moved, np.int32)]).astype(np.int32)
+
+
+def _contains(fat, tight):
+    """AABB.contains (common.py): fat holds tight."""
+    return fat[0] <= tight[0] and fat[1] <= tight[1] and tight[2] <= fat[2] and tight[3] <= fat[3]
+
+
+def _load_body_state(b: _Body, r):
+    """Copy a body record into the construction-time body (for reset_mass_data)."""
+    b.p, b.q = (float(r["px"]), float(r["py"])), (float(r["qc"]), float(r["qs"]))
+    b.lc = (float(r["lcx"]), float(r["lcy"]))
+    b.c0, b.c = (float(r["c0x"]), float(r["c0y"])), (float(r["cx"]), float(r["cy"]))
+    b.a0, b.a, b.alpha0 = float(r["a0"]), float(r["a"]), float(r["alpha0"])
+    b.v, b.w = (float(r["vx"]), float(r["vy"])), float(r["w"])
+    b.force, b.torque = (float(r["fx"]), float(r["fy"])), float(r["torque"])
+    b.mass, b.inv_mass, b.I, b.invI = float(r["mass"]), float(r["inv_mass"]), float(r["I"]), float(r["inv_I"])
+    b.sleep_time = float(r["sleep_time"])
+    fl = int(r["flags"])
+    b.awake, b.allow_sleep, b.bullet = bool(fl & abi.BODY_AWAKE), bool(fl & abi.BODY_ALLOW_SLEEP), bool(fl & abi.BODY_BULLET)

@@ -373,6 +373,49 @@ def run_scene(b2, name, builder, n_steps, snaps, vel_iters=8, pos_iters=3, dt=1.
     print(f"{name}: {len(B)} bodies, {len(F)} fixtures, steps {n_steps} -> {os.path.getsize(path)} bytes")
 
 
+def pair_order_hook(world):
+    """update_pairs in the fixed order of install_hooks, with the fixture
+    numbering read at each call (the script adds and removes fixtures)."""
+    bp = world.contact_manager.broadphase
+
+    def update_pairs(self, callback=None):
+        fidx = fixture_index(world)
+        first = {}
+        for i, node in enumerate(self._move_buffer):
+            if node not in first:
+                first[node] = i
+        pairs = []
+        for node, pos in first.items():
+            for res in self._tree.query(node.aabb):
+                if res is node:
+                    continue
+                if res in first and first[res] < pos:
+                    continue
+                pairs.append((pos, fidx[id(res.user_data.fixture)], node, res))
+        self._move_buffer = []
+        pairs.sort(key=lambda t: (t[0], t[1]))
+        for _, _, a, b in pairs:
+            yield (a.user_data, b.user_data)
+
+    bp.update_pairs = types.MethodType(update_pairs, bp)
+
+
+def run_api_script(b2):
+    """tests/golden/api_script.py on the reference -> api_script.npz."""
+    sys.path.insert(0, HERE)
+    import api_script
+    out = {}
+
+    def snap(label, world):
+        W, B, F, C = export_world(world, b2)
+        out[f"{label}_bodies"], out[f"{label}_aabb"], out[f"{label}_contacts"] = B, F["aabb"].copy(), C
+
+    api_script.script(b2, snap, on_world=pair_order_hook)
+    path = os.path.join(HERE, "api_script.npz")
+    np.savez_compressed(path, **out)
+    print(f"api_script: {len(out) // 3} snapshots -> {os.path.getsize(path)} bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
@@ -383,6 +426,8 @@ def main():
         if args.only and name != args.only:
             continue
         run_scene(b2, name, builder, n, snaps)
+    if not args.only or args.only == "api_script":
+        run_api_script(b2)
 
 
 if __name__ == "__main__":

@@ -115,6 +115,10 @@ class OracleWorld:
         self.lib.or_get_contacts(self.h, out.ctypes.data, n)
         return out
 
+    def set_bodies(self, bodies):
+        b = np.ascontiguousarray(bodies, dtype=abi.BODY)
+        self.lib.or_set_bodies(self.h, b.ctypes.data)
+
     def solver_order(self):
         cap = max(16, 4 * self.lib.or_contact_count(self.h) + 16)
         out = np.zeros(cap, dtype=np.int32)
@@ -123,3 +127,37 @@ class OracleWorld:
 
     def status(self):
         return self.lib.or_status(self.h)
+
+
+class OracleBatch:
+    """The restatement behind the batch interface pypybox2d_gb300.World uses
+    (step / bodies / set_bodies / proxies / contacts / status), so the
+    World's host logic can be checked on the CPU.  Test infrastructure."""
+
+    def __init__(self, W, B, F, C, M, libm=False):
+        self.o = OracleWorld(W, B, F, C if len(C) else None, libm=libm, moves=M)
+
+    def step(self, dt, vel_iters, pos_iters, n_steps=1, **_):
+        for _ in range(n_steps):
+            self.o.step(dt, vel_iters, pos_iters)
+
+    def bodies(self):
+        return self.o.bodies()
+
+    def set_bodies(self, B):
+        self.o.set_bodies(B)
+
+    def proxies(self):
+        return self.o.fixtures()["aabb"].copy()
+
+    def contacts(self, world=0):
+        return self.o.contacts()
+
+    def contact_counts(self):
+        return np.array([len(self.o.contacts())], dtype=np.int32)
+
+    def status(self):
+        return np.array([self.o.status()], dtype=np.uint32)
+
+    def close(self):
+        pass
