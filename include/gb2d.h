@@ -83,6 +83,8 @@ extern "C" {
 #define GB_PREC_F64 0
 #define GB_PREC_F32 1
 
+#define GB_OPT_KERNEL_TIMES 4u   /* gb_step_opts.record_order bit: time each phased-step launch */
+
 /* error codes (also OR-ed into the per-world device status word) */
 #define GB_OK 0
 #define GB_E_ARG (-1)
@@ -192,7 +194,8 @@ typedef struct gb_step_opts {
     int32_t launch_mode;
     int32_t block_threads;
     int32_t record_order; /* bit 0: keep the solver constraint order of the last step;
-                             bit 1: accumulate per-phase SM clocks (gb_batch_phase_clocks) */
+                             bit 1: accumulate per-phase SM clocks (gb_batch_phase_clocks)
+                             bit 2: time every launch of the phased step (gb_batch_kernel_times) */
 } gb_step_opts;
 
 /* Library version and build information. */
@@ -237,6 +240,13 @@ int gb_batch_phase_clocks(gb_batch *batch, int64_t *clocks, void *cuda_stream);
 /* Counters: step launches so far, bytes of device memory held by the
  * batch, world-steps requested so far (3 int64). */
 int gb_batch_counters(gb_batch *batch, int64_t *counters);
+/* Device time of each launch of the phased step (launch_mode 3), summed over
+ * the steps run with GB_OPT_KERNEL_TIMES set: 12 slots, in launch order
+ * (new-fixture pairs, body prologue, contact update, contact update of
+ * sleeping pairs, islands and colouring, velocity integration, solver
+ * set-up, solver, fixture sync and pairs, TOI candidates, first-pass TOI,
+ * TOI event loop).  Measurement only: a timed step waits for its events. */
+int gb_batch_kernel_times(gb_batch *batch, double *total_ms, int32_t capacity, int32_t *n_slots, int64_t *n_steps);
 
 /* Size of the static device scratch of gb_batch_step_static_scratch (32 MiB). */
 #define GB_STATIC_SCRATCH_BYTES (32u << 20)

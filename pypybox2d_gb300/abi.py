@@ -145,8 +145,13 @@ EXPORTED = (
     "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_get_proxies",
     "gb_batch_get_contact_counts", "gb_batch_get_contacts", "gb_batch_get_solver_order",
     "gb_batch_status", "gb_batch_counters", "gb_batch_phase_clocks",
-    "gb_batch_step_static_scratch",
+    "gb_batch_step_static_scratch", "gb_batch_kernel_times",
 )
+
+#: gb_step_opts.record_order bit that times each launch of the phased step
+OPT_KERNEL_TIMES = 4
+KERNEL_SLOTS = ("pairs_new", "pre", "collide", "collide_sleeping", "islands", "vinit", "cinit", "solve",
+                "sync_pairs", "toi_candidates", "toi_first_pass", "toi_events")
 
 #: bytes of the static device scratch behind gb_batch_step_static_scratch
 STATIC_SCRATCH_BYTES = 32 << 20
@@ -188,6 +193,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_counters.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     lib.gb_batch_phase_clocks.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), vp]
     lib.gb_batch_step_static_scratch.argtypes = [vp, ctypes.POINTER(StepOpts), vp]
+    lib.gb_batch_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32, i32p, ctypes.POINTER(ctypes.c_int64)]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

@@ -125,6 +125,7 @@ struct gb_batch {
     gb_contact *d_cstage = nullptr;
     int cstage_cap = 0;
     long long counters[3] = {0, 0, 0};
+    KernelTimer *ktimer = nullptr;   // created by the first timed step
 };
 
 extern "C" {
@@ -302,6 +303,10 @@ int gb_batch_destroy(gb_batch *b) {
     cudaFree(b->d_worlds);
     cudaFree(b->d_bstage);
     cudaFree(b->d_cstage);
+    if (b->ktimer) {
+        for (int k = 0; k <= GB_NKTIME; ++k) cudaEventDestroy(b->ktimer->ev[k]);
+        delete b->ktimer;
+    }
     delete b;
     return 0;
 }
@@ -321,8 +326,17 @@ int gb_batch_step(gb_batch *b, const gb_step_opts *o, void *stream) {
     int mode = (o->launch_mode == 2 || o->launch_mode == 3) ? o->launch_mode : (o->launch_mode == 0 ? 3 : 1);
     int threads = o->block_threads > 0 ? o->block_threads : (mode == 2 ? 128 : 128);
     if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
-    int rc = b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st)
-                                    : gb_launch_step<float>(b->bf, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st);
+    KernelTimer *kt = nullptr;
+    if ((o->record_order & GB_OPT_KERNEL_TIMES) && mode == 3) {
+        if (!b->ktimer) {
+            b->ktimer = new KernelTimer();
+            memset(b->ktimer, 0, sizeof(KernelTimer));
+            for (int k = 0; k <= GB_NKTIME; ++k) CK(cudaEventCreate(&b->ktimer->ev[k]));
+        }
+        kt = b->ktimer;
+    }
+    int rc = b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st, kt)
+                                    : gb_launch_step<float>(b->bf, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st, kt);
     if (rc) return cuda_fail((cudaError_t)rc, "step launch");
     b->counters[0] += 1;
     b->counters[2] += o->n_steps;
@@ -434,6 +448,14 @@ int gb_batch_phase_clocks(gb_batch *b, int64_t *clocks, void *stream) {
     const long long *src = b->prec == GB_PREC_F64 ? b->bd.prof : b->bf.prof;
     CK(cudaMemcpyAsync(clocks, src, sizeof(long long) * (size_t)b->nw * GB_NPROF, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     CK(cudaStreamSynchronize((cudaStream_t)stream));
+    return 0;
+}
+
+int gb_batch_kernel_times(gb_batch *b, double *total_ms, int32_t capacity, int32_t *n_slots, int64_t *n_steps) {
+    if (!b || !total_ms || !n_slots || !n_steps) return fail(GB_E_ARG, "NULL argument");
+    *n_slots = GB_NKTIME;
+    *n_steps = b->ktimer ? b->ktimer->steps : 0;
+    for (int k = 0; k < GB_NKTIME && k < capacity; ++k) total_ms[k] = b->ktimer ? b->ktimer->total_ms[k] : 0.0;
     return 0;
 }
 

@@ -94,7 +94,7 @@ __global__ void k_pack_contacts(Batch<GB_REAL> B, gb_contact *dst, int base, int
 }  // namespace
 
 template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *d_worlds,
-                                        int n_list, int mode, int threads, cudaStream_t st) {
+                                        int n_list, int mode, int threads, cudaStream_t st, KernelTimer *kt) {
     if (n_list <= 0) return 0;
     // the step kernels use ~220 registers per thread: at most 256 threads per CTA
     if (threads > 256) threads = 256;
@@ -110,19 +110,45 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
                                                  (int)solve_smem);
             if (e != cudaSuccess) return (int)e;
         }
+        // kt: an event after every launch, the host accumulates the gaps
+        // (one host synchronisation per step, measurement only)
+        auto mark = [&](int k) { if (kt) cudaEventRecord(kt->ev[k], st); };
         for (int s = 0; s < n_steps; ++s) {
+            mark(0);
             k_world<GB_REAL, PH_PAIRS0><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            mark(1);
             if (nb) k_pre<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
+            mark(2);
             if (ns) k_collide<GB_REAL><<<gs, T, 0, st>>>(B, ns);
+            mark(3);
             k_world<GB_REAL, PH_COLLIDE2><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            mark(4);
             k_world<GB_REAL, PH_ISLANDS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            mark(5);
             if (nb) k_vinit<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
+            mark(6);
             if (ns) k_cinit<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
+            mark(7);
             k_world<GB_REAL, PH_SOLVE><<<n_list, threads, solve_smem, st>>>(B, sp, d_worlds);
+            mark(8);
             k_world<GB_REAL, PH_PAIRS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            mark(9);
             if (ns) k_toi1<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
+            mark(10);
             if (ns) k_toi1b<GB_REAL><<<152 * 4, 128, 0, st>>>(B);
+            mark(11);
             k_world_toi2<GB_REAL><<<n_list, 32, 0, st>>>(B, sp, d_worlds);
+            mark(12);
+            if (kt) {
+                cudaError_t e = cudaEventSynchronize(kt->ev[GB_NKTIME]);
+                if (e != cudaSuccess) return (int)e;
+                for (int k = 0; k < GB_NKTIME; ++k) {
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, kt->ev[k], kt->ev[k + 1]);
+                    kt->total_ms[k] += ms;
+                }
+                kt->steps += 1;
+            }
         }
         return (int)cudaGetLastError();
     }

@@ -4,16 +4,25 @@
 #include <cuda_runtime.h>
 #include "gb_world.cuh"
 
+// Phased-step kernel timing: GB_NKTIME launch slots, GB_NKTIME + 1 events.
+#define GB_NKTIME 12
+struct KernelTimer {
+    cudaEvent_t ev[GB_NKTIME + 1];
+    double total_ms[GB_NKTIME];
+    long long steps;
+};
 template <class R> int gb_launch_step(const Batch<R> &B, const StepParams &sp, int n_steps, const int *d_worlds, int n_list,
-                                      int mode, int threads, cudaStream_t st);
+                                      int mode, int threads, cudaStream_t st, KernelTimer *kt = nullptr);
 template <class R> void gb_launch_unpack_bodies(const Batch<R> &B, const gb_body *d, int n, cudaStream_t st);
 template <class R> void gb_launch_pack_bodies(const Batch<R> &B, gb_body *d, int n, cudaStream_t st);
 template <class R> void gb_launch_unpack_fixtures(const Batch<R> &B, const gb_fixture *d, int n, cudaStream_t st);
 template <class R> void gb_launch_unpack_contacts(const Batch<R> &B, const gb_contact *d, const int *slots, int n, cudaStream_t st);
 template <class R> void gb_launch_pack_contacts(const Batch<R> &B, gb_contact *d, int base, int n, cudaStream_t st);
 
-template <> int gb_launch_step<double>(const Batch<double> &, const StepParams &, int, const int *, int, int, int, cudaStream_t);
-template <> int gb_launch_step<float>(const Batch<float> &, const StepParams &, int, const int *, int, int, int, cudaStream_t);
+template <> int gb_launch_step<double>(const Batch<double> &, const StepParams &, int, const int *, int, int, int, cudaStream_t,
+                                       KernelTimer *);
+template <> int gb_launch_step<float>(const Batch<float> &, const StepParams &, int, const int *, int, int, int, cudaStream_t,
+                                      KernelTimer *);
 template <> void gb_launch_unpack_bodies<double>(const Batch<double> &, const gb_body *, int, cudaStream_t);
 template <> void gb_launch_unpack_bodies<float>(const Batch<float> &, const gb_body *, int, cudaStream_t);
 template <> void gb_launch_pack_bodies<double>(const Batch<double> &, gb_body *, int, cudaStream_t);

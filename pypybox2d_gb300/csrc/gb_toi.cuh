@@ -245,8 +245,37 @@ template <class R> __device__ __forceinline__ void toi_first_pass_contact(const 
     proc[i] = toi_of_contact(w, i) ? 1 : 0;
 }
 
+// Contacts that can take part in the TOI loop of this step: neither fixture
+// a sensor, a bullet or non-dynamic body on one side, not both bodies
+// static (toi_status's conditions that cannot change during the loop; the
+// awake, enabled and sub-step conditions are checked on every pass).
+template <class R> __device__ __forceinline__ bool toi_candidate(const WView<R> &w, int i) {
+    const ContactRec<R> &c = w.con(i);
+    if (fx_sensor(w, c.fa) || fx_sensor(w, c.fb)) return false;
+    int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+    int ta = w.btype(ba), tb = w.btype(bb);
+    if (ta == GB_BODY_STATIC && tb == GB_BODY_STATIC) return false;
+    bool col_a = (w.B.b_flags[w.bb + ba] & GB_BODY_BULLET) || ta != GB_BODY_DYNAMIC;
+    bool col_b = (w.B.b_flags[w.bb + bb] & GB_BODY_BULLET) || tb != GB_BODY_DYNAMIC;
+    return col_a || col_b;
+}
+
+// The contacts of dynamic body b in list order (Body._contacts): its
+// adjacency entries from the start of the loop, then the contacts created
+// since (indices >= nc0).  Calls fn(contact) in that order.
+template <class R, class F> __device__ __forceinline__ void body_contacts(const WView<R> &w, const int *off, const int *adj,
+                                                                         int nc0, int nc, int b, F fn) {
+    for (int e = off[b]; e < off[b + 1]; ++e) fn(adj[e]);
+    for (int i = nc0; i < nc; ++i) {
+        const ContactRec<R> &c = w.con(i);
+        if (w.fbody(c.fa) == b || w.fbody(c.fb) == b) fn(i);
+    }
+}
+
 // The event loop of world.py:612-821; `first_done` means pass 0 already ran
-// (in the batch-wide kernel).
+// (in the batch-wide kernel).  Passes scan the candidate list only, and the
+// contact lists of the event bodies come from a per-body adjacency built
+// once per step.
 template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh,
                                                      bool par_first, bool first_done, PhaseClock *pc = nullptr) {
     PhaseClock dummy;
@@ -254,18 +283,58 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
     PhaseClock &ck = pc ? *pc : dummy;
     int *proc = w.B.s_proc + w.cb;
     int *ids = w.B.s_pref + w.cb;
-    unsigned long long *red = &sh->red;
     TPlan *plan = w.B.s_plan + (size_t)w.wi * GB_TOI_PLAN_CAP;
     unsigned char *bflag = w.B.s_bvis + w.bb;
+    int *cand = w.B.s_cons_of + w.cb;                          // candidate contacts, list order
+    int *off = w.B.s_adjoff + w.bb + w.wi;                     // adjacency of dynamic bodies (nb + 1)
+    int *adj = reinterpret_cast<int *>(w.B.s_kb + w.cb);       // 2 ccap entries
+    int *cursor = w.B.s_seed + w.bb;
+    const int nb = w.H->nb;
+    const int nc0 = w.H->nc;
+    // adjacency: count, scan, scatter, sort each body's entries by index
+    for (int b = g.rank(); b < nb; b += g.size()) cursor[b] = 0;
+    g.sync();
+    for (int i = g.rank(); i < nc0; i += g.size()) {
+        const ContactRec<R> &c = w.con(i);
+        int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+        if (w.btype(ba) == GB_BODY_DYNAMIC) atomicAdd(&cursor[ba], 1);
+        if (w.btype(bb) == GB_BODY_DYNAMIC) atomicAdd(&cursor[bb], 1);
+    }
+    g.sync();
+    int tot = group_scan(g, nb, [&](int b) { return cursor[b]; }, off);
+    g.sync();
+    if (g.rank() == 0) off[nb] = tot;
+    for (int b = g.rank(); b < nb; b += g.size()) cursor[b] = off[b];
+    g.sync();
+    for (int i = g.rank(); i < nc0; i += g.size()) {
+        const ContactRec<R> &c = w.con(i);
+        int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+        if (w.btype(ba) == GB_BODY_DYNAMIC) adj[atomicAdd(&cursor[ba], 1)] = i;
+        if (w.btype(bb) == GB_BODY_DYNAMIC) adj[atomicAdd(&cursor[bb], 1)] = i;
+    }
+    g.sync();
+    for (int b = g.rank(); b < nb; b += g.size())
+        for (int e = off[b] + 1; e < off[b + 1]; ++e) {
+            int v = adj[e], j = e - 1;
+            while (j >= off[b] && adj[j] > v) { adj[j + 1] = adj[j]; --j; }
+            adj[j + 1] = v;
+        }
+    // candidates in list order
+    int ncand = group_scan(g, nc0, [&](int i) { return toi_candidate(w, i) ? 1 : 0; }, ids);
+    g.sync();
+    for (int i = g.rank(); i < nc0; i += g.size())
+        if (toi_candidate(w, i)) cand[ids[i]] = i;
+    g.sync();
     for (int pass = 0; pass < (1 << 20); ++pass) {
         const int nc = w.H->nc;
         if (pass == 0 && first_done) {
             // computed by the batch-wide first pass
         } else if (pass == 0 && par_first) {
-            for (int i = g.rank(); i < nc; i += g.size()) proc[i] = toi_of_contact(w, i) ? 1 : 0;
+            for (int k = g.rank(); k < ncand; k += g.size()) proc[cand[k]] = toi_of_contact(w, cand[k]) ? 1 : 0;
         } else {
             // statuses in parallel; the contacts needing a fresh TOI in list order
-            int nfresh = group_scan(g, nc, [&](int i) {
+            int nfresh = group_scan(g, ncand, [&](int k) {
+                int i = cand[k];
                 int st = toi_status(w, i);
                 proc[i] = st != 0 ? 1 : 0;
                 return st == 2 ? 1 : 0;
@@ -273,8 +342,10 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
             g.sync();
             if (nfresh > 0) {
                 int *fresh = w.B.s_adj + 2 * (size_t)w.cb;   // free during the TOI loop
-                for (int i = g.rank(); i < nc; i += g.size())
-                    if (proc[i] && !(w.con(i).flags & GB_C_TOI)) fresh[ids[i]] = i;
+                for (int k = g.rank(); k < ncand; k += g.size()) {
+                    int i = cand[k];
+                    if (proc[i] && !(w.con(i).flags & GB_C_TOI)) fresh[ids[k]] = i;
+                }
                 g.sync();
                 if (nfresh <= GB_TOI_PLAN_CAP) {
                     // the sweep alignment is order dependent and cheap: rank 0 replays
@@ -293,49 +364,35 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
             }
         }
         g.sync();
-        if (g.rank() == 0) { ck.mark(11); red[0] = dkey(1.0); sh->min_contact = GB_INF_IDX; }
-        g.sync();
-        for (int i = g.rank(); i < nc; i += g.size())
-            if (proc[i] && w.con(i).toi < 1.0) atomicMin(&red[0], dkey(w.con(i).toi));
-        g.sync();
-        double min_alpha = dkey_inv(red[0]);
-        for (int i = g.rank(); i < nc; i += g.size())
-            if (proc[i] && w.con(i).toi < 1.0 && w.con(i).toi == min_alpha) atomicMin(&sh->min_contact, i);
-        g.sync();
-        int mi = sh->min_contact;
+        if (g.rank() == 0) ck.mark(11);
+        // earliest event: lexicographic minimum of (toi, list position)
+        unsigned long long key = ~0ull;
+        int mi = GB_INF_IDX;
+        for (int k = g.rank(); k < ncand; k += g.size()) {
+            int i = cand[k];
+            double t = w.con(i).toi;
+            if (proc[i] && t < 1.0) {
+                unsigned long long kk = dkey(t);
+                if (kk < key || (kk == key && i < mi)) { key = kk; mi = i; }
+            }
+        }
+        g.argmin(key, mi);
+        const double min_alpha = mi == GB_INF_IDX ? 1.0 : dkey_inv(key);
         if (mi == GB_INF_IDX || (1.0 - (10.0 * GB_EPSILON)) < min_alpha) {
             if (g.rank() == 0) w.H->flags |= GB_W_STEP_COMPLETE;
             g.sync();
             break;
         }
-        // contact lists of the event's two bodies (Body._contacts), in parallel
+        // contact lists of the event's two bodies (Body._contacts)
         const ContactRec<R> &mc = w.con(mi);
         const int bia = w.fbody(mc.fa), bib = w.fbody(mc.fb);
         int *la = w.B.s_adj + 2 * (size_t)w.cb;
         int *lb = la + w.H->ccap;
-        int *pa_ = ids;
-        int na = group_scan(g, nc, [&](int i) {
-            const ContactRec<R> &c = w.con(i);
-            return (w.fbody(c.fa) == bia || w.fbody(c.fb) == bia) ? 1 : 0;
-        }, pa_);
-        g.sync();
-        for (int i = g.rank(); i < nc; i += g.size()) {
-            const ContactRec<R> &c = w.con(i);
-            if (w.fbody(c.fa) == bia || w.fbody(c.fb) == bia) la[pa_[i]] = i;
-        }
-        g.sync();
-        int nlb = group_scan(g, nc, [&](int i) {
-            const ContactRec<R> &c = w.con(i);
-            return (w.fbody(c.fa) == bib || w.fbody(c.fb) == bib) ? 1 : 0;
-        }, pa_);
-        g.sync();
-        for (int i = g.rank(); i < nc; i += g.size()) {
-            const ContactRec<R> &c = w.con(i);
-            if (w.fbody(c.fa) == bib || w.fbody(c.fb) == bib) lb[pa_[i]] = i;
-        }
-        g.sync();
         if (g.rank() == 0) {
             ck.mark(12);
+            int na = 0, nlb = 0;
+            if (w.btype(bia) == GB_BODY_DYNAMIC) body_contacts(w, off, adj, nc0, nc, bia, [&](int i) { la[na++] = i; });
+            if (w.btype(bib) == GB_BODY_DYNAMIC) body_contacts(w, off, adj, nc0, nc, bib, [&](int i) { lb[nlb++] = i; });
             sh->nmove = 0;
             toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh, la, na, lb, nlb);
             ck.mark(13);
@@ -344,16 +401,26 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
         // invalidate the TOIs of every contact of a displaced dynamic body and
         // clear the island marks (world.py:804-813)
         const int nisl = sh->nisland;
-        for (int i = g.rank(); i < nc; i += g.size()) {
-            ContactRec<R> &c = w.con(i);
-            int fa = w.fbody(c.fa), fbb = w.fbody(c.fb);
-            bool hit = (bflag[fa] && w.btype(fa) == GB_BODY_DYNAMIC) || (bflag[fbb] && w.btype(fbb) == GB_BODY_DYNAMIC);
-            if (hit) c.flags &= ~(GB_C_TOI | GB_C_ISLAND);
+        const int *isl = w.B.s_stack + w.bb;
+        for (int k = g.rank(); k < nisl; k += g.size()) {
+            int b = isl[k];
+            if (w.btype(b) != GB_BODY_DYNAMIC) continue;
+            body_contacts(w, off, adj, nc0, nc, b, [&](int i) { atomicAnd(&w.con(i).flags, ~(GB_C_TOI | GB_C_ISLAND)); });
         }
         g.sync();
-        for (int k = g.rank(); k < nisl; k += g.size()) bflag[w.B.s_stack[w.bb + k]] = 0;
+        for (int k = g.rank(); k < nisl; k += g.size()) bflag[isl[k]] = 0;
         g.sync();
         find_new_contacts(g, w, sh);
+        // new contacts join the candidate list (they follow every older one)
+        const int nc2 = w.H->nc;
+        if (nc2 > nc) {
+            int nnew = group_scan(g, nc2 - nc, [&](int k) { return toi_candidate(w, nc + k) ? 1 : 0; }, ids);
+            g.sync();
+            for (int k = g.rank(); k < nc2 - nc; k += g.size())
+                if (toi_candidate(w, nc + k)) { cand[ncand + ids[k]] = nc + k; proc[nc + k] = 0; }
+            ncand += nnew;
+            g.sync();
+        }
         if (g.rank() == 0) { ck.mark(14); if (ck.acc) ck.acc[15] += 1; }
     }
 }

@@ -150,6 +150,28 @@ struct GroupCta {
         __syncthreads();
         return base + x - v;
     }
+    // lexicographic minimum of (key, idx) over the group, returned to every
+    // thread (uses sm[0..3 * warps)).  Contains barriers.
+    __device__ void argmin(unsigned long long &key, int &idx) const {
+        int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long k2 = __shfl_xor_sync(0xffffffffu, key, o);
+            int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+            if (k2 < key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+        }
+        if (lane == 0) {
+            sm[3 * warp] = (int)(unsigned)(key & 0xffffffffull);
+            sm[3 * warp + 1] = (int)(unsigned)(key >> 32);
+            sm[3 * warp + 2] = idx;
+        }
+        __syncthreads();
+        for (int k = 0; k < nw; ++k) {
+            unsigned long long k2 = ((unsigned long long)(unsigned)sm[3 * k + 1] << 32) | (unsigned)sm[3 * k];
+            int i2 = sm[3 * k + 2];
+            if (k2 < key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+        }
+        __syncthreads();
+    }
 };
 
 struct GroupWarp {
@@ -168,6 +190,14 @@ struct GroupWarp {
         *total = __shfl_sync(0xffffffffu, x, 31);
         __syncwarp();
         return x - v;
+    }
+    __device__ void argmin(unsigned long long &key, int &idx) const {
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long k2 = __shfl_xor_sync(0xffffffffu, key, o);
+            int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+            if (k2 < key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+        }
+        __syncwarp();
     }
 };
 

@@ -40,8 +40,8 @@ class GpuBatch:
 
     def step(self, dt: float, vel_iters: int = 8, pos_iters: int = 3, n_steps: int = 1, launch_mode: int = 1,
              block_threads: int = 0, record_order: bool = False, stream: int | None = None,
-             profile: bool = False) -> None:
-        flags = (1 if record_order else 0) | (2 if profile else 0)
+             profile: bool = False, kernel_times: bool = False) -> None:
+        flags = (1 if record_order else 0) | (2 if profile else 0) | (abi.OPT_KERNEL_TIMES if kernel_times else 0)
         o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, flags)
         abi.check(self.lib.gb_batch_step(self.h, ctypes.byref(o), ctypes.c_void_p(stream or 0)))
 
@@ -92,6 +92,15 @@ class GpuBatch:
         out = np.zeros((self.n_worlds, 16), dtype=np.int64)
         abi.check(self.lib.gb_batch_phase_clocks(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), None))
         return out
+
+    def kernel_times(self) -> tuple[dict, int]:
+        """Summed device ms per phased-step launch slot and the number of
+        timed steps (steps run with kernel_times=True)."""
+        out = (ctypes.c_double * 16)()
+        n = ctypes.c_int32()
+        steps = ctypes.c_int64()
+        abi.check(self.lib.gb_batch_kernel_times(self.h, out, 16, ctypes.byref(n), ctypes.byref(steps)))
+        return {name: out[k] for k, name in enumerate(abi.KERNEL_SLOTS[:n.value])}, int(steps.value)
 
     def arena_bytes(self) -> int:
         c = (ctypes.c_int64 * 3)()
