@@ -113,6 +113,8 @@ template <class R> __global__ void k_toi1b(Batch<R> B) {
         const ContactRec<R> &c = w.con(i);
         int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
         toi_compute(w, i, 0.0, w.sweep(ba), w.sweep(bb));
+        const double toi = c.toi;
+        if (toi < 1.0) atomicMin(&B.hdr[w.wi].toimin, dkey(toi));
     }
 }
 
@@ -165,10 +167,18 @@ template <class R, int PH> __device__ __forceinline__ void world_phase(const Bat
         bool woke_any = (pf & P_WOKE) != 0;
         if ((pf & P_DEFERRED) && (pf & P_WOKE)) {
             // contacts between sleeping bodies, in list order: a body woken at
-            // position j makes the contacts after j active (sequential rule)
+            // position j makes the contacts after j active (sequential rule);
+            // the deferred contacts are listed in parallel first
+            int *pos = B.s_pref + w.cb;
+            int *dl = B.s_order + w.cb;
+            int nd = group_scan(g, H.nc, [&](int i) { return proc[i] == 0 ? 1 : 0; }, pos);
+            g.sync();
+            for (int i = g.rank(); i < H.nc; i += g.size())
+                if (proc[i] == 0) dl[pos[i]] = i;
+            g.sync();
             if (g.rank() == 0) {
-                for (int i = 0; i < H.nc; ++i) {
-                    if (proc[i] != 0) continue;
+                for (int k = 0; k < nd; ++k) {
+                    const int i = dl[k];
                     bool woke;
                     int r = collide_one(w, i, wake, &woke);
                     proc[i] = r;
@@ -208,17 +218,22 @@ template <class R, int PH> __device__ __forceinline__ void world_phase(const Bat
             if (g.rank() == 0) pc.mark(7);
         }
     } else if (PH == PH_PAIRS) {
+        if (g.rank() == 0) H.toimin = ~0ull;   // k_toi1b lowers it
         if (H.pflags & P_SOLVING) sync_pairs_group(g, w, sp, &sh);
     } else if (PH == PH_TOI2) {
         if ((H.flags & GB_W_CONTINUOUS) && sp.dt > 0.0) {
             const bool par_first = (H.flags & GB_W_STEP_COMPLETE) != 0;
-            if (par_first)   // island flags of the bodies (world.py:600-601)
-                for (int b = g.rank(); b < H.nb; b += g.size()) B.s_bvis[w.bb + b] = 0;
-            g.sync();
-            PhaseClock pc;
-            pc.acc = (sp.profile && g.rank() == 0) ? B.prof + (size_t)wi * GB_NPROF : nullptr;
-            pc.start();
-            toi_loop(g, w, sp, &sh, par_first, par_first, &pc);
+            // the batch-wide first pass found no event: the loop would end at once
+            const bool none = par_first && (H.toimin == ~0ull || (1.0 - (10.0 * GB_EPSILON)) < dkey_inv(H.toimin));
+            if (!none) {
+                if (par_first)   // island flags of the bodies (world.py:600-601)
+                    for (int b = g.rank(); b < H.nb; b += g.size()) B.s_bvis[w.bb + b] = 0;
+                g.sync();
+                PhaseClock pc;
+                pc.acc = (sp.profile && g.rank() == 0) ? B.prof + (size_t)wi * GB_NPROF : nullptr;
+                pc.start();
+                toi_loop(g, w, sp, &sh, par_first, par_first, &pc);
+            }
         }
         g.sync();
         if (g.rank() == 0 && sp.dt > 0.0) H.inv_dt0 = sp.inv_dt;

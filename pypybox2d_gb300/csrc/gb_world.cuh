@@ -54,6 +54,7 @@ struct WorldHdr {              // per-world scalars (device)
     int all_allow;             // every body allows sleep (island.py:168 reads one body's flag)
     uint32_t pflags;           // phase flags of the current step (P_*)
     int _pad;
+    unsigned long long toimin; // dkey of the earliest first-pass time of impact below 1 (~0: none)
 };
 
 template <class R> struct Batch {
