@@ -101,6 +101,7 @@ extern "C" {
 #define GB_ST_ITER_LIMIT 4u
 #define GB_ST_PAIR_OVERFLOW 8u
 #define GB_ST_TOI_ISLAND_CAP 16u
+#define GB_ST_WAIT_TIMEOUT 32u   /* a bounded wait for an in-kernel copy gave up */
 
 /* One rigid body: the state of pypybox2d.Body (body.py:46-84). */
 typedef struct gb_body {

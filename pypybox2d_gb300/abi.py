@@ -50,6 +50,7 @@ ST_NONFINITE = 2
 ST_ITER_LIMIT = 4
 ST_PAIR_OVERFLOW = 8
 ST_TOI_ISLAND_CAP = 16
+ST_WAIT_TIMEOUT = 32
 
 _BODY_FIELDS = [
     ("type", "<i4"), ("flags", "<u4"), ("fixture_start", "<i4"), ("fixture_count", "<i4"),

@@ -78,7 +78,9 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_colour = a.take<int>(ncap); B.s_order = a.take<int>(ncap); B.s_cons_of = a.take<int>(ncap);
     B.s_cvis = a.take<unsigned char>(ncap);
     B.s_kb = a.take<int2>(ncap);
-    B.s_cons = a.take<Cons<R>>(ncap);
+    B.s_cons = a.take<Cons<R>>((size_t)nw * GB_MAX_TOI_CONTACTS);
+    B.s_cv = a.take<ConsVel<R>>(ncap);
+    B.s_cp = a.take<ConsPos<R>>(ncap);
     B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
     B.order_out = a.take<int>(ncap);
     B.prof = a.take<long long>((size_t)nw * GB_NPROF);
@@ -103,7 +105,9 @@ template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb
     B.s_colour = a.take<int>(ncap); B.s_order = a.take<int>(ncap); B.s_cons_of = a.take<int>(ncap);
     B.s_cvis = a.take<unsigned char>(ncap);
     B.s_kb = a.take<int2>(ncap);
-    B.s_cons = a.take<Cons<R>>(ncap);
+    B.s_cons = a.take<Cons<R>>((size_t)nw * GB_MAX_TOI_CONTACTS);
+    B.s_cv = a.take<ConsVel<R>>(ncap);
+    B.s_cp = a.take<ConsPos<R>>(ncap);
     B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
@@ -233,12 +237,20 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         CK(cudaMemcpy(d_cw, cw.data(), sizeof(int) * b->ncap, cudaMemcpyHostToDevice));
     }
     {
-        // solver body cache: sized for the largest world, up to 2048 bodies (48 KiB)
-        int max_nb = 0;
-        for (int i = 0; i < b->nw; ++i) max_nb = std::max(max_nb, b->hdr[i].nb);
-        int cache = max_nb <= 2048 ? max_nb : 0;
-        b->bd.cache_bodies = cache;
-        b->bf.cache_bodies = cache;
+        // solver launches: worlds of GB_SOLVE_BIG_BODIES bodies or more (the
+        // front of the size-sorted list) run in the wide launch; each launch's
+        // shared-memory body cache fits its largest world, up to 2048 bodies
+        int nbig = 0, max_big = 0, max_small = 0;
+        for (int i : b->launch_order) {
+            int n = b->hdr[i].nb;
+            if (n >= GB_SOLVE_BIG_BODIES) { ++nbig; max_big = std::max(max_big, n); }
+            else max_small = std::max(max_small, n);
+        }
+        for (auto *B : {&b->bd.cache_bodies, &b->bf.cache_bodies}) *B = 0;
+        b->bd.n_big = b->bf.n_big = nbig;
+        b->bd.cache_big = b->bf.cache_big = max_big <= 2048 ? max_big : 0;
+        b->bd.cache_small = b->bf.cache_small = max_small;
+        b->bd.pipe_bufs = b->bf.pipe_bufs = GB_SOLVE_PIPE_BUFS;
     }
     CK(cudaMalloc((void **)&b->d_worlds, sizeof(int) * b->nw));
     CK(cudaMemcpy(b->d_worlds, b->launch_order.data(), sizeof(int) * b->nw, cudaMemcpyHostToDevice));

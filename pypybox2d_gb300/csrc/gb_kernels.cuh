@@ -103,11 +103,20 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
         // for the ordered parts (see gb_phases.cuh)
         const int nb = B.n_bodies, ns = B.n_slots, T = 256;
         const int gb = (nb + T - 1) / T, gs = (ns + T - 1) / T;
-        // the solve kernel stages each world's bodies in shared memory
-        const size_t solve_smem = (size_t)B.cache_bodies * GB_CACHE_BYTES_PER_BODY;
-        if (solve_smem > 48 * 1024) {
+        // the solve kernel stages each world's bodies in shared memory and
+        // streams its constraint records through chunk buffers; the largest
+        // worlds (first in the list) get a wider launch of their own
+        const int nbig = B.n_big < n_list ? B.n_big : n_list;
+        const int tbig = GB_SOLVE_BIG_THREADS;
+        Batch<GB_REAL> Bb = B, Bs = B;
+        Bb.cache_bodies = B.cache_big;
+        Bs.cache_bodies = B.cache_small;
+        const size_t smem_big = Bb.cache_bodies > 0 ? solve_smem_bytes<GB_REAL>(Bb.cache_bodies, tbig, B.pipe_bufs) : 0;
+        const size_t smem_small = Bs.cache_bodies > 0 ? solve_smem_bytes<GB_REAL>(Bs.cache_bodies, threads, B.pipe_bufs) : 0;
+        const size_t smem_max = smem_big > smem_small ? smem_big : smem_small;
+        if (smem_max > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(k_world<GB_REAL, PH_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)solve_smem);
+                                                 (int)smem_max);
             if (e != cudaSuccess) return (int)e;
         }
         // kt: an event after every launch, the host accumulates the gaps
@@ -129,7 +138,8 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
             mark(6);
             if (ns) k_cinit<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
             mark(7);
-            k_world<GB_REAL, PH_SOLVE><<<n_list, threads, solve_smem, st>>>(B, sp, d_worlds);
+            if (nbig > 0) k_world<GB_REAL, PH_SOLVE><<<nbig, tbig, smem_big, st>>>(Bb, sp, d_worlds);
+            if (n_list > nbig) k_world<GB_REAL, PH_SOLVE><<<n_list - nbig, threads, smem_small, st>>>(Bs, sp, d_worlds + nbig);
             mark(8);
             k_world<GB_REAL, PH_PAIRS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
             mark(9);

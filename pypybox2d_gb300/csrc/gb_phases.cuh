@@ -212,7 +212,7 @@ template <class R, int PH> __device__ __forceinline__ void world_phase(const Bat
             pc.acc = (sp.profile && g.rank() == 0) ? B.prof + (size_t)wi * GB_NPROF : nullptr;
             pc.start();
             extern __shared__ __align__(16) unsigned char gb_dyn_smem[];
-            BodyCache cache{H.nb <= B.cache_bodies ? gb_dyn_smem : nullptr};
+            BodyCache cache{H.nb <= B.cache_bodies ? gb_dyn_smem : nullptr, B.pipe_bufs};
             solve_group(g, w, sp, &pc, cache);
             sleep_group(g, w, sp);
             if (g.rank() == 0) pc.mark(7);

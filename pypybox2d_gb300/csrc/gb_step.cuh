@@ -13,6 +13,7 @@
 //   continuous ....... world.py:594-821, island.py:181-243, contact.py:866-933
 #pragma once
 #include "gb_world.cuh"
+#include "gb_tma.cuh"
 
 #define GB_MAX_TRANSLATION 2.0
 #define GB_MAX_TRANSLATION_SQR 4.0
@@ -28,7 +29,6 @@
 #define GB_AABB_EXTENSION 0.1
 #define GB_AABB_MULTIPLIER 2.0
 #define GB_MAX_SUB_STEPS 8
-#define GB_MAX_TOI_CONTACTS 32
 #define GB_INF_IDX 0x7fffffff
 
 #define R_SIM 1u      // island is simulated this step
@@ -950,14 +950,15 @@ template <class R, class G> __device__ void constraints_group(const G &g, const 
     for (int k = g.rank(); k < ncons; k += g.size()) {
         if (colour[k] < 0 || colour[k] >= ncol) continue;
         int pos = atomicAdd(&pref[colour[k]], 1);
-        cons[pos].cidx = kc[k];
-        cons[pos].root = kroot[k];
+        ConsPos<R> &cp = w.B.s_cp[w.cb + pos];
+        cp.cidx = kc[k];
+        cp.root = kroot[k];
     }
     if (g.rank() == 0) { w.H->last_ncons = coff[ncol]; w.H->last_ncolours = ncol; }
     g.sync();
     if (sp.record_order) {
         int *out = w.B.order_out + w.cb;
-        for (int k = g.rank(); k < w.H->last_ncons; k += g.size()) out[k] = cons[k].cidx;
+        for (int k = g.rank(); k < w.H->last_ncons; k += g.size()) out[k] = w.B.s_cp[w.cb + k].cidx;
     }
 }
 
@@ -985,155 +986,399 @@ template <class R> __device__ __forceinline__ void integrate_velocity_body(const
 // contact.py:375-496 for constraint k (positions before integration,
 // velocities after)
 template <class R> __device__ __forceinline__ void init_constraint(const WView<R> &w, int k, const StepParams &sp) {
-    Cons<R> &q = w.B.s_cons[w.cb + k];
-    int root = q.root;
-    build_cons(w, q, q.cidx, (w.H->flags & GB_W_WARM_STARTING) != 0, w.H->inv_dt0 * sp.dt);
-    q.root = root;
+    ConsPos<R> &cp = w.B.s_cp[w.cb + k];
+    Cons<R> q;
+    build_cons(w, q, cp.cidx, (w.H->flags & GB_W_WARM_STARTING) != 0, w.H->inv_dt0 * sp.dt);
     int ga = w.bb + q.ia, gbb = w.bb + q.ib;
     init_velocity(q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], w.B.b_v[ga], w.B.b_w[ga], w.B.b_v[gbb], w.B.b_w[gbb]);
+    ConsVel<R> v;
+    for (int j = 0; j < 2; ++j) {
+        v.ni[j] = j < q.mcount ? q.ni[j] : (R)0;
+        v.ti[j] = j < q.mcount ? q.ti[j] : (R)0;
+        v.rA[j] = j < q.npts ? q.rA[j] : mk<R>(0, 0);
+        v.rB[j] = j < q.npts ? q.rB[j] : mk<R>(0, 0);
+        v.nm[j] = j < q.npts ? q.nm[j] : (R)0;
+        v.tm[j] = j < q.npts ? q.tm[j] : (R)0;
+        v.bias[j] = j < q.npts ? q.bias[j] : (R)0;
+    }
+    v.ia = q.ia; v.ib = q.ib; v.npts = q.npts; v._pad = 0;
+    v.normal = q.normal;
+    v.friction = q.friction;
+    const bool two = q.npts == 2;
+    v.k11 = two ? q.k11 : (R)0; v.k12 = two ? q.k12 : (R)0; v.k22 = two ? q.k22 : (R)0;
+    v.nm11 = two ? q.nm11 : (R)0; v.nm12 = two ? q.nm12 : (R)0; v.nm22 = two ? q.nm22 : (R)0;
+    w.B.s_cv[w.cb + k] = v;
+    cp.ia = q.ia; cp.ib = q.ib;
+    cp.mcount = q.mcount; cp.mtype = q.mtype; cp._pad0 = 0; cp._pad1 = 0;
+    cp.lca = q.lca; cp.lcb = q.lcb; cp.ln = q.ln; cp.lp = q.lp;
+    cp.lpts[0] = q.mcount > 0 ? q.lpts[0] : mk<R>(0, 0);
+    cp.lpts[1] = q.mcount > 1 ? q.lpts[1] : mk<R>(0, 0);
+    cp.ra = q.ra; cp.rb = q.rb;
+}
+
+// The full constraint of the velocity passes from its record and the
+// bodies' inverse masses (the fields solve_velocity and warm_start read).
+template <class R> __device__ __forceinline__ Cons<R> vel_cons(const ConsVel<R> &v, R ma, R mb, R iA, R iB) {
+    Cons<R> q;
+    q.ia = v.ia; q.ib = v.ib; q.npts = v.npts;
+    q.ma = ma; q.mb = mb; q.iA = iA; q.iB = iB;
+    q.normal = v.normal; q.friction = v.friction;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        q.ni[j] = v.ni[j]; q.ti[j] = v.ti[j];
+        q.rA[j] = v.rA[j]; q.rB[j] = v.rB[j];
+        q.nm[j] = v.nm[j]; q.tm[j] = v.tm[j]; q.bias[j] = v.bias[j];
+    }
+    q.k11 = v.k11; q.k12 = v.k12; q.k22 = v.k22;
+    q.nm11 = v.nm11; q.nm12 = v.nm12; q.nm21 = v.nm12; q.nm22 = v.nm22;
+    return q;
+}
+// The fields solve_position reads.
+template <class R> __device__ __forceinline__ Cons<R> pos_cons(const ConsPos<R> &p, R ma, R mb, R iA, R iB) {
+    Cons<R> q;
+    q.ia = p.ia; q.ib = p.ib;
+    q.ma = ma; q.mb = mb; q.iA = iA; q.iB = iB;
+    q.mcount = p.mcount; q.mtype = p.mtype;
+    q.lca = p.lca; q.lcb = p.lcb; q.ln = p.ln; q.lp = p.lp;
+    q.lpts[0] = p.lpts[0]; q.lpts[1] = p.lpts[1];
+    q.ra = p.ra; q.rb = p.rb;
+    return q;
 }
 
 // Warm start, velocity iterations, impulse store, position integration,
 // position iterations and transform write-back (island.py:98-159).
-// Bodies of one world staged in shared memory for the solver passes:
-// velocities during the velocity iterations, then positions during the
-// position iterations (the same bytes, 24 per body).
+//
+// With a shared-memory cache (the phased solve kernel) the world's bodies
+// live in shared memory during the passes and the constraint records
+// stream through `nbuf` shared-memory buffers: the records of each colour
+// are cut into chunks of one record per thread, and one thread keeps
+// nbuf - 1 chunks of bulk copies (cp.async.bulk, completion on an mbarrier)
+// in flight ahead of the chunk being solved.  Without a cache every pass
+// reads the records and bodies from global memory.
 struct BodyCache {
     unsigned char *mem;   // nullptr: the passes read and write global memory
+    int nbuf;             // constraint chunk buffers after the bodies (0: none)
 };
-#define GB_CACHE_BYTES_PER_BODY 24
+// shared-memory bytes of the body cache and of one chunk buffer
+template <class R> __host__ __device__ constexpr int cache_bytes_per_body() {
+    return 2 * (int)sizeof(double) + (int)sizeof(double) + 2 * (int)sizeof(R) + 1;   // c, a, inverse masses, static flag
+}
+__host__ __device__ inline size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
+template <class R> __host__ __device__ inline size_t cache_body_bytes(int nb) {
+    return align128((size_t)nb * cache_bytes_per_body<R>());
+}
+template <class R> __host__ __device__ inline size_t chunk_buf_bytes(int threads) {
+    size_t a = sizeof(ConsVel<R>), b = sizeof(ConsPos<R>);
+    return align128((size_t)threads * (a > b ? a : b));
+}
+template <class R> __host__ inline size_t solve_smem_bytes(int nb, int threads, int nbuf) {
+    return cache_body_bytes<R>(nb) + (size_t)nbuf * chunk_buf_bytes<R>(threads) + 64;
+}
+#define GB_MAX_PIPE_BUFS 4
+#define GB_WAIT_POLLS (1 << 18)
+
+// Chunks of the colour-major records: start | count << 22, one per entry.
+template <class G> __device__ int chunk_table(const G &g, const int *coff, int ncol, int cap, int *tab, int lim, uint32_t *status) {
+    if (g.rank() == 0) {
+        int n = 0;
+        for (int cc = 0; cc < ncol; ++cc)
+            for (int s0 = coff[cc]; s0 < coff[cc + 1]; s0 += cap) {
+                int cnt = coff[cc + 1] - s0 < cap ? coff[cc + 1] - s0 : cap;
+                if (n < lim) tab[n++] = s0 | (cnt << 22);
+                else *status |= GB_ST_ITER_LIMIT;   // more chunks than slots: never past the world's scratch
+            }
+        tab[-1] = n;
+    }
+    g.sync();
+    int n = tab[-1];
+    g.sync();
+    return n;
+}
+
+// A run of chunk loads through the buffers: chunk q of the run goes to
+// buffer q % nbuf; rank 0 issues up to nbuf - 1 chunks ahead.
+struct ChunkPipe {
+    unsigned char *buf;
+    unsigned long long *bar;
+    size_t buf_bytes;
+    int nbuf;
+    unsigned parity;     // bit b: parity of the next completion of buffer b
+    int issued;          // chunks issued so far in this run
+};
+
+template <class G, class Rec> __device__ __forceinline__ void pipe_issue(const G &g, ChunkPipe &p, int q, const Rec *base,
+                                                                        const int *tab, int nch) {
+    if (g.rank() == 0) {
+        int e = tab[q % nch];
+        int s0 = e & ((1 << 22) - 1), cnt = e >> 22;
+        int b = q % p.nbuf;
+        unsigned bytes = (unsigned)(cnt * sizeof(Rec));
+        mbar_arrive_expect_tx(&p.bar[b], bytes);
+        bulk_load(p.buf + (size_t)b * p.buf_bytes, base + s0, bytes, &p.bar[b]);
+    }
+}
 
 template <class R, class G> __device__ void solve_group(const G &g, const WView<R> &w, const StepParams &sp, PhaseClock *pcp = nullptr,
-                                                        BodyCache cache = BodyCache{nullptr}) {
+                                                        BodyCache cache = BodyCache{nullptr, 0}) {
     PhaseClock dummy;
     dummy.acc = nullptr;
     PhaseClock &ck = pcp ? *pcp : dummy;
-    const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
+    const int nb = w.H->nb;
     int *parent = w.B.s_parent + w.bb;
     uint32_t *rootf = w.B.s_root + w.bb;
-    int *seed = w.B.s_seed + w.bb;
     unsigned long long *minsep = w.B.s_minsep + w.bb;
-    unsigned long long *minsleep = w.B.s_minsleep + w.bb;
-    unsigned long long *claim = w.B.s_claim + w.bb;
-    int *cons_of = w.B.s_cons_of + w.cb;
-    int *colour = w.B.s_colour + w.cb;
-    int *order = w.B.s_order + w.cb;
-    int *pref = w.B.s_pref + w.cb;
-    Cons<R> *cons = w.B.s_cons + w.cb;
     int *coff = w.B.s_proc + w.cb;
+    ConsVel<R> *cv = w.B.s_cv + w.cb;
+    ConsPos<R> *cpos = w.B.s_cp + w.cb;
     const double dt = sp.dt;
     const bool warm = (w.H->flags & GB_W_WARM_STARTING) != 0;
-    (void)nb; (void)nc; (void)nf; (void)parent; (void)rootf; (void)seed; (void)minsep; (void)minsleep; (void)claim;
-    (void)cons_of; (void)colour; (void)order; (void)pref; (void)cons; (void)coff; (void)dt; (void)warm;
-    // 6. warm start and velocity iterations, colour by colour
     const int ncol = w.H->last_ncolours;
     const int ncons = w.H->last_ncons;
-    // velocities: shared-memory copy (world-local index) or the batch arrays
+    const int rank = g.rank();
+    // 6. warm start and velocity iterations, colour by colour
+    // body views: shared memory (world-local index) or the batch arrays
+    const bool cached = cache.mem != nullptr;
     vec2<R> *vel = w.B.b_v + w.bb;
     R *om = w.B.b_w + w.bb;
-    if (cache.mem) {
-        vel = reinterpret_cast<vec2<R> *>(cache.mem);
-        om = reinterpret_cast<R *>(cache.mem + sizeof(vec2<R>) * (size_t)nb);
-        for (int b = g.rank(); b < nb; b += g.size()) { vel[b] = w.B.b_v[w.bb + b]; om[b] = w.B.b_w[w.bb + b]; }
+    const R *invm = w.B.b_inv_mass + w.bb;
+    const R *invi = w.B.b_inv_I + w.bb;
+    unsigned char *stat = nullptr;
+    vec2<double> *pc = w.B.b_c + w.bb;
+    double *pa = w.B.b_a + w.bb;
+    ChunkPipe pipe{nullptr, nullptr, 0, 0, 0u, 0};
+    if (cached) {
+        // layout: c[nb] (16) | a[nb] (8) | inverse mass, inertia (R) | static flag (1);
+        // the velocity passes keep v[nb], w[nb] in the c/a bytes
+        unsigned char *m = cache.mem;
+        pc = reinterpret_cast<vec2<double> *>(m);
+        pa = reinterpret_cast<double *>(m + 16 * (size_t)nb);
+        vel = reinterpret_cast<vec2<R> *>(m);
+        om = reinterpret_cast<R *>(m + sizeof(vec2<R>) * (size_t)nb);
+        R *im = reinterpret_cast<R *>(m + 24 * (size_t)nb);
+        R *ii = im + nb;
+        stat = reinterpret_cast<unsigned char *>(ii + nb);
+        invm = im; invi = ii;
+        for (int b = rank; b < nb; b += g.size()) {
+            vel[b] = w.B.b_v[w.bb + b]; om[b] = w.B.b_w[w.bb + b];
+            im[b] = w.B.b_inv_mass[w.bb + b]; ii[b] = w.B.b_inv_I[w.bb + b];
+            stat[b] = w.btype(b) == GB_BODY_STATIC ? 1 : 0;
+        }
+        if (cache.nbuf > 0) {
+            pipe.buf = m + cache_body_bytes<R>(nb);
+            pipe.buf_bytes = chunk_buf_bytes<R>(g.size());
+            pipe.nbuf = cache.nbuf;
+            pipe.bar = reinterpret_cast<unsigned long long *>(pipe.buf + (size_t)cache.nbuf * pipe.buf_bytes);
+            if (rank == 0) {
+                for (int b = 0; b < pipe.nbuf; ++b) mbar_init(&pipe.bar[b], 1);
+                fence_async_shared();
+            }
+        }
         g.sync();
     }
-    for (int it = (warm ? -1 : 0); it < sp.vel_iters; ++it) {
-        for (int cc = 0; cc < ncol; ++cc) {
-            int s0 = coff[cc], s1 = coff[cc + 1];
-            for (int j = s0 + g.rank(); j < s1; j += g.size()) {
-                Cons<R> q = cons[j];   // by value: independent loads, no aliasing reloads
-                vec2<R> va = vel[q.ia], vb = vel[q.ib];
-                R wa = om[q.ia], wb = om[q.ib];
-                if (it < 0) warm_start(q, va, wa, vb, wb);
+    auto is_static = [&](int b) { return stat ? stat[b] != 0 : w.btype(b) == GB_BODY_STATIC; };
+    bool failed = false;
+    if (pipe.nbuf > 0 && ncons > 0) {
+        int *tab = w.B.s_pref + w.cb + 1;   // chunk table (entry -1: its length)
+        const int nch = chunk_table(g, coff, ncol, g.size(), tab, w.H->ccap - 1, &w.H->status);
+        const int runs = sp.vel_iters + (warm ? 1 : 0);
+        const int total = runs * nch;
+        const int ahead = pipe.nbuf - 1;
+        // The bulk copies bring the read-only part of the records; the
+        // impulses, the one part the passes write, are loaded and stored by
+        // the thread that owns the record (thread r always solves record r
+        // of a chunk), one chunk ahead, so the copies never race with them.
+        R imp[4] = {(R)0, (R)0, (R)0, (R)0};
+        auto load_imp = [&](int q) {
+            const int e = tab[q % nch];
+            const int s0 = e & ((1 << 22) - 1), cnt = e >> 22;
+            if (rank < cnt) {
+                const ConsVel<R> &gr = cv[s0 + rank];
+                imp[0] = gr.ni[0]; imp[1] = gr.ni[1]; imp[2] = gr.ti[0]; imp[3] = gr.ti[1];
+            }
+        };
+        for (int q = 0; q < ahead && q < total; ++q) pipe_issue(g, pipe, q, cv, tab, nch);
+        if (total > 0) load_imp(0);
+        for (int q = 0; q < total; ++q) {
+            if (q + ahead < total) pipe_issue(g, pipe, q + ahead, cv, tab, nch);
+            const int b = q % pipe.nbuf;
+            bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
+            pipe.parity ^= 1u << b;
+            if (g.any(!ok)) { failed = true; break; }
+            const int e = tab[q % nch];
+            const int s0 = e & ((1 << 22) - 1), cnt = e >> 22;
+            const bool warm_pass = warm && q < nch;
+            if (rank < cnt) {
+                const ConsVel<R> &rec = reinterpret_cast<const ConsVel<R> *>(pipe.buf + (size_t)b * pipe.buf_bytes)[rank];
+                const int ia = rec.ia, ib = rec.ib;
+                Cons<R> k = vel_cons(rec, invm[ia], invm[ib], invi[ia], invi[ib]);
+                k.ni[0] = imp[0]; k.ni[1] = imp[1]; k.ti[0] = imp[2]; k.ti[1] = imp[3];
+                vec2<R> va = vel[ia], vb = vel[ib];
+                R wa = om[ia], wb = om[ib];
+                if (warm_pass) warm_start(k, va, wa, vb, wb);
                 else {
-                    solve_velocity(q, va, wa, vb, wb);
-                    cons[j].ni[0] = q.ni[0]; cons[j].ni[1] = q.ni[1];
-                    cons[j].ti[0] = q.ti[0]; cons[j].ti[1] = q.ti[1];
+                    solve_velocity(k, va, wa, vb, wb);
+                    ConsVel<R> &gr = cv[s0 + rank];
+                    gr.ni[0] = k.ni[0]; gr.ni[1] = k.ni[1]; gr.ti[0] = k.ti[0]; gr.ti[1] = k.ti[1];
                 }
                 // colour classes share no non-static body; static bodies keep v = 0
-                if (w.btype(q.ia) != GB_BODY_STATIC) { vel[q.ia] = va; om[q.ia] = wa; }
-                if (w.btype(q.ib) != GB_BODY_STATIC) { vel[q.ib] = vb; om[q.ib] = wb; }
+                if (!stat[ia]) { vel[ia] = va; om[ia] = wa; }
+                if (!stat[ib]) { vel[ib] = vb; om[ib] = wb; }
             }
+            if (q + 1 < total) load_imp(q + 1);   // after this thread's own stores
             g.sync();
         }
+    } else if (!failed) {
+        for (int it = (warm ? -1 : 0); it < sp.vel_iters; ++it) {
+            for (int cc = 0; cc < ncol; ++cc) {
+                int s0 = coff[cc], s1 = coff[cc + 1];
+                for (int j = s0 + rank; j < s1; j += g.size()) {
+                    const ConsVel<R> rec = cv[j];
+                    const int ia = rec.ia, ib = rec.ib;
+                    Cons<R> k = vel_cons(rec, invm[ia], invm[ib], invi[ia], invi[ib]);
+                    vec2<R> va = vel[ia], vb = vel[ib];
+                    R wa = om[ia], wb = om[ib];
+                    if (it < 0) warm_start(k, va, wa, vb, wb);
+                    else {
+                        solve_velocity(k, va, wa, vb, wb);
+                        cv[j].ni[0] = k.ni[0]; cv[j].ni[1] = k.ni[1];
+                        cv[j].ti[0] = k.ti[0]; cv[j].ti[1] = k.ti[1];
+                    }
+                    if (!is_static(ia)) { vel[ia] = va; om[ia] = wa; }
+                    if (!is_static(ib)) { vel[ib] = vb; om[ib] = wb; }
+                }
+                g.sync();
+            }
+        }
     }
-    if (cache.mem) {
-        for (int b = g.rank(); b < nb; b += g.size()) { w.B.b_v[w.bb + b] = vel[b]; w.B.b_w[w.bb + b] = om[b]; }
+    if (failed) {
+        if (rank == 0) w.H->status |= GB_ST_WAIT_TIMEOUT;
+        // let the copies still in flight land before the buffers are released
+        if (rank == 0)
+            for (int b = 0; b < pipe.nbuf; ++b) mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
+        g.sync();
+        return;
+    }
+    if (cached) {
+        for (int b = rank; b < nb; b += g.size()) { w.B.b_v[w.bb + b] = vel[b]; w.B.b_w[w.bb + b] = om[b]; }
         g.sync();
     }
-    if (g.rank() == 0) { ck.mark(4); if (ck.acc) ck.acc[10] += ncol; }
+    if (rank == 0) { ck.mark(4); if (ck.acc) ck.acc[10] += ncol; }
     // 7. store impulses (contact.py:801-806)
-    for (int k = g.rank(); k < ncons; k += g.size()) {
-        const Cons<R> &q = cons[k];
-        ContactRec<R> &c = w.con(q.cidx);
-        for (int j = 0; j < q.npts && j < c.m.count; ++j) { c.m.ni[j] = q.ni[j]; c.m.ti[j] = q.ti[j]; }
+    for (int k = rank; k < ncons; k += g.size()) {
+        const ConsVel<R> &v = cv[k];
+        ContactRec<R> &c = w.con(cpos[k].cidx);
+        for (int j = 0; j < v.npts && j < c.m.count; ++j) { c.m.ni[j] = v.ni[j]; c.m.ti[j] = v.ti[j]; }
     }
     // 8. integrate positions (island.py:120-138)
-    for (int b = g.rank(); b < nb; b += g.size()) {
+    for (int b = rank; b < nb; b += g.size()) {
         if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
         int gb = w.bb + b;
         vec2<R> v = w.B.b_v[gb];
-        R om = w.B.b_w[gb];
+        R omg = w.B.b_w[gb];
         const R dtr = (R)dt;
         vec2<R> tr = dtr * v;
         if (dot(tr, tr) > (R)GB_MAX_TRANSLATION_SQR) {
             R ratio = (R)GB_MAX_TRANSLATION / len(tr);
             v = ratio * v;
         }
-        R rotation = dtr * om;
+        R rotation = dtr * omg;
         if (sq(rotation) > (R)GB_MAX_ROTATION_SQR) {
             R ratio = (R)GB_MAX_ROTATION / fabs(rotation);
-            om = om * ratio;
+            omg = omg * ratio;
         }
         w.B.b_c[gb] = w.B.b_c[gb] + cvt<double>(dtr * v);
-        w.B.b_a[gb] = w.B.b_a[gb] + (double)(dtr * om);
-        w.B.b_v[gb] = v; w.B.b_w[gb] = om;
+        w.B.b_a[gb] = w.B.b_a[gb] + (double)(dtr * omg);
+        w.B.b_v[gb] = v; w.B.b_w[gb] = omg;
     }
     g.sync();
-    if (g.rank() == 0) ck.mark(5);
+    if (rank == 0) ck.mark(5);
     // 9. position iterations with the per-island early exit (island.py:141-153)
-    vec2<double> *pc = w.B.b_c + w.bb;
-    double *pa = w.B.b_a + w.bb;
-    if (cache.mem) {
-        pc = reinterpret_cast<vec2<double> *>(cache.mem);
-        pa = reinterpret_cast<double *>(cache.mem + sizeof(vec2<double>) * (size_t)nb);
-        for (int b = g.rank(); b < nb; b += g.size()) { pc[b] = w.B.b_c[w.bb + b]; pa[b] = w.B.b_a[w.bb + b]; }
+    if (cached) {
+        for (int b = rank; b < nb; b += g.size()) { pc[b] = w.B.b_c[w.bb + b]; pa[b] = w.B.b_a[w.bb + b]; }
         g.sync();
     }
-    for (int it = 0; it < sp.pos_iters; ++it) {
-        for (int b = g.rank(); b < nb; b += g.size()) minsep[b] = dkey(0.0);
-        g.sync();
-        for (int cc = 0; cc < ncol; ++cc) {
-            int s0 = coff[cc], s1 = coff[cc + 1];
-            for (int j = s0 + g.rank(); j < s1; j += g.size()) {
-                const Cons<R> q = cons[j];
-                if (rootf[q.root] & R_DONE) continue;
-                vec2<double> ca = pc[q.ia], cb = pc[q.ib];
-                double aa = pa[q.ia], ab = pa[q.ib];
-                double ms = solve_position(q, ca, aa, cb, ab, 0.0, false, false, false);
-                atomicMin(&minsep[q.root], dkey(ms));
-                if (w.btype(q.ia) != GB_BODY_STATIC) { pc[q.ia] = ca; pa[q.ia] = aa; }
-                if (w.btype(q.ib) != GB_BODY_STATIC) { pc[q.ib] = cb; pa[q.ib] = ab; }
-            }
-            g.sync();
-        }
+    auto pos_one = [&](const ConsPos<R> &rec) {
+        if (rootf[rec.root] & R_DONE) return;
+        const int ia = rec.ia, ib = rec.ib;
+        Cons<R> k = pos_cons(rec, invm[ia], invm[ib], invi[ia], invi[ib]);
+        vec2<double> ca = pc[ia], cb = pc[ib];
+        double aa = pa[ia], ab = pa[ib];
+        double ms = solve_position(k, ca, aa, cb, ab, 0.0, false, false, false);
+        atomicMin(&minsep[rec.root], dkey(ms));
+        if (!is_static(ia)) { pc[ia] = ca; pa[ia] = aa; }
+        if (!is_static(ib)) { pc[ib] = cb; pa[ib] = ab; }
+    };
+    auto pos_check = [&]() {
         bool pending = false;
-        for (int b = g.rank(); b < nb; b += g.size()) {
+        for (int b = rank; b < nb; b += g.size()) {
             if (parent[b] != b || !(rootf[b] & R_SIM) || (rootf[b] & R_DONE)) continue;
             if (w.btype(b) == GB_BODY_STATIC) continue;
             if (dkey_inv(minsep[b]) >= -3.0 * GB_LINEAR_SLOP) rootf[b] |= R_DONE | R_SOLVED;
             else pending = true;
         }
-        if (!g.any(pending)) break;
+        return g.any(pending);
+    };
+    if (pipe.nbuf > 0 && ncons > 0 && sp.pos_iters > 0) {
+        int *tab = w.B.s_pref + w.cb + 1;
+        const int nch = tab[-1];
+        const int total = sp.pos_iters * nch;
+        const int ahead = pipe.nbuf - 1;
+        int issued = 0;
+        for (; issued < ahead && issued < total; ++issued) pipe_issue(g, pipe, issued, cpos, tab, nch);
+        int q = 0;
+        for (int it = 0; it < sp.pos_iters && !failed; ++it) {
+            for (int b = rank; b < nb; b += g.size()) minsep[b] = dkey(0.0);
+            g.sync();
+            for (int j = 0; j < nch; ++j, ++q) {
+                if (issued < total && issued <= q + ahead) { pipe_issue(g, pipe, issued, cpos, tab, nch); ++issued; }
+                const int b = q % pipe.nbuf;
+                bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
+                pipe.parity ^= 1u << b;
+                if (g.any(!ok)) { failed = true; break; }
+                const int e = tab[j];
+                const int cnt = e >> 22;
+                if (rank < cnt) pos_one(reinterpret_cast<const ConsPos<R> *>(pipe.buf + (size_t)b * pipe.buf_bytes)[rank]);
+                g.sync();
+            }
+            if (failed) break;
+            if (!pos_check()) break;
+        }
+        // drain the chunks issued past an early exit
+        for (; q < issued; ++q) {
+            const int b = q % pipe.nbuf;
+            bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
+            pipe.parity ^= 1u << b;
+            if (!ok) failed = true;
+        }
+        failed = g.any(failed);
+        if (failed) {
+            if (rank == 0) w.H->status |= GB_ST_WAIT_TIMEOUT;
+            g.sync();
+            return;
+        }
+    } else {
+        for (int it = 0; it < sp.pos_iters; ++it) {
+            for (int b = rank; b < nb; b += g.size()) minsep[b] = dkey(0.0);
+            g.sync();
+            for (int cc = 0; cc < ncol; ++cc) {
+                int s0 = coff[cc], s1 = coff[cc + 1];
+                for (int j = s0 + rank; j < s1; j += g.size()) {
+                    const ConsPos<R> rec = cpos[j];
+                    pos_one(rec);
+                }
+                g.sync();
+            }
+            if (!pos_check()) break;
+        }
     }
     g.sync();
-    if (cache.mem) {
-        for (int b = g.rank(); b < nb; b += g.size()) { w.B.b_c[w.bb + b] = pc[b]; w.B.b_a[w.bb + b] = pa[b]; }
+    if (cached) {
+        for (int b = rank; b < nb; b += g.size()) { w.B.b_c[w.bb + b] = pc[b]; w.B.b_a[w.bb + b] = pa[b]; }
         g.sync();
     }
-    if (g.rank() == 0) ck.mark(6);
+    if (rank == 0) ck.mark(6);
     // 10. write back the transforms of the island bodies (island.py:156-159)
-    for (int b = g.rank(); b < nb; b += g.size()) {
+    for (int b = rank; b < nb; b += g.size()) {
         if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
         sync_transform(w, b);
     }

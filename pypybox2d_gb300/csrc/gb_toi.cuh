@@ -86,7 +86,7 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
     vec2<R> vv[2 * GB_MAX_TOI_CONTACTS];
     R ww[2 * GB_MAX_TOI_CONTACTS];
     int idx[2 * GB_MAX_TOI_CONTACTS][2];
-    Cons<R> *ks = w.B.s_cons + w.cb;
+    Cons<R> *ks = w.B.s_cons + (size_t)w.wi * GB_MAX_TOI_CONTACTS;
     for (int i = 0; i < nbi; ++i) {
         int g = w.bb + ib[i];
         pc[i] = w.B.b_c[g]; pa[i] = w.B.b_a[g]; vv[i] = w.B.b_v[g]; ww[i] = w.B.b_w[g];

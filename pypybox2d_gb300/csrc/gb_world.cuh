@@ -42,6 +42,26 @@ template <class R> struct Cons {
     vec2<R> ln, lp, lpts[2];
 };
 
+// The solver's constraint records, stored colour-major.  ConsVel holds what
+// the warm start and the velocity iterations read (the impulses first: the
+// only fields they write back); ConsPos what the position iterations and
+// the impulse store read.  The inverse masses come from the bodies.  Both
+// are multiples of 16 bytes so a run of records moves as one bulk copy.
+template <class R> struct __align__(16) ConsVel {
+    R ni[2], ti[2];
+    int ia, ib, npts, _pad;
+    vec2<R> normal;
+    vec2<R> rA[2], rB[2];
+    R nm[2], tm[2], bias[2];
+    R friction, k11, k12, k22, nm11, nm12, nm22;   // inverse K is symmetric: nm21 = nm12
+};
+template <class R> struct __align__(16) ConsPos {
+    int cidx, ia, ib, root;
+    int mcount, mtype, _pad0, _pad1;
+    vec2<R> lca, lcb, ln, lp, lpts[2];
+    R ra, rb;
+};
+
 struct WorldHdr {              // per-world scalars (device)
     int nb, nf, nc, ccap;      // counts, contact capacity
     int bbase, fbase, cbase;   // batch bases
@@ -60,6 +80,9 @@ struct WorldHdr {              // per-world scalars (device)
 template <class R> struct Batch {
     int n_worlds, n_bodies, n_slots;
     int cache_bodies;         // worlds of at most this many bodies are solved from shared memory
+    int pipe_bufs;            // solver: constraint chunk buffers in shared memory (0: read global memory)
+    int n_big;                // worlds solved by the wide launch (the first n_big of the size-sorted list)
+    int cache_big, cache_small;   // body capacity of the solver's shared memory in the two launches
     WorldHdr *hdr;
     int *b_world;             // world of each body
     int *c_world;             // world of each contact slot
@@ -90,7 +113,9 @@ template <class R> struct Batch {
     int *s_proc, *s_pref, *s_adj, *s_colour, *s_order, *s_cons_of;
     int2 *s_kb;
     unsigned char *s_cvis;
-    Cons<R> *s_cons;
+    Cons<R> *s_cons;             // GB_MAX_TOI_CONTACTS per world: the TOI sub-island solver
+    ConsVel<R> *s_cv;            // colour-major solver records (contact capacity per world)
+    ConsPos<R> *s_cp;
     unsigned long long *s_hash;  // 4 * ccap slots per world (a power of two >= 2*ccap fits)
     int *order_out;              // recorded solver order (contact positions), ccap per world
     long long *prof;             // per-world phase clocks (GB_NPROF per world), when profiling
@@ -99,6 +124,10 @@ template <class R> struct Batch {
     int *toi_n;                  // their count
 };
 #define GB_NPROF 16
+#define GB_SOLVE_BIG_BODIES 512    // worlds this large are solved by the wide launch
+#define GB_SOLVE_BIG_THREADS 128
+#define GB_SOLVE_PIPE_BUFS 2       // constraint chunk buffers of the solver
+#define GB_MAX_TOI_CONTACTS 32     // contacts of one TOI sub-island
 #define GB_TOI_PLAN_CAP 64
 // A TOI computation prepared by the order-dependent sweep alignment.
 struct TPlan { double alpha0; Sweep sa, sb; };

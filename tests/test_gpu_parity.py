@@ -86,3 +86,20 @@ def test_warp_mapping_matches_cta_mapping():
         out.append(g.bodies())
     for o in out[1:]:
         assert_same(o, out[0], "mapping")
+
+
+@pytest.mark.parametrize("n_bodies", [700])
+def test_f64_large_world_bit_exact_with_oracle(n_bodies):
+    """A world large enough for the wide solver launch (512 bodies or more):
+    100 lock steps of an uneven-workload world against the oracle."""
+    from pypybox2d_gb300 import scenes
+    GpuBatch = _gpu()
+    W, B, F, M = scenes.uneven_world(5, n_bodies)
+    gpu = GpuBatch(W, B, F, precision="f64", moves=M)
+    orc = oracle_lib.OracleWorld(W, B, F, libm=False, moves=M)
+    for s in range(1, 101):
+        gpu.step(1 / 60, 8, 3, 1, launch_mode=3, block_threads=64, record_order=True)
+        orc.step(1 / 60, 8, 3, order=gpu.solver_order(0))
+        assert_same(gpu.bodies(), orc.bodies(), f"large world step {s} bodies")
+        assert_same(used_contact_view(gpu.contacts(0)), used_contact_view(orc.contacts()), f"large world step {s} contacts")
+    assert int(gpu.status()[0]) == 0
