@@ -9,7 +9,7 @@ Workloads (``--workload``):
            every box position jittered by a seeded U(-0.01, 0.01) m; 2000 steps.
 Both: dt = 1/60, 8 velocity and 3 position iterations, float32 bulk
 arithmetic with float64 positions, angles, sleep timers and time of impact,
-the 12-launch phased step on one stream.  A "step" is one World.step of
+the 12-13-launch phased step on one stream.  A "step" is one World.step of
 every world of the batch.
 
 Reported (one JSON line on rank 0):
@@ -161,6 +161,13 @@ def solve_bytes_per_step(n_bodies, n_constraints, real_bytes=4):
     solver record read (216 B in float32) and its impulses written back to
     the record and to the contact (32 B)."""
     return n_bodies * (6 * real_bytes + 48 + 16) + n_constraints * (216 + 32)
+
+
+def launches_per_step(W):
+    """Kernel launches of one phased step: 12, plus a second solver launch
+    when the batch mixes worlds below and above 512 bodies."""
+    nbig = int(np.count_nonzero(W["body_count"] >= 512))
+    return 12 + (1 if 0 < nbig < len(W) else 0)
 
 
 def world_slice(W, B, F, M, w):
@@ -424,17 +431,18 @@ def main():
                    "bodies_per_world": {"min": int(dyn.min()), "mean": float(dyn.mean()), "max": int(dyn.max())},
                    "launch": {1: "one persistent launch per timed region, one CTA per world",
                               2: "one persistent launch per timed region, one warp per world",
-                              3: "12 launches per step (batch-wide + per-world)"}[args.mode],
+                              3: f"{launches_per_step(W)} launches per step (batch-wide + per-world)"}[args.mode],
                    "block_threads": args.threads,
                    "l2": f"inputs larger than L2: {batch.arena_bytes() / 2**30:.2f} GiB resident per GPU",
                    "mean_contacts_per_world": float(np.mean(counts))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "whole step (12 launches)",
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": f"whole step ({launches_per_step(W)} launches)",
                      "algorithmic_bytes_per_step": bytes_step},
         "kernels": kernels,
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY.itemsize,
                 "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": args.e2e_steps},
-        "gpu_launches": 12 * steps if args.mode == 3 else 1,
+        "gpu_launches": launches_per_step(W) * steps if args.mode == 3 else 1,
         "clocks": clocks.summary(),
         "status_nonzero_worlds": int(np.count_nonzero(status)),
     }

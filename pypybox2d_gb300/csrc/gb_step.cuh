@@ -1146,6 +1146,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     vec2<double> *pc = w.B.b_c + w.bb;
     double *pa = w.B.b_a + w.bb;
     ChunkPipe pipe{nullptr, nullptr, 0, 0, 0u, 0};
+    int *pipe_fail = nullptr;   // shared flag: some thread's bounded wait gave up
     if (cached) {
         // layout: c[nb] (16) | a[nb] (8) | inverse mass, inertia (R) | static flag (1);
         // the velocity passes keep v[nb], w[nb] in the c/a bytes
@@ -1168,8 +1169,10 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             pipe.buf_bytes = chunk_buf_bytes<R>(g.size());
             pipe.nbuf = cache.nbuf;
             pipe.bar = reinterpret_cast<unsigned long long *>(pipe.buf + (size_t)cache.nbuf * pipe.buf_bytes);
+            pipe_fail = reinterpret_cast<int *>(pipe.bar + pipe.nbuf);
             if (rank == 0) {
                 for (int b = 0; b < pipe.nbuf; ++b) mbar_init(&pipe.bar[b], 1);
+                *pipe_fail = 0;
                 fence_async_shared();
             }
         }
@@ -1201,13 +1204,13 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         for (int q = 0; q < total; ++q) {
             if (q + ahead < total) pipe_issue(g, pipe, q + ahead, cv, tab, nch);
             const int b = q % pipe.nbuf;
-            bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
+            const bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
             pipe.parity ^= 1u << b;
-            if (g.any(!ok)) { failed = true; break; }
+            if (!ok) *pipe_fail = 1;
             const int e = tab[q % nch];
             const int s0 = e & ((1 << 22) - 1), cnt = e >> 22;
             const bool warm_pass = warm && q < nch;
-            if (rank < cnt) {
+            if (ok && rank < cnt) {
                 const ConsVel<R> &rec = reinterpret_cast<const ConsVel<R> *>(pipe.buf + (size_t)b * pipe.buf_bytes)[rank];
                 const int ia = rec.ia, ib = rec.ib;
                 Cons<R> k = vel_cons(rec, invm[ia], invm[ib], invi[ia], invi[ib]);
@@ -1226,6 +1229,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             }
             if (q + 1 < total) load_imp(q + 1);   // after this thread's own stores
             g.sync();
+            if (*pipe_fail) { failed = true; break; }
         }
     } else if (!failed) {
         for (int it = (warm ? -1 : 0); it < sp.vel_iters; ++it) {
@@ -1332,13 +1336,14 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             for (int j = 0; j < nch; ++j, ++q) {
                 if (issued < total && issued <= q + ahead) { pipe_issue(g, pipe, issued, cpos, tab, nch); ++issued; }
                 const int b = q % pipe.nbuf;
-                bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
+                const bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
                 pipe.parity ^= 1u << b;
-                if (g.any(!ok)) { failed = true; break; }
+                if (!ok) *pipe_fail = 1;
                 const int e = tab[j];
                 const int cnt = e >> 22;
-                if (rank < cnt) pos_one(reinterpret_cast<const ConsPos<R> *>(pipe.buf + (size_t)b * pipe.buf_bytes)[rank]);
+                if (ok && rank < cnt) pos_one(reinterpret_cast<const ConsPos<R> *>(pipe.buf + (size_t)b * pipe.buf_bytes)[rank]);
                 g.sync();
+                if (*pipe_fail) { failed = true; ++q; break; }
             }
             if (failed) break;
             if (!pos_check()) break;
