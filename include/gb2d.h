@@ -84,6 +84,12 @@ extern "C" {
 #define GB_PREC_F32 1
 
 #define GB_OPT_KERNEL_TIMES 4u   /* gb_step_opts.record_order bit: time each phased-step launch */
+#define GB_OPT_EVENTS 8u         /* gb_step_opts.record_order bit: record contact events (gb_batch_get_events) */
+
+/* contact events (gb_event.type) */
+#define GB_EV_BEGIN 1            /* two fixtures began to touch (contact.py:263-264) */
+#define GB_EV_END 2              /* they ceased to touch, or a touching contact was destroyed (contact.py:265-266, contact_manager.py:167-168) */
+#define GB_EV_POST_SOLVE 3       /* impulses of a solved contact (island.py:245-252) */
 
 /* error codes (also OR-ed into the per-world device status word) */
 #define GB_OK 0
@@ -102,6 +108,7 @@ extern "C" {
 #define GB_ST_PAIR_OVERFLOW 8u
 #define GB_ST_TOI_ISLAND_CAP 16u
 #define GB_ST_WAIT_TIMEOUT 32u   /* a bounded wait for an in-kernel copy gave up */
+#define GB_ST_EVENT_OVERFLOW 64u /* more contact events than the world's event slots */
 
 /* One rigid body: the state of pypybox2d.Body (body.py:46-84). */
 typedef struct gb_body {
@@ -207,6 +214,19 @@ const char *gb_last_error(void);
  * (6 ints), so bindings can check their record layouts. */
 int gb_struct_sizes(int32_t *sizes);
 
+/* One contact event of a step, replayed to the contact listeners after it.
+ * `key` orders a world's events: (step of the call) << 48 | phase << 40 |
+ * index, where phase 0 is the contact update (index = contact position),
+ * phase 1 the island solve (index = contact position) and phase 2 the
+ * continuous-collision loop (index = order of occurrence). */
+typedef struct gb_event {
+    int32_t type;                 /* GB_EV_* */
+    int32_t fixture_a, fixture_b; /* world-local fixtures of the contact */
+    int32_t point_count;          /* impulse points (post-solve) */
+    int64_t key;
+    double normal_impulse[2], tangent_impulse[2];
+} gb_event;
+
 /* Upload a scene to device memory.  Replaces the host-side construction of
  * the reference's World (world.py:64-91, 183-233). */
 int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out);
@@ -248,6 +268,12 @@ int gb_batch_counters(gb_batch *batch, int64_t *counters);
  * set-up, solver, fixture sync and pairs, TOI candidates, first-pass TOI,
  * TOI event loop).  Measurement only: a timed step waits for its events. */
 int gb_batch_kernel_times(gb_batch *batch, double *total_ms, int32_t capacity, int32_t *n_slots, int64_t *n_steps);
+/* Contact events of one world recorded by the last gb_batch_step call made
+ * with GB_OPT_EVENTS (unsorted; order by `key`).  *n_out = number of events;
+ * events beyond the world's slots (3 per contact slot + 64) are dropped and
+ * flagged GB_ST_EVENT_OVERFLOW. */
+int gb_batch_get_events(gb_batch *batch, int32_t world, gb_event *out, int32_t capacity, int32_t *n_out,
+                        void *cuda_stream);
 
 /* Size of the static device scratch of gb_batch_step_static_scratch (32 MiB). */
 #define GB_STATIC_SCRATCH_BYTES (32u << 20)

@@ -146,8 +146,17 @@ EXPORTED = (
     "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_get_proxies",
     "gb_batch_get_contact_counts", "gb_batch_get_contacts", "gb_batch_get_solver_order",
     "gb_batch_status", "gb_batch_counters", "gb_batch_phase_clocks",
-    "gb_batch_step_static_scratch", "gb_batch_kernel_times",
+    "gb_batch_step_static_scratch", "gb_batch_kernel_times", "gb_batch_get_events",
 )
+
+#: gb_step_opts.record_order bit that records contact events
+OPT_EVENTS = 8
+EV_BEGIN, EV_END, EV_POST_SOLVE = 1, 2, 3
+ST_EVENT_OVERFLOW = 64
+EVENT = np.dtype([
+    ("type", "<i4"), ("fixture_a", "<i4"), ("fixture_b", "<i4"), ("point_count", "<i4"), ("key", "<i8"),
+    ("normal_impulse", "<f8", (2,)), ("tangent_impulse", "<f8", (2,)),
+], align=True)
 
 #: gb_step_opts.record_order bit that times each launch of the phased step
 OPT_KERNEL_TIMES = 4
@@ -195,6 +204,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_phase_clocks.argtypes = [vp, ctypes.POINTER(ctypes.c_int64), vp]
     lib.gb_batch_step_static_scratch.argtypes = [vp, ctypes.POINTER(StepOpts), vp]
     lib.gb_batch_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32, i32p, ctypes.POINTER(ctypes.c_int64)]
+    lib.gb_batch_get_events.argtypes = [vp, i32, vp, i32, i32p, vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

@@ -130,6 +130,8 @@ struct gb_batch {
     int cstage_cap = 0;
     long long counters[3] = {0, 0, 0};
     KernelTimer *ktimer = nullptr;   // created by the first timed step
+    gb_event *d_ev = nullptr;        // contact events, allocated by the first step that records them
+    int *d_ev_n = nullptr;
 };
 
 extern "C" {
@@ -319,6 +321,8 @@ int gb_batch_destroy(gb_batch *b) {
         for (int k = 0; k <= GB_NKTIME; ++k) cudaEventDestroy(b->ktimer->ev[k]);
         delete b->ktimer;
     }
+    cudaFree(b->d_ev);
+    cudaFree(b->d_ev_n);
     delete b;
     return 0;
 }
@@ -335,8 +339,19 @@ int gb_batch_step(gb_batch *b, const gb_step_opts *o, void *stream) {
     sp.pos_iters = o->pos_iters;
     sp.record_order = o->record_order & 1;
     sp.profile = (o->record_order >> 1) & 1;
+    sp.events = (o->record_order & GB_OPT_EVENTS) ? 1 : 0;
+    sp.step_index = 0;
     int mode = (o->launch_mode == 2 || o->launch_mode == 3) ? o->launch_mode : (o->launch_mode == 0 ? 3 : 1);
     int threads = o->block_threads > 0 ? o->block_threads : (mode == 2 ? 128 : 128);
+    if (sp.events) {
+        if (!b->d_ev) {
+            CK(cudaMalloc((void **)&b->d_ev, sizeof(gb_event) * (3 * (size_t)b->ncap + 64 * (size_t)b->nw)));
+            CK(cudaMalloc((void **)&b->d_ev_n, sizeof(int) * b->nw));
+            b->bd.ev = b->bf.ev = b->d_ev;
+            b->bd.ev_n = b->bf.ev_n = b->d_ev_n;
+        }
+        CK(cudaMemsetAsync(b->d_ev_n, 0, sizeof(int) * b->nw, st));
+    }
     if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
     KernelTimer *kt = nullptr;
     if ((o->record_order & GB_OPT_KERNEL_TIMES) && mode == 3) {
@@ -463,6 +478,27 @@ int gb_batch_phase_clocks(gb_batch *b, int64_t *clocks, void *stream) {
     return 0;
 }
 
+int gb_batch_get_events(gb_batch *b, int32_t world, gb_event *out, int32_t capacity, int32_t *n_out, void *stream) {
+    if (!b || !out || !n_out) return fail(GB_E_ARG, "NULL argument");
+    if (world < 0 || world >= b->nw) return fail(GB_E_ARG, "world index out of range");
+    *n_out = 0;
+    if (!b->d_ev) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    int n = 0;
+    CK(cudaMemcpyAsync(&n, b->d_ev_n + world, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const WorldHdr &h = b->hdr[world];
+    n = std::min(n, 3 * h.ccap + 64);
+    *n_out = n;
+    if (n > capacity) return fail(GB_E_ARG, "capacity too small for the world's events");
+    if (n > 0) {
+        CK(cudaMemcpyAsync(out, b->d_ev + 3 * (size_t)h.cbase + 64 * (size_t)world, sizeof(gb_event) * n,
+                           cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return 0;
+}
+
 int gb_batch_kernel_times(gb_batch *b, double *total_ms, int32_t capacity, int32_t *n_slots, int64_t *n_steps) {
     if (!b || !total_ms || !n_slots || !n_steps) return fail(GB_E_ARG, "NULL argument");
     *n_slots = GB_NKTIME;
@@ -544,6 +580,8 @@ extern "C" int gb_batch_step_static_scratch(gb_batch *b, const gb_step_opts *o, 
     sp.pos_iters = o->pos_iters;
     sp.record_order = o->record_order & 1;
     sp.profile = (o->record_order >> 1) & 1;
+    sp.events = 0;   // contact events are recorded by gb_batch_step only
+    sp.step_index = 0;
     int mode = (o->launch_mode == 2 || o->launch_mode == 3) ? o->launch_mode : (o->launch_mode == 0 ? 3 : 1);
     int threads = o->block_threads > 0 ? o->block_threads : 128;
     if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");

@@ -122,13 +122,15 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
         // kt: an event after every launch, the host accumulates the gaps
         // (one host synchronisation per step, measurement only)
         auto mark = [&](int k) { if (kt) cudaEventRecord(kt->ev[k], st); };
+        StepParams sp1 = sp;
         for (int s = 0; s < n_steps; ++s) {
+            const StepParams sp = [&] { StepParams q = sp1; q.step_index = s; return q; }();
             mark(0);
             k_world<GB_REAL, PH_PAIRS0><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
             mark(1);
             if (nb) k_pre<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
             mark(2);
-            if (ns) k_collide<GB_REAL><<<gs, T, 0, st>>>(B, ns);
+            if (ns) k_collide<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
             mark(3);
             k_world<GB_REAL, PH_COLLIDE2><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
             mark(4);

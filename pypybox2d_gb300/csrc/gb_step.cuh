@@ -104,8 +104,26 @@ template <class R> __device__ __forceinline__ bool fx_sensor(const WView<R> &w, 
     return (w.B.f_flags[w.fb + f] & GB_FIX_SENSOR) != 0;
 }
 
-// contact.py:210-268 Contact.update; returns whether touching changed.
-template <class R> __device__ bool contact_update(const WView<R> &w, int i) {
+// Append one contact event of the world (index < 0: keyed by its slot,
+// which is the order of occurrence when one thread records).
+template <class R> __device__ void record_event(const WView<R> &w, const EvCtx &ev, int type, int i, int index, int npts,
+                                                const R *ni, const R *ti) {
+    const ContactRec<R> &c = w.con(i);
+    int slot = atomicAdd(&w.B.ev_n[w.wi], 1);
+    if (slot >= 3 * w.H->ccap + 64) { atomicOr(&w.H->status, GB_ST_EVENT_OVERFLOW); return; }
+    gb_event &e = w.B.ev[3 * (size_t)w.cb + 64 * (size_t)w.wi + slot];
+    e.type = type; e.fixture_a = c.fa; e.fixture_b = c.fb; e.point_count = npts;
+    e.key = ((long long)ev.step << 48) | ((long long)ev.phase << 40) | (long long)(index >= 0 ? index : slot);
+    for (int j = 0; j < 2; ++j) {
+        e.normal_impulse[j] = j < npts ? (double)ni[j] : 0.0;
+        e.tangent_impulse[j] = j < npts ? (double)ti[j] : 0.0;
+    }
+}
+
+// contact.py:210-268 Contact.update; returns whether touching changed (the
+// wake rule; sensors never wake).  With `ev` on, a change of touching, of a
+// sensor too, is recorded as a begin or end event (contact.py:263-266).
+template <class R> __device__ bool contact_update(const WView<R> &w, int i, const EvCtx *ev = nullptr, int ev_index = -1) {
     ContactRec<R> &c = w.con(i);
     Manifold<R> old = c.m;
     c.flags |= GB_C_ENABLED;
@@ -135,6 +153,8 @@ template <class R> __device__ bool contact_update(const WView<R> &w, int i) {
         changed = touching != was;
     }
     if (touching) c.flags |= GB_C_TOUCHING; else c.flags &= ~GB_C_TOUCHING;
+    if (ev && ev->on && touching != was)
+        record_event<R>(w, *ev, touching ? GB_EV_BEGIN : GB_EV_END, i, ev_index, 0, nullptr, nullptr);
     return changed;
 }
 
@@ -443,19 +463,24 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
 // loop starts).  Returns 0 when both bodies are inactive at that point,
 // 1 after Contact.update (*woke: touching changed, both bodies woken), 2 when
 // the contact is to be destroyed.
-template <class R> __device__ int collide_one(const WView<R> &w, int i, const int *wake, bool *woke) {
+template <class R> __device__ int collide_one(const WView<R> &w, int i, const int *wake, bool *woke, const EvCtx *ev = nullptr) {
     ContactRec<R> &c = w.con(i);
     int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
     bool act_a = w.btype(ba) != GB_BODY_STATIC && wake[ba] < i;
     bool act_b = w.btype(bb) != GB_BODY_STATIC && wake[bb] < i;
     *woke = false;
     if (!act_a && !act_b) return 0;
+    bool destroy = false;
     if (c.flags & GB_C_FILTER) {
-        if (!should_collide(w, bb, ba) || !default_filter(w, c.fa, c.fb)) return 2;
-        c.flags &= ~GB_C_FILTER;
+        if (!should_collide(w, bb, ba) || !default_filter(w, c.fa, c.fb)) destroy = true;
+        else c.flags &= ~GB_C_FILTER;
     }
-    if (!aabb_overlap(w.B.f_aabb[w.fb + c.fa], w.B.f_aabb[w.fb + c.fb])) return 2;
-    *woke = contact_update(w, i);
+    if (!destroy && !aabb_overlap(w.B.f_aabb[w.fb + c.fa], w.B.f_aabb[w.fb + c.fb])) destroy = true;
+    if (destroy) {   // contact_manager.py:160-172: a touching contact ends as it is destroyed
+        if (ev && ev->on && (c.flags & GB_C_TOUCHING)) record_event<R>(w, *ev, GB_EV_END, i, i, 0, nullptr, nullptr);
+        return 2;
+    }
+    *woke = contact_update(w, i, ev, i);
     return 1;
 }
 
@@ -481,7 +506,8 @@ template <class R, class G> __device__ void compact_contacts(const G &g, const W
     g.sync();
 }
 
-template <class R, class G> __device__ void collide(const G &g, const WView<R> &w) {
+template <class R, class G> __device__ void collide(const G &g, const WView<R> &w, const StepParams &sp) {
+    const EvCtx ev{sp.events, sp.step_index, GB_EV_PHASE_UPDATE};
     int nb = w.H->nb, nc = w.H->nc;
     int *wake = w.B.s_wake + w.bb;
     int *proc = w.B.s_proc + w.cb;     // 0 = not updated, 1 = updated, 2 = destroy
@@ -497,7 +523,7 @@ template <class R, class G> __device__ void collide(const G &g, const WView<R> &
         for (int i = g.rank(); i < nc; i += g.size()) {
             if (proc[i]) continue;
             bool woke;
-            int r = collide_one(w, i, wake, &woke);
+            int r = collide_one(w, i, wake, &woke, &ev);
             if (r == 0) continue;
             proc[i] = r;
             if (woke) {
@@ -1267,11 +1293,15 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         g.sync();
     }
     if (rank == 0) { ck.mark(4); if (ck.acc) ck.acc[10] += ncol; }
-    // 7. store impulses (contact.py:801-806)
+    // 7. store impulses (contact.py:801-806); the post-solve report of each
+    //    solved contact (island.py:245-252)
+    const EvCtx ev{sp.events, sp.step_index, GB_EV_PHASE_SOLVE};
     for (int k = rank; k < ncons; k += g.size()) {
         const ConsVel<R> &v = cv[k];
-        ContactRec<R> &c = w.con(cpos[k].cidx);
+        const int ci = cpos[k].cidx;
+        ContactRec<R> &c = w.con(ci);
         for (int j = 0; j < v.npts && j < c.m.count; ++j) { c.m.ni[j] = v.ni[j]; c.m.ti[j] = v.ti[j]; }
+        if (ev.on) record_event<R>(w, ev, GB_EV_POST_SOLVE, ci, ci, v.npts, v.ni, v.ti);
     }
     // 8. integrate positions (island.py:120-138)
     for (int b = rank; b < nb; b += g.size()) {

@@ -80,7 +80,7 @@ template <class R> __device__ bool toi_of_contact(const WView<R> &w, int i) {
 // island.py:181-243 Island.solve_toi on rank 0 (island of at most 64
 // bodies and 32 contacts).
 template <class R> __device__ void island_solve_toi(const WView<R> &w, const int *ib, int nbi, const int *ic, int nci,
-                                                    double sub_dt, int vel_iters, int toi_a, int toi_b) {
+                                                    double sub_dt, int vel_iters, int toi_a, int toi_b, const EvCtx *ev = nullptr) {
     vec2<double> pc[2 * GB_MAX_TOI_CONTACTS];
     double pa[2 * GB_MAX_TOI_CONTACTS];
     vec2<R> vv[2 * GB_MAX_TOI_CONTACTS];
@@ -125,6 +125,8 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
             vv[la] = va; ww[la] = wa;
             vv[lb] = vb; ww[lb] = wb;
         }
+    if (ev && ev->on)   // island.py:243 report of the sub-step's impulses
+        for (int k = 0; k < nci; ++k) record_event<R>(w, *ev, GB_EV_POST_SOLVE, ic[k], -1, ks[k].npts, ks[k].ni, ks[k].ti);
     const R dtr = (R)sub_dt;
     for (int i = 0; i < nbi; ++i) {
         vec2<R> v = vv[i];
@@ -155,14 +157,14 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
 // (Body._contacts).  The island bodies are left in s_stack[0..sh->nisland)
 // with their s_bvis marks set; the caller invalidates and clears them.
 template <class R> __device__ void toi_event(const WView<R> &w, int mi, double min_alpha, double dt, int vel_iters, WShared *sh,
-                                             const int *la, int na, const int *lb, int nlb) {
+                                             const int *la, int na, const int *lb, int nlb, const EvCtx *ev = nullptr) {
     ContactRec<R> &mc = w.con(mi);
     unsigned char *bflag = w.B.s_bvis + w.bb;
     int bia = w.fbody(mc.fa), bib = w.fbody(mc.fb);
     Sweep back_a = w.sweep(bia), back_b = w.sweep(bib);
     body_advance(w, bia, min_alpha);
     body_advance(w, bib, min_alpha);
-    contact_update(w, mi);
+    contact_update(w, mi, ev, -1);
     mc.flags &= ~GB_C_TOI;
     mc.toi_count += 1;
     sh->nisland = 0;
@@ -198,7 +200,7 @@ template <class R> __device__ void toi_event(const WView<R> &w, int mi, double m
             if (fx_sensor(w, c.fa) || fx_sensor(w, c.fb)) continue;
             Sweep backup = w.sweep(oi);
             if (!bflag[oi]) body_advance(w, oi, min_alpha);
-            contact_update(w, ci);
+            contact_update(w, ci, ev, -1);
             if (!(c.flags & GB_C_ENABLED) || !(c.flags & GB_C_TOUCHING)) {
                 w.put_sweep(oi, backup);
                 sync_transform(w, oi);
@@ -213,7 +215,7 @@ template <class R> __device__ void toi_event(const WView<R> &w, int mi, double m
         }
     }
     double sub_dt = (1.0 - min_alpha) * dt;
-    island_solve_toi(w, ib, nbi, ic, nci, sub_dt, vel_iters, 0, 1);
+    island_solve_toi(w, ib, nbi, ic, nci, sub_dt, vel_iters, 0, 1, ev);
     int *mv = w.B.s_move + w.fb;
     for (int i = 0; i < nbi; ++i) {
         int bi = ib[i];
@@ -394,7 +396,8 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
             if (w.btype(bia) == GB_BODY_DYNAMIC) body_contacts(w, off, adj, nc0, nc, bia, [&](int i) { la[na++] = i; });
             if (w.btype(bib) == GB_BODY_DYNAMIC) body_contacts(w, off, adj, nc0, nc, bib, [&](int i) { lb[nlb++] = i; });
             sh->nmove = 0;
-            toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh, la, na, lb, nlb);
+            const EvCtx ev{sp.events, sp.step_index, GB_EV_PHASE_TOI};
+            toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh, la, na, lb, nlb, &ev);
             ck.mark(13);
         }
         g.sync();
@@ -456,7 +459,7 @@ template <class R, class G> __device__ void world_step(const G &g, const WView<R
     }
     sp.dt_ratio = w.H->inv_dt0 * sp.dt;
     pc.mark(0);
-    collide(g, w);
+    collide(g, w, sp);
     pc.mark(1);
     if ((w.H->flags & GB_W_STEP_COMPLETE) && sp.dt > 0.0) world_solve(g, w, sp, sh, pc);
     if ((w.H->flags & GB_W_CONTINUOUS) && sp.dt > 0.0) world_solve_toi(g, w, sp, sh);
@@ -484,7 +487,11 @@ template <class R> __global__ void k_step_cta(Batch<R> B, StepParams sp, int n_s
     __syncthreads();
     GroupCta g{sm};
     WView<R> w{B, &H, H.bbase, H.fbase, H.cbase, wi};
-    for (int s = 0; s < n_steps; ++s) world_step(g, w, sp, &sh);
+    for (int s = 0; s < n_steps; ++s) {
+        StepParams q = sp;
+        q.step_index = s;
+        world_step(g, w, q, &sh);
+    }
     __syncthreads();
     if (threadIdx.x == 0) B.hdr[wi] = H;
 }
@@ -502,7 +509,11 @@ template <class R> __global__ void k_step_warp(Batch<R> B, StepParams sp, int n_
     __syncwarp();
     GroupWarp g{sm[lw]};
     WView<R> w{B, &H[lw], H[lw].bbase, H[lw].fbase, H[lw].cbase, wi};
-    for (int s = 0; s < n_steps; ++s) world_step(g, w, sp, &sh[lw]);
+    for (int s = 0; s < n_steps; ++s) {
+        StepParams q = sp;
+        q.step_index = s;
+        world_step(g, w, q, &sh[lw]);
+    }
     __syncwarp();
     if ((threadIdx.x & 31) == 0) B.hdr[wi] = H[lw];
 }

@@ -122,6 +122,8 @@ template <class R> struct Batch {
     struct TPlan *s_plan;        // GB_TOI_PLAN_CAP planned TOI sweeps per world
     int *toi_list;               // contact slots needing a first-pass TOI (batch-wide)
     int *toi_n;                  // their count
+    gb_event *ev;                // contact events: 3 ccap + 64 per world, from 3 cbase + 64 world
+    int *ev_n;                   // events recorded per world
 };
 #define GB_NPROF 16
 #define GB_SOLVE_BIG_BODIES 512    // worlds this large are solved by the wide launch
@@ -137,6 +139,16 @@ struct StepParams {
     int vel_iters, pos_iters;
     int record_order;
     int profile;
+    int events;       // record contact events
+    int step_index;   // step of the current call (event keys)
+};
+
+// Contact-event recording (listeners replayed on the host after the step).
+#define GB_EV_PHASE_UPDATE 0
+#define GB_EV_PHASE_SOLVE 1
+#define GB_EV_PHASE_TOI 2
+struct EvCtx {
+    int on, step, phase;
 };
 
 // Phase clocks: rank 0 adds the SM clock delta since the last mark.

@@ -40,8 +40,9 @@ class GpuBatch:
 
     def step(self, dt: float, vel_iters: int = 8, pos_iters: int = 3, n_steps: int = 1, launch_mode: int = 1,
              block_threads: int = 0, record_order: bool = False, stream: int | None = None,
-             profile: bool = False, kernel_times: bool = False) -> None:
-        flags = (1 if record_order else 0) | (2 if profile else 0) | (abi.OPT_KERNEL_TIMES if kernel_times else 0)
+             profile: bool = False, kernel_times: bool = False, events: bool = False) -> None:
+        flags = ((1 if record_order else 0) | (2 if profile else 0) | (abi.OPT_KERNEL_TIMES if kernel_times else 0) |
+                 (abi.OPT_EVENTS if events else 0))
         o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, flags)
         abi.check(self.lib.gb_batch_step(self.h, ctypes.byref(o), ctypes.c_void_p(stream or 0)))
 
@@ -86,6 +87,22 @@ class GpuBatch:
         abi.check(self.lib.gb_batch_get_solver_order(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                                                      cap, ctypes.byref(n), None))
         return out[:n.value].copy()
+
+    def events(self, world: int = 0) -> np.ndarray:
+        """Contact events of one world from the last step call made with
+        events=True, in replay order (sorted by key)."""
+        n = ctypes.c_int32()
+        cap = 3 * 64 + 64
+        while True:
+            out = np.zeros(cap, dtype=abi.EVENT)
+            rc = self.lib.gb_batch_get_events(self.h, world, out.ctypes.data, cap, ctypes.byref(n), None)
+            if rc == 0:
+                break
+            if n.value <= cap:
+                abi.check(rc)
+            cap = n.value
+        ev = out[:n.value]
+        return ev[np.argsort(ev["key"], kind="stable")]
 
     def phase_clocks(self) -> np.ndarray:
         """Accumulated SM clocks per step phase and world (n_worlds x 16)."""

@@ -422,6 +422,44 @@ class Contact:
         return Vec2(self._rec["m_lpx"], self._rec["m_lpy"])
 
 
+class EventContact:
+    """The contact a listener receives when events are replayed after a
+    step: its fixtures and whether it touched when the event occurred."""
+
+    __slots__ = ("fixture_a", "fixture_b", "touching")
+
+    def __init__(self, fixture_a, fixture_b, touching):
+        self.fixture_a, self.fixture_b, self.touching = fixture_a, fixture_b, touching
+
+    def __repr__(self):
+        return f"EventContact({self.fixture_a!r}, {self.fixture_b!r}, touching={self.touching})"
+
+
+class ContactManager:
+    """contact_manager.py:46-100: the contact listeners of a World.
+
+    The GPU step records begin, end and post-solve events on the device; the
+    world replays them to these callbacks after the step, in a fixed order
+    (contact updates in contact-list order, then post-solve reports in
+    contact-list order, then continuous-collision events as they occurred).
+    pre_solve, which may change a contact before the solver sees it, cannot
+    run inside the GPU step: a world with one set raises on step."""
+
+    def __init__(self):
+        self.begin_contact = None
+        self.end_contact = None
+        self.pre_solve = None
+        self.post_solve = None
+
+    @property
+    def contact_listener(self):
+        return [self.begin_contact, self.end_contact, self.pre_solve, self.post_solve]
+
+    @property
+    def wants_events(self):
+        return self.begin_contact is not None or self.end_contact is not None or self.post_solve is not None
+
+
 def _fixture_list(shapes, fixtures, shape_fixture):
     """Body(shapes=..., fixtures=..., shape_fixture=...) of body.py:20-115."""
     out = []
@@ -468,6 +506,7 @@ class World:
         self._upload_bodies = False
         self._locked = False
         self._inv_dt0 = 0.0
+        self.contact_manager = ContactManager()
 
     # -- properties
     @property
@@ -542,13 +581,19 @@ class World:
         return self.create_body(body, type=Body.KINEMATIC, **kwargs)
 
     def destroy_body(self, body):
-        """world.py:235-270: the body, its fixtures and their contacts leave the world."""
+        """world.py:235-270: the body, its fixtures and their contacts leave the world
+        (touching ones reported to end_contact, contact_manager.py:167-168)."""
         self._check_unlocked()
         self._structural()
         bi = body._index
         B, F, C, M = self._B, self._F, self._C, self._M
         f0, nfix = int(B[bi]["fixture_start"]), int(B[bi]["fixture_count"])
         gone = lambda x: (x >= f0) & (x < f0 + nfix)   # noqa: E731
+        if self.contact_manager.end_contact is not None:
+            for c in C[gone(C["fixture_a"]) | gone(C["fixture_b"])]:
+                if int(c["flags"]) & abi.C_TOUCHING:
+                    self.contact_manager.end_contact(EventContact(self._fixture_at(int(c["fixture_a"])),
+                                                                  self._fixture_at(int(c["fixture_b"])), False))
         C = C[~(gone(C["fixture_a"]) | gone(C["fixture_b"]))].copy()
         for key in ("fixture_a", "fixture_b"):
             C[key] = np.where(C[key] >= f0 + nfix, C[key] - nfix, C[key])
@@ -575,12 +620,17 @@ class World:
 
     # -- the step
     def step(self, dt, vel_iters, pos_iters):
-        """world.py:307-354: one gb_batch_step of this world."""
+        """world.py:307-354: one gb_batch_step of this world, then the
+        contact listeners' events."""
         self._check_unlocked()
+        cm = self.contact_manager
+        if cm.pre_solve is not None:
+            raise NotImplementedError("pre_solve listeners cannot run inside the GPU step")
         self._sync_device()
+        events = cm.wants_events
         self._locked = True
         try:
-            self._gpu.step(float(dt), int(vel_iters), int(pos_iters), 1, launch_mode=1)
+            self._gpu.step(float(dt), int(vel_iters), int(pos_iters), 1, launch_mode=1, events=events)
         finally:
             self._locked = False
         if dt > 0.0:
@@ -589,6 +639,23 @@ class World:
         st = self._gpu.status()
         if st[0]:
             raise RuntimeError(f"GPU world step failed: status bits {int(st[0]):#x}")
+        if events:
+            self._replay(self._gpu.events(0))
+
+    def _replay(self, ev):
+        """Hand the step's recorded events to the listeners, in key order."""
+        cm = self.contact_manager
+        for e in ev:
+            fa, fb = self._fixture_at(int(e["fixture_a"])), self._fixture_at(int(e["fixture_b"]))
+            t = int(e["type"])
+            if t == abi.EV_BEGIN and cm.begin_contact is not None:
+                cm.begin_contact(EventContact(fa, fb, True))
+            elif t == abi.EV_END and cm.end_contact is not None:
+                cm.end_contact(EventContact(fa, fb, False))
+            elif t == abi.EV_POST_SOLVE and cm.post_solve is not None:
+                n = int(e["point_count"])
+                cm.post_solve(EventContact(fa, fb, True),
+                              [(float(e["normal_impulse"][k]), float(e["tangent_impulse"][k])) for k in range(n)])
 
     # ---------------------------------------------------------------- internals
     def _materialise(self):

@@ -400,6 +400,20 @@ def pair_order_hook(world):
     bp.update_pairs = types.MethodType(update_pairs, bp)
 
 
+def events_array(log):
+    """Listener log of api_script -> record array (kind 1 begin, 2 end, 3 post-solve)."""
+    kinds = {"begin": 1, "end": 2, "post": 3}
+    dt = np.dtype([("kind", "<i4"), ("step", "<i4"), ("ba", "<i4"), ("fa", "<i4"), ("bb", "<i4"), ("fb", "<i4"),
+                   ("n", "<i4"), ("imp", "<f8", (4,))])
+    out = np.zeros(len(log), dtype=dt)
+    for k, (kind, step, ba, fa, bb, fb, imp) in enumerate(log):
+        out[k]["kind"], out[k]["step"] = kinds[kind], step
+        out[k]["ba"], out[k]["fa"], out[k]["bb"], out[k]["fb"] = ba, fa, bb, fb
+        out[k]["n"] = len(imp) // 2
+        out[k]["imp"][:len(imp)] = imp
+    return out
+
+
 def run_api_script(b2):
     """tests/golden/api_script.py on the reference -> api_script.npz."""
     sys.path.insert(0, HERE)
@@ -410,10 +424,12 @@ def run_api_script(b2):
         W, B, F, C = export_world(world, b2)
         out[f"{label}_bodies"], out[f"{label}_aabb"], out[f"{label}_contacts"] = B, F["aabb"].copy(), C
 
-    api_script.script(b2, snap, on_world=pair_order_hook)
+    log = []
+    api_script.script(b2, snap, on_world=pair_order_hook, log=log)
+    out["events"] = events_array(log)
     path = os.path.join(HERE, "api_script.npz")
     np.savez_compressed(path, **out)
-    print(f"api_script: {len(out) // 3} snapshots -> {os.path.getsize(path)} bytes")
+    print(f"api_script: {(len(out) - 1) // 3} snapshots, {len(out['events'])} events -> {os.path.getsize(path)} bytes")
 
 
 def main():

@@ -128,3 +128,34 @@ def test_api_session_on_gpu_matches_oracle_bit_for_bit():
         assert np.array_equal(aabb, aabb2), f"{label} fat AABBs"
         same(used(C), used(C2), f"{label} contacts")
     assert all(isinstance(c.touching, bool) for c in world.contacts)
+
+
+@pytest.mark.gpu
+def test_listener_events_match_reference():
+    """begin/end/post-solve events of the API session, replayed after each
+    GPU step, against the reference's listener calls: the begin and end
+    events in the same order at the same steps; per step the same
+    post-solve reports, impulses within 1e-9 relative (the reference takes
+    cos/sin from libm, the GPU from its portable sincos)."""
+    d = np.load(os.path.join(GOLDEN, "api_script.npz"))
+    want = d["events"]
+    log = []
+    api_script.script(b2, lambda label, world: None, log=log)
+    kinds = {"begin": 1, "end": 2, "post": 3}
+    got = [(kinds[k], s, ba, fa, bb, fb, imp) for (k, s, ba, fa, bb, fb, imp) in log]
+    ge = [g[:6] for g in got if g[0] != 3]
+    we = [tuple(int(x) for x in (r["kind"], r["step"], r["ba"], r["fa"], r["bb"], r["fb"])) for r in want if r["kind"] != 3]
+    assert ge == we
+    gp = sorted((g[1], g[2:6], g[6]) for g in got if g[0] == 3)
+    wp = sorted((int(r["step"]), tuple(int(x) for x in (r["ba"], r["fa"], r["bb"], r["fb"])),
+                 tuple(float(x) for x in r["imp"][:2 * int(r["n"])])) for r in want if r["kind"] == 3)
+    assert [(a, b) for a, b, _ in gp] == [(a, b) for a, b, _ in wp]
+    for (_, _, x), (_, _, y) in zip(gp, wp):
+        np.testing.assert_allclose(x, y, rtol=1e-9, atol=1e-12)
+
+
+def test_pre_solve_listener_raises_on_step():
+    w = b2.World()
+    w.contact_manager.pre_solve = lambda c, m: None
+    with pytest.raises(NotImplementedError):
+        w.step(1 / 60, 8, 3)
