@@ -51,8 +51,8 @@ sys.path.insert(0, os.path.join(HERE, "tests"))
 METRIC = "body-steps/s on 1 GB300: batched FP32 vs plain FP64 GPU path at stated step error"
 DT = 1.0 / 60.0
 VI, PI = 8, 3
-DEFAULTS = {"uneven": (8192, 1000), "pyramid": (4096, 2000)}
-SETTLE_STEPS = {"uneven": 300, "pyramid": 300}   # reference arm: untimed steps before its sample
+DEFAULTS = {"uneven": (8192, 1000), "pyramid": (4096, 2000), "bullets": (2048, 600), "large": (1, 600)}
+SETTLE_STEPS = {"uneven": 300, "pyramid": 300, "bullets": 0, "large": 20}   # reference arm: untimed steps before its sample
 
 
 def _peaks():
@@ -127,6 +127,16 @@ def build_workload(name: str, n_worlds: int, seed: int):
     if name == "pyramid":
         W, B, F, M = scenes.pyramid_batch(n_worlds, rows=20, jitter=0.01, seed=seed)
         desc = (f"pyramid x{n_worlds} per GPU, 210 boxes/world on a ground box, jitter U(-0.01,0.01) m, "
+                f"dt=1/60, 8 vel / 3 pos iters, f32 bulk / f64 positions")
+    elif name == "bullets":
+        W, B, F, M = scenes.bullet_batch(n_worlds, seed=seed)
+        desc = (f"bullets x{n_worlds} per GPU: 20-box stack (friction 0.3) on a ground box + 4 bullet circles "
+                f"(r 0.1, density 100) from x=-30, y U(0.5,10), speed U(150,250) m/s, dt=1/60, 8 vel / 3 pos iters, "
+                f"f32 bulk / f64 positions and TOI")
+    elif name == "large":
+        W, B, F, M = scenes.concat([scenes.large_world(seed + w) for w in range(n_worlds)])
+        desc = (f"large world x{n_worlds}: 100000 bodies (60% boxes half-extent U(0.2,0.6), 40% circles r U(0.2,0.6), "
+                f"density 1, friction 0.5) on a jittered 1.5 m grid above a 600 m ground box with 200 m walls, "
                 f"dt=1/60, 8 vel / 3 pos iters, f32 bulk / f64 positions")
     else:
         W, B, F, M = scenes.uneven_batch(n_worlds, seed=seed)
@@ -299,11 +309,11 @@ def f32_step_error(W, B, F, M, w, settle_steps=60):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=0, help="0 = the workload's default (uneven 1000, pyramid 2000)")
+    ap.add_argument("--steps", type=int, default=0, help="0 = the workload's default (uneven 1000, pyramid 2000, bullets 600, large 600)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="uneven", choices=["uneven", "pyramid"])
-    ap.add_argument("--worlds", type=int, default=0, help="0 = the workload's default (uneven 8192, pyramid 4096)")
+    ap.add_argument("--workload", default="uneven", choices=["uneven", "pyramid", "bullets", "large"])
+    ap.add_argument("--worlds", type=int, default=0, help="0 = the workload's default (uneven 8192, pyramid 4096, bullets 2048, large 1)")
     ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
     ap.add_argument("--mode", type=int, default=3, help="1 = one CTA per world (monolithic), 2 = one warp per world, "
                                                         "3 = phase kernels over the whole batch")
@@ -458,7 +468,7 @@ def main():
                                          f"the batch's state after the timed steps ({tcpu:.1f} s, {threads} threads, "
                                          f"float64 C restatement)"}
         # plain float64 path: one world per batch, one launch per world-step
-        n_plain, plain_steps = 16, 5
+        n_plain, plain_steps = min(16, n_worlds), 5
         plain = [GpuBatch(*world_slice(W, B, F, M, w)[:3], precision="f64", moves=world_slice(W, B, F, M, w)[3])
                  for w in range(n_plain)]
         for p in plain:

@@ -414,27 +414,35 @@ def uneven_batch(n_worlds: int = 8192, seed: int = 0, counts=None):
     polygon mass data, centre of mass, the velocity shift of reset_mass_data,
     edge normals and fat AABBs), so world w equals uneven_world(seed + w)."""
     draws = [_uneven_draws(seed + w, None if counts is None else int(counts[w])) for w in range(n_worlds)]
+    cs = SceneBuilder(gravity=(0.0, -10.0), do_sleep=True)
+    cs.create_body(abi.BODY_STATIC, position=(0, 0), fixtures=[(e, {}) for e in _container_edges()])
+    return _assemble(cs, draws)
+
+
+def _assemble(cs: SceneBuilder, draws: list):
+    """Batch records: per world the static body of `cs` (built once) and one
+    dynamic body with one circle or polygon fixture per draw."""
+    n_worlds = len(draws)
     ns = np.array([d["n"] for d in draws])
     cat = {k: np.concatenate([d[k] for d in draws]) for k in draws[0] if k != "n"}
     nbody = int(ns.sum())
+    Wc, Bc, Fc, _ = cs.records()
+    nfc = len(Fc)
     nb_w = ns + 1
-    nf_w = ns + 4
+    nf_w = ns + nfc
     b_start = np.concatenate([[0], np.cumsum(nb_w)[:-1]])
     f_start = np.concatenate([[0], np.cumsum(nf_w)[:-1]])
-    # container (static body 0 of every world, four edge fixtures)
-    cs = SceneBuilder(gravity=(0.0, -10.0), do_sleep=True)
-    cs.create_body(abi.BODY_STATIC, position=(0, 0), fixtures=[(e, {}) for e in _container_edges()])
-    Wc, Bc, Fc, _ = cs.records()
+    # the static body 0 of every world with its fixtures
     B = np.zeros(int(nb_w.sum()), dtype=abi.BODY)
     F = np.zeros(int(nf_w.sum()), dtype=abi.FIXTURE)
     B[b_start] = Bc[0]
-    for k in range(4):
+    for k in range(nfc):
         F[f_start + k] = Fc[k]
     # dynamic bodies: index of body i of world w = b_start[w] + 1 + i
     widx = np.repeat(np.arange(n_worlds), ns)
     local = np.arange(nbody) - np.repeat(np.concatenate([[0], np.cumsum(ns)[:-1]]), ns)
     bi = b_start[widx] + 1 + local
-    fi = f_start[widx] + 4 + local
+    fi = f_start[widx] + nfc + local
     angle = cat["angle"]
     qc = np.fromiter((math.cos(a) for a in angle.tolist()), float, nbody)
     qs = np.fromiter((math.sin(a) for a in angle.tolist()), float, nbody)
@@ -504,7 +512,7 @@ def uneven_batch(n_worlds: int = 8192, seed: int = 0, counts=None):
     Bd = B[bi]
     Bd["type"] = abi.BODY_DYNAMIC
     Bd["flags"] = abi.BODY_AWAKE | abi.BODY_ALLOW_SLEEP | abi.BODY_ACTIVE
-    Bd["fixture_start"] = 4 + local
+    Bd["fixture_start"] = nfc + local
     Bd["fixture_count"] = 1
     Bd["px"], Bd["py"], Bd["qc"], Bd["qs"] = px, py, qc, qs
     Bd["lcx"], Bd["lcy"] = cx, cy
@@ -567,3 +575,83 @@ def uneven_batch(n_worlds: int = 8192, seed: int = 0, counts=None):
     Wv["move_start"], Wv["move_count"] = f_start, nf_w
     M = np.concatenate([np.arange(k, dtype=np.int32) for k in nf_w]) if n_worlds else np.zeros(0, np.int32)
     return Wv, B, F, M
+
+
+# ------------------------------------------------------------ bullet batch
+# A 20-high stack of 0.5 m boxes (density 1, friction 0.3) on a 40 x 0.5 m
+# ground box, and 4 bullet circles (radius 0.1, density 100) fired from
+# x = -30 at heights U(0.5, 10) with speeds U(150, 250) m/s.
+def bullet_builder(seed: int, stack: int = 20, bullets: int = 4) -> SceneBuilder:
+    r = np.random.default_rng((seed, 5))
+    ys = r.uniform(0.5, 10.0, bullets)
+    vs = r.uniform(150.0, 250.0, bullets)
+    s = SceneBuilder(gravity=(0.0, -10.0), do_sleep=True)
+    s.create_body(abi.BODY_STATIC, position=(0, -0.5), fixtures=[(Polygon(box=(40, 0.5)), {})])
+    box = Polygon(box=(0.5, 0.5))
+    for i in range(stack):
+        s.create_body(abi.BODY_DYNAMIC, position=(0.0, 0.5 + 1.0 * i), fixtures=[(box, dict(density=1.0, friction=0.3))])
+    for k in range(bullets):
+        s.create_body(abi.BODY_DYNAMIC, position=(-30.0, float(ys[k])), bullet=True,
+                      linear_velocity=(float(vs[k]), 0.0), fixtures=[(Circle(radius=0.1), dict(density=100.0))])
+    return s
+
+
+def bullet_batch(n_worlds: int = 2048, seed: int = 0):
+    """n_worlds bullet worlds, world w drawn from seed + w."""
+    return concat([bullet_builder(seed + w).records() for w in range(n_worlds)])
+
+
+# ------------------------------------------------------------ one large world
+# n dynamic bodies (60% boxes with half extents U(0.2, 0.6), 40% circles of
+# radius U(0.2, 0.6); density 1, friction 0.5) on a jittered 1.5 m grid,
+# above a static 600 m ground box with two 200 m side walls; gravity (0, -10).
+LARGE_COLS = 390
+
+
+def _large_draws(seed: int, n: int) -> dict:
+    r = np.random.default_rng((seed, 4))
+    cols = max(1, min(LARGE_COLS, n))
+    k = np.arange(n)
+    jit = r.uniform(-0.1, 0.1, size=(n, 2))
+    px = -0.5 * (cols - 1) * 1.5 + (k % cols) * 1.5 + jit[:, 0]
+    py = 2.0 + (k // cols) * 1.5 + jit[:, 1]
+    circle = r.random(n) < 0.4
+    crad = r.uniform(0.2, 0.6, n)
+    hx = r.uniform(0.2, 0.6, n)
+    hy = r.uniform(0.2, 0.6, n)
+    vx = np.zeros((n, abi.MAX_POLY_VERTS))
+    vy = np.zeros((n, abi.MAX_POLY_VERTS))
+    vx[:, 0], vx[:, 1], vx[:, 2], vx[:, 3] = -hx, hx, hx, -hx
+    vy[:, 0], vy[:, 1], vy[:, 2], vy[:, 3] = -hy, -hy, hy, hy
+    z = np.zeros(n)
+    return dict(n=n, px=px, py=py, circle=circle, crad=crad, nv=np.full(n, 4), vx=vx, vy=vy,
+                density=np.ones(n), friction=np.full(n, 0.5), restitution=z.copy(), v=np.zeros((n, 2)),
+                w=z.copy(), angle=z.copy())
+
+
+def _large_container() -> SceneBuilder:
+    cs = SceneBuilder(gravity=(0.0, -10.0), do_sleep=True)
+    ground = Polygon(vertices=[(-300.0, -1.0), (300.0, -1.0), (300.0, 0.0), (-300.0, 0.0)])
+    left = Polygon(vertices=[(-301.0, 0.0), (-300.0, 0.0), (-300.0, 200.0), (-301.0, 200.0)])
+    right = Polygon(vertices=[(300.0, 0.0), (301.0, 0.0), (301.0, 200.0), (300.0, 200.0)])
+    cs.create_body(abi.BODY_STATIC, position=(0, 0), fixtures=[(ground, {}), (left, {}), (right, {})])
+    return cs
+
+
+def large_builder(seed: int = 0, n: int = 100000) -> SceneBuilder:
+    """The large world built body by body through SceneBuilder (small n)."""
+    d = _large_draws(seed, n)
+    s = _large_container()
+    for i in range(n):
+        if d["circle"][i]:
+            shape = Circle(radius=float(d["crad"][i]))
+        else:
+            shape = Polygon(vertices=list(zip(d["vx"][i, :4].tolist(), d["vy"][i, :4].tolist())))
+        s.create_body(abi.BODY_DYNAMIC, position=(float(d["px"][i]), float(d["py"][i])), angle=0.0,
+                      fixtures=[(shape, dict(density=1.0, friction=0.5, restitution=0.0))])
+    return s
+
+
+def large_world(seed: int = 0, n: int = 100000):
+    """One large world, assembled with numpy (equals large_builder's records)."""
+    return _assemble(_large_container(), [_large_draws(seed, n)])

@@ -88,13 +88,15 @@ def test_warp_mapping_matches_cta_mapping():
         assert_same(o, out[0], "mapping")
 
 
-@pytest.mark.parametrize("n_bodies", [700])
-def test_f64_large_world_bit_exact_with_oracle(n_bodies):
-    """A world large enough for the wide solver launch (512 bodies or more):
-    100 lock steps of an uneven-workload world against the oracle."""
+@pytest.mark.parametrize("kind,n_bodies", [("uneven", 700), ("large", 900)])
+def test_f64_large_world_bit_exact_with_oracle(kind, n_bodies):
+    """Worlds large enough for the wide solver launch (512 bodies or more):
+    100 lock steps of an uneven-workload world and of a piece of the
+    large-world workload (boxes and circles falling into a walled ground)
+    against the oracle."""
     from pypybox2d_gb300 import scenes
     GpuBatch = _gpu()
-    W, B, F, M = scenes.uneven_world(5, n_bodies)
+    W, B, F, M = scenes.uneven_world(5, n_bodies) if kind == "uneven" else scenes.large_world(5, n_bodies)
     gpu = GpuBatch(W, B, F, precision="f64", moves=M)
     orc = oracle_lib.OracleWorld(W, B, F, libm=False, moves=M)
     for s in range(1, 101):

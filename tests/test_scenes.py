@@ -75,3 +75,19 @@ def test_uneven_batch_equals_worlds_built_one_body_at_a_time():
     assert np.array_equal(M, M2)
     n = W["body_count"] - 1
     assert ((n >= scenes.UNEVEN_MIN) & (n <= scenes.UNEVEN_MAX)).all()
+
+
+def test_large_world_equals_world_built_one_body_at_a_time():
+    W, B, F, M = scenes.large_world(3, 120)
+    W2, B2, F2, M2 = scenes.large_builder(3, 120).records()
+    same(W, W2, "world")
+    same(B, B2, "bodies")
+    same(F, F2, "fixtures")
+    assert np.array_equal(M, M2)
+
+
+def test_bullet_batch_layout():
+    W, B, F, M = scenes.bullet_batch(3, seed=9)
+    assert len(W) == 3 and (W["body_count"] == 25).all()
+    bullets = B[(B["flags"] & abi.BODY_BULLET) != 0]
+    assert len(bullets) == 12 and (bullets["vx"] >= 120).all()
