@@ -87,6 +87,8 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
     B.toi_n = a.take<int>(1);
+    B.g_scr = a.take<long long>(2 * (size_t)GB_GRID_MAX_CTAS + 8);
+    B.g_sh = a.take<unsigned char>(GB_GRID_SHARED_BYTES);
 }
 // Re-points the per-step scratch arrays of a batch into one region laid out
 // by `a` (a.base == nullptr only measures it).  The state that outlives a step
@@ -253,6 +255,12 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         b->bd.cache_big = b->bf.cache_big = max_big <= 2048 ? max_big : 0;
         b->bd.cache_small = b->bf.cache_small = max_small;
         b->bd.pipe_bufs = b->bf.pipe_bufs = GB_SOLVE_PIPE_BUFS;
+        // the largest worlds run each phase as one cooperative grid
+        int nh = 0;
+        for (int i : b->launch_order)
+            if (b->hdr[i].nb >= GB_HUGE_BODIES && nh < GB_MAX_HUGE) { b->bd.huge_ids[nh] = b->bf.huge_ids[nh] = i; ++nh; }
+            else break;
+        b->bd.n_huge = b->bf.n_huge = nh;
     }
     CK(cudaMalloc((void **)&b->d_worlds, sizeof(int) * b->nw));
     CK(cudaMemcpy(b->d_worlds, b->launch_order.data(), sizeof(int) * b->nw, cudaMemcpyHostToDevice));

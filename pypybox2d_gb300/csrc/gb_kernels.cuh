@@ -4,6 +4,7 @@
 // reproduces the CPU restatement bit for bit) and gb_f32.cu (GB_REAL = float).
 #pragma once
 #include <cuda_runtime.h>
+#include <type_traits>
 #include "gb_phases.cuh"
 #include "gb_launch.h"
 
@@ -93,6 +94,28 @@ __global__ void k_pack_contacts(Batch<GB_REAL> B, gb_contact *dst, int base, int
 
 }  // namespace
 
+// CTAs of a cooperative launch of k_world_grid<PH>: all resident at once.
+template <int PH> static int grid_ctas() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_world_grid<GB_REAL, PH>, GB_GRID_THREADS, 0);
+        n = sms * (per_sm > 0 ? per_sm : 1);
+        if (n > GB_GRID_MAX_CTAS) n = GB_GRID_MAX_CTAS;
+    }
+    return n;
+}
+template <int PH> static cudaError_t launch_grid(const Batch<GB_REAL> &B, const StepParams &sp, int wi, cudaStream_t st) {
+    Batch<GB_REAL> b = B;
+    StepParams p = sp;
+    int w = wi;
+    void *args[] = {&b, &p, &w};
+    return cudaLaunchCooperativeKernel((const void *)k_world_grid<GB_REAL, PH>, dim3(grid_ctas<PH>()), dim3(GB_GRID_THREADS),
+                                       args, 0, st);
+}
+
 template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *d_worlds,
                                         int n_list, int mode, int threads, cudaStream_t st, KernelTimer *kt) {
     if (n_list <= 0) return 0;
@@ -106,7 +129,17 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
         // the solve kernel stages each world's bodies in shared memory and
         // streams its constraint records through chunk buffers; the largest
         // worlds (first in the list) get a wider launch of their own
+        const int nhuge = B.n_huge < n_list ? B.n_huge : n_list;
         const int nbig = B.n_big < n_list ? B.n_big : n_list;
+        const int n_norm = n_list - nhuge;
+        const int *w_norm = d_worlds + nhuge;
+        auto grid_phase = [&](auto ph, const StepParams &spp) -> cudaError_t {
+            for (int h = 0; h < nhuge; ++h) {
+                cudaError_t e = launch_grid<decltype(ph)::value>(B, spp, B.huge_ids[h], st);
+                if (e != cudaSuccess) return e;
+            }
+            return cudaSuccess;
+        };
         const int tbig = GB_SOLVE_BIG_THREADS;
         Batch<GB_REAL> Bb = B, Bs = B;
         Bb.cache_bodies = B.cache_big;
@@ -125,31 +158,40 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
         StepParams sp1 = sp;
         for (int s = 0; s < n_steps; ++s) {
             const StepParams sp = [&] { StepParams q = sp1; q.step_index = s; return q; }();
+            cudaError_t ge;
+#define GB_GRID(PHX) if ((ge = grid_phase(std::integral_constant<int, PHX>{}, sp)) != cudaSuccess) return (int)ge
             mark(0);
-            k_world<GB_REAL, PH_PAIRS0><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            GB_GRID(PH_PAIRS0);
+            if (n_norm) k_world<GB_REAL, PH_PAIRS0><<<n_norm, threads, 0, st>>>(B, sp, w_norm);
             mark(1);
             if (nb) k_pre<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
             mark(2);
             if (ns) k_collide<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
             mark(3);
-            k_world<GB_REAL, PH_COLLIDE2><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            GB_GRID(PH_COLLIDE2);
+            if (n_norm) k_world<GB_REAL, PH_COLLIDE2><<<n_norm, threads, 0, st>>>(B, sp, w_norm);
             mark(4);
-            k_world<GB_REAL, PH_ISLANDS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            GB_GRID(PH_ISLANDS);
+            if (n_norm) k_world<GB_REAL, PH_ISLANDS><<<n_norm, threads, 0, st>>>(B, sp, w_norm);
             mark(5);
             if (nb) k_vinit<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
             mark(6);
             if (ns) k_cinit<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
             mark(7);
-            if (nbig > 0) k_world<GB_REAL, PH_SOLVE><<<nbig, tbig, smem_big, st>>>(Bb, sp, d_worlds);
+            GB_GRID(PH_SOLVE);
+            if (nbig > nhuge) k_world<GB_REAL, PH_SOLVE><<<nbig - nhuge, tbig, smem_big, st>>>(Bb, sp, w_norm);
             if (n_list > nbig) k_world<GB_REAL, PH_SOLVE><<<n_list - nbig, threads, smem_small, st>>>(Bs, sp, d_worlds + nbig);
             mark(8);
-            k_world<GB_REAL, PH_PAIRS><<<n_list, threads, 0, st>>>(B, sp, d_worlds);
+            GB_GRID(PH_PAIRS);
+            if (n_norm) k_world<GB_REAL, PH_PAIRS><<<n_norm, threads, 0, st>>>(B, sp, w_norm);
             mark(9);
             if (ns) k_toi1<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
             mark(10);
             if (ns) k_toi1b<GB_REAL><<<152 * 4, 128, 0, st>>>(B);
             mark(11);
-            k_world_toi2<GB_REAL><<<n_list, 32, 0, st>>>(B, sp, d_worlds);
+            GB_GRID(PH_TOI2);
+            if (n_norm) k_world_toi2<GB_REAL><<<n_norm, 32, 0, st>>>(B, sp, w_norm);
+#undef GB_GRID
             mark(12);
             if (kt) {
                 cudaError_t e = cudaEventSynchronize(kt->ev[GB_NKTIME]);

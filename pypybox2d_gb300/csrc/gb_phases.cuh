@@ -139,17 +139,13 @@ template <class R> __global__ void __launch_bounds__(32, 24) k_world_toi2(Batch<
     world_phase<R, PH_TOI2>(B, sp, worlds[blockIdx.x]);
 }
 
-template <class R, int PH> __device__ __forceinline__ void world_phase(const Batch<R> &B, const StepParams &sp, const int wi) {
-    __shared__ int sm[96];
-    __shared__ WorldHdr H;
-    __shared__ WShared sh;
-    if (threadIdx.x == 0) { H = B.hdr[wi]; sh.nmove = 0; }
-    __syncthreads();
-    GroupCta g{sm};
+template <class R, int PH, class G> __device__ __forceinline__ void phase_body(const Batch<R> &B, const StepParams &sp, const int wi,
+                                                                              const G &g, WorldHdr &H, WShared &sh,
+                                                                              unsigned char *dyn) {
     WView<R> w{B, &H, H.bbase, H.fbase, H.cbase, wi};
     const bool solving = (H.flags & GB_W_STEP_COMPLETE) && sp.dt > 0.0;
     if (PH == PH_PAIRS0) {
-        if (threadIdx.x == 0) H.pflags = 0;
+        if (g.rank() == 0) H.pflags = 0;
         if (H.flags & GB_W_NEW_FIXTURE) {
             int nf = H.nf;
             int n0 = H.nmove0;
@@ -213,8 +209,7 @@ template <class R, int PH> __device__ __forceinline__ void world_phase(const Bat
             PhaseClock pc;
             pc.acc = (sp.profile && g.rank() == 0) ? B.prof + (size_t)wi * GB_NPROF : nullptr;
             pc.start();
-            extern __shared__ __align__(16) unsigned char gb_dyn_smem[];
-            BodyCache cache{H.nb <= B.cache_bodies ? gb_dyn_smem : nullptr, B.pipe_bufs};
+            BodyCache cache{(dyn && H.nb <= B.cache_bodies) ? dyn : nullptr, B.pipe_bufs};
             solve_group(g, w, sp, &pc, cache);
             sleep_group(g, w, sp);
             if (g.rank() == 0) pc.mark(7);
@@ -245,6 +240,32 @@ template <class R, int PH> __device__ __forceinline__ void world_phase(const Bat
                 B.b_torque[w.bb + b] = (R)0;
             }
     }
+}
+
+template <class R, int PH> __device__ __forceinline__ void world_phase(const Batch<R> &B, const StepParams &sp, const int wi) {
+    __shared__ int sm[96];
+    __shared__ WorldHdr H;
+    __shared__ WShared sh;
+    extern __shared__ __align__(16) unsigned char gb_dyn_smem[];
+    if (threadIdx.x == 0) { H = B.hdr[wi]; sh.nmove = 0; }
+    __syncthreads();
+    GroupCta g{sm};
+    phase_body<R, PH>(B, sp, wi, g, H, sh, gb_dyn_smem);
     __syncthreads();
     if (threadIdx.x == 0) B.hdr[wi] = H;
+}
+
+static_assert(sizeof(WShared) <= GB_GRID_SHARED_BYTES, "WShared of grid worlds");
+
+// The largest worlds (GB_HUGE_BODIES bodies or more) are advanced by a whole
+// cooperative grid: the same phase code with every group operation grid-wide
+// and the world header and scalars in global memory.
+template <class R, int PH> __global__ void __launch_bounds__(GB_GRID_THREADS) k_world_grid(Batch<R> B, StepParams sp, int wi) {
+    __shared__ int sm[96];
+    GroupGrid g{sm, B.g_scr};
+    WorldHdr &H = B.hdr[wi];
+    WShared &sh = *reinterpret_cast<WShared *>(B.g_sh);
+    if (g.rank() == 0) sh.nmove = 0;
+    g.sync();
+    phase_body<R, PH>(B, sp, wi, g, H, sh, nullptr);
 }

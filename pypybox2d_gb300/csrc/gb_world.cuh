@@ -11,6 +11,7 @@
 // results independent of the group size, so the CTA and warp mappings are
 // bit-identical.
 #pragma once
+#include <cooperative_groups.h>
 #include "gb_collide.cuh"
 
 // ---------------------------------------------------------------- layout
@@ -77,6 +78,12 @@ struct WorldHdr {              // per-world scalars (device)
     unsigned long long toimin; // dkey of the earliest first-pass time of impact below 1 (~0: none)
 };
 
+#define GB_HUGE_BODIES 16384       // worlds this large run as one cooperative grid per phase
+#define GB_MAX_HUGE 8
+#define GB_GRID_THREADS 256
+#define GB_GRID_MAX_CTAS 1024
+#define GB_GRID_SHARED_BYTES 1024   // global room for the WShared of a grid world
+
 template <class R> struct Batch {
     int n_worlds, n_bodies, n_slots;
     int cache_bodies;         // worlds of at most this many bodies are solved from shared memory
@@ -124,6 +131,11 @@ template <class R> struct Batch {
     int *toi_n;                  // their count
     gb_event *ev;                // contact events: 3 ccap + 64 per world, from 3 cbase + 64 world
     int *ev_n;                   // events recorded per world
+    // worlds advanced by a cooperative grid (the first n_huge of the size-sorted list)
+    int n_huge;
+    int huge_ids[GB_MAX_HUGE];
+    long long *g_scr;            // their group scratch (2 x grid + 8)
+    void *g_sh;                  // their WShared
 };
 #define GB_NPROF 16
 #define GB_SOLVE_BIG_BODIES 512    // worlds this large are solved by the wide launch
@@ -240,6 +252,66 @@ struct GroupWarp {
             if (k2 < key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
         }
         __syncwarp();
+    }
+};
+
+// A whole cooperative grid working on one world: grid-wide ranks, barriers
+// (grid.sync) and reductions through a global scratch of 2 x gridDim + 8
+// entries (the CTA leaders combine the per-CTA partials).
+struct GroupGrid {
+    int *sm;               // this CTA's shared scratch (>= 96 ints)
+    long long *gs;         // global scratch
+    __device__ __forceinline__ int rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
+    __device__ __forceinline__ int size() const { return gridDim.x * blockDim.x; }
+    __device__ __forceinline__ void sync() const { cooperative_groups::this_grid().sync(); }
+    __device__ bool any(bool p) const {
+        int b = __syncthreads_or(p);
+        if (threadIdx.x == 0) gs[blockIdx.x] = b;
+        sync();
+        if (threadIdx.x == 0) {
+            int r = 0;
+            for (int k = 0; k < (int)gridDim.x; ++k) r |= gs[k] != 0;
+            sm[0] = r;
+        }
+        __syncthreads();
+        bool res = sm[0] != 0;
+        sync();
+        return res;
+    }
+    __device__ int exscan(int v, int *total) const {
+        GroupCta c{sm};
+        int ctot;
+        int ex = c.exscan(v, &ctot);
+        if (threadIdx.x == 0) gs[blockIdx.x] = ctot;
+        sync();
+        if (threadIdx.x == 0) {
+            long long base = 0, tot = 0;
+            for (int k = 0; k < (int)gridDim.x; ++k) { if (k < (int)blockIdx.x) base += gs[k]; tot += gs[k]; }
+            sm[64] = (int)base; sm[65] = (int)tot;
+        }
+        __syncthreads();
+        int base = sm[64];
+        *total = sm[65];
+        sync();
+        return base + ex;
+    }
+    __device__ void argmin(unsigned long long &key, int &idx) const {
+        GroupCta c{sm};
+        c.argmin(key, idx);
+        if (threadIdx.x == 0) { gs[2 * blockIdx.x] = (long long)key; gs[2 * blockIdx.x + 1] = idx; }
+        sync();
+        if (threadIdx.x == 0) {
+            for (int k = 0; k < (int)gridDim.x; ++k) {
+                unsigned long long k2 = (unsigned long long)gs[2 * k];
+                int i2 = (int)gs[2 * k + 1];
+                if (k2 < key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
+            }
+            sm[66] = (int)(unsigned)(key & 0xffffffffull); sm[67] = (int)(unsigned)(key >> 32); sm[68] = idx;
+        }
+        __syncthreads();
+        key = ((unsigned long long)(unsigned)sm[67] << 32) | (unsigned)sm[66];
+        idx = sm[68];
+        sync();
     }
 };
 

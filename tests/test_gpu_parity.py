@@ -105,3 +105,19 @@ def test_f64_large_world_bit_exact_with_oracle(kind, n_bodies):
         assert_same(gpu.bodies(), orc.bodies(), f"large world step {s} bodies")
         assert_same(used_contact_view(gpu.contacts(0)), used_contact_view(orc.contacts()), f"large world step {s} contacts")
     assert int(gpu.status()[0]) == 0
+
+
+def test_f64_grid_world_bit_exact_with_oracle():
+    """A world of 16384+ bodies runs every per-world phase as one cooperative
+    grid; 6 lock steps of a 17000-body piece of the large-world workload."""
+    from pypybox2d_gb300 import scenes
+    GpuBatch = _gpu()
+    W, B, F, M = scenes.large_world(9, 17000)
+    gpu = GpuBatch(W, B, F, precision="f64", moves=M)
+    orc = oracle_lib.OracleWorld(W, B, F, libm=False, moves=M)
+    for s in range(1, 7):
+        gpu.step(1 / 60, 8, 3, 1, launch_mode=3, block_threads=64, record_order=True)
+        orc.step(1 / 60, 8, 3, order=gpu.solver_order(0))
+        assert_same(gpu.bodies(), orc.bodies(), f"grid world step {s} bodies")
+        assert_same(used_contact_view(gpu.contacts(0)), used_contact_view(orc.contacts()), f"grid world step {s} contacts")
+    assert int(gpu.status()[0]) == 0
