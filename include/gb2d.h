@@ -170,7 +170,8 @@ typedef struct gb_world_desc {
     int32_t body_start, body_count;       /* into the batch body array */
     int32_t fixture_start, fixture_count; /* into the batch fixture array */
     int32_t contact_start, contact_count; /* initial contacts (into the batch contact array) */
-    int32_t contact_capacity;             /* device contact slots reserved for this world */
+    int32_t contact_capacity;             /* device contact slots reserved for this world (0: 6 per
+                                             fixture, 10 for worlds of 16384 bodies or more) */
     uint32_t flags;                       /* GB_W_* */
     int32_t move_start, move_count;       /* pending broad-phase move buffer (into scene.moves);
                                              with GB_W_NEW_FIXTURE and move_count == 0 every

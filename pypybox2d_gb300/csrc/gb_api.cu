@@ -87,7 +87,7 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
     B.toi_n = a.take<int>(1);
-    B.g_scr = a.take<long long>(2 * (size_t)GB_GRID_MAX_CTAS + 8);
+    B.g_scr = a.take<long long>(4 * (size_t)GB_GRID_MAX_CTAS + 8);
     B.g_sh = a.take<unsigned char>(GB_GRID_SHARED_BYTES);
 }
 // Re-points the per-step scratch arrays of a batch into one region laid out
@@ -200,7 +200,10 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
                 return fail(GB_E_ARG, "world " + std::to_string(i) + ": move buffer entry outside the world");
             }
         }
-        int cap = d.contact_capacity > 0 ? d.contact_capacity : 6 * d.fixture_count;
+        // default slots: 6 per fixture; 10 for worlds run as a cooperative grid,
+        // whose dense piles hold more fat-AABB pairs per fixture
+        int per = d.body_count >= GB_HUGE_BODIES ? 10 : 6;
+        int cap = d.contact_capacity > 0 ? d.contact_capacity : per * d.fixture_count;
         cap = std::max(std::max(cap, 64), d.contact_count + 16);
         WorldHdr &h = b->hdr[i];
         memset(&h, 0, sizeof(h));

@@ -261,7 +261,9 @@ static_assert(sizeof(WShared) <= GB_GRID_SHARED_BYTES, "WShared of grid worlds")
 // cooperative grid: the same phase code with every group operation grid-wide
 // and the world header and scalars in global memory.
 template <class R, int PH> __global__ void __launch_bounds__(GB_GRID_THREADS) k_world_grid(Batch<R> B, StepParams sp, int wi) {
-    __shared__ int sm[96];
+    __shared__ __align__(16) int sm[96];   // GroupGrid reads sm + 16 as long longs
+    if (threadIdx.x == 0) sm[80] = 0;
+    __syncthreads();
     GroupGrid g{sm, B.g_scr};
     WorldHdr &H = B.hdr[wi];
     WShared &sh = *reinterpret_cast<WShared *>(B.g_sh);

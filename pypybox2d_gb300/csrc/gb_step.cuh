@@ -254,23 +254,37 @@ template <class R, class G> __device__ void build_pair_grid(const G &g, const WV
         sh->nbig = 0;
     }
     g.sync();
+    // each thread reduces its proxies, then one atomic per warp
+    float lsum = 0.0f;
     for (int f = g.rank(); f < nf; f += g.size()) {
         dbox b = aabb[f];
-        atomicAdd(&sh->gsum, (float)fmax(b.z - b.x, b.w - b.y));
+        lsum += (float)fmax(b.z - b.x, b.w - b.y);
     }
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sh->gsum, lsum);
     g.sync();
     if (g.rank() == 0) sh->cut = 4.0 * (double)sh->gsum / (double)nf;
     g.sync();
     const double cut = sh->cut;
+    unsigned long long r[6] = {~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull};
     for (int f = g.rank(); f < nf; f += g.size()) {
         dbox b = aabb[f];
         if (grid_big(b, cut)) continue;
-        atomicMin(&sh->gred[0], dkey(b.x));
-        atomicMin(&sh->gred[1], dkey(b.y));
-        atomicMax(&sh->gred[2], dkey(b.x));
-        atomicMax(&sh->gred[3], dkey(b.y));
-        atomicMax(&sh->gred[4], dkey(b.z - b.x));
-        atomicMax(&sh->gred[5], dkey(b.w - b.y));
+        unsigned long long k[6] = {dkey(b.x), dkey(b.y), dkey(b.x), dkey(b.y), dkey(b.z - b.x), dkey(b.w - b.y)};
+        for (int j = 0; j < 2; ++j) r[j] = k[j] < r[j] ? k[j] : r[j];
+        for (int j = 2; j < 6; ++j) r[j] = k[j] > r[j] ? k[j] : r[j];
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int j = 0; j < 6; ++j) {
+            unsigned long long x = __shfl_xor_sync(0xffffffffu, r[j], o);
+            r[j] = j < 2 ? (x < r[j] ? x : r[j]) : (x > r[j] ? x : r[j]);
+        }
+    if ((threadIdx.x & 31) == 0) {
+        if (r[0] != ~0ull) {
+            atomicMin(&sh->gred[0], r[0]); atomicMin(&sh->gred[1], r[1]);
+            atomicMax(&sh->gred[2], r[2]); atomicMax(&sh->gred[3], r[3]);
+            atomicMax(&sh->gred[4], r[4]); atomicMax(&sh->gred[5], r[5]);
+        }
     }
     g.sync();
     if (g.rank() == 0) {

@@ -256,62 +256,87 @@ struct GroupWarp {
 };
 
 // A whole cooperative grid working on one world: grid-wide ranks, barriers
-// (grid.sync) and reductions through a global scratch of 2 x gridDim + 8
-// entries (the CTA leaders combine the per-CTA partials).
+// (grid.sync) and reductions.  A reduction writes one partial per CTA to a
+// global scratch, syncs the grid once, and every CTA then reduces the
+// partials with all its threads.  Consecutive reductions alternate between
+// two halves of the scratch, so a CTA may start the next one while others
+// still read the previous.  Scratch: 4 x gridDim longs.
 struct GroupGrid {
-    int *sm;               // this CTA's shared scratch (>= 96 ints)
+    int *sm;               // this CTA's shared scratch (>= 96 ints; [80] counts reductions)
     long long *gs;         // global scratch
     __device__ __forceinline__ int rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
     __device__ __forceinline__ int size() const { return gridDim.x * blockDim.x; }
     __device__ __forceinline__ void sync() const { cooperative_groups::this_grid().sync(); }
-    __device__ bool any(bool p) const {
-        int b = __syncthreads_or(p);
-        if (threadIdx.x == 0) gs[blockIdx.x] = b;
-        sync();
-        if (threadIdx.x == 0) {
-            int r = 0;
-            for (int k = 0; k < (int)gridDim.x; ++k) r |= gs[k] != 0;
-            sm[0] = r;
-        }
+    // this reduction's half of the scratch (2 x gridDim longs)
+    __device__ __forceinline__ long long *half() const {
+        long long *h = gs + ((sm[80] & 1) ? 2 * (size_t)gridDim.x : 0);
+        return h;
+    }
+    __device__ __forceinline__ void next() const {
         __syncthreads();
-        bool res = sm[0] != 0;
+        if (threadIdx.x == 0) sm[80] += 1;
+        __syncthreads();
+    }
+    // sums over the CTA of (a, b); every thread gets them
+    __device__ void cta_sum2(long long &a, long long &b) const {
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        long long *s64 = reinterpret_cast<long long *>(sm + 16);   // sm[16..47]: 8 warps x 2 longs
+        int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+        if (lane == 0) { s64[2 * warp] = a; s64[2 * warp + 1] = b; }
+        __syncthreads();
+        a = 0; b = 0;
+        for (int k = 0; k < nw; ++k) { a += s64[2 * k]; b += s64[2 * k + 1]; }
+        __syncthreads();
+    }
+    __device__ bool any(bool p) const {
+        int bflag = __syncthreads_or(p);
+        long long *h = half();
+        if (threadIdx.x == 0) h[blockIdx.x] = bflag;
         sync();
-        return res;
+        long long a = 0, b = 0;
+        for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) a |= h[k];
+        cta_sum2(a, b);
+        next();
+        return a != 0;
     }
     __device__ int exscan(int v, int *total) const {
         GroupCta c{sm};
         int ctot;
         int ex = c.exscan(v, &ctot);
-        if (threadIdx.x == 0) gs[blockIdx.x] = ctot;
+        long long *h = half();
+        if (threadIdx.x == 0) h[blockIdx.x] = ctot;
         sync();
-        if (threadIdx.x == 0) {
-            long long base = 0, tot = 0;
-            for (int k = 0; k < (int)gridDim.x; ++k) { if (k < (int)blockIdx.x) base += gs[k]; tot += gs[k]; }
-            sm[64] = (int)base; sm[65] = (int)tot;
+        long long base = 0, tot = 0;
+        for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+            long long x = h[k];
+            if (k < (int)blockIdx.x) base += x;
+            tot += x;
         }
-        __syncthreads();
-        int base = sm[64];
-        *total = sm[65];
-        sync();
-        return base + ex;
+        cta_sum2(base, tot);
+        *total = (int)tot;
+        next();
+        return (int)base + ex;
     }
     __device__ void argmin(unsigned long long &key, int &idx) const {
         GroupCta c{sm};
         c.argmin(key, idx);
-        if (threadIdx.x == 0) { gs[2 * blockIdx.x] = (long long)key; gs[2 * blockIdx.x + 1] = idx; }
+        long long *h = half();
+        if (threadIdx.x == 0) { h[2 * blockIdx.x] = (long long)key; h[2 * blockIdx.x + 1] = idx; }
         sync();
-        if (threadIdx.x == 0) {
-            for (int k = 0; k < (int)gridDim.x; ++k) {
-                unsigned long long k2 = (unsigned long long)gs[2 * k];
-                int i2 = (int)gs[2 * k + 1];
-                if (k2 < key || (k2 == key && i2 < idx)) { key = k2; idx = i2; }
-            }
-            sm[66] = (int)(unsigned)(key & 0xffffffffull); sm[67] = (int)(unsigned)(key >> 32); sm[68] = idx;
+        unsigned long long bk = ~0ull;
+        int bi = 0x7fffffff;
+        for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+            unsigned long long k2 = (unsigned long long)h[2 * k];
+            int i2 = (int)h[2 * k + 1];
+            if (k2 < bk || (k2 == bk && i2 < bi)) { bk = k2; bi = i2; }
         }
-        __syncthreads();
-        key = ((unsigned long long)(unsigned)sm[67] << 32) | (unsigned)sm[66];
-        idx = sm[68];
-        sync();
+        c.argmin(bk, bi);
+        key = bk;
+        idx = bi;
+        next();
     }
 };
 
