@@ -73,7 +73,7 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_minsleep = a.take<unsigned long long>(nb);
     B.s_bvis = a.take<unsigned char>(nb);
     B.s_move = a.take<int>(nf); B.s_first = a.take<int>(nf); B.s_cnt = a.take<int>(nf);
-    B.s_grid = a.take<int>(3 * (size_t)nf + 2 * (size_t)nw);
+    B.s_grid = a.take<int>(12 * (size_t)nf + 2 * (size_t)nw);
     B.s_proc = a.take<int>(ncap); B.s_pref = a.take<int>(ncap); B.s_adj = a.take<int>(2 * (size_t)ncap);
     B.s_colour = a.take<int>(ncap); B.s_order = a.take<int>(ncap); B.s_cons_of = a.take<int>(ncap);
     B.s_cvis = a.take<unsigned char>(ncap);
@@ -102,7 +102,7 @@ template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb
     B.s_minsleep = a.take<unsigned long long>(nb);
     B.s_bvis = a.take<unsigned char>(nb);
     B.s_first = a.take<int>(nf); B.s_cnt = a.take<int>(nf);
-    B.s_grid = a.take<int>(3 * (size_t)nf + 2 * (size_t)nw);
+    B.s_grid = a.take<int>(12 * (size_t)nf + 2 * (size_t)nw);
     B.s_proc = a.take<int>(ncap); B.s_pref = a.take<int>(ncap); B.s_adj = a.take<int>(2 * (size_t)ncap);
     B.s_colour = a.take<int>(ncap); B.s_order = a.take<int>(ncap); B.s_cons_of = a.take<int>(ncap);
     B.s_cvis = a.take<unsigned char>(ncap);

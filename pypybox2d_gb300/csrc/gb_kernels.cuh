@@ -166,7 +166,10 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
             mark(1);
             if (nb) k_pre<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
             mark(2);
-            if (ns) k_collide<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
+            if (ns) {
+                if (sp.events) k_collide<GB_REAL, true><<<gs, T, 0, st>>>(B, ns, sp);
+                else k_collide<GB_REAL, false><<<gs, T, 0, st>>>(B, ns, sp);
+            }
             mark(3);
             GB_GRID(PH_COLLIDE2);
             if (n_norm) k_world<GB_REAL, PH_COLLIDE2><<<n_norm, threads, 0, st>>>(B, sp, w_norm);

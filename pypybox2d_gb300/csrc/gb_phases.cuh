@@ -47,7 +47,7 @@ template <class R> __global__ void k_pre(Batch<R> B, int n_bodies, StepParams sp
     if ((H->flags & GB_W_CONTINUOUS) && (H->flags & GB_W_STEP_COMPLETE) && sp.dt > 0.0) B.b_alpha0[b] = 0.0;
 }
 
-template <class R> __global__ void k_collide(Batch<R> B, int n_slots, StepParams sp) {
+template <class R, bool EV> __global__ void k_collide(Batch<R> B, int n_slots, StepParams sp) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n_slots) return;
     int wi = B.c_world[s];
@@ -57,7 +57,7 @@ template <class R> __global__ void k_collide(Batch<R> B, int n_slots, StepParams
     int *wake = B.s_wake + w.bb;
     bool woke;
     const EvCtx ev{sp.events, sp.step_index, GB_EV_PHASE_UPDATE};
-    int r = collide_one(w, i, wake, &woke, &ev);
+    int r = collide_one<R, EV>(w, i, wake, &woke, &ev);
     B.s_proc[s] = r;
     if (r == 0) { atomicOr(&w.H->pflags, P_DEFERRED); return; }
     if (r == 2) { atomicOr(&w.H->pflags, P_DESTROY); return; }

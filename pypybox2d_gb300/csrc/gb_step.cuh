@@ -49,6 +49,7 @@ struct WShared {
     int ncons, ncolours;
     int pass;
     int all_allow_sleep;
+    int lhcap;            // slots of the TOI loop's pair hash
     // pair-finding grid of the world (find_new_contacts)
     unsigned long long gred[6];
     float gsum;
@@ -106,8 +107,8 @@ template <class R> __device__ __forceinline__ bool fx_sensor(const WView<R> &w, 
 
 // Append one contact event of the world (index < 0: keyed by its slot,
 // which is the order of occurrence when one thread records).
-template <class R> __device__ void record_event(const WView<R> &w, const EvCtx &ev, int type, int i, int index, int npts,
-                                                const R *ni, const R *ti) {
+template <class R> __device__ __noinline__ void record_event(const WView<R> &w, const EvCtx &ev, int type, int i, int index, int npts,
+                                                             const R *ni, const R *ti) {
     const ContactRec<R> &c = w.con(i);
     int slot = atomicAdd(&w.B.ev_n[w.wi], 1);
     if (slot >= 3 * w.H->ccap + 64) { atomicOr(&w.H->status, GB_ST_EVENT_OVERFLOW); return; }
@@ -123,7 +124,8 @@ template <class R> __device__ void record_event(const WView<R> &w, const EvCtx &
 // contact.py:210-268 Contact.update; returns whether touching changed (the
 // wake rule; sensors never wake).  With `ev` on, a change of touching, of a
 // sensor too, is recorded as a begin or end event (contact.py:263-266).
-template <class R> __device__ bool contact_update(const WView<R> &w, int i, const EvCtx *ev = nullptr, int ev_index = -1) {
+template <class R, bool EV = true> __device__ bool contact_update(const WView<R> &w, int i, const EvCtx *ev = nullptr,
+                                                                  int ev_index = -1) {
     ContactRec<R> &c = w.con(i);
     Manifold<R> old = c.m;
     c.flags |= GB_C_ENABLED;
@@ -153,7 +155,7 @@ template <class R> __device__ bool contact_update(const WView<R> &w, int i, cons
         changed = touching != was;
     }
     if (touching) c.flags |= GB_C_TOUCHING; else c.flags &= ~GB_C_TOUCHING;
-    if (ev && ev->on && touching != was)
+    if (EV && ev && ev->on && touching != was)
         record_event<R>(w, *ev, touching ? GB_EV_BEGIN : GB_EV_END, i, ev_index, 0, nullptr, nullptr);
     return changed;
 }
@@ -227,14 +229,19 @@ template <class R> __device__ __forceinline__ bool pair_candidate(const WView<R>
     return true;
 }
 
-// Uniform grid over the lower corners of the world's fat AABBs, rebuilt for
-// each pair-finding pass.  Proxies larger than four times the mean extent
-// (ground boxes, container edges) are "big": they stay out of the grid and
-// are tested against every moved proxy, and a moved big proxy tests every
-// proxy.  The grid only prunes candidates: every pair is still decided by
-// the exact float64 overlap test, and the pairs of a moved proxy are sorted
-// by the other proxy's index, so the result does not depend on the grid.
+// Uniform grid over the world's fat AABBs, rebuilt for each pair-finding
+// pass: a proxy is listed in every cell its box overlaps (cells twice the
+// mean extent, so a box spans at most 3 x 3); proxies larger than four times
+// the mean extent (ground boxes, container edges) are "big": they stay out
+// of the grid and are tested against every moved proxy.  A moved proxy, big
+// or not, scans the cells its box overlaps and takes a listed proxy only in
+// the cell holding the lower-left corner of the two boxes' intersection, so
+// each overlapping pair is seen once.
+// The grid only prunes: every pair is still decided by the exact float64
+// overlap test, and the pairs of a moved proxy are sorted by the other
+// proxy's index, so the result does not depend on the grid.
 #define GB_GRID_MIN_MOVES 8
+#define GB_GRID_ITEMS_PER_FIXTURE 9
 static __device__ __forceinline__ int grid_cell(double x, double x0, double inv_h, int n) {
     double t = floor((x - x0) * inv_h);
     t = fmin(fmax(t, 0.0), (double)(n - 1));
@@ -244,13 +251,16 @@ static __device__ __forceinline__ bool grid_big(const dbox &b, double cut) {
     return (b.z - b.x) > cut || (b.w - b.y) > cut;
 }
 
-template <class R, class G> __device__ void build_pair_grid(const G &g, const WView<R> &w, WShared *sh, int *goff, int *gitem) {
+// Scratch of one world (s_grid): cell ends (2 nf + 2), listed proxies
+// (9 nf), big proxies (nf).
+template <class R, class G> __device__ void build_pair_grid(const G &g, const WView<R> &w, WShared *sh, int *goff, int *gitem,
+                                                            int *gbig) {
     const int nf = w.H->nf;
     const dbox *aabb = w.B.f_aabb + w.fb;
     if (g.rank() == 0) {
         sh->gsum = 0.0f;
         sh->gred[0] = sh->gred[1] = ~0ull;
-        sh->gred[2] = sh->gred[3] = sh->gred[4] = sh->gred[5] = 0ull;
+        sh->gred[2] = sh->gred[3] = 0ull;
         sh->nbig = 0;
     }
     g.sync();
@@ -266,35 +276,31 @@ template <class R, class G> __device__ void build_pair_grid(const G &g, const WV
     if (g.rank() == 0) sh->cut = 4.0 * (double)sh->gsum / (double)nf;
     g.sync();
     const double cut = sh->cut;
-    unsigned long long r[6] = {~0ull, ~0ull, 0ull, 0ull, 0ull, 0ull};
+    unsigned long long r[4] = {~0ull, ~0ull, 0ull, 0ull};
     for (int f = g.rank(); f < nf; f += g.size()) {
         dbox b = aabb[f];
         if (grid_big(b, cut)) continue;
-        unsigned long long k[6] = {dkey(b.x), dkey(b.y), dkey(b.x), dkey(b.y), dkey(b.z - b.x), dkey(b.w - b.y)};
+        unsigned long long k[4] = {dkey(b.x), dkey(b.y), dkey(b.z), dkey(b.w)};
         for (int j = 0; j < 2; ++j) r[j] = k[j] < r[j] ? k[j] : r[j];
-        for (int j = 2; j < 6; ++j) r[j] = k[j] > r[j] ? k[j] : r[j];
+        for (int j = 2; j < 4; ++j) r[j] = k[j] > r[j] ? k[j] : r[j];
     }
     for (int o = 16; o > 0; o >>= 1)
-        for (int j = 0; j < 6; ++j) {
+        for (int j = 0; j < 4; ++j) {
             unsigned long long x = __shfl_xor_sync(0xffffffffu, r[j], o);
             r[j] = j < 2 ? (x < r[j] ? x : r[j]) : (x > r[j] ? x : r[j]);
         }
-    if ((threadIdx.x & 31) == 0) {
-        if (r[0] != ~0ull) {
-            atomicMin(&sh->gred[0], r[0]); atomicMin(&sh->gred[1], r[1]);
-            atomicMax(&sh->gred[2], r[2]); atomicMax(&sh->gred[3], r[3]);
-            atomicMax(&sh->gred[4], r[4]); atomicMax(&sh->gred[5], r[5]);
-        }
+    if ((threadIdx.x & 31) == 0 && r[0] != ~0ull) {
+        atomicMin(&sh->gred[0], r[0]); atomicMin(&sh->gred[1], r[1]);
+        atomicMax(&sh->gred[2], r[2]); atomicMax(&sh->gred[3], r[3]);
     }
     g.sync();
     if (g.rank() == 0) {
         int gx = 1, gy = 1;
-        double x0 = 0.0, y0 = 0.0, h = 1.0, mw = 0.0, mh = 0.0;
+        double x0 = 0.0, y0 = 0.0, h = 1.0;
         if (sh->gred[0] != ~0ull) {
             x0 = dkey_inv(sh->gred[0]); y0 = dkey_inv(sh->gred[1]);
             double sx = dkey_inv(sh->gred[2]) - x0, sy = dkey_inv(sh->gred[3]) - y0;
-            mw = dkey_inv(sh->gred[4]); mh = dkey_inv(sh->gred[5]);
-            h = fmax(fmax(mw, mh), 1e-6);
+            h = fmax(0.5 * cut, 1e-6);   // twice the mean extent
             const double cap = 2.0 * nf;
             for (int k = 0; k < 64; ++k) {   // at most 2 nf cells
                 double cx = floor(sx / h) + 1.0, cy = floor(sy / h) + 1.0;
@@ -302,7 +308,7 @@ template <class R, class G> __device__ void build_pair_grid(const G &g, const WV
                 h *= 1.5;
             }
         }
-        sh->x0 = x0; sh->y0 = y0; sh->inv_h = 1.0 / h; sh->maxw = mw; sh->maxh = mh;
+        sh->x0 = x0; sh->y0 = y0; sh->inv_h = 1.0 / h;
         sh->gx = gx; sh->gy = gy;
     }
     g.sync();
@@ -314,21 +320,30 @@ template <class R, class G> __device__ void build_pair_grid(const G &g, const WV
     for (int f = g.rank(); f < nf; f += g.size()) {
         dbox b = aabb[f];
         if (grid_big(b, cut)) continue;
-        atomicAdd(&goff[grid_cell(b.y, y0, ih, gy) * gx + grid_cell(b.x, x0, ih, gx)], 1);
+        const int cx0 = grid_cell(b.x, x0, ih, gx), cx1 = grid_cell(b.z, x0, ih, gx);
+        const int cy0 = grid_cell(b.y, y0, ih, gy), cy1 = grid_cell(b.w, y0, ih, gy);
+        for (int cy = cy0; cy <= cy1; ++cy)
+            for (int cx = cx0; cx <= cx1; ++cx) atomicAdd(&goff[cy * gx + cx], 1);
     }
     g.sync();
-    int nsmall = group_scan(g, ncell, [&](int c) { return goff[c]; }, goff);
+    int nitems = group_scan(g, ncell, [&](int c) { return goff[c]; }, goff);
     g.sync();
-    if (g.rank() == 0) sh->nsmall = nsmall;
+    if (nitems > GB_GRID_ITEMS_PER_FIXTURE * nf) {   // cannot happen for boxes below the cut; never past the scratch
+        if (g.rank() == 0) sh->gx = 0;
+        g.sync();
+        return;
+    }
     // scatter: afterwards goff[c] is the end of cell c (its start is goff[c - 1])
     for (int f = g.rank(); f < nf; f += g.size()) {
         dbox b = aabb[f];
         if (grid_big(b, cut)) {
-            gitem[nsmall + atomicAdd(&sh->nbig, 1)] = f;
-        } else {
-            int c = grid_cell(b.y, y0, ih, gy) * gx + grid_cell(b.x, x0, ih, gx);
-            gitem[atomicAdd(&goff[c], 1)] = f;
+            gbig[atomicAdd(&sh->nbig, 1)] = f;
+            continue;
         }
+        const int cx0 = grid_cell(b.x, x0, ih, gx), cx1 = grid_cell(b.z, x0, ih, gx);
+        const int cy0 = grid_cell(b.y, y0, ih, gy), cy1 = grid_cell(b.w, y0, ih, gy);
+        for (int cy = cy0; cy <= cy1; ++cy)
+            for (int cx = cx0; cx <= cx1; ++cx) gitem[atomicAdd(&goff[cy * gx + cx], 1)] = f;
     }
     g.sync();
 }
@@ -373,14 +388,19 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
     g.sync();
     // candidate proxies of a moved proxy: the grid cells its fat AABB can
     // reach plus the big proxies, or every proxy (in index order)
-    const bool use_grid = nmove >= GB_GRID_MIN_MOVES;
-    int *goff = w.B.s_grid + 3 * (size_t)w.fb + 2 * (size_t)w.wi;
+    int *goff = w.B.s_grid + 12 * (size_t)w.fb + 2 * (size_t)w.wi;
     int *gitem = goff + 2 * (size_t)nf + 2;
-    if (use_grid) build_pair_grid(g, w, sh, goff, gitem);
+    int *gbig = gitem + GB_GRID_ITEMS_PER_FIXTURE * (size_t)nf;
+    bool use_grid = nmove >= GB_GRID_MIN_MOVES;
+    if (use_grid) {
+        build_pair_grid(g, w, sh, goff, gitem, gbig);
+        use_grid = sh->gx > 0;
+    }
     const dbox *aabb = w.B.f_aabb + w.fb;
-    auto gridded = [&](int p) { return use_grid && !grid_big(aabb[p], sh->cut); };
+    // with a grid every moved proxy, big ones too, scans the cells its box
+    // overlaps (the ground box: the bottom row) and the big list
     auto each_candidate = [&](int i, int p, auto &&emit) {
-        if (!gridded(p)) {
+        if (!use_grid) {
             for (int q = 0; q < nf; ++q)
                 if (pair_candidate(w, i, p, q, first, hash, hmask)) emit(q);
             return;
@@ -388,22 +408,21 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
         const dbox b = aabb[p];
         const double x0 = sh->x0, y0 = sh->y0, ih = sh->inv_h;
         const int gx = sh->gx, gy = sh->gy;
-        // a proxy overlapping b has its lower corner within the largest
-        // gridded extent below b's lower corner (with a rounding margin)
-        const double lx = b.x - (sh->maxw + (fabs(b.x) + sh->maxw) * 1e-12);
-        const double ly = b.y - (sh->maxh + (fabs(b.y) + sh->maxh) * 1e-12);
-        const int cx0 = grid_cell(lx, x0, ih, gx), cx1 = grid_cell(b.z, x0, ih, gx);
-        const int cy0 = grid_cell(ly, y0, ih, gy), cy1 = grid_cell(b.w, y0, ih, gy);
+        const int cx0 = grid_cell(b.x, x0, ih, gx), cx1 = grid_cell(b.z, x0, ih, gx);
+        const int cy0 = grid_cell(b.y, y0, ih, gy), cy1 = grid_cell(b.w, y0, ih, gy);
         for (int cy = cy0; cy <= cy1; ++cy)
             for (int cx = cx0; cx <= cx1; ++cx) {
                 int c = cy * gx + cx;
                 for (int k = c ? goff[c - 1] : 0; k < goff[c]; ++k) {
                     int q = gitem[k];
+                    const dbox o = aabb[q];
+                    // the cell of the intersection's lower-left corner owns the pair
+                    if (grid_cell(fmax(b.x, o.x), x0, ih, gx) != cx || grid_cell(fmax(b.y, o.y), y0, ih, gy) != cy) continue;
                     if (pair_candidate(w, i, p, q, first, hash, hmask)) emit(q);
                 }
             }
-        for (int k = sh->nsmall; k < sh->nsmall + sh->nbig; ++k) {
-            int q = gitem[k];
+        for (int k = 0; k < sh->nbig; ++k) {
+            int q = gbig[k];
             if (pair_candidate(w, i, p, q, first, hash, hmask)) emit(q);
         }
     };
@@ -431,7 +450,7 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
             if (k < room) { pq[k] = q; pp[k] = p; }
             ++k;
         });
-        if (gridded(p)) {
+        if (use_grid) {
             const int end = k < room ? k : room;
             for (int a = base + 1; a < end; ++a) {   // insertion sort by proxy index
                 int v = pq[a], b = a - 1;
@@ -477,7 +496,8 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
 // loop starts).  Returns 0 when both bodies are inactive at that point,
 // 1 after Contact.update (*woke: touching changed, both bodies woken), 2 when
 // the contact is to be destroyed.
-template <class R> __device__ int collide_one(const WView<R> &w, int i, const int *wake, bool *woke, const EvCtx *ev = nullptr) {
+template <class R, bool EV = true> __device__ int collide_one(const WView<R> &w, int i, const int *wake, bool *woke,
+                                                             const EvCtx *ev = nullptr) {
     ContactRec<R> &c = w.con(i);
     int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
     bool act_a = w.btype(ba) != GB_BODY_STATIC && wake[ba] < i;
@@ -491,10 +511,10 @@ template <class R> __device__ int collide_one(const WView<R> &w, int i, const in
     }
     if (!destroy && !aabb_overlap(w.B.f_aabb[w.fb + c.fa], w.B.f_aabb[w.fb + c.fb])) destroy = true;
     if (destroy) {   // contact_manager.py:160-172: a touching contact ends as it is destroyed
-        if (ev && ev->on && (c.flags & GB_C_TOUCHING)) record_event<R>(w, *ev, GB_EV_END, i, i, 0, nullptr, nullptr);
+        if (EV && ev && ev->on && (c.flags & GB_C_TOUCHING)) record_event<R>(w, *ev, GB_EV_END, i, i, 0, nullptr, nullptr);
         return 2;
     }
-    *woke = contact_update(w, i, ev, i);
+    *woke = contact_update<R, EV>(w, i, ev, i);
     return 1;
 }
 

@@ -274,6 +274,151 @@ template <class R, class F> __device__ __forceinline__ void body_contacts(const 
     }
 }
 
+// Hash set of the world's contact pairs (unordered fixture pairs), open
+// addressing; the TOI loop keeps one for its whole run.
+static __device__ __forceinline__ unsigned long long pair_key(int p, int q) {
+    return (((unsigned long long)(unsigned)min(p, q) << 32) | (unsigned)max(p, q)) + 1ull;
+}
+static __device__ __forceinline__ bool pair_hash_has(const unsigned long long *hash, int hmask, int p, int q) {
+    const unsigned long long key = pair_key(p, q);
+    unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 32) & hmask;
+    for (int probe = 0; probe <= hmask; ++probe) {
+        unsigned long long k = hash[h];
+        if (k == key) return true;
+        if (k == 0ull) return false;
+        h = (h + 1) & hmask;
+    }
+    return false;
+}
+static __device__ __forceinline__ void pair_hash_put(unsigned long long *hash, int hmask, int p, int q) {
+    const unsigned long long key = pair_key(p, q);
+    unsigned h = (unsigned)((key * 0x9E3779B97F4A7C15ull) >> 32) & hmask;
+    for (int probe = 0; probe <= hmask; ++probe) {
+        unsigned long long prev = atomicCAS(&hash[h], 0ull, key);
+        if (prev == 0ull || prev == key) return;
+        h = (h + 1) & hmask;
+    }
+}
+
+// Pair finding after a TOI event (broadphase.py:83-109 +
+// contact_manager.py:102-158 for the few proxies the event re-fattened):
+// every (moved proxy, proxy) pair is tested in parallel, existing pairs come
+// from the loop's pair hash, and each moved proxy's new pairs are sorted by
+// the other proxy's index -- the pairs and the order of find_new_contacts,
+// without its passes over every contact and proxy of the world.
+// Slots for a pair hash of n contacts: a power of two of at least 2 (n + 64),
+// at most the largest power of two in the world's 4 x ccap scratch slots.
+template <class R> __device__ __forceinline__ int pair_hash_cap(const WView<R> &w, int n) {
+    int hmax = 16;
+    while (2 * hmax <= 4 * w.H->ccap) hmax <<= 1;
+    int hcap = 16;
+    while (hcap < 2 * (n + 64) && hcap < hmax) hcap <<= 1;
+    return hcap;
+}
+// (Re)build the loop's pair hash over contacts [0, nc).
+template <class R, class G> __device__ void build_loop_hash(const G &g, const WView<R> &w, WShared *sh, unsigned long long *hash, int nc,
+                                                            int n_expected) {
+    const int hcap = pair_hash_cap(w, n_expected);
+    for (int k = g.rank(); k < hcap; k += g.size()) hash[k] = 0ull;
+    g.sync();
+    for (int i = g.rank(); i < nc; i += g.size()) pair_hash_put(hash, hcap - 1, w.con(i).fa, w.con(i).fb);
+    if (g.rank() == 0) sh->lhcap = hcap;
+    g.sync();
+}
+
+template <class R, class G> __device__ void toi_find_pairs(const G &g, const WView<R> &w, WShared *sh, unsigned long long *hash) {
+    const int nmove = sh->nmove;
+    if (nmove == 0) return;
+    int hmask = sh->lhcap - 1;
+    const int nf = w.H->nf;
+    const int *mv = w.B.s_move + w.fb;
+    int *cnt = w.B.s_cnt + w.fb;      // new pairs per move-buffer entry, then their start
+    int *cur = w.B.s_first + w.fb;    // fill counters
+    int *pq = w.B.s_colour + w.cb;    // other proxy of new pair t (free during the TOI loop)
+    int *pp = w.B.s_order + w.cb;     // moved proxy of new pair t
+    const int nc = w.H->nc, ccap = w.H->ccap, room = ccap - nc;
+    for (int i = g.rank(); i < nmove; i += g.size()) { cnt[i] = 0; cur[i] = 0; }
+    g.sync();
+    auto earlier = [&](int i, int f) {
+        for (int j = 0; j < i; ++j)
+            if (mv[j] == f) return true;
+        return false;
+    };
+    auto new_pair = [&](int i, int q) -> bool {
+        const int p = mv[i];
+        if (q == p || earlier(i, q)) return false;   // a proxy moved earlier made this pair
+        if (!aabb_overlap(w.B.f_aabb[w.fb + q], w.B.f_aabb[w.fb + p])) return false;
+        const int ba = w.fbody(p), bb = w.fbody(q);
+        if (ba == bb) return false;
+        if (pair_hash_has(hash, hmask, p, q)) return false;
+        if (!should_collide(w, bb, ba)) return false;
+        if (!default_filter(w, p, q)) return false;
+        bool prim;
+        return pair_registered(w.B.f_type[w.fb + p], w.B.f_type[w.fb + q], &prim);
+    };
+    const long long items = (long long)nmove * nf;
+    for (long long t = g.rank(); t < items; t += g.size()) {
+        const int i = (int)(t / nf), q = (int)(t - (long long)i * nf);
+        if (!earlier(i, mv[i]) && new_pair(i, q)) atomicAdd(&cnt[i], 1);
+    }
+    g.sync();
+    if (g.rank() == 0) {
+        int acc = 0;
+        for (int i = 0; i < nmove; ++i) { int c = cnt[i]; cnt[i] = acc; acc += c; }
+        sh->red = (unsigned long long)acc;
+    }
+    g.sync();
+    const int total = (int)sh->red;
+    for (long long t = g.rank(); t < items; t += g.size()) {
+        const int i = (int)(t / nf), q = (int)(t - (long long)i * nf);
+        if (!earlier(i, mv[i]) && new_pair(i, q)) {
+            const int k = cnt[i] + atomicAdd(&cur[i], 1);
+            if (k < room) { pq[k] = q; pp[k] = mv[i]; }
+        }
+    }
+    g.sync();
+    for (int i = g.rank(); i < nmove; i += g.size()) {   // by the other proxy's index
+        const int b0 = cnt[i], b1 = min(b0 + cur[i], room);
+        for (int a = b0 + 1; a < b1; ++a) {
+            int v = pq[a], b = a - 1;
+            while (b >= b0 && pq[b] > v) { pq[b + 1] = pq[b]; --b; }
+            pq[b + 1] = v;
+        }
+    }
+    g.sync();
+    const int ncreate = total < room ? total : room;
+    if (2 * (nc + ncreate) > sh->lhcap) {   // keep the hash at most half full
+        build_loop_hash(g, w, sh, hash, nc, 2 * (nc + ncreate));
+        hmask = sh->lhcap - 1;
+    }
+    for (int t = g.rank(); t < ncreate; t += g.size()) {
+        const int p = pp[t], q = pq[t];
+        int fa = p, fb = q;
+        bool prim;
+        pair_registered(w.B.f_type[w.fb + p], w.B.f_type[w.fb + q], &prim);
+        if (!prim) { fa = q; fb = p; }
+        ContactRec<R> &c = w.con(nc + t);
+        c.fa = fa; c.fb = fb;
+        c.flags = 0; c.toi_count = 0; c.toi = 0.0;
+        R fra = w.B.f_friction[w.fb + fa], frb = w.B.f_friction[w.fb + fb];
+        c.friction = sqrt(fra * frb);
+        c.restitution = pymax(w.B.f_restitution[w.fb + fa], w.B.f_restitution[w.fb + fb]);
+        Manifold<R> &m = c.m;
+        m.type = GB_M_CIRCLES; m.count = 0;
+        m.ln = mk<R>(0, 0); m.lp = mk<R>(0, 0);
+        for (int k = 0; k < 2; ++k) { m.plp[k] = mk<R>(0, 0); m.ni[k] = (R)0; m.ti[k] = (R)0; m.id[k] = 0; }
+        pair_hash_put(hash, hmask, p, q);
+    }
+    g.sync();
+    if (g.rank() == 0) {
+        int nn = nc + total;
+        if (nn > ccap) { w.H->status |= GB_ST_CONTACT_OVERFLOW; nn = ccap; }
+        w.H->nc = nn;
+        sh->nmove = 0;
+    }
+    g.sync();
+}
+
 // The event loop of world.py:612-821; `first_done` means pass 0 already ran
 // (in the batch-wide kernel).  Passes scan the candidate list only, and the
 // contact lists of the event bodies come from a per-body adjacency built
@@ -321,6 +466,9 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
             while (j >= off[b] && adj[j] > v) { adj[j + 1] = adj[j]; --j; }
             adj[j + 1] = v;
         }
+    // the pair hash of the loop (every contact, then those events create)
+    unsigned long long *lhash = w.B.s_hash + 4 * (size_t)w.cb;
+    build_loop_hash(g, w, sh, lhash, nc0, nc0);
     // candidates in list order
     int ncand = group_scan(g, nc0, [&](int i) { return toi_candidate(w, i) ? 1 : 0; }, ids);
     g.sync();
@@ -413,7 +561,7 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
         g.sync();
         for (int k = g.rank(); k < nisl; k += g.size()) bflag[isl[k]] = 0;
         g.sync();
-        find_new_contacts(g, w, sh);
+        toi_find_pairs(g, w, sh, lhash);
         // new contacts join the candidate list (they follow every older one)
         const int nc2 = w.H->nc;
         if (nc2 > nc) {

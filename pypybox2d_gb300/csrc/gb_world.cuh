@@ -115,7 +115,7 @@ template <class R> struct Batch {
     unsigned char *s_bvis;
     // scratch (fixture-indexed)
     int *s_move, *s_first, *s_cnt;
-    int *s_grid;              // pair-finding grid: 3 nf + 2 ints per world (cell ends, proxies by cell)
+    int *s_grid;              // pair-finding grid: 12 nf + 2 ints per world (cell ends, listed and big proxies)
     // scratch (contact-slot-indexed)
     int *s_proc, *s_pref, *s_adj, *s_colour, *s_order, *s_cons_of;
     int2 *s_kb;
