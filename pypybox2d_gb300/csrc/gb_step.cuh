@@ -105,20 +105,26 @@ template <class R> __device__ __forceinline__ bool fx_sensor(const WView<R> &w, 
     return (w.B.f_flags[w.fb + f] & GB_FIX_SENSOR) != 0;
 }
 
-// Append one contact event of the world (index < 0: keyed by its slot,
-// which is the order of occurrence when one thread records).
-template <class R> __device__ __noinline__ void record_event(const WView<R> &w, const EvCtx &ev, int type, int i, int index, int npts,
-                                                             const R *ni, const R *ti) {
+// Append one contact event of a world (index < 0: keyed by its slot, which
+// is the order of occurrence when one thread records).  Out of line and
+// with scalar arguments, so the kernels that may record keep their
+// registers and stack for the common case of no recording.
+static __device__ __noinline__ void put_event(gb_event *ev, int *ev_n, int cap, uint32_t *status, int step, int phase, int type,
+                                              int fa, int fb, int index, int npts, double n0, double n1, double t0, double t1) {
+    int slot = atomicAdd(ev_n, 1);
+    if (slot >= cap) { atomicOr(status, GB_ST_EVENT_OVERFLOW); return; }
+    gb_event &e = ev[slot];
+    e.type = type; e.fixture_a = fa; e.fixture_b = fb; e.point_count = npts;
+    e.key = ((long long)step << 48) | ((long long)phase << 40) | (long long)(index >= 0 ? index : slot);
+    e.normal_impulse[0] = npts > 0 ? n0 : 0.0; e.normal_impulse[1] = npts > 1 ? n1 : 0.0;
+    e.tangent_impulse[0] = npts > 0 ? t0 : 0.0; e.tangent_impulse[1] = npts > 1 ? t1 : 0.0;
+}
+template <class R> __device__ __forceinline__ void record_event(const WView<R> &w, const EvCtx &ev, int type, int i, int index,
+                                                                int npts, const R *ni, const R *ti) {
     const ContactRec<R> &c = w.con(i);
-    int slot = atomicAdd(&w.B.ev_n[w.wi], 1);
-    if (slot >= 3 * w.H->ccap + 64) { atomicOr(&w.H->status, GB_ST_EVENT_OVERFLOW); return; }
-    gb_event &e = w.B.ev[3 * (size_t)w.cb + 64 * (size_t)w.wi + slot];
-    e.type = type; e.fixture_a = c.fa; e.fixture_b = c.fb; e.point_count = npts;
-    e.key = ((long long)ev.step << 48) | ((long long)ev.phase << 40) | (long long)(index >= 0 ? index : slot);
-    for (int j = 0; j < 2; ++j) {
-        e.normal_impulse[j] = j < npts ? (double)ni[j] : 0.0;
-        e.tangent_impulse[j] = j < npts ? (double)ti[j] : 0.0;
-    }
+    put_event(w.B.ev + 3 * (size_t)w.cb + 64 * (size_t)w.wi, w.B.ev_n + w.wi, 3 * w.H->ccap + 64, &w.H->status, ev.step, ev.phase,
+              type, c.fa, c.fb, index, npts, npts > 0 ? (double)ni[0] : 0.0, npts > 1 ? (double)ni[1] : 0.0,
+              npts > 0 ? (double)ti[0] : 0.0, npts > 1 ? (double)ti[1] : 0.0);
 }
 
 // contact.py:210-268 Contact.update; returns whether touching changed (the
