@@ -963,9 +963,14 @@ template <class R, class G> __device__ void constraints_group(const G &g, const 
     g.sync();
     // 3. graph colouring: Jones-Plassmann rounds with fixed hash priorities;
     //    a constraint is coloured when it holds the highest key on each of its
-    //    non-static bodies.  Colour classes share no non-static body, so each
-    //    class is solved in parallel exactly as a sequential pass would.
-    int ncol = 0;
+    //    non-static bodies, with the lowest colour free on both (per-body
+    //    masks of the colours taken so far; beyond 64 colours, a colour of its
+    //    own round).  Colour classes share no non-static body, so each class
+    //    is solved in parallel exactly as a sequential pass would.
+    unsigned long long *used = w.B.s_minsep + w.bb;   // free until the position iterations
+    for (int b = g.rank(); b < nb; b += g.size()) used[b] = 0ull;
+    if (g.rank() == 0) w.H->last_ncolours = 0;
+    int maxc = -1;
     for (int round = 0; round <= ncons; ++round) {   // >= 1 constraint is coloured per round
         for (int b = g.rank(); b < nb; b += g.size()) claim[b] = 0ull;
         g.sync();
@@ -988,12 +993,47 @@ template <class R, class G> __device__ void constraints_group(const G &g, const 
             h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
             unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
             bool win = (q.x < 0 || claim[q.x] == key) && (q.y < 0 || claim[q.y] == key);
-            if (win) colour[k] = round;
+            if (!win) continue;
+            // this round's winners share no body: their mask reads and writes do not race
+            unsigned long long taken = (q.x >= 0 ? used[q.x] : 0ull) | (q.y >= 0 ? used[q.y] : 0ull);
+            int c = __ffsll((long long)~taken) - 1;
+            if (c < 0) c = 64 + round;
+            else {
+                if (q.x >= 0) used[q.x] |= 1ull << c;
+                if (q.y >= 0) used[q.y] |= 1ull << c;
+            }
+            colour[k] = c;
+            maxc = c > maxc ? c : maxc;
         }
-        ncol = round + 1;
         g.sync();
     }
+    // number the colours in use densely (masks leave no gaps below 64; the
+    // round colours above it may)
+    for (int k = g.rank(); k < ncons; k += g.size()) atomicMax(&w.H->last_ncolours, colour[k] + 1);
     g.sync();
+    int ncol = w.H->last_ncolours;
+    (void)maxc;
+    if (ncol > 64) {
+        if (ncol + 1 > w.H->ccap) {   // never index past the world's slots
+            if (g.rank() == 0) w.H->status |= GB_ST_ITER_LIMIT;
+            ncol = w.H->ccap - 1;
+        }
+        for (int cc = g.rank(); cc < ncol; cc += g.size()) pref[cc] = 0;
+        g.sync();
+        for (int k = g.rank(); k < ncons; k += g.size())
+            if (colour[k] >= 0 && colour[k] < ncol) pref[colour[k]] = 1;
+        g.sync();
+        if (g.rank() == 0) {
+            int d = 0;
+            for (int cc = 0; cc < ncol; ++cc) { int u = pref[cc]; pref[cc] = d; d += u; }
+            w.H->last_ncolours = d;
+        }
+        g.sync();
+        for (int k = g.rank(); k < ncons; k += g.size())
+            if (colour[k] >= 0 && colour[k] < ncol) colour[k] = pref[colour[k]];
+        g.sync();
+        ncol = w.H->last_ncolours;
+    }
     // The constraints are stored colour-major: constraint slots [coff[c],
     // coff[c+1]) hold colour c.  Positions inside a colour come from atomics:
     // a colour's constraints share no non-static body, so their order there
