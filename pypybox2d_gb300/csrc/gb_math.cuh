@@ -99,25 +99,49 @@ static GB_HD rot2<double> rot_of(double a) {
     return q;
 }
 
-// float32 rotation of a float64 angle: the same reduction in float64, then
-// a float32 Taylor polynomial (sin to x^11, cos to x^12; truncation below
-// 1e-10 on [-pi/4, pi/4]).
-static GB_HD rot2<float> rot_of_f32(double a) {
-    const double TWO_OVER_PI = 0.6366197723675814;
-    const double P1 = 1.5707963267341256;
-    const double P2 = 6.077100506303966e-11;
-    double k = rint(a * TWO_OVER_PI);
-    float r = (float)((a - k * P1) - k * P2);
+// float32 Taylor polynomials of sin and cos on [-pi/4, pi/4] (sin to x^11,
+// cos to x^12; truncation below 1e-10) and the quadrant swap.
+static GB_HD rot2<float> rot_poly_f32(float r, int quad) {
     float r2 = r * r;
     float sn = r + (r * r2) * (-1.0f / 6.0f + r2 * (1.0f / 120.0f + r2 * (-1.0f / 5040.0f + r2 * (2.7557319e-06f + r2 * -2.5052108e-08f))));
     float cs = 1.0f + r2 * (-0.5f + r2 * (1.0f / 24.0f + r2 * (-1.0f / 720.0f + r2 * (2.4801587e-05f + r2 * (-2.7557319e-07f + r2 * 2.0876757e-09f)))));
-    int quad = (int)(((long long)k) & 3);
     rot2<float> q;
     if (quad == 0) { q.c = cs; q.s = sn; }
     else if (quad == 1) { q.c = -sn; q.s = cs; }
     else if (quad == 2) { q.c = -cs; q.s = -sn; }
     else { q.c = sn; q.s = -cs; }
     return q;
+}
+
+// float32 rotation of a float64 angle: the same reduction in float64, then
+// the float32 polynomials.
+static GB_HD rot2<float> rot_of_f32(double a) {
+    const double TWO_OVER_PI = 0.6366197723675814;
+    const double P1 = 1.5707963267341256;
+    const double P2 = 6.077100506303966e-11;
+    double k = rint(a * TWO_OVER_PI);
+    float r = (float)((a - k * P1) - k * P2);
+    return rot_poly_f32(r, (int)(((long long)k) & 3));
+}
+
+// float32 rotation of a float32 angle of a few pi at most: reduction by
+// pi/2 in float32 (pi/2 = P1 + P2, P1 the float nearest pi/2, so k * P1 is
+// exact for |k| <= 2), then the float32 polynomials.  No float64 arithmetic.
+static GB_HD rot2<float> rot_f32(float x) {
+    const float k = rintf(x * 0.63661977f);
+    float r = fmaf(-k, 1.57079637f, x);
+    r = fmaf(-k, -4.37113900e-08f, r);
+    return rot_poly_f32(r, ((int)k) & 3);
+}
+
+// A float64 angle reduced to [-pi, pi] and rounded to float32 (the
+// step-start angle of the float32 position passes).
+static GB_HD float angle_f32(double a) {
+    const double INV_TWO_PI = 0.15915494309189535;
+    const double Q1 = 6.283185307179586;      // float64 nearest 2 pi
+    const double Q2 = 2.4492935982947064e-16;  // 2 pi - Q1
+    double k = rint(a * INV_TWO_PI);
+    return (float)((a - k * Q1) - k * Q2);
 }
 
 template <class R> struct Rot;

@@ -12,6 +12,7 @@
 //                      dynamictree.py:152-188
 //   continuous ....... world.py:594-821, island.py:181-243, contact.py:866-933
 #pragma once
+#include <type_traits>
 #include "gb_world.cuh"
 #include "gb_tma.cuh"
 
@@ -812,6 +813,59 @@ template <class R> __device__ double solve_position(const Cons<R> &k, vec2<doubl
     return minsep;
 }
 
+// The float32 form of solve_position for the batched solver: each body is
+// its step-start position rounded to float32 (cf) and its step-start angle
+// reduced to [-pi, pi] (ar), plus the corrections of this step's position
+// passes (dc, da), so the passes run without float64 arithmetic; the caller
+// adds the corrections to the float64 pose once, after the passes.
+static __device__ float solve_position_f32d(const Cons<float> &k, vec2<float> cfa, float ara, vec2<float> &dca, float &daa,
+                                            vec2<float> cfb, float arb, vec2<float> &dcb, float &dab, float minsep) {
+    const float ma = k.ma, mb = k.mb, iA = k.iA, iB = k.iB;
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (j >= k.mcount) break;
+        const vec2<float> ca = cfa + dca, cb = cfb + dcb;
+        xform2<float> xa, xb;
+        xa.q = rot_f32(ara + daa);
+        xa.p = ca - rmul(xa.q, k.lca);
+        xb.q = rot_f32(arb + dab);
+        xb.p = cb - rmul(xb.q, k.lcb);
+        vec2<float> normal, point;
+        float sep;
+        if (k.mtype == GB_M_CIRCLES) {
+            vec2<float> pA = xmul(xa, k.lp), pB = xmul(xb, k.lpts[0]);
+            normal = normalized(pB - pA);
+            point = 0.5f * (pA + pB);
+            sep = dot(pB - pA, normal) - k.ra - k.rb;
+        } else if (k.mtype == GB_M_FACE_A) {
+            normal = rmul(xa.q, k.ln);
+            vec2<float> plane = xmul(xa, k.lp);
+            vec2<float> clip = xmul(xb, k.lpts[j]);
+            sep = dot(clip - plane, normal) - k.ra - k.rb;
+            point = clip;
+        } else {
+            normal = rmul(xb.q, k.ln);
+            vec2<float> plane = xmul(xb, k.lp);
+            vec2<float> clip = xmul(xa, k.lpts[j]);
+            sep = dot(clip - plane, normal) - k.ra - k.rb;
+            point = clip;
+            normal = -normal;
+        }
+        vec2<float> ra = point - ca, rb = point - cb;
+        minsep = pymin(minsep, sep);
+        float C = cclamp((float)GB_BAUMGARTE * (sep + (float)GB_LINEAR_SLOP), (float)-GB_MAX_LINEAR_CORRECTION, 0.0f);
+        float rna = sq(cross(ra, normal)), rnb = sq(cross(rb, normal));
+        float K = ma + mb + (iA * rna) + (iB * rnb);
+        float impulse = K > 0.0f ? -C / K : 0.0f;
+        vec2<float> P = impulse * normal;
+        dca = dca - ma * P;
+        daa = daa - iA * cross(ra, P);
+        dcb = dcb + mb * P;
+        dab = dab + iB * cross(rb, P);
+    }
+    return minsep;
+}
+
 // ------------------------------------------------------------ islands + solve
 template <class R> __device__ __forceinline__ bool qualifies(const WView<R> &w, const ContactRec<R> &c) {
     return (c.flags & GB_C_ENABLED) && (c.flags & GB_C_TOUCHING) && !fx_sensor(w, c.fa) && !fx_sensor(w, c.fb);
@@ -1407,14 +1461,44 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     g.sync();
     if (rank == 0) ck.mark(5);
     // 9. position iterations with the per-island early exit (island.py:141-153)
+    // float32 batches with the body cache run the passes on float32 deltas
+    // (solve_position_f32d): cf | dc | ar | da in the cache's 24 bytes a body
+    constexpr bool F32D = std::is_same<R, float>::value;
+    vec2<float> *cf = nullptr, *dcv = nullptr;
+    float *ar = nullptr, *dav = nullptr;
     if (cached) {
-        for (int b = rank; b < nb; b += g.size()) { pc[b] = w.B.b_c[w.bb + b]; pa[b] = w.B.b_a[w.bb + b]; }
+        if constexpr (F32D) {
+            unsigned char *m = cache.mem;
+            cf = reinterpret_cast<vec2<float> *>(m);
+            dcv = reinterpret_cast<vec2<float> *>(m + 8 * (size_t)nb);
+            ar = reinterpret_cast<float *>(m + 16 * (size_t)nb);
+            dav = reinterpret_cast<float *>(m + 20 * (size_t)nb);
+            for (int b = rank; b < nb; b += g.size()) {
+                cf[b] = cvt<float>(w.B.b_c[w.bb + b]);
+                ar[b] = angle_f32(w.B.b_a[w.bb + b]);
+                dcv[b] = mk<float>(0.0f, 0.0f);
+                dav[b] = 0.0f;
+            }
+        } else {
+            for (int b = rank; b < nb; b += g.size()) { pc[b] = w.B.b_c[w.bb + b]; pa[b] = w.B.b_a[w.bb + b]; }
+        }
         g.sync();
     }
     auto pos_one = [&](const ConsPos<R> &rec) {
         if (rootf[rec.root] & R_DONE) return;
         const int ia = rec.ia, ib = rec.ib;
         Cons<R> k = pos_cons(rec, invm[ia], invm[ib], invi[ia], invi[ib]);
+        if constexpr (F32D) {
+            if (cached) {
+                vec2<float> dca = dcv[ia], dcb = dcv[ib];
+                float daa = dav[ia], dab = dav[ib];
+                const float ms = solve_position_f32d(k, cf[ia], ar[ia], dca, daa, cf[ib], ar[ib], dcb, dab, 0.0f);
+                atomicMin(&minsep[rec.root], dkey((double)ms));
+                if (!is_static(ia)) { dcv[ia] = dca; dav[ia] = daa; }
+                if (!is_static(ib)) { dcv[ib] = dcb; dav[ib] = dab; }
+                return;
+            }
+        }
         vec2<double> ca = pc[ia], cb = pc[ib];
         double aa = pa[ia], ab = pa[ib];
         double ms = solve_position(k, ca, aa, cb, ab, 0.0, false, false, false);
@@ -1488,7 +1572,20 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     }
     g.sync();
     if (cached) {
-        for (int b = rank; b < nb; b += g.size()) { w.B.b_c[w.bb + b] = pc[b]; w.B.b_a[w.bb + b] = pa[b]; }
+        if constexpr (F32D) {
+            for (int b = rank; b < nb; b += g.size()) {
+                const vec2<float> d = dcv[b];
+                const float e = dav[b];
+                if (d.x == 0.0f && d.y == 0.0f && e == 0.0f) continue;
+                vec2<double> c = w.B.b_c[w.bb + b];
+                if (d.x != 0.0f) c.x = c.x + (double)d.x;
+                if (d.y != 0.0f) c.y = c.y + (double)d.y;
+                w.B.b_c[w.bb + b] = c;
+                if (e != 0.0f) w.B.b_a[w.bb + b] = w.B.b_a[w.bb + b] + (double)e;
+            }
+        } else {
+            for (int b = rank; b < nb; b += g.size()) { w.B.b_c[w.bb + b] = pc[b]; w.B.b_a[w.bb + b] = pa[b]; }
+        }
         g.sync();
     }
     if (rank == 0) ck.mark(6);
