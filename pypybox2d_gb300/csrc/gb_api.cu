@@ -309,8 +309,13 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
             CK(cudaMalloc((void **)&d_s, sizeof(int) * slots.size()));
             CK(cudaMemcpy(d_c, hc.data(), sizeof(gb_contact) * hc.size(), cudaMemcpyHostToDevice));
             CK(cudaMemcpy(d_s, slots.data(), sizeof(int) * slots.size(), cudaMemcpyHostToDevice));
-            if (precision == GB_PREC_F64) gb_launch_unpack_contacts<double>(b->bd, d_c, d_s, (int)hc.size(), 0);
-            else gb_launch_unpack_contacts<float>(b->bf, d_c, d_s, (int)hc.size(), 0);
+            if (precision == GB_PREC_F64) {
+                gb_launch_unpack_contacts<double>(b->bd, d_c, d_s, (int)hc.size(), 0);
+                gb_launch_refresh_toi_cand<double>(b->bd, 0);
+            } else {
+                gb_launch_unpack_contacts<float>(b->bf, d_c, d_s, (int)hc.size(), 0);
+                gb_launch_refresh_toi_cand<float>(b->bf, 0);
+            }
             CK(cudaDeviceSynchronize());
             cudaFree(d_c);
             cudaFree(d_s);
@@ -386,8 +391,14 @@ int gb_batch_set_bodies(gb_batch *b, const gb_body *bodies, int32_t n, void *str
     if (n != b->nb) return fail(GB_E_ARG, "body count mismatch");
     cudaStream_t st = (cudaStream_t)stream;
     CK(cudaMemcpyAsync(b->d_bstage, bodies, sizeof(gb_body) * n, cudaMemcpyHostToDevice, st));
-    if (b->prec == GB_PREC_F64) gb_launch_unpack_bodies<double>(b->bd, b->d_bstage, n, st);
-    else gb_launch_unpack_bodies<float>(b->bf, b->d_bstage, n, st);
+    // body types and bullet flags decide which contacts can take part in the TOI loop
+    if (b->prec == GB_PREC_F64) {
+        gb_launch_unpack_bodies<double>(b->bd, b->d_bstage, n, st);
+        gb_launch_refresh_toi_cand<double>(b->bd, st);
+    } else {
+        gb_launch_unpack_bodies<float>(b->bf, b->d_bstage, n, st);
+        gb_launch_refresh_toi_cand<float>(b->bf, st);
+    }
     CK(cudaGetLastError());
     return 0;
 }

@@ -592,7 +592,7 @@ struct Sweep { vec2<double> lc, c0, c; double a0, a, alpha0; };
 static __device__ __forceinline__ xform2<double> sweep_xf(const Sweep &sw, double beta) {
     xform2<double> x;
     x.p = (1.0 - beta) * sw.c0 + beta * sw.c;
-    x.q = rot_of((1.0 - beta) * sw.a0 + beta * sw.a);
+    x.q = pose_rot((1.0 - beta) * sw.a0 + beta * sw.a);
     x.p = x.p - rmul(x.q, sw.lc);
     return x;
 }

@@ -64,7 +64,7 @@ __global__ void k_unpack_contacts(Batch<GB_REAL> B, const gb_contact *src, const
     if (i >= n) return;
     const gb_contact &g = src[i];
     ContactRec<GB_REAL> c;
-    c.fa = g.fixture_a; c.fb = g.fixture_b; c.flags = g.flags; c.toi_count = g.toi_count; c.toi = g.toi;
+    c.fa = g.fixture_a; c.fb = g.fixture_b; c.flags = g.flags & ~GB_C_TOI_CAND; c.toi_count = g.toi_count; c.toi = g.toi;
     c.friction = (GB_REAL)g.friction; c.restitution = (GB_REAL)g.restitution;
     c.m.type = g.m_type; c.m.count = g.m_point_count;
     c.m.ln = mk<GB_REAL>((GB_REAL)g.m_lnx, (GB_REAL)g.m_lny); c.m.lp = mk<GB_REAL>((GB_REAL)g.m_lpx, (GB_REAL)g.m_lpy);
@@ -81,7 +81,7 @@ __global__ void k_pack_contacts(Batch<GB_REAL> B, gb_contact *dst, int base, int
     const ContactRec<GB_REAL> &c = B.c[base + i];
     gb_contact g;
     g.fixture_a = c.fa; g.fixture_b = c.fb; g.child_a = 0; g.child_b = 0;
-    g.flags = c.flags; g.toi_count = c.toi_count; g.toi = c.toi;
+    g.flags = c.flags & ~GB_C_TOI_CAND; g.toi_count = c.toi_count; g.toi = c.toi;
     g.friction = (double)c.friction; g.restitution = (double)c.restitution;
     g.m_type = c.m.type; g.m_point_count = c.m.count;
     g.m_lnx = (double)c.m.ln.x; g.m_lny = (double)c.m.ln.y; g.m_lpx = (double)c.m.lp.x; g.m_lpy = (double)c.m.lp.y;
@@ -90,6 +90,16 @@ __global__ void k_pack_contacts(Batch<GB_REAL> B, gb_contact *dst, int base, int
         g.p_ni[k] = (double)c.m.ni[k]; g.p_ti[k] = (double)c.m.ti[k]; g.p_id[k] = c.m.id[k];
     }
     dst[i] = g;
+}
+
+__global__ void k_refresh_toi_cand(Batch<GB_REAL> B, int n_slots) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_slots) return;
+    WView<GB_REAL> w = view_global(B, B.c_world[s]);
+    int i = s - w.cb;
+    if (i >= w.H->nc) return;
+    ContactRec<GB_REAL> &c = w.con(i);
+    c.flags = (c.flags & ~GB_C_TOI_CAND) | (toi_candidate(w, i) ? GB_C_TOI_CAND : 0u);
 }
 
 }  // namespace
@@ -234,4 +244,8 @@ template <> void gb_launch_unpack_contacts<GB_REAL>(const Batch<GB_REAL> &B, con
 }
 template <> void gb_launch_pack_contacts<GB_REAL>(const Batch<GB_REAL> &B, gb_contact *d, int base, int n, cudaStream_t st) {
     if (n > 0) k_pack_contacts<<<(n + 255) / 256, 256, 0, st>>>(B, d, base, n);
+}
+template <> void gb_launch_refresh_toi_cand<GB_REAL>(const Batch<GB_REAL> &B, cudaStream_t st) {
+    const int n = B.n_slots;
+    if (n > 0) k_refresh_toi_cand<<<(n + 255) / 256, 256, 0, st>>>(B, n);
 }

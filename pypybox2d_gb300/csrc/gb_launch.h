@@ -18,6 +18,8 @@ template <class R> void gb_launch_pack_bodies(const Batch<R> &B, gb_body *d, int
 template <class R> void gb_launch_unpack_fixtures(const Batch<R> &B, const gb_fixture *d, int n, cudaStream_t st);
 template <class R> void gb_launch_unpack_contacts(const Batch<R> &B, const gb_contact *d, const int *slots, int n, cudaStream_t st);
 template <class R> void gb_launch_pack_contacts(const Batch<R> &B, gb_contact *d, int base, int n, cudaStream_t st);
+// recompute the device-only TOI candidate flag of every contact (after an upload)
+template <class R> void gb_launch_refresh_toi_cand(const Batch<R> &B, cudaStream_t st);
 
 template <> int gb_launch_step<double>(const Batch<double> &, const StepParams &, int, const int *, int, int, int, cudaStream_t,
                                        KernelTimer *);
@@ -33,3 +35,5 @@ template <> void gb_launch_unpack_contacts<double>(const Batch<double> &, const 
 template <> void gb_launch_unpack_contacts<float>(const Batch<float> &, const gb_contact *, const int *, int, cudaStream_t);
 template <> void gb_launch_pack_contacts<double>(const Batch<double> &, gb_contact *, int, int, cudaStream_t);
 template <> void gb_launch_pack_contacts<float>(const Batch<float> &, gb_contact *, int, int, cudaStream_t);
+template <> void gb_launch_refresh_toi_cand<double>(const Batch<double> &, cudaStream_t);
+template <> void gb_launch_refresh_toi_cand<float>(const Batch<float> &, cudaStream_t);

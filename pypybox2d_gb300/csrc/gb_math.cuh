@@ -144,6 +144,22 @@ static GB_HD float angle_f32(double a) {
     return (float)((a - k * Q1) - k * Q2);
 }
 
+// Rotation of the float64 poses (body transforms, sweeps, fat boxes).  The
+// float64 unit takes the portable sincos above (bit-exact with the CPU
+// restatement); the float32 unit (GB_POSE_ROT_F32) the float32 rotation,
+// widened: its narrow phase and solver read float32 rotations anyway, and
+// GB300 issues float64 arithmetic at a small fraction of the float32 rate.
+static GB_HD rot2<double> pose_rot(double a) {
+#if defined(GB_POSE_ROT_F32)
+    const rot2<float> q = rot_of_f32(a);
+    rot2<double> r;
+    r.c = (double)q.c; r.s = (double)q.s;
+    return r;
+#else
+    return rot_of(a);
+#endif
+}
+
 template <class R> struct Rot;
 template <> struct Rot<double> { GB_HD static rot2<double> of(double a) { return rot_of(a); } };
 template <> struct Rot<float> { GB_HD static rot2<float> of(double a) { return rot_of_f32(a); } };

@@ -97,6 +97,17 @@ template <class R> __global__ void k_toi1(Batch<R> B, int n_slots, StepParams sp
     if (i >= w.H->nc) return;
     if (!((w.H->flags & GB_W_CONTINUOUS) && sp.dt > 0.0)) return;
     if (!(w.H->flags & GB_W_STEP_COMPLETE)) return;   // k_toi2 then runs the whole loop in order
+    ContactRec<R> &c = w.con(i);
+    const uint32_t f = c.flags;
+    if (!(f & GB_C_TOI_CAND)) {
+        // a contact that cannot take part: the same reset, stored only
+        // where it changes (most such contacts are already reset)
+        if (f & (GB_C_TOI | GB_C_ISLAND)) c.flags = f & ~(GB_C_TOI | GB_C_ISLAND);
+        if (c.toi_count != 0) c.toi_count = 0;
+        if (__double_as_longlong(c.toi) != __double_as_longlong(1.0)) c.toi = 1.0;
+        B.s_proc[s] = 0;
+        return;
+    }
     toi_reset_contact(w, i);
     int st = toi_status(w, i);
     B.s_proc[s] = st != 0 ? 1 : 0;

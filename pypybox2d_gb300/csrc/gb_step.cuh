@@ -73,7 +73,7 @@ template <class R> __device__ __forceinline__ void sleep_body(const WView<R> &w,
 // body.py:887-889
 template <class R> __device__ __forceinline__ void sync_transform(const WView<R> &w, int b) {
     int g = w.bb + b;
-    rot2<double> q = rot_of(w.B.b_a[g]);
+    rot2<double> q = pose_rot(w.B.b_a[g]);
     vec2<double> p = w.B.b_c[g] - rmul(q, w.B.b_lc[g]);
     w.B.b_xp[g] = p; w.B.b_xq[g] = q;
 }
@@ -83,7 +83,7 @@ template <class R> __device__ void body_advance(const WView<R> &w, int b, double
     sweep_advance(s, alpha);
     s.c = s.c0; s.a = s.a0;
     w.put_sweep(b, s);
-    rot2<double> q = rot_of(s.a);
+    rot2<double> q = pose_rot(s.a);
     w.B.b_xq[w.bb + b] = q;
     w.B.b_xp[w.bb + b] = s.c - rmul(q, s.lc);
 }
@@ -167,6 +167,42 @@ template <class R, bool EV = true> __device__ bool contact_update(const WView<R>
     return changed;
 }
 
+// Contacts that can take part in the TOI loop of this step: neither fixture
+// a sensor, a bullet or non-dynamic body on one side, not both bodies
+// static (toi_status's conditions that cannot change during the loop; the
+// awake, enabled and sub-step conditions are checked on every pass).
+template <class R> __device__ __forceinline__ bool toi_candidate(const WView<R> &w, int i) {
+    const ContactRec<R> &c = w.con(i);
+    if (fx_sensor(w, c.fa) || fx_sensor(w, c.fb)) return false;
+    int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
+    int ta = w.btype(ba), tb = w.btype(bb);
+    if (ta == GB_BODY_STATIC && tb == GB_BODY_STATIC) return false;
+    bool col_a = (w.B.b_flags[w.bb + ba] & GB_BODY_BULLET) || ta != GB_BODY_DYNAMIC;
+    bool col_b = (w.B.b_flags[w.bb + bb] & GB_BODY_BULLET) || tb != GB_BODY_DYNAMIC;
+    return col_a || col_b;
+}
+
+// shapes.py compute_aabb (child 0) for the float32 unit: the rotated
+// vertices' extent in float32 about the body origin p, widened and added to
+// p; equal to shape_aabb to float32 rounding of the extent (~1e-7 m).
+template <class R> __device__ dbox shape_aabb_f32(const WView<R> &w, int f, vec2<double> p, rot2<float> q) {
+    const Shape<R> s = w.shape(f);
+    const float r = (float)s.radius;
+    vec2<float> lo, hi;
+    if (s.type == GB_SHAPE_CIRCLE) {
+        lo = hi = rmul(q, cvt<float>(s.v[0]));
+    } else {
+        const int n = (s.type == GB_SHAPE_POLYGON) ? s.count : 2;
+        lo = hi = rmul(q, cvt<float>(s.v[0]));
+        for (int i = 1; i < n; ++i) {
+            const vec2<float> v = rmul(q, cvt<float>(s.v[i]));
+            lo = mk<float>(fminf(lo.x, v.x), fminf(lo.y, v.y));
+            hi = mk<float>(fmaxf(hi.x, v.x), fmaxf(hi.y, v.y));
+        }
+    }
+    return mkbox(p.x + (double)(lo.x - r), p.y + (double)(lo.y - r), p.x + (double)(hi.x + r), p.y + (double)(hi.y + r));
+}
+
 // shapes.py compute_aabb (child 0), float64
 template <class R> __device__ dbox shape_aabb(const WView<R> &w, int f, xform2<double> x) {
     Shape<R> s = w.shape(f);
@@ -190,13 +226,26 @@ template <class R> __device__ dbox shape_aabb(const WView<R> &w, int f, xform2<d
 template <class R> __device__ bool sync_fixture(const WView<R> &w, int f) {
     int b = w.fbody(f);
     int gbi = w.bb + b;
+#if defined(GB_POSE_ROT_F32)
+    // float32 unit: the shape's extent about the body origin in float32,
+    // added to the float64 origin (shape_aabb_f32)
+    const rot2<float> q1 = rot_of_f32(w.B.b_a0[gbi]);
+    const vec2<double> p1 = w.B.b_c0[gbi] - cvt<double>(rmul(q1, cvt<float>(w.B.b_lc[gbi])));
+    const vec2<double> p2 = w.B.b_xp[gbi];
+    const rot2<double> q2d = w.B.b_xq[gbi];
+    rot2<float> q2;
+    q2.c = (float)q2d.c; q2.s = (float)q2d.s;
+    dbox a1 = shape_aabb_f32(w, f, p1, q1), a2 = shape_aabb_f32(w, f, p2, q2);
+    vec2<double> disp = p2 - p1;
+#else
     xform2<double> x1;
     x1.q = rot_of(w.B.b_a0[gbi]);
     x1.p = w.B.b_c0[gbi] - rmul(x1.q, w.B.b_lc[gbi]);
     xform2<double> x2 = w.xfd(b);
     dbox a1 = shape_aabb(w, f, x1), a2 = shape_aabb(w, f, x2);
-    dbox ab = mkbox(cmin(a1.x, a2.x), cmin(a1.y, a2.y), cmax(a1.z, a2.z), cmax(a1.w, a2.w));
     vec2<double> disp = x2.p - x1.p;
+#endif
+    dbox ab = mkbox(cmin(a1.x, a2.x), cmin(a1.y, a2.y), cmax(a1.z, a2.z), cmax(a1.w, a2.w));
     dbox fat = w.B.f_aabb[w.fb + f];
     if (fat.x <= ab.x && fat.y <= ab.y && ab.z <= fat.z && ab.w <= fat.w) return false;
     dbox nb = mkbox(ab.x - GB_AABB_EXTENSION, ab.y - GB_AABB_EXTENSION, ab.z + GB_AABB_EXTENSION, ab.w + GB_AABB_EXTENSION);
@@ -477,7 +526,8 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
         if (!prim) { fa = q; fb = p; }
         ContactRec<R> &c = w.con(nc + t);
         c.fa = fa; c.fb = fb;
-        c.flags = 0; c.toi_count = 0; c.toi = 0.0;
+        c.flags = toi_candidate(w, nc + t) ? GB_C_TOI_CAND : 0u;
+        c.toi_count = 0; c.toi = 0.0;
         R fra = w.B.f_friction[w.fb + fa], frb = w.B.f_friction[w.fb + fb];
         c.friction = sqrt(fra * frb);
         c.restitution = pymax(w.B.f_restitution[w.fb + fa], w.B.f_restitution[w.fb + fb]);

@@ -247,21 +247,6 @@ template <class R> __device__ __forceinline__ void toi_first_pass_contact(const 
     proc[i] = toi_of_contact(w, i) ? 1 : 0;
 }
 
-// Contacts that can take part in the TOI loop of this step: neither fixture
-// a sensor, a bullet or non-dynamic body on one side, not both bodies
-// static (toi_status's conditions that cannot change during the loop; the
-// awake, enabled and sub-step conditions are checked on every pass).
-template <class R> __device__ __forceinline__ bool toi_candidate(const WView<R> &w, int i) {
-    const ContactRec<R> &c = w.con(i);
-    if (fx_sensor(w, c.fa) || fx_sensor(w, c.fb)) return false;
-    int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
-    int ta = w.btype(ba), tb = w.btype(bb);
-    if (ta == GB_BODY_STATIC && tb == GB_BODY_STATIC) return false;
-    bool col_a = (w.B.b_flags[w.bb + ba] & GB_BODY_BULLET) || ta != GB_BODY_DYNAMIC;
-    bool col_b = (w.B.b_flags[w.bb + bb] & GB_BODY_BULLET) || tb != GB_BODY_DYNAMIC;
-    return col_a || col_b;
-}
-
 // The contacts of dynamic body b in list order (Body._contacts): its
 // adjacency entries from the start of the loop, then the contacts created
 // since (indices >= nc0).  Calls fn(contact) in that order.
@@ -399,7 +384,8 @@ template <class R, class G> __device__ void toi_find_pairs(const G &g, const WVi
         if (!prim) { fa = q; fb = p; }
         ContactRec<R> &c = w.con(nc + t);
         c.fa = fa; c.fb = fb;
-        c.flags = 0; c.toi_count = 0; c.toi = 0.0;
+        c.flags = toi_candidate(w, nc + t) ? GB_C_TOI_CAND : 0u;
+        c.toi_count = 0; c.toi = 0.0;
         R fra = w.B.f_friction[w.fb + fa], frb = w.B.f_friction[w.fb + fb];
         c.friction = sqrt(fra * frb);
         c.restitution = pymax(w.B.f_restitution[w.fb + fa], w.B.f_restitution[w.fb + fb]);
@@ -470,10 +456,10 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
     unsigned long long *lhash = w.B.s_hash + 4 * (size_t)w.cb;
     build_loop_hash(g, w, sh, lhash, nc0, nc0);
     // candidates in list order
-    int ncand = group_scan(g, nc0, [&](int i) { return toi_candidate(w, i) ? 1 : 0; }, ids);
+    int ncand = group_scan(g, nc0, [&](int i) { return (w.con(i).flags & GB_C_TOI_CAND) ? 1 : 0; }, ids);
     g.sync();
     for (int i = g.rank(); i < nc0; i += g.size())
-        if (toi_candidate(w, i)) cand[ids[i]] = i;
+        if (w.con(i).flags & GB_C_TOI_CAND) cand[ids[i]] = i;
     g.sync();
     for (int pass = 0; pass < (1 << 20); ++pass) {
         const int nc = w.H->nc;
@@ -565,10 +551,10 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
         // new contacts join the candidate list (they follow every older one)
         const int nc2 = w.H->nc;
         if (nc2 > nc) {
-            int nnew = group_scan(g, nc2 - nc, [&](int k) { return toi_candidate(w, nc + k) ? 1 : 0; }, ids);
+            int nnew = group_scan(g, nc2 - nc, [&](int k) { return (w.con(nc + k).flags & GB_C_TOI_CAND) ? 1 : 0; }, ids);
             g.sync();
             for (int k = g.rank(); k < nc2 - nc; k += g.size())
-                if (toi_candidate(w, nc + k)) { cand[ncand + ids[k]] = nc + k; proc[nc + k] = 0; }
+                if (w.con(nc + k).flags & GB_C_TOI_CAND) { cand[ncand + ids[k]] = nc + k; proc[nc + k] = 0; }
             ncand += nnew;
             g.sync();
         }

@@ -142,6 +142,9 @@ template <class R> struct Batch {
 #define GB_SOLVE_BIG_THREADS 128
 #define GB_SOLVE_PIPE_BUFS 2       // constraint chunk buffers of the solver
 #define GB_MAX_TOI_CONTACTS 32     // contacts of one TOI sub-island
+// contact flag kept on the device only (cleared in exported records): the
+// contact can take part in the TOI loop (toi_candidate)
+#define GB_C_TOI_CAND 0x80000000u
 #define GB_TOI_PLAN_CAP 64
 // A TOI computation prepared by the order-dependent sweep alignment.
 struct TPlan { double alpha0; Sweep sa, sb; };
