@@ -134,6 +134,8 @@ struct gb_batch {
     KernelTimer *ktimer = nullptr;   // created by the first timed step
     gb_event *d_ev = nullptr;        // contact events, allocated by the first step that records them
     int *d_ev_n = nullptr;
+    SideStream side{};               // the solver's second stream (gb_launch.h)
+    bool has_side = false;
 };
 
 extern "C" {
@@ -323,6 +325,18 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
     }
     CK(cudaDeviceSynchronize());
     cudaFree(d_fst);
+    {
+        // the solver's side stream, at the lowest priority so the wide launch
+        // on the caller's stream keeps first claim on freed SM resources
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (cudaStreamCreateWithPriority(&b->side.s, cudaStreamNonBlocking, least) == cudaSuccess) {
+            if (cudaEventCreateWithFlags(&b->side.fork, cudaEventDisableTiming) == cudaSuccess &&
+                cudaEventCreateWithFlags(&b->side.join, cudaEventDisableTiming) == cudaSuccess)
+                b->has_side = true;
+        }
+        (void)cudaGetLastError();   // without a side stream both solver launches share the caller's
+    }
     *out = b;
     return 0;
 }
@@ -339,6 +353,11 @@ int gb_batch_destroy(gb_batch *b) {
     }
     cudaFree(b->d_ev);
     cudaFree(b->d_ev_n);
+    if (b->has_side) {
+        cudaEventDestroy(b->side.fork);
+        cudaEventDestroy(b->side.join);
+        cudaStreamDestroy(b->side.s);
+    }
     delete b;
     return 0;
 }
@@ -378,8 +397,10 @@ int gb_batch_step(gb_batch *b, const gb_step_opts *o, void *stream) {
         }
         kt = b->ktimer;
     }
-    int rc = b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st, kt)
-                                    : gb_launch_step<float>(b->bf, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st, kt);
+    int rc = b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st, kt,
+                                                             b->has_side ? &b->side : nullptr)
+                                    : gb_launch_step<float>(b->bf, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st, kt,
+                                                            b->has_side ? &b->side : nullptr);
     if (rc) return cuda_fail((cudaError_t)rc, "step launch");
     b->counters[0] += 1;
     b->counters[2] += o->n_steps;
@@ -585,7 +606,7 @@ template <class R> int step_static(gb_batch *b, const Batch<R> &arena_view, cons
     // every scratch array is written before it is read inside a step, except
     // the first-pass TOI list counter
     CK(cudaMemsetAsync(B.toi_n, 0, sizeof(int), st));
-    rc = gb_launch_step<R>(B, sp, n_steps, b->d_worlds, b->nw, mode, threads, st);
+    rc = gb_launch_step<R>(B, sp, n_steps, b->d_worlds, b->nw, mode, threads, st, nullptr, b->has_side ? &b->side : nullptr);
     if (rc) return cuda_fail((cudaError_t)rc, "step launch (static scratch)");
     return 0;
 }

@@ -127,7 +127,8 @@ template <int PH> static cudaError_t launch_grid(const Batch<GB_REAL> &B, const 
 }
 
 template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *d_worlds,
-                                        int n_list, int mode, int threads, cudaStream_t st, KernelTimer *kt) {
+                                        int n_list, int mode, int threads, cudaStream_t st, KernelTimer *kt,
+                                        const SideStream *side) {
     if (n_list <= 0) return 0;
     // the step kernels use ~220 registers per thread: at most 256 threads per CTA
     if (threads > 256) threads = 256;
@@ -151,6 +152,11 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
             return cudaSuccess;
         };
         const int tbig = GB_SOLVE_BIG_THREADS;
+        // per-phase CTA widths: the island and pair phases run more threads
+        // a world than the solver (measured on the uneven 8192-world batch:
+        // islands 2.6 -> 1.3 ms at 4x, pair phases best at 2x)
+        const int t_isl = threads * 4 < 256 ? threads * 4 : 256;
+        const int t_pair = threads * 2 < 256 ? threads * 2 : 256;
         Batch<GB_REAL> Bb = B, Bs = B;
         Bb.cache_bodies = B.cache_big;
         Bs.cache_bodies = B.cache_small;
@@ -182,21 +188,33 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
             }
             mark(3);
             GB_GRID(PH_COLLIDE2);
-            if (n_norm) k_world<GB_REAL, PH_COLLIDE2><<<n_norm, threads, 0, st>>>(B, sp, w_norm);
+            if (n_norm) k_world<GB_REAL, PH_COLLIDE2><<<n_norm, t_pair, 0, st>>>(B, sp, w_norm);
             mark(4);
             GB_GRID(PH_ISLANDS);
-            if (n_norm) k_world<GB_REAL, PH_ISLANDS><<<n_norm, threads, 0, st>>>(B, sp, w_norm);
+            if (n_norm) k_world<GB_REAL, PH_ISLANDS><<<n_norm, t_isl, 0, st>>>(B, sp, w_norm);
             mark(5);
             if (nb) k_vinit<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
             mark(6);
             if (ns) k_cinit<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
             mark(7);
             GB_GRID(PH_SOLVE);
-            if (nbig > nhuge) k_world<GB_REAL, PH_SOLVE><<<nbig - nhuge, tbig, smem_big, st>>>(Bb, sp, w_norm);
-            if (n_list > nbig) k_world<GB_REAL, PH_SOLVE><<<n_list - nbig, threads, smem_small, st>>>(Bs, sp, d_worlds + nbig);
+            if (side && nbig > nhuge && n_list > nbig) {
+                // the larger worlds first on the caller's stream; the smaller
+                // ones beside them on the low-priority side stream, filling
+                // the shared memory the wide launch leaves free on each SM
+                cudaEventRecord(side->fork, st);
+                cudaStreamWaitEvent(side->s, side->fork, 0);
+                k_world<GB_REAL, PH_SOLVE><<<nbig - nhuge, tbig, smem_big, st>>>(Bb, sp, w_norm);
+                k_world<GB_REAL, PH_SOLVE><<<n_list - nbig, threads, smem_small, side->s>>>(Bs, sp, d_worlds + nbig);
+                cudaEventRecord(side->join, side->s);
+                cudaStreamWaitEvent(st, side->join, 0);
+            } else {
+                if (nbig > nhuge) k_world<GB_REAL, PH_SOLVE><<<nbig - nhuge, tbig, smem_big, st>>>(Bb, sp, w_norm);
+                if (n_list > nbig) k_world<GB_REAL, PH_SOLVE><<<n_list - nbig, threads, smem_small, st>>>(Bs, sp, d_worlds + nbig);
+            }
             mark(8);
             GB_GRID(PH_PAIRS);
-            if (n_norm) k_world<GB_REAL, PH_PAIRS><<<n_norm, threads, 0, st>>>(B, sp, w_norm);
+            if (n_norm) k_world<GB_REAL, PH_PAIRS><<<n_norm, t_pair, 0, st>>>(B, sp, w_norm);
             mark(9);
             if (ns) k_toi1<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
             mark(10);

@@ -11,8 +11,16 @@ struct KernelTimer {
     double total_ms[GB_NKTIME];
     long long steps;
 };
+// A second stream of the batch (lowest priority) for the solver launch of
+// the smaller worlds, which then runs beside the launch of the larger ones;
+// fork and join are events on the caller's stream.
+struct SideStream {
+    cudaStream_t s;
+    cudaEvent_t fork, join;
+};
 template <class R> int gb_launch_step(const Batch<R> &B, const StepParams &sp, int n_steps, const int *d_worlds, int n_list,
-                                      int mode, int threads, cudaStream_t st, KernelTimer *kt = nullptr);
+                                      int mode, int threads, cudaStream_t st, KernelTimer *kt = nullptr,
+                                      const SideStream *side = nullptr);
 template <class R> void gb_launch_unpack_bodies(const Batch<R> &B, const gb_body *d, int n, cudaStream_t st);
 template <class R> void gb_launch_pack_bodies(const Batch<R> &B, gb_body *d, int n, cudaStream_t st);
 template <class R> void gb_launch_unpack_fixtures(const Batch<R> &B, const gb_fixture *d, int n, cudaStream_t st);
@@ -22,9 +30,9 @@ template <class R> void gb_launch_pack_contacts(const Batch<R> &B, gb_contact *d
 template <class R> void gb_launch_refresh_toi_cand(const Batch<R> &B, cudaStream_t st);
 
 template <> int gb_launch_step<double>(const Batch<double> &, const StepParams &, int, const int *, int, int, int, cudaStream_t,
-                                       KernelTimer *);
+                                       KernelTimer *, const SideStream *);
 template <> int gb_launch_step<float>(const Batch<float> &, const StepParams &, int, const int *, int, int, int, cudaStream_t,
-                                      KernelTimer *);
+                                      KernelTimer *, const SideStream *);
 template <> void gb_launch_unpack_bodies<double>(const Batch<double> &, const gb_body *, int, cudaStream_t);
 template <> void gb_launch_unpack_bodies<float>(const Batch<float> &, const gb_body *, int, cudaStream_t);
 template <> void gb_launch_pack_bodies<double>(const Batch<double> &, gb_body *, int, cudaStream_t);
