@@ -72,6 +72,7 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_claim = a.take<unsigned long long>(nb); B.s_minsep = a.take<unsigned long long>(nb);
     B.s_minsleep = a.take<unsigned long long>(nb);
     B.s_bvis = a.take<unsigned char>(nb);
+    B.s_pose = a.take<float4>(nb);
     B.s_move = a.take<int>(nf); B.s_first = a.take<int>(nf); B.s_cnt = a.take<int>(nf);
     B.s_grid = a.take<int>(12 * (size_t)nf + 2 * (size_t)nw);
     B.s_proc = a.take<int>(ncap); B.s_pref = a.take<int>(ncap); B.s_adj = a.take<int>(2 * (size_t)ncap);
@@ -101,6 +102,7 @@ template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb
     B.s_claim = a.take<unsigned long long>(nb); B.s_minsep = a.take<unsigned long long>(nb);
     B.s_minsleep = a.take<unsigned long long>(nb);
     B.s_bvis = a.take<unsigned char>(nb);
+    B.s_pose = a.take<float4>(nb);
     B.s_first = a.take<int>(nf); B.s_cnt = a.take<int>(nf);
     B.s_grid = a.take<int>(12 * (size_t)nf + 2 * (size_t)nw);
     B.s_proc = a.take<int>(ncap); B.s_pref = a.take<int>(ncap); B.s_adj = a.take<int>(2 * (size_t)ncap);

@@ -75,6 +75,11 @@ template <class R> __global__ void k_vinit(Batch<R> B, int n_bodies, StepParams 
     WView<R> w = view_global(B, B.b_world[b]);
     if (!(w.H->pflags & P_SOLVING)) return;
     integrate_velocity_body(w, b - w.bb, sp.dt);
+#if defined(GB_POSE_ROT_F32)
+    const rot2<float> q = rot_of_f32(B.b_a[b]);
+    const vec2<double> c = B.b_c[b];
+    B.s_pose[b] = make_float4((float)c.x, (float)c.y, q.c, q.s);
+#endif
 }
 
 template <class R> __global__ void k_cinit(Batch<R> B, int n_slots, StepParams sp) {
@@ -83,7 +88,11 @@ template <class R> __global__ void k_cinit(Batch<R> B, int n_slots, StepParams s
     WView<R> w = view_global(B, B.c_world[s]);
     int k = s - w.cb;
     if (!(w.H->pflags & P_SOLVING) || k >= w.H->last_ncons) return;
+#if defined(GB_POSE_ROT_F32)
+    init_constraint(w, k, sp, true);   // poses from k_vinit (s_pose)
+#else
     init_constraint(w, k, sp);
+#endif
 }
 
 // First TOI pass, part 1: reset every contact's TOI state (world.py:604-609)

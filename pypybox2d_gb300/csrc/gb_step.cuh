@@ -660,9 +660,10 @@ template <class R> __device__ __forceinline__ xform2<R> pose_xf(vec2<double> c, 
 }
 
 // contact.py:414-496 initialize_velocity_constraints + contact_util.py:195-245
-template <class R> __device__ void init_velocity(Cons<R> &k, vec2<double> ca, double aa, vec2<double> cb, double ab,
-                                                 vec2<R> va, R wa, vec2<R> vb, R wb) {
-    xform2<R> xa = pose_xf<R>(ca, aa, k.lca), xb = pose_xf<R>(cb, ab, k.lcb);
+// (the transforms and centres of both bodies given; init_velocity below
+// derives them from the float64 poses)
+template <class R> __device__ void init_velocity_xf(Cons<R> &k, xform2<R> xa, xform2<R> xb, vec2<R> car, vec2<R> cbr,
+                                                    vec2<R> va, R wa, vec2<R> vb, R wb) {
     vec2<R> normal, pts[2];
     if (k.mtype == GB_M_CIRCLES) {
         normal = mk<R>(1, 0);
@@ -693,7 +694,6 @@ template <class R> __device__ void init_velocity(Cons<R> &k, vec2<double> ca, do
     }
     k.normal = normal;
     vec2<R> tangent = cross(normal, (R)1);
-    vec2<R> car = cvt<R>(ca), cbr = cvt<R>(cb);
     for (int i = 0; i < k.npts; ++i) {
         vec2<R> ra = pts[i] - car, rb = pts[i] - cbr;
         k.rA[i] = ra; k.rB[i] = rb;
@@ -722,6 +722,11 @@ template <class R> __device__ void init_velocity(Cons<R> &k, vec2<double> ca, do
             k.npts = 1;
         }
     }
+}
+
+template <class R> __device__ __forceinline__ void init_velocity(Cons<R> &k, vec2<double> ca, double aa, vec2<double> cb, double ab,
+                                                                 vec2<R> va, R wa, vec2<R> vb, R wb) {
+    init_velocity_xf(k, pose_xf<R>(ca, aa, k.lca), pose_xf<R>(cb, ab, k.lcb), cvt<R>(ca), cvt<R>(cb), va, wa, vb, wb);
 }
 
 // contact.py:498-525
@@ -1195,12 +1200,26 @@ template <class R> __device__ __forceinline__ void integrate_velocity_body(const
 
 // contact.py:375-496 for constraint k (positions before integration,
 // velocities after)
-template <class R> __device__ __forceinline__ void init_constraint(const WView<R> &w, int k, const StepParams &sp) {
+template <class R> __device__ __forceinline__ void init_constraint(const WView<R> &w, int k, const StepParams &sp,
+                                                                   bool use_pose = false) {
     ConsPos<R> &cp = w.B.s_cp[w.cb + k];
     Cons<R> q;
     build_cons(w, q, cp.cidx, (w.H->flags & GB_W_WARM_STARTING) != 0, w.H->inv_dt0 * sp.dt);
     int ga = w.bb + q.ia, gbb = w.bb + q.ib;
-    init_velocity(q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], w.B.b_v[ga], w.B.b_w[ga], w.B.b_v[gbb], w.B.b_w[gbb]);
+    if (use_pose) {
+        // the float32 centres and rotations k_vinit stored: the same values
+        // pose_xf derives from the float64 poses, without float64 arithmetic
+        const float4 pa = w.B.s_pose[ga], pb = w.B.s_pose[gbb];
+        xform2<R> xa, xb;
+        xa.q.c = (R)pa.z; xa.q.s = (R)pa.w;
+        xa.p = mk<R>((R)pa.x, (R)pa.y) - rmul(xa.q, q.lca);
+        xb.q.c = (R)pb.z; xb.q.s = (R)pb.w;
+        xb.p = mk<R>((R)pb.x, (R)pb.y) - rmul(xb.q, q.lcb);
+        init_velocity_xf(q, xa, xb, mk<R>((R)pa.x, (R)pa.y), mk<R>((R)pb.x, (R)pb.y), w.B.b_v[ga], w.B.b_w[ga], w.B.b_v[gbb],
+                         w.B.b_w[gbb]);
+    } else {
+        init_velocity(q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], w.B.b_v[ga], w.B.b_w[ga], w.B.b_v[gbb], w.B.b_w[gbb]);
+    }
     ConsVel<R> v;
     for (int j = 0; j < 2; ++j) {
         v.ni[j] = j < q.mcount ? q.ni[j] : (R)0;
@@ -1265,13 +1284,17 @@ template <class R> __device__ __forceinline__ Cons<R> pos_cons(const ConsPos<R> 
 // nbuf - 1 chunks of bulk copies (cp.async.bulk, completion on an mbarrier)
 // in flight ahead of the chunk being solved.  Without a cache every pass
 // reads the records and bodies from global memory.
+static __device__ __forceinline__ bool is_neg_zero(float x) { return __float_as_uint(x) == 0x80000000u; }
+static __device__ __forceinline__ bool is_neg_zero(double x) {
+    return (unsigned long long)__double_as_longlong(x) == 0x8000000000000000ull;
+}
 struct BodyCache {
     unsigned char *mem;   // nullptr: the passes read and write global memory
     int nbuf;             // constraint chunk buffers after the bodies (0: none)
 };
 // shared-memory bytes of the body cache and of one chunk buffer
 template <class R> __host__ __device__ constexpr int cache_bytes_per_body() {
-    return 2 * (int)sizeof(double) + (int)sizeof(double) + 2 * (int)sizeof(R) + 1;   // c, a, inverse masses, static flag
+    return 2 * (int)sizeof(double) + (int)sizeof(double) + 2 * (int)sizeof(R);   // c, a, inverse mass and inertia
 }
 __host__ __device__ inline size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
 template <class R> __host__ __device__ inline size_t cache_body_bytes(int nb) {
@@ -1352,13 +1375,15 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     R *om = w.B.b_w + w.bb;
     const R *invm = w.B.b_inv_mass + w.bb;
     const R *invi = w.B.b_inv_I + w.bb;
-    unsigned char *stat = nullptr;
+    const R *stat_ii = nullptr;   // cached inverse inertias, -0 marking a static body
     vec2<double> *pc = w.B.b_c + w.bb;
     double *pa = w.B.b_a + w.bb;
     ChunkPipe pipe{nullptr, nullptr, 0, 0, 0u, 0};
     int *pipe_fail = nullptr;   // shared flag: some thread's bounded wait gave up
     if (cached) {
-        // layout: c[nb] (16) | a[nb] (8) | inverse mass, inertia (R) | static flag (1);
+        // layout: c[nb] (16) | a[nb] (8) | inverse mass, inertia (R); a static
+        // body's inverse inertia is stored as -0 (its zero inertia changes no
+        // sum or product the passes form; the sign marks it as static);
         // the velocity passes keep v[nb], w[nb] in the c/a bytes
         unsigned char *m = cache.mem;
         pc = reinterpret_cast<vec2<double> *>(m);
@@ -1367,12 +1392,12 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         om = reinterpret_cast<R *>(m + sizeof(vec2<R>) * (size_t)nb);
         R *im = reinterpret_cast<R *>(m + 24 * (size_t)nb);
         R *ii = im + nb;
-        stat = reinterpret_cast<unsigned char *>(ii + nb);
+        stat_ii = ii;
         invm = im; invi = ii;
         for (int b = rank; b < nb; b += g.size()) {
             vel[b] = w.B.b_v[w.bb + b]; om[b] = w.B.b_w[w.bb + b];
-            im[b] = w.B.b_inv_mass[w.bb + b]; ii[b] = w.B.b_inv_I[w.bb + b];
-            stat[b] = w.btype(b) == GB_BODY_STATIC ? 1 : 0;
+            im[b] = w.B.b_inv_mass[w.bb + b];
+            ii[b] = w.btype(b) == GB_BODY_STATIC ? -(R)0 : w.B.b_inv_I[w.bb + b];
         }
         if (cache.nbuf > 0) {
             pipe.buf = m + cache_body_bytes<R>(nb);
@@ -1388,7 +1413,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         }
         g.sync();
     }
-    auto is_static = [&](int b) { return stat ? stat[b] != 0 : w.btype(b) == GB_BODY_STATIC; };
+    auto is_static = [&](int b) { return stat_ii ? is_neg_zero(stat_ii[b]) : w.btype(b) == GB_BODY_STATIC; };
     bool failed = false;
     if (pipe.nbuf > 0 && ncons > 0) {
         int *tab = w.B.s_pref + w.cb + 1;   // chunk table (entry -1: its length)
@@ -1434,8 +1459,8 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
                     gr.ni[0] = k.ni[0]; gr.ni[1] = k.ni[1]; gr.ti[0] = k.ti[0]; gr.ti[1] = k.ti[1];
                 }
                 // colour classes share no non-static body; static bodies keep v = 0
-                if (!stat[ia]) { vel[ia] = va; om[ia] = wa; }
-                if (!stat[ib]) { vel[ib] = vb; om[ib] = wb; }
+                if (!is_neg_zero(stat_ii[ia])) { vel[ia] = va; om[ia] = wa; }
+                if (!is_neg_zero(stat_ii[ib])) { vel[ib] = vb; om[ib] = wb; }
             }
             if (q + 1 < total) load_imp(q + 1);   // after this thread's own stores
             g.sync();

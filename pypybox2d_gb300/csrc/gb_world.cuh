@@ -113,6 +113,7 @@ template <class R> struct Batch {
     uint32_t *s_root;         // per-root bits
     unsigned long long *s_claim, *s_minsep, *s_minsleep;
     unsigned char *s_bvis;
+    float4 *s_pose;              // float32 unit: each body's float32 centre and rotation at the solver set-up
     // scratch (fixture-indexed)
     int *s_move, *s_first, *s_cnt;
     int *s_grid;              // pair-finding grid: 12 nf + 2 ints per world (cell ends, listed and big proxies)
