@@ -11,6 +11,7 @@
 // event is group-parallel.
 #pragma once
 #include "gb_step.cuh"
+#include "gb_toi_f32.cuh"
 
 // world.py:617-653 for contact i at the start of a TOI pass: 0 = skipped
 // (disabled, sub-stepped too often, sensor, inactive, no bullet or
@@ -52,12 +53,22 @@ template <class R> __device__ double toi_align(const WView<R> &w, int i, Sweep *
 // world.py:669-681: the time of impact from the aligned sweeps (float64)
 template <class R> __device__ void toi_compute(const WView<R> &w, int i, double alpha0, const Sweep &sa, const Sweep &sb) {
     ContactRec<R> &c = w.con(i);
+    double beta;
+    bool lim = false;
+#if defined(GB_POSE_ROT_F32)
+    // float32 unit: float32 arithmetic on sweeps relative to sweep A's start
+    FProxy pa, pb;
+    fproxy_init(pa, w.shape(c.fa));
+    fproxy_init(pb, w.shape(c.fb));
+    float beta_f = 1.0f;
+    int state = time_of_impact_f32(pa, pb, fsweep_of(sa, sa.c0), fsweep_of(sb, sa.c0), 1.0f, &beta_f, &lim);
+    beta = (double)beta_f;
+#else
     DProxy pa, pb;
     dproxy_init(pa, w.shape(c.fa));
     dproxy_init(pb, w.shape(c.fb));
-    double beta;
-    bool lim = false;
     int state = time_of_impact(pa, pb, sa, sb, 1.0, &beta, &lim);
+#endif
     if (lim) atomicOr(&w.H->status, GB_ST_ITER_LIMIT);
     double alpha = (state == TOI_TOUCHING) ? pymin(alpha0 + (1.0 - alpha0) * beta, 1.0) : 1.0;
     c.toi = alpha;
