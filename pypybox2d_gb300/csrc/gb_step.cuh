@@ -874,8 +874,15 @@ template <class R> __device__ double solve_position(const Cons<R> &k, vec2<doubl
 // passes (dc, da), so the passes run without float64 arithmetic; the caller
 // adds the corrections to the float64 pose once, after the passes.
 static __device__ float solve_position_f32d(const Cons<float> &k, vec2<float> cfa, float ara, vec2<float> &dca, float &daa,
-                                            vec2<float> cfb, float arb, vec2<float> &dcb, float &dab, float minsep) {
-    const float ma = k.ma, mb = k.mb, iA = k.iA, iB = k.iB;
+                                            vec2<float> cfb, float arb, vec2<float> &dcb, float &dab, float minsep,
+                                            bool toi = false, bool toi_a = false, bool toi_b = false) {
+    float ma = k.ma, mb = k.mb, iA = k.iA, iB = k.iB;
+    float baum = (float)GB_BAUMGARTE;
+    if (toi) {
+        baum = (float)GB_TOI_BAUMGARTE;
+        if (!toi_a) { ma = 0.0f; iA = 0.0f; }
+        if (!toi_b) { mb = 0.0f; iB = 0.0f; }
+    }
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
         if (j >= k.mcount) break;
@@ -908,7 +915,7 @@ static __device__ float solve_position_f32d(const Cons<float> &k, vec2<float> cf
         }
         vec2<float> ra = point - ca, rb = point - cb;
         minsep = pymin(minsep, sep);
-        float C = cclamp((float)GB_BAUMGARTE * (sep + (float)GB_LINEAR_SLOP), (float)-GB_MAX_LINEAR_CORRECTION, 0.0f);
+        float C = cclamp(baum * (sep + (float)GB_LINEAR_SLOP), (float)-GB_MAX_LINEAR_CORRECTION, 0.0f);
         float rna = sq(cross(ra, normal)), rnb = sq(cross(rb, normal));
         float K = ma + mb + (iA * rna) + (iB * rnb);
         float impulse = K > 0.0f ? -C / K : 0.0f;

@@ -112,6 +112,32 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
         }
         idx[k][0] = la; idx[k][1] = lb;
     }
+#if defined(GB_POSE_ROT_F32)
+    // float32 unit: the position passes on float32 deltas (solve_position_f32d);
+    // only the two TOI bodies move
+    {
+        vec2<float> cf[2 * GB_MAX_TOI_CONTACTS], dc[2 * GB_MAX_TOI_CONTACTS];
+        float ar[2 * GB_MAX_TOI_CONTACTS], da[2 * GB_MAX_TOI_CONTACTS];
+        for (int i = 0; i < nbi; ++i) {
+            cf[i] = cvt<float>(pc[i]); ar[i] = angle_f32(pa[i]);
+            dc[i] = mk<float>(0.0f, 0.0f); da[i] = 0.0f;
+        }
+        for (int it = 0; it < 20; ++it) {
+            float minsep = 0.0f;
+            for (int k = 0; k < nci; ++k) {
+                int la = idx[k][0], lb = idx[k][1];
+                minsep = solve_position_f32d(ks[k], cf[la], ar[la], dc[la], da[la], cf[lb], ar[lb], dc[lb], da[lb], minsep, true,
+                                             la == toi_a || la == toi_b, lb == toi_a || lb == toi_b);
+            }
+            if (minsep >= -1.5f * (float)GB_LINEAR_SLOP) break;
+        }
+        for (int i = 0; i < nbi; ++i) {
+            if (dc[i].x != 0.0f) pc[i].x = pc[i].x + (double)dc[i].x;
+            if (dc[i].y != 0.0f) pc[i].y = pc[i].y + (double)dc[i].y;
+            if (da[i] != 0.0f) pa[i] = pa[i] + (double)da[i];
+        }
+    }
+#else
     for (int it = 0; it < 20; ++it) {
         double minsep = 0.0;
         for (int k = 0; k < nci; ++k) {
@@ -121,6 +147,7 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
         }
         if (minsep >= -1.5 * GB_LINEAR_SLOP) break;
     }
+#endif
     w.B.b_c0[w.bb + ib[toi_a]] = pc[toi_a]; w.B.b_a0[w.bb + ib[toi_a]] = pa[toi_a];
     w.B.b_c0[w.bb + ib[toi_b]] = pc[toi_b]; w.B.b_a0[w.bb + ib[toi_b]] = pa[toi_b];
     for (int k = 0; k < nci; ++k) {
