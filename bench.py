@@ -8,9 +8,12 @@ Workloads (``--workload``):
   pyramid  4096 copies of the 20-row pyramid (210 boxes on a ground box),
            every box position jittered by a seeded U(-0.01, 0.01) m; 2000 steps.
 Both: dt = 1/60, 8 velocity and 3 position iterations, float32 bulk
-arithmetic with float64 positions, angles, sleep timers and time of impact,
-the 12-13-launch phased step on one stream.  A "step" is one World.step of
-every world of the batch.
+arithmetic with float64 positions, angles, sleep timers and time of impact.
+After the warm-up the launch autotuner (gb_batch_autotune) picks the launch
+configuration from trials that start from the warmed-up state and leave it
+unchanged; the timed steps then replay captured CUDA graphs of
+``--graph-steps`` phased steps (12-13 launches each).  A "step" is one
+World.step of every world of the batch.
 
 Reported (one JSON line on rank 0):
   value    dynamic body-steps/s with the batch resident in HBM (device time,
@@ -23,6 +26,8 @@ Reported (one JSON line on rank 0):
            per contact, from live counts) over the event-timed step, and of
            the dominant launch with its own byte model (``kernels``)
   kernels  event-timed device ms per launch slot of the phased step
+  autotune the tuner's trials and choice; graph: steps per captured graph and
+           the same steps as one plain gb_batch_step call
   cpu_baseline  the CPU restatement (oracle/, C, float64) on the host cores
            stepping a bounded sample of the same worlds
   plain    the float64 path launched per world, one step per launch
@@ -173,10 +178,11 @@ def solve_bytes_per_step(n_bodies, n_constraints, real_bytes=4):
     return n_bodies * (6 * real_bytes + 48 + 16) + n_constraints * (216 + 32)
 
 
-def launches_per_step(W):
+def launches_per_step(W, big_bodies: int = 512):
     """Kernel launches of one phased step: 12, plus a second solver launch
-    when the batch mixes worlds below and above 512 bodies."""
-    nbig = int(np.count_nonzero(W["body_count"] >= 512))
+    when the batch mixes worlds below and above the wide launch's threshold
+    (big_bodies)."""
+    nbig = int(np.count_nonzero(W["body_count"] >= big_bodies))
     return 12 + (1 if 0 < nbig < len(W) else 0)
 
 
@@ -321,6 +327,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--ktime-steps", type=int, default=20, help="steps of the per-launch timing pass")
     ap.add_argument("--no-extras", action="store_true", help="skip cpu baseline, plain path and error legs")
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch autotuner (use --mode / --threads)")
+    ap.add_argument("--tune-steps", type=int, default=3, help="timed steps per autotuner trial")
+    ap.add_argument("--graph-steps", type=int, default=50, help="steps per captured CUDA graph in the timed region "
+                                                                "(0 = one gb_batch_step call)")
     args = ap.parse_args()
 
     if args.impl == "reference":
@@ -357,12 +367,45 @@ def main():
     batch.step(DT, VI, PI, args.warmup, launch_mode=args.mode, block_threads=args.threads, stream=sh)
     torch.cuda.synchronize()
 
+    # launch autotuner: trials from the warmed-up state, which it restores
+    mode, threads = args.mode, args.threads
+    tune = None
+    if not args.no_tune:
+        import time
+        t0 = time.time()
+        best, trials = batch.autotune(DT, VI, PI, steps_per_trial=args.tune_steps, stream=sh)
+        mode, threads = 0, 0          # steps take the tuned launch configuration
+        tune = {"best": best, "trials": len(trials), "steps_per_trial": args.tune_steps,
+                "seconds": round(time.time() - t0, 2),
+                "table": [[t["launch_mode"], t["block_threads"], t["pipe_bufs"], t["big_bodies"],
+                           round(t["ms_per_step"], 3)] for t in trials],
+                "columns": ["launch_mode", "block_threads", "pipe_bufs", "big_bodies", "ms_per_step"]}
+    cfg = batch.launch_config() if tune else {"launch_mode": args.mode, "block_threads": args.threads,
+                                              "pipe_bufs": 2, "big_bodies": 512}
+    eff_mode = cfg["launch_mode"]
+
+    # the timed steps: captured rollouts of graph_steps phased steps replayed
+    # back to back (the remainder, if any, as one plain call)
+    graph, graph_info, n_graph = None, None, 0
+    if args.graph_steps > 0 and eff_mode == 3:
+        g_steps = min(args.graph_steps, steps)
+        try:
+            graph = batch.capture(DT, VI, PI, n_steps=g_steps, launch_mode=mode, block_threads=threads)
+            n_graph = steps // g_steps
+            graph_info = {"steps_per_graph": g_steps, "graph_launches": n_graph, "plain_steps": steps - n_graph * g_steps}
+        except abi.GB2DError as ex:
+            graph_info = {"unavailable": str(ex)}
+    rest = steps - (n_graph * graph.n_steps if graph else 0)
+
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         barrier()
         torch.cuda.synchronize()
         e0.record(stream)
-        batch.step(DT, VI, PI, steps, launch_mode=args.mode, block_threads=args.threads, stream=sh)
+        for _ in range(n_graph):
+            graph.launch(stream=sh)
+        if rest:
+            batch.step(DT, VI, PI, rest, launch_mode=mode, block_threads=threads, stream=sh)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -391,8 +434,8 @@ def main():
 
     # per-launch device times (separate pass, one host wait per step)
     kt = {}
-    if args.mode == 3 and args.ktime_steps > 0:
-        batch.step(DT, VI, PI, args.ktime_steps, launch_mode=3, block_threads=args.threads, stream=sh, kernel_times=True)
+    if eff_mode == 3 and args.ktime_steps > 0:
+        batch.step(DT, VI, PI, args.ktime_steps, launch_mode=mode, block_threads=threads, stream=sh, kernel_times=True)
         torch.cuda.synchronize()
         tot, nsteps = batch.kernel_times()
         kt = {k: v / max(nsteps, 1) for k, v in tot.items()}
@@ -410,6 +453,18 @@ def main():
                                             "unit": "GB/s", "frac": sb / (kt[top] / 1e3) / 1e9 / peak,
                                             "algorithmic_bytes_per_launch": sb}
 
+    # the same steps as one plain gb_batch_step call, for the graphs' effect
+    if graph is not None:
+        nd = min(steps, 100)
+        e6, e7 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e6.record(stream)
+        batch.step(DT, VI, PI, nd, launch_mode=mode, block_threads=threads, stream=sh)
+        e7.record(stream)
+        torch.cuda.synchronize()
+        graph_info["plain_call_ms_per_step"] = e6.elapsed_time(e7) / nd
+        graph_info["plain_call_steps"] = nd
+
     # e2e through the C ABI with pinned host buffers
     n_b = len(B)
     pinned = torch.empty(n_b * abi.BODY.itemsize, dtype=torch.uint8, pin_memory=True)
@@ -419,7 +474,7 @@ def main():
     ptr = pinned.data_ptr()
     e2 = torch.cuda.Event(enable_timing=True)
     e3 = torch.cuda.Event(enable_timing=True)
-    opts = abi.StepOpts(DT, VI, PI, 1, args.mode, args.threads, 0)
+    opts = abi.StepOpts(DT, VI, PI, 1, mode, threads, 0)
     barrier()
     torch.cuda.synchronize()
     e2.record(stream)
@@ -441,18 +496,21 @@ def main():
                    "bodies_per_world": {"min": int(dyn.min()), "mean": float(dyn.mean()), "max": int(dyn.max())},
                    "launch": {1: "one persistent launch per timed region, one CTA per world",
                               2: "one persistent launch per timed region, one warp per world",
-                              3: f"{launches_per_step(W)} launches per step (batch-wide + per-world)"}[args.mode],
-                   "block_threads": args.threads,
+                              3: f"{launches_per_step(W, cfg['big_bodies'])} launches per step (batch-wide + per-world)"
+                              + (f", captured as CUDA graphs of {graph.n_steps} steps" if graph else "")}[eff_mode],
+                   "launch_config": cfg,
                    "l2": f"inputs larger than L2: {batch.arena_bytes() / 2**30:.2f} GiB resident per GPU",
                    "mean_contacts_per_world": float(np.mean(counts))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": f"whole step ({launches_per_step(W)} launches)",
+                     "kernel": f"whole step ({launches_per_step(W, cfg['big_bodies'])} launches)",
                      "algorithmic_bytes_per_step": bytes_step},
         "kernels": kernels,
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY.itemsize,
                 "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": args.e2e_steps},
-        "gpu_launches": launches_per_step(W) * steps if args.mode == 3 else 1,
+        "gpu_launches": launches_per_step(W, cfg["big_bodies"]) * steps if eff_mode == 3 else 1,
+        "autotune": tune,
+        "graph": graph_info,
         "clocks": clocks.summary(),
         "status_nonzero_worlds": int(np.count_nonzero(status)),
     }

@@ -194,8 +194,11 @@ typedef struct gb_scene {
 
 typedef struct gb_batch gb_batch; /* opaque device-resident batch of worlds */
 
-/* Step options.  launch_mode: 0 = autotuned, 1 = one CTA per world,
- * 2 = one warp per world.  block_threads: CTA size for mode 1 (0 = tuned). */
+/* Step options.  launch_mode: 0 = the batch's launch configuration
+ * (gb_batch_set_launch_config, gb_batch_autotune), 1 = one CTA per world,
+ * 2 = one warp per world, 3 = phased (batch-wide and per-world launches).
+ * block_threads: CTA width (0 = the launch configuration's for mode 0,
+ * 128 otherwise). */
 typedef struct gb_step_opts {
     double dt;
     int32_t vel_iters, pos_iters;
@@ -275,6 +278,91 @@ int gb_batch_kernel_times(gb_batch *batch, double *total_ms, int32_t capacity, i
  * flagged GB_ST_EVENT_OVERFLOW. */
 int gb_batch_get_events(gb_batch *batch, int32_t world, gb_event *out, int32_t capacity, int32_t *n_out,
                         void *cuda_stream);
+
+/* How the step is mapped onto the GPU.  Every mapping gives the same float64
+ * results; only the time differs.  In float32 the phased configurations give
+ * the same results as long as each world's solver keeps its shared-memory
+ * body cache (worlds of up to 2048 bodies); launch modes 1 and 2 and uncached
+ * worlds round differently, within the float32 step error.  A batch starts
+ * with {3, 128, 2, 512}.  No counterpart in the reference (one CPython world
+ * has no launch geometry). */
+typedef struct gb_launch_config {
+    int32_t launch_mode;    /* 1 = one CTA per world, 2 = one warp per world, 3 = phased */
+    int32_t block_threads;  /* CTA width: mode 1 the world's CTA, mode 2 warps per CTA x 32, mode 3 the
+                               solver CTA of the smaller worlds (islands 4x, pair phases 2x, up to 256) */
+    int32_t pipe_bufs;      /* mode 3 solver: constraint-chunk buffers in shared memory, 0..4
+                               (0: records read from global memory) */
+    int32_t big_bodies;     /* mode 3 solver: worlds of this many bodies or more get the wide launch */
+    double ms_per_step;     /* autotune output (device ms per step); ignored on input */
+} gb_launch_config;
+#define GB_LAUNCH_CONFIG_BYTES 24
+/* Set the configuration that steps with launch_mode 0 use (and pipe_bufs /
+ * big_bodies for every phased step).  The batch state is not touched. */
+int gb_batch_set_launch_config(gb_batch *batch, const gb_launch_config *cfg);
+int gb_batch_get_launch_config(gb_batch *batch, gb_launch_config *cfg);
+/* Autotuner.  Times candidate configurations on the batch's own next
+ * opts->n_steps steps: the device arena is copied aside once, every trial
+ * starts from that copy, and the copy is put back at the end, so the batch
+ * state after the call is the state before it (the call needs device memory
+ * for one more arena while it runs).  Stages, each keeping the best so far:
+ * (1) mapping: phased with 32/64/128 threads, one CTA per world with 128/256
+ * threads, one warp per world with 2/4 warps per CTA (phased only for
+ * batches with cooperative-grid worlds); (2) big_bodies 256/512/1024/2048/
+ * none; (3) pipe_bufs 0-4.  Each trial's steps are timed with CUDA events on
+ * `cuda_stream`.  trials[] receives every trial in order (ms_per_step < 0:
+ * not runnable, e.g. too much shared memory); the best becomes the batch's
+ * launch configuration.  opts->record_order must be 0. */
+int gb_batch_autotune(gb_batch *batch, const gb_step_opts *opts, gb_launch_config *trials, int32_t capacity,
+                      int32_t *n_out, gb_launch_config *best, void *cuda_stream);
+
+/* A multi-step rollout captured as one CUDA graph (the 12-13 launches of
+ * each of opts->n_steps phased steps), replayed by gb_graph_launch with no
+ * host work per step.  Replaces calling World.step n_steps times
+ * (world.py:307-354).  The graph keeps the options, launch configuration and
+ * device buffers of the capture: replays read and advance the batch's
+ * current device state, so gb_batch_set_bodies and the getters may be used
+ * between replays; a later gb_batch_set_launch_config does not change an
+ * existing graph.  Not available: GB_OPT_KERNEL_TIMES (host timing), batches
+ * with cooperative-grid worlds (16384+ bodies), launch modes 1 and 2. */
+typedef struct gb_graph gb_graph;
+int gb_graph_capture(gb_batch *batch, const gb_step_opts *opts, gb_graph **out);
+/* Replay the captured steps on `cuda_stream` (asynchronous). */
+int gb_graph_launch(gb_graph *graph, void *cuda_stream);
+int gb_graph_destroy(gb_graph *graph);
+
+/* One ray of gb_batch_ray_cast, from (p1x, p1y) to (p2x, p2y) in one world. */
+typedef struct gb_ray {
+    int32_t world, _pad0;
+    double p1x, p1y, p2x, p2y;
+} gb_ray;
+/* The closest hit of a ray: what World.ray_cast (world.py:387-440) leaves in
+ * a callback that returns the fraction it is given.  fixture = -1 (and
+ * fraction 1) when no fixture is hit. */
+typedef struct gb_ray_hit {
+    int32_t fixture, _pad0;   /* world-local fixture index */
+    double px, py;            /* (1 - fraction) * p1 + fraction * p2 */
+    double nx, ny;            /* the shape's normal at the hit (edges: in the edge's frame, as shapes.py:655-702) */
+    double fraction;
+} gb_ray_hit;
+/* One box of gb_batch_query_aabb: lower (lx, ly), upper (ux, uy). */
+typedef struct gb_aabb_query {
+    int32_t world, _pad0;
+    double lx, ly, ux, uy;
+} gb_aabb_query;
+/* Closest hit of every ray against the fixtures of its world (circle,
+ * polygon and edge ray casts of shapes.py:147-171, 265-314, 655-702, behind
+ * the broad-phase segment test of dynamictree.py:209-250 with
+ * max_fraction 1).  Ties go to the lower fixture index.  A ray of zero length
+ * is rejected (GB_E_ARG), as dynamictree.py:222-224 raises.  Host arrays in
+ * and out; the call waits for its results.  Replaces World.ray_cast with a
+ * closest-hit callback, for many rays at once. */
+int gb_batch_ray_cast(gb_batch *batch, const gb_ray *rays, int32_t n_rays, gb_ray_hit *hits, void *cuda_stream);
+/* Fixtures whose fat AABB overlaps each query box (World.query_aabb,
+ * world.py:371-385; DynamicTree.query, dynamictree.py:190-207), in fixture
+ * order: query q's first max_per_query fixtures go to
+ * fixtures[q * max_per_query ...], counts[q] is how many overlap in all. */
+int gb_batch_query_aabb(gb_batch *batch, const gb_aabb_query *queries, int32_t n_queries, int32_t *fixtures,
+                        int32_t max_per_query, int32_t *counts, void *cuda_stream);
 
 /* Size of the static device scratch of gb_batch_step_static_scratch (32 MiB). */
 #define GB_STATIC_SCRATCH_BYTES (32u << 20)

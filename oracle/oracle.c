@@ -1219,3 +1219,145 @@ int or_batch_get_bodies(const or_batch *b, int wi, gb_body *out) {
     or_get_bodies(b->w[wi], out);
     return b->w[wi]->nb;
 }
+
+/* ------------------------------------------------------------------ queries
+ * World.ray_cast with a closest-hit callback (world.py:387-440) and
+ * World.query_aabb (world.py:371-385) over one world's host records
+ * (fixture.body indexes `bodies`, fixtures world-local). */
+
+/* AABB.test_overlap (aabbmodule.c AABB_test_overlap): node box a, other box b */
+static int or_box_overlap(const double *a, double blx, double bly, double bhx, double bhy) {
+    return !((blx - a[2]) > 0.0 || (bly - a[3]) > 0.0 || (a[0] - bhx) > 0.0 || (a[1] - bhy) > 0.0);
+}
+
+/* Circle.ray_cast (shapes.py:147-171), max_fraction 1 */
+static int or_ray_circle(const gb_fixture *f, xform xf, v2 p1, v2 p2, v2 *normal, double *fraction) {
+    v2 position = vadd(xf.p, rmul(xf.q, V(f->vx[0], f->vy[0])));
+    v2 s = vsub(p1, position);
+    double b = vdot(s, s) - SQ(f->radius);
+    v2 r = vsub(p2, p1);
+    double c = vdot(s, r);
+    double rr = vdot(r, r);
+    double sigma = c * c - rr * b;
+    if (sigma < 0.0 || rr < DBL_EPSILON) return 0;
+    double a = -(c + sqrt(sigma));
+    if (0.0 <= a && a <= 1.0 * rr) {
+        a /= rr;
+        *fraction = a;
+        *normal = vnormalized(vadd(s, vscale(a, r)));
+        return 1;
+    }
+    return 0;
+}
+
+/* Polygon.ray_cast (shapes.py:265-314), max_fraction 1 */
+static int or_ray_polygon(const gb_fixture *f, xform xf, v2 p1, v2 p2, v2 *normal, double *fraction) {
+    v2 q1 = rmul_t(xf.q, vsub(p1, xf.p));
+    v2 q2 = rmul_t(xf.q, vsub(p2, xf.p));
+    v2 d = vsub(q2, q1);
+    double lower = 0.0, upper = 1.0;
+    int tagged = -1;
+    for (int k = 0; k < f->vertex_count; ++k) {
+        v2 nk = V(f->nx[k], f->ny[k]);
+        double numerator = vdot(nk, vsub(V(f->vx[k], f->vy[k]), q1));
+        double denominator = vdot(nk, d);
+        if (denominator == 0.0) {
+            if (numerator < 0.0) return 0;
+        } else {
+            if (denominator < 0.0 && numerator < lower * denominator) {
+                lower = numerator / denominator;
+                tagged = k;
+            } else if (denominator > 0.0 && numerator < upper * denominator) {
+                upper = numerator / denominator;
+            }
+        }
+        if (upper < lower) return 0;
+    }
+    if (tagged < 0) return 0;
+    *normal = rmul(xf.q, V(f->nx[tagged], f->ny[tagged]));
+    *fraction = lower;
+    return 1;
+}
+
+/* Edge.ray_cast (shapes.py:655-702); the normal stays in the edge's frame */
+static int or_ray_edge(const gb_fixture *f, xform xf, v2 p1, v2 p2, v2 *normal, double *fraction) {
+    v2 q1 = rmul_t(xf.q, vsub(p1, xf.p));
+    v2 q2 = rmul_t(xf.q, vsub(p2, xf.p));
+    v2 d = vsub(q2, q1);
+    v2 v1 = V(f->vx[0], f->vy[0]), v2_ = V(f->vx[1], f->vy[1]);
+    v2 e = vsub(v2_, v1);
+    v2 nn = vnormalized(V(e.y, -e.x));
+    double numerator = vdot(nn, vsub(v1, q1));
+    double denominator = vdot(nn, d);
+    if (denominator == 0.0) return 0;
+    double t = numerator / denominator;
+    if (t < 0.0 || 1.0 < t) return 0;
+    v2 q = vadd(q1, vscale(t, d));
+    v2 r = vsub(v2_, v1);
+    double rr = vdot(r, r);
+    if (rr == 0.0) return 0;
+    double s = vdot(vsub(q, v1), r) / rr;
+    if (s < 0.0 || 1.0 < s) return 0;
+    *fraction = t;
+    *normal = numerator > 0.0 ? vneg(nn) : nn;
+    return 1;
+}
+
+void or_ray_cast_records(const gb_body *bodies, const gb_fixture *fixtures, int nf, const gb_ray *rays, int n,
+                         gb_ray_hit *hits) {
+    for (int q = 0; q < n; ++q) {
+        v2 p1 = V(rays[q].p1x, rays[q].p1y), p2 = V(rays[q].p2x, rays[q].p2y);
+        /* DynamicTree.ray_cast's segment tests (dynamictree.py:222-250) */
+        v2 r = vnormalized(vsub(p2, p1));
+        v2 v = vcross_sv(1.0, r);
+        v2 abs_v = V(fabs(v.x), fabs(v.y));
+        v2 t = vadd(p1, vscale(1.0, vsub(p2, p1)));
+        double slx = pymin(p1.x, t.x), sly = pymin(p1.y, t.y), shx = pymax(p1.x, t.x), shy = pymax(p1.y, t.y);
+        gb_ray_hit o;
+        memset(&o, 0, sizeof(o));
+        o.fixture = -1;
+        o.fraction = 1.0;
+        double best = 2.0;
+        v2 best_n = V(0.0, 0.0);
+        for (int k = 0; k < nf; ++k) {
+            const gb_fixture *f = &fixtures[k];
+            const double *a = f->aabb;
+            if (!or_box_overlap(a, slx, sly, shx, shy)) continue;
+            v2 c = V(0.5 * (a[2] + a[0]), 0.5 * (a[3] + a[1]));
+            v2 h = V(0.5 * (a[2] - a[0]), 0.5 * (a[3] - a[1]));
+            double separation = fabs(vdot(v, vsub(p1, c))) - vdot(abs_v, h);
+            if (separation > 0.0) continue;
+            const gb_body *b = &bodies[f->body];
+            xform xf;
+            xf.p = V(b->px, b->py);
+            xf.q.c = b->qc;
+            xf.q.s = b->qs;
+            v2 nrm;
+            double fr = 0.0;
+            int hit = 0;
+            if (f->shape_type == GB_SHAPE_CIRCLE) hit = or_ray_circle(f, xf, p1, p2, &nrm, &fr);
+            else if (f->shape_type == GB_SHAPE_POLYGON) hit = or_ray_polygon(f, xf, p1, p2, &nrm, &fr);
+            else if (f->shape_type == GB_SHAPE_EDGE) hit = or_ray_edge(f, xf, p1, p2, &nrm, &fr);
+            if (hit && fr < best) { best = fr; o.fixture = k; best_n = nrm; }
+        }
+        if (o.fixture >= 0) {
+            /* world.py:431: (1 - fraction) * point1 + fraction * point2 */
+            v2 pt = vadd(vscale(1.0 - best, p1), vscale(best, p2));
+            o.px = pt.x; o.py = pt.y; o.nx = best_n.x; o.ny = best_n.y; o.fraction = best;
+        }
+        hits[q] = o;
+    }
+}
+
+void or_query_aabb_records(const gb_fixture *fixtures, int nf, const gb_aabb_query *qs, int n, int32_t *out, int cap,
+                           int32_t *counts) {
+    for (int q = 0; q < n; ++q) {
+        int found = 0;
+        for (int k = 0; k < nf; ++k)
+            if (or_box_overlap(fixtures[k].aabb, qs[q].lx, qs[q].ly, qs[q].ux, qs[q].uy)) {
+                if (found < cap) out[(size_t)q * cap + found] = k;
+                ++found;
+            }
+        counts[q] = found;
+    }
+}

@@ -54,6 +54,14 @@ void or_batch_destroy(or_batch *b);
 double or_batch_step(or_batch *b, double dt, int vel_iters, int pos_iters, int n_steps, int threads);
 int or_batch_get_bodies(const or_batch *b, int world, gb_body *out);
 
+/* World.ray_cast with a closest-hit callback and World.query_aabb over one
+ * world's records (bodies and fixtures world-local; the rays' and queries'
+ * world fields are not read). */
+void or_ray_cast_records(const gb_body *bodies, const gb_fixture *fixtures, int nf, const gb_ray *rays, int n,
+                         gb_ray_hit *hits);
+void or_query_aabb_records(const gb_fixture *fixtures, int nf, const gb_aabb_query *qs, int n, int32_t *out, int cap,
+                           int32_t *counts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -112,6 +112,30 @@ class StepOpts(ctypes.Structure):
     ]
 
 
+class LaunchConfig(ctypes.Structure):
+    """ctypes form of ``gb_launch_config``."""
+    _fields_ = [
+        ("launch_mode", ctypes.c_int32), ("block_threads", ctypes.c_int32),
+        ("pipe_bufs", ctypes.c_int32), ("big_bodies", ctypes.c_int32),
+        ("ms_per_step", ctypes.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+#: gb_ray, gb_ray_hit, gb_aabb_query (world queries)
+RAY = np.dtype([("world", "<i4"), ("_pad0", "<i4"), ("p1x", "<f8"), ("p1y", "<f8"), ("p2x", "<f8"), ("p2y", "<f8")],
+               align=True)
+RAY_HIT = np.dtype([("fixture", "<i4"), ("_pad0", "<i4"), ("px", "<f8"), ("py", "<f8"), ("nx", "<f8"), ("ny", "<f8"),
+                    ("fraction", "<f8")], align=True)
+AABB_QUERY = np.dtype([("world", "<i4"), ("_pad0", "<i4"), ("lx", "<f8"), ("ly", "<f8"), ("ux", "<f8"), ("uy", "<f8")],
+                      align=True)
+
+#: sizeof(gb_launch_config) (GB_LAUNCH_CONFIG_BYTES)
+LAUNCH_CONFIG_BYTES = 24
+
+
 def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,
                contacts: np.ndarray | None = None, moves: np.ndarray | None = None) -> tuple[Scene, tuple]:
     """Pack contiguous record arrays into a ``gb_scene``; the returned tuple
@@ -147,6 +171,9 @@ EXPORTED = (
     "gb_batch_get_contact_counts", "gb_batch_get_contacts", "gb_batch_get_solver_order",
     "gb_batch_status", "gb_batch_counters", "gb_batch_phase_clocks",
     "gb_batch_step_static_scratch", "gb_batch_kernel_times", "gb_batch_get_events",
+    "gb_batch_set_launch_config", "gb_batch_get_launch_config", "gb_batch_autotune",
+    "gb_graph_capture", "gb_graph_launch", "gb_graph_destroy",
+    "gb_batch_ray_cast", "gb_batch_query_aabb",
 )
 
 #: gb_step_opts.record_order bit that records contact events
@@ -205,6 +232,15 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_step_static_scratch.argtypes = [vp, ctypes.POINTER(StepOpts), vp]
     lib.gb_batch_kernel_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), i32, i32p, ctypes.POINTER(ctypes.c_int64)]
     lib.gb_batch_get_events.argtypes = [vp, i32, vp, i32, i32p, vp]
+    cfgp = ctypes.POINTER(LaunchConfig)
+    lib.gb_batch_set_launch_config.argtypes = [vp, cfgp]
+    lib.gb_batch_get_launch_config.argtypes = [vp, cfgp]
+    lib.gb_batch_autotune.argtypes = [vp, ctypes.POINTER(StepOpts), cfgp, i32, i32p, cfgp, vp]
+    lib.gb_graph_capture.argtypes = [vp, ctypes.POINTER(StepOpts), ctypes.POINTER(vp)]
+    lib.gb_graph_launch.argtypes = [vp, vp]
+    lib.gb_graph_destroy.argtypes = [vp]
+    lib.gb_batch_ray_cast.argtypes = [vp, vp, i32, vp, vp]
+    lib.gb_batch_query_aabb.argtypes = [vp, vp, i32, i32p, i32, i32p, vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

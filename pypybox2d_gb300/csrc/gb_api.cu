@@ -138,7 +138,38 @@ struct gb_batch {
     int *d_ev_n = nullptr;
     SideStream side{};               // the solver's second stream (gb_launch.h)
     bool has_side = false;
+    gb_launch_config cfg{3, 128, GB_SOLVE_PIPE_BUFS, GB_SOLVE_BIG_BODIES, 0.0};   // launch_mode 0 steps
+    std::vector<gb_graph *> graphs;  // captured rollouts, disarmed when the batch is destroyed
+    char *d_query = nullptr;         // staging of query inputs and outputs, grown on demand
+    size_t query_bytes = 0;
 };
+
+// A captured rollout (gb_graph_capture).  `b` is null once its batch is gone.
+struct gb_graph {
+    gb_batch *b = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int n_steps = 0;
+};
+
+namespace {
+// launch mode and CTA width of a step call: launch_mode 0 takes the batch's
+// launch configuration
+void resolve_mapping(const gb_batch *b, const gb_step_opts *o, int *mode, int *threads) {
+    if (o->launch_mode == 0) *mode = b->cfg.launch_mode;
+    else *mode = (o->launch_mode == 2 || o->launch_mode == 3) ? o->launch_mode : 1;
+    *threads = o->block_threads > 0 ? o->block_threads : (o->launch_mode == 0 ? b->cfg.block_threads : 128);
+}
+// contact-event buffers, allocated by the first step that records events
+int ensure_event_buffers(gb_batch *b) {
+    if (!b->d_ev) {
+        CK(cudaMalloc((void **)&b->d_ev, sizeof(gb_event) * (3 * (size_t)b->ncap + 64 * (size_t)b->nw)));
+        CK(cudaMalloc((void **)&b->d_ev_n, sizeof(int) * b->nw));
+        b->bd.ev = b->bf.ev = b->d_ev;
+        b->bd.ev_n = b->bf.ev_n = b->d_ev_n;
+    }
+    return 0;
+}
+}  // namespace
 
 extern "C" {
 
@@ -345,6 +376,11 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
 
 int gb_batch_destroy(gb_batch *b) {
     if (!b) return 0;
+    for (gb_graph *g : b->graphs) {
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        g->exec = nullptr;
+        g->b = nullptr;
+    }
     cudaFree(b->arena);
     cudaFree(b->d_worlds);
     cudaFree(b->d_bstage);
@@ -355,6 +391,7 @@ int gb_batch_destroy(gb_batch *b) {
     }
     cudaFree(b->d_ev);
     cudaFree(b->d_ev_n);
+    cudaFree(b->d_query);
     if (b->has_side) {
         cudaEventDestroy(b->side.fork);
         cudaEventDestroy(b->side.join);
@@ -378,15 +415,11 @@ int gb_batch_step(gb_batch *b, const gb_step_opts *o, void *stream) {
     sp.profile = (o->record_order >> 1) & 1;
     sp.events = (o->record_order & GB_OPT_EVENTS) ? 1 : 0;
     sp.step_index = 0;
-    int mode = (o->launch_mode == 2 || o->launch_mode == 3) ? o->launch_mode : (o->launch_mode == 0 ? 3 : 1);
-    int threads = o->block_threads > 0 ? o->block_threads : (mode == 2 ? 128 : 128);
+    int mode = 0, threads = 0;
+    resolve_mapping(b, o, &mode, &threads);
     if (sp.events) {
-        if (!b->d_ev) {
-            CK(cudaMalloc((void **)&b->d_ev, sizeof(gb_event) * (3 * (size_t)b->ncap + 64 * (size_t)b->nw)));
-            CK(cudaMalloc((void **)&b->d_ev_n, sizeof(int) * b->nw));
-            b->bd.ev = b->bf.ev = b->d_ev;
-            b->bd.ev_n = b->bf.ev_n = b->d_ev_n;
-        }
+        int rc = ensure_event_buffers(b);
+        if (rc) return rc;
         CK(cudaMemsetAsync(b->d_ev_n, 0, sizeof(int) * b->nw, st));
     }
     if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
@@ -557,6 +590,319 @@ int gb_batch_counters(gb_batch *b, int64_t *c) {
     c[0] = b->counters[0];
     c[1] = (int64_t)b->arena_bytes;
     c[2] = b->counters[2];
+    return 0;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------
+// Launch configurations, the autotuner and captured rollouts.
+static_assert(sizeof(gb_launch_config) == GB_LAUNCH_CONFIG_BYTES, "gb_launch_config layout");
+namespace {
+StepParams params_of(const gb_step_opts *o) {
+    StepParams sp;
+    sp.dt = o->dt;
+    sp.inv_dt = o->dt > 0.0 ? 1.0 / o->dt : 0.0;
+    sp.dt_ratio = 0.0;
+    sp.vel_iters = o->vel_iters;
+    sp.pos_iters = o->pos_iters;
+    sp.record_order = o->record_order & 1;
+    sp.profile = (o->record_order >> 1) & 1;
+    sp.events = (o->record_order & GB_OPT_EVENTS) ? 1 : 0;
+    sp.step_index = 0;
+    return sp;
+}
+
+int launch_steps(gb_batch *b, const StepParams &sp, int n_steps, int mode, int threads, cudaStream_t st) {
+    const SideStream *side = b->has_side ? &b->side : nullptr;
+    return b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, n_steps, b->d_worlds, b->nw, mode, threads, st, nullptr, side)
+                                  : gb_launch_step<float>(b->bf, sp, n_steps, b->d_worlds, b->nw, mode, threads, st, nullptr, side);
+}
+
+bool has_grid_worlds(const gb_batch *b) { return (b->prec == GB_PREC_F64 ? b->bd.n_huge : b->bf.n_huge) > 0; }
+
+// Check a launch configuration against the batch and, with `apply`, make it
+// the batch's: the wide solver launch takes the worlds of big_bodies bodies
+// or more (the front of the size-sorted list), and each solver launch's
+// shared-memory body cache fits its largest world up to 2048 bodies.
+int apply_config(gb_batch *b, const gb_launch_config &c, bool apply) {
+    if (c.launch_mode < 1 || c.launch_mode > 3) return fail(GB_E_ARG, "launch_mode must be 1, 2 or 3");
+    if (c.block_threads < 32 || c.block_threads > 1024 || c.block_threads % 32)
+        return fail(GB_E_ARG, "block_threads must be a multiple of 32 from 32 to 1024");
+    if (c.pipe_bufs < 0 || c.pipe_bufs > GB_CFG_MAX_PIPE_BUFS) return fail(GB_E_ARG, "pipe_bufs must be 0 to 4");
+    if (c.big_bodies < 1) return fail(GB_E_ARG, "big_bodies must be positive");
+    if (c.launch_mode != 3 && has_grid_worlds(b))
+        return fail(GB_E_UNSUPPORTED, "worlds of 16384 bodies or more run only in the phased launch (mode 3)");
+    // worlds run as a cooperative grid (the front of the list) always count
+    // as big, so the per-world solver launches never take them
+    const int big_from = std::min(c.big_bodies, (int)GB_HUGE_BODIES);
+    int nbig = 0, max_big = 0, max_small = 0;
+    for (int i : b->launch_order) {
+        int n = b->hdr[i].nb;
+        if (n >= big_from) { ++nbig; max_big = std::max(max_big, n); }
+        else max_small = std::max(max_small, n);
+    }
+    const int cache_big = max_big <= 2048 ? max_big : 0, cache_small = max_small <= 2048 ? max_small : 0;
+    if (c.launch_mode == 3) {
+        int dev = 0, optin = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+        const int t_small = std::min(c.block_threads, 256);
+        auto smem = [&](int cache, int threads) -> size_t {
+            if (cache <= 0) return 0;
+            return b->prec == GB_PREC_F64 ? gb_solve_smem<double>(cache, threads, c.pipe_bufs)
+                                          : gb_solve_smem<float>(cache, threads, c.pipe_bufs);
+        };
+        const size_t need = std::max(smem(cache_big, GB_SOLVE_BIG_THREADS), smem(cache_small, t_small));
+        if (need > (size_t)optin)
+            return fail(GB_E_ARG, "configuration needs " + std::to_string(need) + " bytes of shared memory per CTA; the device allows " +
+                                      std::to_string(optin));
+    }
+    if (!apply) return 0;
+    for (Batch<double> *B : {&b->bd}) { B->n_big = nbig; B->cache_big = cache_big; B->cache_small = cache_small; B->pipe_bufs = c.pipe_bufs; }
+    for (Batch<float> *B : {&b->bf}) { B->n_big = nbig; B->cache_big = cache_big; B->cache_small = cache_small; B->pipe_bufs = c.pipe_bufs; }
+    b->cfg = c;
+    return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int gb_batch_set_launch_config(gb_batch *b, const gb_launch_config *cfg) {
+    if (!b || !cfg) return fail(GB_E_ARG, "batch or cfg is NULL");
+    gb_launch_config c = *cfg;
+    c.ms_per_step = 0.0;
+    return apply_config(b, c, true);
+}
+
+int gb_batch_get_launch_config(gb_batch *b, gb_launch_config *cfg) {
+    if (!b || !cfg) return fail(GB_E_ARG, "batch or cfg is NULL");
+    *cfg = b->cfg;
+    return 0;
+}
+
+int gb_batch_autotune(gb_batch *b, const gb_step_opts *o, gb_launch_config *trials, int32_t capacity, int32_t *n_out,
+                      gb_launch_config *best, void *stream) {
+    if (!b || !o) return fail(GB_E_ARG, "batch or opts is NULL");
+    if (o->n_steps < 1 || o->vel_iters < 0 || o->pos_iters < 0)
+        return fail(GB_E_ARG, "autotune needs n_steps >= 1 and non-negative iterations");
+    if (o->record_order != 0) return fail(GB_E_ARG, "autotune steps record nothing: record_order must be 0");
+    if (capacity < 0 || (capacity > 0 && !trials)) return fail(GB_E_ARG, "trials is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    const StepParams sp = params_of(o);
+    const gb_launch_config start = b->cfg;
+    char *snap = nullptr;
+    CK(cudaMalloc((void **)&snap, b->arena_bytes));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        cudaFree(snap);
+        return fail(GB_E_CUDA, "cudaEventCreate");
+    }
+    int err = 0;
+    cudaError_t ce = cudaMemcpyAsync(snap, b->arena, b->arena_bytes, cudaMemcpyDeviceToDevice, st);
+    if (ce != cudaSuccess) err = cuda_fail(ce, "autotune: copy of the arena");
+    std::vector<gb_launch_config> log;
+    gb_launch_config best_c = start;
+    best_c.ms_per_step = -1.0;
+    // one trial: from the saved state, an untimed run (first launches load
+    // their kernels), then the timed run from the saved state again
+    auto trial = [&](gb_launch_config c) {
+        c.ms_per_step = -1.0;
+        if (err) return;
+        if (apply_config(b, c, true) == 0) {
+            float ms = 0.0f;
+            int rc = 0;
+            for (int pass = 0; pass < 2 && rc == 0; ++pass) {
+                rc = (int)cudaMemcpyAsync(b->arena, snap, b->arena_bytes, cudaMemcpyDeviceToDevice, st);
+                if (rc == 0) rc = (int)cudaEventRecord(e0, st);
+                if (rc == 0) rc = launch_steps(b, sp, o->n_steps, c.launch_mode, c.block_threads, st);
+                if (rc == 0) rc = (int)cudaEventRecord(e1, st);
+                if (rc == 0) rc = (int)cudaEventSynchronize(e1);
+                if (rc == 0) rc = (int)cudaEventElapsedTime(&ms, e0, e1);
+            }
+            if (rc != 0) err = cuda_fail((cudaError_t)rc, "autotune trial");
+            else c.ms_per_step = (double)ms / o->n_steps;
+        }
+        log.push_back(c);
+        if (c.ms_per_step >= 0.0 && (best_c.ms_per_step < 0.0 || c.ms_per_step < best_c.ms_per_step)) best_c = c;
+    };
+    // stage 1: world-to-thread mapping
+    {
+        std::vector<std::pair<int, int>> maps = {{3, 32}, {3, 64}, {3, 128}};
+        if (!has_grid_worlds(b)) {
+            maps.push_back({1, 128}); maps.push_back({1, 256});
+            maps.push_back({2, 64}); maps.push_back({2, 128});
+        }
+        for (auto &m : maps) {
+            gb_launch_config c = start;
+            c.launch_mode = m.first;
+            c.block_threads = m.second;
+            trial(c);
+        }
+    }
+    // stages 2 and 3 (phased launch): wide-launch threshold, then chunk buffers
+    if (!err && best_c.ms_per_step >= 0.0 && best_c.launch_mode == 3) {
+        const gb_launch_config base = best_c;
+        for (int bb : {256, 512, 1024, 2048, 1 << 30})
+            if (bb != base.big_bodies) { gb_launch_config c = base; c.big_bodies = bb; trial(c); }
+    }
+    if (!err && best_c.ms_per_step >= 0.0 && best_c.launch_mode == 3) {
+        const gb_launch_config base = best_c;
+        for (int pb = 0; pb <= GB_CFG_MAX_PIPE_BUFS; ++pb)
+            if (pb != base.pipe_bufs) { gb_launch_config c = base; c.pipe_bufs = pb; trial(c); }
+    }
+    // the best configuration stays; the state goes back to the saved one
+    const bool found = !err && best_c.ms_per_step >= 0.0;
+    apply_config(b, found ? best_c : start, true);
+    if (found) b->cfg.ms_per_step = best_c.ms_per_step;
+    ce = cudaMemcpyAsync(b->arena, snap, b->arena_bytes, cudaMemcpyDeviceToDevice, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(snap);
+    if (err) return err;
+    if (ce != cudaSuccess) return cuda_fail(ce, "autotune: restoring the arena");
+    if (!found) return fail(GB_E_ARG, "autotune: no candidate configuration could run on this batch");
+    if (n_out) *n_out = (int32_t)log.size();
+    for (int k = 0; k < capacity && k < (int)log.size(); ++k) trials[k] = log[k];
+    if (best) *best = b->cfg;
+    return 0;
+}
+
+int gb_graph_capture(gb_batch *b, const gb_step_opts *o, gb_graph **out) {
+    if (!b || !o || !out) return fail(GB_E_ARG, "batch, opts or out is NULL");
+    *out = nullptr;
+    if (o->n_steps < 1 || o->vel_iters < 0 || o->pos_iters < 0)
+        return fail(GB_E_ARG, "graph capture needs n_steps >= 1 and non-negative iterations");
+    if (o->record_order & GB_OPT_KERNEL_TIMES) return fail(GB_E_UNSUPPORTED, "per-launch timing waits on the host and is not captured");
+    int mode = 0, threads = 0;
+    resolve_mapping(b, o, &mode, &threads);
+    if (mode != 3) return fail(GB_E_UNSUPPORTED, "only the phased launch (mode 3) is captured");
+    if (has_grid_worlds(b)) return fail(GB_E_UNSUPPORTED, "worlds of 16384 bodies or more (cooperative launches) are not captured");
+    if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
+    const StepParams sp = params_of(o);
+    if (sp.events) {
+        int rc = ensure_event_buffers(b);
+        if (rc) return rc;
+    }
+    cudaStream_t cs = nullptr;
+    CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) { cudaStreamDestroy(cs); return cuda_fail(e, "cudaStreamBeginCapture"); }
+    int rc = 0;
+    if (sp.events) rc = (int)cudaMemsetAsync(b->d_ev_n, 0, sizeof(int) * b->nw, cs);
+    if (rc == 0) rc = launch_steps(b, sp, o->n_steps, mode, threads, cs);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (rc != 0 || e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        return cuda_fail(rc != 0 ? (cudaError_t)rc : (e != cudaSuccess ? e : cudaErrorStreamCaptureInvalidated), "graph capture");
+    }
+    cudaGraphExec_t ex = nullptr;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    gb_graph *gr = new gb_graph;
+    gr->b = b;
+    gr->exec = ex;
+    gr->n_steps = o->n_steps;
+    b->graphs.push_back(gr);
+    *out = gr;
+    return 0;
+}
+
+int gb_graph_launch(gb_graph *g, void *stream) {
+    if (!g) return fail(GB_E_ARG, "graph is NULL");
+    if (!g->b || !g->exec) return fail(GB_E_ARG, "the graph's batch was destroyed");
+    CK(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+    g->b->counters[0] += 1;
+    g->b->counters[2] += g->n_steps;
+    return 0;
+}
+
+}  // extern "C"
+
+namespace {
+// device staging of at least `bytes` for the query entry points
+int query_staging(gb_batch *b, size_t bytes, cudaStream_t st) {
+    if (bytes <= b->query_bytes) return 0;
+    CK(cudaStreamSynchronize(st));
+    cudaFree(b->d_query);
+    b->d_query = nullptr;
+    b->query_bytes = 0;
+    bytes = std::max(bytes, (size_t)1 << 20);
+    CK(cudaMalloc((void **)&b->d_query, bytes));
+    b->query_bytes = bytes;
+    return 0;
+}
+size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+}  // namespace
+
+extern "C" {
+
+int gb_batch_ray_cast(gb_batch *b, const gb_ray *rays, int32_t n, gb_ray_hit *hits, void *stream) {
+    if (!b) return fail(GB_E_ARG, "batch is NULL");
+    if (n < 0) return fail(GB_E_ARG, "negative ray count");
+    if (n == 0) return 0;
+    if (!rays || !hits) return fail(GB_E_ARG, "rays or hits is NULL");
+    for (int i = 0; i < n; ++i) {
+        const gb_ray &r = rays[i];
+        if (r.world < 0 || r.world >= b->nw) return fail(GB_E_ARG, "ray " + std::to_string(i) + ": world out of range");
+        const double dx = r.p2x - r.p1x, dy = r.p2y - r.p1y;
+        if (!(dx * dx + dy * dy > 0.0)) return fail(GB_E_ARG, "ray " + std::to_string(i) + ": p2 - p1 has no length");
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t in_b = up256(sizeof(gb_ray) * (size_t)n), out_b = sizeof(gb_ray_hit) * (size_t)n;
+    int rc = query_staging(b, in_b + out_b, st);
+    if (rc) return rc;
+    gb_ray *d_rays = reinterpret_cast<gb_ray *>(b->d_query);
+    gb_ray_hit *d_hits = reinterpret_cast<gb_ray_hit *>(b->d_query + in_b);
+    CK(cudaMemcpyAsync(d_rays, rays, sizeof(gb_ray) * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (b->prec == GB_PREC_F64) gb_launch_ray_cast<double>(b->bd, d_rays, n, d_hits, st);
+    else gb_launch_ray_cast<float>(b->bf, d_rays, n, d_hits, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(hits, d_hits, out_b, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_query_aabb(gb_batch *b, const gb_aabb_query *qs, int32_t n, int32_t *fixtures, int32_t cap, int32_t *counts,
+                        void *stream) {
+    if (!b) return fail(GB_E_ARG, "batch is NULL");
+    if (n < 0 || cap < 0) return fail(GB_E_ARG, "negative query count or capacity");
+    if (n == 0) return 0;
+    if (!qs || !counts || (cap > 0 && !fixtures)) return fail(GB_E_ARG, "queries, fixtures or counts is NULL");
+    for (int i = 0; i < n; ++i)
+        if (qs[i].world < 0 || qs[i].world >= b->nw) return fail(GB_E_ARG, "query " + std::to_string(i) + ": world out of range");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t in_b = up256(sizeof(gb_aabb_query) * (size_t)n), cnt_b = up256(sizeof(int) * (size_t)n);
+    const size_t out_b = sizeof(int) * (size_t)n * (size_t)cap;
+    int rc = query_staging(b, in_b + cnt_b + out_b, st);
+    if (rc) return rc;
+    gb_aabb_query *d_q = reinterpret_cast<gb_aabb_query *>(b->d_query);
+    int *d_cnt = reinterpret_cast<int *>(b->d_query + in_b);
+    int *d_out = reinterpret_cast<int *>(b->d_query + in_b + cnt_b);
+    CK(cudaMemcpyAsync(d_q, qs, sizeof(gb_aabb_query) * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (b->prec == GB_PREC_F64) gb_launch_query_aabb<double>(b->bd, d_q, n, d_out, cap, d_cnt, st);
+    else gb_launch_query_aabb<float>(b->bf, d_q, n, d_out, cap, d_cnt, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(counts, d_cnt, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    if (out_b) CK(cudaMemcpyAsync(fixtures, d_out, out_b, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_graph_destroy(gb_graph *g) {
+    if (!g) return 0;
+    if (g->b) {
+        auto &v = g->b->graphs;
+        v.erase(std::remove(v.begin(), v.end(), g), v.end());
+    }
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    delete g;
     return 0;
 }
 

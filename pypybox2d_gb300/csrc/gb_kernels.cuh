@@ -7,6 +7,7 @@
 #include <type_traits>
 #include "gb_phases.cuh"
 #include "gb_launch.h"
+#include "gb_query.cuh"
 
 namespace {
 
@@ -266,4 +267,15 @@ template <> void gb_launch_pack_contacts<GB_REAL>(const Batch<GB_REAL> &B, gb_co
 template <> void gb_launch_refresh_toi_cand<GB_REAL>(const Batch<GB_REAL> &B, cudaStream_t st) {
     const int n = B.n_slots;
     if (n > 0) k_refresh_toi_cand<<<(n + 255) / 256, 256, 0, st>>>(B, n);
+}
+static_assert(GB_CFG_MAX_PIPE_BUFS <= GB_MAX_PIPE_BUFS, "launch configurations may ask for more chunk buffers than the solver has barriers");
+template <> size_t gb_solve_smem<GB_REAL>(int cache_bodies, int threads, int nbuf) {
+    return solve_smem_bytes<GB_REAL>(cache_bodies, threads, nbuf);
+}
+template <> void gb_launch_ray_cast<GB_REAL>(const Batch<GB_REAL> &B, const gb_ray *rays, int n, gb_ray_hit *hits, cudaStream_t st) {
+    if (n > 0) k_ray_cast<GB_REAL><<<(n + 7) / 8, 256, 0, st>>>(B, rays, n, hits);
+}
+template <> void gb_launch_query_aabb<GB_REAL>(const Batch<GB_REAL> &B, const gb_aabb_query *qs, int n, int *out, int cap,
+                                               int *counts, cudaStream_t st) {
+    if (n > 0) k_query_aabb<GB_REAL><<<(n + 7) / 8, 256, 0, st>>>(B, qs, n, out, cap, counts);
 }

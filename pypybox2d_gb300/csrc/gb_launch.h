@@ -26,6 +26,14 @@ template <class R> void gb_launch_pack_bodies(const Batch<R> &B, gb_body *d, int
 template <class R> void gb_launch_unpack_fixtures(const Batch<R> &B, const gb_fixture *d, int n, cudaStream_t st);
 template <class R> void gb_launch_unpack_contacts(const Batch<R> &B, const gb_contact *d, const int *slots, int n, cudaStream_t st);
 template <class R> void gb_launch_pack_contacts(const Batch<R> &B, gb_contact *d, int base, int n, cudaStream_t st);
+// shared memory of the phased solver launch: body cache of `cache_bodies`
+// bodies plus `nbuf` constraint-chunk buffers for `threads` threads
+template <class R> size_t gb_solve_smem(int cache_bodies, int threads, int nbuf);
+#define GB_CFG_MAX_PIPE_BUFS 4
+// world queries (gb_query.cuh): device arrays in and out
+template <class R> void gb_launch_ray_cast(const Batch<R> &B, const gb_ray *rays, int n, gb_ray_hit *hits, cudaStream_t st);
+template <class R> void gb_launch_query_aabb(const Batch<R> &B, const gb_aabb_query *qs, int n, int *out, int cap, int *counts,
+                                             cudaStream_t st);
 // recompute the device-only TOI candidate flag of every contact (after an upload)
 template <class R> void gb_launch_refresh_toi_cand(const Batch<R> &B, cudaStream_t st);
 
@@ -44,4 +52,10 @@ template <> void gb_launch_unpack_contacts<float>(const Batch<float> &, const gb
 template <> void gb_launch_pack_contacts<double>(const Batch<double> &, gb_contact *, int, int, cudaStream_t);
 template <> void gb_launch_pack_contacts<float>(const Batch<float> &, gb_contact *, int, int, cudaStream_t);
 template <> void gb_launch_refresh_toi_cand<double>(const Batch<double> &, cudaStream_t);
+template <> size_t gb_solve_smem<double>(int, int, int);
+template <> size_t gb_solve_smem<float>(int, int, int);
 template <> void gb_launch_refresh_toi_cand<float>(const Batch<float> &, cudaStream_t);
+template <> void gb_launch_ray_cast<double>(const Batch<double> &, const gb_ray *, int, gb_ray_hit *, cudaStream_t);
+template <> void gb_launch_ray_cast<float>(const Batch<float> &, const gb_ray *, int, gb_ray_hit *, cudaStream_t);
+template <> void gb_launch_query_aabb<double>(const Batch<double> &, const gb_aabb_query *, int, int *, int, int *, cudaStream_t);
+template <> void gb_launch_query_aabb<float>(const Batch<float> &, const gb_aabb_query *, int, int *, int, int *, cudaStream_t);

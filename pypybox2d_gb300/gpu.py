@@ -54,6 +54,61 @@ class GpuBatch:
         o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, 0)
         abi.check(self.lib.gb_batch_step_static_scratch(self.h, ctypes.byref(o), ctypes.c_void_p(stream or 0)))
 
+    def launch_config(self) -> dict:
+        """The configuration steps with launch_mode=0 use (gb_batch_get_launch_config)."""
+        c = abi.LaunchConfig()
+        abi.check(self.lib.gb_batch_get_launch_config(self.h, ctypes.byref(c)))
+        return c.as_dict()
+
+    def set_launch_config(self, launch_mode: int = 3, block_threads: int = 128, pipe_bufs: int = 2,
+                          big_bodies: int = 512) -> None:
+        """Pin a launch configuration (for example one an earlier autotune chose)."""
+        c = abi.LaunchConfig(launch_mode, block_threads, pipe_bufs, big_bodies, 0.0)
+        abi.check(self.lib.gb_batch_set_launch_config(self.h, ctypes.byref(c)))
+
+    def autotune(self, dt: float, vel_iters: int = 8, pos_iters: int = 3, steps_per_trial: int = 3,
+                 stream: int | None = None) -> tuple[dict, list[dict]]:
+        """Time candidate launch configurations on this batch's next
+        ``steps_per_trial`` steps (gb_batch_autotune) and keep the fastest.
+        The batch state is unchanged afterwards.  Returns (best, trials)."""
+        o = abi.StepOpts(dt, vel_iters, pos_iters, steps_per_trial, 0, 0, 0)
+        cap = 32
+        trials = (abi.LaunchConfig * cap)()
+        n = ctypes.c_int32()
+        best = abi.LaunchConfig()
+        abi.check(self.lib.gb_batch_autotune(self.h, ctypes.byref(o), trials, cap, ctypes.byref(n), ctypes.byref(best),
+                                             ctypes.c_void_p(stream or 0)))
+        return best.as_dict(), [trials[k].as_dict() for k in range(min(n.value, cap))]
+
+    def capture(self, dt: float, vel_iters: int = 8, pos_iters: int = 3, n_steps: int = 1, launch_mode: int = 3,
+                block_threads: int = 0, record_order: bool = False, events: bool = False) -> "StepGraph":
+        """Capture ``n_steps`` phased steps as one CUDA graph (gb_graph_capture)."""
+        flags = (1 if record_order else 0) | (abi.OPT_EVENTS if events else 0)
+        o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, flags)
+        h = ctypes.c_void_p()
+        abi.check(self.lib.gb_graph_capture(self.h, ctypes.byref(o), ctypes.byref(h)))
+        return StepGraph(self, h, n_steps)
+
+    def ray_cast(self, rays: np.ndarray, stream: int | None = None) -> np.ndarray:
+        """Closest hit of each ray (``abi.RAY`` records) -> ``abi.RAY_HIT``
+        records (gb_batch_ray_cast)."""
+        r = np.ascontiguousarray(rays, dtype=abi.RAY)
+        out = np.zeros(len(r), dtype=abi.RAY_HIT)
+        abi.check(self.lib.gb_batch_ray_cast(self.h, r.ctypes.data, len(r), out.ctypes.data, ctypes.c_void_p(stream or 0)))
+        return out
+
+    def query_aabb(self, boxes: np.ndarray, max_per_query: int = 64,
+                   stream: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+        """Fixtures whose fat AABB overlaps each box (``abi.AABB_QUERY``
+        records): (fixtures[n, max_per_query], counts[n]) (gb_batch_query_aabb)."""
+        q = np.ascontiguousarray(boxes, dtype=abi.AABB_QUERY)
+        out = np.full((len(q), max_per_query), -1, dtype=np.int32)
+        counts = np.zeros(len(q), dtype=np.int32)
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        abi.check(self.lib.gb_batch_query_aabb(self.h, q.ctypes.data, len(q), out.ctypes.data_as(i32p), max_per_query,
+                                               counts.ctypes.data_as(i32p), ctypes.c_void_p(stream or 0)))
+        return out, counts
+
     def bodies(self, stream: int | None = None) -> np.ndarray:
         out = np.zeros(self.n_bodies, dtype=abi.BODY)
         abi.check(self.lib.gb_batch_get_bodies(self.h, out.ctypes.data, self.n_bodies, ctypes.c_void_p(stream or 0)))
@@ -128,3 +183,25 @@ class GpuBatch:
         out = np.zeros(self.n_worlds, dtype=np.uint32)
         abi.check(self.lib.gb_batch_status(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), None))
         return out
+
+
+class StepGraph:
+    """A captured multi-step rollout of a GpuBatch; ``launch()`` replays it
+    on a stream and advances the batch by ``n_steps`` steps."""
+
+    def __init__(self, batch: GpuBatch, handle: ctypes.c_void_p, n_steps: int):
+        self.batch, self.h, self.n_steps = batch, handle, n_steps
+
+    def launch(self, stream: int | None = None) -> None:
+        abi.check(self.batch.lib.gb_graph_launch(self.h, ctypes.c_void_p(stream or 0)))
+
+    def close(self) -> None:
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.batch.lib.gb_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

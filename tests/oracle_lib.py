@@ -161,3 +161,29 @@ class OracleBatch:
 
     def close(self):
         pass
+
+
+def ray_cast_records(B, F, rays, libm: bool = True) -> np.ndarray:
+    """The restatement's closest hits (or_ray_cast_records) of one world."""
+    lib = load(libm)
+    lib.or_ray_cast_records.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_void_p]
+    B = np.ascontiguousarray(B, dtype=abi.BODY)
+    F = np.ascontiguousarray(F, dtype=abi.FIXTURE)
+    r = np.ascontiguousarray(rays, dtype=abi.RAY)
+    out = np.zeros(len(r), dtype=abi.RAY_HIT)
+    lib.or_ray_cast_records(B.ctypes.data, F.ctypes.data, len(F), r.ctypes.data, len(r), out.ctypes.data)
+    return out
+
+
+def query_aabb_records(F, boxes, cap: int, libm: bool = True) -> tuple[np.ndarray, np.ndarray]:
+    """The restatement's overlapping fixtures (or_query_aabb_records) of one world."""
+    lib = load(libm)
+    lib.or_query_aabb_records.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_int, ctypes.c_void_p]
+    F = np.ascontiguousarray(F, dtype=abi.FIXTURE)
+    q = np.ascontiguousarray(boxes, dtype=abi.AABB_QUERY)
+    out = np.full((len(q), cap), -1, dtype=np.int32)
+    counts = np.zeros(len(q), dtype=np.int32)
+    lib.or_query_aabb_records(F.ctypes.data, len(F), q.ctypes.data, len(q), out.ctypes.data, cap, counts.ctypes.data)
+    return out, counts

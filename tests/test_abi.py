@@ -60,3 +60,9 @@ def test_bad_scene_is_rejected_before_any_device_call(lib):
     h = ctypes.c_void_p()
     assert lib.gb_batch_create(ctypes.byref(s), 0, ctypes.byref(h)) == -1
     assert b"outside" in lib.gb_last_error()
+
+
+def test_launch_config_layout():
+    text = open(os.path.join(REPO, "include", "gb2d.h")).read()
+    m = re.search(r"#define GB_LAUNCH_CONFIG_BYTES (\d+)", text)
+    assert m and int(m.group(1)) == ctypes.sizeof(abi.LaunchConfig) == abi.LAUNCH_CONFIG_BYTES
