@@ -329,6 +329,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip cpu baseline, plain path and error legs")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch autotuner (use --mode / --threads)")
     ap.add_argument("--tune-steps", type=int, default=3, help="timed steps per autotuner trial")
+    ap.add_argument("--launch-config", default="", help="mode,threads,pipe_bufs,big_bodies: pin this launch "
+                                                         "configuration instead of tuning")
     ap.add_argument("--graph-steps", type=int, default=50, help="steps per captured CUDA graph in the timed region "
                                                                 "(0 = one gb_batch_step call)")
     args = ap.parse_args()
@@ -370,7 +372,10 @@ def main():
     # launch autotuner: trials from the warmed-up state, which it restores
     mode, threads = args.mode, args.threads
     tune = None
-    if not args.no_tune:
+    if args.launch_config:
+        batch.set_launch_config(*[int(x) for x in args.launch_config.split(",")])
+        mode, threads = 0, 0
+    elif not args.no_tune:
         import time
         t0 = time.time()
         best, trials = batch.autotune(DT, VI, PI, steps_per_trial=args.tune_steps, stream=sh)
@@ -380,8 +385,9 @@ def main():
                 "table": [[t["launch_mode"], t["block_threads"], t["pipe_bufs"], t["big_bodies"],
                            round(t["ms_per_step"], 3)] for t in trials],
                 "columns": ["launch_mode", "block_threads", "pipe_bufs", "big_bodies", "ms_per_step"]}
-    cfg = batch.launch_config() if tune else {"launch_mode": args.mode, "block_threads": args.threads,
-                                              "pipe_bufs": 2, "big_bodies": 512}
+    cfg = batch.launch_config() if (tune or args.launch_config) else {"launch_mode": args.mode,
+                                                                      "block_threads": args.threads,
+                                                                      "pipe_bufs": 2, "big_bodies": 512}
     eff_mode = cfg["launch_mode"]
 
     # the timed steps: captured rollouts of graph_steps phased steps replayed
@@ -421,7 +427,7 @@ def main():
     total_dyn = float(dyn.sum()) * ws
     value = total_dyn * steps / t
 
-    # roofline of the whole step: survey byte model per world-step, live counts
+    # roofline of the whole step: algorithmic bytes per world-step from live counts
     bytes_step = algorithmic_bytes_per_step(len(B), F, float(np.sum(counts)))
     achieved = bytes_step * steps / t / 1e9
     peak, peak_kind = _peaks()
@@ -491,6 +497,7 @@ def main():
     out = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t / steps, "higher_is_better": True, "scaling": "weak",
+        "world_steps_per_s": float(n_worlds) * ws * steps / t,
         "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
         "config": {"workload": desc, "worlds_per_gpu": n_worlds, "dynamic_bodies_per_gpu": int(dyn.sum()),
                    "bodies_per_world": {"min": int(dyn.min()), "mean": float(dyn.mean()), "max": int(dyn.max())},

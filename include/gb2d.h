@@ -357,6 +357,12 @@ typedef struct gb_aabb_query {
  * and out; the call waits for its results.  Replaces World.ray_cast with a
  * closest-hit callback, for many rays at once. */
 int gb_batch_ray_cast(gb_batch *batch, const gb_ray *rays, int32_t n_rays, gb_ray_hit *hits, void *cuda_stream);
+/* Every hit of every ray: what the generator form of World.ray_cast yields
+ * when each fraction is left at 1 (world.py:387-440), in fixture order (the
+ * reference's come in tree order).  Ray q's first max_per_ray hits go to
+ * hits[q * max_per_ray ...], counts[q] is how many there are in all. */
+int gb_batch_ray_cast_all(gb_batch *batch, const gb_ray *rays, int32_t n_rays, gb_ray_hit *hits, int32_t max_per_ray,
+                          int32_t *counts, void *cuda_stream);
 /* Fixtures whose fat AABB overlaps each query box (World.query_aabb,
  * world.py:371-385; DynamicTree.query, dynamictree.py:190-207), in fixture
  * order: query q's first max_per_query fixtures go to

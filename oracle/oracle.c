@@ -1303,6 +1303,63 @@ static int or_ray_edge(const gb_fixture *f, xform xf, v2 p1, v2 p2, v2 *normal, 
     return 1;
 }
 
+/* DynamicTree.ray_cast's segment tests (dynamictree.py:222-250) at
+ * max_fraction 1, then the fixture's shape ray cast */
+typedef struct { v2 p1, p2, v, abs_v; double slx, sly, shx, shy; } or_seg;
+static or_seg or_ray_seg(const gb_ray *ray) {
+    or_seg s;
+    s.p1 = V(ray->p1x, ray->p1y);
+    s.p2 = V(ray->p2x, ray->p2y);
+    v2 r = vnormalized(vsub(s.p2, s.p1));
+    s.v = vcross_sv(1.0, r);
+    s.abs_v = V(fabs(s.v.x), fabs(s.v.y));
+    v2 t = vadd(s.p1, vscale(1.0, vsub(s.p2, s.p1)));
+    s.slx = pymin(s.p1.x, t.x); s.sly = pymin(s.p1.y, t.y); s.shx = pymax(s.p1.x, t.x); s.shy = pymax(s.p1.y, t.y);
+    return s;
+}
+static int or_ray_fixture(const gb_body *bodies, const gb_fixture *f, const or_seg *s, v2 *nrm, double *fr) {
+    const double *a = f->aabb;
+    if (!or_box_overlap(a, s->slx, s->sly, s->shx, s->shy)) return 0;
+    v2 c = V(0.5 * (a[2] + a[0]), 0.5 * (a[3] + a[1]));
+    v2 h = V(0.5 * (a[2] - a[0]), 0.5 * (a[3] - a[1]));
+    double separation = fabs(vdot(s->v, vsub(s->p1, c))) - vdot(s->abs_v, h);
+    if (separation > 0.0) return 0;
+    const gb_body *b = &bodies[f->body];
+    xform xf;
+    xf.p = V(b->px, b->py);
+    xf.q.c = b->qc;
+    xf.q.s = b->qs;
+    if (f->shape_type == GB_SHAPE_CIRCLE) return or_ray_circle(f, xf, s->p1, s->p2, nrm, fr);
+    if (f->shape_type == GB_SHAPE_POLYGON) return or_ray_polygon(f, xf, s->p1, s->p2, nrm, fr);
+    if (f->shape_type == GB_SHAPE_EDGE) return or_ray_edge(f, xf, s->p1, s->p2, nrm, fr);
+    return 0;
+}
+static gb_ray_hit or_make_hit(const or_seg *s, int k, v2 n, double fr) {
+    gb_ray_hit o;
+    memset(&o, 0, sizeof(o));
+    v2 pt = vadd(vscale(1.0 - fr, s->p1), vscale(fr, s->p2));   /* world.py:431 */
+    o.fixture = k; o.px = pt.x; o.py = pt.y; o.nx = n.x; o.ny = n.y; o.fraction = fr;
+    return o;
+}
+
+/* every hit of each ray, in fixture order: the generator form of
+ * World.ray_cast with each fraction left at 1 */
+void or_ray_cast_all_records(const gb_body *bodies, const gb_fixture *fixtures, int nf, const gb_ray *rays, int n,
+                             gb_ray_hit *hits, int cap, int32_t *counts) {
+    for (int q = 0; q < n; ++q) {
+        or_seg s = or_ray_seg(&rays[q]);
+        int found = 0;
+        for (int k = 0; k < nf; ++k) {
+            v2 nrm;
+            double fr = 0.0;
+            if (!or_ray_fixture(bodies, &fixtures[k], &s, &nrm, &fr)) continue;
+            if (found < cap) hits[(size_t)q * cap + found] = or_make_hit(&s, k, nrm, fr);
+            ++found;
+        }
+        counts[q] = found;
+    }
+}
+
 void or_ray_cast_records(const gb_body *bodies, const gb_fixture *fixtures, int nf, const gb_ray *rays, int n,
                          gb_ray_hit *hits) {
     for (int q = 0; q < n; ++q) {

@@ -59,6 +59,8 @@ int or_batch_get_bodies(const or_batch *b, int world, gb_body *out);
  * world fields are not read). */
 void or_ray_cast_records(const gb_body *bodies, const gb_fixture *fixtures, int nf, const gb_ray *rays, int n,
                          gb_ray_hit *hits);
+void or_ray_cast_all_records(const gb_body *bodies, const gb_fixture *fixtures, int nf, const gb_ray *rays, int n,
+                             gb_ray_hit *hits, int cap, int32_t *counts);
 void or_query_aabb_records(const gb_fixture *fixtures, int nf, const gb_aabb_query *qs, int n, int32_t *out, int cap,
                            int32_t *counts);
 

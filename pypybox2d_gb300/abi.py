@@ -173,7 +173,7 @@ EXPORTED = (
     "gb_batch_step_static_scratch", "gb_batch_kernel_times", "gb_batch_get_events",
     "gb_batch_set_launch_config", "gb_batch_get_launch_config", "gb_batch_autotune",
     "gb_graph_capture", "gb_graph_launch", "gb_graph_destroy",
-    "gb_batch_ray_cast", "gb_batch_query_aabb",
+    "gb_batch_ray_cast", "gb_batch_ray_cast_all", "gb_batch_query_aabb",
 )
 
 #: gb_step_opts.record_order bit that records contact events
@@ -241,6 +241,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_graph_destroy.argtypes = [vp]
     lib.gb_batch_ray_cast.argtypes = [vp, vp, i32, vp, vp]
     lib.gb_batch_query_aabb.argtypes = [vp, vp, i32, i32p, i32, i32p, vp]
+    lib.gb_batch_ray_cast_all.argtypes = [vp, vp, i32, vp, i32, i32p, vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

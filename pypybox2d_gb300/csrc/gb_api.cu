@@ -839,6 +839,16 @@ int query_staging(gb_batch *b, size_t bytes, cudaStream_t st) {
     return 0;
 }
 size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+// rays name a world of the batch and have a length (dynamictree.py:222-224 raises otherwise)
+int check_rays(const gb_batch *b, const gb_ray *rays, int n) {
+    for (int i = 0; i < n; ++i) {
+        const gb_ray &r = rays[i];
+        if (r.world < 0 || r.world >= b->nw) return fail(GB_E_ARG, "ray " + std::to_string(i) + ": world out of range");
+        const double dx = r.p2x - r.p1x, dy = r.p2y - r.p1y;
+        if (!(dx * dx + dy * dy > 0.0)) return fail(GB_E_ARG, "ray " + std::to_string(i) + ": p2 - p1 has no length");
+    }
+    return 0;
+}
 }  // namespace
 
 extern "C" {
@@ -848,15 +858,11 @@ int gb_batch_ray_cast(gb_batch *b, const gb_ray *rays, int32_t n, gb_ray_hit *hi
     if (n < 0) return fail(GB_E_ARG, "negative ray count");
     if (n == 0) return 0;
     if (!rays || !hits) return fail(GB_E_ARG, "rays or hits is NULL");
-    for (int i = 0; i < n; ++i) {
-        const gb_ray &r = rays[i];
-        if (r.world < 0 || r.world >= b->nw) return fail(GB_E_ARG, "ray " + std::to_string(i) + ": world out of range");
-        const double dx = r.p2x - r.p1x, dy = r.p2y - r.p1y;
-        if (!(dx * dx + dy * dy > 0.0)) return fail(GB_E_ARG, "ray " + std::to_string(i) + ": p2 - p1 has no length");
-    }
+    int rc = check_rays(b, rays, n);
+    if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const size_t in_b = up256(sizeof(gb_ray) * (size_t)n), out_b = sizeof(gb_ray_hit) * (size_t)n;
-    int rc = query_staging(b, in_b + out_b, st);
+    rc = query_staging(b, in_b + out_b, st);
     if (rc) return rc;
     gb_ray *d_rays = reinterpret_cast<gb_ray *>(b->d_query);
     gb_ray_hit *d_hits = reinterpret_cast<gb_ray_hit *>(b->d_query + in_b);
@@ -865,6 +871,32 @@ int gb_batch_ray_cast(gb_batch *b, const gb_ray *rays, int32_t n, gb_ray_hit *hi
     else gb_launch_ray_cast<float>(b->bf, d_rays, n, d_hits, st);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(hits, d_hits, out_b, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_ray_cast_all(gb_batch *b, const gb_ray *rays, int32_t n, gb_ray_hit *hits, int32_t cap, int32_t *counts,
+                          void *stream) {
+    if (!b) return fail(GB_E_ARG, "batch is NULL");
+    if (n < 0 || cap < 0) return fail(GB_E_ARG, "negative ray count or capacity");
+    if (n == 0) return 0;
+    if (!rays || !counts || (cap > 0 && !hits)) return fail(GB_E_ARG, "rays, hits or counts is NULL");
+    int rc = check_rays(b, rays, n);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t in_b = up256(sizeof(gb_ray) * (size_t)n), cnt_b = up256(sizeof(int) * (size_t)n);
+    const size_t out_b = sizeof(gb_ray_hit) * (size_t)n * (size_t)cap;
+    rc = query_staging(b, in_b + cnt_b + out_b, st);
+    if (rc) return rc;
+    gb_ray *d_rays = reinterpret_cast<gb_ray *>(b->d_query);
+    int *d_cnt = reinterpret_cast<int *>(b->d_query + in_b);
+    gb_ray_hit *d_hits = reinterpret_cast<gb_ray_hit *>(b->d_query + in_b + cnt_b);
+    CK(cudaMemcpyAsync(d_rays, rays, sizeof(gb_ray) * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (b->prec == GB_PREC_F64) gb_launch_ray_cast_all<double>(b->bd, d_rays, n, d_hits, cap, d_cnt, st);
+    else gb_launch_ray_cast_all<float>(b->bf, d_rays, n, d_hits, cap, d_cnt, st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(counts, d_cnt, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, st));
+    if (out_b) CK(cudaMemcpyAsync(hits, d_hits, out_b, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return 0;
 }

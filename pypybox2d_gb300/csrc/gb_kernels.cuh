@@ -279,3 +279,7 @@ template <> void gb_launch_query_aabb<GB_REAL>(const Batch<GB_REAL> &B, const gb
                                                int *counts, cudaStream_t st) {
     if (n > 0) k_query_aabb<GB_REAL><<<(n + 7) / 8, 256, 0, st>>>(B, qs, n, out, cap, counts);
 }
+template <> void gb_launch_ray_cast_all<GB_REAL>(const Batch<GB_REAL> &B, const gb_ray *rays, int n, gb_ray_hit *hits, int cap,
+                                                 int *counts, cudaStream_t st) {
+    if (n > 0) k_ray_cast_all<GB_REAL><<<(n + 7) / 8, 256, 0, st>>>(B, rays, n, hits, cap, counts);
+}

@@ -34,6 +34,8 @@ template <class R> size_t gb_solve_smem(int cache_bodies, int threads, int nbuf)
 template <class R> void gb_launch_ray_cast(const Batch<R> &B, const gb_ray *rays, int n, gb_ray_hit *hits, cudaStream_t st);
 template <class R> void gb_launch_query_aabb(const Batch<R> &B, const gb_aabb_query *qs, int n, int *out, int cap, int *counts,
                                              cudaStream_t st);
+template <class R> void gb_launch_ray_cast_all(const Batch<R> &B, const gb_ray *rays, int n, gb_ray_hit *hits, int cap,
+                                               int *counts, cudaStream_t st);
 // recompute the device-only TOI candidate flag of every contact (after an upload)
 template <class R> void gb_launch_refresh_toi_cand(const Batch<R> &B, cudaStream_t st);
 
@@ -59,3 +61,5 @@ template <> void gb_launch_ray_cast<double>(const Batch<double> &, const gb_ray 
 template <> void gb_launch_ray_cast<float>(const Batch<float> &, const gb_ray *, int, gb_ray_hit *, cudaStream_t);
 template <> void gb_launch_query_aabb<double>(const Batch<double> &, const gb_aabb_query *, int, int *, int, int *, cudaStream_t);
 template <> void gb_launch_query_aabb<float>(const Batch<float> &, const gb_aabb_query *, int, int *, int, int *, cudaStream_t);
+template <> void gb_launch_ray_cast_all<double>(const Batch<double> &, const gb_ray *, int, gb_ray_hit *, int, int *, cudaStream_t);
+template <> void gb_launch_ray_cast_all<float>(const Batch<float> &, const gb_ray *, int, gb_ray_hit *, int, int *, cudaStream_t);

@@ -106,44 +106,73 @@ __device__ __forceinline__ bool box_overlap(const dbox &a, double blx, double bl
 
 }  // namespace gbq
 
+namespace gbq {
+// A ray with the segment tests of DynamicTree.ray_cast (dynamictree.py:
+// 222-250) at max_fraction 1 (World.ray_cast passes 1.0)
+struct RaySeg {
+    vec2<double> p1, p2, v, abs_v;
+    double slx, sly, shx, shy;
+};
+__device__ __forceinline__ RaySeg ray_seg(const gb_ray &ray) {
+    RaySeg s;
+    s.p1 = mk<double>(ray.p1x, ray.p1y);
+    s.p2 = mk<double>(ray.p2x, ray.p2y);
+    const vec2<double> r = normalized(s.p2 - s.p1);
+    s.v = cross(1.0, r);
+    s.abs_v = mk<double>(fabs(s.v.x), fabs(s.v.y));
+    const vec2<double> t = s.p1 + 1.0 * (s.p2 - s.p1);
+    s.slx = pymin(s.p1.x, t.x); s.sly = pymin(s.p1.y, t.y);
+    s.shx = pymax(s.p1.x, t.x); s.shy = pymax(s.p1.y, t.y);
+    return s;
+}
+// world-local fixture k: reported by the tree and hit by its shape?
+template <class R> __device__ bool ray_fixture(const Batch<R> &B, const WorldHdr &H, int k, const RaySeg &s,
+                                               vec2<double> *nrm, double *fr) {
+    const int f = H.fbase + k;
+    const dbox a = B.f_aabb[f];
+    if (!box_overlap(a, s.slx, s.sly, s.shx, s.shy)) return false;
+    const vec2<double> c = mk<double>(0.5 * (a.z + a.x), 0.5 * (a.w + a.y));
+    const vec2<double> h = mk<double>(0.5 * (a.z - a.x), 0.5 * (a.w - a.y));
+    const double separation = fabs(dot(s.v, s.p1 - c)) - dot(s.abs_v, h);
+    if (separation > 0.0) return false;
+    const int b = H.bbase + B.f_body[f];
+    xform2<double> xf;
+    xf.p = B.b_xp[b];
+    xf.q = B.b_xq[b];
+    const int type = B.f_type[f];
+    if (type == GB_SHAPE_CIRCLE) return ray_circle(B, f, xf, s.p1, s.p2, nrm, fr);
+    if (type == GB_SHAPE_POLYGON) return ray_polygon(B, f, xf, s.p1, s.p2, nrm, fr);
+    if (type == GB_SHAPE_EDGE) return ray_edge(B, f, xf, s.p1, s.p2, nrm, fr);
+    return false;
+}
+// world.py:431: (1 - fraction) * point1 + fraction * point2
+__device__ __forceinline__ gb_ray_hit make_hit(const RaySeg &s, int k, vec2<double> n, double fr) {
+    gb_ray_hit o;
+    o.fixture = k;
+    o._pad0 = 0;
+    const vec2<double> pt = (1.0 - fr) * s.p1 + fr * s.p2;
+    o.px = pt.x; o.py = pt.y; o.nx = n.x; o.ny = n.y; o.fraction = fr;
+    return o;
+}
+}  // namespace gbq
+
 // One warp per ray: the closest hit over the ray's world (ties: the lower
-// fixture index).  The tree's pruning (dynamictree.py:226-250) is evaluated
-// for each fixture with max_fraction 1 (World.ray_cast passes 1.0).
+// fixture index).
 template <class R> __global__ void k_ray_cast(Batch<R> B, const gb_ray *rays, int n, gb_ray_hit *hits) {
     const int lane = threadIdx.x & 31;
     const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (q >= n) return;
     const gb_ray ray = rays[q];
     const WorldHdr &H = B.hdr[ray.world];
-    const vec2<double> p1 = mk<double>(ray.p1x, ray.p1y), p2 = mk<double>(ray.p2x, ray.p2y);
-    const vec2<double> r = normalized(p2 - p1);
-    const vec2<double> v = cross(1.0, r);
-    const vec2<double> abs_v = mk<double>(fabs(v.x), fabs(v.y));
-    const vec2<double> t = p1 + 1.0 * (p2 - p1);
-    const double slx = pymin(p1.x, t.x), sly = pymin(p1.y, t.y), shx = pymax(p1.x, t.x), shy = pymax(p1.y, t.y);
+    const gbq::RaySeg seg = gbq::ray_seg(ray);
+    const vec2<double> p1 = seg.p1, p2 = seg.p2;
     double best = 2.0;
     int best_f = -1;
     vec2<double> best_n = mk<double>(0.0, 0.0);
     for (int k = lane; k < H.nf; k += 32) {
-        const int f = H.fbase + k;
-        const dbox a = B.f_aabb[f];
-        if (!gbq::box_overlap(a, slx, sly, shx, shy)) continue;
-        const vec2<double> c = mk<double>(0.5 * (a.z + a.x), 0.5 * (a.w + a.y));
-        const vec2<double> h = mk<double>(0.5 * (a.z - a.x), 0.5 * (a.w - a.y));
-        const double separation = fabs(dot(v, p1 - c)) - dot(abs_v, h);
-        if (separation > 0.0) continue;
-        const int b = H.bbase + B.f_body[f];
-        xform2<double> xf;
-        xf.p = B.b_xp[b];
-        xf.q = B.b_xq[b];
         vec2<double> nrm;
         double fr = 0.0;
-        bool hit = false;
-        const int type = B.f_type[f];
-        if (type == GB_SHAPE_CIRCLE) hit = gbq::ray_circle(B, f, xf, p1, p2, &nrm, &fr);
-        else if (type == GB_SHAPE_POLYGON) hit = gbq::ray_polygon(B, f, xf, p1, p2, &nrm, &fr);
-        else if (type == GB_SHAPE_EDGE) hit = gbq::ray_edge(B, f, xf, p1, p2, &nrm, &fr);
-        if (hit && fr < best) { best = fr; best_f = k; best_n = nrm; }
+        if (gbq::ray_fixture(B, H, k, seg, &nrm, &fr) && fr < best) { best = fr; best_f = k; best_n = nrm; }
     }
     // lexicographic (fraction, fixture) minimum over the warp
     for (int off = 16; off > 0; off >>= 1) {
@@ -168,6 +197,31 @@ template <class R> __global__ void k_ray_cast(Batch<R> B, const gb_ray *rays, in
         }
         hits[q] = o;
     }
+}
+
+// One warp per ray: every hit (the generator form of World.ray_cast with
+// each fraction left at 1), in fixture order; the first `cap` go to
+// hits[q * cap ...], counts[q] is the full number.
+template <class R> __global__ void k_ray_cast_all(Batch<R> B, const gb_ray *rays, int n, gb_ray_hit *hits, int cap,
+                                                  int *counts) {
+    const int lane = threadIdx.x & 31;
+    const int q = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= n) return;
+    const gb_ray ray = rays[q];
+    const WorldHdr &H = B.hdr[ray.world];
+    const gbq::RaySeg seg = gbq::ray_seg(ray);
+    int found = 0;
+    for (int k0 = 0; k0 < H.nf; k0 += 32) {
+        const int k = k0 + lane;
+        vec2<double> nrm = mk<double>(0.0, 0.0);
+        double fr = 0.0;
+        const bool hit = k < H.nf && gbq::ray_fixture(B, H, k, seg, &nrm, &fr);
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        const int pos = found + __popc(m & ((1u << lane) - 1u));
+        if (hit && pos < cap) hits[(size_t)q * cap + pos] = gbq::make_hit(seg, k, nrm, fr);
+        found += __popc(m);
+    }
+    if (lane == 0) counts[q] = found;
 }
 
 // One warp per query box: the fixtures whose fat AABB overlaps it

@@ -97,6 +97,18 @@ class GpuBatch:
         abi.check(self.lib.gb_batch_ray_cast(self.h, r.ctypes.data, len(r), out.ctypes.data, ctypes.c_void_p(stream or 0)))
         return out
 
+    def ray_cast_all(self, rays: np.ndarray, max_per_ray: int = 64,
+                     stream: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+        """Every hit of each ray (``abi.RAY`` records), in fixture order:
+        (``abi.RAY_HIT`` [n, max_per_ray], counts[n]) (gb_batch_ray_cast_all)."""
+        r = np.ascontiguousarray(rays, dtype=abi.RAY)
+        out = np.zeros((len(r), max_per_ray), dtype=abi.RAY_HIT)
+        counts = np.zeros(len(r), dtype=np.int32)
+        abi.check(self.lib.gb_batch_ray_cast_all(self.h, r.ctypes.data, len(r), out.ctypes.data, max_per_ray,
+                                                 counts.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                 ctypes.c_void_p(stream or 0)))
+        return out, counts
+
     def query_aabb(self, boxes: np.ndarray, max_per_query: int = 64,
                    stream: int | None = None) -> tuple[np.ndarray, np.ndarray]:
         """Fixtures whose fat AABB overlaps each box (``abi.AABB_QUERY``

@@ -642,6 +642,106 @@ class World:
         if events:
             self._replay(self._gpu.events(0))
 
+    # -- queries
+    def query_aabb(self, aabb, callback=None):
+        """world.py:371-385: the fixtures whose broad-phase (fat) AABB
+        overlaps `aabb` (an object with lower_bound / upper_bound, or
+        (lower, upper), or (lx, ly, ux, uy)); one gb_batch_query_aabb.  The
+        fixtures come in fixture order (the reference's in tree order).
+        Without a callback, an iterator; with one, called per fixture until
+        it returns a false value."""
+        lx, ly, ux, uy = _box_of(aabb)
+        self._sync_device()
+        q = np.zeros(1, dtype=abi.AABB_QUERY)
+        q["lx"], q["ly"], q["ux"], q["uy"] = lx, ly, ux, uy
+        out, n = self._gpu.query_aabb(q, max_per_query=max(1, len(self._F)))
+        fixtures = [self._fixture_at(int(k)) for k in out[0, :int(n[0])]]
+        if callback is None:
+            return iter(fixtures)
+        for f in fixtures:
+            if not callback(f):
+                break
+        return None
+
+    def ray_cast_closest(self, point1, point2):
+        """The closest fixture on the segment point1 -> point2: what
+        World.ray_cast (world.py:387-440) leaves in a callback that returns
+        the fraction it is given.  Returns (fixture, point, normal, fraction)
+        or None; one gb_batch_ray_cast."""
+        p1, p2 = Vec2(*point1), Vec2(*point2)
+        self._sync_device()
+        r = np.zeros(1, dtype=abi.RAY)
+        r["p1x"], r["p1y"], r["p2x"], r["p2y"] = p1[0], p1[1], p2[0], p2[1]
+        try:
+            h = self._gpu.ray_cast(r)[0]
+        except abi.GB2DError as ex:
+            if "no length" in str(ex):
+                raise ValueError("||p2 - p1||^2 > 0.0") from ex   # dynamictree.py:222-224
+            raise
+        if int(h["fixture"]) < 0:
+            return None
+        return (self._fixture_at(int(h["fixture"])), Vec2(float(h["px"]), float(h["py"])),
+                Vec2(float(h["nx"]), float(h["ny"])), float(h["fraction"]))
+
+    def ray_cast(self, point1, point2, callback=None):
+        """world.py:387-440.  The fixtures on the segment come from one
+        gb_batch_ray_cast_all and are handed over in order of fraction (the
+        reference hands them over in its tree's order), with the reference's
+        answers: -1 skips the fixture, 0 ends the cast, a fraction clips the
+        ray (later hits beyond it are skipped), 1 goes on.  A closest-hit
+        callback therefore ends as with the reference, and an all-hits one
+        sees the same hits.  Without a callback, a generator of
+        [fixture, point, normal, fraction] lists whose last entry the caller
+        may set to the same answers."""
+        hits = self._ray_hits(point1, point2)
+        if callback is not None:
+            self._ray_walk(hits, lambda entry: callback(*entry))
+            return None
+        return self._ray_generator(hits)
+
+    def _ray_hits(self, point1, point2):
+        p1, p2 = Vec2(*point1), Vec2(*point2)
+        self._sync_device()
+        r = np.zeros(1, dtype=abi.RAY)
+        r["p1x"], r["p1y"], r["p2x"], r["p2y"] = p1[0], p1[1], p2[0], p2[1]
+        cap = max(1, len(self._F))
+        try:
+            out, n = self._gpu.ray_cast_all(r, max_per_ray=cap)
+        except abi.GB2DError as ex:
+            if "no length" in str(ex):
+                raise ValueError("||p2 - p1||^2 > 0.0") from ex   # dynamictree.py:222-224
+            raise
+        h = out[0, :int(n[0])]
+        h = h[np.lexsort((h["fixture"], h["fraction"]))]
+        return [(self._fixture_at(int(x["fixture"])), Vec2(float(x["px"]), float(x["py"])),
+                 Vec2(float(x["nx"]), float(x["ny"])), float(x["fraction"])) for x in h]
+
+    @staticmethod
+    def _ray_walk(hits, answer):
+        max_fraction = 1.0
+        for hit in hits:
+            if hit[3] > max_fraction:
+                continue
+            value = answer(list(hit))
+            if value == 0.0:
+                break
+            if value > 0.0:
+                max_fraction = value
+
+    @staticmethod
+    def _ray_generator(hits):
+        max_fraction = 1.0
+        for hit in hits:
+            if hit[3] > max_fraction:
+                continue
+            entry = list(hit)
+            yield entry
+            value = entry[-1]
+            if value == 0.0:
+                break
+            if value > 0.0:
+                max_fraction = value
+
     def _replay(self, ev):
         """Hand the step's recorded events to the listeners, in key order."""
         cm = self.contact_manager
@@ -755,6 +855,17 @@ class World:
                 moved.append(start + k)
         if moved:
             self._M = np.concatenate([self._M, np.array(moved, np.int32)]).astype(np.int32)
+
+
+def _box_of(aabb):
+    """(lx, ly, ux, uy) of an AABB given as an object with lower_bound /
+    upper_bound, as (lower, upper) or as four numbers."""
+    if hasattr(aabb, "lower_bound"):
+        lo, hi = aabb.lower_bound, aabb.upper_bound
+        return float(lo[0]), float(lo[1]), float(hi[0]), float(hi[1])
+    if len(aabb) == 2:
+        return float(aabb[0][0]), float(aabb[0][1]), float(aabb[1][0]), float(aabb[1][1])
+    return tuple(float(x) for x in aabb)
 
 
 def _contains(fat, tight):

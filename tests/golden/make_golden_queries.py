@@ -11,8 +11,9 @@ and query boxes are put to the reference's own World.ray_cast
 
   * every ray's hits are collected through the generator form with the
     fraction left at 1 (no clipping), so each fixture the tree reports and
-    the shape hits is seen; the closest hit (lowest fraction) is the
-    expected answer.  Rays whose two closest hits share one fraction are left
+    the shape hits is seen: all of them (in fixture order) are the expected
+    answer of the all-hits query, the closest (lowest fraction) that of the
+    closest-hit query.  Rays whose two closest hits share one fraction are left
     out (their winner would depend on the tree's visiting order).
   * every query box's fixtures are collected and sorted by fixture index.
 
@@ -72,7 +73,7 @@ def main():
         fidx = mg.fixture_index(world)
         rng = np.random.default_rng(20261204 + len(name))
         p1, p2 = rays_for(rng, F)
-        rays, hits = [], []
+        rays, hits, all_hits, all_counts = [], [], [], []
         for a, b in zip(p1, p2):
             found = []
             for ret in world.ray_cast((float(a[0]), float(a[1])), (float(b[0]), float(b[1]))):
@@ -83,6 +84,9 @@ def main():
             if len(found) > 1 and found[0][0] == found[1][0]:
                 continue
             rays.append((a[0], a[1], b[0], b[1]))
+            by_fixture = sorted(found, key=lambda h: h[1])
+            all_counts.append(len(by_fixture))
+            all_hits.extend((k, px, py, nx, ny, fr) for fr, k, px, py, nx, ny in by_fixture)
             if found:
                 fr, k, px, py, nx, ny = found[0]
                 hits.append((k, px, py, nx, ny, fr))
@@ -99,6 +103,8 @@ def main():
         out[f"{name}_rays"] = np.array(rays, dtype=np.float64)
         out[f"{name}_hits"] = np.array(hits, dtype=[("fixture", "<i4"), ("px", "<f8"), ("py", "<f8"),
                                                     ("nx", "<f8"), ("ny", "<f8"), ("fraction", "<f8")])
+        out[f"{name}_all_counts"] = np.array(all_counts, dtype=np.int32)
+        out[f"{name}_all_hits"] = np.array(all_hits, dtype=out[f"{name}_hits"].dtype)
         out[f"{name}_boxes"] = boxes
         out[f"{name}_box_counts"] = np.array(counts, dtype=np.int32)
         out[f"{name}_box_fixtures"] = np.array(lists, dtype=np.int32)

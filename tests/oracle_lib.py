@@ -187,3 +187,18 @@ def query_aabb_records(F, boxes, cap: int, libm: bool = True) -> tuple[np.ndarra
     counts = np.zeros(len(q), dtype=np.int32)
     lib.or_query_aabb_records(F.ctypes.data, len(F), q.ctypes.data, len(q), out.ctypes.data, cap, counts.ctypes.data)
     return out, counts
+
+
+def ray_cast_all_records(B, F, rays, cap: int, libm: bool = True) -> tuple[np.ndarray, np.ndarray]:
+    """The restatement's every hit (or_ray_cast_all_records) of one world."""
+    lib = load(libm)
+    lib.or_ray_cast_all_records.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    B = np.ascontiguousarray(B, dtype=abi.BODY)
+    F = np.ascontiguousarray(F, dtype=abi.FIXTURE)
+    r = np.ascontiguousarray(rays, dtype=abi.RAY)
+    out = np.zeros((len(r), cap), dtype=abi.RAY_HIT)
+    counts = np.zeros(len(r), dtype=np.int32)
+    lib.or_ray_cast_all_records(B.ctypes.data, F.ctypes.data, len(F), r.ctypes.data, len(r), out.ctypes.data, cap,
+                                counts.ctypes.data)
+    return out, counts

@@ -38,6 +38,21 @@ def _load(scene):
     return W, B, F, rays, d[f"{scene}_hits"], boxes, counts, lists
 
 
+def _load_all(scene):
+    """Every hit of every ray, in fixture order: (counts, per-ray lists)."""
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    counts = d[f"{scene}_all_counts"]
+    return counts, np.split(d[f"{scene}_all_hits"], np.cumsum(counts)[:-1])
+
+
+def _check_all(out, n, counts, lists, what):
+    assert np.array_equal(n, counts), f"{what}: hit counts differ"
+    for q, hs in enumerate(lists):
+        got = out[q, :len(hs)]
+        for f in ("fixture", "px", "py", "nx", "ny", "fraction"):
+            assert np.array_equal(got[f], hs[f]), f"{what}: ray {q} field {f} differs"
+
+
 def _check_hits(got, want, what):
     assert np.array_equal(got["fixture"], want["fixture"]), f"{what}: hit fixtures differ at " \
         f"{np.argwhere(got['fixture'] != want['fixture'])[:5].ravel()}"
@@ -61,6 +76,10 @@ def test_oracle_queries_match_reference(scene):
     _check_hits(oracle_lib.ray_cast_records(B, F, rays, libm=True), want, f"{scene} oracle rays")
     out, n = oracle_lib.query_aabb_records(F, boxes, CAP, libm=True)
     _check_lists(out, n, counts, lists, f"{scene} oracle boxes")
+    ac, al = _load_all(scene)
+    assert ac.sum() > 300 and ac.max() <= CAP
+    out, n = oracle_lib.ray_cast_all_records(B, F, rays, CAP, libm=True)
+    _check_all(out, n, ac, al, f"{scene} oracle all hits")
 
 
 def _batch(scene, precision, copies=1):
@@ -86,6 +105,9 @@ def test_gpu_queries_match_reference_f64(scene):
         _check_hits(g.ray_cast(rays), want, f"{scene} world {w} gpu rays")
         out, n = g.query_aabb(boxes, CAP)
         _check_lists(out, n, counts, lists, f"{scene} world {w} gpu boxes")
+        ac, al = _load_all(scene)
+        out, n = g.ray_cast_all(rays, CAP)
+        _check_all(out, n, ac, al, f"{scene} world {w} gpu all hits")
 
 
 @pytest.mark.gpu
@@ -116,3 +138,58 @@ def test_gpu_queries_reject_bad_input():
     with pytest.raises(abi.GB2DError, match="world out of range"):
         g.ray_cast(bad)
 
+
+@pytest.mark.gpu
+def test_world_api_queries():
+    """World.ray_cast / ray_cast_closest / query_aabb of the drop-in API
+    against the restatement on the same records."""
+    import pypybox2d_gb300 as b2
+    world = b2.World((0, -10), True)
+    world.create_static_body(position=(0, -1)).create_polygon_fixture(box=(20, 1))
+    for i in range(12):
+        b = world.create_dynamic_body(position=(-6 + i, 1 + 0.7 * (i % 3)), angle=0.3 * i)
+        if i % 2:
+            b.create_circle_fixture(0.4, density=1.0)
+        else:
+            b.create_polygon_fixture(box=(0.4, 0.3), density=1.0)
+    for _ in range(20):
+        world.step(1 / 60, 8, 3)
+    world._materialise()
+    B, F = world._B.copy(), world._F.copy()
+    rng = np.random.default_rng(7)
+    rays = np.zeros(64, dtype=abi.RAY)
+    rays["p1x"], rays["p1y"] = rng.uniform(-8, 8, 64), rng.uniform(4, 6, 64)
+    rays["p2x"], rays["p2y"] = rays["p1x"] + rng.uniform(-3, 3, 64), rng.uniform(-3, 0, 64)
+    want = oracle_lib.ray_cast_records(B, F, rays, libm=False)
+    n_hit = 0
+    for r, w in zip(rays, want):
+        got = world.ray_cast_closest((r["p1x"], r["p1y"]), (r["p2x"], r["p2y"]))
+        if w["fixture"] < 0:
+            assert got is None
+            continue
+        n_hit += 1
+        fixture, point, normal, fraction = got
+        assert fixture is world._fixture_at(int(w["fixture"]))
+        assert (point[0], point[1], normal[0], normal[1], fraction) == (w["px"], w["py"], w["nx"], w["ny"], w["fraction"])
+        seen = []
+        world.ray_cast((r["p1x"], r["p1y"]), (r["p2x"], r["p2y"]), lambda f, p, n, fr: seen.append(f) or fr)
+        assert seen == [fixture]
+    assert n_hit > 10
+    # every hit: a callback that answers 1, and the generator left at 1
+    every, counts = oracle_lib.ray_cast_all_records(B, F, rays, 64, libm=False)
+    for r, hs, c in zip(rays, every, counts):
+        want = sorted((float(h["fraction"]), int(h["fixture"])) for h in hs[:c])
+        seen = []
+        world.ray_cast((r["p1x"], r["p1y"]), (r["p2x"], r["p2y"]),
+                       lambda f, p, n, fr: seen.append((fr, f)) or 1.0)
+        assert [(fr, f) for fr, f in seen] == [(fr, world._fixture_at(k)) for fr, k in want]
+        gen = []
+        for entry in world.ray_cast((r["p1x"], r["p1y"]), (r["p2x"], r["p2y"])):
+            gen.append(entry[0])
+            entry[-1] = 1.0
+        assert gen == [f for _, f in seen]
+    out, n = oracle_lib.query_aabb_records(F, np.array([(0, 0, -3.0, -0.5, 2.0, 3.0)], dtype=abi.AABB_QUERY), 64)
+    got = list(world.query_aabb(((-3.0, -0.5), (2.0, 3.0))))
+    assert got == [world._fixture_at(int(k)) for k in out[0, :n[0]]] and len(got) >= 3
+    with pytest.raises(ValueError):
+        world.ray_cast_closest((1.0, 1.0), (1.0, 1.0))
