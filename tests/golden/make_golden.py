@@ -310,6 +310,28 @@ def scene_sleep(b2):
     return world
 
 
+def scene_kinematic(b2, seed=9):
+    """Kinematic bodies: a platform sliding sideways and a spinning paddle
+    (both moved by their velocities alone) under falling boxes and circles,
+    above a static ground box."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    world.create_static_body(position=(0, -0.5), shapes=b2.Polygon(box=(30, 0.5)))
+    world.create_kinematic_body(position=(-4, 3), linear_velocity=(1.5, 0.0),
+                                shapes=b2.Polygon(box=(3, 0.25)))
+    world.create_kinematic_body(position=(5, 2.5), angular_velocity=1.2,
+                                shapes=b2.Polygon(box=(2.5, 0.2)))
+    for i in range(24):
+        x, y = rng.uniform(-7, 8), 5 + 0.9 * i
+        body = world.create_dynamic_body(position=(x, y), angle=rng.uniform(-1, 1))
+        if i % 3 == 0:
+            body.create_circle_fixture(radius=rng.uniform(0.2, 0.45), density=1.0, friction=0.4)
+        else:
+            body.create_polygon_fixture(box=(rng.uniform(0.2, 0.5), rng.uniform(0.2, 0.5)), density=1.0,
+                                        friction=0.4, restitution=rng.uniform(0, 0.3))
+    return world
+
+
 def scene_uneven(b2, seed=11, n=250):
     """One world of the uneven-batch workload (pypybox2d_gb300.scenes draws:
     100 m container of 4 edges, circles and convex polygons on a 2.1 m grid,
@@ -341,6 +363,7 @@ SCENES = {
     "bullets": (scene_bullets, 60, (1, 2, 3, 5, 10, 20, 40, 60)),
     "sleep": (scene_sleep, 90, (1, 10, 29, 30, 31, 45, 60, 90)),
     "uneven": (scene_uneven, 240, (1, 2, 5, 30, 60, 120, 180, 240)),
+    "kinematic": (scene_kinematic, 180, (1, 2, 5, 20, 60, 120, 180)),
 }
 
 

@@ -19,7 +19,7 @@ from pypybox2d_gb300 import abi
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-STEPS = {"pyramid": 40, "pyramid5": 150, "mixed": 120, "bullets": 60, "sleep": 90, "uneven": 240}
+STEPS = {"pyramid": 40, "pyramid5": 150, "mixed": 120, "bullets": 60, "sleep": 90, "uneven": 240, "kinematic": 180}
 
 
 def _gpu():
