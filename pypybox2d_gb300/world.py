@@ -502,6 +502,7 @@ class World:
         self._C = np.zeros(0, dtype=abi.CONTACT)
         self._M = np.zeros(0, dtype=np.int32)
         self._gpu = None
+        self._owner = None          # the WorldBatch stepping this world, if any
         self._host_fresh = True     # host records equal the device state
         self._upload_bodies = False
         self._locked = False
@@ -623,6 +624,8 @@ class World:
         """world.py:307-354: one gb_batch_step of this world, then the
         contact listeners' events."""
         self._check_unlocked()
+        if self._owner is not None:
+            raise RuntimeError("this world is stepped by a WorldBatch; call the batch's step")
         cm = self.contact_manager
         if cm.pre_solve is not None:
             raise NotImplementedError("pre_solve listeners cannot run inside the GPU step")
@@ -651,10 +654,10 @@ class World:
         Without a callback, an iterator; with one, called per fixture until
         it returns a false value."""
         lx, ly, ux, uy = _box_of(aabb)
-        self._sync_device()
+        gpu, wi = self._query_gpu()
         q = np.zeros(1, dtype=abi.AABB_QUERY)
-        q["lx"], q["ly"], q["ux"], q["uy"] = lx, ly, ux, uy
-        out, n = self._gpu.query_aabb(q, max_per_query=max(1, len(self._F)))
+        q["world"], q["lx"], q["ly"], q["ux"], q["uy"] = wi, lx, ly, ux, uy
+        out, n = gpu.query_aabb(q, max_per_query=max(1, len(self._F)))
         fixtures = [self._fixture_at(int(k)) for k in out[0, :int(n[0])]]
         if callback is None:
             return iter(fixtures)
@@ -669,11 +672,11 @@ class World:
         the fraction it is given.  Returns (fixture, point, normal, fraction)
         or None; one gb_batch_ray_cast."""
         p1, p2 = Vec2(*point1), Vec2(*point2)
-        self._sync_device()
+        gpu, wi = self._query_gpu()
         r = np.zeros(1, dtype=abi.RAY)
-        r["p1x"], r["p1y"], r["p2x"], r["p2y"] = p1[0], p1[1], p2[0], p2[1]
+        r["world"], r["p1x"], r["p1y"], r["p2x"], r["p2y"] = wi, p1[0], p1[1], p2[0], p2[1]
         try:
-            h = self._gpu.ray_cast(r)[0]
+            h = gpu.ray_cast(r)[0]
         except abi.GB2DError as ex:
             if "no length" in str(ex):
                 raise ValueError("||p2 - p1||^2 > 0.0") from ex   # dynamictree.py:222-224
@@ -701,12 +704,12 @@ class World:
 
     def _ray_hits(self, point1, point2):
         p1, p2 = Vec2(*point1), Vec2(*point2)
-        self._sync_device()
+        gpu, wi = self._query_gpu()
         r = np.zeros(1, dtype=abi.RAY)
-        r["p1x"], r["p1y"], r["p2x"], r["p2y"] = p1[0], p1[1], p2[0], p2[1]
+        r["world"], r["p1x"], r["p1y"], r["p2x"], r["p2y"] = wi, p1[0], p1[1], p2[0], p2[1]
         cap = max(1, len(self._F))
         try:
-            out, n = self._gpu.ray_cast_all(r, max_per_ray=cap)
+            out, n = gpu.ray_cast_all(r, max_per_ray=cap)
         except abi.GB2DError as ex:
             if "no length" in str(ex):
                 raise ValueError("||p2 - p1||^2 > 0.0") from ex   # dynamictree.py:222-224
@@ -760,6 +763,9 @@ class World:
     # ---------------------------------------------------------------- internals
     def _materialise(self):
         """Download the device state into the host records (once per step)."""
+        if self._owner is not None and not self._host_fresh:
+            self._owner._pull(self)
+            return
         if self._gpu is None or self._host_fresh:
             return
         self._B = self._gpu.bodies()
@@ -770,6 +776,9 @@ class World:
 
     def _structural(self):
         """The next step re-uploads the whole world from the host records."""
+        if self._owner is not None:
+            raise NotImplementedError("structural changes (bodies, fixtures, transforms, gravity) of a world "
+                                      "inside a WorldBatch: build a new batch after the change")
         self._materialise()
         if self._gpu is not None:
             self._gpu.close()
@@ -783,8 +792,16 @@ class World:
         return self._B[i]
 
     def _mark_bodies_edited(self):
-        if self._gpu is not None:
+        if self._gpu is not None or self._owner is not None:
             self._upload_bodies = True
+
+    def _query_gpu(self):
+        """The device batch holding this world's current state, and the
+        world's index in it."""
+        if self._owner is not None:
+            return self._owner._device_for(self)
+        self._sync_device()
+        return self._gpu, 0
 
     def _fixture_at(self, f):
         bi = int(self._F[f]["body"])
@@ -885,3 +902,169 @@ def _load_body_state(b: _Body, r):
     b.sleep_time = float(r["sleep_time"])
     fl = int(r["flags"])
     b.awake, b.allow_sleep, b.bullet = bool(fl & abi.BODY_AWAKE), bool(fl & abi.BODY_ALLOW_SLEEP), bool(fl & abi.BODY_BULLET)
+
+
+def _concat_worlds(recs):
+    """Per-world (W, B, F, C, M) host records -> one batch's records (the
+    world descriptors' ranges shifted; everything inside a world stays
+    world-local)."""
+    Ws, nb, nf, nc, nm = [], 0, 0, 0, 0
+    for W, B, F, C, M in recs:
+        W = W.copy()
+        W["body_start"], W["fixture_start"], W["contact_start"], W["move_start"] = nb, nf, nc, nm
+        Ws.append(W)
+        nb, nf, nc, nm = nb + len(B), nf + len(F), nc + len(C), nm + len(M)
+    cat = np.concatenate
+    return (cat(Ws), cat([r[1] for r in recs]), cat([r[2] for r in recs]), cat([r[3] for r in recs]),
+            cat([np.asarray(r[4], dtype=np.int32) for r in recs]).astype(np.int32))
+
+
+class WorldBatch:
+    """Independent worlds advanced together: one device batch and one launch
+    sequence a step for all of them (the batched form of World.step,
+    world.py:307-354).
+
+    The worlds are built through the World API first.  While the batch holds
+    them, their body getters, setters, forces, contacts, listeners and
+    queries work as before; World.step and structural changes (new bodies or
+    fixtures, transforms, gravity) raise, and every step is a
+    WorldBatch.step.  ``close()`` hands the worlds back."""
+
+    def __init__(self, worlds, precision=None):
+        worlds = list(worlds)
+        if not worlds:
+            raise ValueError("a WorldBatch needs at least one world")
+        for w in worlds:
+            w._check_unlocked()
+            if w._owner is not None:
+                raise ValueError("a world can belong to one WorldBatch at a time")
+        recs = []
+        for w in worlds:
+            w._materialise()
+            W = w._sb.world_record(len(w._B), len(w._F), len(w._M))
+            W["contact_count"] = len(w._C)
+            W["inv_dt0"] = w._inv_dt0
+            recs.append((W, w._B, w._F, w._C, w._M))
+        W, B, F, C, M = _concat_worlds(recs)
+        from .gpu import GpuBatch
+        self._gpu = GpuBatch(W, B, F, contacts=C if len(C) else None, precision=precision or worlds[0]._precision,
+                             moves=M)
+        self._worlds = worlds
+        self._index = {id(w): i for i, w in enumerate(worlds)}
+        self._ranges = [(int(r["body_start"]), int(r["body_count"]), int(r["fixture_start"]), int(r["fixture_count"]))
+                        for r in W]
+        self._all = None        # (bodies, fat AABBs) of the whole batch, downloaded once after a step
+        self._graphs = {}
+        for w in worlds:
+            if w._gpu is not None:
+                w._gpu.close()
+                w._gpu = None
+            w._owner = self
+            w._host_fresh = True
+            w._upload_bodies = False
+
+    @property
+    def worlds(self):
+        return list(self._worlds)
+
+    @property
+    def device(self):
+        """The underlying GpuBatch (C ABI handle)."""
+        return self._gpu
+
+    def autotune(self, dt, vel_iters=8, pos_iters=3, steps_per_trial=3):
+        """Pick the launch configuration from trial steps (gb_batch_autotune);
+        the worlds' state is unchanged."""
+        self._push_edits()
+        self._graphs.clear()
+        return self._gpu.autotune(float(dt), int(vel_iters), int(pos_iters), steps_per_trial)
+
+    def step(self, dt, vel_iters, pos_iters, n_steps=1, graph=False, stream=None):
+        """n_steps calls of World.step on every world of the batch, in one
+        gb_batch_step call, or (graph=True) as a captured CUDA graph replayed
+        (captured once per (dt, iterations, n_steps)).  Listeners are called
+        afterwards, world by world, in each world's event order."""
+        for w in self._worlds:
+            w._check_unlocked()
+            if w.contact_manager.pre_solve is not None:
+                raise NotImplementedError("pre_solve listeners cannot run inside the GPU step")
+        self._push_edits()
+        events = any(w.contact_manager.wants_events for w in self._worlds)
+        for w in self._worlds:
+            w._locked = True
+        try:
+            if graph:
+                key = (float(dt), int(vel_iters), int(pos_iters), int(n_steps), events)
+                g = self._graphs.get(key)
+                if g is None:
+                    g = self._gpu.capture(float(dt), int(vel_iters), int(pos_iters), int(n_steps), launch_mode=0,
+                                          events=events)
+                    self._graphs[key] = g
+                g.launch(stream)
+            else:
+                self._gpu.step(float(dt), int(vel_iters), int(pos_iters), int(n_steps), launch_mode=0, events=events,
+                               stream=stream)
+        finally:
+            for w in self._worlds:
+                w._locked = False
+        self._all = None
+        for w in self._worlds:
+            w._host_fresh = False
+            if dt > 0.0 and n_steps > 0:
+                w._inv_dt0 = 1.0 / dt
+        st = self._gpu.status()
+        if st.any():
+            bad = [int(i) for i in np.flatnonzero(st)]
+            raise RuntimeError(f"GPU world step failed in worlds {bad[:8]}: status bits {int(st[bad[0]]):#x}")
+        if events:
+            for i, w in enumerate(self._worlds):
+                if w.contact_manager.wants_events:
+                    w._replay(self._gpu.events(i))
+
+    def close(self):
+        """Copy the state back into the worlds and release them: each World
+        steps on its own again (from its host records)."""
+        if self._gpu is None:
+            return
+        for w in self._worlds:
+            w._materialise()
+        for w in self._worlds:
+            w._owner = None
+            w._upload_bodies = False
+        for g in self._graphs.values():
+            g.close()
+        self._graphs.clear()
+        self._gpu.close()
+        self._gpu = None
+
+    # ------------------------------------------------------------ internals
+    def _pull(self, w):
+        """Download world w's state (bodies, fat AABBs, contacts) into its
+        host records; the whole batch's bodies and boxes come down once a step."""
+        if self._all is None:
+            self._all = (self._gpu.bodies(), self._gpu.proxies())
+        B, A = self._all
+        i = self._index[id(w)]
+        b0, nb, f0, nf = self._ranges[i]
+        w._B = B[b0:b0 + nb].copy()
+        w._F["aabb"] = A[f0:f0 + nf]
+        w._C = self._gpu.contacts(i)
+        w._M = np.zeros(0, np.int32)
+        w._host_fresh = True
+
+    def _push_edits(self):
+        """Upload the bodies of the whole batch when a world's bodies were
+        edited on the host (velocities, forces, awake flags)."""
+        if not any(w._upload_bodies for w in self._worlds):
+            return
+        for w in self._worlds:
+            w._materialise()
+        B = np.concatenate([w._B for w in self._worlds])
+        self._gpu.set_bodies(B)
+        self._all = None
+        for w in self._worlds:
+            w._upload_bodies = False
+
+    def _device_for(self, w):
+        self._push_edits()
+        return self._gpu, self._index[id(w)]
