@@ -746,7 +746,18 @@ class World:
                 max_fraction = value
 
     def _replay(self, ev):
-        """Hand the step's recorded events to the listeners, in key order."""
+        """Hand the step's recorded events to the listeners, in key order.
+        The world is locked meanwhile, as during the reference's step
+        (world.py:321-354), where the listeners run: world.locked is True and
+        structural changes raise LockedError."""
+        was = self._locked
+        self._locked = True
+        try:
+            self._replay_events(ev)
+        finally:
+            self._locked = was
+
+    def _replay_events(self, ev):
         cm = self.contact_manager
         for e in ev:
             fa, fb = self._fixture_at(int(e["fixture_a"])), self._fixture_at(int(e["fixture_b"]))

@@ -100,3 +100,22 @@ def test_world_batch_follows_the_lone_worlds():
     for i in range(3):
         _same_worlds(A[i], S[i], f"after close world {i}")
     assert logA == logS
+
+
+def test_listeners_run_with_the_world_locked():
+    """As inside the reference's step (world.py:321-354): a listener sees
+    world.locked and cannot change the world's structure."""
+    from pypybox2d_gb300 import abi
+    w = build(0)
+    seen = []
+
+    def begin(c):
+        seen.append(w.locked)
+        w.create_dynamic_body(position=(0, 5))
+
+    w.contact_manager.begin_contact = begin
+    ev = np.zeros(1, dtype=abi.EVENT)
+    ev["type"], ev["fixture_a"], ev["fixture_b"] = abi.EV_BEGIN, 0, 1
+    with pytest.raises(b2.LockedError):
+        w._replay(ev)
+    assert seen == [True] and not w.locked and w.body_count == 1 + 6
