@@ -325,6 +325,55 @@ class Body:
             self.awake = True
         return True
 
+    # -- frames (body.py: Transform and Mat22 products of the body's _xf)
+    def get_world_point(self, local_point):
+        """xf * local_point (Transform_mul)"""
+        r = self._rec()
+        x, y = float(local_point[0]), float(local_point[1])
+        return Vec2(r["px"] + r["qc"] * x + (-r["qs"]) * y, r["py"] + r["qs"] * x + r["qc"] * y)
+
+    def get_world_vector(self, local_vector):
+        """R * local_vector (Mat22_mul)"""
+        r = self._rec()
+        x, y = float(local_vector[0]), float(local_vector[1])
+        return Vec2(r["qc"] * x + (-r["qs"]) * y, r["qs"] * x + r["qc"] * y)
+
+    def get_local_point(self, world_point):
+        """xf^T * world_point (Transform_mul_t_vec)"""
+        r = self._rec()
+        x, y = float(world_point[0]) - r["px"], float(world_point[1]) - r["py"]
+        return Vec2(r["qc"] * x + r["qs"] * y, (-r["qs"]) * x + r["qc"] * y)
+
+    def get_local_vector(self, world_vector):
+        """R^T * world_vector (Mat22_mul_t_vec)"""
+        r = self._rec()
+        x, y = float(world_vector[0]), float(world_vector[1])
+        return Vec2(r["qc"] * x + r["qs"] * y, (-r["qs"]) * x + r["qc"] * y)
+
+    def get_linear_velocity_from_world_point(self, world_point):
+        """v + cross(w, p - c)"""
+        r = self._rec()
+        dx, dy = float(world_point[0]) - r["cx"], float(world_point[1]) - r["cy"]
+        w = r["w"]
+        return Vec2(r["vx"] + (-w * dy), r["vy"] + w * dx)
+
+    def get_linear_velocity_from_local_point(self, local_point):
+        return self.get_linear_velocity_from_world_point(self.get_world_point(local_point))
+
+    @property
+    def allow_sleep(self):
+        return self.sleeping_allowed
+
+    @allow_sleep.setter
+    def allow_sleep(self, flag):
+        self.sleeping_allowed = flag
+
+    @property
+    def contact_list(self):
+        """The world's contacts that involve one of this body's fixtures."""
+        mine = {id(f) for f in self.fixtures}
+        return [c for c in self._world.contacts if id(c.fixture_a) in mine or id(c.fixture_b) in mine]
+
     def apply_force(self, force, point):
         if not self._wake_for_force():
             return
@@ -519,6 +568,59 @@ class World:
         self._check_unlocked()
         self._structural()
         self._sb.gravity = (float(g[0]), float(g[1]))
+
+    def _flag(self, bit):
+        return bool(self._sb.flags & bit)
+
+    def _set_flag(self, bit, value):
+        """World flags live in the world descriptor: a change re-uploads the
+        world before the next step (world.py:139-181 only store the flag)."""
+        self._check_unlocked()
+        if bool(value) == self._flag(bit):
+            return
+        self._structural()
+        self._sb.flags = (self._sb.flags | bit) if value else (self._sb.flags & ~bit)
+
+    @property
+    def warm_starting(self):
+        return self._flag(abi.W_WARM_STARTING)
+
+    @warm_starting.setter
+    def warm_starting(self, v):
+        self._set_flag(abi.W_WARM_STARTING, v)
+
+    @property
+    def continuous_physics(self):
+        return self._flag(abi.W_CONTINUOUS)
+
+    @continuous_physics.setter
+    def continuous_physics(self, v):
+        self._set_flag(abi.W_CONTINUOUS, v)
+
+    @property
+    def allow_sleep(self):
+        return self._flag(abi.W_ALLOW_SLEEP)
+
+    @allow_sleep.setter
+    def allow_sleep(self, v):
+        self._set_flag(abi.W_ALLOW_SLEEP, v)
+
+    @property
+    def auto_clear_forces(self):
+        return self._flag(abi.W_AUTO_CLEAR_FORCES)
+
+    @auto_clear_forces.setter
+    def auto_clear_forces(self, v):
+        self._set_flag(abi.W_AUTO_CLEAR_FORCES, v)
+
+    @property
+    def sub_stepping(self):
+        return False
+
+    @sub_stepping.setter
+    def sub_stepping(self, v):
+        if v:
+            raise NotImplementedError("sub_stepping is not supported by the GPU world step")
 
     @property
     def locked(self):

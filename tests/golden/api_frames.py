@@ -1,0 +1,36 @@
+"""Body frame helpers and World flags through the World API, run on the
+reference by make_golden_queries.py and on pypybox2d_gb300 by
+tests/test_world_batch.py (no step: host records only).
+
+Returns one row per (body, probe point): the body's get_world_point,
+get_world_vector, get_local_point, get_local_vector,
+get_linear_velocity_from_world_point and
+get_linear_velocity_from_local_point of the probe, and the World flags."""
+
+PROBES = ((0.0, 0.0), (1.25, -0.5), (-3.0, 2.75), (0.1, 0.3))
+
+
+def build(b2):
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    world.create_static_body(position=(0, -1)).create_polygon_fixture(box=(10, 1))
+    for i in range(5):
+        b = world.create_dynamic_body(position=(-4.0 + 2.0 * i, 1.5 + 0.3 * i), angle=0.7 * i - 1.1,
+                                      linear_velocity=(0.5 * i - 1.0, 0.25 * i), angular_velocity=0.4 * i - 0.9)
+        if i % 2:
+            b.create_circle_fixture(radius=0.4, density=1.0)
+        else:
+            b.create_polygon_fixture(box=(0.5, 0.25), density=2.0)
+    return world
+
+
+def rows(b2):
+    world = build(b2)
+    out = []
+    for body in world.bodies:
+        for p in PROBES:
+            vals = (body.get_world_point(p), body.get_world_vector(p), body.get_local_point(p),
+                    body.get_local_vector(p), body.get_linear_velocity_from_world_point(p),
+                    body.get_linear_velocity_from_local_point(p))
+            out.append([float(c) for v in vals for c in (v[0], v[1])])
+    flags = [world.warm_starting, world.continuous_physics, world.allow_sleep, world.auto_clear_forces]
+    return out, flags

@@ -18,7 +18,8 @@ and query boxes are put to the reference's own World.ray_cast
   * every query box's fixtures are collected and sorted by fixture index.
 
 Output: tests/golden/queries.npz (per scene: the exported state, the rays,
-the expected hits, the query boxes, the expected fixture lists).
+the expected hits, the query boxes, the expected fixture lists; plus the
+Body frame helpers of tests/golden/api_frames.py).
 """
 from __future__ import annotations
 
@@ -111,6 +112,11 @@ def main():
         n_hit = int(np.sum(out[f"{name}_hits"]["fixture"] >= 0))
         print(f"{name}: {len(B)} bodies, {len(F)} fixtures, {len(rays)} rays ({n_hit} hit), "
               f"{len(boxes)} boxes ({int(np.sum(counts))} fixtures listed)")
+    # Body frame helpers and World flags of a small API-built world (api_frames.py)
+    import api_frames
+    frame_rows, flags = api_frames.rows(b2)
+    out["frames"] = np.array(frame_rows, dtype=np.float64)
+    out["frame_world_flags"] = np.array(flags, dtype=np.int32)
     path = os.path.join(HERE, "queries.npz")
     np.savez_compressed(path, **out)
     print(f"-> {path} ({os.path.getsize(path)} bytes)")

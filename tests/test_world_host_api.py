@@ -1,0 +1,42 @@
+"""Host-side parts of the World API that need no step: the Body frame
+helpers (body.py:662-708) and the World flags (world.py:139-181, 447-468),
+pinned against the reference's own results for the same API calls
+(tests/golden/api_frames.py, recorded by tests/golden/make_golden_queries.py).
+Bit-exact: the helpers are single Transform / Mat22 products in the
+reference's operation order."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import pypybox2d_gb300 as b2
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+sys.path.insert(0, GOLDEN)
+import api_frames  # noqa: E402
+
+
+def test_body_frame_helpers_match_reference():
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    rows, flags = api_frames.rows(b2)
+    want = d["frames"]
+    got = np.array(rows, dtype=np.float64)
+    assert got.shape == want.shape
+    bad = got != want
+    assert not bad.any(), f"frame helper differs at {np.argwhere(bad)[0]}: {got[bad][0]!r} vs {want[bad][0]!r}"
+    assert [int(f) for f in flags] == list(d["frame_world_flags"])
+
+
+def test_world_flags_round_trip():
+    w = api_frames.build(b2)
+    for name in ("warm_starting", "continuous_physics", "allow_sleep", "auto_clear_forces"):
+        assert getattr(w, name) is True
+        setattr(w, name, False)
+        assert getattr(w, name) is False
+        setattr(w, name, True)
+    assert w.sub_stepping is False
+    with pytest.raises(NotImplementedError):
+        w.sub_stepping = True
+    body = w.bodies[1]
+    assert body.allow_sleep == body.sleeping_allowed
