@@ -2,4 +2,4 @@
 World.step hot path behind the reference's World/Body/Fixture API."""
 
 from .shapes import Circle, Edge, Loop, Polygon, Shape  # noqa: E402,F401
-from .world import Body, Contact, ContactManager, EventContact, Fixture, LockedError, Vec2, World, WorldBatch  # noqa: E402,F401
+from .world import Body, Contact, ContactManager, EventContact, Fixture, LockedError, MassData, Vec2, World, WorldBatch  # noqa: E402,F401

@@ -83,6 +83,16 @@ class Vec2(tuple):
         return f"Vec2({self[0]:g}, {self[1]:g})"
 
 
+class MassData:
+    """common.py MassData: mass, centre (local) and rotational inertia I."""
+
+    def __init__(self, mass=0.0, center=(0.0, 0.0), I=0.0):
+        self.mass, self.center, self.I = float(mass), Vec2(*center), float(I)
+
+    def __repr__(self):
+        return f"MassData(mass={self.mass!r}, center={tuple(self.center)!r}, I={self.I!r})"
+
+
 class Fixture:
     """fixture.py:43-71: a shape with its material and filter data."""
 
@@ -195,6 +205,14 @@ class Body:
     @property
     def mass(self):
         return float(self._rec()["mass"])
+
+    @property
+    def mass_data(self):
+        """body.py mass_data: the mass, the rotational inertia about the body
+        origin and the local centre of mass."""
+        r = self._rec()
+        cx, cy = float(r["lcx"]), float(r["lcy"])
+        return MassData(float(r["mass"]), Vec2(cx, cy), float(r["I"]) + float(r["mass"]) * (cx * cx + cy * cy))
 
     @property
     def inertia(self):

@@ -5,7 +5,8 @@ tests/test_world_batch.py (no step: host records only).
 Returns one row per (body, probe point): the body's get_world_point,
 get_world_vector, get_local_point, get_local_vector,
 get_linear_velocity_from_world_point and
-get_linear_velocity_from_local_point of the probe, and the World flags."""
+get_linear_velocity_from_local_point of the probe and its mass_data, and
+the World flags."""
 
 PROBES = ((0.0, 0.0), (1.25, -0.5), (-3.0, 2.75), (0.1, 0.3))
 
@@ -31,6 +32,8 @@ def rows(b2):
             vals = (body.get_world_point(p), body.get_world_vector(p), body.get_local_point(p),
                     body.get_local_vector(p), body.get_linear_velocity_from_world_point(p),
                     body.get_linear_velocity_from_local_point(p))
-            out.append([float(c) for v in vals for c in (v[0], v[1])])
+            md = body.mass_data
+            out.append([float(c) for v in vals for c in (v[0], v[1])] +
+                       [float(md.mass), float(md.I), float(md.center[0]), float(md.center[1])])
     flags = [world.warm_starting, world.continuous_physics, world.allow_sleep, world.auto_clear_forces]
     return out, flags
