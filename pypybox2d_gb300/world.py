@@ -631,6 +631,26 @@ class World:
     def auto_clear_forces(self, v):
         self._set_flag(abi.W_AUTO_CLEAR_FORCES, v)
 
+    @staticmethod
+    def default_contact_filter(filter_a, filter_b):
+        """world.py:958-970, the rule the kernels apply to every new pair:
+        a shared non-zero group decides by its sign, otherwise each
+        fixture's mask must take the other's category."""
+        ga, gb = filter_a.group_index, filter_b.group_index
+        if ga == gb and ga != 0:
+            return ga > 0
+        return (filter_a.mask_bits & filter_b.category_bits) != 0 and (filter_a.category_bits & filter_b.mask_bits) != 0
+
+    @property
+    def contact_filter(self):
+        """world.py:123-136; only the default filter runs inside the GPU step."""
+        return None
+
+    @contact_filter.setter
+    def contact_filter(self, fcn):
+        if fcn is not None:
+            raise NotImplementedError("a custom contact filter cannot run inside the GPU step")
+
     @property
     def sub_stepping(self):
         return False

@@ -40,3 +40,22 @@ def test_world_flags_round_trip():
         w.sub_stepping = True
     body = w.bodies[1]
     assert body.allow_sleep == body.sleeping_allowed
+
+
+def test_default_contact_filter():
+    F = b2.Fixture
+    cases = [
+        (F(group_index=2), F(group_index=2), True),        # same positive group: always
+        (F(group_index=-3), F(group_index=-3), False),     # same negative group: never
+        (F(group_index=-3, category_bits=1, mask_bits=1), F(group_index=4, category_bits=1, mask_bits=1), True),
+        (F(category_bits=0x2, mask_bits=0x1), F(category_bits=0x1, mask_bits=0x2), True),
+        (F(category_bits=0x2, mask_bits=0x4), F(category_bits=0x1, mask_bits=0x2), False),
+        (F(category_bits=0x2, mask_bits=0x1), F(category_bits=0x1, mask_bits=0x4), False),
+    ]
+    for a, b, want in cases:
+        assert b2.World.default_contact_filter(a, b) is want
+    w = b2.World()
+    assert w.contact_filter is None
+    w.contact_filter = None
+    with pytest.raises(NotImplementedError):
+        w.contact_filter = lambda a, b: True
