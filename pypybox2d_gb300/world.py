@@ -435,6 +435,29 @@ class Body:
         fx = Fixture(shape, friction, restitution, density, category_bits, mask_bits, group_index, sensor, user_data)
         return self.attach_fixture(fx)
 
+    def create_fixtures(self, shape_list, fixture=None, friction=0.2, restitution=0.0, density=0.0,
+                        category_bits=0x0001, mask_bits=0xFFFF, group_index=0, sensor=False):
+        """body.py create_fixtures: one fixture per shape, with the material
+        and filter of `fixture` when given."""
+        if isinstance(shape_list, Shape):
+            shape_list = [shape_list]
+        if fixture is not None:
+            friction, restitution, density = fixture.friction, fixture.restitution, fixture.density
+            category_bits, mask_bits, group_index = fixture.category_bits, fixture.mask_bits, fixture.group_index
+            sensor = fixture.sensor
+        for shape in shape_list:
+            self.create_fixture(shape, friction, restitution, density, category_bits, mask_bits, group_index, sensor)
+
+    def destroy_fixture(self, fixture):
+        """body.py destroy_fixture: the fixture leaves the body, its contacts
+        are destroyed (touching ones reported to end_contact,
+        contact_manager.py:167-168), its proxy leaves the broad phase and
+        the body's mass data is reset."""
+        self._world._check_unlocked()
+        if fixture._body is not self or fixture not in self.fixtures:
+            raise ValueError("This fixture does not belong to this body")
+        self._world._destroy_fixture(self, fixture)
+
     def attach_fixture(self, fixture):
         self._world._check_unlocked()
         if fixture._body is not None:
@@ -998,6 +1021,44 @@ class World:
         self._M = np.concatenate([M, np.array([pos], np.int32)]).astype(np.int32)
         fixture._body, fixture._slot = body, len(body.fixtures)
         body.fixtures.append(fixture)
+
+    def _destroy_fixture(self, body, fixture):
+        self._structural()
+        bi = body._index
+        k = body.fixtures.index(fixture)
+        B, F, C, M = self._B, self._F, self._C, self._M
+        fi = int(B[bi]["fixture_start"]) + k
+        hit = (C["fixture_a"] == fi) | (C["fixture_b"] == fi)
+        if self.contact_manager.end_contact is not None:
+            for c in C[hit]:
+                if int(c["flags"]) & abi.C_TOUCHING:
+                    self.contact_manager.end_contact(EventContact(self._fixture_at(int(c["fixture_a"])),
+                                                                  self._fixture_at(int(c["fixture_b"])), False))
+        C = C[~hit].copy()
+        for key in ("fixture_a", "fixture_b"):
+            C[key] = np.where(C[key] > fi, C[key] - 1, C[key])
+        M = M[M != fi]
+        M = np.where(M > fi, M - 1, M).astype(np.int32)
+        F = np.delete(F, fi)
+        B["fixture_count"][bi] -= 1
+        B["fixture_start"] = np.where(np.arange(len(B)) > bi, B["fixture_start"] - 1, B["fixture_start"])
+        # the construction-time body: current state, fixture gone, mass data reset
+        b = self._sb.bodies[bi]
+        _load_body_state(b, B[bi])
+        b.fixtures.pop(k)
+        if k < len(b.aabbs):
+            b.aabbs.pop(k)
+        self._sb.moves = [(bb, kk - 1 if (bb == bi and kk > k) else kk) for (bb, kk) in self._sb.moves
+                          if not (bb == bi and kk == k)]
+        b.reset_mass_data()
+        rb, _ = self._sb.body_records(bi)
+        for key in ("lcx", "lcy", "c0x", "c0y", "cx", "cy", "vx", "vy", "mass", "inv_mass", "I", "inv_I"):
+            B[bi][key] = rb[key]
+        self._B, self._F, self._C, self._M = B, F, C, M
+        body.fixtures.pop(k)
+        fixture._body, fixture._slot = None, -1
+        for j, f in enumerate(body.fixtures):
+            f._slot = j
 
     def _set_transform(self, bi, pos, angle):
         """body.py:_transform_updated: new transform and sweep; the fixtures

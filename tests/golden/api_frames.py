@@ -37,3 +37,30 @@ def rows(b2):
                        [float(md.mass), float(md.I), float(md.center[0]), float(md.center[1])])
     flags = [world.warm_starting, world.continuous_physics, world.allow_sleep, world.auto_clear_forces]
     return out, flags
+
+
+def destroy_rows(b2, on_world=lambda world: None):
+    """create_fixtures on a dynamic body, then destroy_fixture twice: the
+    body's mass data and fixture count after each call (and the world)."""
+    world = build(b2)
+    on_world(world)
+    body = world.bodies[2]
+    body.create_fixtures([b2.Polygon(box=(0.3, 0.2)), b2.Circle(radius=0.25, position=(0.4, -0.1))], density=3.0,
+                         friction=0.7)
+    out = []
+
+    def record():
+        md = body.mass_data
+        out.append([float(len(body.fixtures)), float(md.mass), float(md.I), float(md.center[0]),
+                    float(md.center[1]), float(body.world_center[0]), float(body.world_center[1]),
+                    float(body.linear_velocity[0]), float(body.linear_velocity[1])])
+
+    record()
+    body.destroy_fixture(body.fixtures[0])
+    record()
+    body.destroy_fixture(body.fixtures[1])
+    record()
+    return out, world
+
+
+STEPS_AFTER_DESTROY = 40

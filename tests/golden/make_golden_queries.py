@@ -117,6 +117,13 @@ def main():
     frame_rows, flags = api_frames.rows(b2)
     out["frames"] = np.array(frame_rows, dtype=np.float64)
     out["frame_world_flags"] = np.array(flags, dtype=np.int32)
+    rows, world = api_frames.destroy_rows(b2, on_world=mg.pair_order_hook)
+    out["destroy_fixture"] = np.array(rows, dtype=np.float64)
+    for _ in range(api_frames.STEPS_AFTER_DESTROY):
+        world.step(1.0 / 60, 8, 3)
+    W2, B2, F2, C2 = mg.export_world(world, b2)
+    out["destroy_fixture_bodies"] = B2
+    out["destroy_fixture_contacts"] = C2
     path = os.path.join(HERE, "queries.npz")
     np.savez_compressed(path, **out)
     print(f"-> {path} ({os.path.getsize(path)} bytes)")

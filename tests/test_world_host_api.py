@@ -59,3 +59,43 @@ def test_default_contact_filter():
     w.contact_filter = None
     with pytest.raises(NotImplementedError):
         w.contact_filter = lambda a, b: True
+
+
+def test_create_fixtures_and_destroy_fixture_match_reference():
+    """create_fixtures, then destroy_fixture twice on a dynamic body: fixture
+    count, mass data, centre of mass and the velocity shift of
+    reset_mass_data (body.py:587-641) after each call, bit for bit."""
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    rows, world = api_frames.destroy_rows(b2)
+    got = np.array(rows, dtype=np.float64)
+    want = d["destroy_fixture"]
+    assert got.shape == want.shape
+    bad = got != want
+    assert not bad.any(), f"differs at {np.argwhere(bad)[0]}: {got[bad][0]!r} vs {want[bad][0]!r}"
+    w = api_frames.build(b2)
+    other = w.bodies[1].fixtures[0]
+    with pytest.raises(ValueError):
+        w.bodies[2].destroy_fixture(other)
+
+
+def test_records_after_destroy_fixture_step_like_the_reference():
+    """The host records the API leaves after create_fixtures / destroy_fixture
+    (bodies, fixtures, fat AABBs, the pending move buffer) stepped by the
+    CPU restatement reproduce the reference's world after the same calls and
+    the same steps, bit for bit: they are what the next GPU step uploads."""
+    import oracle_lib
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    _, w = api_frames.destroy_rows(b2)
+    B, F, C, M = w._B, w._F, w._C, w._M
+    assert list(B["fixture_start"]) == list(np.concatenate([[0], np.cumsum(B["fixture_count"])[:-1]]))
+    W = w._sb.world_record(len(B), len(F), len(M))
+    W["contact_count"] = len(C)
+    W["inv_dt0"] = w._inv_dt0
+    orc = oracle_lib.OracleWorld(W, B, F, contacts=C if len(C) else None, libm=True, moves=M)
+    for _ in range(api_frames.STEPS_AFTER_DESTROY):
+        orc.step(1 / 60, 8, 3)
+    want = d["destroy_fixture_bodies"]
+    got = orc.bodies()
+    for name in ("cx", "cy", "a", "vx", "vy", "w", "flags", "sleep_time"):
+        assert np.array_equal(got[name], want[name]), f"bodies.{name}"
+    assert len(orc.contacts()) == len(d["destroy_fixture_contacts"])
