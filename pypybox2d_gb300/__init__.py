@@ -1,5 +1,5 @@
 """pypybox2d_gb300 -- GB300 (sm_103a) implementation of pypybox2d's
 World.step hot path behind the reference's World/Body/Fixture API."""
 
-from .shapes import Circle, Edge, Loop, Polygon, Shape  # noqa: E402,F401
-from .world import Body, Contact, ContactManager, EventContact, Fixture, LockedError, MassData, Vec2, World, WorldBatch  # noqa: E402,F401
+from .shapes import Circle, Edge, Loop, MassData, Polygon, Shape  # noqa: E402,F401
+from .world import Body, Contact, ContactManager, EventContact, Fixture, LockedError, Vec2, World, WorldBatch  # noqa: E402,F401

@@ -35,7 +35,7 @@ import numpy as np
 
 from . import abi
 from .scenes import AABB_EXTENSION, SceneBuilder, _Body
-from .shapes import Circle, Edge, Loop, Polygon, Shape
+from .shapes import Circle, Edge, Loop, MassData, Polygon, Shape
 
 
 class LockedError(RuntimeError):
@@ -81,16 +81,6 @@ class Vec2(tuple):
 
     def __repr__(self):
         return f"Vec2({self[0]:g}, {self[1]:g})"
-
-
-class MassData:
-    """common.py MassData: mass, centre (local) and rotational inertia I."""
-
-    def __init__(self, mass=0.0, center=(0.0, 0.0), I=0.0):
-        self.mass, self.center, self.I = float(mass), Vec2(*center), float(I)
-
-    def __repr__(self):
-        return f"MassData(mass={self.mass!r}, center={tuple(self.center)!r}, I={self.I!r})"
 
 
 class Fixture:
@@ -213,6 +203,36 @@ class Body:
         r = self._rec()
         cx, cy = float(r["lcx"]), float(r["lcy"])
         return MassData(float(r["mass"]), Vec2(cx, cy), float(r["I"]) + float(r["mass"]) * (cx * cx + cy * cy))
+
+    @mass_data.setter
+    def mass_data(self, md):
+        """body.py mass_data setter: override the fixtures' mass data of a
+        dynamic body; the centre of mass moves and its velocity follows."""
+        self._world._check_unlocked()
+        if self.type != Body.DYNAMIC:
+            return
+        r = self._edit()
+        mass = float(md.mass)
+        if mass <= 0.0:
+            mass = 1.0
+        inv_mass, I, invI = 1.0 / mass, 0.0, 0.0
+        cx, cy = float(md.center[0]), float(md.center[1])
+        if float(md.I) > 0.0 and not (int(r["flags"]) & abi.BODY_FIXED_ROTATION):
+            I = float(md.I) - mass * (cx * cx + cy * cy)
+            invI = 1.0 / I
+        r["mass"], r["inv_mass"], r["I"], r["inv_I"] = mass, inv_mass, I, invI
+        ox, oy = float(r["cx"]), float(r["cy"])
+        r["lcx"], r["lcy"] = cx, cy
+        c0x = r["px"] + r["qc"] * cx + (-r["qs"]) * cy          # xf * local_center
+        c0y = r["py"] + r["qs"] * cx + r["qc"] * cy
+        r["c0x"], r["c0y"], r["cx"], r["cy"] = c0x, c0y, c0x, c0y
+        w = float(r["w"])                                       # v += cross(w, c - old_c)
+        r["vx"], r["vy"] = r["vx"] + (-w * (c0y - oy)), r["vy"] + w * (c0x - ox)
+
+    def reset_mass_data(self):
+        """body.py:587-641: mass data from the fixtures' shapes and densities."""
+        self._world._check_unlocked()
+        self._world._reset_mass_data(self)
 
     @property
     def inertia(self):
@@ -1021,6 +1041,16 @@ class World:
         self._M = np.concatenate([M, np.array([pos], np.int32)]).astype(np.int32)
         fixture._body, fixture._slot = body, len(body.fixtures)
         body.fixtures.append(fixture)
+
+    def _reset_mass_data(self, body):
+        bi = body._index
+        r = self._body_record(bi, write=True)
+        b = self._sb.bodies[bi]
+        _load_body_state(b, r)
+        b.reset_mass_data()
+        rb, _ = self._sb.body_records(bi)
+        for key in ("lcx", "lcy", "c0x", "c0y", "cx", "cy", "vx", "vy", "mass", "inv_mass", "I", "inv_I"):
+            r[key] = rb[key]
 
     def _destroy_fixture(self, body, fixture):
         self._structural()

@@ -64,3 +64,30 @@ def destroy_rows(b2, on_world=lambda world: None):
 
 
 STEPS_AFTER_DESTROY = 40
+
+
+def mass_rows(b2, on_world=lambda world: None):
+    """mass_data overrides (a normal one, one with zero mass and inertia) and
+    reset_mass_data: each body's mass data, centre and velocity after each
+    call (and the world)."""
+    world = build(b2)
+    on_world(world)
+    MassData = b2.shapes.MassData
+    out = []
+
+    def record(body):
+        md = body.mass_data
+        out.append([float(md.mass), float(md.I), float(md.center[0]), float(md.center[1]),
+                    float(body.world_center[0]), float(body.world_center[1]),
+                    float(body.linear_velocity[0]), float(body.linear_velocity[1])])
+
+    a, b, c = world.bodies[2], world.bodies[3], world.bodies[0]
+    a.mass_data = MassData(mass=2.5, center=(0.1, -0.2), I=0.8)
+    record(a)
+    b.mass_data = MassData(mass=0.0, center=(0.05, 0.05), I=0.0)
+    record(b)
+    c.mass_data = MassData(mass=3.0, center=(1.0, 1.0), I=2.0)     # static: unchanged
+    record(c)
+    b.reset_mass_data()
+    record(b)
+    return out, world

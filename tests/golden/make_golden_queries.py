@@ -124,6 +124,11 @@ def main():
     W2, B2, F2, C2 = mg.export_world(world, b2)
     out["destroy_fixture_bodies"] = B2
     out["destroy_fixture_contacts"] = C2
+    rows, world = api_frames.mass_rows(b2, on_world=mg.pair_order_hook)
+    out["mass_data"] = np.array(rows, dtype=np.float64)
+    for _ in range(api_frames.STEPS_AFTER_DESTROY):
+        world.step(1.0 / 60, 8, 3)
+    out["mass_data_bodies"] = mg.export_world(world, b2)[1]
     path = os.path.join(HERE, "queries.npz")
     np.savez_compressed(path, **out)
     print(f"-> {path} ({os.path.getsize(path)} bytes)")

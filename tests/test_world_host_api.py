@@ -99,3 +99,24 @@ def test_records_after_destroy_fixture_step_like_the_reference():
     for name in ("cx", "cy", "a", "vx", "vy", "w", "flags", "sleep_time"):
         assert np.array_equal(got[name], want[name]), f"bodies.{name}"
     assert len(orc.contacts()) == len(d["destroy_fixture_contacts"])
+
+
+def test_mass_data_setter_and_reset_match_reference():
+    """mass_data overrides and reset_mass_data (body.py:575-641), then 40
+    steps of the restatement on the records left behind, against the
+    reference after the same calls and steps, bit for bit."""
+    import oracle_lib
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    rows, w = api_frames.mass_rows(b2)
+    got = np.array(rows, dtype=np.float64)
+    want = d["mass_data"]
+    bad = got != want
+    assert got.shape == want.shape and not bad.any(), f"differs at {np.argwhere(bad)[:3].tolist()}"
+    B, F, C, M = w._B, w._F, w._C, w._M
+    W = w._sb.world_record(len(B), len(F), len(M))
+    orc = oracle_lib.OracleWorld(W, B, F, contacts=None, libm=True, moves=M)
+    for _ in range(api_frames.STEPS_AFTER_DESTROY):
+        orc.step(1 / 60, 8, 3)
+    want_b, got_b = d["mass_data_bodies"], orc.bodies()
+    for name in ("cx", "cy", "a", "vx", "vy", "w", "mass", "I", "lcx", "lcy"):
+        assert np.array_equal(got_b[name], want_b[name]), f"bodies.{name}"
