@@ -142,6 +142,18 @@ class Body:
     def type(self):
         return int(self._rec()["type"])
 
+    @type.setter
+    def type(self, t):
+        """body.py type setter: mass data reset for the new type, a static
+        body stops, the body wakes, forces clear, and its fixtures are
+        refiltered (contacts flagged for filtering, proxies touched)."""
+        self._world._check_unlocked()
+        if t == self.type:
+            return
+        if t not in (Body.STATIC, Body.DYNAMIC, Body.KINEMATIC):
+            raise ValueError("Invalid body type")
+        self._world._set_type(self, int(t))
+
     @property
     def static(self):
         return self.type == Body.STATIC
@@ -292,6 +304,10 @@ class Body:
     def sleeping(self):
         return not self.awake
 
+    @sleeping.setter
+    def sleeping(self, sleeping):
+        self.awake = not sleeping
+
     @property
     def bullet(self):
         return bool(self._rec()["flags"] & abi.BODY_BULLET)
@@ -321,6 +337,16 @@ class Body:
     @property
     def fixed_rotation(self):
         return bool(self._rec()["flags"] & abi.BODY_FIXED_ROTATION)
+
+    @fixed_rotation.setter
+    def fixed_rotation(self, flag):
+        """body.py fixed_rotation setter: the flag, then reset_mass_data."""
+        r = self._edit()
+        if flag:
+            r["flags"] |= abi.BODY_FIXED_ROTATION
+        else:
+            r["flags"] &= np.uint32(0xFFFFFFFF ^ abi.BODY_FIXED_ROTATION)
+        self._world._reset_mass_data(self)
 
     @property
     def linear_damping(self):
@@ -1052,6 +1078,33 @@ class World:
         for key in ("lcx", "lcy", "c0x", "c0y", "cx", "cy", "vx", "vy", "mass", "inv_mass", "I", "inv_I"):
             r[key] = rb[key]
 
+    def _set_type(self, body, t):
+        self._structural()
+        bi = body._index
+        B, C = self._B, self._C
+        r = B[bi]
+        r["type"] = t
+        b = self._sb.bodies[bi]
+        _load_body_state(b, r)
+        b.type = t
+        b.reset_mass_data()
+        rb, _ = self._sb.body_records(bi)
+        for key in ("lcx", "lcy", "c0x", "c0y", "cx", "cy", "vx", "vy", "mass", "inv_mass", "I", "inv_I"):
+            r[key] = rb[key]
+        if t == Body.STATIC:
+            r["vx"] = r["vy"] = r["w"] = 0.0
+        if not int(r["flags"]) & abi.BODY_AWAKE:
+            r["sleep_time"] = 0.0
+        r["flags"] |= abi.BODY_AWAKE
+        r["fx"] = r["fy"] = r["torque"] = 0.0
+        # fixture._refilter (fixture.py:269-285): flag the fixtures' contacts,
+        # touch their proxies (they join the move buffer)
+        f0, nfix = int(r["fixture_start"]), int(r["fixture_count"])
+        mine = lambda x: (x >= f0) & (x < f0 + nfix)   # noqa: E731
+        C["flags"] = np.where(mine(C["fixture_a"]) | mine(C["fixture_b"]), C["flags"] | abi.C_FILTER, C["flags"])
+        self._M = np.concatenate([self._M, np.arange(f0, f0 + nfix, dtype=np.int32)]).astype(np.int32)
+        self._sb.moves.extend((bi, k) for k in range(nfix))
+
     def _destroy_fixture(self, body, fixture):
         self._structural()
         bi = body._index
@@ -1144,6 +1197,7 @@ def _load_body_state(b: _Body, r):
     b.sleep_time = float(r["sleep_time"])
     fl = int(r["flags"])
     b.awake, b.allow_sleep, b.bullet = bool(fl & abi.BODY_AWAKE), bool(fl & abi.BODY_ALLOW_SLEEP), bool(fl & abi.BODY_BULLET)
+    b.fixed_rotation = bool(fl & abi.BODY_FIXED_ROTATION)
 
 
 def _concat_worlds(recs):

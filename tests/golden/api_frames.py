@@ -91,3 +91,24 @@ def mass_rows(b2, on_world=lambda world: None):
     b.reset_mass_data()
     record(b)
     return out, world
+
+
+def type_rows(b2, on_world=lambda world: None):
+    """fixed_rotation, sleeping and type setters: each changed body's type,
+    mass data, velocity and sleep state afterwards (and the world)."""
+    world = build(b2)
+    on_world(world)
+    bodies = world.bodies
+    bodies[1].fixed_rotation = True
+    bodies[2].sleeping = True
+    bodies[3].type = b2.Body.STATIC
+    bodies[4].type = b2.Body.KINEMATIC
+    bodies[5].type = b2.Body.KINEMATIC
+    bodies[5].type = b2.Body.DYNAMIC
+    out = []
+    for body in bodies:
+        md = body.mass_data
+        out.append([float(body.type), float(md.mass), float(md.I), float(md.center[0]), float(md.center[1]),
+                    float(body.linear_velocity[0]), float(body.linear_velocity[1]), float(body.angular_velocity),
+                    float(body.awake), float(body.fixed_rotation)])
+    return out, world

@@ -129,6 +129,12 @@ def main():
     for _ in range(api_frames.STEPS_AFTER_DESTROY):
         world.step(1.0 / 60, 8, 3)
     out["mass_data_bodies"] = mg.export_world(world, b2)[1]
+    rows, world = api_frames.type_rows(b2, on_world=mg.pair_order_hook)
+    out["body_setters"] = np.array(rows, dtype=np.float64)
+    for _ in range(api_frames.STEPS_AFTER_DESTROY):
+        world.step(1.0 / 60, 8, 3)
+    _, B2, _, C2 = mg.export_world(world, b2)
+    out["body_setters_bodies"], out["body_setters_contacts"] = B2, C2
     path = os.path.join(HERE, "queries.npz")
     np.savez_compressed(path, **out)
     print(f"-> {path} ({os.path.getsize(path)} bytes)")

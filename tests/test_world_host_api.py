@@ -120,3 +120,24 @@ def test_mass_data_setter_and_reset_match_reference():
     want_b, got_b = d["mass_data_bodies"], orc.bodies()
     for name in ("cx", "cy", "a", "vx", "vy", "w", "mass", "I", "lcx", "lcy"):
         assert np.array_equal(got_b[name], want_b[name]), f"bodies.{name}"
+
+
+def test_type_fixed_rotation_and_sleeping_setters_match_reference():
+    """Body.type (with mass reset, wake, refilter), fixed_rotation and
+    sleeping setters, then 40 restated steps on the records they leave,
+    against the reference after the same calls and steps, bit for bit."""
+    import oracle_lib
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    rows, w = api_frames.type_rows(b2)
+    got, want = np.array(rows, dtype=np.float64), d["body_setters"]
+    bad = got != want
+    assert got.shape == want.shape and not bad.any(), f"differs at {np.argwhere(bad)[:3].tolist()}"
+    B, F, C, M = w._B, w._F, w._C, w._M
+    W = w._sb.world_record(len(B), len(F), len(M))
+    orc = oracle_lib.OracleWorld(W, B, F, contacts=None, libm=True, moves=M)
+    for _ in range(api_frames.STEPS_AFTER_DESTROY):
+        orc.step(1 / 60, 8, 3)
+    want_b, got_b = d["body_setters_bodies"], orc.bodies()
+    for name in ("type", "cx", "cy", "a", "vx", "vy", "w", "flags", "sleep_time", "mass", "I"):
+        assert np.array_equal(got_b[name], want_b[name]), f"bodies.{name}"
+    assert len(orc.contacts()) == len(d["body_setters_contacts"])
