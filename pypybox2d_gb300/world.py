@@ -90,13 +90,89 @@ class Fixture:
                  mask_bits=0xFFFF, group_index=0, sensor=False, user_data=None, body=None):
         if isinstance(shape, Loop):
             raise NotImplementedError("Loop shapes are not supported by the GPU world step")
-        self._shape = shape
-        self.friction, self.restitution, self.density = float(friction), float(restitution), float(density)
-        self.category_bits, self.mask_bits, self.group_index = category_bits, mask_bits, group_index
-        self.sensor = bool(sensor)
-        self.user_data = user_data
         self._body = None
         self._slot = -1
+        self._shape = shape
+        self._friction, self._restitution, self._density = float(friction), float(restitution), float(density)
+        self._category_bits, self._mask_bits, self._group_index = category_bits, mask_bits, group_index
+        self._sensor = bool(sensor)
+        self.user_data = user_data
+
+    # fixture.py:122-225: material and filter data.  On a fixture of a world
+    # the change reaches the world's fixture records (re-uploaded before the
+    # next step); the filter fields also refilter the fixture's contacts.
+    @property
+    def friction(self):
+        return self._friction
+
+    @friction.setter
+    def friction(self, v):
+        self._friction = float(v)
+        self._push()
+
+    @property
+    def restitution(self):
+        return self._restitution
+
+    @restitution.setter
+    def restitution(self, v):
+        self._restitution = float(v)
+        self._push()
+
+    @property
+    def density(self):
+        return self._density
+
+    @density.setter
+    def density(self, v):
+        if not math.isfinite(float(v)) or float(v) < 0:
+            raise ValueError("Invalid density")
+        self._density = float(v)
+        self._push()
+
+    @property
+    def sensor(self):
+        return self._sensor
+
+    @sensor.setter
+    def sensor(self, v):
+        if bool(v) != self._sensor:
+            if self._body is not None:
+                self._body.awake = True
+            self._sensor = bool(v)
+            self._push()
+
+    @property
+    def category_bits(self):
+        return self._category_bits
+
+    @category_bits.setter
+    def category_bits(self, v):
+        self._category_bits = v
+        self._push(refilter=True)
+
+    @property
+    def mask_bits(self):
+        return self._mask_bits
+
+    @mask_bits.setter
+    def mask_bits(self, v):
+        self._mask_bits = v
+        self._push(refilter=True)
+
+    @property
+    def group_index(self):
+        return self._group_index
+
+    @group_index.setter
+    def group_index(self, v):
+        self._group_index = v
+        self._push(refilter=True)
+
+    def _push(self, refilter=False):
+        body = self._body
+        if body is not None and body._world is not None:
+            body._world._set_fixture(self, refilter)
 
     def __copy__(self):
         return Fixture(self._shape, self.friction, self.restitution, self.density, self.category_bits,
@@ -1077,6 +1153,27 @@ class World:
         rb, _ = self._sb.body_records(bi)
         for key in ("lcx", "lcy", "c0x", "c0y", "cx", "cy", "vx", "vy", "mass", "inv_mass", "I", "inv_I"):
             r[key] = rb[key]
+
+    def _set_fixture(self, fixture, refilter):
+        """A fixture's material or filter changed: its record (and the
+        construction-time copy used by reset_mass_data) follow; with
+        `refilter`, fixture._refilter (fixture.py:269-285)."""
+        self._structural()
+        body = fixture._body
+        bi, k = body._index, fixture._slot
+        fi = int(self._B[bi]["fixture_start"]) + k
+        r = self._F[fi]
+        r["friction"], r["restitution"], r["density"] = fixture.friction, fixture.restitution, fixture.density
+        r["category_bits"], r["mask_bits"], r["group_index"] = fixture.category_bits, fixture.mask_bits, fixture.group_index
+        r["flags"] = (int(r["flags"]) | abi.FIX_SENSOR) if fixture.sensor else (int(r["flags"]) & ~abi.FIX_SENSOR)
+        sf = self._sb.bodies[bi].fixtures[k]
+        sf.friction, sf.restitution, sf.density = fixture.friction, fixture.restitution, fixture.density
+        sf.category, sf.mask, sf.group, sf.sensor = fixture.category_bits, fixture.mask_bits, fixture.group_index, fixture.sensor
+        if refilter:
+            C = self._C
+            C["flags"] = np.where((C["fixture_a"] == fi) | (C["fixture_b"] == fi), C["flags"] | abi.C_FILTER, C["flags"])
+            self._M = np.concatenate([self._M, np.array([fi], np.int32)]).astype(np.int32)
+            self._sb.moves.append((bi, k))
 
     def _set_type(self, body, t):
         self._structural()

@@ -112,3 +112,29 @@ def type_rows(b2, on_world=lambda world: None):
                     float(body.linear_velocity[0]), float(body.linear_velocity[1]), float(body.angular_velocity),
                     float(body.awake), float(body.fixed_rotation)])
     return out, world
+
+
+def fixture_rows(b2, on_world=lambda world: None):
+    """Fixture material and filter setters: friction, restitution, density
+    (then reset_mass_data), sensor, group index and mask bits; each body's
+    mass data afterwards (and the world)."""
+    world = build(b2)
+    on_world(world)
+    bodies = world.bodies
+    bodies[1].fixtures[0].friction = 0.95
+    bodies[2].fixtures[0].restitution = 0.6
+    bodies[3].fixtures[0].density = 4.0
+    bodies[3].reset_mass_data()
+    bodies[4].fixtures[0].sensor = True
+    bodies[0].fixtures[0].group_index = -2
+    bodies[5].fixtures[0].group_index = -2
+    bodies[1].fixtures[0].mask_bits = 0xFFFE
+    bodies[1].fixtures[0].category_bits = 0x0002
+    out = []
+    for body in bodies:
+        md = body.mass_data
+        f = body.fixtures[0]
+        out.append([float(md.mass), float(md.I), float(f.friction), float(f.restitution), float(f.density),
+                    float(f.sensor), float(f.group_index), float(f.mask_bits), float(f.category_bits),
+                    float(body.awake)])
+    return out, world

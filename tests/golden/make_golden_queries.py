@@ -135,6 +135,12 @@ def main():
         world.step(1.0 / 60, 8, 3)
     _, B2, _, C2 = mg.export_world(world, b2)
     out["body_setters_bodies"], out["body_setters_contacts"] = B2, C2
+    rows, world = api_frames.fixture_rows(b2, on_world=mg.pair_order_hook)
+    out["fixture_setters"] = np.array(rows, dtype=np.float64)
+    for _ in range(api_frames.STEPS_AFTER_DESTROY):
+        world.step(1.0 / 60, 8, 3)
+    _, B2, _, C2 = mg.export_world(world, b2)
+    out["fixture_setters_bodies"], out["fixture_setters_contacts"] = B2, C2
     path = os.path.join(HERE, "queries.npz")
     np.savez_compressed(path, **out)
     print(f"-> {path} ({os.path.getsize(path)} bytes)")

@@ -141,3 +141,28 @@ def test_type_fixed_rotation_and_sleeping_setters_match_reference():
     for name in ("type", "cx", "cy", "a", "vx", "vy", "w", "flags", "sleep_time", "mass", "I"):
         assert np.array_equal(got_b[name], want_b[name]), f"bodies.{name}"
     assert len(orc.contacts()) == len(d["body_setters_contacts"])
+
+
+def test_fixture_setters_match_reference():
+    """Fixture friction, restitution, density, sensor and filter setters
+    (fixture.py:122-225, refiltering on filter changes), then 40 restated
+    steps on the records they leave, against the reference: bodies and the
+    contacts (pairs, mixed friction and restitution, flags) bit for bit."""
+    import oracle_lib
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    rows, w = api_frames.fixture_rows(b2)
+    got, want = np.array(rows, dtype=np.float64), d["fixture_setters"]
+    bad = got != want
+    assert got.shape == want.shape and not bad.any(), f"differs at {np.argwhere(bad)[:3].tolist()}"
+    B, F, C, M = w._B, w._F, w._C, w._M
+    W = w._sb.world_record(len(B), len(F), len(M))
+    orc = oracle_lib.OracleWorld(W, B, F, contacts=None, libm=True, moves=M)
+    for _ in range(api_frames.STEPS_AFTER_DESTROY):
+        orc.step(1 / 60, 8, 3)
+    want_b, got_b = d["fixture_setters_bodies"], orc.bodies()
+    for name in ("cx", "cy", "a", "vx", "vy", "w", "flags", "mass", "I"):
+        assert np.array_equal(got_b[name], want_b[name]), f"bodies.{name}"
+    want_c, got_c = d["fixture_setters_contacts"], orc.contacts()
+    assert len(got_c) == len(want_c) and len(want_c) > 0
+    for name in ("fixture_a", "fixture_b", "friction", "restitution", "flags"):
+        assert np.array_equal(got_c[name], want_c[name]), f"contacts.{name}"
