@@ -607,9 +607,41 @@ class Contact:
     """A read-only view of one contact after a step (contact.py:55-87)."""
 
     def __init__(self, world, rec):
+        self._world = world
         self._rec = rec
         self.fixture_a = world._fixture_at(int(rec["fixture_a"]))
         self.fixture_b = world._fixture_at(int(rec["fixture_b"]))
+
+    child_index_a = property(lambda self: 0)
+    child_index_b = property(lambda self: 0)
+    body_a = property(lambda self: self.fixture_a.body)
+    body_b = property(lambda self: self.fixture_b.body)
+    shape_a = property(lambda self: self.fixture_a.shape)
+    shape_b = property(lambda self: self.fixture_b.shape)
+
+    def other_body(self, body):
+        """contact.py:91-98"""
+        return self.fixture_b.body if body is self.fixture_a.body else self.fixture_a.body
+
+    @property
+    def manifold(self):
+        """contact_util.py Manifold of this contact: type, local normal and
+        point, and its points (local point, impulses, feature id as the
+        (index_a, index_b, type_a, type_b) tuple of ClipVertex.id)."""
+        c = self._rec
+        n = int(c["m_point_count"])
+        pts = []
+        for k in range(n):
+            i = int(c["p_id"][k])
+            pts.append(ManifoldPoint(Vec2(c["p_lx"][k], c["p_ly"][k]), float(c["p_ni"][k]), float(c["p_ti"][k]),
+                                     (i & 255, (i >> 8) & 255, (i >> 16) & 255, (i >> 24) & 255)))
+        return Manifold(int(c["m_type"]), Vec2(c["m_lnx"], c["m_lny"]), Vec2(c["m_lpx"], c["m_lpy"]), pts)
+
+    @property
+    def world_manifold(self):
+        """contact_util.py:195-245: the manifold's normal (A to B) and world
+        points under the bodies' current transforms; (normal, [points])."""
+        return world_manifold(self._rec, self._world._B, self._world._F)
 
     touching = property(lambda self: bool(self._rec["flags"] & abi.C_TOUCHING))
     enabled = property(lambda self: bool(self._rec["flags"] & abi.C_ENABLED))
@@ -632,6 +664,31 @@ class Contact:
     @property
     def local_point(self):
         return Vec2(self._rec["m_lpx"], self._rec["m_lpy"])
+
+
+class ManifoldPoint:
+    """contact_util.py ManifoldPoint (read-only copy)."""
+    __slots__ = ("local_point", "normal_impulse", "tangent_impulse", "id")
+
+    def __init__(self, local_point, normal_impulse, tangent_impulse, id):
+        self.local_point, self.normal_impulse, self.tangent_impulse, self.id = local_point, normal_impulse, tangent_impulse, id
+
+
+class Manifold:
+    """contact_util.py Manifold (read-only copy): CIRCLES, FACE_A or FACE_B."""
+    CIRCLES, FACE_A, FACE_B = abi.M_CIRCLES, abi.M_FACE_A, abi.M_FACE_B
+    __slots__ = ("type", "local_normal", "local_point", "points")
+
+    def __init__(self, type, local_normal, local_point, points):
+        self.type, self.local_normal, self.local_point, self.points = type, local_normal, local_point, points
+
+    @property
+    def point_count(self):
+        return len(self.points)
+
+    @property
+    def used_points(self):
+        return list(self.points)
 
 
 class EventContact:
@@ -1264,6 +1321,63 @@ class World:
                 moved.append(start + k)
         if moved:
             self._M = np.concatenate([self._M, np.array(moved, np.int32)]).astype(np.int32)
+
+
+_EPSILON_SQR = 2.220446049250313e-16 ** 2       # settings.py EPSILON_SQR
+
+
+def _normalized(x, y):
+    """Vec2_normalized (vec2module.c): unchanged below FLT_EPSILON."""
+    length = math.sqrt(x * x + y * y)
+    if length < 1.1920928955078125e-07:
+        return x, y
+    inv = 1.0 / length
+    return x * inv, y * inv
+
+
+def world_manifold(c, B, F):
+    """WorldManifold (contact_util.py:195-245) of contact record `c` with the
+    body records `B` and fixture records `F` of its world (world-local
+    indices): (normal from A to B, [world points])."""
+    fa, fb = int(c["fixture_a"]), int(c["fixture_b"])
+    ra, rb = float(F[fa]["radius"]), float(F[fb]["radius"])
+    ba, bb = B[int(F[fa]["body"])], B[int(F[fb]["body"])]
+    n = int(c["m_point_count"])
+    if n == 0:
+        return Vec2(0.0, 0.0), []
+
+    def xmul(b, x, y):      # Transform_mul
+        return (b["px"] + b["qc"] * x + (-b["qs"]) * y, b["py"] + b["qs"] * x + b["qc"] * y)
+
+    def rmul(b, x, y):      # Mat22_mul
+        return (b["qc"] * x + (-b["qs"]) * y, b["qs"] * x + b["qc"] * y)
+
+    t = int(c["m_type"])
+    if t == abi.M_CIRCLES:
+        nx, ny = 1.0, 0.0
+        pa = xmul(ba, c["m_lpx"], c["m_lpy"])
+        pb = xmul(bb, c["p_lx"][0], c["p_ly"][0])
+        dx, dy = pa[0] - pb[0], pa[1] - pb[1]
+        if dx * dx + dy * dy > _EPSILON_SQR:
+            nx, ny = _normalized(pb[0] - pa[0], pb[1] - pa[1])
+        ca = (pa[0] + ra * nx, pa[1] + ra * ny)
+        cb = (pb[0] - rb * nx, pb[1] - rb * ny)
+        return Vec2(nx, ny), [Vec2(0.5 * (ca[0] + cb[0]), 0.5 * (ca[1] + cb[1]))]
+    face_a = t == abi.M_FACE_A
+    bp, bc, rp, rc = (ba, bb, ra, rb) if face_a else (bb, ba, rb, ra)
+    nx, ny = rmul(bp, c["m_lnx"], c["m_lny"])
+    plane = xmul(bp, c["m_lpx"], c["m_lpy"])
+    pts = []
+    for k in range(n):
+        clip = xmul(bc, c["p_lx"][k], c["p_ly"][k])
+        s = rp - ((clip[0] - plane[0]) * nx + (clip[1] - plane[1]) * ny)
+        c1 = (clip[0] + s * nx, clip[1] + s * ny)        # on the reference face's side
+        c2 = (clip[0] - rc * nx, clip[1] - rc * ny)
+        ca, cb = (c1, c2) if face_a else (c2, c1)
+        pts.append(Vec2(0.5 * (ca[0] + cb[0]), 0.5 * (ca[1] + cb[1])))
+    if not face_a:
+        nx, ny = -nx, -ny
+    return Vec2(nx, ny), pts
 
 
 def _box_of(aabb):

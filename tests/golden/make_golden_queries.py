@@ -101,6 +101,15 @@ def main():
             counts.append(len(ks))
             lists.extend(ks)
         out[f"{name}_world"], out[f"{name}_bodies"], out[f"{name}_fixtures"] = W, B, F
+        # Contact.world_manifold (contact_util.py:195-245) of every contact,
+        # in contact-list order: normal, two points (NaN where unused)
+        wm = np.full((len(C), 6), np.nan)
+        for i, c in enumerate(world.contact_manager.contacts):
+            m = c.world_manifold
+            wm[i, 0], wm[i, 1] = m.normal.x, m.normal.y
+            for k, p in enumerate(m.points):
+                wm[i, 2 + 2 * k], wm[i, 3 + 2 * k] = p.x, p.y
+        out[f"{name}_contacts"], out[f"{name}_world_manifolds"] = C, wm
         out[f"{name}_rays"] = np.array(rays, dtype=np.float64)
         out[f"{name}_hits"] = np.array(hits, dtype=[("fixture", "<i4"), ("px", "<f8"), ("py", "<f8"),
                                                     ("nx", "<f8"), ("ny", "<f8"), ("fraction", "<f8")])

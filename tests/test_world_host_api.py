@@ -166,3 +166,44 @@ def test_fixture_setters_match_reference():
     assert len(got_c) == len(want_c) and len(want_c) > 0
     for name in ("fixture_a", "fixture_b", "friction", "restitution", "flags"):
         assert np.array_equal(got_c[name], want_c[name]), f"contacts.{name}"
+
+
+@pytest.mark.parametrize("scene", ["mixed", "uneven"])
+def test_world_manifold_matches_reference(scene):
+    """Contact.world_manifold (contact_util.py:195-245: circles, face A and
+    face B manifolds) of every contact of two stepped reference worlds, from
+    the exported records, bit for bit."""
+    from pypybox2d_gb300.world import world_manifold
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    B, F, C, want = d[f"{scene}_bodies"], d[f"{scene}_fixtures"], d[f"{scene}_contacts"], d[f"{scene}_world_manifolds"]
+    types = set()
+    for i, c in enumerate(C):
+        normal, pts = world_manifold(c, B, F)
+        got = np.full(6, np.nan)
+        got[0], got[1] = normal[0], normal[1]
+        for k, p in enumerate(pts):
+            got[2 + 2 * k], got[3 + 2 * k] = p[0], p[1]
+        same = (got == want[i]) | (np.isnan(got) & np.isnan(want[i]))
+        assert same.all(), f"contact {i} (type {int(c['m_type'])}): {got} vs {want[i]}"
+        if int(c["m_point_count"]):
+            types.add(int(c["m_type"]))
+    assert types == {0, 1, 2} or scene == "uneven"
+
+
+def test_manifold_view_decodes_feature_ids():
+    from pypybox2d_gb300 import abi
+    from pypybox2d_gb300.world import Contact
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    C = d["mixed_contacts"]
+    c = next(r for r in C if r["m_point_count"] == 2)
+
+    class _W:            # the two fixture lookups a Contact makes
+        def _fixture_at(self, f):
+            return f
+    m = Contact(_W(), c).manifold
+    assert m.type == int(c["m_type"]) and m.point_count == 2
+    for k, p in enumerate(m.points):
+        i = int(c["p_id"][k])
+        assert p.id == (i & 255, (i >> 8) & 255, (i >> 16) & 255, i >> 24)
+        assert (p.local_point[0], p.local_point[1], p.normal_impulse) == (c["p_lx"][k], c["p_ly"][k], c["p_ni"][k])
+    assert m.type in (abi.M_CIRCLES, abi.M_FACE_A, abi.M_FACE_B)
