@@ -150,6 +150,15 @@ def main():
         world.step(1.0 / 60, 8, 3)
     _, B2, _, C2 = mg.export_world(world, b2)
     out["fixture_setters_bodies"], out["fixture_setters_contacts"] = B2, C2
+    # host-side edits between steps on a world with live contacts (api_edits.py)
+    import api_edits
+
+    def snap_edits(label, world):
+        _, B3, F3, C3 = mg.export_world(world, b2)
+        out[f"edits_{label}_bodies"], out[f"edits_{label}_aabb"], out[f"edits_{label}_contacts"] = B3, F3["aabb"].copy(), C3
+
+    _, end_log = api_edits.script(b2, snap_edits, on_world=mg.pair_order_hook)
+    out["edits_end_log"] = np.array(end_log, dtype=np.int32).reshape(-1, 2)
     path = os.path.join(HERE, "queries.npz")
     np.savez_compressed(path, **out)
     print(f"-> {path} ({os.path.getsize(path)} bytes)")

@@ -207,3 +207,41 @@ def test_manifold_view_decodes_feature_ids():
         assert p.id == (i & 255, (i >> 8) & 255, (i >> 16) & 255, i >> 24)
         assert (p.local_point[0], p.local_point[1], p.normal_impulse) == (c["p_lx"][k], c["p_ly"][k], c["p_ni"][k])
     assert m.type in (abi.M_CIRCLES, abi.M_FACE_A, abi.M_FACE_B)
+
+
+def test_host_edits_between_steps_match_reference():
+    """tests/golden/api_edits.py: fixture, filter, mass and body edits (and
+    a fixture destroyed while touching) between steps of a world with live
+    contacts, the World stepped by the libm build of the restatement:
+    bodies, fat AABBs, contacts and the end_contact calls equal the
+    reference's session bit for bit.  This checks the records every edit
+    leaves for the next device upload."""
+    import types
+    import api_edits
+    import oracle_lib
+
+    class OracleBackedWorld(b2.World):
+        def _make_batch(self, W, B, F, C, M):
+            return oracle_lib.OracleBatch(W, B, F, C, M, libm=True)
+
+    d = np.load(os.path.join(GOLDEN, "queries.npz"))
+    snaps = {}
+
+    def snap(label, world):
+        world._materialise()
+        snaps[label] = (world._B.copy(), world._F["aabb"].copy(), world._C.copy())
+
+    ns = types.SimpleNamespace(World=OracleBackedWorld, Body=b2.Body, shapes=b2.shapes)
+    _, log = api_edits.script(ns, snap)
+    assert tuple(snaps) == api_edits.SNAPS
+    for label, (B, aabb, C) in snaps.items():
+        want_b = d[f"edits_{label}_bodies"]
+        for name in want_b.dtype.names:
+            if not name.startswith("_pad"):
+                assert np.array_equal(B[name], want_b[name]), f"{label} bodies.{name}"
+        assert np.array_equal(aabb, d[f"edits_{label}_aabb"]), f"{label} fat AABBs"
+        want_c = d[f"edits_{label}_contacts"]
+        assert len(C) == len(want_c), f"{label} contact count"
+        for name in ("fixture_a", "fixture_b", "flags", "friction", "restitution", "m_point_count", "m_type"):
+            assert np.array_equal(C[name], want_c[name]), f"{label} contacts.{name}"
+    assert np.array_equal(np.array(log, dtype=np.int32).reshape(-1, 2), d["edits_end_log"])
