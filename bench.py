@@ -378,14 +378,19 @@ def main():
     elif not args.no_tune:
         import time
         t0 = time.time()
-        best, trials = batch.autotune(DT, VI, PI, steps_per_trial=args.tune_steps, stream=sh)
-        mode, threads = 0, 0          # steps take the tuned launch configuration
-        tune = {"best": best, "trials": len(trials), "steps_per_trial": args.tune_steps,
-                "seconds": round(time.time() - t0, 2),
-                "table": [[t["launch_mode"], t["block_threads"], t["pipe_bufs"], t["big_bodies"],
-                           round(t["ms_per_step"], 3)] for t in trials],
-                "columns": ["launch_mode", "block_threads", "pipe_bufs", "big_bodies", "ms_per_step"]}
-    cfg = batch.launch_config() if (tune or args.launch_config) else {"launch_mode": args.mode,
+        try:
+            best, trials = batch.autotune(DT, VI, PI, steps_per_trial=args.tune_steps, stream=sh)
+        except abi.GB2DError as ex:   # e.g. no device memory for the arena copy: keep --mode / --threads
+            tune = {"unavailable": str(ex)}
+        else:
+            mode, threads = 0, 0          # steps take the tuned launch configuration
+            tune = {"best": best, "trials": len(trials), "steps_per_trial": args.tune_steps,
+                    "seconds": round(time.time() - t0, 2),
+                    "table": [[t["launch_mode"], t["block_threads"], t["pipe_bufs"], t["big_bodies"],
+                               round(t["ms_per_step"], 3)] for t in trials],
+                    "columns": ["launch_mode", "block_threads", "pipe_bufs", "big_bodies", "ms_per_step"]}
+    tuned = tune is not None and "best" in tune
+    cfg = batch.launch_config() if (tuned or args.launch_config) else {"launch_mode": args.mode,
                                                                       "block_threads": args.threads,
                                                                       "pipe_bufs": 2, "big_bodies": 512}
     eff_mode = cfg["launch_mode"]
