@@ -987,6 +987,21 @@ class World:
         if events:
             self._replay(self._gpu.events(0))
 
+    # -- outside the GPU step: joints, controllers, loose bodies
+    def add_body(self, body):
+        """world.py:183-206 adds a Body built outside a world; bodies here are
+        made by create_*_body only."""
+        raise NotImplementedError("add_body: create bodies with World.create_*_body")
+
+    def _unsupported(self, *args, **kwargs):
+        raise NotImplementedError("joints and controllers are not part of the GPU world step")
+
+    add_joint = destroy_joint = _unsupported
+    create_distance_joint = create_friction_joint = create_gear_joint = _unsupported
+    create_mouse_joint = create_prismatic_joint = create_pulley_joint = _unsupported
+    create_revolute_joint = create_rope_joint = create_weld_joint = create_wheel_joint = _unsupported
+    add_controller = destroy_controller = create_buoyancy_controller = create_gravity_controller = _unsupported
+
     # -- queries
     def query_aabb(self, aabb, callback=None):
         """world.py:371-385: the fixtures whose broad-phase (fat) AABB

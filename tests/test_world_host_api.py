@@ -245,3 +245,13 @@ def test_host_edits_between_steps_match_reference():
         for name in ("fixture_a", "fixture_b", "flags", "friction", "restitution", "m_point_count", "m_type"):
             assert np.array_equal(C[name], want_c[name]), f"{label} contacts.{name}"
     assert np.array_equal(np.array(log, dtype=np.int32).reshape(-1, 2), d["edits_end_log"])
+
+
+def test_joints_and_controllers_raise_clearly():
+    w = b2.World()
+    for name in ("create_revolute_joint", "create_distance_joint", "create_weld_joint", "add_joint",
+                 "create_gravity_controller", "create_buoyancy_controller", "add_controller"):
+        with pytest.raises(NotImplementedError):
+            getattr(w, name)()
+    with pytest.raises(NotImplementedError):
+        w.add_body(object())
