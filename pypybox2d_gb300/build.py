@@ -1,9 +1,11 @@
 """In-tree build of libgb2d.so for sm_103a (nvcc, no cmake).
 
-Three translation units compile in parallel:
+Three translation units:
   gb_f64.cu  float64 step kernels, -fmad=false (bit-exact with the CPU restatement)
   gb_f32.cu  float32-bulk step kernels
   gb_api.cu  the C ABI (include/gb2d.h)
+The two precision units are each compiled once per part (-DGB_PART=k, see
+csrc/gb_kernels.cuh), so that 19 objects compile in parallel.
 """
 from __future__ import annotations
 
@@ -19,11 +21,13 @@ OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libgb2d.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-diag-suppress", "177,550"]
-UNITS = {
-    "gb_f64.cu": ["-fmad=false"],
-    "gb_f32.cu": [],
-    "gb_api.cu": [],
-}
+N_PARTS = 9
+# (source, extra flags, object)
+UNITS = [("gb_api.cu", [], "gb_api.o")] + [
+    (src, [*flags, f"-DGB_PART={k}"], src.replace(".cu", f"_p{k}.o"))
+    for src, flags in (("gb_f64.cu", ["-fmad=false"]), ("gb_f32.cu", []))
+    for k in range(N_PARTS)
+]
 
 
 def _nvcc() -> str:
@@ -53,8 +57,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = _nvcc()
 
     def compile_unit(item):
-        src, extra = item
-        obj = os.path.join(OUT, src.replace(".cu", ".o"))
+        src, extra, obj = item
+        obj = os.path.join(OUT, obj)
         cmd = [nvcc, *ARCH, *COMMON, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -63,8 +67,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(compile_unit, UNITS.items()))
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), max(2, os.cpu_count() or 2))) as ex:
+        objs = list(ex.map(compile_unit, UNITS))
     tmp = LIB + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

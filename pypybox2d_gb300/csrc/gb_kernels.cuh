@@ -9,6 +9,18 @@
 #include "gb_launch.h"
 #include "gb_query.cuh"
 
+// Each precision unit is compiled once per part, in parallel, and a part
+// instantiates only its own kernels: 0 batch-wide kernels, record
+// (un)packing, queries and the step orchestration; 1 and 8 the one-launch
+// step kernels (one CTA, one warp per world); 2-5 the per-world phase
+// kernels; 6-7 their cooperative-grid forms.  Without GB_PART every part is
+// built.
+#ifndef GB_PART
+#define GB_PART -1
+#endif
+#define GB_IN_PART(p) (GB_PART < 0 || GB_PART == (p))
+
+#if GB_IN_PART(0)
 namespace {
 
 __global__ void k_unpack_bodies(Batch<GB_REAL> B, const gb_body *src, int n) {
@@ -104,148 +116,219 @@ __global__ void k_refresh_toi_cand(Batch<GB_REAL> B, int n_slots) {
 }
 
 }  // namespace
+#endif  // GB_IN_PART(0)
 
-// CTAs of a cooperative launch of k_world_grid<PH>: all resident at once.
-template <int PH> static int grid_ctas() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_world_grid<GB_REAL, PH>, GB_GRID_THREADS, 0);
-        n = sms * (per_sm > 0 ? per_sm : 1);
-        if (n > GB_GRID_MAX_CTAS) n = GB_GRID_MAX_CTAS;
+// Launchers of the kernels that live in the other parts (declared here,
+// defined by the part that instantiates the kernel).
+template <int PH> cudaError_t gb_world_launch(int blocks, int threads, size_t smem, cudaStream_t st, const Batch<GB_REAL> &B,
+                                              const StepParams &sp, const int *worlds);
+template <int PH> cudaError_t gb_grid_launch(const Batch<GB_REAL> &B, const StepParams &sp, int wi, cudaStream_t st);
+#define GB_DECL_PHASE_LAUNCHERS(PH)                                                                                        \
+    template <> cudaError_t gb_world_launch<PH>(int, int, size_t, cudaStream_t, const Batch<GB_REAL> &, const StepParams &, \
+                                                const int *);                                                              \
+    template <> cudaError_t gb_grid_launch<PH>(const Batch<GB_REAL> &, const StepParams &, int, cudaStream_t);
+GB_DECL_PHASE_LAUNCHERS(PH_PAIRS0)
+GB_DECL_PHASE_LAUNCHERS(PH_COLLIDE2)
+GB_DECL_PHASE_LAUNCHERS(PH_ISLANDS)
+GB_DECL_PHASE_LAUNCHERS(PH_SOLVE)
+GB_DECL_PHASE_LAUNCHERS(PH_PAIRS)
+GB_DECL_PHASE_LAUNCHERS(PH_TOI2)
+#undef GB_DECL_PHASE_LAUNCHERS
+cudaError_t gb_cta_step_launch(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *worlds, int n_list,
+                               int threads, cudaStream_t st);
+cudaError_t gb_warp_step_launch(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *worlds, int n_list,
+                                int threads, cudaStream_t st);
+
+#if GB_IN_PART(1)
+cudaError_t gb_cta_step_launch(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *worlds, int n_list,
+                               int threads, cudaStream_t st) {
+    k_step_cta<GB_REAL><<<n_list, threads, 0, st>>>(B, sp, n_steps, worlds);
+    return cudaGetLastError();
+}
+#endif
+#if GB_IN_PART(8)
+cudaError_t gb_warp_step_launch(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *worlds, int n_list,
+                                int threads, cudaStream_t st) {
+    int wpc = threads / 32;
+    if (wpc < 1) wpc = 1;
+    const int blocks = (n_list + wpc - 1) / wpc;
+    k_step_warp<GB_REAL><<<blocks, wpc * 32, 0, st>>>(B, sp, n_steps, worlds, n_list);
+    return cudaGetLastError();
+}
+#endif
+
+// Per-world phase kernels: one CTA per listed world (the TOI event loop one
+// warp per world).  The solver's dynamic shared memory above the default
+// 48 KB is opted into once per size.
+#define GB_DEF_WORLD_LAUNCH(PH)                                                                                              \
+    template <> cudaError_t gb_world_launch<PH>(int blocks, int threads, size_t smem, cudaStream_t st, const Batch<GB_REAL> &B, \
+                                                const StepParams &sp, const int *worlds) {                                    \
+        if (blocks <= 0) return cudaSuccess;                                                                                 \
+        if constexpr (PH == PH_TOI2) {                                                                                       \
+            k_world_toi2<GB_REAL><<<blocks, 32, 0, st>>>(B, sp, worlds);                                                     \
+        } else {                                                                                                             \
+            if (smem > 48 * 1024) {                                                                                          \
+                static size_t opted = 0;                                                                                     \
+                if (smem > opted) {                                                                                          \
+                    cudaError_t e = cudaFuncSetAttribute(k_world<GB_REAL, PH>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                                         (int)smem);                                                         \
+                    if (e != cudaSuccess) return e;                                                                          \
+                    opted = smem;                                                                                            \
+                }                                                                                                            \
+            }                                                                                                                \
+            k_world<GB_REAL, PH><<<blocks, threads, smem, st>>>(B, sp, worlds);                                              \
+        }                                                                                                                    \
+        return cudaGetLastError();                                                                                           \
     }
-    return n;
-}
-template <int PH> static cudaError_t launch_grid(const Batch<GB_REAL> &B, const StepParams &sp, int wi, cudaStream_t st) {
-    Batch<GB_REAL> b = B;
-    StepParams p = sp;
-    int w = wi;
-    void *args[] = {&b, &p, &w};
-    return cudaLaunchCooperativeKernel((const void *)k_world_grid<GB_REAL, PH>, dim3(grid_ctas<PH>()), dim3(GB_GRID_THREADS),
-                                       args, 0, st);
-}
+// Cooperative grid over one world (GB_HUGE_BODIES bodies or more): as many
+// CTAs as are resident at once.
+#define GB_DEF_GRID_LAUNCH(PH)                                                                                               \
+    template <> cudaError_t gb_grid_launch<PH>(const Batch<GB_REAL> &B, const StepParams &sp, int wi, cudaStream_t st) {     \
+        static int n = 0;                                                                                                    \
+        if (n == 0) {                                                                                                        \
+            int dev = 0, sms = 0, per_sm = 0;                                                                                \
+            cudaGetDevice(&dev);                                                                                             \
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);                                               \
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_world_grid<GB_REAL, PH>, GB_GRID_THREADS, 0);           \
+            n = sms * (per_sm > 0 ? per_sm : 1);                                                                             \
+            if (n > GB_GRID_MAX_CTAS) n = GB_GRID_MAX_CTAS;                                                                  \
+        }                                                                                                                    \
+        Batch<GB_REAL> b = B;                                                                                                \
+        StepParams p = sp;                                                                                                   \
+        int w = wi;                                                                                                          \
+        void *args[] = {&b, &p, &w};                                                                                         \
+        return cudaLaunchCooperativeKernel((const void *)k_world_grid<GB_REAL, PH>, dim3(n), dim3(GB_GRID_THREADS), args, 0, \
+                                           st);                                                                              \
+    }
+#if GB_IN_PART(2)
+GB_DEF_WORLD_LAUNCH(PH_PAIRS0)
+GB_DEF_WORLD_LAUNCH(PH_PAIRS)
+#endif
+#if GB_IN_PART(3)
+GB_DEF_WORLD_LAUNCH(PH_COLLIDE2)
+GB_DEF_WORLD_LAUNCH(PH_ISLANDS)
+#endif
+#if GB_IN_PART(4)
+GB_DEF_WORLD_LAUNCH(PH_SOLVE)
+#endif
+#if GB_IN_PART(5)
+GB_DEF_WORLD_LAUNCH(PH_TOI2)
+#endif
+#if GB_IN_PART(6)
+GB_DEF_GRID_LAUNCH(PH_PAIRS0)
+GB_DEF_GRID_LAUNCH(PH_PAIRS)
+GB_DEF_GRID_LAUNCH(PH_COLLIDE2)
+#endif
+#if GB_IN_PART(7)
+GB_DEF_GRID_LAUNCH(PH_ISLANDS)
+GB_DEF_GRID_LAUNCH(PH_SOLVE)
+GB_DEF_GRID_LAUNCH(PH_TOI2)
+#endif
+#undef GB_DEF_WORLD_LAUNCH
+#undef GB_DEF_GRID_LAUNCH
 
+#if GB_IN_PART(0)
 template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *d_worlds,
                                         int n_list, int mode, int threads, cudaStream_t st, KernelTimer *kt,
                                         const SideStream *side) {
     if (n_list <= 0) return 0;
     // the step kernels use ~220 registers per thread: at most 256 threads per CTA
     if (threads > 256) threads = 256;
-    if (mode == 3) {
-        // phased: batch-wide kernels for the per-element work, per-world CTAs
-        // for the ordered parts (see gb_phases.cuh)
-        const int nb = B.n_bodies, ns = B.n_slots, T = 256;
-        const int gb = (nb + T - 1) / T, gs = (ns + T - 1) / T;
-        // the solve kernel stages each world's bodies in shared memory and
-        // streams its constraint records through chunk buffers; the largest
-        // worlds (first in the list) get a wider launch of their own
-        const int nhuge = B.n_huge < n_list ? B.n_huge : n_list;
-        const int nbig = B.n_big < n_list ? B.n_big : n_list;
-        const int n_norm = n_list - nhuge;
-        const int *w_norm = d_worlds + nhuge;
-        auto grid_phase = [&](auto ph, const StepParams &spp) -> cudaError_t {
-            for (int h = 0; h < nhuge; ++h) {
-                cudaError_t e = launch_grid<decltype(ph)::value>(B, spp, B.huge_ids[h], st);
-                if (e != cudaSuccess) return e;
-            }
-            return cudaSuccess;
-        };
-        const int tbig = GB_SOLVE_BIG_THREADS;
-        // per-phase CTA widths: the island and pair phases run more threads
-        // a world than the solver (measured on the uneven 8192-world batch:
-        // islands 2.6 -> 1.3 ms at 4x, pair phases best at 2x)
-        const int t_isl = threads * 4 < 256 ? threads * 4 : 256;
-        const int t_pair = threads * 2 < 256 ? threads * 2 : 256;
-        Batch<GB_REAL> Bb = B, Bs = B;
-        Bb.cache_bodies = B.cache_big;
-        Bs.cache_bodies = B.cache_small;
-        const size_t smem_big = Bb.cache_bodies > 0 ? solve_smem_bytes<GB_REAL>(Bb.cache_bodies, tbig, B.pipe_bufs) : 0;
-        const size_t smem_small = Bs.cache_bodies > 0 ? solve_smem_bytes<GB_REAL>(Bs.cache_bodies, threads, B.pipe_bufs) : 0;
-        const size_t smem_max = smem_big > smem_small ? smem_big : smem_small;
-        if (smem_max > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k_world<GB_REAL, PH_SOLVE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)smem_max);
-            if (e != cudaSuccess) return (int)e;
+    if (mode == 2) return (int)gb_warp_step_launch(B, sp, n_steps, d_worlds, n_list, threads, st);
+    if (mode != 3) return (int)gb_cta_step_launch(B, sp, n_steps, d_worlds, n_list, threads, st);
+    // phased: batch-wide kernels for the per-element work, per-world CTAs
+    // for the ordered parts (see gb_phases.cuh)
+    const int nb = B.n_bodies, ns = B.n_slots, T = 256;
+    const int gb = (nb + T - 1) / T, gs = (ns + T - 1) / T;
+    // the solve kernel stages each world's bodies in shared memory and
+    // streams its constraint records through chunk buffers; the largest
+    // worlds (first in the list) get a wider launch of their own
+    const int nhuge = B.n_huge < n_list ? B.n_huge : n_list;
+    const int nbig = B.n_big < n_list ? B.n_big : n_list;
+    const int n_norm = n_list - nhuge;
+    const int *w_norm = d_worlds + nhuge;
+    const int tbig = GB_SOLVE_BIG_THREADS;
+    // per-phase CTA widths: the island and pair phases run more threads
+    // a world than the solver (measured on the uneven 8192-world batch:
+    // islands 2.6 -> 1.3 ms at 4x, pair phases best at 2x)
+    const int t_isl = threads * 4 < 256 ? threads * 4 : 256;
+    const int t_pair = threads * 2 < 256 ? threads * 2 : 256;
+    Batch<GB_REAL> Bb = B, Bs = B;
+    Bb.cache_bodies = B.cache_big;
+    Bs.cache_bodies = B.cache_small;
+    const size_t smem_big = Bb.cache_bodies > 0 ? solve_smem_bytes<GB_REAL>(Bb.cache_bodies, tbig, B.pipe_bufs) : 0;
+    const size_t smem_small = Bs.cache_bodies > 0 ? solve_smem_bytes<GB_REAL>(Bs.cache_bodies, threads, B.pipe_bufs) : 0;
+    // kt: an event after every launch, the host accumulates the gaps
+    // (one host synchronisation per step, measurement only)
+    auto mark = [&](int k) { if (kt) cudaEventRecord(kt->ev[k], st); };
+    cudaError_t e = cudaSuccess;
+#define GB_CK(call) do { if ((e = (call)) != cudaSuccess) return (int)e; } while (0)
+#define GB_GRID(PHX) for (int h = 0; h < nhuge; ++h) GB_CK(gb_grid_launch<PHX>(B, sp, B.huge_ids[h], st))
+    const StepParams sp1 = sp;
+    for (int s = 0; s < n_steps; ++s) {
+        const StepParams sp = [&] { StepParams q = sp1; q.step_index = s; return q; }();
+        mark(0);
+        GB_GRID(PH_PAIRS0);
+        GB_CK(gb_world_launch<PH_PAIRS0>(n_norm, threads, 0, st, B, sp, w_norm));
+        mark(1);
+        if (nb) k_pre<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
+        mark(2);
+        if (ns) {
+            if (sp.events) k_collide<GB_REAL, true><<<gs, T, 0, st>>>(B, ns, sp);
+            else k_collide<GB_REAL, false><<<gs, T, 0, st>>>(B, ns, sp);
         }
-        // kt: an event after every launch, the host accumulates the gaps
-        // (one host synchronisation per step, measurement only)
-        auto mark = [&](int k) { if (kt) cudaEventRecord(kt->ev[k], st); };
-        StepParams sp1 = sp;
-        for (int s = 0; s < n_steps; ++s) {
-            const StepParams sp = [&] { StepParams q = sp1; q.step_index = s; return q; }();
-            cudaError_t ge;
-#define GB_GRID(PHX) if ((ge = grid_phase(std::integral_constant<int, PHX>{}, sp)) != cudaSuccess) return (int)ge
-            mark(0);
-            GB_GRID(PH_PAIRS0);
-            if (n_norm) k_world<GB_REAL, PH_PAIRS0><<<n_norm, threads, 0, st>>>(B, sp, w_norm);
-            mark(1);
-            if (nb) k_pre<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
-            mark(2);
-            if (ns) {
-                if (sp.events) k_collide<GB_REAL, true><<<gs, T, 0, st>>>(B, ns, sp);
-                else k_collide<GB_REAL, false><<<gs, T, 0, st>>>(B, ns, sp);
+        GB_CK(cudaGetLastError());
+        mark(3);
+        GB_GRID(PH_COLLIDE2);
+        GB_CK(gb_world_launch<PH_COLLIDE2>(n_norm, t_pair, 0, st, B, sp, w_norm));
+        mark(4);
+        GB_GRID(PH_ISLANDS);
+        GB_CK(gb_world_launch<PH_ISLANDS>(n_norm, t_isl, 0, st, B, sp, w_norm));
+        mark(5);
+        if (nb) k_vinit<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
+        mark(6);
+        if (ns) k_cinit<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
+        GB_CK(cudaGetLastError());
+        mark(7);
+        GB_GRID(PH_SOLVE);
+        if (side && nbig > nhuge && n_list > nbig) {
+            // the larger worlds first on the caller's stream; the smaller
+            // ones beside them on the low-priority side stream, filling
+            // the shared memory the wide launch leaves free on each SM
+            GB_CK(cudaEventRecord(side->fork, st));
+            GB_CK(cudaStreamWaitEvent(side->s, side->fork, 0));
+            GB_CK(gb_world_launch<PH_SOLVE>(nbig - nhuge, tbig, smem_big, st, Bb, sp, w_norm));
+            GB_CK(gb_world_launch<PH_SOLVE>(n_list - nbig, threads, smem_small, side->s, Bs, sp, d_worlds + nbig));
+            GB_CK(cudaEventRecord(side->join, side->s));
+            GB_CK(cudaStreamWaitEvent(st, side->join, 0));
+        } else {
+            if (nbig > nhuge) GB_CK(gb_world_launch<PH_SOLVE>(nbig - nhuge, tbig, smem_big, st, Bb, sp, w_norm));
+            if (n_list > nbig) GB_CK(gb_world_launch<PH_SOLVE>(n_list - nbig, threads, smem_small, st, Bs, sp, d_worlds + nbig));
+        }
+        mark(8);
+        GB_GRID(PH_PAIRS);
+        GB_CK(gb_world_launch<PH_PAIRS>(n_norm, t_pair, 0, st, B, sp, w_norm));
+        mark(9);
+        if (ns) k_toi1<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
+        mark(10);
+        if (ns) k_toi1b<GB_REAL><<<152 * 4, 128, 0, st>>>(B);
+        GB_CK(cudaGetLastError());
+        mark(11);
+        GB_GRID(PH_TOI2);
+        GB_CK(gb_world_launch<PH_TOI2>(n_norm, 32, 0, st, B, sp, w_norm));
+        mark(12);
+        if (kt) {
+            GB_CK(cudaEventSynchronize(kt->ev[GB_NKTIME]));
+            for (int k = 0; k < GB_NKTIME; ++k) {
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, kt->ev[k], kt->ev[k + 1]);
+                kt->total_ms[k] += ms;
             }
-            mark(3);
-            GB_GRID(PH_COLLIDE2);
-            if (n_norm) k_world<GB_REAL, PH_COLLIDE2><<<n_norm, t_pair, 0, st>>>(B, sp, w_norm);
-            mark(4);
-            GB_GRID(PH_ISLANDS);
-            if (n_norm) k_world<GB_REAL, PH_ISLANDS><<<n_norm, t_isl, 0, st>>>(B, sp, w_norm);
-            mark(5);
-            if (nb) k_vinit<GB_REAL><<<gb, T, 0, st>>>(B, nb, sp);
-            mark(6);
-            if (ns) k_cinit<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
-            mark(7);
-            GB_GRID(PH_SOLVE);
-            if (side && nbig > nhuge && n_list > nbig) {
-                // the larger worlds first on the caller's stream; the smaller
-                // ones beside them on the low-priority side stream, filling
-                // the shared memory the wide launch leaves free on each SM
-                cudaEventRecord(side->fork, st);
-                cudaStreamWaitEvent(side->s, side->fork, 0);
-                k_world<GB_REAL, PH_SOLVE><<<nbig - nhuge, tbig, smem_big, st>>>(Bb, sp, w_norm);
-                k_world<GB_REAL, PH_SOLVE><<<n_list - nbig, threads, smem_small, side->s>>>(Bs, sp, d_worlds + nbig);
-                cudaEventRecord(side->join, side->s);
-                cudaStreamWaitEvent(st, side->join, 0);
-            } else {
-                if (nbig > nhuge) k_world<GB_REAL, PH_SOLVE><<<nbig - nhuge, tbig, smem_big, st>>>(Bb, sp, w_norm);
-                if (n_list > nbig) k_world<GB_REAL, PH_SOLVE><<<n_list - nbig, threads, smem_small, st>>>(Bs, sp, d_worlds + nbig);
-            }
-            mark(8);
-            GB_GRID(PH_PAIRS);
-            if (n_norm) k_world<GB_REAL, PH_PAIRS><<<n_norm, t_pair, 0, st>>>(B, sp, w_norm);
-            mark(9);
-            if (ns) k_toi1<GB_REAL><<<gs, T, 0, st>>>(B, ns, sp);
-            mark(10);
-            if (ns) k_toi1b<GB_REAL><<<152 * 4, 128, 0, st>>>(B);
-            mark(11);
-            GB_GRID(PH_TOI2);
-            if (n_norm) k_world_toi2<GB_REAL><<<n_norm, 32, 0, st>>>(B, sp, w_norm);
+            kt->steps += 1;
+        }
+    }
 #undef GB_GRID
-            mark(12);
-            if (kt) {
-                cudaError_t e = cudaEventSynchronize(kt->ev[GB_NKTIME]);
-                if (e != cudaSuccess) return (int)e;
-                for (int k = 0; k < GB_NKTIME; ++k) {
-                    float ms = 0.0f;
-                    cudaEventElapsedTime(&ms, kt->ev[k], kt->ev[k + 1]);
-                    kt->total_ms[k] += ms;
-                }
-                kt->steps += 1;
-            }
-        }
-        return (int)cudaGetLastError();
-    }
-    if (mode == 2) {
-        int wpc = threads / 32;
-        if (wpc < 1) wpc = 1;
-        int blocks = (n_list + wpc - 1) / wpc;
-        k_step_warp<GB_REAL><<<blocks, wpc * 32, 0, st>>>(B, sp, n_steps, d_worlds, n_list);
-    } else {
-        k_step_cta<GB_REAL><<<n_list, threads, 0, st>>>(B, sp, n_steps, d_worlds);
-    }
+#undef GB_CK
     return (int)cudaGetLastError();
 }
 
@@ -283,3 +366,4 @@ template <> void gb_launch_ray_cast_all<GB_REAL>(const Batch<GB_REAL> &B, const 
                                                  int *counts, cudaStream_t st) {
     if (n > 0) k_ray_cast_all<GB_REAL><<<(n + 7) / 8, 256, 0, st>>>(B, rays, n, hits, cap, counts);
 }
+#endif  // GB_IN_PART(0)
