@@ -375,11 +375,16 @@ int gb_batch_query_aabb(gb_batch *batch, const gb_aabb_query *queries, int32_t n
 /* gb_batch_step with the step's scratch arrays placed in one static device
  * array of GB_STATIC_SCRATCH_BYTES instead of the batch arena; the call
  * allocates no device memory.  No counterpart in the reference (its step
- * allocates Python objects per call).  The first call on a device looks up
- * the array's address (loading the module), so make one call before any
- * stream capture.  A batch whose scratch exceeds the array is rejected with
- * GB_E_SCRATCH before any launch.  All calls on a device share the array:
- * calls whose work may overlap (other streams or host threads) race. */
+ * allocates Python objects per call).  launch_mode 0 takes the batch's
+ * launch configuration, exactly as gb_batch_step does.  Contact events and
+ * per-launch timing (GB_OPT_EVENTS, GB_OPT_KERNEL_TIMES) are refused with
+ * GB_E_UNSUPPORTED.  The first call on a device looks up the array's address
+ * (loading the module) and keeps it for that device, so make one call before
+ * any stream capture, and do not call it again after a cudaDeviceReset of
+ * that device (the kept address belongs to the old context).  A batch whose
+ * scratch exceeds the array is rejected with GB_E_SCRATCH before any launch.
+ * All calls on a device share the array: calls whose work may overlap (other
+ * streams or host threads) race. */
 int gb_batch_step_static_scratch(gb_batch *batch, const gb_step_opts *opts, void *cuda_stream);
 
 #ifdef __cplusplus

@@ -7,7 +7,8 @@
 # setup.py extension (setup.py:43-54) without its networked bootstrap; no
 # FMA contraction, as the x86-64 default.
 set -e
-REF=${REF:-/root/reference}
+# REF: the reference source tree (required)
+: "${REF:?set REF to the pypybox2d source tree}"
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

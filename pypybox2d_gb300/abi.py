@@ -192,7 +192,9 @@ KERNEL_SLOTS = ("pairs_new", "pre", "collide", "collide_sleeping", "islands", "v
 
 #: bytes of the static device scratch behind gb_batch_step_static_scratch
 STATIC_SCRATCH_BYTES = 32 << 20
-E_SCRATCH = -7
+
+#: C-ABI status codes (include/gb2d.h GB_E_*)
+E_OK, E_ARG, E_CUDA, E_CONTACT_OVERFLOW, E_UNSUPPORTED, E_NONFINITE, E_ITER_LIMIT, E_SCRATCH = 0, -1, -2, -3, -4, -5, -6, -7
 
 _lib = None
 

@@ -995,18 +995,14 @@ template <class R> int step_static(gb_batch *b, const Batch<R> &arena_view, cons
 extern "C" int gb_batch_step_static_scratch(gb_batch *b, const gb_step_opts *o, void *stream) {
     if (!b || !o) return fail(GB_E_ARG, "batch or opts is NULL");
     if (o->n_steps < 0 || o->vel_iters < 0 || o->pos_iters < 0) return fail(GB_E_ARG, "negative step count or iterations");
-    StepParams sp;
-    sp.dt = o->dt;
-    sp.inv_dt = o->dt > 0.0 ? 1.0 / o->dt : 0.0;
-    sp.dt_ratio = 0.0;
-    sp.vel_iters = o->vel_iters;
-    sp.pos_iters = o->pos_iters;
-    sp.record_order = o->record_order & 1;
-    sp.profile = (o->record_order >> 1) & 1;
-    sp.events = 0;   // contact events are recorded by gb_batch_step only
-    sp.step_index = 0;
-    int mode = (o->launch_mode == 2 || o->launch_mode == 3) ? o->launch_mode : (o->launch_mode == 0 ? 3 : 1);
-    int threads = o->block_threads > 0 ? o->block_threads : 128;
+    // contact events and per-launch timing need buffers and host waits that
+    // this entry point does not have: refuse them rather than drop them
+    if (o->record_order & (GB_OPT_EVENTS | GB_OPT_KERNEL_TIMES))
+        return fail(GB_E_UNSUPPORTED, "gb_batch_step_static_scratch records no contact events and no launch times "
+                                      "(GB_OPT_EVENTS, GB_OPT_KERNEL_TIMES): use gb_batch_step");
+    const StepParams sp = params_of(o);
+    int mode = 0, threads = 0;
+    resolve_mapping(b, o, &mode, &threads);   // launch_mode 0: the batch's launch configuration, as gb_batch_step
     if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
     cudaStream_t st = (cudaStream_t)stream;
     int rc = b->prec == GB_PREC_F64 ? step_static<double>(b, b->bd, sp, o->n_steps, mode, threads, st)

@@ -1,7 +1,7 @@
 """Generate the golden vectors of the World.step path by running the
 reference pypybox2d itself (C-extension math mode) in this container.
 
-Usage:  python tests/golden/make_golden.py [--ref /root/reference]
+Usage:  python tests/golden/make_golden.py --ref <pypybox2d source tree>   (or GB2D_REFERENCE=<tree>)
 
 The reference is imported from its source tree (read only); its C extension
 `_common` must first be compiled by oracle/build_ref.sh into oracle/_ref/.
@@ -457,7 +457,8 @@ def run_api_script(b2):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("GB2D_REFERENCE"), required="GB2D_REFERENCE" not in os.environ,
+                    help="the pypybox2d source tree (default: $GB2D_REFERENCE)")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
     b2 = load_reference(args.ref)

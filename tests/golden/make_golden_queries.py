@@ -1,7 +1,7 @@
 """Generate the golden vectors of the world queries by running the reference
 pypybox2d itself (C-extension math mode) in this container.
 
-Usage:  python tests/golden/make_golden_queries.py [--ref /root/reference]
+Usage:  python tests/golden/make_golden_queries.py --ref <pypybox2d source tree>   (or GB2D_REFERENCE=<tree>)
 
 For the mixed (edges, circles, polygons) and uneven scenes of
 make_golden.py, the reference world is stepped (with the same pair-order
@@ -60,7 +60,8 @@ def boxes_for(rng, F):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("GB2D_REFERENCE"), required="GB2D_REFERENCE" not in os.environ,
+                    help="the pypybox2d source tree (default: $GB2D_REFERENCE)")
     args = ap.parse_args()
     b2 = mg.load_reference(args.ref)
     from pypybox2d.common import AABB, Vec2

@@ -7,6 +7,16 @@ same doubles after every call.  Tolerance: none (bit-exact) in both
 precisions, since the kernels, launch sequence and reduction orders are the
 same and only the scratch addresses differ.
 
+Covered: the monolithic and phased launches; launch_mode 0 after
+gb_batch_set_launch_config (the batch's configuration, as gb_batch_step
+takes it); a batch whose solver runs as a wide launch on the caller's stream
+beside a narrow one on the side stream; a world of 16384+ bodies run as a
+cooperative grid, whose grid reductions use the arena next to the static
+arrays (its contact capacity is set so its scratch fits the 32 MiB array; at
+the default 10 slots per fixture such a world needs more and is refused, as
+the oversize test shows for a large batch); and the option bits the entry
+point refuses.
+
 The file is named to be collected last; it also passes on its own.
 """
 import ctypes
@@ -93,3 +103,65 @@ def test_oversized_batch_is_rejected_before_any_launch():
     assert "static scratch holds" in msg and str(abi.STATIC_SCRATCH_BYTES) in msg
     _same(g.bodies(), before, "rejected call")
     assert int(g.arena_bytes()) > 0
+
+
+@pytest.mark.parametrize("cfg", [(2, 64, 0, 512), (3, 64, 0, 512), (3, 32, 2, 256)],
+                         ids=["warp-per-world", "phased-64", "phased-32-chunked"])
+def test_static_scratch_follows_the_launch_config(cfg):
+    """launch_mode 0 means the batch's launch configuration in both entry points."""
+    W, B, F, M = scenes.uneven_batch(6, seed=3, counts=[40, 300, 25, 120, 60, 15])
+    ref, st = _twins(W, B, F, "f64", moves=M)
+    for g in (ref, st):
+        g.set_launch_config(*cfg)
+    for call in range(CALLS):
+        ref.step(1 / 60, 8, 3, 10, launch_mode=0)
+        st.step_static_scratch(1 / 60, 8, 3, 10, launch_mode=0)
+        _same(st.bodies(), ref.bodies(), f"config {cfg} call {call} bodies")
+        for w in range(len(W)):
+            _same(st.contacts(w), ref.contacts(w), f"config {cfg} call {call} world {w} contacts")
+    assert not st.status().any()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_static_scratch_with_the_side_stream_solver(precision):
+    """Worlds of 512+ bodies solve in the wide launch on the caller's stream,
+    the rest beside them on the batch's side stream."""
+    W, B, F, M = scenes.uneven_batch(5, seed=11, counts=[700, 560, 120, 60, 20])
+    ref, st = _twins(W, B, F, precision, moves=M)
+    for g in (ref, st):
+        g.set_launch_config(3, 64, 0, 512)
+    for call in range(CALLS):
+        ref.step(1 / 60, 8, 3, 10, launch_mode=0)
+        st.step_static_scratch(1 / 60, 8, 3, 10, launch_mode=0)
+        _same(st.bodies(), ref.bodies(), f"{precision} side stream call {call} bodies")
+        for w in range(len(W)):
+            _same(st.contacts(w), ref.contacts(w), f"{precision} side stream call {call} world {w} contacts")
+    assert not st.status().any()
+
+
+def test_static_scratch_with_a_cooperative_grid_world():
+    """A world of 16400 bodies runs every per-world phase as one cooperative
+    grid; 40000 contact slots keep its step scratch inside the static array."""
+    W, B, F, M = scenes.large_world(0, n=16400)
+    W = W.copy()
+    W["contact_capacity"] = 40000
+    ref, st = _twins(W, B, F, "f64", moves=M)
+    for call in range(CALLS):
+        ref.step(1 / 60, 8, 3, STEPS_PER_CALL, launch_mode=3)
+        st.step_static_scratch(1 / 60, 8, 3, STEPS_PER_CALL, launch_mode=3)
+        _same(st.bodies(), ref.bodies(), f"grid world call {call} bodies")
+        _same(st.contacts(0), ref.contacts(0), f"grid world call {call} contacts")
+    assert int(st.status()[0]) == 0
+
+
+@pytest.mark.parametrize("bit", [abi.OPT_EVENTS, abi.OPT_KERNEL_TIMES], ids=["events", "kernel-times"])
+def test_static_scratch_refuses_recording_options(bit):
+    from pypybox2d_gb300.gpu import GpuBatch
+    W, B, F, dt, (vi, pi) = _golden("mixed")
+    g = GpuBatch(W, B, F, precision="f64")
+    before = g.bodies()
+    o = abi.StepOpts(dt, vi, pi, 1, 3, 0, bit)
+    rc = g.lib.gb_batch_step_static_scratch(g.h, ctypes.byref(o), None)
+    assert rc == abi.E_UNSUPPORTED
+    assert "gb_batch_step" in g.lib.gb_last_error().decode()
+    _same(g.bodies(), before, "refused call")
