@@ -255,6 +255,21 @@ int gb_batch_get_contacts(gb_batch *batch, int32_t world, gb_contact *out, int32
  * the step ran with record_order set. */
 int gb_batch_get_solver_order(gb_batch *batch, int32_t world, int32_t *order, int32_t capacity,
                               int32_t *n_out, void *cuda_stream);
+/* Step record of one world's bodies (world-local order) from the last step
+ * run with record_order bit 0 set: per body, bits 0-7 the position
+ * iterations its island ran before the early exit (island.py:141-153; 0:
+ * not in a simulated island), bits 8-15 the TOI position-pass iterations
+ * over the TOI events it took part in (contact.py:866-933, island.py:181-243),
+ * bits 16-23 the number of those events (world.py:693-817), each capped at
+ * 255; bit 24 the parity of its constraints' contact points that took the
+ * restitution bias (relative normal velocity below -1 m/s, contact.py:470-475)
+ * and bit 25 of its 2-point constraints that dropped to one point
+ * (contact.py:487-496) in the island solve, bits 26/27 the same in TOI
+ * sub-steps (non-static bodies).  These are decisions of the step that its
+ * final state does not show; nothing in the reference (measurement for the
+ * parity tests). */
+int gb_batch_get_step_record(gb_batch *batch, int32_t world, int32_t *out, int32_t capacity, int32_t *n_out,
+                             void *cuda_stream);
 /* Per-world status words (GB_ST_* bits), n_worlds uint32. */
 int gb_batch_status(gb_batch *batch, uint32_t *status, void *cuda_stream);
 /* Accumulated SM clock cycles per step phase, 16 int64 per world
@@ -369,6 +384,23 @@ int gb_batch_ray_cast_all(gb_batch *batch, const gb_ray *rays, int32_t n_rays, g
  * fixtures[q * max_per_query ...], counts[q] is how many overlap in all. */
 int gb_batch_query_aabb(gb_batch *batch, const gb_aabb_query *queries, int32_t n_queries, int32_t *fixtures,
                         int32_t max_per_query, int32_t *counts, void *cuda_stream);
+
+/* Checkpoint and resume of a batch's whole device state: bodies and sweeps,
+ * fixtures with their fat AABBs, contacts with manifolds, impulses and flags,
+ * world headers (contact counts, status words, inv_dt0) and the pending
+ * broad-phase move buffers.  The reference has no world serialisation (only
+ * its math types pickle: common.py:176-179, 394-398, 649-652, 725-728, and
+ * Body/Fixture copy, body.py:118-140, fixture.py:76-85); these calls give the
+ * GPU batch one.  A snapshot is GB_SNAPSHOT_HEADER_BYTES of header (layout
+ * identity: precision and record counts) followed by the device arena; it
+ * restores only into a batch made from a scene of the same layout.  `dst` /
+ * `src` may be host or device memory (copied with cudaMemcpyDefault); the
+ * calls return once the copy is complete.  The launch configuration and
+ * captured graphs are not part of the state and are kept. */
+#define GB_SNAPSHOT_HEADER_BYTES 64
+int gb_batch_snapshot_bytes(gb_batch *batch, uint64_t *bytes);
+int gb_batch_snapshot(gb_batch *batch, void *dst, uint64_t bytes, void *cuda_stream);
+int gb_batch_restore(gb_batch *batch, const void *src, uint64_t bytes, void *cuda_stream);
 
 /* Size of the static device scratch of gb_batch_step_static_scratch (32 MiB). */
 #define GB_STATIC_SCRATCH_BYTES (32u << 20)

@@ -87,6 +87,7 @@ typedef struct {
     double k11, k12, k22, nm11, nm12, nm21, nm22;
     int mtype;
     v2 ln, lp, lpts[2];
+    int dec;                  /* set-up decisions: restitution bias of point 0/1 (bits 0/1), block dropped (bit 2) */
 } or_cons;
 
 struct or_world {
@@ -113,7 +114,17 @@ struct or_world {
     /* counters */
     long long n_toi_calls, n_toi_events;
     int status;
+    /* step record of the last step, per body: position iterations of its
+     * island (bits 0-7), TOI position-pass iterations (8-15) and TOI events
+     * (16-23), each capped at 255; set-up decision parities (24-27) */
+    int *rec;
 };
+
+static void rec_add(int *x, int shift, int v) {
+    int cur = (*x >> shift) & 0xff;
+    int nv = cur + v > 255 ? 255 : cur + v;
+    *x = (*x & ~(0xff << shift)) | (nv << shift);
+}
 
 /* ------------------------------------------------------------------ */
 static inline xform body_xf(const gb_body *b) { xform x; x.p = V(b->px, b->py); x.q.c = b->qc; x.q.s = b->qs; return x; }
@@ -412,6 +423,7 @@ static void build_constraint(or_world *w, or_cons *k, int cid, int warm, double 
 
 /* contact.py:414-496 initialize_velocity_constraints (+ contact_util.py:195-245 WorldManifold) */
 static void init_velocity(or_cons *k, const v2 *pc, const double *pa, const v2 *vv, const double *ww) {
+    k->dec = 0;
     v2 ca = pc[k->ia], cb = pc[k->ib];
     double aa = pa[k->ia], ab = pa[k->ib];
     v2 va = vv[k->ia], vb = vv[k->ib];
@@ -462,7 +474,7 @@ static void init_velocity(or_cons *k, const v2 *pc, const double *pa, const v2 *
         k->tm[i] = kt > 0.0 ? 1.0 / kt : 0.0;
         k->bias[i] = 0.0;
         double vrel = vdot(normal, vsub(vsub(vadd(vb, vcross_sv(wb, rb)), va), vcross_sv(wa, ra)));
-        if (vrel < -VELOCITY_THRESHOLD) k->bias[i] = -k->restitution * vrel;
+        if (vrel < -VELOCITY_THRESHOLD) { k->bias[i] = -k->restitution * vrel; k->dec |= 1 << i; }
     }
     if (k->npts == 2) {
         double rn1a = vcross(k->rA[0], normal), rn1b = vcross(k->rB[0], normal);
@@ -477,6 +489,7 @@ static void init_velocity(or_cons *k, const v2 *pc, const double *pa, const v2 *
             k->nm11 = det * k22; k->nm12 = -det * k12; k->nm21 = -det * k12; k->nm22 = det * k11;
         } else {
             k->npts = 1;
+            k->dec |= 4;
         }
     }
 }
@@ -641,6 +654,16 @@ static int cmp_rank(const void *x, const void *y) {
     return (ra < rb) ? -1 : (ra > rb ? 1 : 0);
 }
 
+/* Step record: parity of the restitution-bias points (bit `shift`) and of
+ * the block solver's drop to one point (bit shift + 1) of a constraint,
+ * toggled on its non-static bodies (`bodies`: island body ids). */
+static void rec_decisions(or_world *w, const int *bodies, const or_cons *k, int shift) {
+    int bits = ((((k->dec & 1) + ((k->dec >> 1) & 1)) & 1) << shift) | (((k->dec >> 2) & 1) << (shift + 1));
+    if (!bits) return;
+    if (w->b[bodies[k->ia]].type != GB_BODY_STATIC) w->rec[bodies[k->ia]] ^= bits;
+    if (w->b[bodies[k->ib]].type != GB_BODY_STATIC) w->rec[bodies[k->ib]] ^= bits;
+}
+
 /* island.py:65-179 Island.solve */
 static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts, int nci, double dt, double inv_dt,
                          double dt_ratio, int vel_iters, int pos_iters, int warm) {
@@ -673,6 +696,7 @@ static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts,
     or_cons *ks = (or_cons *)malloc(sizeof(or_cons) * (size_t)(nci > 0 ? nci : 1));
     for (int i = 0; i < nci; ++i) build_constraint(w, &ks[i], contacts[i], warm, dt_ratio);
     for (int i = 0; i < nci; ++i) init_velocity(&ks[i], pc, pa, vv, ww);
+    for (int i = 0; i < nci; ++i) rec_decisions(w, bodies, &ks[i], 24);
     if (warm)
         for (int i = 0; i < nci; ++i) warm_start(&ks[i], vv, ww);
     for (int it = 0; it < vel_iters; ++it)
@@ -699,12 +723,14 @@ static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts,
         pa[i] = pa[i] + dt * om;
         vv[i] = v; ww[i] = om;
     }
-    int position_solved = 0;
+    int position_solved = 0, its = pos_iters;
     for (int it = 0; it < pos_iters; ++it) {
         double minsep = 0.0;
         for (int i = 0; i < nci; ++i) minsep = solve_position(&ks[i], pc, pa, minsep, -1, -1);
-        if (minsep >= -3.0 * OR_LINEAR_SLOP) { position_solved = 1; break; }
+        if (minsep >= -3.0 * OR_LINEAR_SLOP) { position_solved = 1; its = it + 1; break; }
     }
+    for (int i = 0; i < nbi; ++i)
+        if (w->b[bodies[i]].type != GB_BODY_STATIC) w->rec[bodies[i]] = (w->rec[bodies[i]] & ~0xff) | (its > 255 ? 255 : its);
     for (int i = 0; i < nbi; ++i) {
         gb_body *b = &w->b[bodies[i]];
         b->cx = pc[i].x; b->cy = pc[i].y; b->a = pa[i];
@@ -815,15 +841,20 @@ static void island_solve_toi(or_world *w, const int *bodies, int nbi, int *conta
     }
     or_cons *ks = (or_cons *)malloc(sizeof(or_cons) * (size_t)(nci > 0 ? nci : 1));
     for (int i = 0; i < nci; ++i) build_constraint(w, &ks[i], contacts[i], 0, 1.0);
+    int its = 0;
     for (int it = 0; it < 20; ++it) {
         double minsep = 0.0;
         for (int i = 0; i < nci; ++i) minsep = solve_position(&ks[i], pc, pa, minsep, toi_a, toi_b);
+        its = it + 1;
         if (minsep >= -1.5 * OR_LINEAR_SLOP) break;
     }
+    rec_add(&w->rec[bodies[toi_a]], 8, its); rec_add(&w->rec[bodies[toi_a]], 16, 1);
+    rec_add(&w->rec[bodies[toi_b]], 8, its); rec_add(&w->rec[bodies[toi_b]], 16, 1);
     gb_body *ba = &w->b[bodies[toi_a]], *bb = &w->b[bodies[toi_b]];
     ba->c0x = pc[toi_a].x; ba->c0y = pc[toi_a].y; ba->a0 = pa[toi_a];
     bb->c0x = pc[toi_b].x; bb->c0y = pc[toi_b].y; bb->a0 = pa[toi_b];
     for (int i = 0; i < nci; ++i) init_velocity(&ks[i], pc, pa, vv, ww);
+    for (int i = 0; i < nci; ++i) rec_decisions(w, bodies, &ks[i], 26);
     for (int it = 0; it < vel_iters; ++it)
         for (int i = 0; i < nci; ++i) solve_velocity(&ks[i], vv, ww);
     for (int i = 0; i < nbi; ++i) {
@@ -994,6 +1025,7 @@ static void world_solve_toi(or_world *w, double dt, int vel_iters) {
 
 /* world.py:307-354 World.step */
 void or_step(or_world *w, double dt, int vel_iters, int pos_iters) {
+    memset(w->rec, 0, sizeof(int) * (size_t)(w->nb ? w->nb : 1));
     if (w->wflags & GB_W_NEW_FIXTURE) {
         find_new_contacts(w);
         w->wflags &= ~GB_W_NEW_FIXTURE;
@@ -1022,6 +1054,7 @@ or_world *or_create(const gb_world_desc *wd, const gb_body *bodies, const gb_fix
     w->bcon = (ivec *)calloc(w->nb ? w->nb : 1, sizeof(ivec));
     w->island_flag_b = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
     w->island_index = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
+    w->rec = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
     w->wflags = wd->flags;
     w->gravity = V(wd->gx, wd->gy);
     w->inv_dt0 = wd->inv_dt0;
@@ -1058,7 +1091,7 @@ void or_destroy(or_world *w) {
     free(w->bcon);
     free(w->order.d); free(w->move.d); free(w->last_order.d);
     free(w->island_flag_b); free(w->island_index); free(w->hook_rank);
-    free(w->hook_pending); free(w->pos_of);
+    free(w->hook_pending); free(w->pos_of); free(w->rec);
     free(w->c); free(w->b); free(w->f);
     free(w);
 }
@@ -1108,6 +1141,7 @@ int or_get_solver_order(const or_world *w, int *out, int cap) {
 }
 
 long long or_toi_calls(const or_world *w) { return w->n_toi_calls; }
+void or_get_step_record(const or_world *w, int *out) { memcpy(out, w->rec, sizeof(int) * (size_t)w->nb); }
 long long or_toi_events(const or_world *w) { return w->n_toi_events; }
 
 /* ------------------------------------------------------------------ */

@@ -174,6 +174,7 @@ EXPORTED = (
     "gb_batch_set_launch_config", "gb_batch_get_launch_config", "gb_batch_autotune",
     "gb_graph_capture", "gb_graph_launch", "gb_graph_destroy",
     "gb_batch_ray_cast", "gb_batch_ray_cast_all", "gb_batch_query_aabb",
+    "gb_batch_snapshot_bytes", "gb_batch_snapshot", "gb_batch_restore", "gb_batch_get_step_record",
 )
 
 #: gb_step_opts.record_order bit that records contact events
@@ -244,6 +245,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_ray_cast.argtypes = [vp, vp, i32, vp, vp]
     lib.gb_batch_query_aabb.argtypes = [vp, vp, i32, i32p, i32, i32p, vp]
     lib.gb_batch_ray_cast_all.argtypes = [vp, vp, i32, vp, i32, i32p, vp]
+    lib.gb_batch_snapshot_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+    lib.gb_batch_snapshot.argtypes = [vp, vp, ctypes.c_uint64, vp]
+    lib.gb_batch_restore.argtypes = [vp, vp, ctypes.c_uint64, vp]
+    lib.gb_batch_get_step_record.argtypes = [vp, i32, i32p, i32, i32p, vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

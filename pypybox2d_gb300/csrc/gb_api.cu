@@ -84,6 +84,7 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_cp = a.take<ConsPos<R>>(ncap);
     B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
     B.order_out = a.take<int>(ncap);
+    B.rec = a.take<int>(nb);
     B.prof = a.take<long long>((size_t)nw * GB_NPROF);
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
@@ -539,6 +540,19 @@ int gb_batch_get_solver_order(gb_batch *b, int32_t world, int32_t *order, int32_
     return 0;
 }
 
+int gb_batch_get_step_record(gb_batch *b, int32_t world, int32_t *out, int32_t capacity, int32_t *n_out, void *stream) {
+    if (!b || !out || !n_out) return fail(GB_E_ARG, "NULL argument");
+    if (world < 0 || world >= b->nw) return fail(GB_E_ARG, "world index out of range");
+    const WorldHdr &h = b->hdr[world];
+    *n_out = h.nb;
+    if (h.nb > capacity) return fail(GB_E_ARG, "capacity too small for the world's bodies");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int *src = (b->prec == GB_PREC_F64 ? b->bd.rec : b->bf.rec) + h.bbase;
+    if (h.nb > 0) CK(cudaMemcpyAsync(out, src, sizeof(int) * h.nb, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
 int gb_batch_status(gb_batch *b, uint32_t *status, void *stream) {
     if (!b || !status) return fail(GB_E_ARG, "NULL argument");
     std::vector<WorldHdr> h;
@@ -923,6 +937,62 @@ int gb_batch_query_aabb(gb_batch *b, const gb_aabb_query *qs, int32_t n, int32_t
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(counts, d_cnt, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, st));
     if (out_b) CK(cudaMemcpyAsync(fixtures, d_out, out_b, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+// ------------------------------------------------------------------------
+// Snapshots: a 64-byte header naming the layout, then the arena.
+namespace {
+struct SnapHeader {
+    char magic[8];
+    int32_t precision, n_worlds, n_bodies, n_fixtures, n_slots, _pad;
+    uint64_t arena_bytes;
+    char _rest[GB_SNAPSHOT_HEADER_BYTES - 8 - 6 * 4 - 8];
+};
+static_assert(sizeof(SnapHeader) == GB_SNAPSHOT_HEADER_BYTES, "snapshot header layout");
+SnapHeader snap_header(const gb_batch *b) {
+    SnapHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, "GB2DSNP1", 8);
+    h.precision = b->prec; h.n_worlds = b->nw; h.n_bodies = b->nb; h.n_fixtures = b->nf; h.n_slots = b->ncap;
+    h.arena_bytes = b->arena_bytes;
+    return h;
+}
+}  // namespace
+
+int gb_batch_snapshot_bytes(gb_batch *b, uint64_t *bytes) {
+    if (!b || !bytes) return fail(GB_E_ARG, "batch or bytes is NULL");
+    *bytes = GB_SNAPSHOT_HEADER_BYTES + (uint64_t)b->arena_bytes;
+    return 0;
+}
+
+int gb_batch_snapshot(gb_batch *b, void *dst, uint64_t bytes, void *stream) {
+    if (!b || !dst) return fail(GB_E_ARG, "batch or dst is NULL");
+    if (bytes < GB_SNAPSHOT_HEADER_BYTES + (uint64_t)b->arena_bytes)
+        return fail(GB_E_ARG, "snapshot buffer too small (see gb_batch_snapshot_bytes)");
+    cudaStream_t st = (cudaStream_t)stream;
+    const SnapHeader h = snap_header(b);
+    char *d = static_cast<char *>(dst);
+    CK(cudaMemcpyAsync(d, &h, sizeof(h), cudaMemcpyDefault, st));
+    CK(cudaMemcpyAsync(d + GB_SNAPSHOT_HEADER_BYTES, b->arena, b->arena_bytes, cudaMemcpyDefault, st));
+    CK(cudaStreamSynchronize(st));   // `h` lives on this stack frame
+    return 0;
+}
+
+int gb_batch_restore(gb_batch *b, const void *src, uint64_t bytes, void *stream) {
+    if (!b || !src) return fail(GB_E_ARG, "batch or src is NULL");
+    if (bytes < GB_SNAPSHOT_HEADER_BYTES + (uint64_t)b->arena_bytes)
+        return fail(GB_E_ARG, "snapshot too small for this batch");
+    cudaStream_t st = (cudaStream_t)stream;
+    SnapHeader h;
+    CK(cudaMemcpyAsync(&h, src, sizeof(h), cudaMemcpyDefault, st));
+    CK(cudaStreamSynchronize(st));
+    const SnapHeader want = snap_header(b);
+    if (memcmp(&h, &want, sizeof(h)) != 0)
+        return fail(GB_E_ARG, "snapshot was taken from a batch of another layout (precision or record counts differ)");
+    CK(cudaMemcpyAsync(b->arena, static_cast<const char *>(src) + GB_SNAPSHOT_HEADER_BYTES, b->arena_bytes,
+                       cudaMemcpyDefault, st));
     CK(cudaStreamSynchronize(st));
     return 0;
 }

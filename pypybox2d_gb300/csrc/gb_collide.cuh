@@ -597,13 +597,7 @@ static __device__ __forceinline__ xform2<double> sweep_xf(const Sweep &sw, doubl
     return x;
 }
 static __device__ __forceinline__ void sweep_advance(Sweep &sw, double alpha) {
-#if defined(GB_POSE_ROT_F32)
-    // float32 unit: the fraction in float32 (a float64 division costs ~1000
-    // cycles on GB300; the poses it interpolates move by ~1e-7 m)
-    double beta = (double)((float)(alpha - sw.alpha0) / (float)(1.0 - sw.alpha0));
-#else
     double beta = (alpha - sw.alpha0) / (1.0 - sw.alpha0);
-#endif
     sw.c0 = (1.0 - beta) * sw.c0 + beta * sw.c;
     sw.a0 = (1.0 - beta) * sw.a0 + beta * sw.a;
     sw.alpha0 = alpha;

@@ -665,6 +665,7 @@ template <class R> __device__ __forceinline__ xform2<R> pose_xf(vec2<double> c, 
 template <class R> __device__ void init_velocity_xf(Cons<R> &k, xform2<R> xa, xform2<R> xb, vec2<R> car, vec2<R> cbr,
                                                     vec2<R> va, R wa, vec2<R> vb, R wb) {
     vec2<R> normal, pts[2];
+    k.dec = 0;
     if (k.mtype == GB_M_CIRCLES) {
         normal = mk<R>(1, 0);
         vec2<R> pA = xmul(xa, k.lp), pB = xmul(xb, k.lpts[0]);
@@ -705,7 +706,7 @@ template <class R> __device__ void init_velocity_xf(Cons<R> &k, xform2<R> xa, xf
         k.tm[i] = kt > (R)0 ? (R)1 / kt : (R)0;
         k.bias[i] = (R)0;
         R vrel = dot(normal, ((vb + cross(wb, rb)) - va) - cross(wa, ra));
-        if (vrel < (R)-GB_VELOCITY_THRESHOLD) k.bias[i] = -k.restitution * vrel;
+        if (vrel < (R)-GB_VELOCITY_THRESHOLD) { k.bias[i] = -k.restitution * vrel; k.dec |= 1 << i; }
     }
     if (k.npts == 2) {
         R rn1a = cross(k.rA[0], normal), rn1b = cross(k.rB[0], normal);
@@ -720,6 +721,7 @@ template <class R> __device__ void init_velocity_xf(Cons<R> &k, xform2<R> xa, xf
             k.nm11 = det * k22; k.nm12 = -det * k12; k.nm21 = -det * k12; k.nm22 = det * k11;
         } else {
             k.npts = 1;
+            k.dec |= 4;
         }
     }
 }
@@ -1227,6 +1229,11 @@ template <class R> __device__ __forceinline__ void init_constraint(const WView<R
     } else {
         init_velocity(q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], w.B.b_v[ga], w.B.b_w[ga], w.B.b_v[gbb], w.B.b_w[gbb]);
     }
+    if (sp.record_order) {   // step record: the set-up decisions of this constraint
+        const int bits = rec_setup_bits(q.dec, GB_REC_SETUP_SHIFT);
+        if (bits && w.btype(q.ia) != GB_BODY_STATIC) atomicXor(&w.B.rec[ga], bits);
+        if (bits && w.btype(q.ib) != GB_BODY_STATIC) atomicXor(&w.B.rec[gbb], bits);
+    }
     ConsVel<R> v;
     for (int j = 0; j < 2; ++j) {
         v.ni[j] = j < q.mcount ? q.ni[j] : (R)0;
@@ -1267,6 +1274,17 @@ template <class R> __device__ __forceinline__ Cons<R> vel_cons(const ConsVel<R> 
     }
     q.k11 = v.k11; q.k12 = v.k12; q.k22 = v.k22;
     q.nm11 = v.nm11; q.nm12 = v.nm12; q.nm21 = v.nm12; q.nm22 = v.nm22;
+    return q;
+}
+// The fields solve_position reads, widened to float64.
+template <class R> __device__ __forceinline__ Cons<double> pos_cons_f64(const Cons<R> &k) {
+    Cons<double> q;
+    q.ia = k.ia; q.ib = k.ib;
+    q.ma = (double)k.ma; q.mb = (double)k.mb; q.iA = (double)k.iA; q.iB = (double)k.iB;
+    q.mcount = k.mcount; q.mtype = k.mtype;
+    q.lca = cvt<double>(k.lca); q.lcb = cvt<double>(k.lcb); q.ln = cvt<double>(k.ln); q.lp = cvt<double>(k.lp);
+    q.lpts[0] = cvt<double>(k.lpts[0]); q.lpts[1] = cvt<double>(k.lpts[1]);
+    q.ra = (double)k.ra; q.rb = (double)k.rb;
     return q;
 }
 // The fields solve_position reads.
@@ -1588,12 +1606,14 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         if (!is_static(ia)) { pc[ia] = ca; pa[ia] = aa; }
         if (!is_static(ib)) { pc[ib] = cb; pa[ib] = ab; }
     };
-    auto pos_check = [&]() {
+    // island early exit; bits 8-15 of the root's flags keep the number of
+    // iterations the island ran (the step record)
+    auto pos_check = [&](int it) {
         bool pending = false;
         for (int b = rank; b < nb; b += g.size()) {
             if (parent[b] != b || !(rootf[b] & R_SIM) || (rootf[b] & R_DONE)) continue;
             if (w.btype(b) == GB_BODY_STATIC) continue;
-            if (dkey_inv(minsep[b]) >= -3.0 * GB_LINEAR_SLOP) rootf[b] |= R_DONE | R_SOLVED;
+            if (dkey_inv(minsep[b]) >= -3.0 * GB_LINEAR_SLOP) rootf[b] |= R_DONE | R_SOLVED | ((uint32_t)(it + 1) << 8);
             else pending = true;
         }
         return g.any(pending);
@@ -1622,7 +1642,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
                 if (*pipe_fail) { failed = true; ++q; break; }
             }
             if (failed) break;
-            if (!pos_check()) break;
+            if (!pos_check(it)) break;
         }
         // drain the chunks issued past an early exit
         for (; q < issued; ++q) {
@@ -1649,10 +1669,17 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
                 }
                 g.sync();
             }
-            if (!pos_check()) break;
+            if (!pos_check(it)) break;
         }
     }
     g.sync();
+    if (sp.record_order)   // step record: position iterations of each body's island
+        for (int b = rank; b < nb; b += g.size()) {
+            if (w.btype(b) == GB_BODY_STATIC || !(rootf[parent[b]] & R_SIM)) continue;
+            const uint32_t rf = rootf[parent[b]];
+            const int its = (rf & R_DONE) ? (int)((rf >> 8) & 0xffu) : sp.pos_iters;
+            w.B.rec[w.bb + b] = (w.B.rec[w.bb + b] & ~0xff) | (its > 255 ? 255 : its);
+        }
     if (cached) {
         if constexpr (F32D) {
             for (int b = rank; b < nb; b += g.size()) {

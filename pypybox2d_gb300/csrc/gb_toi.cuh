@@ -11,7 +11,6 @@
 // event is group-parallel.
 #pragma once
 #include "gb_step.cuh"
-#include "gb_toi_f32.cuh"
 
 // world.py:617-653 for contact i at the start of a TOI pass: 0 = skipped
 // (disabled, sub-stepped too often, sensor, inactive, no bullet or
@@ -50,25 +49,20 @@ template <class R> __device__ double toi_align(const WView<R> &w, int i, Sweep *
     return alpha0;
 }
 
-// world.py:669-681: the time of impact from the aligned sweeps (float64)
+// world.py:669-681: the time of impact from the aligned sweeps.  Float64 in
+// both units: the root finder stops anywhere inside its tolerance band
+// (a quarter of the linear slop, toi.py:233-234) and the TOI position pass
+// stops at -1.5 slop (contact.py:931), which is where the TOI target leaves
+// the separation, so float32 arithmetic here moves the bodies by up to
+// ~1e-3 m against the float64 step.
 template <class R> __device__ void toi_compute(const WView<R> &w, int i, double alpha0, const Sweep &sa, const Sweep &sb) {
     ContactRec<R> &c = w.con(i);
     double beta;
     bool lim = false;
-#if defined(GB_POSE_ROT_F32)
-    // float32 unit: float32 arithmetic on sweeps relative to sweep A's start
-    FProxy pa, pb;
-    fproxy_init(pa, w.shape(c.fa));
-    fproxy_init(pb, w.shape(c.fb));
-    float beta_f = 1.0f;
-    int state = time_of_impact_f32(pa, pb, fsweep_of(sa, sa.c0), fsweep_of(sb, sa.c0), 1.0f, &beta_f, &lim);
-    beta = (double)beta_f;
-#else
     DProxy pa, pb;
     dproxy_init(pa, w.shape(c.fa));
     dproxy_init(pb, w.shape(c.fb));
     int state = time_of_impact(pa, pb, sa, sb, 1.0, &beta, &lim);
-#endif
     if (lim) atomicOr(&w.H->status, GB_ST_ITER_LIMIT);
     double alpha = (state == TOI_TOUCHING) ? pymin(alpha0 + (1.0 - alpha0) * beta, 1.0) : 1.0;
     c.toi = alpha;
@@ -112,47 +106,35 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
         }
         idx[k][0] = la; idx[k][1] = lb;
     }
-#if defined(GB_POSE_ROT_F32)
-    // float32 unit: the position passes on float32 deltas (solve_position_f32d);
-    // only the two TOI bodies move
-    {
-        vec2<float> cf[2 * GB_MAX_TOI_CONTACTS], dc[2 * GB_MAX_TOI_CONTACTS];
-        float ar[2 * GB_MAX_TOI_CONTACTS], da[2 * GB_MAX_TOI_CONTACTS];
-        for (int i = 0; i < nbi; ++i) {
-            cf[i] = cvt<float>(pc[i]); ar[i] = angle_f32(pa[i]);
-            dc[i] = mk<float>(0.0f, 0.0f); da[i] = 0.0f;
-        }
-        for (int it = 0; it < 20; ++it) {
-            float minsep = 0.0f;
-            for (int k = 0; k < nci; ++k) {
-                int la = idx[k][0], lb = idx[k][1];
-                minsep = solve_position_f32d(ks[k], cf[la], ar[la], dc[la], da[la], cf[lb], ar[lb], dc[lb], da[lb], minsep, true,
-                                             la == toi_a || la == toi_b, lb == toi_a || lb == toi_b);
-            }
-            if (minsep >= -1.5f * (float)GB_LINEAR_SLOP) break;
-        }
-        for (int i = 0; i < nbi; ++i) {
-            if (dc[i].x != 0.0f) pc[i].x = pc[i].x + (double)dc[i].x;
-            if (dc[i].y != 0.0f) pc[i].y = pc[i].y + (double)dc[i].y;
-            if (da[i] != 0.0f) pa[i] = pa[i] + (double)da[i];
-        }
-    }
-#else
+    // the position passes in float64 in both units (their early exit at
+    // -1.5 slop is where the TOI leaves the separation: see toi_compute)
+    int its = 0;
     for (int it = 0; it < 20; ++it) {
         double minsep = 0.0;
         for (int k = 0; k < nci; ++k) {
             int la = idx[k][0], lb = idx[k][1];
-            minsep = solve_position(ks[k], pc[la], pa[la], pc[lb], pa[lb], minsep, true,
-                                    la == toi_a || la == toi_b, lb == toi_a || lb == toi_b);
+            const Cons<double> kd = pos_cons_f64(ks[k]);
+            minsep = solve_position(kd, pc[la], pa[la], pc[lb], pa[lb], minsep, true, la == toi_a || la == toi_b,
+                                    lb == toi_a || lb == toi_b);
         }
+        its = it + 1;
         if (minsep >= -1.5 * GB_LINEAR_SLOP) break;
     }
-#endif
+    if (ev && ev->rec)
+        for (int t : {toi_a, toi_b}) {
+            rec_add_byte(&ev->rec[ib[t]], GB_REC_TOI_ITERS_SHIFT, its);
+            rec_add_byte(&ev->rec[ib[t]], GB_REC_TOI_EVENTS_SHIFT, 1);
+        }
     w.B.b_c0[w.bb + ib[toi_a]] = pc[toi_a]; w.B.b_a0[w.bb + ib[toi_a]] = pa[toi_a];
     w.B.b_c0[w.bb + ib[toi_b]] = pc[toi_b]; w.B.b_a0[w.bb + ib[toi_b]] = pa[toi_b];
     for (int k = 0; k < nci; ++k) {
         int la = idx[k][0], lb = idx[k][1];
         init_velocity(ks[k], pc[la], pa[la], pc[lb], pa[lb], vv[la], ww[la], vv[lb], ww[lb]);
+        if (ev && ev->rec) {   // step record: the sub-step's set-up decisions
+            const int bits = rec_setup_bits(ks[k].dec, GB_REC_SETUP_SHIFT + 2);
+            if (w.btype(ib[la]) != GB_BODY_STATIC) ev->rec[ib[la]] ^= bits;
+            if (w.btype(ib[lb]) != GB_BODY_STATIC) ev->rec[ib[lb]] ^= bits;
+        }
     }
     for (int it = 0; it < vel_iters; ++it)
         for (int k = 0; k < nci; ++k) {
@@ -568,7 +550,7 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
             if (w.btype(bia) == GB_BODY_DYNAMIC) body_contacts(w, off, adj, nc0, nc, bia, [&](int i) { la[na++] = i; });
             if (w.btype(bib) == GB_BODY_DYNAMIC) body_contacts(w, off, adj, nc0, nc, bib, [&](int i) { lb[nlb++] = i; });
             sh->nmove = 0;
-            const EvCtx ev{sp.events, sp.step_index, GB_EV_PHASE_TOI};
+            const EvCtx ev{sp.events, sp.step_index, GB_EV_PHASE_TOI, sp.record_order ? w.B.rec + w.bb : nullptr};
             toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh, la, na, lb, nlb, &ev);
             ck.mark(13);
         }
@@ -617,6 +599,8 @@ template <class R, class G> __device__ void world_step(const G &g, const WView<R
     PhaseClock pc;
     pc.acc = (sp.profile && g.rank() == 0) ? w.B.prof + (size_t)w.wi * GB_NPROF : nullptr;
     pc.start();
+    if (sp.record_order)
+        for (int b = g.rank(); b < w.H->nb; b += g.size()) w.B.rec[w.bb + b] = 0;
     if (w.H->flags & GB_W_NEW_FIXTURE) {
         int nf = w.H->nf;
         int n0 = w.H->nmove0;

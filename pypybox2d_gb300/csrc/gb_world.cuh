@@ -41,6 +41,7 @@ template <class R> struct Cons {
     R ni[2], ti[2], nm[2], tm[2], bias[2];
     R k11, k12, k22, nm11, nm12, nm21, nm22;
     vec2<R> ln, lp, lpts[2];
+    int dec;             // set-up decisions: restitution bias of point 0/1 (bits 0/1), block dropped to one point (bit 2)
 };
 
 // The solver's constraint records, stored colour-major.  ConsVel holds what
@@ -130,6 +131,7 @@ template <class R> struct Batch {
     struct TPlan *s_plan;        // GB_TOI_PLAN_CAP planned TOI sweeps per world
     int *toi_list;               // contact slots needing a first-pass TOI (batch-wide)
     int *toi_n;                  // their count
+    int *rec;                    // per body: the step record of the last record_order step
     gb_event *ev;                // contact events: 3 ccap + 64 per world, from 3 cbase + 64 world
     int *ev_n;                   // events recorded per world
     // worlds advanced by a cooperative grid (the first n_huge of the size-sorted list)
@@ -165,7 +167,25 @@ struct StepParams {
 #define GB_EV_PHASE_TOI 2
 struct EvCtx {
     int on, step, phase;
+    int *rec;         // the world's step record (record_order steps), else null
 };
+
+// Step record of a body (record_order steps; gb_batch_get_step_record):
+// decisions of the step that its final state does not show.
+#define GB_REC_TOI_ITERS_SHIFT 8    // TOI position-pass iterations, summed over its events (contact.py:866-933)
+#define GB_REC_TOI_EVENTS_SHIFT 16  // TOI events it took part in (world.py:693-817)
+#define GB_REC_SETUP_SHIFT 24       // parity of its constraints' restitution-bias points (bit 24) and block-solver
+                                    // drops (bit 25) in the island solve; bits 26/27 the same in TOI sub-steps
+                                    // (contact.py:470-496); bits 0-7: position iterations of its island
+static __device__ __forceinline__ void rec_add_byte(int *x, int shift, int v) {
+    int cur = (*x >> shift) & 0xff;
+    int nv = cur + v > 255 ? 255 : cur + v;
+    *x = (*x & ~(0xff << shift)) | (nv << shift);
+}
+// the parity bits of one constraint's set-up decisions (Cons::dec) at `shift`
+static __device__ __forceinline__ int rec_setup_bits(int dec, int shift) {
+    return ((((dec & 1) + ((dec >> 1) & 1)) & 1) << shift) | (((dec >> 2) & 1) << (shift + 1));
+}
 
 // Phase clocks: rank 0 adds the SM clock delta since the last mark.
 struct PhaseClock {

@@ -196,6 +196,44 @@ class GpuBatch:
         abi.check(self.lib.gb_batch_status(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), None))
         return out
 
+    def step_record(self, world: int = 0) -> np.ndarray:
+        """Per body of the world (world-local order) the step record of the
+        last step run with ``record_order`` (gb_batch_get_step_record):
+        bits 0-7 position iterations of its island, 8-15 TOI position-pass
+        iterations, 16-23 TOI events, 24-27 parities of its constraints'
+        restitution-bias and block-solver decisions (island solve, TOI)."""
+        cap = int(self.worlds["body_count"][world])
+        out = np.zeros(max(cap, 1), dtype=np.int32)
+        n = ctypes.c_int32()
+        abi.check(self.lib.gb_batch_get_step_record(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap,
+                                                    ctypes.byref(n), None))
+        return out[:n.value].copy()
+
+    def snapshot_bytes(self) -> int:
+        n = ctypes.c_uint64()
+        abi.check(self.lib.gb_batch_snapshot_bytes(self.h, ctypes.byref(n)))
+        return int(n.value)
+
+    def snapshot(self, dst_ptr: int | None = None, nbytes: int = 0, stream: int | None = None):
+        """The batch's whole device state (gb_batch_snapshot).  Without
+        ``dst_ptr`` it goes to a new host array, which is returned; with it, to
+        the caller's buffer of ``nbytes`` (host or device address)."""
+        if dst_ptr is None:
+            out = np.empty(self.snapshot_bytes(), dtype=np.uint8)
+            abi.check(self.lib.gb_batch_snapshot(self.h, out.ctypes.data, out.nbytes, ctypes.c_void_p(stream or 0)))
+            return out
+        abi.check(self.lib.gb_batch_snapshot(self.h, ctypes.c_void_p(dst_ptr), nbytes, ctypes.c_void_p(stream or 0)))
+        return None
+
+    def restore(self, src, nbytes: int = 0, stream: int | None = None) -> None:
+        """Put back a snapshot (gb_batch_restore): a host array from
+        ``snapshot()``, or a host/device address with its size."""
+        if isinstance(src, np.ndarray):
+            ptr, nbytes = src.ctypes.data, src.nbytes
+        else:
+            ptr = int(src)
+        abi.check(self.lib.gb_batch_restore(self.h, ctypes.c_void_p(ptr), nbytes, ctypes.c_void_p(stream or 0)))
+
 
 class StepGraph:
     """A captured multi-step rollout of a GpuBatch; ``launch()`` replays it

@@ -52,6 +52,8 @@ def load(libm: bool = False) -> ctypes.CDLL:
     lib.or_set_solver_order.argtypes = [vp, vp, i32]
     lib.or_get_solver_order.argtypes = [vp, vp, i32]
     lib.or_get_solver_order.restype = i32
+    lib.or_get_step_record.argtypes = [vp, vp]
+    lib.or_get_step_record.restype = None
     lib.or_toi_calls.argtypes = [vp]
     lib.or_toi_calls.restype = ctypes.c_longlong
     lib.or_toi_events.argtypes = [vp]
@@ -127,6 +129,12 @@ class OracleWorld:
 
     def status(self):
         return self.lib.or_status(self.h)
+
+    def step_record(self):
+        """Per body the step record of the last step (or_get_step_record)."""
+        out = np.zeros(max(self.nb, 1), dtype=np.int32)
+        self.lib.or_get_step_record(self.h, out.ctypes.data)
+        return out[:self.nb].copy()
 
 
 class OracleBatch:

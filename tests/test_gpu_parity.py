@@ -2,7 +2,9 @@
 
 The float64 path (-fmad=false, portable sincos) must reproduce the oracle
 bit for bit -- bodies, fat AABBs, contact list, manifolds, impulses, feature
-ids, touching/enabled flags, sleep state -- step after step, with the
+ids, touching/enabled flags, sleep state, and the step record (position
+iterations of each island, TOI position-pass iterations and events and the
+solver set-up decisions of each body) -- step after step, with the
 oracle solving each island in the GPU's graph-coloured constraint order
 (the solver-order hook).  The scenes are the reference-exported initial
 states of the golden vectors (pyramid, mixed edge/circle/polygon box,
@@ -64,6 +66,7 @@ def run_lockstep(scene, steps, launch_mode=1, block_threads=0):
         assert_same(gpu.bodies(), orc.bodies(), f"{scene} step {s} bodies")
         assert np.array_equal(gpu.proxies(), orc.fixtures()["aabb"]), f"{scene} step {s} fat AABBs"
         assert_same(used_contact_view(gpu.contacts(0)), used_contact_view(orc.contacts()), f"{scene} step {s} contacts")
+        assert np.array_equal(gpu.step_record(0), orc.step_record()), f"{scene} step {s} step record"
     assert int(gpu.status()[0]) == 0
     return gpu, orc
 
@@ -104,6 +107,7 @@ def test_f64_large_world_bit_exact_with_oracle(kind, n_bodies):
         orc.step(1 / 60, 8, 3, order=gpu.solver_order(0))
         assert_same(gpu.bodies(), orc.bodies(), f"large world step {s} bodies")
         assert_same(used_contact_view(gpu.contacts(0)), used_contact_view(orc.contacts()), f"large world step {s} contacts")
+        assert np.array_equal(gpu.step_record(0), orc.step_record()), f"large world step {s} step record"
     assert int(gpu.status()[0]) == 0
 
 
@@ -120,4 +124,5 @@ def test_f64_grid_world_bit_exact_with_oracle():
         orc.step(1 / 60, 8, 3, order=gpu.solver_order(0))
         assert_same(gpu.bodies(), orc.bodies(), f"grid world step {s} bodies")
         assert_same(used_contact_view(gpu.contacts(0)), used_contact_view(orc.contacts()), f"grid world step {s} contacts")
+        assert np.array_equal(gpu.step_record(0), orc.step_record()), f"grid world step {s} step record"
     assert int(gpu.status()[0]) == 0
