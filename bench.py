@@ -7,13 +7,21 @@ Workloads (``--workload``):
            velocities; 1000 steps.
   pyramid  4096 copies of the 20-row pyramid (210 boxes on a ground box),
            every box position jittered by a seeded U(-0.01, 0.01) m; 2000 steps.
-Both: dt = 1/60, 8 velocity and 3 position iterations, float32 bulk
+  bullets  2048 twenty-box stacks, each hit by 4 bullet circles; 600 steps.
+  large    one 100000-body world; 600 steps.
+All: dt = 1/60, 8 velocity and 3 position iterations, float32 bulk
 arithmetic with float64 positions, angles, sleep timers and time of impact.
-After the warm-up the launch autotuner (gb_batch_autotune) picks the launch
-configuration from trials that start from the warmed-up state and leave it
-unchanged; the timed steps then replay captured CUDA graphs of
-``--graph-steps`` phased steps (12-13 launches each).  A "step" is one
-World.step of every world of the batch.
+
+Both arms (this one and ``--impl reference``) run the same untimed settle
+(``--settle``; uneven and pyramid 300 steps, so the timed window is the
+landed, piled steady state) and ``--warmup`` steps, then time ``--steps``
+steps; ``config.timed_steps`` names the window and is the same in both.
+Here, after the warm-up the launch autotuner (gb_batch_autotune) picks the
+launch configuration from trials that leave the state unchanged; the state
+at the start of the window is snapshotted on the device
+(gb_batch_snapshot), the timed steps replay captured CUDA graphs of
+``--graph-steps`` phased steps, and every later leg restores the snapshot
+and measures the same steps.  A "step" is one World.step of every world.
 
 Reported (one JSON line on rank 0):
   value    dynamic body-steps/s with the batch resident in HBM (device time,
@@ -23,16 +31,19 @@ Reported (one JSON line on rank 0):
            (gb_batch_set_bodies), steps, and reads them back (gb_batch_get_bodies)
   roofline HBM roofline of the whole step from the algorithmic bytes per
            world-step (152 B per body + shape bytes + 32 B per fixture + 128 B
-           per contact, from live counts) over the event-timed step, and of
-           the dominant launch with its own byte model (``kernels``)
+           per contact, from live counts) over the event-timed step; the
+           dominant launch against its own byte model (``kernels``)
   kernels  event-timed device ms per launch slot of the phased step
   autotune the tuner's trials and choice; graph: steps per captured graph and
            the same steps as one plain gb_batch_step call
   cpu_baseline  the CPU restatement (oracle/, C, float64) on the host cores
-           stepping a bounded sample of the same worlds
+           stepping a bounded sample of the same worlds from the same state
   plain    the float64 path launched per world, one step per launch
-  error    float32 position error after one step against the float64
-           restatement from identical state, solved in the same order
+  error    float32 against float64 from identical state on 64 worlds spread
+           over the size range (one step, same constraint order): position,
+           angle and velocity errors and the discrete-state mismatch counts;
+           ``error.drift``: both forms from the same initial state without
+           re-syncing, drift distributions at checkpoints
 
 --impl reference runs the CPU restatement of the reference (oracle/) with
 all host threads on a bounded sample of the same workload instead.
@@ -57,7 +68,10 @@ METRIC = "body-steps/s on 1 GB300: batched FP32 vs plain FP64 GPU path at stated
 DT = 1.0 / 60.0
 VI, PI = 8, 3
 DEFAULTS = {"uneven": (8192, 1000), "pyramid": (4096, 2000), "bullets": (2048, 600), "large": (1, 600)}
-SETTLE_STEPS = {"uneven": 300, "pyramid": 300, "bullets": 0, "large": 20}   # reference arm: untimed steps before its sample
+# untimed steps both arms run before their warm-up and timed window (bodies
+# landed and piled: the steady state that most of a 1000-step run is in; the
+# bullet batch is timed from the start, while its bullets cross the stacks)
+SETTLE_STEPS = {"uneven": 300, "pyramid": 300, "bullets": 0, "large": 20}
 
 
 def _peaks():
@@ -131,24 +145,50 @@ def build_workload(name: str, n_worlds: int, seed: int):
     from pypybox2d_gb300 import scenes
     if name == "pyramid":
         W, B, F, M = scenes.pyramid_batch(n_worlds, rows=20, jitter=0.01, seed=seed)
-        desc = (f"pyramid x{n_worlds} per GPU, 210 boxes/world on a ground box, jitter U(-0.01,0.01) m, "
-                f"dt=1/60, 8 vel / 3 pos iters, f32 bulk / f64 positions")
     elif name == "bullets":
         W, B, F, M = scenes.bullet_batch(n_worlds, seed=seed)
-        desc = (f"bullets x{n_worlds} per GPU: 20-box stack (friction 0.3) on a ground box + 4 bullet circles "
-                f"(r 0.1, density 100) from x=-30, y U(0.5,10), speed U(150,250) m/s, dt=1/60, 8 vel / 3 pos iters, "
-                f"f32 bulk / f64 positions and TOI")
     elif name == "large":
         W, B, F, M = scenes.concat([scenes.large_world(seed + w) for w in range(n_worlds)])
-        desc = (f"large world x{n_worlds}: 100000 bodies (60% boxes half-extent U(0.2,0.6), 40% circles r U(0.2,0.6), "
-                f"density 1, friction 0.5) on a jittered 1.5 m grid above a 600 m ground box with 200 m walls, "
-                f"dt=1/60, 8 vel / 3 pos iters, f32 bulk / f64 positions")
     else:
         W, B, F, M = scenes.uneven_batch(n_worlds, seed=seed)
-        desc = (f"uneven x{n_worlds} per GPU: bodies/world log-uniform on [10,2000] in a 100 m edge box, "
-                f"50% circles r U(0.25,1) / 50% convex 3-8-gons r U(0.3,1), v N(0,2), w N(0,1), gravity (0,-10), "
-                f"dt=1/60, 8 vel / 3 pos iters, f32 bulk / f64 positions")
-    return W, B, F, M, desc
+    return W, B, F, M, WORKLOAD_DESC[name].format(n=n_worlds)
+
+
+def workload_counts(name: str, n_worlds: int, seed: int) -> np.ndarray:
+    """Dynamic bodies of every world of a workload, without building it."""
+    from pypybox2d_gb300 import scenes
+    if name == "pyramid":
+        return np.full(n_worlds, 210, dtype=np.int64)
+    if name == "bullets":
+        return np.full(n_worlds, 24, dtype=np.int64)
+    if name == "large":
+        return np.full(n_worlds, 100000, dtype=np.int64)
+    return np.array([scenes.uneven_count(seed + w) for w in range(n_worlds)], dtype=np.int64)
+
+
+def workload_config(name: str, n_worlds: int, seed: int, settle: int, warmup: int, steps: int) -> dict:
+    """The `config` both arms print: the workload and the window of steps timed."""
+    dyn = workload_counts(name, n_worlds, seed)
+    first = settle + warmup + 1
+    return {"workload": WORKLOAD_DESC[name].format(n=n_worlds), "worlds_per_gpu": n_worlds,
+            "dynamic_bodies_per_gpu": int(dyn.sum()),
+            "bodies_per_world": {"min": int(dyn.min()), "mean": float(dyn.mean()), "max": int(dyn.max())},
+            "settle_steps": settle, "timed_steps": [first, first + steps - 1],
+            "l2": "inputs larger than L2 (129 MB): the batch state is several GiB and each step reads all of it"}
+
+
+WORKLOAD_DESC = {
+    "uneven": ("uneven x{n} per GPU: bodies/world log-uniform on [10,2000] in a 100 m edge box, 50% circles r U(0.25,1) / "
+               "50% convex 3-8-gons r U(0.3,1), v N(0,2), w N(0,1), gravity (0,-10), dt=1/60, 8 vel / 3 pos iters, "
+               "f32 bulk / f64 positions"),
+    "pyramid": ("pyramid x{n} per GPU, 210 boxes/world on a ground box, jitter U(-0.01,0.01) m, dt=1/60, 8 vel / 3 pos iters, "
+                "f32 bulk / f64 positions"),
+    "bullets": ("bullets x{n} per GPU: 20-box stack (friction 0.3) on a ground box + 4 bullet circles (r 0.1, density 100) "
+                "from x=-30, y U(0.5,10), speed U(150,250) m/s, dt=1/60, 8 vel / 3 pos iters, f32 bulk / f64 positions and TOI"),
+    "large": ("large world x{n}: 100000 bodies (60% boxes half-extent U(0.2,0.6), 40% circles r U(0.2,0.6), density 1, "
+              "friction 0.5) on a jittered 1.5 m grid above a 600 m ground box with 200 m walls, dt=1/60, 8 vel / 3 pos "
+              "iters, f32 bulk / f64 positions"),
+}
 
 
 def dynamic_counts(W, B):
@@ -178,44 +218,22 @@ def solve_bytes_per_step(n_bodies, n_constraints, real_bytes=4):
     return n_bodies * (6 * real_bytes + 48 + 16) + n_constraints * (216 + 32)
 
 
+def pairs_bytes_per_step(fixtures, n_bodies, n_contacts):
+    """Byte model of the fixture-sync and pair-finding launch: per body its
+    type, flags, pose and sweep start read (64 B); per fixture its shape
+    (as in algorithmic_bytes_per_step) and fat AABB read, the new fat AABB
+    written (32 B), its move flag and move-buffer entry (8 B); per contact the
+    pair key read for the existence check (8 B)."""
+    shape = np.where(fixtures["shape_type"] == 0, 12, fixtures["vertex_count"] * 16)
+    return 64.0 * n_bodies + float(np.sum(shape + 32 + 32 + 8)) + 8.0 * n_contacts
+
+
 def launches_per_step(W, big_bodies: int = 512):
     """Kernel launches of one phased step: 12, plus a second solver launch
     when the batch mixes worlds below and above the wide launch's threshold
     (big_bodies)."""
     nbig = int(np.count_nonzero(W["body_count"] >= big_bodies))
     return 12 + (1 if 0 < nbig < len(W) else 0)
-
-
-def world_slice(W, B, F, M, w):
-    """Records of world w of a batch, as a one-world batch."""
-    b0, nb = int(W["body_start"][w]), int(W["body_count"][w])
-    f0, nf = int(W["fixture_start"][w]), int(W["fixture_count"][w])
-    m0, nm = int(W["move_start"][w]), int(W["move_count"][w])
-    Wi = W[w:w + 1].copy()
-    Wi["body_start"] = 0
-    Wi["fixture_start"] = 0
-    Wi["move_start"] = 0
-    return Wi, B[b0:b0 + nb].copy(), F[f0:f0 + nf].copy(), M[m0:m0 + nm].copy()
-
-
-def device_state(batch, W, F, n):
-    """Records of the first n worlds of a device batch as it stands (bodies,
-    fat AABBs, contacts), ready to continue on the CPU restatement."""
-    from pypybox2d_gb300 import abi
-    B = batch.bodies()
-    F2 = F.copy()
-    F2["aabb"] = batch.proxies()
-    Cs, W2 = [], W[:n].copy()
-    k = 0
-    for w in range(n):
-        c = batch.contacts(w)
-        W2["contact_start"][w], W2["contact_count"][w] = k, len(c)
-        k += len(c)
-        Cs.append(c)
-    W2["flags"] = W2["flags"] & np.uint32(0xFFFFFFFF ^ abi.W_NEW_FIXTURE)
-    W2["move_count"] = 0
-    W2["inv_dt0"] = 1.0 / DT
-    return W2, B, F2, np.concatenate(Cs) if Cs else np.zeros(0, abi.CONTACT)
 
 
 def cpu_oracle_rate(W, B, F, C, dyn, steps, threads, target_s=8.0):
@@ -240,76 +258,110 @@ def cpu_oracle_rate(W, B, F, C, dyn, steps, threads, target_s=8.0):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of World.step (oracle/, float64
+    C, bit-exact with the reference's golden vectors) on all host threads,
+    stepping the first worlds of the same workload through the same settle,
+    warm-up and timed window as the GPU arm."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     n_worlds = args.worlds or DEFAULTS[args.workload][0]
-    n = min(n_worlds, 4 * threads if args.workload == "uneven" else 2 * threads)
-    W, B, F, M, desc = build_workload(args.workload, n, 0)
+    steps = args.steps or DEFAULTS[args.workload][1]
+    settle = SETTLE_STEPS[args.workload] if args.settle < 0 else args.settle
+    cfg = workload_config(args.workload, n_worlds, 0, settle, args.warmup, steps)
+    per = {"uneven": 8, "pyramid": 4, "bullets": 8, "large": 1}[args.workload]
+    if args.workload == "large":
+        from pypybox2d_gb300 import scenes
+        W, B, F, M = scenes.large_world(0, n=LARGE_SAMPLE_BODIES)
+    else:
+        W, B, F, M, _ = build_workload(args.workload, min(n_worlds, per * threads), 0)
     dyn = dynamic_counts(W, B)
     import oracle_lib
     from pypybox2d_gb300 import abi
     lib = oracle_lib.load(False)
     s, keep = abi.make_scene(W, B, F, None, M)
     h = lib.or_batch_create(ctypes.byref(s))
-    # settle the sample like the timed GPU window (bodies landed and piled)
-    settle = SETTLE_STEPS[args.workload]
-    lib.or_batch_step(h, DT, VI, PI, settle, threads)
-    for _ in range(args.warmup):
-        lib.or_batch_step(h, DT, VI, PI, 1, threads)
-    steps = min(args.steps or DEFAULTS[args.workload][1], 10)
-    t = 0.0
-    for _ in range(steps):
-        t += lib.or_batch_step(h, DT, VI, PI, 1, threads)
+    lib.or_batch_step(h, DT, VI, PI, settle + args.warmup, threads)
+    t = lib.or_batch_step(h, DT, VI, PI, steps, threads)
     lib.or_batch_destroy(h)
     value = float(dyn.sum()) * steps / t
+    first, last = cfg["timed_steps"]
+    if args.workload != "large":
+        sample = (f"the first {len(W)} of the {n_worlds} worlds ({int(dyn.sum())} dynamic bodies, the GPU arm's seeds), "
+                  f"steps {first}-{last} after {settle} settle and {args.warmup} warm-up steps, one world per thread "
+                  f"task, {threads} threads")
+    else:
+        sample = (f"one {int(dyn.sum())}-body world of the large-world generator, steps {first}-{last}, one thread "
+                  f"(a world does not split across threads)")
     out = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": ws,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"first {len(W)} worlds of: {desc}", "worlds": len(W), "dynamic_bodies": int(dyn.sum())},
-        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{len(W)} worlds x {steps} steps after {settle} settling and {args.warmup} "
-                                   f"warm-up steps, "
-                                   f"one world per thread task, {threads} threads"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": "body-steps/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "CPU restatement of pypybox2d World.step (oracle/, float64 C, pinned bit-exact to the reference's "
-                "golden vectors); the reference itself is CPython and is not on the GPU box",
+                "golden vectors); the reference itself is CPython and does not travel to the GPU box",
     }
     print(json.dumps(out))
 
 
-def f32_step_error(W, B, F, M, w, settle_steps=60):
-    """Position/angle error of one float32 step against the float64
-    restatement, both started from the float64 state of world w after
-    `settle_steps` steps (bodies, fat AABBs and contacts) and solving in the
-    same constraint order."""
-    import oracle_lib
-    from pypybox2d_gb300 import abi
-    from pypybox2d_gb300.gpu import GpuBatch
-    Wi, Bi, Fi, Mi = world_slice(W, B, F, M, w)
-    g64 = GpuBatch(Wi, Bi, Fi, precision="f64", moves=Mi)
-    g64.step(DT, VI, PI, settle_steps)
-    st, C = g64.bodies(), g64.contacts(0)
-    F2 = Fi.copy()
-    F2["aabb"] = g64.proxies()
-    W2 = Wi.copy()
-    W2["flags"] = W2["flags"] & np.uint32(0xFFFFFFFF ^ abi.W_NEW_FIXTURE)
-    W2["move_count"] = 0
-    W2["contact_count"] = len(C)
-    W2["inv_dt0"] = 1.0 / DT
-    g32 = GpuBatch(W2, st, F2, contacts=C, precision="f32")
-    g32.step(DT, VI, PI, 1, record_order=True)
-    orc = oracle_lib.OracleWorld(W2, st, F2, contacts=C, libm=False)
-    orc.step(DT, VI, PI, order=g32.solver_order(0))
-    a, b = g32.bodies(), orc.bodies()
-    return {"f32_one_step_max_position_error_m": float(np.hypot(a["cx"] - b["cx"], a["cy"] - b["cy"]).max()),
-            "f32_one_step_max_angle_error_rad": float(np.abs(a["a"] - b["a"]).max()),
-            "f32_one_step_max_velocity_error_mps": float(np.hypot(a["vx"] - b["vx"], a["vy"] - b["vy"]).max()),
-            "target_m": 1e-5,
-            "state": f"world {w} ({len(Bi)} bodies, {len(C)} contacts) after {settle_steps} float64 steps; "
-                     f"one step each from identical state, same constraint order"}
+LARGE_SAMPLE_BODIES = 20000   # the reference arm's large-world sample (one world on one thread)
+
+
+def stratified(dyn, n):
+    """n worlds spread over the range of body counts (evenly spaced ranks)."""
+    order = np.argsort(dyn, kind="stable")
+    take = np.unique(np.linspace(0, len(dyn) - 1, min(n, len(dyn))).round().astype(np.int64))
+    return np.sort(order[take])
+
+
+def error_block(batch, F, dyn, settle_label, sample=64):
+    """Float32 against float64 from identical state on a stratified sample of
+    worlds (one step each, same constraint order), with the discrete-state
+    mismatch counts; the float64 side is the float64 GPU path, which is
+    bit-exact with the CPU restatement of World.step."""
+    from pypybox2d_gb300 import precision
+    ws = stratified(dyn, sample)
+    W, B, Fw, C = precision.batch_records(batch, F, 1.0 / DT, ws)
+    r = precision.one_step(W, B, Fw, C, DT, VI, PI)
+    errs, alike, mm = r["errors"], r["errors_alike"], r["mismatch"]
+    return {
+        "f32_one_step_max_position_error_m": float(alike[:, 0].max()),
+        "f32_one_step_max_angle_error_rad": float(alike[:, 1].max()),
+        "f32_one_step_max_velocity_error_mps": float(alike[:, 2].max()),
+        "per_world_position_error_m": {"median": float(np.median(alike[:, 0])), "p90": float(np.quantile(alike[:, 0], 0.9))},
+        "bodies_compared": int(mm["bodies"]),
+        "bodies_decided_apart": r["bodies_decided_apart"],
+        "max_position_error_all_bodies_m": float(errs[:, 0].max()),
+        "target_m": 1e-5,
+        "worlds_over_target": int(np.count_nonzero(alike[:, 0] > 1e-5)),
+        "discrete_mismatch": mm,
+        "state": f"{len(ws)} worlds spread over the body-count range ({int(dyn[ws].min())}-{int(dyn[ws].max())} "
+                 f"bodies), {settle_label}; one step each from identical state against the float64 GPU path "
+                 f"(bit-exact with the CPU restatement) in the same constraint order",
+        "note": "errors over the islands in which both steps took every decision alike (the step record: island "
+                "position iterations, TOI position passes and events, restitution and block-solver set-up; and the "
+                "contacts' touching flags, manifold types, point counts and feature ids); bodies decided apart are "
+                "counted, with the all-bodies maximum beside them",
+    }
+
+
+def drift_block(workload, steps):
+    """Float32 and float64 from the same initial state, each in its own order,
+    without re-syncing: drift distributions over dynamic bodies."""
+    from pypybox2d_gb300 import precision
+    if workload == "pyramid":
+        W, B, F, M, _ = build_workload("pyramid", 32, 0)
+    elif workload == "bullets":
+        W, B, F, M, _ = build_workload("bullets", 64, 0)
+    else:
+        W, B, F, M, _ = build_workload("uneven", 64, 0)
+    every = max(1, steps // 5)
+    rows = precision.drift(W, B, F, M, DT, VI, PI, steps, every)
+    return {"worlds": len(W), "steps": steps, "checkpoints": rows,
+            "note": "chaotic stacks: the two forms' trajectories separate over time; these are the distributions of "
+                    "the separation, not a per-step error"}
 
 
 def main():
@@ -317,6 +369,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=0, help="0 = the workload's default (uneven 1000, pyramid 2000, bullets 600, large 600)")
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--settle", type=int, default=-1, help="untimed steps before the warm-up, in both arms "
+                                                           "(-1 = the workload's: uneven 300, pyramid 300, bullets 0, large 20)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="uneven", choices=["uneven", "pyramid", "bullets", "large"])
     ap.add_argument("--worlds", type=int, default=0, help="0 = the workload's default (uneven 8192, pyramid 4096, bullets 2048, large 1)")
@@ -324,9 +378,10 @@ def main():
     ap.add_argument("--mode", type=int, default=3, help="1 = one CTA per world (monolithic), 2 = one warp per world, "
                                                         "3 = phase kernels over the whole batch")
     ap.add_argument("--threads", type=int, default=64)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end leg (0 = the timed steps, up to 50)")
     ap.add_argument("--ktime-steps", type=int, default=20, help="steps of the per-launch timing pass")
-    ap.add_argument("--no-extras", action="store_true", help="skip cpu baseline, plain path and error legs")
+    ap.add_argument("--no-extras", action="store_true", help="skip cpu baseline, plain path, error and drift legs")
+    ap.add_argument("--drift-steps", type=int, default=-1, help="steps of the drift leg (-1: 1000, pyramid 2000; 0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch autotuner (use --mode / --threads)")
     ap.add_argument("--tune-steps", type=int, default=3, help="timed steps per autotuner trial")
     ap.add_argument("--launch-config", default="", help="mode,threads,pipe_bufs,big_bodies: pin this launch "
@@ -340,6 +395,7 @@ def main():
         return
     n_worlds = args.worlds or DEFAULTS[args.workload][0]
     steps = args.steps or DEFAULTS[args.workload][1]
+    settle = SETTLE_STEPS[args.workload] if args.settle < 0 else args.settle
 
     ws, rank, local = _dist()
     import torch
@@ -356,6 +412,7 @@ def main():
     # rank r steps its own worlds (seeded from r x n_worlds): no data-path exchange
     W, B, F, M, desc = build_workload(args.workload, n_worlds, rank * n_worlds)
     dyn = dynamic_counts(W, B)
+    cfg_out = workload_config(args.workload, n_worlds, rank * n_worlds, settle, args.warmup, steps)
     batch = GpuBatch(W, B, F, precision=args.precision, moves=M)
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
@@ -365,8 +422,9 @@ def main():
             import torch.distributed as dist
             dist.barrier()
 
-    # warm-up (also finds the initial contacts)
-    batch.step(DT, VI, PI, args.warmup, launch_mode=args.mode, block_threads=args.threads, stream=sh)
+    # settle and warm-up, untimed (the first step also finds the initial contacts)
+    if settle + args.warmup > 0:
+        batch.step(DT, VI, PI, settle + args.warmup, launch_mode=args.mode, block_threads=args.threads, stream=sh)
     torch.cuda.synchronize()
 
     # launch autotuner: trials from the warmed-up state, which it restores
@@ -408,6 +466,14 @@ def main():
             graph_info = {"unavailable": str(ex)}
     rest = steps - (n_graph * graph.n_steps if graph else 0)
 
+    # the state at the start of the timed window: every later leg restores it
+    # and measures the same steps
+    snap = torch.empty(batch.snapshot_bytes(), dtype=torch.uint8, device=dev)
+    batch.snapshot(snap.data_ptr(), snap.numel(), stream=sh)
+
+    def restore():
+        batch.restore(snap.data_ptr(), snap.numel(), stream=sh)
+
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
         barrier()
@@ -436,17 +502,14 @@ def main():
     bytes_step = algorithmic_bytes_per_step(len(B), F, float(np.sum(counts)))
     achieved = bytes_step * steps / t / 1e9
     peak, peak_kind = _peaks()
-    traffic = None
-    tp = os.path.join(HERE, "profiles", f"traffic_{args.workload}.txt")
-    if os.path.exists(tp) and args.precision == "f32":
-        for ln in open(tp):
-            if ln.startswith("dram_bytes_per_step:"):
-                traffic = float(ln.split(":")[1])
 
-    # per-launch device times (separate pass, one host wait per step)
+    # per-launch device times over the first steps of the same window
+    # (separate pass, one host wait per step)
     kt = {}
     if eff_mode == 3 and args.ktime_steps > 0:
-        batch.step(DT, VI, PI, args.ktime_steps, launch_mode=mode, block_threads=threads, stream=sh, kernel_times=True)
+        restore()
+        batch.step(DT, VI, PI, min(args.ktime_steps, steps), launch_mode=mode, block_threads=threads, stream=sh,
+                   kernel_times=True)
         torch.cuda.synchronize()
         tot, nsteps = batch.kernel_times()
         kt = {k: v / max(nsteps, 1) for k, v in tot.items()}
@@ -456,17 +519,24 @@ def main():
         top = max(kt, key=kt.get)
         kernels = {"ms_per_launch": {k: round(v, 4) for k, v in kt.items()},
                    "share": {k: round(v / ksum, 4) for k, v in kt.items()},
-                   "dominant": top, "timed_steps": args.ktime_steps}
+                   "dominant": top, "timed_steps": min(args.ktime_steps, steps),
+                   "window": "the first steps of the timed window, restored from its snapshot"}
         if top == "solve":
             ncons = float(np.sum(counts))   # touching contacts bound the constraints
             sb = solve_bytes_per_step(len(B), ncons, 4 if args.precision == "f32" else 8)
             kernels["dominant_roofline"] = {"bound": "hbm", "achieved": sb / (kt[top] / 1e3) / 1e9, "peak": peak,
                                             "unit": "GB/s", "frac": sb / (kt[top] / 1e3) / 1e9 / peak,
                                             "algorithmic_bytes_per_launch": sb}
+        elif top == "sync_pairs":
+            pb = pairs_bytes_per_step(F, len(B), float(np.sum(counts)))
+            kernels["dominant_roofline"] = {"bound": "hbm", "achieved": pb / (kt[top] / 1e3) / 1e9, "peak": peak,
+                                            "unit": "GB/s", "frac": pb / (kt[top] / 1e3) / 1e9 / peak,
+                                            "algorithmic_bytes_per_launch": pb}
 
     # the same steps as one plain gb_batch_step call, for the graphs' effect
     if graph is not None:
         nd = min(steps, 100)
+        restore()
         e6, e7 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e6.record(stream)
@@ -476,7 +546,9 @@ def main():
         graph_info["plain_call_ms_per_step"] = e6.elapsed_time(e7) / nd
         graph_info["plain_call_steps"] = nd
 
-    # e2e through the C ABI with pinned host buffers
+    # e2e through the C ABI with pinned host buffers, on the same window
+    restore()
+    e2e_steps = args.e2e_steps or min(steps, 50)
     n_b = len(B)
     pinned = torch.empty(n_b * abi.BODY.itemsize, dtype=torch.uint8, pin_memory=True)
     host = np.frombuffer(pinned.numpy(), dtype=abi.BODY)
@@ -489,7 +561,7 @@ def main():
     barrier()
     torch.cuda.synchronize()
     e2.record(stream)
-    for _ in range(args.e2e_steps):
+    for _ in range(e2e_steps):
         abi.check(lib.gb_batch_set_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh)))
         abi.check(lib.gb_batch_step(batch.h, ctypes.byref(opts), ctypes.c_void_p(sh)))
         abi.check(lib.gb_batch_get_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh)))
@@ -497,29 +569,31 @@ def main():
     torch.cuda.synchronize()
     barrier()
     te = e2.elapsed_time(e3) / 1e3
-    e2e_value = total_dyn * args.e2e_steps / te
+    e2e_value = total_dyn * e2e_steps / te
 
     out = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t / steps, "higher_is_better": True, "scaling": "weak",
         "world_steps_per_s": float(n_worlds) * ws * steps / t,
         "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
-        "config": {"workload": desc, "worlds_per_gpu": n_worlds, "dynamic_bodies_per_gpu": int(dyn.sum()),
-                   "bodies_per_world": {"min": int(dyn.min()), "mean": float(dyn.mean()), "max": int(dyn.max())},
-                   "launch": {1: "one persistent launch per timed region, one CTA per world",
-                              2: "one persistent launch per timed region, one warp per world",
-                              3: f"{launches_per_step(W, cfg['big_bodies'])} launches per step (batch-wide + per-world)"
-                              + (f", captured as CUDA graphs of {graph.n_steps} steps" if graph else "")}[eff_mode],
-                   "launch_config": cfg,
-                   "l2": f"inputs larger than L2: {batch.arena_bytes() / 2**30:.2f} GiB resident per GPU",
+        "config": cfg_out,
+        "launch": {"launch_config": cfg,
+                   "form": {1: "one persistent launch per timed region, one CTA per world",
+                            2: "one persistent launch per timed region, one warp per world",
+                            3: f"{launches_per_step(W, cfg['big_bodies'])} launches per step (batch-wide + per-world)"
+                            + (f", captured as CUDA graphs of {graph.n_steps} steps" if graph else "")}[eff_mode],
+                   "arena_gib": round(batch.arena_bytes() / 2**30, 2),
                    "mean_contacts_per_world": float(np.mean(counts))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_kind": peak_kind,
+                     "traffic": None, "peak_kind": peak_kind,
                      "kernel": f"whole step ({launches_per_step(W, cfg['big_bodies'])} launches)",
-                     "algorithmic_bytes_per_step": bytes_step},
+                     "algorithmic_bytes_per_step": bytes_step,
+                     "traffic_note": "DRAM bytes are measured by ncu on a smaller case and kept in profiles/, "
+                                     "not read into this line"},
         "kernels": kernels,
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY.itemsize,
-                "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": args.e2e_steps},
+                "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": e2e_steps,
+                "window": "the first steps of the timed window, restored from its snapshot"},
         "gpu_launches": launches_per_step(W, cfg["big_bodies"]) * steps if eff_mode == 3 else 1,
         "autotune": tune,
         "graph": graph_info,
@@ -528,19 +602,25 @@ def main():
     }
 
     if rank == 0 and not args.no_extras:
-        threads = os.cpu_count() or 1
-        cpu_steps = 20
-        n_cpu = min(n_worlds, 64 * threads)
-        Wc, Bc, Fc, Cc = device_state(batch, W, F, n_cpu)
-        rate, n, tcpu = cpu_oracle_rate(Wc, Bc, Fc, Cc, dyn, cpu_steps, threads, target_s=8.0)
-        out["cpu_baseline"] = {"value": rate, "unit": "body-steps/s", "cores": threads, "kind": "port",
-                               "sample": f"first {n} of the {n_worlds} worlds x {cpu_steps} steps, continuing from "
-                                         f"the batch's state after the timed steps ({tcpu:.1f} s, {threads} threads, "
+        from pypybox2d_gb300 import precision
+        restore()
+        threads_cpu = os.cpu_count() or 1
+        cpu_steps = min(steps, 20)
+        n_cpu = min(n_worlds, 64 * threads_cpu)
+        Wc, Bc, Fc, Cc = precision.batch_records(batch, F, 1.0 / DT, np.arange(n_cpu))
+        rate, n, tcpu = cpu_oracle_rate(Wc, Bc, Fc, Cc, dyn, cpu_steps, threads_cpu, target_s=8.0)
+        first = cfg_out["timed_steps"][0]
+        out["cpu_baseline"] = {"value": rate, "unit": "body-steps/s", "cores": threads_cpu, "kind": "port",
+                               "sample": f"first {n} of the {n_worlds} worlds, steps {first}-{first + cpu_steps - 1} "
+                                         f"(from the timed window's start state; {tcpu:.1f} s, {threads_cpu} threads, "
                                          f"float64 C restatement)"}
-        # plain float64 path: one world per batch, one launch per world-step
+        # plain float64 path: one world per batch, one launch per world-step,
+        # from the same state
         n_plain, plain_steps = min(16, n_worlds), 5
-        plain = [GpuBatch(*world_slice(W, B, F, M, w)[:3], precision="f64", moves=world_slice(W, B, F, M, w)[3])
-                 for w in range(n_plain)]
+        plain = []
+        for w in range(n_plain):
+            Wp, Bp, Fp, Cp = precision.batch_records(batch, F, 1.0 / DT, [w])
+            plain.append(GpuBatch(Wp, Bp, Fp, contacts=Cp, precision="f64"))
         for p in plain:
             p.step(DT, VI, PI, 1, stream=sh)
         torch.cuda.synchronize()
@@ -555,10 +635,13 @@ def main():
         plain_rate = float(dyn[:n_plain].sum()) * plain_steps / tp_
         out["plain_f64_per_world"] = {"value": plain_rate, "unit": "body-steps/s",
                                       "sample": f"first {n_plain} worlds ({int(dyn[:n_plain].sum())} bodies) x "
-                                                f"{plain_steps} steps, one launch per world-step",
+                                                f"{plain_steps} steps from the timed window's start state, one launch "
+                                                f"per world-step",
                                       "batched_over_plain": value / plain_rate}
-        wi = int(np.argmax(dyn >= 200)) if (dyn >= 200).any() else 0
-        out["error"] = f32_step_error(W, B, F, M, wi)
+        out["error"] = error_block(batch, F, dyn, f"at the timed window's start (step {first})")
+        drift_steps = args.drift_steps if args.drift_steps >= 0 else (2000 if args.workload == "pyramid" else 1000)
+        if drift_steps > 0 and args.workload != "large":
+            out["error"]["drift"] = drift_block(args.workload, drift_steps)
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:
