@@ -256,7 +256,10 @@ int gb_batch_get_contacts(gb_batch *batch, int32_t world, gb_contact *out, int32
 int gb_batch_get_solver_order(gb_batch *batch, int32_t world, int32_t *order, int32_t capacity,
                               int32_t *n_out, void *cuda_stream);
 /* Step record of one world's bodies (world-local order) from the last step
- * run with record_order bit 0 set: per body, bits 0-7 the position
+ * run with record_order bit 0 set: out[0..n) the decisions of each body,
+ * out[n..2n) its island in the solve (the smallest world-local index of the
+ * island's non-static bodies, -1: not in a simulated island); *n_out = n,
+ * capacity >= 2n.  Decisions per body: bits 0-7 the position
  * iterations its island ran before the early exit (island.py:141-153; 0:
  * not in a simulated island), bits 8-15 the TOI position-pass iterations
  * over the TOI events it took part in (contact.py:866-933, island.py:181-243),

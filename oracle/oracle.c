@@ -118,6 +118,7 @@ struct or_world {
      * island (bits 0-7), TOI position-pass iterations (8-15) and TOI events
      * (16-23), each capped at 255; set-up decision parities (24-27) */
     int *rec;
+    int *rec_island;  /* island of each body in the last solve: its smallest non-static body id (-1: none) */
 };
 
 static void rec_add(int *x, int shift, int v) {
@@ -729,8 +730,14 @@ static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts,
         for (int i = 0; i < nci; ++i) minsep = solve_position(&ks[i], pc, pa, minsep, -1, -1);
         if (minsep >= -3.0 * OR_LINEAR_SLOP) { position_solved = 1; its = it + 1; break; }
     }
+    int root = -1;
     for (int i = 0; i < nbi; ++i)
-        if (w->b[bodies[i]].type != GB_BODY_STATIC) w->rec[bodies[i]] = (w->rec[bodies[i]] & ~0xff) | (its > 255 ? 255 : its);
+        if (w->b[bodies[i]].type != GB_BODY_STATIC && (root < 0 || bodies[i] < root)) root = bodies[i];
+    for (int i = 0; i < nbi; ++i)
+        if (w->b[bodies[i]].type != GB_BODY_STATIC) {
+            w->rec[bodies[i]] = (w->rec[bodies[i]] & ~0xff) | (its > 255 ? 255 : its);
+            w->rec_island[bodies[i]] = root;
+        }
     for (int i = 0; i < nbi; ++i) {
         gb_body *b = &w->b[bodies[i]];
         b->cx = pc[i].x; b->cy = pc[i].y; b->a = pa[i];
@@ -1026,6 +1033,7 @@ static void world_solve_toi(or_world *w, double dt, int vel_iters) {
 /* world.py:307-354 World.step */
 void or_step(or_world *w, double dt, int vel_iters, int pos_iters) {
     memset(w->rec, 0, sizeof(int) * (size_t)(w->nb ? w->nb : 1));
+    for (int i = 0; i < w->nb; ++i) w->rec_island[i] = -1;
     if (w->wflags & GB_W_NEW_FIXTURE) {
         find_new_contacts(w);
         w->wflags &= ~GB_W_NEW_FIXTURE;
@@ -1055,6 +1063,7 @@ or_world *or_create(const gb_world_desc *wd, const gb_body *bodies, const gb_fix
     w->island_flag_b = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
     w->island_index = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
     w->rec = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
+    w->rec_island = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
     w->wflags = wd->flags;
     w->gravity = V(wd->gx, wd->gy);
     w->inv_dt0 = wd->inv_dt0;
@@ -1091,7 +1100,7 @@ void or_destroy(or_world *w) {
     free(w->bcon);
     free(w->order.d); free(w->move.d); free(w->last_order.d);
     free(w->island_flag_b); free(w->island_index); free(w->hook_rank);
-    free(w->hook_pending); free(w->pos_of); free(w->rec);
+    free(w->hook_pending); free(w->pos_of); free(w->rec); free(w->rec_island);
     free(w->c); free(w->b); free(w->f);
     free(w);
 }
@@ -1141,7 +1150,10 @@ int or_get_solver_order(const or_world *w, int *out, int cap) {
 }
 
 long long or_toi_calls(const or_world *w) { return w->n_toi_calls; }
-void or_get_step_record(const or_world *w, int *out) { memcpy(out, w->rec, sizeof(int) * (size_t)w->nb); }
+void or_get_step_record(const or_world *w, int *out) {
+    memcpy(out, w->rec, sizeof(int) * (size_t)w->nb);
+    memcpy(out + w->nb, w->rec_island, sizeof(int) * (size_t)w->nb);
+}
 long long or_toi_events(const or_world *w) { return w->n_toi_events; }
 
 /* ------------------------------------------------------------------ */

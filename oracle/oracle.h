@@ -36,7 +36,9 @@ int or_get_contacts(const or_world *w, gb_contact *out, int cap);
 void or_set_solver_order(or_world *w, const int *order, int n);
 /* Constraint order used by the last step (contact-list positions). */
 int or_get_solver_order(const or_world *w, int *out, int cap);
-/* per body the step record of the last step: position iterations of its
+/* out[0..nb): per body the step record of the last step; out[nb..2nb): its
+ * island in the solve (smallest non-static body id, -1: none).  Record:
+ * position iterations of its
  * island (bits 0-7), TOI position-pass iterations (8-15), TOI events (16-23),
  * parity of its constraints' restitution-bias points and block-solver drops
  * in the island solve (bits 24, 25) and in TOI sub-steps (26, 27) */

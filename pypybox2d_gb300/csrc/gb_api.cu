@@ -85,6 +85,7 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
     B.order_out = a.take<int>(ncap);
     B.rec = a.take<int>(nb);
+    B.rec_island = a.take<int>(nb);
     B.prof = a.take<long long>((size_t)nw * GB_NPROF);
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
@@ -545,10 +546,12 @@ int gb_batch_get_step_record(gb_batch *b, int32_t world, int32_t *out, int32_t c
     if (world < 0 || world >= b->nw) return fail(GB_E_ARG, "world index out of range");
     const WorldHdr &h = b->hdr[world];
     *n_out = h.nb;
-    if (h.nb > capacity) return fail(GB_E_ARG, "capacity too small for the world's bodies");
+    if (2 * h.nb > capacity) return fail(GB_E_ARG, "capacity too small: 2 ints per body of the world");
     cudaStream_t st = (cudaStream_t)stream;
     const int *src = (b->prec == GB_PREC_F64 ? b->bd.rec : b->bf.rec) + h.bbase;
+    const int *isl = (b->prec == GB_PREC_F64 ? b->bd.rec_island : b->bf.rec_island) + h.bbase;
     if (h.nb > 0) CK(cudaMemcpyAsync(out, src, sizeof(int) * h.nb, cudaMemcpyDeviceToHost, st));
+    if (h.nb > 0) CK(cudaMemcpyAsync(out + h.nb, isl, sizeof(int) * h.nb, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     return 0;
 }

@@ -43,7 +43,7 @@ template <class R> __global__ void k_pre(Batch<R> B, int n_bodies, StepParams sp
     const WorldHdr *H = &B.hdr[B.b_world[b]];
     uint32_t f = B.b_flags[b];
     B.s_wake[b] = ((f & GB_BODY_AWAKE) && B.b_type[b] != GB_BODY_STATIC) ? -1 : GB_INF_IDX;
-    if (sp.record_order) B.rec[b] = 0;
+    if (sp.record_order) { B.rec[b] = 0; B.rec_island[b] = -1; }
     // world.py:599-602 (alpha0 is read by nothing before the TOI loop)
     if ((H->flags & GB_W_CONTINUOUS) && (H->flags & GB_W_STEP_COMPLETE) && sp.dt > 0.0) B.b_alpha0[b] = 0.0;
 }

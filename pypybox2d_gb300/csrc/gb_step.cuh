@@ -1679,6 +1679,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             const uint32_t rf = rootf[parent[b]];
             const int its = (rf & R_DONE) ? (int)((rf >> 8) & 0xffu) : sp.pos_iters;
             w.B.rec[w.bb + b] = (w.B.rec[w.bb + b] & ~0xff) | (its > 255 ? 255 : its);
+            w.B.rec_island[w.bb + b] = parent[b];
         }
     if (cached) {
         if constexpr (F32D) {

@@ -600,7 +600,7 @@ template <class R, class G> __device__ void world_step(const G &g, const WView<R
     pc.acc = (sp.profile && g.rank() == 0) ? w.B.prof + (size_t)w.wi * GB_NPROF : nullptr;
     pc.start();
     if (sp.record_order)
-        for (int b = g.rank(); b < w.H->nb; b += g.size()) w.B.rec[w.bb + b] = 0;
+        for (int b = g.rank(); b < w.H->nb; b += g.size()) { w.B.rec[w.bb + b] = 0; w.B.rec_island[w.bb + b] = -1; }
     if (w.H->flags & GB_W_NEW_FIXTURE) {
         int nf = w.H->nf;
         int n0 = w.H->nmove0;

@@ -132,6 +132,7 @@ template <class R> struct Batch {
     int *toi_list;               // contact slots needing a first-pass TOI (batch-wide)
     int *toi_n;                  // their count
     int *rec;                    // per body: the step record of the last record_order step
+    int *rec_island;             // per body: its island in that step's solve (world-local union-find root, -1: none)
     gb_event *ev;                // contact events: 3 ccap + 64 per world, from 3 cbase + 64 world
     int *ev_n;                   // events recorded per world
     // worlds advanced by a cooperative grid (the first n_huge of the size-sorted list)

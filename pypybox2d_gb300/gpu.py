@@ -201,13 +201,15 @@ class GpuBatch:
         last step run with ``record_order`` (gb_batch_get_step_record):
         bits 0-7 position iterations of its island, 8-15 TOI position-pass
         iterations, 16-23 TOI events, 24-27 parities of its constraints'
-        restitution-bias and block-solver decisions (island solve, TOI)."""
-        cap = int(self.worlds["body_count"][world])
-        out = np.zeros(max(cap, 1), dtype=np.int32)
+        restitution-bias and block-solver decisions (island solve, TOI).
+        Returns [2, n]: row 0 the decisions, row 1 each body's island in the
+        solve (smallest non-static body index of the island, -1: none)."""
+        nb = int(self.worlds["body_count"][world])
+        out = np.zeros(max(2 * nb, 1), dtype=np.int32)
         n = ctypes.c_int32()
-        abi.check(self.lib.gb_batch_get_step_record(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap,
-                                                    ctypes.byref(n), None))
-        return out[:n.value].copy()
+        abi.check(self.lib.gb_batch_get_step_record(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                    2 * nb, ctypes.byref(n), None))
+        return out[:2 * n.value].reshape(2, n.value).copy()
 
     def snapshot_bytes(self) -> int:
         n = ctypes.c_uint64()

@@ -140,50 +140,20 @@ REC_FIELDS = {   # step-record fields (gb_batch_get_step_record): (shift, mask)
 
 
 def record_mismatch(W, ra, rb):
-    """Bodies whose step records differ.  ``ra``/``rb`` are per-world arrays;
-    returns a boolean mask over the batch's bodies and the counts per field."""
+    """Bodies whose step records differ.  ``ra``/``rb`` are per-world
+    step records ([2, n]: decisions, islands); returns a boolean mask over the
+    batch's bodies and the counts per field."""
     n = int(W["body_start"][-1] + W["body_count"][-1]) if len(W) else 0
     mask = np.zeros(n, dtype=bool)
     counts = {k: 0 for k in REC_FIELDS}
     for w, (x, y) in enumerate(zip(ra, rb)):
         b0 = int(W["body_start"][w])
+        x, y = x[0], y[0]
         for name, (sh, m) in REC_FIELDS.items():
             d = ((x >> sh) & m) != ((y >> sh) & m)
             counts[name] += int(np.count_nonzero(d))
             mask[b0:b0 + len(x)] |= d
     return mask, counts
-
-
-def islands(W, B, F, Cs):
-    """Island label of every body of the batch (union-find over touching,
-    enabled, non-sensor contacts between non-static bodies, as
-    world.py:475-573 links them; static bodies get -1)."""
-    n = len(B)
-    parent = np.arange(n)
-
-    def find(x):
-        while parent[x] != x:
-            parent[x] = parent[parent[x]]
-            x = parent[x]
-        return x
-
-    static = B["type"] == abi.BODY_STATIC
-    sensor = (F["flags"] & abi.FIX_SENSOR) != 0
-    for w, c in enumerate(Cs):
-        b0, f0 = int(W["body_start"][w]), int(W["fixture_start"][w])
-        live = ((c["flags"] & abi.C_TOUCHING) != 0) & ((c["flags"] & abi.C_ENABLED) != 0)
-        for fa, fb in zip(c["fixture_a"][live], c["fixture_b"][live]):
-            if sensor[f0 + fa] or sensor[f0 + fb]:
-                continue
-            a, b = b0 + int(F["body"][f0 + fa]), b0 + int(F["body"][f0 + fb])
-            if static[a] or static[b]:
-                continue
-            ra, rb = find(a), find(b)
-            if ra != rb:
-                parent[max(ra, rb)] = min(ra, rb)
-    lab = np.array([find(i) for i in range(n)])
-    lab[static] = -1
-    return lab
 
 
 def contact_apart(W, F, C32, C64, n_bodies):
@@ -247,7 +217,8 @@ def one_step(W, B, F, C, dt, vel_iters, pos_iters, reference=None, launch=(3, 64
     ``mismatch`` (discrete counts, step-record fields included),
     ``bodies_decided_apart`` (bodies of islands in which some decision
     differs: a step-record field or a contact's touching flag, manifold type,
-    point count or feature ids)."""
+    point count or feature ids), ``decisions_apart`` (how many such decisions:
+    step-record fields per body plus bodies of differing contacts)."""
     from .gpu import GpuBatch
     g32 = GpuBatch(W, B, F, contacts=C, precision="f32")
     g32.step(dt, vel_iters, pos_iters, 1, launch_mode=launch[0], block_threads=launch[1], record_order=True)
@@ -267,11 +238,19 @@ def one_step(W, B, F, C, dt, vel_iters, pos_iters, reference=None, launch=(3, 64
     g32.close()
     errs = world_errors(W, B32, B64)
     apart, rec_counts = record_mismatch(W, R32, R64)
-    apart |= contact_apart(W, F, C32, C64, len(B))
-    # a decision taken apart moves its whole island (Gauss-Seidel couples it)
-    lab = islands(W, B64, F, C64)
-    hit = np.unique(lab[apart & (lab >= 0)])
-    apart |= np.isin(lab, hit) & (lab >= 0)
+    capart = contact_apart(W, F, C32, C64, len(B))
+    decisions_apart = sum(rec_counts.values()) + int(np.count_nonzero(capart))
+    apart |= capart
+    # a decision taken apart moves its whole island (Gauss-Seidel couples it):
+    # the islands of the solve, as both steps recorded them
+    for R in (R32, R64):
+        lab = np.full(len(B), -1, dtype=np.int64)
+        for w, r in enumerate(R):
+            b0 = int(W["body_start"][w])
+            isl = r[1].astype(np.int64)
+            lab[b0:b0 + len(isl)] = np.where(isl >= 0, b0 + isl, -1)
+        hit = np.unique(lab[apart & (lab >= 0)])
+        apart |= np.isin(lab, hit) & (lab >= 0)
     Ba, Bb = B32.copy(), B64.copy()
     Ba[apart] = Bb[apart]
     errs_alike = world_errors(W, Ba, Bb)
@@ -282,6 +261,7 @@ def one_step(W, B, F, C, dt, vel_iters, pos_iters, reference=None, launch=(3, 64
     mm = mismatch(d32, d64, moved32, moved64)
     mm.update(rec_counts)
     return {"errors": errs, "errors_alike": errs_alike, "mismatch": mm, "bodies_decided_apart": int(apart.sum()),
+            "decisions_apart": decisions_apart,
             "f32": (B32, P32, C32, R32), "f64": (B64, P64, C64, R64)}
 
 

@@ -132,9 +132,9 @@ class OracleWorld:
 
     def step_record(self):
         """Per body the step record of the last step (or_get_step_record)."""
-        out = np.zeros(max(self.nb, 1), dtype=np.int32)
+        out = np.zeros(max(2 * self.nb, 1), dtype=np.int32)
         self.lib.or_get_step_record(self.h, out.ctypes.data)
-        return out[:self.nb].copy()
+        return out[:2 * self.nb].reshape(2, self.nb).copy()
 
 
 class OracleBatch:

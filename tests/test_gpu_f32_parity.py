@@ -16,9 +16,11 @@ the restitution-bias and block-solver choices of its constraints
 (contact.py:470-496).  Some of these sit on a threshold by construction: a
 TOI event of a body moving in a straight line puts the separation after one
 TOI position pass exactly on that pass's -1.5 slop early exit, so rounding
-decides whether one more pass runs (3/32 of the slop, 4.7e-4 m).  Islands
-with such a decision taken apart are counted ("decided apart"), held to
-MAX_DECIDED_APART_RATE of the bodies compared.
+decides whether one more pass runs (3/32 of the slop, 4.7e-4 m).  The
+decisions taken apart (step-record fields per body, plus the bodies of
+contacts whose narrow-phase results differ) are counted and held to
+MAX_DECISIONS_APART_RATE of the bodies compared; the islands they sit in (as
+the solve's step record names them) are left out of the continuous bound.
 Discrete state (pair set, contact order, touching flags, manifold types,
 point counts, feature ids, awake flags, re-fattened proxies): the counts of
 differences are printed and held to MAX_DISCRETE_RATE of the contacts (and
@@ -37,7 +39,7 @@ pytestmark = pytest.mark.gpu
 DT, VI, PI = 1.0 / 60.0, 8, 3
 TOL_M = 1e-5
 MAX_DISCRETE_RATE = 1e-3
-MAX_DECIDED_APART_RATE = 2e-2
+MAX_DECISIONS_APART_RATE = 5e-3
 
 
 def _oracle_step(W, B, F, C, orders):
@@ -66,7 +68,7 @@ def _check(label, W, B, F, C):
     contact_diffs = mm["pairs"] + mm["touching"] + mm["manifold_type"] + mm["point_count"] + mm["feature_ids"]
     assert contact_diffs <= MAX_DISCRETE_RATE * max(mm["contacts"], 1), f"{label}: {mm}"
     assert mm["awake"] <= MAX_DISCRETE_RATE * max(mm["bodies"], 1), f"{label}: {mm}"
-    assert r["bodies_decided_apart"] <= MAX_DECIDED_APART_RATE * max(mm["bodies"], 1), f"{label}: {mm}"
+    assert r["decisions_apart"] <= MAX_DECISIONS_APART_RATE * max(mm["bodies"], 1), f"{label}: {mm}"
     return r
 
 
