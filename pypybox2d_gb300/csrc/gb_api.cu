@@ -65,6 +65,7 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.f_cat = a.take<uint32_t>(nf); B.f_mask = a.take<uint32_t>(nf); B.f_group = a.take<int>(nf);
     B.f_v = a.take<vec2<R>>((size_t)nf * GB_MAX_POLY_VERTS); B.f_n = a.take<vec2<R>>((size_t)nf * GB_MAX_POLY_VERTS);
     B.f_aabb = a.take<dbox>(nf);
+    B.f_aabbf = a.take<float4>(nf);
     B.c = a.take<ContactRec<R>>(ncap);
     B.s_parent = a.take<int>(nb); B.s_wake = a.take<int>(nb); B.s_seed = a.take<int>(nb); B.s_stack = a.take<int>(nb);
     B.s_adjoff = a.take<int>(nb + nw);

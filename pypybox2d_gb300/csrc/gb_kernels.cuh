@@ -69,6 +69,7 @@ __global__ void k_unpack_fixtures(Batch<GB_REAL> B, const gb_fixture *src, int n
         B.f_n[(size_t)i * GB_MAX_POLY_VERTS + k] = mk<GB_REAL>((GB_REAL)f.nx[k], (GB_REAL)f.ny[k]);
     }
     B.f_aabb[i] = mkbox(f.aabb[0], f.aabb[1], f.aabb[2], f.aabb[3]);
+    B.f_aabbf[i] = boxf_of(B.f_aabb[i]);
 }
 
 // contacts: host records (one world per launch range) <-> device ContactRec

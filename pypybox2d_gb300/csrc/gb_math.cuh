@@ -42,6 +42,8 @@ template <class R> struct rot2 { R c, s; };
 // axis-aligned box: lower (lx, ly), upper (ux, uy)
 struct __align__(16) dbox { double x, y, z, w; };
 static GB_HD dbox mkbox(double lx, double ly, double ux, double uy) { dbox b; b.x = lx; b.y = ly; b.z = ux; b.w = uy; return b; }
+// float32 copy of a fat box (each coordinate rounded to nearest)
+static GB_HD float4 boxf_of(const dbox &b) { return make_float4((float)b.x, (float)b.y, (float)b.z, (float)b.w); }
 template <class R> struct xform2 { vec2<R> p; rot2<R> q; };
 
 // Mat22_mul
@@ -161,7 +163,11 @@ static GB_HD rot2<double> pose_rot(double a) {
 }
 
 template <class R> struct Rot;
-template <> struct Rot<double> { GB_HD static rot2<double> of(double a) { return rot_of(a); } };
+// float64 rotations of the solver's positions: the portable sincos in the
+// float64 unit (bit-exact with the CPU restatement); in the float32 unit the
+// float32-accurate rotation of the poses (the TOI position pass, whose
+// float64 arithmetic would otherwise spend most of its time in the sincos)
+template <> struct Rot<double> { GB_HD static rot2<double> of(double a) { return pose_rot(a); } };
 template <> struct Rot<float> { GB_HD static rot2<float> of(double a) { return rot_of_f32(a); } };
 
 // Order-preserving map of a double to uint64 (for atomicMin over doubles).

@@ -55,7 +55,7 @@ struct WShared {
     unsigned long long gred[6];
     float gsum;
     int gx, gy, nsmall, nbig;
-    double x0, y0, inv_h, maxw, maxh, cut;
+    float x0, y0, inv_h, cut;
 };
 
 // body.py:781-793 awake setter
@@ -88,9 +88,19 @@ template <class R> __device__ void body_advance(const WView<R> &w, int b, double
     w.B.b_xp[w.bb + b] = s.c - rmul(q, s.lc);
 }
 
-// aabbmodule.c AABB_test_overlap
+// Order-preserving integer key of a finite double (-0 keyed as +0): for
+// finite x, y, (x - y) > 0 holds exactly when x > y, so comparing keys gives
+// the reference's float64 tests without float64 arithmetic (a float64
+// instruction costs a GB300 warp ~64 cycles).
+static __device__ __forceinline__ long long okey(double d) {
+    long long b = __double_as_longlong(d);
+    if ((b << 1) == 0) b = 0;
+    return b < 0 ? (b ^ 0x7fffffffffffffffLL) : b;
+}
+// aabbmodule.c AABB_test_overlap: !((b.lx - a.ux) > 0 || (b.ly - a.uy) > 0 ||
+// (a.lx - b.ux) > 0 || (a.ly - b.uy) > 0)
 static __device__ __forceinline__ bool aabb_overlap(dbox a, dbox b) {
-    return !((b.x - a.z) > 0.0 || (b.y - a.w) > 0.0 || (a.x - b.z) > 0.0 || (a.y - b.w) > 0.0);
+    return !(okey(b.x) > okey(a.z) || okey(b.y) > okey(a.w) || okey(a.x) > okey(b.z) || okey(a.y) > okey(b.w));
 }
 
 // world.py:958-970
@@ -247,12 +257,14 @@ template <class R> __device__ bool sync_fixture(const WView<R> &w, int f) {
 #endif
     dbox ab = mkbox(cmin(a1.x, a2.x), cmin(a1.y, a2.y), cmax(a1.z, a2.z), cmax(a1.w, a2.w));
     dbox fat = w.B.f_aabb[w.fb + f];
-    if (fat.x <= ab.x && fat.y <= ab.y && ab.z <= fat.z && ab.w <= fat.w) return false;
+    if (okey(fat.x) <= okey(ab.x) && okey(fat.y) <= okey(ab.y) && okey(ab.z) <= okey(fat.z) && okey(ab.w) <= okey(fat.w))
+        return false;
     dbox nb = mkbox(ab.x - GB_AABB_EXTENSION, ab.y - GB_AABB_EXTENSION, ab.z + GB_AABB_EXTENSION, ab.w + GB_AABB_EXTENSION);
     vec2<double> d = GB_AABB_MULTIPLIER * disp;
     if (d.x < 0.0) { nb.x = nb.x + d.x; nb.y = nb.y + 0.0; } else { nb.z = nb.z + d.x; nb.w = nb.w + 0.0; }
     if (d.y < 0.0) { nb.x = nb.x + 0.0; nb.y = nb.y + d.y; } else { nb.z = nb.z + 0.0; nb.w = nb.w + d.y; }
     w.B.f_aabb[w.fb + f] = nb;
+    w.B.f_aabbf[w.fb + f] = boxf_of(nb);
     return true;
 }
 
@@ -298,13 +310,26 @@ template <class R> __device__ __forceinline__ bool pair_candidate(const WView<R>
 // proxy's index, so the result does not depend on the grid.
 #define GB_GRID_MIN_MOVES 8
 #define GB_GRID_ITEMS_PER_FIXTURE 9
-static __device__ __forceinline__ int grid_cell(double x, double x0, double inv_h, int n) {
-    double t = floor((x - x0) * inv_h);
-    t = fmin(fmax(t, 0.0), (double)(n - 1));
+// The grid works on the float32 copies of the fat boxes: any map from a
+// coordinate to a cell that does not decrease with the coordinate lists and
+// finds every overlapping pair (the pair's lower-left intersection corner
+// lies in both boxes' cell ranges), and the pairs themselves are decided by
+// the exact test on the float64 boxes.
+static __device__ __forceinline__ int grid_cell(float x, float x0, float inv_h, int n) {
+    float t = floorf((x - x0) * inv_h);
+    t = fminf(fmaxf(t, 0.0f), (float)(n - 1));
     return (int)t;
 }
-static __device__ __forceinline__ bool grid_big(const dbox &b, double cut) {
+static __device__ __forceinline__ bool grid_big(const float4 &b, float cut) {
     return (b.z - b.x) > cut || (b.w - b.y) > cut;
+}
+// order-preserving unsigned key of a float (for shared-memory min/max)
+static __device__ __forceinline__ unsigned fkey(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u >> 31) ? ~u : (u | 0x80000000u);
+}
+static __device__ __forceinline__ float fkey_inv(unsigned k) {
+    return __uint_as_float((k >> 31) ? (k & 0x7fffffffu) : ~k);
 }
 
 // Scratch of one world (s_grid): cell ends (2 nf + 2), listed proxies
@@ -312,7 +337,7 @@ static __device__ __forceinline__ bool grid_big(const dbox &b, double cut) {
 template <class R, class G> __device__ void build_pair_grid(const G &g, const WView<R> &w, WShared *sh, int *goff, int *gitem,
                                                             int *gbig) {
     const int nf = w.H->nf;
-    const dbox *aabb = w.B.f_aabb + w.fb;
+    const float4 *aabb = w.B.f_aabbf + w.fb;
     if (g.rank() == 0) {
         sh->gsum = 0.0f;
         sh->gred[0] = sh->gred[1] = ~0ull;
@@ -323,58 +348,58 @@ template <class R, class G> __device__ void build_pair_grid(const G &g, const WV
     // each thread reduces its proxies, then one atomic per warp
     float lsum = 0.0f;
     for (int f = g.rank(); f < nf; f += g.size()) {
-        dbox b = aabb[f];
-        lsum += (float)fmax(b.z - b.x, b.w - b.y);
+        const float4 b = aabb[f];
+        lsum += fmaxf(b.z - b.x, b.w - b.y);
     }
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(&sh->gsum, lsum);
     g.sync();
-    if (g.rank() == 0) sh->cut = 4.0 * (double)sh->gsum / (double)nf;
+    if (g.rank() == 0) sh->cut = 4.0f * sh->gsum / (float)nf;
     g.sync();
-    const double cut = sh->cut;
-    unsigned long long r[4] = {~0ull, ~0ull, 0ull, 0ull};
+    const float cut = sh->cut;
+    unsigned r[4] = {~0u, ~0u, 0u, 0u};
     for (int f = g.rank(); f < nf; f += g.size()) {
-        dbox b = aabb[f];
+        const float4 b = aabb[f];
         if (grid_big(b, cut)) continue;
-        unsigned long long k[4] = {dkey(b.x), dkey(b.y), dkey(b.z), dkey(b.w)};
+        const unsigned k[4] = {fkey(b.x), fkey(b.y), fkey(b.z), fkey(b.w)};
         for (int j = 0; j < 2; ++j) r[j] = k[j] < r[j] ? k[j] : r[j];
         for (int j = 2; j < 4; ++j) r[j] = k[j] > r[j] ? k[j] : r[j];
     }
     for (int o = 16; o > 0; o >>= 1)
         for (int j = 0; j < 4; ++j) {
-            unsigned long long x = __shfl_xor_sync(0xffffffffu, r[j], o);
+            unsigned x = __shfl_xor_sync(0xffffffffu, r[j], o);
             r[j] = j < 2 ? (x < r[j] ? x : r[j]) : (x > r[j] ? x : r[j]);
         }
-    if ((threadIdx.x & 31) == 0 && r[0] != ~0ull) {
-        atomicMin(&sh->gred[0], r[0]); atomicMin(&sh->gred[1], r[1]);
-        atomicMax(&sh->gred[2], r[2]); atomicMax(&sh->gred[3], r[3]);
+    if ((threadIdx.x & 31) == 0 && r[0] != ~0u) {
+        atomicMin(&sh->gred[0], (unsigned long long)r[0]); atomicMin(&sh->gred[1], (unsigned long long)r[1]);
+        atomicMax(&sh->gred[2], (unsigned long long)r[2]); atomicMax(&sh->gred[3], (unsigned long long)r[3]);
     }
     g.sync();
     if (g.rank() == 0) {
         int gx = 1, gy = 1;
-        double x0 = 0.0, y0 = 0.0, h = 1.0;
+        float x0 = 0.0f, y0 = 0.0f, h = 1.0f;
         if (sh->gred[0] != ~0ull) {
-            x0 = dkey_inv(sh->gred[0]); y0 = dkey_inv(sh->gred[1]);
-            double sx = dkey_inv(sh->gred[2]) - x0, sy = dkey_inv(sh->gred[3]) - y0;
-            h = fmax(0.5 * cut, 1e-6);   // twice the mean extent
-            const double cap = 2.0 * nf;
+            x0 = fkey_inv((unsigned)sh->gred[0]); y0 = fkey_inv((unsigned)sh->gred[1]);
+            const float sx = fkey_inv((unsigned)sh->gred[2]) - x0, sy = fkey_inv((unsigned)sh->gred[3]) - y0;
+            h = fmaxf(0.5f * cut, 1e-6f);   // twice the mean extent
+            const float cap = 2.0f * (float)nf;
             for (int k = 0; k < 64; ++k) {   // at most 2 nf cells
-                double cx = floor(sx / h) + 1.0, cy = floor(sy / h) + 1.0;
+                const float cx = floorf(sx / h) + 1.0f, cy = floorf(sy / h) + 1.0f;
                 if (cx * cy <= cap) { gx = (int)cx; gy = (int)cy; break; }
-                h *= 1.5;
+                h *= 1.5f;
             }
         }
-        sh->x0 = x0; sh->y0 = y0; sh->inv_h = 1.0 / h;
+        sh->x0 = x0; sh->y0 = y0; sh->inv_h = 1.0f / h;
         sh->gx = gx; sh->gy = gy;
     }
     g.sync();
     const int ncell = sh->gx * sh->gy;
-    const double x0 = sh->x0, y0 = sh->y0, ih = sh->inv_h;
+    const float x0 = sh->x0, y0 = sh->y0, ih = sh->inv_h;
     const int gx = sh->gx, gy = sh->gy;
     for (int c = g.rank(); c < ncell; c += g.size()) goff[c] = 0;
     g.sync();
     for (int f = g.rank(); f < nf; f += g.size()) {
-        dbox b = aabb[f];
+        const float4 b = aabb[f];
         if (grid_big(b, cut)) continue;
         const int cx0 = grid_cell(b.x, x0, ih, gx), cx1 = grid_cell(b.z, x0, ih, gx);
         const int cy0 = grid_cell(b.y, y0, ih, gy), cy1 = grid_cell(b.w, y0, ih, gy);
@@ -391,7 +416,7 @@ template <class R, class G> __device__ void build_pair_grid(const G &g, const WV
     }
     // scatter: afterwards goff[c] is the end of cell c (its start is goff[c - 1])
     for (int f = g.rank(); f < nf; f += g.size()) {
-        dbox b = aabb[f];
+        const float4 b = aabb[f];
         if (grid_big(b, cut)) {
             gbig[atomicAdd(&sh->nbig, 1)] = f;
             continue;
@@ -452,7 +477,7 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
         build_pair_grid(g, w, sh, goff, gitem, gbig);
         use_grid = sh->gx > 0;
     }
-    const dbox *aabb = w.B.f_aabb + w.fb;
+    const float4 *aabb = w.B.f_aabbf + w.fb;
     // with a grid every moved proxy, big ones too, scans the cells its box
     // overlaps (the ground box: the bottom row) and the big list
     auto each_candidate = [&](int i, int p, auto &&emit) {
@@ -461,8 +486,8 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
                 if (pair_candidate(w, i, p, q, first, hash, hmask)) emit(q);
             return;
         }
-        const dbox b = aabb[p];
-        const double x0 = sh->x0, y0 = sh->y0, ih = sh->inv_h;
+        const float4 b = aabb[p];
+        const float x0 = sh->x0, y0 = sh->y0, ih = sh->inv_h;
         const int gx = sh->gx, gy = sh->gy;
         const int cx0 = grid_cell(b.x, x0, ih, gx), cx1 = grid_cell(b.z, x0, ih, gx);
         const int cy0 = grid_cell(b.y, y0, ih, gy), cy1 = grid_cell(b.w, y0, ih, gy);
@@ -471,9 +496,9 @@ template <class R, class G> __device__ void find_new_contacts(const G &g, const 
                 int c = cy * gx + cx;
                 for (int k = c ? goff[c - 1] : 0; k < goff[c]; ++k) {
                     int q = gitem[k];
-                    const dbox o = aabb[q];
+                    const float4 o = aabb[q];
                     // the cell of the intersection's lower-left corner owns the pair
-                    if (grid_cell(fmax(b.x, o.x), x0, ih, gx) != cx || grid_cell(fmax(b.y, o.y), y0, ih, gy) != cy) continue;
+                    if (grid_cell(fmaxf(b.x, o.x), x0, ih, gx) != cx || grid_cell(fmaxf(b.y, o.y), y0, ih, gy) != cy) continue;
                     if (pair_candidate(w, i, p, q, first, hash, hmask)) emit(q);
                 }
             }

@@ -107,6 +107,7 @@ template <class R> struct Batch {
     uint32_t *f_cat, *f_mask; int *f_group;
     vec2<R> *f_v, *f_n;       // 8 slots per fixture
     dbox *f_aabb;          // fat AABB
+    float4 *f_aabbf;       // its float32 copy (rounded to nearest), read by the pair-finding grid
     // contacts
     ContactRec<R> *c;
     // scratch (body-indexed)
