@@ -273,6 +273,15 @@ int gb_batch_get_solver_order(gb_batch *batch, int32_t world, int32_t *order, in
  * parity tests). */
 int gb_batch_get_step_record(gb_batch *batch, int32_t world, int32_t *out, int32_t capacity, int32_t *n_out,
                              void *cuda_stream);
+/* Poll limit of the solver's waits for its in-kernel bulk copies (default
+ * 262144).  A wait that reaches it sets GB_ST_WAIT_TIMEOUT in its world's
+ * status word, waits with the default limit for the copies still in flight
+ * and ends that world's solve for the step; the context stays usable.  A
+ * limit of 0 makes every such wait give up at once, so callers can exercise
+ * that path without a fault.  No counterpart in the reference. */
+int gb_batch_set_wait_polls(gb_batch *batch, int32_t polls);
+/* Zero every world's status word (after the caller has handled a failure). */
+int gb_batch_clear_status(gb_batch *batch, void *cuda_stream);
 /* Per-world status words (GB_ST_* bits), n_worlds uint32. */
 int gb_batch_status(gb_batch *batch, uint32_t *status, void *cuda_stream);
 /* Accumulated SM clock cycles per step phase, 16 int64 per world
@@ -327,9 +336,10 @@ int gb_batch_get_launch_config(gb_batch *batch, gb_launch_config *cfg);
  * threads, one warp per world with 2/4 warps per CTA (phased only for
  * batches with cooperative-grid worlds); (2) big_bodies 256/512/1024/2048/
  * none; (3) pipe_bufs 0-4.  Each trial's steps are timed with CUDA events on
- * `cuda_stream`.  trials[] receives every trial in order (ms_per_step < 0:
- * not runnable, e.g. too much shared memory); the best becomes the batch's
- * launch configuration.  opts->record_order must be 0. */
+ * `cuda_stream`.  trials[] receives every trial in order (ms_per_step -1:
+ * not runnable, e.g. too much shared memory; -2: its steps raised a status
+ * bit, e.g. a copy wait that gave up, and it is not a candidate); the best
+ * becomes the batch's launch configuration.  opts->record_order must be 0. */
 int gb_batch_autotune(gb_batch *batch, const gb_step_opts *opts, gb_launch_config *trials, int32_t capacity,
                       int32_t *n_out, gb_launch_config *best, void *cuda_stream);
 

@@ -1150,6 +1150,7 @@ int or_get_solver_order(const or_world *w, int *out, int cap) {
 }
 
 long long or_toi_calls(const or_world *w) { return w->n_toi_calls; }
+void or_clear_status(or_world *w) { w->status = 0; }
 void or_get_step_record(const or_world *w, int *out) {
     memcpy(out, w->rec, sizeof(int) * (size_t)w->nb);
     memcpy(out + w->nb, w->rec_island, sizeof(int) * (size_t)w->nb);

@@ -43,6 +43,7 @@ int or_get_solver_order(const or_world *w, int *out, int cap);
  * parity of its constraints' restitution-bias points and block-solver drops
  * in the island solve (bits 24, 25) and in TOI sub-steps (26, 27) */
 void or_get_step_record(const or_world *w, int *out);
+void or_clear_status(or_world *w);
 long long or_toi_calls(const or_world *w);
 long long or_toi_events(const or_world *w);
 

@@ -175,6 +175,7 @@ EXPORTED = (
     "gb_graph_capture", "gb_graph_launch", "gb_graph_destroy",
     "gb_batch_ray_cast", "gb_batch_ray_cast_all", "gb_batch_query_aabb",
     "gb_batch_snapshot_bytes", "gb_batch_snapshot", "gb_batch_restore", "gb_batch_get_step_record",
+    "gb_batch_set_wait_polls", "gb_batch_clear_status",
 )
 
 #: gb_step_opts.record_order bit that records contact events
@@ -249,6 +250,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_snapshot.argtypes = [vp, vp, ctypes.c_uint64, vp]
     lib.gb_batch_restore.argtypes = [vp, vp, ctypes.c_uint64, vp]
     lib.gb_batch_get_step_record.argtypes = [vp, i32, i32p, i32, i32p, vp]
+    lib.gb_batch_set_wait_polls.argtypes = [vp, i32]
+    lib.gb_batch_clear_status.argtypes = [vp, vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

@@ -296,6 +296,7 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         b->bd.cache_big = b->bf.cache_big = max_big <= 2048 ? max_big : 0;
         b->bd.cache_small = b->bf.cache_small = max_small;
         b->bd.pipe_bufs = b->bf.pipe_bufs = GB_SOLVE_PIPE_BUFS;
+        b->bd.wait_polls = b->bf.wait_polls = GB_WAIT_POLLS;
         // the largest worlds run each phase as one cooperative grid
         int nh = 0;
         for (int i : b->launch_order)
@@ -557,6 +558,24 @@ int gb_batch_get_step_record(gb_batch *b, int32_t world, int32_t *out, int32_t c
     return 0;
 }
 
+int gb_batch_set_wait_polls(gb_batch *b, int32_t polls) {
+    if (!b) return fail(GB_E_ARG, "batch is NULL");
+    if (polls < 0) return fail(GB_E_ARG, "polls must be >= 0");
+    b->bd.wait_polls = b->bf.wait_polls = polls;
+    return 0;
+}
+
+int gb_batch_clear_status(gb_batch *b, void *stream) {
+    if (!b) return fail(GB_E_ARG, "batch is NULL");
+    WorldHdr *d = b->prec == GB_PREC_F64 ? b->bd.hdr : b->bf.hdr;
+    cudaStream_t st = (cudaStream_t)stream;
+    // status is a 32-bit field of every header: clear it in place
+    for (int i = 0; i < b->nw; ++i)
+        CK(cudaMemsetAsync(reinterpret_cast<char *>(d + i) + offsetof(WorldHdr, status), 0, sizeof(uint32_t), st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
 int gb_batch_status(gb_batch *b, uint32_t *status, void *stream) {
     if (!b || !status) return fail(GB_E_ARG, "NULL argument");
     std::vector<WorldHdr> h;
@@ -723,6 +742,9 @@ int gb_batch_autotune(gb_batch *b, const gb_step_opts *o, gb_launch_config *tria
     std::vector<gb_launch_config> log;
     gb_launch_config best_c = start;
     best_c.ms_per_step = -1.0;
+    // the status words the trials start from (they are part of the saved state)
+    std::vector<WorldHdr> h0, h1;
+    if (!err) err = read_headers(b, h0, st);
     // one trial: from the saved state, an untimed run (first launches load
     // their kernels), then the timed run from the saved state again
     auto trial = [&](gb_launch_config c) {
@@ -741,6 +763,11 @@ int gb_batch_autotune(gb_batch *b, const gb_step_opts *o, gb_launch_config *tria
             }
             if (rc != 0) err = cuda_fail((cudaError_t)rc, "autotune trial");
             else c.ms_per_step = (double)ms / o->n_steps;
+            // a trial whose steps raised a status bit (a wait that gave up
+            // ends its solve early, an overflow drops work) is not a candidate
+            if (!err && (err = read_headers(b, h1, st)) == 0)
+                for (int i = 0; i < b->nw; ++i)
+                    if (h1[i].status != h0[i].status) { c.ms_per_step = -2.0; break; }
         }
         log.push_back(c);
         if (c.ms_per_step >= 0.0 && (best_c.ms_per_step < 0.0 || c.ms_per_step < best_c.ms_per_step)) best_c = c;

@@ -1358,7 +1358,6 @@ template <class R> __host__ inline size_t solve_smem_bytes(int nb, int threads, 
     return cache_body_bytes<R>(nb) + (size_t)nbuf * chunk_buf_bytes<R>(threads) + 64;
 }
 #define GB_MAX_PIPE_BUFS 4
-#define GB_WAIT_POLLS (1 << 18)
 
 // Chunks of the colour-major records: start | count << 22, one per entry.
 template <class G> __device__ int chunk_table(const G &g, const int *coff, int ncol, int cap, int *tab, int lim, uint32_t *status) {
@@ -1387,7 +1386,23 @@ struct ChunkPipe {
     int nbuf;
     unsigned parity;     // bit b: parity of the next completion of buffer b
     int issued;          // chunks issued so far in this run
+    int consumed;        // chunks whose completion this thread has seen in this run
 };
+
+// After an early exit or a wait that gave up: rank 0 (which issued every
+// copy) waits, with the full limit, for each chunk it issued and has not
+// seen complete, so no copy lands after the block has left its shared
+// memory.  Returns false when one of those waits gives up as well.
+template <class G> __device__ bool pipe_drain(const G &g, ChunkPipe &p) {
+    bool ok = true;
+    if (g.rank() == 0)
+        for (; p.consumed < p.issued; ++p.consumed) {
+            const int b = p.consumed % p.nbuf;
+            if (!mbar_wait(&p.bar[b], (p.parity >> b) & 1u, GB_WAIT_POLLS)) { ok = false; break; }
+            p.parity ^= 1u << b;
+        }
+    return !g.any(!ok);
+}
 
 template <class G, class Rec> __device__ __forceinline__ void pipe_issue(const G &g, ChunkPipe &p, int q, const Rec *base,
                                                                         const int *tab, int nch) {
@@ -1428,7 +1443,8 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     const R *stat_ii = nullptr;   // cached inverse inertias, -0 marking a static body
     vec2<double> *pc = w.B.b_c + w.bb;
     double *pa = w.B.b_a + w.bb;
-    ChunkPipe pipe{nullptr, nullptr, 0, 0, 0u, 0};
+    ChunkPipe pipe{nullptr, nullptr, 0, 0, 0u, 0, 0};
+    const int polls = w.B.wait_polls;   // limit of the chunk waits (GB_WAIT_POLLS unless a test lowers it)
     int *pipe_fail = nullptr;   // shared flag: some thread's bounded wait gave up
     if (cached) {
         // layout: c[nb] (16) | a[nb] (8) | inverse mass, inertia (R); a static
@@ -1484,14 +1500,15 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
                 imp[0] = gr.ni[0]; imp[1] = gr.ni[1]; imp[2] = gr.ti[0]; imp[3] = gr.ti[1];
             }
         };
-        for (int q = 0; q < ahead && q < total; ++q) pipe_issue(g, pipe, q, cv, tab, nch);
+        pipe.issued = pipe.consumed = 0;
+        for (int q = 0; q < ahead && q < total; ++q) { pipe_issue(g, pipe, q, cv, tab, nch); ++pipe.issued; }
         if (total > 0) load_imp(0);
         for (int q = 0; q < total; ++q) {
-            if (q + ahead < total) pipe_issue(g, pipe, q + ahead, cv, tab, nch);
+            if (q + ahead < total) { pipe_issue(g, pipe, q + ahead, cv, tab, nch); ++pipe.issued; }
             const int b = q % pipe.nbuf;
-            const bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
-            pipe.parity ^= 1u << b;
-            if (!ok) *pipe_fail = 1;
+            const bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, polls);
+            if (ok) { pipe.parity ^= 1u << b; ++pipe.consumed; }
+            else *pipe_fail = 1;
             const int e = tab[q % nch];
             const int s0 = e & ((1 << 22) - 1), cnt = e >> 22;
             const bool warm_pass = warm && q < nch;
@@ -1541,10 +1558,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     }
     if (failed) {
         if (rank == 0) w.H->status |= GB_ST_WAIT_TIMEOUT;
-        // let the copies still in flight land before the buffers are released
-        if (rank == 0)
-            for (int b = 0; b < pipe.nbuf; ++b) mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
-        g.sync();
+        pipe_drain(g, pipe);   // the copies still in flight land before the block returns
         return;
     }
     if (cached) {
@@ -1579,9 +1593,16 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             R ratio = (R)GB_MAX_ROTATION / fabs(rotation);
             omg = omg * ratio;
         }
-        w.B.b_c[gb] = w.B.b_c[gb] + cvt<double>(dtr * v);
-        w.B.b_a[gb] = w.B.b_a[gb] + (double)(dtr * omg);
+        const vec2<double> cn = w.B.b_c[gb] + cvt<double>(dtr * v);
+        const double an = w.B.b_a[gb] + (double)(dtr * omg);
+        w.B.b_c[gb] = cn;
+        w.B.b_a[gb] = an;
         w.B.b_v[gb] = v; w.B.b_w[gb] = omg;
+        // a body whose state stopped being finite (the reference would carry
+        // the NaN on, body.py:49-63 only checks arguments): flag the world
+        if (!(finite_bits(cn.x) && finite_bits(cn.y) && finite_bits(an) && finite_bits(v.x) && finite_bits(v.y) &&
+              finite_bits(omg)))
+            atomicOr(&w.H->status, GB_ST_NONFINITE);
     }
     g.sync();
     if (rank == 0) ck.mark(5);
@@ -1648,35 +1669,32 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         const int nch = tab[-1];
         const int total = sp.pos_iters * nch;
         const int ahead = pipe.nbuf - 1;
-        int issued = 0;
-        for (; issued < ahead && issued < total; ++issued) pipe_issue(g, pipe, issued, cpos, tab, nch);
+        pipe.issued = pipe.consumed = 0;
+        for (; pipe.issued < ahead && pipe.issued < total; ++pipe.issued) pipe_issue(g, pipe, pipe.issued, cpos, tab, nch);
         int q = 0;
         for (int it = 0; it < sp.pos_iters && !failed; ++it) {
             for (int b = rank; b < nb; b += g.size()) minsep[b] = dkey(0.0);
             g.sync();
             for (int j = 0; j < nch; ++j, ++q) {
-                if (issued < total && issued <= q + ahead) { pipe_issue(g, pipe, issued, cpos, tab, nch); ++issued; }
+                if (pipe.issued < total && pipe.issued <= q + ahead) {
+                    pipe_issue(g, pipe, pipe.issued, cpos, tab, nch);
+                    ++pipe.issued;
+                }
                 const int b = q % pipe.nbuf;
-                const bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
-                pipe.parity ^= 1u << b;
-                if (!ok) *pipe_fail = 1;
+                const bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, polls);
+                if (ok) { pipe.parity ^= 1u << b; ++pipe.consumed; }
+                else *pipe_fail = 1;
                 const int e = tab[j];
                 const int cnt = e >> 22;
                 if (ok && rank < cnt) pos_one(reinterpret_cast<const ConsPos<R> *>(pipe.buf + (size_t)b * pipe.buf_bytes)[rank]);
                 g.sync();
-                if (*pipe_fail) { failed = true; ++q; break; }
+                if (*pipe_fail) { failed = true; break; }
             }
             if (failed) break;
             if (!pos_check(it)) break;
         }
-        // drain the chunks issued past an early exit
-        for (; q < issued; ++q) {
-            const int b = q % pipe.nbuf;
-            bool ok = mbar_wait(&pipe.bar[b], (pipe.parity >> b) & 1u, GB_WAIT_POLLS);
-            pipe.parity ^= 1u << b;
-            if (!ok) failed = true;
-        }
-        failed = g.any(failed);
+        // the chunks issued past an early exit or a wait that gave up
+        if (!pipe_drain(g, pipe)) failed = true;
         if (failed) {
             if (rank == 0) w.H->status |= GB_ST_WAIT_TIMEOUT;
             g.sync();

@@ -163,10 +163,15 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
         }
         int g = w.bb + ib[i];
         if (w.btype(ib[i]) != GB_BODY_STATIC) {
-            w.B.b_c[g] = pc[i] + cvt<double>(dtr * v);
-            w.B.b_a[g] = pa[i] + (double)(dtr * om);
+            const vec2<double> cn = pc[i] + cvt<double>(dtr * v);
+            const double an = pa[i] + (double)(dtr * om);
+            w.B.b_c[g] = cn;
+            w.B.b_a[g] = an;
             w.B.b_v[g] = v; w.B.b_w[g] = om;
             sync_transform(w, ib[i]);
+            if (!(finite_bits(cn.x) && finite_bits(cn.y) && finite_bits(an) && finite_bits(v.x) && finite_bits(v.y) &&
+                  finite_bits(om)))
+                atomicOr(&w.H->status, GB_ST_NONFINITE);
         }
     }
 }

@@ -91,6 +91,7 @@ template <class R> struct Batch {
     int pipe_bufs;            // solver: constraint chunk buffers in shared memory (0: read global memory)
     int n_big;                // worlds solved by the wide launch (the first n_big of the size-sorted list)
     int cache_big, cache_small;   // body capacity of the solver's shared memory in the two launches
+    int wait_polls;           // poll limit of the solver's waits for its bulk copies (GB_WAIT_POLLS; a test may lower it)
     WorldHdr *hdr;
     int *b_world;             // world of each body
     int *c_world;             // world of each contact slot
@@ -143,6 +144,12 @@ template <class R> struct Batch {
     void *g_sh;                  // their WShared
 };
 #define GB_NPROF 16
+#define GB_WAIT_POLLS (1 << 18)    // default poll limit of the solver's waits for its bulk copies
+// finite float64 / float32 value (integer test of the exponent bits)
+static __device__ __forceinline__ bool finite_bits(double x) {
+    return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
+static __device__ __forceinline__ bool finite_bits(float x) { return (__float_as_uint(x) & 0x7f800000u) != 0x7f800000u; }
 #define GB_SOLVE_BIG_BODIES 512    // worlds this large are solved by the wide launch
 #define GB_SOLVE_BIG_THREADS 128
 #define GB_SOLVE_PIPE_BUFS 2       // constraint chunk buffers of the solver

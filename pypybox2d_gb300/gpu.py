@@ -211,6 +211,13 @@ class GpuBatch:
                                                     2 * nb, ctypes.byref(n), None))
         return out[:2 * n.value].reshape(2, n.value).copy()
 
+    def set_wait_polls(self, polls: int) -> None:
+        """Poll limit of the solver's in-kernel copy waits (gb_batch_set_wait_polls)."""
+        abi.check(self.lib.gb_batch_set_wait_polls(self.h, int(polls)))
+
+    def clear_status(self) -> None:
+        abi.check(self.lib.gb_batch_clear_status(self.h, None))
+
     def snapshot_bytes(self) -> int:
         n = ctypes.c_uint64()
         abi.check(self.lib.gb_batch_snapshot_bytes(self.h, ctypes.byref(n)))

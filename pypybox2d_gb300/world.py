@@ -38,8 +38,7 @@ from .scenes import AABB_EXTENSION, SceneBuilder, _Body
 from .shapes import Circle, Edge, Loop, MassData, Polygon, Shape
 
 
-class LockedError(RuntimeError):
-    """A world was changed during a step (common.py:84-86)."""
+from .errors import EmptyFixtureError, LockedError, PhysicsError, StepError, step_error  # noqa: E402,F401
 
 
 class Vec2(tuple):
@@ -747,6 +746,31 @@ def _fixture_list(shapes, fixtures, shape_fixture):
     return out
 
 
+def _check_body_args(btype, kw):
+    """body.py:49-63 with the C extension's Vec2.valid / is_valid_float
+    (vec2module.c valid_float, common.py:942): only NaN is invalid.  The
+    damping checks there read `not valid and > 0`, which no NaN satisfies, so
+    they never raise; kept as they are."""
+    def nan(x):
+        return x != x
+    px, py = kw.get("position", (0.0, 0.0))
+    vx, vy = kw.get("linear_velocity", (0.0, 0.0))
+    if nan(float(px)) or nan(float(py)):
+        raise ValueError("Invalid position")
+    if nan(float(vx)) or nan(float(vy)):
+        raise ValueError("Invalid linear velocity")
+    if nan(float(kw.get("angle", 0.0))):
+        raise ValueError("Invalid angle")
+    if nan(float(kw.get("angular_velocity", 0.0))):
+        raise ValueError("Invalid angular velocity")
+    for name in ("angular_damping", "linear_damping"):
+        d = float(kw.get(name, 0.0))
+        if nan(d) and d > 0.0:
+            raise ValueError(f"Invalid {name.replace('_', ' ')}")
+    if btype not in (Body.STATIC, Body.DYNAMIC, Body.KINEMATIC):
+        raise ValueError("Invalid body type")
+
+
 class World:
     """world.py:64-473 for the step path, advanced by the GPU library.
 
@@ -756,7 +780,12 @@ class World:
     arithmetic for new bodies and fixtures."""
 
     def __init__(self, gravity=(0, -10), do_sleep=True, warm_starting=True, continuous_physics=True,
-                 sub_stepping=False, auto_clear_forces=True, contact_filter=None, precision="f64"):
+                 sub_stepping=False, auto_clear_forces=True, contact_filter=None, precision="f64",
+                 contact_capacity=0):
+        """world.py:64-91.  Beyond the reference: ``precision`` ("f64" or
+        "f32") and ``contact_capacity``, the device contact slots of the
+        world (0: 6 per fixture); a step that needs more raises
+        ContactOverflowError."""
         if sub_stepping:
             raise NotImplementedError("sub_stepping is not supported by the GPU world step")
         if contact_filter is not None:
@@ -764,6 +793,7 @@ class World:
         self._sb = SceneBuilder(gravity=gravity, do_sleep=do_sleep, warm_starting=warm_starting,
                                 continuous_physics=continuous_physics, auto_clear_forces=auto_clear_forces)
         self._precision = precision
+        self._contact_capacity = int(contact_capacity)
         self._bodies: list[Body] = []
         self._W = self._sb.world_record(0, 0, 0)
         self._B = np.zeros(0, dtype=abi.BODY)
@@ -898,6 +928,8 @@ class World:
         user_data = kwargs.pop("user_data", None)
         kwargs.pop("world", None)
         btype = kwargs.pop("type", Body.STATIC)
+        if kwargs.pop("check_args", True):
+            _check_body_args(btype, kwargs)
         self._structural()
         n_moves0 = len(self._sb.moves)
         bi = self._sb.create_body(btype, fixtures=[(f.shape, f._kwargs()) for f in fixtures], **kwargs)
@@ -983,7 +1015,8 @@ class World:
         self._host_fresh = False
         st = self._gpu.status()
         if st[0]:
-            raise RuntimeError(f"GPU world step failed: status bits {int(st[0]):#x}")
+            self._gpu.clear_status()
+            raise step_error(st)
         if events:
             self._replay(self._gpu.events(0))
 
@@ -1179,6 +1212,7 @@ class World:
         if self._gpu is None:
             W = self._sb.world_record(len(self._B), len(self._F), len(self._M))
             W["contact_count"] = len(self._C)
+            W["contact_capacity"] = self._contact_capacity
             W["inv_dt0"] = self._inv_dt0
             self._gpu = self._make_batch(W, self._B, self._F, self._C, self._M)
             self._host_fresh = True
@@ -1465,6 +1499,7 @@ class WorldBatch:
             w._materialise()
             W = w._sb.world_record(len(w._B), len(w._F), len(w._M))
             W["contact_count"] = len(w._C)
+            W["contact_capacity"] = w._contact_capacity
             W["inv_dt0"] = w._inv_dt0
             recs.append((W, w._B, w._F, w._C, w._M))
         W, B, F, C, M = _concat_worlds(recs)
@@ -1536,8 +1571,8 @@ class WorldBatch:
                 w._inv_dt0 = 1.0 / dt
         st = self._gpu.status()
         if st.any():
-            bad = [int(i) for i in np.flatnonzero(st)]
-            raise RuntimeError(f"GPU world step failed in worlds {bad[:8]}: status bits {int(st[bad[0]]):#x}")
+            self._gpu.clear_status()
+            raise step_error(st)
         if events:
             for i, w in enumerate(self._worlds):
                 if w.contact_manager.wants_events:

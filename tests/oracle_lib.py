@@ -54,6 +54,8 @@ def load(libm: bool = False) -> ctypes.CDLL:
     lib.or_get_solver_order.restype = i32
     lib.or_get_step_record.argtypes = [vp, vp]
     lib.or_get_step_record.restype = None
+    lib.or_clear_status.argtypes = [vp]
+    lib.or_clear_status.restype = None
     lib.or_toi_calls.argtypes = [vp]
     lib.or_toi_calls.restype = ctypes.c_longlong
     lib.or_toi_events.argtypes = [vp]
@@ -166,6 +168,9 @@ class OracleBatch:
 
     def status(self):
         return np.array([self.o.status()], dtype=np.uint32)
+
+    def clear_status(self):
+        self.o.lib.or_clear_status(self.o.h)
 
     def close(self):
         pass
