@@ -356,6 +356,46 @@ def scene_uneven(b2, seed=11, n=250):
     return world
 
 
+def scene_sensor_filter(b2, seed=13):
+    """Sensors and collision filtering (contact.py:222-233 sensor touching,
+    world.py:958-970 default filter): a static sensor box the bodies fall
+    through; a dynamic circle carrying a large sensor ring; four boxes of
+    group -1 (never collide with each other) falling through one another
+    onto the ground; two boxes of group 2 (always collide) stacked; a
+    category-2 plank on posts and a box whose mask leaves category 2 out, so
+    it falls through the plank."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    world.create_static_body(position=(0, -0.5), shapes=b2.Polygon(box=(20, 0.5)))
+    region = world.create_static_body(position=(-6.0, 3.0))
+    region.create_polygon_fixture(box=(2.0, 1.5), sensor=True)
+    for k in range(3):   # bodies falling through the sensor region
+        b = world.create_dynamic_body(position=(-6.5 + 1.0 * k, 7.0 + 1.2 * k), angle=rng.uniform(-0.5, 0.5))
+        if k % 2:
+            b.create_circle_fixture(radius=0.4, density=1.0, friction=0.5)
+        else:
+            b.create_polygon_fixture(box=(0.4, 0.3), density=1.0, friction=0.5)
+    ring = world.create_dynamic_body(position=(-1.0, 1.5))
+    ring.create_circle_fixture(radius=0.5, density=2.0, friction=0.4)
+    ring.create_circle_fixture(radius=1.6, sensor=True)
+    for k in range(4):   # group -1: they pass through each other
+        b = world.create_dynamic_body(position=(2.0 + 0.3 * k, 1.0 + 0.7 * k), angle=0.2 * k)
+        b.create_polygon_fixture(box=(0.5, 0.5), density=1.0, friction=0.6, group_index=-1)
+    for k in range(2):   # group 2: they collide
+        b = world.create_dynamic_body(position=(5.0, 0.6 + 1.1 * k))
+        b.create_polygon_fixture(box=(0.5, 0.5), density=1.0, friction=0.6, group_index=2)
+    posts = world.create_static_body(position=(9.0, 0.0))
+    posts.create_polygon_fixture(vertices=[(-2.2, 0.0), (-1.8, 0.0), (-1.8, 2.0), (-2.2, 2.0)])
+    posts.create_polygon_fixture(vertices=[(1.8, 0.0), (2.2, 0.0), (2.2, 2.0), (1.8, 2.0)])
+    plank = world.create_dynamic_body(position=(9.0, 2.3))
+    plank.create_polygon_fixture(box=(2.5, 0.2), density=1.0, friction=0.6, category_bits=0x0002)
+    ghost = world.create_dynamic_body(position=(9.0, 4.0))
+    ghost.create_polygon_fixture(box=(0.4, 0.4), density=1.0, friction=0.6, mask_bits=0xFFFD)
+    solid = world.create_dynamic_body(position=(9.8, 4.5))
+    solid.create_polygon_fixture(box=(0.3, 0.3), density=1.0, friction=0.6)
+    return world
+
+
 SCENES = {
     "pyramid": (scene_pyramid, 300, (1, 2, 3, 5, 10, 30, 100, 200, 300)),
     "pyramid5": (lambda b2: scene_pyramid(b2, rows=5), 150, (1, 2, 5, 20, 60, 150)),
@@ -364,6 +404,7 @@ SCENES = {
     "sleep": (scene_sleep, 90, (1, 10, 29, 30, 31, 45, 60, 90)),
     "uneven": (scene_uneven, 240, (1, 2, 5, 30, 60, 120, 180, 240)),
     "kinematic": (scene_kinematic, 180, (1, 2, 5, 20, 60, 120, 180)),
+    "sensor_filter": (scene_sensor_filter, 150, (1, 2, 5, 20, 40, 60, 90, 120, 150)),
 }
 
 

@@ -75,7 +75,7 @@ def test_wait_timeout_flags_and_the_context_stays_usable():
     g = GpuBatch(W, B, F, precision="f32", moves=M)
     for x in (ref, g):
         x.set_launch_config(3, 64, 2, 512)           # constraint chunks stream through 2 shared-memory buffers
-        x.step(DT, 8, 3, 10, launch_mode=0)
+        x.step(DT, 8, 3, 40, launch_mode=0)          # landed: every world has constraints to stream
     snap = g.snapshot()
     g.set_wait_polls(0)                              # every chunk wait gives up at once
     g.step(DT, 8, 3, 2, launch_mode=0)
@@ -99,7 +99,7 @@ def test_autotuner_discards_trials_that_raise_status_bits():
     from pypybox2d_gb300.gpu import GpuBatch
     W, B, F, M = scenes.pyramid_batch(16, rows=10, jitter=0.01, seed=4)
     g = GpuBatch(W, B, F, precision="f32", moves=M)
-    g.step(DT, 8, 3, 5, launch_mode=3, block_threads=64)
+    g.step(DT, 8, 3, 40, launch_mode=3, block_threads=64)   # landed: the solver has constraints
     g.set_wait_polls(0)
     best, trials = g.autotune(DT, 8, 3, steps_per_trial=2)
     chunked = [t for t in trials if t["launch_mode"] == 3 and t["pipe_bufs"] > 0]

@@ -8,7 +8,8 @@ solver set-up decisions of each body) -- step after step, with the
 oracle solving each island in the GPU's graph-coloured constraint order
 (the solver-order hook).  The scenes are the reference-exported initial
 states of the golden vectors (pyramid, mixed edge/circle/polygon box,
-bullets with time-of-impact events, sleeping bodies).
+bullets with time-of-impact events, sleeping bodies, kinematic bodies, and
+sensors with group and category/mask filtering).
 """
 import os
 
@@ -21,7 +22,8 @@ from pypybox2d_gb300 import abi
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-STEPS = {"pyramid": 40, "pyramid5": 150, "mixed": 120, "bullets": 60, "sleep": 90, "uneven": 240, "kinematic": 180}
+STEPS = {"pyramid": 40, "pyramid5": 150, "mixed": 120, "bullets": 60, "sleep": 90, "uneven": 240, "kinematic": 180,
+         "sensor_filter": 150}
 
 
 def _gpu():
