@@ -397,14 +397,14 @@ def scene_sensor_filter(b2, seed=13):
 
 
 SCENES = {
-    "pyramid": (scene_pyramid, 300, (1, 2, 3, 5, 10, 30, 100, 200, 300)),
-    "pyramid5": (lambda b2: scene_pyramid(b2, rows=5), 150, (1, 2, 5, 20, 60, 150)),
-    "mixed": (scene_mixed, 200, (1, 2, 5, 20, 60, 120, 200)),
-    "bullets": (scene_bullets, 60, (1, 2, 3, 5, 10, 20, 40, 60)),
-    "sleep": (scene_sleep, 90, (1, 10, 29, 30, 31, 45, 60, 90)),
-    "uneven": (scene_uneven, 240, (1, 2, 5, 30, 60, 120, 180, 240)),
-    "kinematic": (scene_kinematic, 180, (1, 2, 5, 20, 60, 120, 180)),
-    "sensor_filter": (scene_sensor_filter, 150, (1, 2, 5, 20, 40, 60, 90, 120, 150)),
+    "pyramid": (scene_pyramid, 300, (1, 2, 3, 5, 10, 30, 31, 100, 101, 200, 201, 300)),
+    "pyramid5": (lambda b2: scene_pyramid(b2, rows=5), 150, (1, 2, 5, 20, 21, 60, 61, 150)),
+    "mixed": (scene_mixed, 200, (1, 2, 5, 20, 21, 60, 61, 120, 121, 200)),
+    "bullets": (scene_bullets, 60, (1, 2, 3, 5, 10, 11, 20, 21, 40, 41, 60)),
+    "sleep": (scene_sleep, 90, (1, 10, 29, 30, 31, 45, 46, 60, 90)),
+    "uneven": (scene_uneven, 240, (1, 2, 5, 30, 31, 60, 61, 120, 121, 180, 240)),
+    "kinematic": (scene_kinematic, 180, (1, 2, 5, 20, 21, 60, 61, 120, 121, 180)),
+    "sensor_filter": (scene_sensor_filter, 150, (1, 2, 5, 20, 21, 40, 60, 61, 90, 120, 121, 150)),
 }
 
 
