@@ -165,6 +165,50 @@ typedef struct gb_contact {
     uint32_t p_id[2];             /* index_a | index_b<<8 | type_a<<16 | type_b<<24 */
 } gb_contact;
 
+/* joint types (pypybox2d/joints/: revolute.py, prismatic.py, distance.py, weld.py) */
+#define GB_JOINT_REVOLUTE 1
+#define GB_JOINT_PRISMATIC 2
+#define GB_JOINT_DISTANCE 3
+#define GB_JOINT_WELD 4
+
+/* gb_joint.flags */
+#define GB_J_COLLIDE_CONNECTED 1u /* Joint._collide_connected */
+#define GB_J_LIMIT 2u             /* _limit_enabled (revolute, prismatic) */
+#define GB_J_MOTOR 4u             /* _motor_enabled (revolute, prismatic) */
+
+/* gb_joint.limit_state, as joints/joint.py:35 */
+#define GB_LIMIT_INACTIVE 0
+#define GB_LIMIT_LOWER 1
+#define GB_LIMIT_UPPER 2
+#define GB_LIMIT_EQUAL 3
+
+/* One joint: its definition and the state it carries between steps
+ * (joints/joint.py:41-59 and the kind's __init__).  Joints of a batch are
+ * sorted by world; within a world they are in World.joints order (creation
+ * order), which is also the order of every body's joint list.  Anchors and
+ * the prismatic axis are the local values the reference computes at
+ * creation (body.get_local_point / get_local_vector; the axis is not
+ * normalised, prismatic.py:82-85). */
+typedef struct gb_joint {
+    int32_t world;                 /* world of the batch */
+    int32_t type;                  /* GB_JOINT_* */
+    int32_t body_a, body_b;        /* world-local bodies */
+    uint32_t flags;                /* GB_J_* */
+    int32_t limit_state;           /* GB_LIMIT_* (revolute, prismatic) */
+    double la_x, la_y, lb_x, lb_y; /* _local_anchor_a, _local_anchor_b */
+    double ref_angle;              /* _reference_angle (revolute, prismatic, weld) */
+    double ax_x, ax_y;             /* prismatic _local_x_axis */
+    double lower, upper;           /* revolute _lower_angle/_upper_angle, prismatic _lower_limit/_upper_limit */
+    double max_motor;              /* revolute _max_motor_torque, prismatic _max_motor_force */
+    double motor_speed;
+    double length, frequency, damping_ratio; /* distance */
+    double impulse[3];             /* _impulse (distance: impulse[0]) */
+    double motor_impulse;          /* _motor_impulse */
+    double gamma, bias;            /* distance: kept from the last set-up with frequency > 0 (distance.py:246-266) */
+    double ux, uy;                 /* last set-up: distance _u, prismatic _axis (for the reaction force) */
+    double perp_x, perp_y;         /* last set-up: prismatic _perp */
+} gb_joint;
+
 /* One world of a batch. */
 typedef struct gb_world_desc {
     int32_t body_start, body_count;       /* into the batch body array */
@@ -190,6 +234,8 @@ typedef struct gb_scene {
     const gb_contact *contacts;
     int32_t n_moves, _pad0;
     const int32_t *moves;                 /* world-local fixture indices (BroadPhase._move_buffer) */
+    int32_t n_joints, _pad1;
+    const gb_joint *joints;               /* sorted by world (NULL when n_joints is 0) */
 } gb_scene;
 
 typedef struct gb_batch gb_batch; /* opaque device-resident batch of worlds */
@@ -217,6 +263,8 @@ const char *gb_last_error(void);
 /* sizeof of gb_body, gb_fixture, gb_contact, gb_world_desc, gb_scene, gb_step_opts
  * (6 ints), so bindings can check their record layouts. */
 int gb_struct_sizes(int32_t *sizes);
+/* sizeof(gb_joint). */
+int gb_joint_size(void);
 
 /* One contact event of a step, replayed to the contact listeners after it.
  * `key` orders a world's events: (step of the call) << 48 | phase << 40 |
@@ -255,6 +303,18 @@ int gb_batch_get_contacts(gb_batch *batch, int32_t world, gb_contact *out, int32
  * the step ran with record_order set. */
 int gb_batch_get_solver_order(gb_batch *batch, int32_t world, int32_t *order, int32_t capacity,
                               int32_t *n_out, void *cuda_stream);
+/* The same for the joints (world-local joint indices in the order the
+ * passes visited them; every pass visits the joints before the contacts in
+ * the velocity iterations and after them in the position iterations, as
+ * island.py:107-148 does). */
+int gb_batch_get_joint_order(gb_batch *batch, int32_t world, int32_t *order, int32_t capacity,
+                             int32_t *n_out, void *cuda_stream);
+/* Copy the joints of the whole batch (scene order) with their carried state
+ * to host memory / overwrite them from host memory (definition and state:
+ * the setters of the joint classes).  The world and bodies of each joint must be
+ * the ones the batch was made with. */
+int gb_batch_get_joints(gb_batch *batch, gb_joint *joints, int32_t n_joints, void *cuda_stream);
+int gb_batch_set_joints(gb_batch *batch, const gb_joint *joints, int32_t n_joints, void *cuda_stream);
 /* Step record of one world's bodies (world-local order) from the last step
  * run with record_order bit 0 set: out[0..n) the decisions of each body,
  * out[n..2n) its island in the solve (the smallest world-local index of the

@@ -33,6 +33,7 @@
 #include <stdint.h>
 #include <pthread.h>
 #include "oracle_collide.h"
+#include "oracle_joints.h"
 #include "oracle.h"
 
 #define MAX_TRANSLATION 2.0
@@ -119,6 +120,14 @@ struct or_world {
      * (16-23), each capped at 255; set-up decision parities (24-27) */
     int *rec;
     int *rec_island;  /* island of each body in the last solve: its smallest non-static body id (-1: none) */
+    /* joints (World.joints order) and each body's joint list (Body.joints) */
+    gb_joint *j;
+    int nj;
+    ivec *bjoint;
+    int *jflag;           /* Joint._island_flag */
+    int *jhook_rank;      /* joint solver order hook: rank per joint */
+    int jhook_set;
+    ivec last_jorder;     /* joints in solver order, last _solve */
 };
 
 static void rec_add(int *x, int shift, int v) {
@@ -245,9 +254,16 @@ static int default_filter(const gb_fixture *a, const gb_fixture *b) {
     return ((a->mask_bits & b->category_bits) != 0) && ((a->category_bits & b->mask_bits) != 0);
 }
 
-/* body.py:891-909 _should_collide (no joints in this restatement) */
-static int should_collide(const gb_body *a, const gb_body *b) {
-    if (a->type != GB_BODY_DYNAMIC && b->type != GB_BODY_DYNAMIC) return 0;
+/* body.py:912-927 _should_collide of body `a` with body `b`: one of them
+ * dynamic, and no joint between them that turns collision off */
+static int should_collide(const or_world *w, int a, int b) {
+    if (w->b[a].type != GB_BODY_DYNAMIC && w->b[b].type != GB_BODY_DYNAMIC) return 0;
+    const ivec *lst = &w->bjoint[a];
+    for (int i = 0; i < lst->n; ++i) {
+        const gb_joint *J = &w->j[lst->d[i]];
+        if ((J->body_a == a && J->body_b == b) || (J->body_b == a && J->body_a == b))
+            if (!(J->flags & GB_J_COLLIDE_CONNECTED)) return 0;
+    }
     return 1;
 }
 
@@ -326,7 +342,7 @@ static void find_new_contacts(or_world *w) {
             if (c->fa == fb && c->fb == fa && c->ia == 0 && c->ib == 0) { exists = 1; break; }
         }
         if (exists) continue;
-        if (!should_collide(&w->b[bb], &w->b[ba])) continue;
+        if (!should_collide(w, bb, ba)) continue;
         if (!default_filter(&w->f[fa], &w->f[fb])) continue;
         create_contact(w, fa, 0, fb, 0);
     }
@@ -390,7 +406,10 @@ static void collide(or_world *w) {
         int act_b = body_awake(bb) && bb->type != GB_BODY_STATIC;
         if (!act_a && !act_b) continue;
         if (c->flags & GB_C_FILTER) {
-            if (!should_collide(bb, ba) || !default_filter(&w->f[c->fa], &w->f[c->fb])) { rm[nrm++] = id; continue; }
+            if (!should_collide(w, w->f[c->fb].body, w->f[c->fa].body) || !default_filter(&w->f[c->fa], &w->f[c->fb])) {
+                rm[nrm++] = id;
+                continue;
+            }
             c->flags &= ~GB_C_FILTER;
         }
         if (!aabb_overlap(w->f[c->fa].aabb, w->f[c->fb].aabb)) { rm[nrm++] = id; continue; }
@@ -654,6 +673,11 @@ static int cmp_rank(const void *x, const void *y) {
     int ra = rank_w->hook_rank[a], rb = rank_w->hook_rank[b];
     return (ra < rb) ? -1 : (ra > rb ? 1 : 0);
 }
+static int cmp_jrank(const void *x, const void *y) {
+    int a = *(const int *)x, b = *(const int *)y;
+    int ra = rank_w->jhook_rank[a], rb = rank_w->jhook_rank[b];
+    return (ra < rb) ? -1 : (ra > rb ? 1 : 0);
+}
 
 /* Step record: parity of the restitution-bias points (bit `shift`) and of
  * the block solver's drop to one point (bit shift + 1) of a constraint,
@@ -666,8 +690,8 @@ static void rec_decisions(or_world *w, const int *bodies, const or_cons *k, int 
 }
 
 /* island.py:65-179 Island.solve */
-static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts, int nci, double dt, double inv_dt,
-                         double dt_ratio, int vel_iters, int pos_iters, int warm) {
+static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts, int nci, int *joints, int nji, double dt,
+                         double inv_dt, double dt_ratio, int vel_iters, int pos_iters, int warm) {
     (void)inv_dt;
     v2 *pc = (v2 *)malloc(sizeof(v2) * nbi);
     double *pa = (double *)malloc(sizeof(double) * nbi);
@@ -700,8 +724,31 @@ static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts,
     for (int i = 0; i < nci; ++i) rec_decisions(w, bodies, &ks[i], 24);
     if (warm)
         for (int i = 0; i < nci; ++i) warm_start(&ks[i], vv, ww);
-    for (int it = 0; it < vel_iters; ++it)
+    /* joints: set-up with their warm start after the contacts' (island.py:107-108) */
+    if (w->jhook_set) {
+        rank_w = w;
+        qsort(joints, nji, sizeof(int), cmp_jrank);
+    }
+    for (int i = 0; i < nji; ++i) iv_push(&w->last_jorder, joints[i]);
+    or_jcons *jk = (or_jcons *)malloc(sizeof(or_jcons) * (size_t)(nji > 0 ? nji : 1));
+    for (int i = 0; i < nji; ++i) {
+        gb_joint *J = &w->j[joints[i]];
+        const gb_body *ba = &w->b[J->body_a], *bb = &w->b[J->body_b];
+        or_jcons *k = &jk[i];
+        k->j = joints[i];
+        k->ia = w->island_index[J->body_a];
+        k->ib = w->island_index[J->body_b];
+        k->lca = V(ba->lcx, ba->lcy);
+        k->lcb = V(bb->lcx, bb->lcy);
+        k->ma = ba->inv_mass; k->mb = bb->inv_mass;
+        k->iA = ba->inv_I; k->iB = bb->inv_I;
+        joint_init(J, k, pc, pa, vv, ww, dt, dt_ratio, warm);
+    }
+    /* velocity iterations: the joints, then the contacts (island.py:110-113) */
+    for (int it = 0; it < vel_iters; ++it) {
+        for (int i = 0; i < nji; ++i) joint_solve_velocity(&w->j[jk[i].j], &jk[i], vv, ww, dt);
         for (int i = 0; i < nci; ++i) solve_velocity(&ks[i], vv, ww);
+    }
     /* store_impulses */
     for (int i = 0; i < nci; ++i) {
         or_contact *c = &w->c[ks[i].cid];
@@ -728,8 +775,15 @@ static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts,
     for (int it = 0; it < pos_iters; ++it) {
         double minsep = 0.0;
         for (int i = 0; i < nci; ++i) minsep = solve_position(&ks[i], pc, pa, minsep, -1, -1);
-        if (minsep >= -3.0 * OR_LINEAR_SLOP) { position_solved = 1; its = it + 1; break; }
+        /* the contacts, then every joint (island.py:141-153) */
+        int joints_okay = 1;
+        for (int i = 0; i < nji; ++i) {
+            int ok = joint_solve_position(&w->j[jk[i].j], &jk[i], pc, pa);
+            joints_okay = joints_okay && ok;
+        }
+        if (minsep >= -3.0 * OR_LINEAR_SLOP && joints_okay) { position_solved = 1; its = it + 1; break; }
     }
+    free(jk);
     int root = -1;
     for (int i = 0; i < nbi; ++i)
         if (w->b[bodies[i]].type != GB_BODY_STATIC && (root < 0 || bodies[i] < root)) root = bodies[i];
@@ -775,6 +829,9 @@ static void world_solve(or_world *w, double dt, double inv_dt, double dt_ratio, 
     int *bflag = w->island_flag_b;
     for (int i = 0; i < nb; ++i) bflag[i] = 0;
     for (int k = 0; k < w->order.n; ++k) w->c[w->order.d[k]].flags &= ~GB_C_ISLAND;
+    for (int k = 0; k < w->nj; ++k) w->jflag[k] = 0;
+    int *ijoints = (int *)malloc(sizeof(int) * (w->nj ? w->nj : 1));
+    w->last_jorder.n = 0;
     int *stack = (int *)malloc(sizeof(int) * (nb ? nb : 1));
     int *ibodies = (int *)malloc(sizeof(int) * (nb ? nb : 1));
     int *icontacts = (int *)malloc(sizeof(int) * (w->order.n ? w->order.n : 1));
@@ -795,7 +852,7 @@ static void world_solve(or_world *w, double dt, double inv_dt, double dt_ratio, 
         if (bflag[seed]) continue;
         if (!body_awake(sb) || !(sb->flags & GB_BODY_ACTIVE)) continue;
         if (sb->type == GB_BODY_STATIC) continue;
-        int nbi = 0, nci = 0, sp = 0;
+        int nbi = 0, nci = 0, nji = 0, sp = 0;
         stack[sp++] = seed;
         bflag[seed] = 1;
         while (sp > 0) {
@@ -823,8 +880,22 @@ static void world_solve(or_world *w, double dt, double inv_dt, double dt_ratio, 
                 stack[sp++] = ob;
                 bflag[ob] = 1;
             }
+            /* the body's joints (world.py:547-567); joints to inactive bodies are not simulated */
+            ivec *jl = &w->bjoint[bi];
+            for (int i = 0; i < jl->n; ++i) {
+                int jj = jl->d[i];
+                if (w->jflag[jj]) continue;
+                const gb_joint *J = &w->j[jj];
+                int ob = (J->body_a == bi) ? J->body_b : J->body_a;
+                if (!(w->b[ob].flags & GB_BODY_ACTIVE)) continue;
+                ijoints[nji++] = jj;
+                w->jflag[jj] = 1;
+                if (bflag[ob]) continue;
+                stack[sp++] = ob;
+                bflag[ob] = 1;
+            }
         }
-        island_solve(w, ibodies, nbi, icontacts, nci, dt, inv_dt, dt_ratio, vel_iters, pos_iters,
+        island_solve(w, ibodies, nbi, icontacts, nci, ijoints, nji, dt, inv_dt, dt_ratio, vel_iters, pos_iters,
                      (w->wflags & GB_W_WARM_STARTING) != 0);
         for (int i = 0; i < nbi; ++i)
             if (w->b[ibodies[i]].type == GB_BODY_STATIC) bflag[ibodies[i]] = 0;
@@ -832,7 +903,7 @@ static void world_solve(or_world *w, double dt, double inv_dt, double dt_ratio, 
     for (int i = 0; i < nb; ++i)
         if (bflag[i] && w->b[i].type != GB_BODY_STATIC) sync_fixtures(w, i);
     find_new_contacts(w);
-    free(stack); free(ibodies); free(icontacts); free(tmp);
+    free(stack); free(ibodies); free(icontacts); free(tmp); free(ijoints);
 }
 
 /* island.py:181-243 Island.solve_toi */
@@ -1047,6 +1118,7 @@ void or_step(or_world *w, double dt, int vel_iters, int pos_iters) {
     if (w->wflags & GB_W_AUTO_CLEAR_FORCES)
         for (int i = 0; i < w->nb; ++i) { w->b[i].fx = 0.0; w->b[i].fy = 0.0; w->b[i].torque = 0.0; }
     w->hook_set = 0;
+    w->jhook_set = 0;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1064,6 +1136,7 @@ or_world *or_create(const gb_world_desc *wd, const gb_body *bodies, const gb_fix
     w->island_index = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
     w->rec = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
     w->rec_island = (int *)calloc(w->nb ? w->nb : 1, sizeof(int));
+    w->bjoint = (ivec *)calloc(w->nb ? w->nb : 1, sizeof(ivec));
     w->wflags = wd->flags;
     w->gravity = V(wd->gx, wd->gy);
     w->inv_dt0 = wd->inv_dt0;
@@ -1101,6 +1174,9 @@ void or_destroy(or_world *w) {
     free(w->order.d); free(w->move.d); free(w->last_order.d);
     free(w->island_flag_b); free(w->island_index); free(w->hook_rank);
     free(w->hook_pending); free(w->pos_of); free(w->rec); free(w->rec_island);
+    if (w->bjoint)
+        for (int i = 0; i < w->nb; ++i) free(w->bjoint[i].d);
+    free(w->bjoint); free(w->j); free(w->jflag); free(w->jhook_rank); free(w->last_jorder.d);
     free(w->c); free(w->b); free(w->f);
     free(w);
 }
@@ -1151,6 +1227,55 @@ int or_get_solver_order(const or_world *w, int *out, int cap) {
 
 long long or_toi_calls(const or_world *w) { return w->n_toi_calls; }
 void or_clear_status(or_world *w) { w->status = 0; }
+
+/* The joints of a world (World.joints order, each added by World.add_joint,
+ * world.py:252-283); replaces any joints given before.  Returns -1 (and
+ * keeps the old joints) for a joint with a bad body index or type. */
+int or_set_joints(or_world *w, const gb_joint *joints, int n) {
+    for (int i = 0; i < n; ++i) {
+        const gb_joint *J = &joints[i];
+        if (J->body_a < 0 || J->body_a >= w->nb || J->body_b < 0 || J->body_b >= w->nb || J->body_a == J->body_b ||
+            J->type < GB_JOINT_REVOLUTE || J->type > GB_JOINT_WELD)
+            return -1;
+    }
+    for (int i = 0; i < w->nb; ++i) w->bjoint[i].n = 0;
+    w->j = (gb_joint *)realloc(w->j, sizeof(gb_joint) * (size_t)(n ? n : 1));
+    w->jflag = (int *)realloc(w->jflag, sizeof(int) * (size_t)(n ? n : 1));
+    w->jhook_rank = (int *)realloc(w->jhook_rank, sizeof(int) * (size_t)(n ? n : 1));
+    if (n) memcpy(w->j, joints, sizeof(gb_joint) * (size_t)n);
+    w->nj = n;
+    for (int i = 0; i < n; ++i) {
+        iv_push(&w->bjoint[w->j[i].body_a], i);
+        iv_push(&w->bjoint[w->j[i].body_b], i);
+    }
+    return 0;
+}
+/* World.add_joint's flagging of the contacts between a new joint's bodies
+ * (world.py:275-281), for a joint that turns collision off */
+void or_flag_joint_contacts(or_world *w, int j) {
+    const gb_joint *J = &w->j[j];
+    if (J->flags & GB_J_COLLIDE_CONNECTED) return;
+    ivec *lst = &w->bcon[J->body_b];
+    for (int i = 0; i < lst->n; ++i) {
+        or_contact *c = &w->c[lst->d[i]];
+        int other = (w->f[c->fa].body == J->body_b) ? w->f[c->fb].body : w->f[c->fa].body;
+        if (other == J->body_a) c->flags |= GB_C_FILTER;
+    }
+}
+int or_joint_count(const or_world *w) { return w->nj; }
+void or_get_joints(const or_world *w, gb_joint *out) { if (w->nj) memcpy(out, w->j, sizeof(gb_joint) * (size_t)w->nj); }
+/* Solve the next step's joints in this order (world joint indices); joints
+ * not listed come after the listed ones, in index order. */
+void or_set_joint_order(or_world *w, const int *order, int n) {
+    for (int k = 0; k < w->nj; ++k) w->jhook_rank[k] = n + k;
+    for (int i = 0; i < n; ++i)
+        if (order[i] >= 0 && order[i] < w->nj) w->jhook_rank[order[i]] = i;
+    w->jhook_set = 1;
+}
+int or_get_joint_order(const or_world *w, int *out, int cap) {
+    for (int i = 0; i < w->last_jorder.n && i < cap; ++i) out[i] = w->last_jorder.d[i];
+    return w->last_jorder.n;
+}
 void or_get_step_record(const or_world *w, int *out) {
     memcpy(out, w->rec, sizeof(int) * (size_t)w->nb);
     memcpy(out + w->nb, w->rec_island, sizeof(int) * (size_t)w->nb);
@@ -1169,6 +1294,16 @@ typedef struct {
     pthread_mutex_t mu;
 } or_job;
 
+/* the joints of world `wi` of a scene (sorted by world) */
+static void scene_joints(or_world *w, const gb_scene *scene, int wi) {
+    if (scene->n_joints <= 0 || !scene->joints) return;
+    int s0 = 0;
+    while (s0 < scene->n_joints && scene->joints[s0].world < wi) ++s0;
+    int s1 = s0;
+    while (s1 < scene->n_joints && scene->joints[s1].world == wi) ++s1;
+    if (s1 > s0) or_set_joints(w, scene->joints + s0, s1 - s0);
+}
+
 static void *or_worker(void *arg) {
     or_job *j = (or_job *)arg;
     for (;;) {
@@ -1178,6 +1313,7 @@ static void *or_worker(void *arg) {
         if (wi >= j->scene->n_worlds) break;
         const gb_world_desc *wd = &j->scene->worlds[wi];
         or_world *w = or_create(wd, j->scene->bodies, j->scene->fixtures, j->scene->contacts, j->scene->moves);
+        scene_joints(w, j->scene, wi);
         for (int s = 0; s < j->steps; ++s) or_step(w, j->dt, j->vi, j->pi);
         if (j->out) or_get_bodies(w, j->out + wd->body_start);
         or_destroy(w);
@@ -1214,8 +1350,10 @@ or_batch *or_batch_create(const gb_scene *scene) {
     or_batch *b = (or_batch *)calloc(1, sizeof(or_batch));
     b->n = scene->n_worlds;
     b->w = (or_world **)calloc(b->n ? b->n : 1, sizeof(or_world *));
-    for (int i = 0; i < b->n; ++i)
+    for (int i = 0; i < b->n; ++i) {
         b->w[i] = or_create(&scene->worlds[i], scene->bodies, scene->fixtures, scene->contacts, scene->moves);
+        scene_joints(b->w[i], scene, i);
+    }
     return b;
 }
 

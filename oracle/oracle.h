@@ -44,6 +44,18 @@ int or_get_solver_order(const or_world *w, int *out, int cap);
  * in the island solve (bits 24, 25) and in TOI sub-steps (26, 27) */
 void or_get_step_record(const or_world *w, int *out);
 void or_clear_status(or_world *w);
+/* The world's joints, in World.joints order (replaces any given before);
+ * -1 for a bad body index or type. */
+int or_set_joints(or_world *w, const gb_joint *joints, int n);
+/* World.add_joint's filter flag on the contacts between joint j's bodies
+ * (world.py:275-281; nothing for a joint with collide_connected). */
+void or_flag_joint_contacts(or_world *w, int j);
+int or_joint_count(const or_world *w);
+void or_get_joints(const or_world *w, gb_joint *out);
+/* Solve the next step's joints in this order (world joint indices). */
+void or_set_joint_order(or_world *w, const int *order, int n);
+/* Joint order of the last step. */
+int or_get_joint_order(const or_world *w, int *out, int cap);
 long long or_toi_calls(const or_world *w);
 long long or_toi_events(const or_world *w);
 

@@ -1,0 +1,640 @@
+/*
+ * oracle_joints.h -- TEST INFRASTRUCTURE: float64 restatement of the joint
+ * constraints pypybox2d's island solver runs beside the contacts
+ * (island.py:107-113, 145-148): revolute (joints/revolute.py:240-453),
+ * prismatic (joints/prismatic.py:238-513), distance
+ * (joints/distance.py:175-311) and weld (joints/weld.py:118-257).
+ *
+ * Every expression keeps the reference's operation order.  Two properties of
+ * the reference's C extension shape the arithmetic: Vec2 has no in-place
+ * operators (vec2module.c:636-652), so `x *= s` rebinds x and leaves other
+ * names bound to the old vector (the distance joint's effective mass uses
+ * the unnormalised direction, distance.py:212-222); Vec3 and Mat33 are
+ * Python classes (common.py:227-612) whose dot, cross and solves are
+ * restated below as written there.  Included by oracle.c only.
+ */
+#ifndef ORACLE_JOINTS_H
+#define ORACLE_JOINTS_H
+
+#include "oracle_math.h"
+#include "../include/gb2d.h"
+
+/* settings.py:61-94 */
+#define OR_LINEAR_SLOP_J 0.005
+#ifndef OR_ANGULAR_SLOP
+#define OR_ANGULAR_SLOP (2.0 / 180.0 * 3.141592653589793)
+#endif
+#define OR_MAX_LINEAR_CORRECTION_J 0.2
+#define OR_MAX_ANGULAR_CORRECTION (8.0 / 180.0 * 3.141592653589793)
+#define OR_PI 3.141592653589793
+
+typedef struct { double x, y, z; } v3;
+static inline v3 V3(double x, double y, double z) { v3 r; r.x = x; r.y = y; r.z = z; return r; }
+/* Vec3.dot: (x * vx) + (y * vy) + (z * vz), left to right */
+static inline double v3dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+/* Vec3.cross */
+static inline v3 v3cross(v3 s, v3 v) { return V3(s.y * v.z - s.z * v.y, s.z * v.x - s.x * v.z, s.x * v.y - s.y * v.x); }
+static inline v3 v3add(v3 a, v3 b) { return V3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 v3sub(v3 a, v3 b) { return V3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 v3neg(v3 a) { return V3(-a.x, -a.y, -a.z); }
+/* Vec3.__mul__(number): Vec3(value * x, value * y, value * z) */
+static inline v3 v3scale(double s, v3 a) { return V3(s * a.x, s * a.y, s * a.z); }
+
+/* Mat33 (column-major, common.py:533-612) */
+typedef struct { v3 c1, c2, c3; } m33;
+/* Mat33.solve3x3 */
+static inline v3 m33_solve3(m33 m, v3 b) {
+    double det = v3dot(m.c1, v3cross(m.c2, m.c3));
+    if (det != 0.0) det = 1.0 / det;
+    return V3(det * v3dot(b, v3cross(m.c2, m.c3)), det * v3dot(m.c1, v3cross(b, m.c3)), det * v3dot(m.c1, v3cross(m.c2, b)));
+}
+/* Mat33.solve2x2 (upper 2x2 block) */
+static inline v2 m33_solve2(m33 m, v2 v) {
+    double a11 = m.c1.x, a12 = m.c2.x, a21 = m.c1.y, a22 = m.c2.y;
+    double det = a11 * a22 - a12 * a21;
+    if (det != 0.0) det = 1.0 / det;
+    return V(det * (a22 * v.x - a12 * v.y), det * (a11 * v.y - a21 * v.x));
+}
+/* Mat22.solve (mat22module.c:500-516); K given by its columns */
+static inline v2 m22_solve(v2 c1, v2 c2, v2 v) {
+    double a = c1.x, b = c2.x, c = c1.y, d = c2.y;
+    double det = a * d - b * c;
+    if (det != 0.0) det = 1.0 / det;
+    return V(det * (d * v.x - b * v.y), det * (a * v.y - c * v.x));
+}
+
+/* What _init_velocity_constraints leaves on the joint for the passes of one
+ * step (the underscore attributes it sets). */
+typedef struct {
+    int j;                 /* joint index in the world */
+    int ia, ib;            /* island indices of body_a, body_b */
+    double ma, mb, iA, iB; /* _inv_mass_a/_b, _inv_Ia/_Ib */
+    v2 lca, lcb;           /* _local_center_a/_b */
+    v2 ra, rb;             /* _ra, _rb */
+    m33 m;                 /* revolute/weld _mass, prismatic _k */
+    double motor_mass;     /* revolute, prismatic */
+    v2 u;                  /* distance _u */
+    double dmass;          /* distance _mass */
+    v2 axis, perp;         /* prismatic */
+    double s1, s2, a1, a2;
+} or_jcons;
+
+static inline v2 j_la(const gb_joint *J) { return V(J->la_x, J->la_y); }
+static inline v2 j_lb(const gb_joint *J) { return V(J->lb_x, J->lb_y); }
+
+/* the carried _impulse minus its z component: `_impulse -= (0, 0, z)` */
+static inline void j_drop_z(gb_joint *J) { J->impulse[2] = J->impulse[2] - J->impulse[2]; }
+
+/* ------------------------------------------------------------ revolute */
+static void revolute_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt_ratio,
+                          int warm) {
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    double aa = pa[k->ia], ab = pa[k->ib];
+    (void)pc;
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    v2 ra = k->ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    k->m.c3 = V3(-ra.y * ia - rb.y * ib, ra.x * ia + rb.x * ib, ia + ib);
+    k->m.c2 = V3(-ra.y * ra.x * ia - rb.y * rb.x * ib, ma + mb + ra.x * ra.x * ia + rb.x * rb.x * ib, k->m.c3.y);
+    k->m.c1 = V3(ma + mb + ra.y * ra.y * ia + rb.y * rb.y * ib, k->m.c2.x, k->m.c3.x);
+    k->motor_mass = ia + ib;
+    int fixed_rotation = (k->motor_mass == 0.0);
+    if (k->motor_mass > 0.0) k->motor_mass = 1.0 / k->motor_mass;
+    if (!(J->flags & GB_J_MOTOR) || fixed_rotation) J->motor_impulse = 0.0;
+    if ((J->flags & GB_J_LIMIT) && !fixed_rotation) {
+        double joint_angle = ab - aa - J->ref_angle;
+        if (fabs(J->upper - J->lower) < 2.0 * OR_ANGULAR_SLOP) {
+            J->limit_state = GB_LIMIT_EQUAL;
+        } else if (joint_angle <= J->lower) {
+            if (J->limit_state != GB_LIMIT_LOWER) j_drop_z(J);
+            J->limit_state = GB_LIMIT_LOWER;
+        } else if (joint_angle >= J->upper) {
+            if (J->limit_state != GB_LIMIT_UPPER) j_drop_z(J);
+            J->limit_state = GB_LIMIT_UPPER;
+        } else {
+            J->limit_state = GB_LIMIT_INACTIVE;
+            j_drop_z(J);
+        }
+    } else {
+        J->limit_state = GB_LIMIT_INACTIVE;
+    }
+    if (warm) {
+        J->impulse[0] = dt_ratio * J->impulse[0];
+        J->impulse[1] = dt_ratio * J->impulse[1];
+        J->impulse[2] = dt_ratio * J->impulse[2];
+        J->motor_impulse = J->motor_impulse * dt_ratio;
+        v2 P = V(J->impulse[0], J->impulse[1]);
+        va = vsub(va, vscale(ma, P));
+        wa = wa - ia * (vcross(ra, P) + J->motor_impulse + J->impulse[2]);
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + ib * (vcross(rb, P) + J->motor_impulse + J->impulse[2]);
+    } else {
+        J->impulse[0] = J->impulse[1] = J->impulse[2] = 0.0;
+        J->motor_impulse = 0.0;
+    }
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void revolute_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww, double dt) {
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ra = k->ra, rb = k->rb;
+    int fixed_rotation = ((ia + ib) == 0.0);
+    if ((J->flags & GB_J_MOTOR) && J->limit_state != GB_LIMIT_EQUAL && !fixed_rotation) {
+        double Cdot = wb - wa - J->motor_speed;
+        double impulse = k->motor_mass * (-Cdot);
+        double old_impulse = J->motor_impulse;
+        double max_impulse = dt * J->max_motor;
+        J->motor_impulse = cclamp(J->motor_impulse + impulse, -max_impulse, max_impulse);
+        impulse = J->motor_impulse - old_impulse;
+        wa = wa - ia * impulse;
+        wb = wb + ib * impulse;
+    }
+    if ((J->flags & GB_J_LIMIT) && J->limit_state != GB_LIMIT_INACTIVE && !fixed_rotation) {
+        v2 Cdot1 = vsub(vsub(vadd(vb, vcross_sv(wb, rb)), va), vcross_sv(wa, ra));
+        double Cdot2 = wb - wa;
+        v3 impulse = v3neg(m33_solve3(k->m, V3(Cdot1.x, Cdot1.y, Cdot2)));
+        v3 acc = V3(J->impulse[0], J->impulse[1], J->impulse[2]);
+        if (J->limit_state == GB_LIMIT_EQUAL) {
+            acc = v3add(acc, impulse);
+        } else if (J->limit_state == GB_LIMIT_LOWER || J->limit_state == GB_LIMIT_UPPER) {
+            double new_impulse = acc.z + impulse.z;
+            int clamp_it = J->limit_state == GB_LIMIT_LOWER ? (new_impulse < 0.0) : (new_impulse > 0.0);
+            if (clamp_it) {
+                v2 rhs = vadd(vneg(Cdot1), vscale(acc.z, V(k->m.c3.x, k->m.c3.y)));
+                v2 reduced = m33_solve2(k->m, rhs);
+                impulse = V3(reduced.x, reduced.y, -acc.z);
+                acc = v3add(acc, V3(reduced.x, reduced.y, -acc.z));
+            } else {
+                acc = v3add(acc, impulse);
+            }
+        }
+        J->impulse[0] = acc.x; J->impulse[1] = acc.y; J->impulse[2] = acc.z;
+        v2 P = V(impulse.x, impulse.y);
+        va = vsub(va, vscale(ma, P));
+        wa = wa - ia * (vcross(ra, P) + impulse.z);
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + ib * (vcross(rb, P) + impulse.z);
+    } else {
+        v2 Cdot = vsub(vsub(vadd(vb, vcross_sv(wb, rb)), va), vcross_sv(wa, ra));
+        v2 impulse = m33_solve2(k->m, vneg(Cdot));
+        J->impulse[0] = J->impulse[0] + impulse.x;
+        J->impulse[1] = J->impulse[1] + impulse.y;
+        J->impulse[2] = J->impulse[2] + 0.0;
+        va = vsub(va, vscale(ma, impulse));
+        wa = wa - ia * vcross(ra, impulse);
+        vb = vadd(vb, vscale(mb, impulse));
+        wb = wb + ib * vcross(rb, impulse);
+    }
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static int revolute_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    int fixed_rotation = ((ia + ib) == 0.0);
+    double angular_error = 0.0, position_error = 0.0;
+    if ((J->flags & GB_J_LIMIT) && J->limit_state != GB_LIMIT_INACTIVE && !fixed_rotation) {
+        double angle = ab - aa - J->ref_angle;
+        double limit_impulse = 0.0;
+        if (J->limit_state == GB_LIMIT_EQUAL) {
+            double C = cclamp(angle - J->lower, -OR_MAX_ANGULAR_CORRECTION, OR_MAX_ANGULAR_CORRECTION);
+            limit_impulse = -k->motor_mass * C;
+            angular_error = fabs(C);
+        } else if (J->limit_state == GB_LIMIT_LOWER) {
+            double C = angle - J->lower;
+            angular_error = -C;
+            C = cclamp(C + OR_ANGULAR_SLOP, -OR_MAX_ANGULAR_CORRECTION, 0.0);
+            limit_impulse = -k->motor_mass * C;
+        } else if (J->limit_state == GB_LIMIT_UPPER) {
+            double C = angle - J->upper;
+            angular_error = C;
+            C = cclamp(C - OR_ANGULAR_SLOP, 0.0, OR_MAX_ANGULAR_CORRECTION);
+            limit_impulse = -k->motor_mass * C;
+        }
+        aa = aa - ia * limit_impulse;
+        ab = ab + ib * limit_impulse;
+    }
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    v2 ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 C = vsub(vsub(vadd(cb, rb), ca), ra);
+    position_error = vlen(C);
+    double rax = ra.x, ray = ra.y, rbx = rb.x, rby = rb.y;
+    v2 c1 = V(ma + mb + ia * ray * ray + ib * rby * rby, -ia * rax * ray - ib * rbx * rby);
+    v2 c2 = V(c1.y, ma + mb + ia * rax * rax + ib * rbx * rbx);
+    v2 impulse = vneg(m22_solve(c1, c2, C));
+    ca = vsub(ca, vscale(ma, impulse));
+    aa = aa - ia * vcross(ra, impulse);
+    cb = vadd(cb, vscale(mb, impulse));
+    ab = ab + ib * vcross(rb, impulse);
+    pc[k->ia] = ca; pa[k->ia] = aa;
+    pc[k->ib] = cb; pa[k->ib] = ab;
+    return position_error <= OR_LINEAR_SLOP_J && angular_error <= OR_ANGULAR_SLOP;
+}
+
+/* ------------------------------------------------------------ prismatic */
+/* prismatic.py:82-85: local y axis = scalar_cross(1.0, local x axis) */
+static inline v2 j_ly(const gb_joint *J) { return vcross_sv(1.0, V(J->ax_x, J->ax_y)); }
+
+static void prismatic_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt_ratio,
+                           int warm) {
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    v2 ra = k->ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 d = vsub(vsub(vadd(cb, rb), ca), ra);
+    v2 axis = k->axis = rmul(qa, V(J->ax_x, J->ax_y));
+    double a1 = k->a1 = vcross(vadd(d, ra), axis);
+    double a2 = k->a2 = vcross(rb, axis);
+    k->motor_mass = ma + mb + ia * SQ(a1) + ib * SQ(a2);
+    if (k->motor_mass > 0.0) k->motor_mass = 1.0 / k->motor_mass;
+    v2 perp = k->perp = rmul(qa, j_ly(J));
+    double s1 = k->s1 = vcross(vadd(d, ra), perp);
+    double s2 = k->s2 = vcross(rb, perp);
+    double k11 = ma + mb + ia * SQ(s1) + ib * SQ(s2);
+    double k12 = ia * s1 + ib * s2;
+    double k13 = ia * s1 * a1 + ib * s2 * a2;
+    double k22 = ia + ib;
+    if (k22 == 0.0) k22 = 1.0;
+    double k23 = ia * a1 + ib * a2;
+    double k33 = ma + mb + ia * SQ(a1) + ib * SQ(a2);
+    k->m.c1 = V3(k11, k12, k13);
+    k->m.c2 = V3(k12, k22, k23);
+    k->m.c3 = V3(k13, k23, k33);
+    if (J->flags & GB_J_LIMIT) {
+        double joint_translation = vdot(axis, d);
+        if (fabs(J->upper - J->lower) < 2.0 * OR_LINEAR_SLOP_J) {
+            J->limit_state = GB_LIMIT_EQUAL;
+        } else if (joint_translation <= J->lower) {
+            if (J->limit_state != GB_LIMIT_LOWER) { J->limit_state = GB_LIMIT_LOWER; j_drop_z(J); }
+        } else if (joint_translation >= J->upper) {
+            if (J->limit_state != GB_LIMIT_UPPER) { J->limit_state = GB_LIMIT_UPPER; j_drop_z(J); }
+        } else {
+            J->limit_state = GB_LIMIT_INACTIVE;
+            j_drop_z(J);
+        }
+    } else {
+        J->limit_state = GB_LIMIT_INACTIVE;
+        j_drop_z(J);
+    }
+    if (!(J->flags & GB_J_MOTOR)) J->motor_impulse = 0.0;
+    if (warm) {
+        J->impulse[0] = dt_ratio * J->impulse[0];
+        J->impulse[1] = dt_ratio * J->impulse[1];
+        J->impulse[2] = dt_ratio * J->impulse[2];
+        J->motor_impulse = J->motor_impulse * dt_ratio;
+        double ix = J->impulse[0], iy = J->impulse[1], iz = J->impulse[2], mi = J->motor_impulse;
+        v2 P = vadd(vscale(ix, perp), vscale(mi + iz, axis));
+        double L1 = ix * s1 + iy + (mi + iz) * a1;
+        double L2 = ix * s2 + iy + (mi + iz) * a2;
+        va = vsub(va, vscale(ma, P));
+        wa = wa - ia * L1;
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + ib * L2;
+    } else {
+        J->impulse[0] = J->impulse[1] = J->impulse[2] = 0.0;
+        J->motor_impulse = 0.0;
+    }
+    J->ux = axis.x; J->uy = axis.y;
+    J->perp_x = perp.x; J->perp_y = perp.y;
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void prismatic_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww, double dt) {
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    double a1 = k->a1, a2 = k->a2, s1 = k->s1, s2 = k->s2;
+    v2 perp = k->perp, axis = k->axis;
+    if ((J->flags & GB_J_MOTOR) && J->limit_state != GB_LIMIT_EQUAL) {
+        double Cdot = vdot(axis, vsub(vb, va)) + a2 * wb - a1 * wa;
+        double impulse = k->motor_mass * (J->motor_speed - Cdot);
+        double old_impulse = J->motor_impulse;
+        double max_impulse = dt * J->max_motor;
+        J->motor_impulse = cclamp(J->motor_impulse + impulse, -max_impulse, max_impulse);
+        impulse = J->motor_impulse - old_impulse;
+        v2 P = vscale(impulse, axis);
+        double L1 = impulse * a1, L2 = impulse * a2;
+        va = vsub(va, vscale(ma, P));
+        wa = wa - ia * L1;
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + ib * L2;
+    }
+    v2 Cdot1 = V(vdot(perp, vsub(vb, va)) + s2 * wb - s1 * wa, wb - wa);
+    v2 P;
+    double L1, L2;
+    if ((J->flags & GB_J_LIMIT) && J->limit_state != GB_LIMIT_INACTIVE) {
+        double Cdot2 = vdot(axis, vsub(vb, va)) + a2 * wb - a1 * wa;
+        v3 Cdot = V3(Cdot1.x, Cdot1.y, Cdot2);
+        v3 old = V3(J->impulse[0], J->impulse[1], J->impulse[2]);
+        v3 df = m33_solve3(k->m, v3neg(Cdot));
+        v3 acc = v3add(old, df);
+        double iz;
+        if (J->limit_state == GB_LIMIT_LOWER) iz = pymax(acc.z, 0.0);
+        else if (J->limit_state == GB_LIMIT_UPPER) iz = pymin(acc.z, 0.0);
+        else iz = acc.z;
+        v2 b = vsub(vneg(Cdot1), vscale(acc.z - old.z, V(k->m.c3.x, k->m.c3.y)));
+        v2 f2r = vadd(m33_solve2(k->m, b), V(old.x, old.y));
+        acc = V3(f2r.x, f2r.y, iz);
+        J->impulse[0] = acc.x; J->impulse[1] = acc.y; J->impulse[2] = acc.z;
+        df = v3sub(acc, old);
+        P = vadd(vscale(df.x, perp), vscale(df.z, axis));
+        L1 = df.x * s1 + df.y + df.z * a1;
+        L2 = df.x * s2 + df.y + df.z * a2;
+    } else {
+        v2 df = m33_solve2(k->m, vneg(Cdot1));
+        J->impulse[0] = J->impulse[0] + df.x;
+        J->impulse[1] = J->impulse[1] + df.y;
+        J->impulse[2] = J->impulse[2] + 0.0;
+        P = vscale(df.x, perp);
+        L1 = df.x * s1 + df.y;
+        L2 = df.x * s2 + df.y;
+    }
+    va = vsub(va, vscale(ma, P));
+    wa = wa - ia * L1;
+    vb = vadd(vb, vscale(mb, P));
+    wb = wb + ib * L2;
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static int prismatic_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    v2 ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 d = vsub(vsub(vadd(cb, rb), ca), ra);
+    v2 axis = rmul(qa, V(J->ax_x, J->ax_y));
+    double a1 = vcross(vadd(d, ra), axis);
+    double a2 = vcross(rb, axis);
+    v2 perp = rmul(qa, j_ly(J));
+    double s1 = vcross(vadd(d, ra), perp);
+    double s2 = vcross(rb, perp);
+    v2 C1 = V(vdot(perp, d), ab - aa - J->ref_angle);
+    double linear_error = fabs(C1.x), angular_error = fabs(C1.y);
+    int active = 0;
+    double C2 = 0.0;
+    if (J->flags & GB_J_LIMIT) {
+        double translation = vdot(axis, d);
+        if (fabs(J->upper - J->lower) < 2.0 * OR_LINEAR_SLOP_J) {
+            C2 = cclamp(translation, -OR_MAX_LINEAR_CORRECTION_J, OR_MAX_LINEAR_CORRECTION_J);
+            linear_error = pymax(linear_error, translation);
+            active = 1;
+        } else if (translation <= J->lower) {
+            C2 = cclamp(translation - J->lower + OR_LINEAR_SLOP_J, -OR_MAX_LINEAR_CORRECTION_J, 0.0);
+            linear_error = pymax(linear_error, J->lower - translation);
+            active = 1;
+        } else if (translation >= J->upper) {
+            C2 = cclamp(translation - J->upper - OR_LINEAR_SLOP_J, 0.0, OR_MAX_LINEAR_CORRECTION_J);
+            linear_error = pymax(linear_error, translation - J->upper);
+            active = 1;
+        }
+    }
+    double ix, iy, iz;
+    if (active) {
+        double k11 = ma + mb + ia * SQ(s1) + ib * SQ(s2);
+        double k12 = ia * s1 + ib * s2;
+        double k13 = ia * s1 * a1 + ib * s2 * a2;
+        double k22 = ia + ib;
+        if (k22 == 0.0) k22 = 1.0;
+        double k23 = ia * a1 + ib * a2;
+        double k33 = ma + mb + ia * SQ(a1) + ib * SQ(a2);
+        m33 K;
+        K.c1 = V3(k11, k12, k13); K.c2 = V3(k12, k22, k23); K.c3 = V3(k13, k23, k33);
+        v3 impulse = m33_solve3(K, v3neg(V3(C1.x, C1.y, C2)));
+        ix = impulse.x; iy = impulse.y; iz = impulse.z;
+    } else {
+        double k11 = ma + mb + ia * s1 * s1 + ib * s2 * s2;
+        double k12 = ia * s1 + ib * s2;
+        double k22 = ia + ib;
+        if (k22 == 0.0) k22 = 1.0;
+        m33 K = k->m;   /* the step's _k with its first two columns replaced (prismatic.py:493-494) */
+        K.c1 = V3(k11, k12, 0.0);
+        K.c2 = V3(k12, k22, 0.0);
+        v2 impulse1 = m33_solve2(K, vneg(C1));
+        ix = impulse1.x; iy = impulse1.y; iz = 0.0;
+    }
+    v2 P = vadd(vscale(ix, perp), vscale(iz, axis));
+    double L1 = ix * s1 + iy + iz * a1;
+    double L2 = ix * s2 + iy + iz * a2;
+    ca = vsub(ca, vscale(ma, P));
+    cb = vadd(cb, vscale(mb, P));
+    aa = aa - ia * L1;
+    ab = ab + ib * L2;
+    pc[k->ia] = ca; pa[k->ia] = aa;
+    pc[k->ib] = cb; pa[k->ib] = ab;
+    return (linear_error <= OR_LINEAR_SLOP_J) && (angular_error <= OR_ANGULAR_SLOP);
+}
+
+/* ------------------------------------------------------------ distance */
+static void distance_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt,
+                          double dt_ratio, int warm) {
+    double ma = k->ma, mb = k->mb, iA = k->iA, iB = k->iB;
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    v2 ra = k->ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 u = vsub(vsub(vadd(cb, rb), ca), ra);   /* `u` keeps this vector: `self._u *= ...` rebinds only _u */
+    double length = vlen(u);
+    if (length > OR_LINEAR_SLOP_J) k->u = vscale(1.0 / length, u);
+    else k->u = V(0.0, 0.0);
+    double cr_au = SQ(vcross(ra, u));
+    double cr_bu = SQ(vcross(rb, u));
+    double inv_mass = ma + iA * cr_au + mb + iB * cr_bu;
+    k->dmass = inv_mass != 0.0 ? 1.0 / inv_mass : 0.0;
+    if (J->frequency > 0.0) {
+        double C = length - J->length;
+        double omega = 2.0 * OR_PI * J->frequency;
+        double dd = 2.0 * k->dmass * J->damping_ratio * omega;
+        double kk = k->dmass * SQ(omega);
+        double gamma = dt * (dd + dt * kk);
+        J->gamma = gamma != 0.0 ? 1.0 / gamma : 0.0;
+        J->bias = C * dt * kk * J->gamma;
+        double mass = inv_mass + J->gamma;
+        k->dmass = mass != 0.0 ? 1.0 / mass : 0.0;
+    }
+    if (warm) {
+        J->impulse[0] = J->impulse[0] * dt_ratio;
+        v2 P = vscale(J->impulse[0], k->u);
+        va = vsub(va, vscale(ma, P));
+        wa = wa - iA * vcross(ra, P);
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + iB * vcross(rb, P);
+    } else {
+        J->impulse[0] = 0.0;
+    }
+    J->ux = k->u.x; J->uy = k->u.y;
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void distance_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww) {
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    v2 ra = k->ra, rb = k->rb;
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 vpa = vadd(va, vcross_sv(wa, ra));
+    v2 vpb = vadd(vb, vcross_sv(wb, rb));
+    double Cdot = vdot(k->u, vsub(vpb, vpa));
+    double impulse = -k->dmass * (Cdot + J->bias + J->gamma * J->impulse[0]);
+    J->impulse[0] = J->impulse[0] + impulse;
+    v2 P = vscale(impulse, k->u);
+    va = vsub(va, vscale(ma, P));
+    wa = wa - ia * vcross(ra, P);
+    vb = vadd(vb, vscale(mb, P));
+    wb = wb + ib * vcross(rb, P);
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static int distance_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
+    if (J->frequency > 0.0) return 1;   /* soft constraints have no position correction */
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 u = vsub(vsub(vadd(cb, rb), ca), ra);
+    double length = vlen(u);
+    u = vnormalized(u);
+    double C = length - J->length;
+    double impulse = -k->dmass * cclamp(C, -OR_MAX_LINEAR_CORRECTION_J, OR_MAX_LINEAR_CORRECTION_J);
+    v2 P = vscale(impulse, u);
+    ca = vsub(ca, vscale(ma, P));
+    aa = aa - ia * vcross(ra, P);
+    cb = vadd(cb, vscale(mb, P));
+    ab = ab + ib * vcross(rb, P);
+    pc[k->ia] = ca; pa[k->ia] = aa;
+    pc[k->ib] = cb; pa[k->ib] = ab;
+    return fabs(C) < OR_LINEAR_SLOP_J;
+}
+
+/* ------------------------------------------------------------ weld */
+static void weld_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt_ratio,
+                      int warm) {
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    double aa = pa[k->ia], ab = pa[k->ib];
+    (void)pc;
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    v2 ra = k->ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    double c2x = -ra.y * ra.x * ia - rb.y * rb.x * ib;
+    double c3x = -ra.y * ia - rb.y * ib;
+    k->m.c1 = V3(ma + mb + ra.y * ra.y * ia + rb.y * rb.y * ib, c2x, c3x);
+    /* weld.py:163-165: the velocity mass keeps c3x in col2.z */
+    k->m.c2 = V3(c2x, ma + mb + ra.x * ra.x * ia + rb.x * rb.x * ib, c3x);
+    k->m.c3 = V3(c3x, ra.x * ia + rb.x * ib, ia + ib);
+    if (warm) {
+        J->impulse[0] = dt_ratio * J->impulse[0];
+        J->impulse[1] = dt_ratio * J->impulse[1];
+        J->impulse[2] = dt_ratio * J->impulse[2];
+        double ix = J->impulse[0], iy = J->impulse[1], iz = J->impulse[2];
+        v2 P = V(ix, iy);
+        va = vsub(va, vscale(ma, P));
+        wa = wa - ia * (vcross(ra, P) + iz);
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + ib * (vcross(rb, P) + iz);
+    } else {
+        J->impulse[0] = J->impulse[1] = J->impulse[2] = 0.0;
+    }
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void weld_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww) {
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    v2 ra = k->ra, rb = k->rb;
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 Cdot1 = vsub(vsub(vadd(vb, vcross_sv(wb, rb)), va), vcross_sv(wa, ra));
+    double Cdot2 = wb - wa;
+    v3 impulse = m33_solve3(k->m, v3neg(V3(Cdot1.x, Cdot1.y, Cdot2)));
+    J->impulse[0] = J->impulse[0] + impulse.x;
+    J->impulse[1] = J->impulse[1] + impulse.y;
+    J->impulse[2] = J->impulse[2] + impulse.z;
+    v2 P = V(impulse.x, impulse.y);
+    va = vsub(va, vscale(ma, P));
+    wa = wa - ia * (vcross(ra, P) + impulse.z);
+    vb = vadd(vb, vscale(mb, P));
+    wb = wb + ib * (vcross(rb, P) + impulse.z);
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static int weld_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 C1 = vsub(vsub(vadd(cb, rb), ca), ra);
+    double C2 = ab - aa - J->ref_angle;
+    double position_error = vlen(C1);
+    double angular_error = fabs(C2);
+    double c2x = -ra.y * ra.x * ia - rb.y * rb.x * ib;
+    double c3x = -ra.y * ia - rb.y * ib;
+    double c3y = ra.x * ia + rb.x * ib;
+    m33 mass;
+    mass.c1 = V3(ma + mb + ra.y * ra.y * ia + rb.y * rb.y * ib, c2x, c3x);
+    mass.c2 = V3(c2x, ma + mb + ra.x * ra.x * ia + rb.x * rb.x * ib, c3y);
+    mass.c3 = V3(-ra.y * ia - rb.y * ib, ra.x * ia + rb.x * ib, ia + ib);
+    v3 impulse = v3neg(m33_solve3(mass, V3(C1.x, C1.y, C2)));
+    v2 P = V(impulse.x, impulse.y);
+    ca = vsub(ca, vscale(ma, P));
+    aa = aa - ia * (vcross(ra, P) + impulse.z);
+    cb = vadd(cb, vscale(mb, P));
+    ab = ab + ib * (vcross(rb, P) + impulse.z);
+    pc[k->ia] = ca; pa[k->ia] = aa;
+    pc[k->ib] = cb; pa[k->ib] = ab;
+    return position_error <= OR_LINEAR_SLOP_J && angular_error <= OR_ANGULAR_SLOP;
+}
+
+/* ------------------------------------------------------------ dispatch */
+static void joint_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt,
+                       double dt_ratio, int warm) {
+    switch (J->type) {
+    case GB_JOINT_REVOLUTE: revolute_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
+    case GB_JOINT_PRISMATIC: prismatic_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
+    case GB_JOINT_DISTANCE: distance_init(J, k, pc, pa, vv, ww, dt, dt_ratio, warm); break;
+    default: weld_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
+    }
+}
+static void joint_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww, double dt) {
+    switch (J->type) {
+    case GB_JOINT_REVOLUTE: revolute_solve_velocity(J, k, vv, ww, dt); break;
+    case GB_JOINT_PRISMATIC: prismatic_solve_velocity(J, k, vv, ww, dt); break;
+    case GB_JOINT_DISTANCE: distance_solve_velocity(J, k, vv, ww); break;
+    default: weld_solve_velocity(J, k, vv, ww); break;
+    }
+}
+static int joint_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
+    switch (J->type) {
+    case GB_JOINT_REVOLUTE: return revolute_solve_position(J, k, pc, pa);
+    case GB_JOINT_PRISMATIC: return prismatic_solve_position(J, k, pc, pa);
+    case GB_JOINT_DISTANCE: return distance_solve_position(J, k, pc, pa);
+    default: return weld_solve_position(J, k, pc, pa);
+    }
+}
+
+#endif /* ORACLE_JOINTS_H */

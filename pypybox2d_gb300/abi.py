@@ -84,6 +84,20 @@ CONTACT = np.dtype([
     ("p_id", "<u4", (2,)),
 ], align=True)
 
+JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE, JOINT_WELD = 1, 2, 3, 4
+J_COLLIDE_CONNECTED, J_LIMIT, J_MOTOR = 1, 2, 4
+LIMIT_INACTIVE, LIMIT_LOWER, LIMIT_UPPER, LIMIT_EQUAL = 0, 1, 2, 3
+
+#: ``gb_joint``: a joint's definition and carried state (joints/joint.py and the four kinds)
+JOINT = np.dtype([
+    ("world", "<i4"), ("type", "<i4"), ("body_a", "<i4"), ("body_b", "<i4"), ("flags", "<u4"), ("limit_state", "<i4"),
+    ("la_x", "<f8"), ("la_y", "<f8"), ("lb_x", "<f8"), ("lb_y", "<f8"), ("ref_angle", "<f8"),
+    ("ax_x", "<f8"), ("ax_y", "<f8"), ("lower", "<f8"), ("upper", "<f8"), ("max_motor", "<f8"), ("motor_speed", "<f8"),
+    ("length", "<f8"), ("frequency", "<f8"), ("damping_ratio", "<f8"),
+    ("impulse", "<f8", (3,)), ("motor_impulse", "<f8"), ("gamma", "<f8"), ("bias", "<f8"),
+    ("ux", "<f8"), ("uy", "<f8"), ("perp_x", "<f8"), ("perp_y", "<f8"),
+], align=True)
+
 WORLD = np.dtype([
     ("body_start", "<i4"), ("body_count", "<i4"), ("fixture_start", "<i4"), ("fixture_count", "<i4"),
     ("contact_start", "<i4"), ("contact_count", "<i4"), ("contact_capacity", "<i4"), ("flags", "<u4"),
@@ -100,6 +114,7 @@ class Scene(ctypes.Structure):
         ("worlds", ctypes.c_void_p), ("bodies", ctypes.c_void_p),
         ("fixtures", ctypes.c_void_p), ("contacts", ctypes.c_void_p),
         ("n_moves", ctypes.c_int32), ("_pad0", ctypes.c_int32), ("moves", ctypes.c_void_p),
+        ("n_joints", ctypes.c_int32), ("_pad1", ctypes.c_int32), ("joints", ctypes.c_void_p),
     ]
 
 
@@ -137,9 +152,11 @@ LAUNCH_CONFIG_BYTES = 24
 
 
 def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,
-               contacts: np.ndarray | None = None, moves: np.ndarray | None = None) -> tuple[Scene, tuple]:
+               contacts: np.ndarray | None = None, moves: np.ndarray | None = None,
+               joints: np.ndarray | None = None) -> tuple[Scene, tuple]:
     """Pack contiguous record arrays into a ``gb_scene``; the returned tuple
-    keeps the arrays alive as long as the scene is used."""
+    keeps the arrays alive as long as the scene is used.  ``joints`` are
+    sorted by their ``world`` field (stable: each world keeps its order)."""
     worlds = np.ascontiguousarray(worlds, dtype=WORLD)
     bodies = np.ascontiguousarray(bodies, dtype=BODY)
     fixtures = np.ascontiguousarray(fixtures, dtype=FIXTURE)
@@ -158,7 +175,12 @@ def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,
     moves = np.ascontiguousarray(moves if moves is not None else np.zeros(0, np.int32), dtype=np.int32)
     s.n_moves = len(moves)
     s.moves = moves.ctypes.data if len(moves) else None
-    return s, (worlds, bodies, fixtures, contacts, moves)
+    joints = np.ascontiguousarray(joints if joints is not None else np.zeros(0, JOINT), dtype=JOINT)
+    if len(joints) and np.any(np.diff(joints["world"]) < 0):
+        joints = joints[np.argsort(joints["world"], kind="stable")]
+    s.n_joints = len(joints)
+    s.joints = joints.ctypes.data if len(joints) else None
+    return s, (worlds, bodies, fixtures, contacts, moves, joints)
 
 
 _PKG_DIR = os.path.dirname(os.path.abspath(__file__))
@@ -176,6 +198,7 @@ EXPORTED = (
     "gb_batch_ray_cast", "gb_batch_ray_cast_all", "gb_batch_query_aabb",
     "gb_batch_snapshot_bytes", "gb_batch_snapshot", "gb_batch_restore", "gb_batch_get_step_record",
     "gb_batch_set_wait_polls", "gb_batch_clear_status",
+    "gb_joint_size", "gb_batch_get_joint_order", "gb_batch_get_joints", "gb_batch_set_joints",
 )
 
 #: gb_step_opts.record_order bit that records contact events
@@ -252,6 +275,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_get_step_record.argtypes = [vp, i32, i32p, i32, i32p, vp]
     lib.gb_batch_set_wait_polls.argtypes = [vp, i32]
     lib.gb_batch_clear_status.argtypes = [vp, vp]
+    lib.gb_joint_size.argtypes = []
+    lib.gb_batch_get_joint_order.argtypes = [vp, i32, i32p, i32, i32p, vp]
+    lib.gb_batch_get_joints.argtypes = [vp, vp, i32, vp]
+    lib.gb_batch_set_joints.argtypes = [vp, vp, i32, vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

@@ -45,7 +45,7 @@ struct Arena {
     }
 };
 
-template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap) {
+template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap, int nj) {
     B.n_worlds = nw;
     B.n_bodies = nb;
     B.n_slots = ncap;
@@ -93,12 +93,24 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.toi_n = a.take<int>(1);
     B.g_scr = a.take<long long>(4 * (size_t)GB_GRID_MAX_CTAS + 8);
     B.g_sh = a.take<unsigned char>(GB_GRID_SHARED_BYTES);
+    B.n_joints = nj;
+    B.j = a.take<gb_joint>(nj);
+    B.b_joff = a.take<int>(nb + nw);
+    B.b_jadj = a.take<int>(2 * (size_t)nj);
+    B.s_jc = a.take<JCons>(nj);
+    B.s_jkj = a.take<int>(nj);
+    B.s_jkb = a.take<int2>(nj);
+    B.s_jcol = a.take<int>(nj);
+    B.s_jpref = a.take<int>(nj);
+    B.s_joff = a.take<int>(nj + nw);
+    B.s_jvis = a.take<unsigned char>(nj);
+    B.jorder_out = a.take<int>(nj);
 }
 // Re-points the per-step scratch arrays of a batch into one region laid out
 // by `a` (a.base == nullptr only measures it).  The state that outlives a step
 // stays in the batch arena: the pending move buffer (s_move, read by the
 // first step), the recorded solver order and the phase clocks.
-template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap) {
+template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap, int nj) {
     B.s_parent = a.take<int>(nb); B.s_wake = a.take<int>(nb); B.s_seed = a.take<int>(nb); B.s_stack = a.take<int>(nb);
     B.s_adjoff = a.take<int>(nb + nw);
     B.s_root = a.take<uint32_t>(nb);
@@ -119,13 +131,21 @@ template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
     B.toi_n = a.take<int>(1);
+    B.s_jc = a.take<JCons>(nj);
+    B.s_jkj = a.take<int>(nj);
+    B.s_jkb = a.take<int2>(nj);
+    B.s_jcol = a.take<int>(nj);
+    B.s_jpref = a.take<int>(nj);
+    B.s_joff = a.take<int>(nj + nw);
+    B.s_jvis = a.take<unsigned char>(nj);
 }
 }  // namespace
 
 struct gb_batch {
     int prec = GB_PREC_F64;
-    int nw = 0, nb = 0, nf = 0, ncap = 0;
+    int nw = 0, nb = 0, nf = 0, ncap = 0, nj = 0;
     std::vector<WorldHdr> hdr;     // host copy of the headers at creation
+    std::vector<gb_joint> joints;  // the joints at creation (world, type and bodies are fixed for the batch)
     std::vector<int> launch_order; // worlds sorted by body count, largest first
     char *arena = nullptr;
     size_t arena_bytes = 0;
@@ -178,6 +198,7 @@ extern "C" {
 
 const char *gb_version(void) { return "gb2d 0.1 sm_103a"; }
 const char *gb_last_error(void) { return g_err.c_str(); }
+int gb_joint_size(void) { return (int)sizeof(gb_joint); }
 
 int gb_struct_sizes(int32_t *sizes) {
     if (!sizes) return fail(GB_E_ARG, "sizes is NULL");
@@ -253,13 +274,33 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         cbase += cap;
     }
     b->ncap = cbase;
+    // joints: sorted by world, bodies inside their world, known kinds
+    if (scene->n_joints < 0 || (scene->n_joints > 0 && !scene->joints)) {
+        delete b;
+        return fail(GB_E_ARG, "bad joint array");
+    }
+    b->nj = scene->n_joints;
+    b->joints.assign(scene->joints, scene->joints + b->nj);
+    for (int i = 0; i < b->nj; ++i) {
+        const gb_joint &J = b->joints[i];
+        const bool ok = J.world >= 0 && J.world < b->nw && (i == 0 || J.world >= b->joints[i - 1].world) &&
+                        J.body_a >= 0 && J.body_a < b->hdr[J.world].nb && J.body_b >= 0 && J.body_b < b->hdr[J.world].nb &&
+                        J.body_a != J.body_b && J.type >= GB_JOINT_REVOLUTE && J.type <= GB_JOINT_WELD;
+        if (!ok) {
+            delete b;
+            return fail(J.type < GB_JOINT_REVOLUTE || J.type > GB_JOINT_WELD ? GB_E_UNSUPPORTED : GB_E_ARG,
+                        "joint " + std::to_string(i) + ": world out of order, body outside its world or unknown type");
+        }
+        if (b->hdr[J.world].nj == 0) b->hdr[J.world].jbase = i;
+        b->hdr[J.world].nj += 1;
+    }
     b->launch_order.resize(b->nw);
     for (int i = 0; i < b->nw; ++i) b->launch_order[i] = i;
     std::stable_sort(b->launch_order.begin(), b->launch_order.end(),
                      [&](int x, int y) { return b->hdr[x].nb > b->hdr[y].nb; });
     Arena a;
-    if (precision == GB_PREC_F64) carve(a, b->bd, b->nw, b->nb, b->nf, b->ncap);
-    else carve(a, b->bf, b->nw, b->nb, b->nf, b->ncap);
+    if (precision == GB_PREC_F64) carve(a, b->bd, b->nw, b->nb, b->nf, b->ncap, b->nj);
+    else carve(a, b->bf, b->nw, b->nb, b->nf, b->ncap, b->nj);
     size_t bytes = a.off + 256;
     cudaError_t e = cudaMalloc((void **)&b->arena, bytes);
     if (e != cudaSuccess) { delete b; return cuda_fail(e, "cudaMalloc(arena)"); }
@@ -267,8 +308,8 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
     CK(cudaMemset(b->arena, 0, bytes));
     Arena a2;
     a2.base = b->arena;
-    if (precision == GB_PREC_F64) carve(a2, b->bd, b->nw, b->nb, b->nf, b->ncap);
-    else carve(a2, b->bf, b->nw, b->nb, b->nf, b->ncap);
+    if (precision == GB_PREC_F64) carve(a2, b->bd, b->nw, b->nb, b->nf, b->ncap, b->nj);
+    else carve(a2, b->bf, b->nw, b->nb, b->nf, b->ncap, b->nj);
     {
         std::vector<int> bw(std::max(1, b->nb), 0), cw(std::max(1, b->ncap), 0);
         for (int i = 0; i < b->nw; ++i) {
@@ -303,6 +344,31 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
             if (b->hdr[i].nb >= GB_HUGE_BODIES && nh < GB_MAX_HUGE) { b->bd.huge_ids[nh] = b->bf.huge_ids[nh] = i; ++nh; }
             else break;
         b->bd.n_huge = b->bf.n_huge = nh;
+    }
+    if (b->nj > 0) {
+        // the joints and each body's joint list (Body.joints: World.joints order)
+        std::vector<int> joff((size_t)b->nb + b->nw, 0), jadj(2 * (size_t)b->nj, 0);
+        for (int w = 0; w < b->nw; ++w) {
+            const WorldHdr &h = b->hdr[w];
+            int *off = joff.data() + h.bbase + w;
+            for (int k = 0; k < h.nj; ++k) {
+                const gb_joint &J = b->joints[h.jbase + k];
+                off[J.body_a + 1] += 1;
+                off[J.body_b + 1] += 1;
+            }
+            for (int k = 0; k < h.nb; ++k) off[k + 1] += off[k];
+            std::vector<int> cur(off, off + h.nb);
+            int *adj = jadj.data() + 2 * (size_t)h.jbase;
+            for (int k = 0; k < h.nj; ++k) {
+                const gb_joint &J = b->joints[h.jbase + k];
+                adj[cur[J.body_a]++] = k;
+                adj[cur[J.body_b]++] = k;
+            }
+        }
+        const bool f64 = precision == GB_PREC_F64;
+        CK(cudaMemcpy(f64 ? b->bd.j : b->bf.j, b->joints.data(), sizeof(gb_joint) * b->nj, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(f64 ? b->bd.b_joff : b->bf.b_joff, joff.data(), sizeof(int) * joff.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(f64 ? b->bd.b_jadj : b->bf.b_jadj, jadj.data(), sizeof(int) * jadj.size(), cudaMemcpyHostToDevice));
     }
     CK(cudaMalloc((void **)&b->d_worlds, sizeof(int) * b->nw));
     CK(cudaMemcpy(b->d_worlds, b->launch_order.data(), sizeof(int) * b->nw, cudaMemcpyHostToDevice));
@@ -539,6 +605,47 @@ int gb_batch_get_solver_order(gb_batch *b, int32_t world, int32_t *order, int32_
     if (n > capacity) return fail(GB_E_ARG, "capacity too small");
     const int *src = (b->prec == GB_PREC_F64 ? b->bd.order_out : b->bf.order_out) + h[world].cbase;
     if (n > 0) CK(cudaMemcpyAsync(order, src, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_get_joint_order(gb_batch *b, int32_t world, int32_t *order, int32_t capacity, int32_t *n_out, void *stream) {
+    if (!b || !order || !n_out) return fail(GB_E_ARG, "NULL argument");
+    if (world < 0 || world >= b->nw) return fail(GB_E_ARG, "world out of range");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<WorldHdr> h;
+    int rc = read_headers(b, h, st);
+    if (rc) return rc;
+    const int n = h[world].nj > 0 ? h[world].last_njcons : 0;
+    *n_out = n;
+    if (n > capacity) return fail(GB_E_ARG, "capacity too small");
+    const int *src = (b->prec == GB_PREC_F64 ? b->bd.jorder_out : b->bf.jorder_out) + h[world].jbase;
+    if (n > 0) CK(cudaMemcpyAsync(order, src, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_get_joints(gb_batch *b, gb_joint *joints, int32_t n, void *stream) {
+    if (!b || (!joints && n > 0)) return fail(GB_E_ARG, "NULL argument");
+    if (n != b->nj) return fail(GB_E_ARG, "n_joints must equal the batch's joint count");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n > 0)
+        CK(cudaMemcpyAsync(joints, b->prec == GB_PREC_F64 ? b->bd.j : b->bf.j, sizeof(gb_joint) * n, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_set_joints(gb_batch *b, const gb_joint *joints, int32_t n, void *stream) {
+    if (!b || (!joints && n > 0)) return fail(GB_E_ARG, "NULL argument");
+    if (n != b->nj) return fail(GB_E_ARG, "n_joints must equal the batch's joint count");
+    for (int i = 0; i < n; ++i) {
+        const gb_joint &J = joints[i], &K = b->joints[i];
+        if (J.world != K.world || J.type != K.type || J.body_a != K.body_a || J.body_b != K.body_b)
+            return fail(GB_E_ARG, "joint " + std::to_string(i) + ": world, type and bodies are fixed for the batch");
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n > 0)
+        CK(cudaMemcpyAsync(b->prec == GB_PREC_F64 ? b->bd.j : b->bf.j, joints, sizeof(gb_joint) * n, cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
     return 0;
 }
@@ -1074,7 +1181,7 @@ template <class R> int step_static(gb_batch *b, const Batch<R> &arena_view, cons
                                    int threads, cudaStream_t st) {
     Batch<R> B = arena_view;
     Arena need;
-    carve_step_scratch(need, B, b->nw, b->nb, b->nf, b->ncap);
+    carve_step_scratch(need, B, b->nw, b->nb, b->nf, b->ncap, b->nj);
     if (need.off > (size_t)GB_STATIC_SCRATCH_BYTES)
         return fail(GB_E_SCRATCH, "batch needs " + std::to_string(need.off) + " bytes of step scratch; the static scratch holds " +
                                       std::to_string((size_t)GB_STATIC_SCRATCH_BYTES) + " (use gb_batch_step)");
@@ -1083,7 +1190,7 @@ template <class R> int step_static(gb_batch *b, const Batch<R> &arena_view, cons
     if (rc) return rc;
     Arena a;
     a.base = static_cast<char *>(base);
-    carve_step_scratch(a, B, b->nw, b->nb, b->nf, b->ncap);
+    carve_step_scratch(a, B, b->nw, b->nb, b->nf, b->ncap, b->nj);
     // every scratch array is written before it is read inside a step, except
     // the first-pass TOI list counter
     CK(cudaMemsetAsync(B.toi_n, 0, sizeof(int), st));

@@ -224,6 +224,7 @@ template <class R, int PH, class G> __device__ __forceinline__ void phase_body(c
             constraints_group(g, w, sp);
         } else if (g.rank() == 0) {
             H.last_ncons = 0;
+            H.last_njcons = 0;
         }
     } else if (PH == PH_SOLVE) {
         if (H.pflags & P_SOLVING) {

@@ -14,6 +14,7 @@
 #pragma once
 #include <type_traits>
 #include "gb_world.cuh"
+#include "gb_joints.cuh"
 #include "gb_tma.cuh"
 
 #define GB_MAX_TRANSLATION 2.0
@@ -37,6 +38,7 @@
 #define R_SOLVED 4u   // position_solved
 #define R_DFS 8u      // needs the depth-first body order
 #define R_STATIC_IN 16u  // (bodies) static body attached to a simulated island
+#define R_JBAD 32u    // a joint of the island is not yet within tolerance in this position iteration
 
 
 // Group-shared scratch scalars of one world.
@@ -109,8 +111,20 @@ template <class R> __device__ __forceinline__ bool default_filter(const WView<R>
     if (ga == gb && ga != 0) return ga > 0;
     return ((w.B.f_mask[w.fb + fa] & w.B.f_cat[w.fb + fb]) != 0) && ((w.B.f_cat[w.fb + fa] & w.B.f_mask[w.fb + fb]) != 0);
 }
+// body.py:912-927 _should_collide: one body dynamic, and no joint between
+// the two that turns collision off (the joint list of body ba)
 template <class R> __device__ __forceinline__ bool should_collide(const WView<R> &w, int ba, int bb) {
-    return w.btype(ba) == GB_BODY_DYNAMIC || w.btype(bb) == GB_BODY_DYNAMIC;
+    if (w.btype(ba) != GB_BODY_DYNAMIC && w.btype(bb) != GB_BODY_DYNAMIC) return false;
+    if (w.H->nj == 0) return true;
+    const int *off = w.B.b_joff + w.bb + w.wi;
+    const int *adj = w.B.b_jadj + 2 * (size_t)w.H->jbase;
+    const gb_joint *J = w.B.j + w.H->jbase;
+    for (int e = off[ba]; e < off[ba + 1]; ++e) {
+        const gb_joint &q = J[adj[e]];
+        if (((q.body_a == ba && q.body_b == bb) || (q.body_b == ba && q.body_a == bb)) && !(q.flags & GB_J_COLLIDE_CONNECTED))
+            return false;
+    }
+    return true;
 }
 template <class R> __device__ __forceinline__ bool fx_sensor(const WView<R> &w, int f) {
     return (w.B.f_flags[w.fb + f] & GB_FIX_SENSOR) != 0;
@@ -1005,9 +1019,37 @@ template <class R> __device__ void island_dfs(const WView<R> &w, int seed, int *
             stack[sp++] = other;
             bvis[other] = 1;
         }
+        // the body's joints, in its joint-list order (world.py:547-567)
+        if (w.H->nj > 0) {
+            const int *joff = w.B.b_joff + w.bb + w.wi;
+            const int *jadj = w.B.b_jadj + 2 * (size_t)w.H->jbase;
+            unsigned char *jvis = w.B.s_jvis + w.H->jbase;
+            const gb_joint *J = w.B.j + w.H->jbase;
+            for (int e = joff[b]; e < joff[b + 1]; ++e) {
+                const int j = jadj[e];
+                if (jvis[j]) continue;
+                const int other = J[j].body_a == b ? J[j].body_b : J[j].body_a;
+                if (!(w.B.b_flags[w.bb + other] & GB_BODY_ACTIVE)) continue;
+                jvis[j] = 1;
+                if (bvis[other]) continue;
+                stack[sp++] = other;
+                bvis[other] = 1;
+            }
+        }
     }
     *last = lb;
     *last_ns = lns;
+}
+
+// A joint of the world takes part in this step's solve: both bodies active
+// and a non-static one in a simulated island (world.py:547-567).
+template <class R> __device__ __forceinline__ bool joint_simulated(const WView<R> &w, const gb_joint &J, const int *parent,
+                                                                   const uint32_t *rootf) {
+    const uint32_t fa = w.B.b_flags[w.bb + J.body_a], fb = w.B.b_flags[w.bb + J.body_b];
+    if (!(fa & GB_BODY_ACTIVE) || !(fb & GB_BODY_ACTIVE)) return false;
+    const bool sa = w.btype(J.body_a) == GB_BODY_STATIC, sb = w.btype(J.body_b) == GB_BODY_STATIC;
+    if (sa && sb) return false;
+    return (rootf[parent[sa ? J.body_b : J.body_a]] & R_SIM) != 0;
 }
 
 // Island search by union-find (world.py:495-573 without the visit order):
@@ -1043,6 +1085,13 @@ template <class R, class G> __device__ void islands_group(const G &g, const WVie
         int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
         if (w.btype(ba) != GB_BODY_STATIC && w.btype(bb) != GB_BODY_STATIC) uf_union(parent, ba, bb);
     }
+    // joints link their bodies when both are active and neither is static
+    for (int j = g.rank(); j < w.H->nj; j += g.size()) {
+        const gb_joint &J = w.B.j[w.H->jbase + j];
+        const int ba = J.body_a, bb = J.body_b;
+        if (w.btype(ba) == GB_BODY_STATIC || w.btype(bb) == GB_BODY_STATIC) continue;
+        if ((w.B.b_flags[w.bb + ba] & GB_BODY_ACTIVE) && (w.B.b_flags[w.bb + bb] & GB_BODY_ACTIVE)) uf_union(parent, ba, bb);
+    }
     g.sync();
     for (int b = g.rank(); b < nb; b += g.size()) parent[b] = uf_find(parent, b);
     g.sync();
@@ -1058,6 +1107,88 @@ template <class R, class G> __device__ void islands_group(const G &g, const WVie
     all_allow = !g.any(!all_allow);
     if (g.rank() == 0) w.H->all_allow = all_allow ? 1 : 0;
     g.sync();
+}
+
+// Graph colouring of n constraints over their non-static bodies kb[k] (-1:
+// static): Jones-Plassmann rounds with fixed hash priorities; a constraint is
+// coloured when it holds the highest key on each of its non-static bodies,
+// with the lowest colour free on both (per-body masks of the colours taken
+// so far; beyond 64 colours, a colour of its own round).  Colour classes
+// share no non-static body, so each class is solved in parallel exactly as a
+// sequential pass would.  The colours in use are then numbered densely;
+// returns their number.  colour[k] must be -1 on entry.  *shared is a
+// group-shared int, tmp `cap` ints of scratch; more than cap - 1 colours
+// (never, while n < cap) flags GB_ST_ITER_LIMIT and leaves the constraints
+// beyond with colours >= the count returned.
+template <class R, class G> __device__ int jp_colour(const G &g, const WView<R> &w, int n, const int2 *kb, int *colour,
+                                                     int *shared, int *tmp, int cap) {
+    const int nb = w.H->nb;
+    unsigned long long *claim = w.B.s_claim + w.bb;
+    unsigned long long *used = w.B.s_minsep + w.bb;   // free until the position iterations
+    for (int b = g.rank(); b < nb; b += g.size()) used[b] = 0ull;
+    if (g.rank() == 0) *shared = 0;
+    for (int round = 0; round <= n; ++round) {   // >= 1 constraint is coloured per round
+        for (int b = g.rank(); b < nb; b += g.size()) claim[b] = 0ull;
+        g.sync();
+        bool left = false;
+        for (int k = g.rank(); k < n; k += g.size()) {
+            if (colour[k] >= 0) continue;
+            left = true;
+            int2 q = kb[k];
+            unsigned h = (unsigned)k * 2654435761u;
+            h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
+            unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
+            if (q.x >= 0) atomicMax(&claim[q.x], key);
+            if (q.y >= 0) atomicMax(&claim[q.y], key);
+        }
+        if (!g.any(left)) break;
+        for (int k = g.rank(); k < n; k += g.size()) {
+            if (colour[k] >= 0) continue;
+            int2 q = kb[k];
+            unsigned h = (unsigned)k * 2654435761u;
+            h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
+            unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
+            bool win = (q.x < 0 || claim[q.x] == key) && (q.y < 0 || claim[q.y] == key);
+            if (!win) continue;
+            // this round's winners share no body: their mask reads and writes do not race
+            unsigned long long taken = (q.x >= 0 ? used[q.x] : 0ull) | (q.y >= 0 ? used[q.y] : 0ull);
+            int c = __ffsll((long long)~taken) - 1;
+            if (c < 0) c = 64 + round;
+            else {
+                if (q.x >= 0) used[q.x] |= 1ull << c;
+                if (q.y >= 0) used[q.y] |= 1ull << c;
+            }
+            colour[k] = c;
+        }
+        g.sync();
+    }
+    // number the colours in use densely (masks leave no gaps below 64; the
+    // round colours above it may)
+    for (int k = g.rank(); k < n; k += g.size()) atomicMax(shared, colour[k] + 1);
+    g.sync();
+    int ncol = *shared;
+    if (ncol > 64) {
+        if (ncol + 1 > cap) {   // never index past the world's slots
+            if (g.rank() == 0) w.H->status |= GB_ST_ITER_LIMIT;
+            ncol = cap - 1;
+        }
+        for (int cc = g.rank(); cc < ncol; cc += g.size()) tmp[cc] = 0;
+        g.sync();
+        for (int k = g.rank(); k < n; k += g.size())
+            if (colour[k] >= 0 && colour[k] < ncol) tmp[colour[k]] = 1;
+        g.sync();
+        if (g.rank() == 0) {
+            int d = 0;
+            for (int cc = 0; cc < ncol; ++cc) { int u = tmp[cc]; tmp[cc] = d; d += u; }
+            *shared = d;
+        }
+        g.sync();
+        for (int k = g.rank(); k < n; k += g.size())
+            if (colour[k] >= 0 && colour[k] < ncol) colour[k] = tmp[colour[k]];
+        g.sync();
+        ncol = *shared;
+    }
+    return ncol;
 }
 
 // Constraint list of the simulated islands in contact-list order, graph
@@ -1104,79 +1235,8 @@ template <class R, class G> __device__ void constraints_group(const G &g, const 
         if (sb) wake_body(w, bb);
     }
     g.sync();
-    // 3. graph colouring: Jones-Plassmann rounds with fixed hash priorities;
-    //    a constraint is coloured when it holds the highest key on each of its
-    //    non-static bodies, with the lowest colour free on both (per-body
-    //    masks of the colours taken so far; beyond 64 colours, a colour of its
-    //    own round).  Colour classes share no non-static body, so each class
-    //    is solved in parallel exactly as a sequential pass would.
-    unsigned long long *used = w.B.s_minsep + w.bb;   // free until the position iterations
-    for (int b = g.rank(); b < nb; b += g.size()) used[b] = 0ull;
-    if (g.rank() == 0) w.H->last_ncolours = 0;
-    int maxc = -1;
-    for (int round = 0; round <= ncons; ++round) {   // >= 1 constraint is coloured per round
-        for (int b = g.rank(); b < nb; b += g.size()) claim[b] = 0ull;
-        g.sync();
-        bool left = false;
-        for (int k = g.rank(); k < ncons; k += g.size()) {
-            if (colour[k] >= 0) continue;
-            left = true;
-            int2 q = kb[k];
-            unsigned h = (unsigned)k * 2654435761u;
-            h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
-            unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
-            if (q.x >= 0) atomicMax(&claim[q.x], key);
-            if (q.y >= 0) atomicMax(&claim[q.y], key);
-        }
-        if (!g.any(left)) break;
-        for (int k = g.rank(); k < ncons; k += g.size()) {
-            if (colour[k] >= 0) continue;
-            int2 q = kb[k];
-            unsigned h = (unsigned)k * 2654435761u;
-            h ^= h >> 15; h *= 0x2c1b3c6du; h ^= h >> 12;
-            unsigned long long key = ((unsigned long long)h << 32) | (unsigned)(0x7fffffff - k);
-            bool win = (q.x < 0 || claim[q.x] == key) && (q.y < 0 || claim[q.y] == key);
-            if (!win) continue;
-            // this round's winners share no body: their mask reads and writes do not race
-            unsigned long long taken = (q.x >= 0 ? used[q.x] : 0ull) | (q.y >= 0 ? used[q.y] : 0ull);
-            int c = __ffsll((long long)~taken) - 1;
-            if (c < 0) c = 64 + round;
-            else {
-                if (q.x >= 0) used[q.x] |= 1ull << c;
-                if (q.y >= 0) used[q.y] |= 1ull << c;
-            }
-            colour[k] = c;
-            maxc = c > maxc ? c : maxc;
-        }
-        g.sync();
-    }
-    // number the colours in use densely (masks leave no gaps below 64; the
-    // round colours above it may)
-    for (int k = g.rank(); k < ncons; k += g.size()) atomicMax(&w.H->last_ncolours, colour[k] + 1);
-    g.sync();
-    int ncol = w.H->last_ncolours;
-    (void)maxc;
-    if (ncol > 64) {
-        if (ncol + 1 > w.H->ccap) {   // never index past the world's slots
-            if (g.rank() == 0) w.H->status |= GB_ST_ITER_LIMIT;
-            ncol = w.H->ccap - 1;
-        }
-        for (int cc = g.rank(); cc < ncol; cc += g.size()) pref[cc] = 0;
-        g.sync();
-        for (int k = g.rank(); k < ncons; k += g.size())
-            if (colour[k] >= 0 && colour[k] < ncol) pref[colour[k]] = 1;
-        g.sync();
-        if (g.rank() == 0) {
-            int d = 0;
-            for (int cc = 0; cc < ncol; ++cc) { int u = pref[cc]; pref[cc] = d; d += u; }
-            w.H->last_ncolours = d;
-        }
-        g.sync();
-        for (int k = g.rank(); k < ncons; k += g.size())
-            if (colour[k] >= 0 && colour[k] < ncol) colour[k] = pref[colour[k]];
-        g.sync();
-        ncol = w.H->last_ncolours;
-    }
+    // 3. graph colouring (jp_colour)
+    int ncol = jp_colour(g, w, ncons, kb, colour, &w.H->last_ncolours, pref, w.H->ccap);
     // The constraints are stored colour-major: constraint slots [coff[c],
     // coff[c+1]) hold colour c.  Positions inside a colour come from atomics:
     // a colour's constraints share no non-static body, so their order there
@@ -1209,6 +1269,62 @@ template <class R, class G> __device__ void constraints_group(const G &g, const 
         int *out = w.B.order_out + w.cb;
         for (int k = g.rank(); k < w.H->last_ncons; k += g.size()) out[k] = w.B.s_cp[w.cb + k].cidx;
     }
+    // 4. joints of the simulated islands (World.joints order), coloured and
+    //    laid out colour-major on their own: every velocity iteration solves
+    //    all joints before the contacts and every position iteration after
+    //    them (island.py:107-148)
+    const int nj = w.H->nj;
+    if (nj == 0) {
+        if (g.rank() == 0) { w.H->last_njcons = 0; w.H->last_njcolours = 0; }
+        g.sync();
+        return;
+    }
+    const int jb = w.H->jbase;
+    const gb_joint *J = w.B.j + jb;
+    int *jkj = w.B.s_jkj + jb;
+    int2 *jkb = w.B.s_jkb + jb;
+    int *jcol = w.B.s_jcol + jb;
+    int *jpref = w.B.s_jpref + jb;
+    int *joff = w.B.s_joff + jb + w.wi;   // nj + 1 slots
+    const int njc = group_scan(g, nj, [&](int j) { return joint_simulated(w, J[j], parent, rootf) ? 1 : 0; }, jpref);
+    g.sync();
+    for (int j = g.rank(); j < nj; j += g.size()) {
+        if (!joint_simulated(w, J[j], parent, rootf)) continue;
+        const int k = jpref[j];
+        const int ba = J[j].body_a, bb = J[j].body_b;
+        const bool sa = w.btype(ba) == GB_BODY_STATIC, sb = w.btype(bb) == GB_BODY_STATIC;
+        jkj[k] = j;
+        jkb[k] = make_int2(sa ? -1 : ba, sb ? -1 : bb);
+        jcol[k] = -1;
+        if (sa) wake_body(w, ba);   // the depth-first search wakes every body it reaches (world.py:520)
+        if (sb) wake_body(w, bb);
+    }
+    g.sync();
+    const int njcol = njc > 0 ? jp_colour(g, w, njc, jkb, jcol, &w.H->last_njcolours, joff, nj + 1) : 0;
+    for (int cc = g.rank(); cc <= njcol; cc += g.size()) joff[cc] = 0;
+    g.sync();
+    for (int k = g.rank(); k < njc; k += g.size())
+        if (jcol[k] >= 0 && jcol[k] < njcol) atomicAdd(&joff[jcol[k] + 1], 1);
+    g.sync();
+    if (g.rank() == 0)
+        for (int cc = 1; cc <= njcol; ++cc) joff[cc] += joff[cc - 1];
+    g.sync();
+    for (int cc = g.rank(); cc < njcol; cc += g.size()) jpref[cc] = joff[cc];
+    g.sync();
+    for (int k = g.rank(); k < njc; k += g.size()) {
+        if (jcol[k] < 0 || jcol[k] >= njcol) continue;
+        const int pos = atomicAdd(&jpref[jcol[k]], 1);
+        const int j = jkj[k];
+        JCons &q = w.B.s_jc[jb + pos];
+        q.j = j;
+        q.ia = J[j].body_a;
+        q.ib = J[j].body_b;
+        q.root = parent[w.btype(q.ia) == GB_BODY_STATIC ? q.ib : q.ia];
+    }
+    if (g.rank() == 0) { w.H->last_njcons = joff[njcol]; w.H->last_njcolours = njcol; }
+    g.sync();
+    if (sp.record_order)
+        for (int k = g.rank(); k < w.H->last_njcons; k += g.size()) w.B.jorder_out[jb + k] = w.B.s_jc[jb + k].j;
 }
 
 // island.py:71-95 for one body of a simulated island
@@ -1433,6 +1549,14 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     const int ncol = w.H->last_ncolours;
     const int ncons = w.H->last_ncons;
     const int rank = g.rank();
+    // joints: set up after the contacts' warm start, solved before the
+    // contacts in each velocity iteration and after them in each position
+    // iteration (island.py:107-148); worlds with joints in the solve take the
+    // plain passes (no constraint-chunk pipeline, float64 position cache)
+    const int njc = w.H->last_njcons, njcol = w.H->last_njcolours;
+    JCons *jc = w.B.s_jc + w.H->jbase;
+    const int *joff = w.B.s_joff + w.H->jbase + w.wi;
+    gb_joint *JJ = w.B.j + w.H->jbase;
     // 6. warm start and velocity iterations, colour by colour
     // body views: shared memory (world-local index) or the batch arrays
     const bool cached = cache.mem != nullptr;
@@ -1481,7 +1605,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     }
     auto is_static = [&](int b) { return stat_ii ? is_neg_zero(stat_ii[b]) : w.btype(b) == GB_BODY_STATIC; };
     bool failed = false;
-    if (pipe.nbuf > 0 && ncons > 0) {
+    if (pipe.nbuf > 0 && ncons > 0 && njc == 0) {
         int *tab = w.B.s_pref + w.cb + 1;   // chunk table (entry -1: its length)
         const int nch = chunk_table(g, coff, ncol, g.size(), tab, w.H->ccap - 1, &w.H->status);
         const int runs = sp.vel_iters + (warm ? 1 : 0);
@@ -1534,7 +1658,36 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             if (*pipe_fail) { failed = true; break; }
         }
     } else if (!failed) {
+        // one pass over the joints, colour by colour: 0 = set-up with warm
+        // start, 1 = velocity iteration
+        const double dt_ratio = w.H->inv_dt0 * dt;
+        auto joint_pass = [&](int what) {
+            for (int cc = 0; cc < njcol; ++cc) {
+                for (int k = joff[cc] + rank; k < joff[cc + 1]; k += g.size()) {
+                    JCons &q = jc[k];
+                    gb_joint &J = JJ[q.j];
+                    const int ia = q.ia, ib = q.ib;
+                    vec2<double> va = cvt<double>(vel[ia]), vb = cvt<double>(vel[ib]);
+                    double wa = (double)om[ia], wb = (double)om[ib];
+                    if (what == 0) {
+                        const int ga = w.bb + ia, gbb = w.bb + ib;
+                        q.lca = w.B.b_lc[ga]; q.lcb = w.B.b_lc[gbb];
+                        q.ma = (double)w.B.b_inv_mass[ga]; q.mb = (double)w.B.b_inv_mass[gbb];
+                        q.iA = (double)w.B.b_inv_I[ga]; q.iB = (double)w.B.b_inv_I[gbb];
+                        joint_init(J, q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], va, wa, vb, wb, dt, dt_ratio,
+                                   warm);
+                    } else {
+                        joint_velocity(J, q, va, wa, vb, wb, dt);
+                    }
+                    if (!is_static(ia)) { vel[ia] = cvt<R>(va); om[ia] = (R)wa; }
+                    if (!is_static(ib)) { vel[ib] = cvt<R>(vb); om[ib] = (R)wb; }
+                }
+                g.sync();
+            }
+        };
         for (int it = (warm ? -1 : 0); it < sp.vel_iters; ++it) {
+            if (it == 0 && njc > 0) joint_pass(0);
+            if (it >= 0 && njc > 0) joint_pass(1);
             for (int cc = 0; cc < ncol; ++cc) {
                 int s0 = coff[cc], s1 = coff[cc + 1];
                 for (int j = s0 + rank; j < s1; j += g.size()) {
@@ -1555,6 +1708,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
                 g.sync();
             }
         }
+        if (sp.vel_iters <= 0 && njc > 0) joint_pass(0);   // the set-up runs with no velocity iteration too
     }
     if (failed) {
         if (rank == 0) w.H->status |= GB_ST_WAIT_TIMEOUT;
@@ -1610,10 +1764,11 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
     // float32 batches with the body cache run the passes on float32 deltas
     // (solve_position_f32d): cf | dc | ar | da in the cache's 24 bytes a body
     constexpr bool F32D = std::is_same<R, float>::value;
+    const bool f32d = F32D && cached && njc == 0;   // joints take the float64 position cache
     vec2<float> *cf = nullptr, *dcv = nullptr;
     float *ar = nullptr, *dav = nullptr;
     if (cached) {
-        if constexpr (F32D) {
+        if (f32d) {
             unsigned char *m = cache.mem;
             cf = reinterpret_cast<vec2<float> *>(m);
             dcv = reinterpret_cast<vec2<float> *>(m + 8 * (size_t)nb);
@@ -1635,7 +1790,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         const int ia = rec.ia, ib = rec.ib;
         Cons<R> k = pos_cons(rec, invm[ia], invm[ib], invi[ia], invi[ib]);
         if constexpr (F32D) {
-            if (cached) {
+            if (f32d) {
                 vec2<float> dca = dcv[ia], dcb = dcv[ib];
                 float daa = dav[ia], dab = dav[ib];
                 const float ms = solve_position_f32d(k, cf[ia], ar[ia], dca, daa, cf[ib], ar[ib], dcb, dab, 0.0f);
@@ -1659,12 +1814,30 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         for (int b = rank; b < nb; b += g.size()) {
             if (parent[b] != b || !(rootf[b] & R_SIM) || (rootf[b] & R_DONE)) continue;
             if (w.btype(b) == GB_BODY_STATIC) continue;
-            if (dkey_inv(minsep[b]) >= -3.0 * GB_LINEAR_SLOP) rootf[b] |= R_DONE | R_SOLVED | ((uint32_t)(it + 1) << 8);
+            if (dkey_inv(minsep[b]) >= -3.0 * GB_LINEAR_SLOP && !(rootf[b] & R_JBAD))
+                rootf[b] |= R_DONE | R_SOLVED | ((uint32_t)(it + 1) << 8);
             else pending = true;
         }
         return g.any(pending);
     };
-    if (pipe.nbuf > 0 && ncons > 0 && sp.pos_iters > 0) {
+    // the joints' position pass after the contacts', colour by colour; a
+    // joint out of tolerance keeps its island iterating (island.py:145-153)
+    auto joint_pos_pass = [&]() {
+        for (int cc = 0; cc < njcol; ++cc) {
+            for (int k = joff[cc] + rank; k < joff[cc + 1]; k += g.size()) {
+                const JCons &q = jc[k];
+                if (rootf[q.root] & R_DONE) continue;
+                const int ia = q.ia, ib = q.ib;
+                vec2<double> ca = pc[ia], cb = pc[ib];
+                double aa = pa[ia], ab = pa[ib];
+                if (!joint_position(JJ[q.j], q, ca, aa, cb, ab)) atomicOr(&rootf[q.root], R_JBAD);
+                if (!is_static(ia)) { pc[ia] = ca; pa[ia] = aa; }
+                if (!is_static(ib)) { pc[ib] = cb; pa[ib] = ab; }
+            }
+            g.sync();
+        }
+    };
+    if (pipe.nbuf > 0 && ncons > 0 && sp.pos_iters > 0 && njc == 0) {
         int *tab = w.B.s_pref + w.cb + 1;
         const int nch = tab[-1];
         const int total = sp.pos_iters * nch;
@@ -1702,7 +1875,10 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
         }
     } else {
         for (int it = 0; it < sp.pos_iters; ++it) {
-            for (int b = rank; b < nb; b += g.size()) minsep[b] = dkey(0.0);
+            for (int b = rank; b < nb; b += g.size()) {
+                minsep[b] = dkey(0.0);
+                if (njc > 0 && parent[b] == b) rootf[b] &= ~R_JBAD;
+            }
             g.sync();
             for (int cc = 0; cc < ncol; ++cc) {
                 int s0 = coff[cc], s1 = coff[cc + 1];
@@ -1712,6 +1888,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
                 }
                 g.sync();
             }
+            if (njc > 0) joint_pos_pass();
             if (!pos_check(it)) break;
         }
     }
@@ -1725,7 +1902,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
             w.B.rec_island[w.bb + b] = parent[b];
         }
     if (cached) {
-        if constexpr (F32D) {
+        if (f32d) {
             for (int b = rank; b < nb; b += g.size()) {
                 const vec2<float> d = dcv[b];
                 const float e = dav[b];
@@ -1832,6 +2009,7 @@ template <class R, class G> __device__ void sleep_group(const G &g, const WView<
                 w.B.s_bvis[w.bb + b] = 0;
             }
             for (int i = g.rank(); i < nc; i += g.size()) w.B.s_cvis[w.cb + i] = 0;
+            for (int j = g.rank(); j < w.H->nj; j += g.size()) w.B.s_jvis[w.H->jbase + j] = 0;
             g.sync();
             if (g.rank() == 0) {
                 unsigned char *bvis = w.B.s_bvis + w.bb;

@@ -64,6 +64,22 @@ template <class R> struct __align__(16) ConsPos {
     R ra, rb;
 };
 
+// One joint's set-up for a step (float64 in both units): the attributes a
+// joint's _init_velocity_constraints leaves for the passes (pypybox2d/joints).
+struct d3 { double x, y, z; };
+struct m33d { d3 c1, c2, c3; };   // Mat33, column-major (common.py:533-612)
+struct __align__(16) JCons {
+    int j, ia, ib, root;        // world-local joint and bodies, island (union-find root)
+    double ma, mb, iA, iB;
+    vec2<double> lca, lcb, ra, rb;
+    m33d m;                     // revolute/weld _mass, prismatic _k
+    double motor_mass;
+    vec2<double> u;             // distance
+    double dmass;
+    vec2<double> axis, perp;    // prismatic
+    double s1, s2, a1, a2;
+};
+
 struct WorldHdr {              // per-world scalars (device)
     int nb, nf, nc, ccap;      // counts, contact capacity
     int bbase, fbase, cbase;   // batch bases
@@ -75,8 +91,11 @@ struct WorldHdr {              // per-world scalars (device)
     int nmove0;                // pending move buffer given at creation (in s_move)
     int all_allow;             // every body allows sleep (island.py:168 reads one body's flag)
     uint32_t pflags;           // phase flags of the current step (P_*)
-    int _pad;
+    int nj;                    // joints of the world
     unsigned long long toimin; // dkey of the earliest first-pass time of impact below 1 (~0: none)
+    int jbase;                 // batch index of its first joint
+    int last_njcons, last_njcolours;   // joint constraints and their colours in the current step
+    int _pad2;
 };
 
 #define GB_HUGE_BODIES 16384       // worlds this large run as one cooperative grid per phase
@@ -137,6 +156,19 @@ template <class R> struct Batch {
     int *rec_island;             // per body: its island in that step's solve (world-local union-find root, -1: none)
     gb_event *ev;                // contact events: 3 ccap + 64 per world, from 3 cbase + 64 world
     int *ev_n;                   // events recorded per world
+    // joints (float64 records in both units, batch order = world order, then World.joints order)
+    int n_joints;
+    gb_joint *j;
+    int *b_joff;                 // each body's joint list: world-local offsets, nb + 1 per world (from bbase + world)
+    int *b_jadj;                 // world-local joint indices of the lists (2 per joint, from 2 jbase)
+    JCons *s_jc;                 // the step's joint set-up, colour-major (per joint slot)
+    int *s_jkj;                  // joint of each joint constraint (constraint order = World.joints order)
+    int2 *s_jkb;                 // its non-static bodies (-1: static)
+    int *s_jcol;                 // its colour
+    int *s_jpref;                // scan / colour-compaction scratch (per joint slot)
+    int *s_joff;                 // colour offsets of the colour-major layout: nj + 1 per world (from jbase + world)
+    unsigned char *s_jvis;       // depth-first search marks (Joint._island_flag)
+    int *jorder_out;             // recorded joint order of the last record_order step (per joint slot)
     // worlds advanced by a cooperative grid (the first n_huge of the size-sorted list)
     int n_huge;
     int huge_ids[GB_MAX_HUGE];

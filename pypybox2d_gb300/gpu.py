@@ -17,11 +17,13 @@ from . import abi
 class GpuBatch:
     """A batch of independent worlds resident in device memory."""
 
-    def __init__(self, worlds, bodies, fixtures, contacts=None, precision: str = "f64", moves=None):
+    def __init__(self, worlds, bodies, fixtures, contacts=None, precision: str = "f64", moves=None, joints=None):
         self.lib = abi.load_library()
         self.prec = abi.PREC_F64 if precision in ("f64", "float64", abi.PREC_F64) else abi.PREC_F32
-        scene, keep = abi.make_scene(worlds, bodies, fixtures, contacts, moves)
+        scene, keep = abi.make_scene(worlds, bodies, fixtures, contacts, moves, joints)
         self.worlds, self.n_bodies, self.n_fixtures = keep[0], len(keep[1]), len(keep[2])
+        self.joint_worlds = keep[5]["world"].copy()
+        self.n_joints = len(keep[5])
         h = ctypes.c_void_p()
         abi.check(self.lib.gb_batch_create(ctypes.byref(scene), self.prec, ctypes.byref(h)))
         self.h = h
@@ -154,6 +156,27 @@ class GpuBatch:
         abi.check(self.lib.gb_batch_get_solver_order(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                                                      cap, ctypes.byref(n), None))
         return out[:n.value].copy()
+
+    def joint_order(self, world: int = 0) -> np.ndarray:
+        """World-local joint indices in the order the last record_order step
+        solved them (gb_batch_get_joint_order)."""
+        cap = self.n_joints + 1
+        out = np.zeros(cap, dtype=np.int32)
+        n = ctypes.c_int32()
+        abi.check(self.lib.gb_batch_get_joint_order(self.h, world, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                                    cap, ctypes.byref(n), None))
+        return out[:n.value].copy()
+
+    def joints(self, world: int | None = None) -> np.ndarray:
+        """The joints with their carried state (``abi.JOINT``; all, or one world's)."""
+        out = np.zeros(self.n_joints, dtype=abi.JOINT)
+        abi.check(self.lib.gb_batch_get_joints(self.h, out.ctypes.data, self.n_joints, None))
+        return out if world is None else out[out["world"] == world]
+
+    def set_joints(self, joints: np.ndarray) -> None:
+        """Overwrite every joint's definition and state (same worlds, kinds and bodies)."""
+        j = np.ascontiguousarray(joints, dtype=abi.JOINT)
+        abi.check(self.lib.gb_batch_set_joints(self.h, j.ctypes.data, len(j), None))
 
     def events(self, world: int = 0) -> np.ndarray:
         """Contact events of one world from the last step call made with

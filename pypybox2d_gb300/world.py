@@ -23,9 +23,15 @@ them (``gb_batch_create``) and from then on the device owns the state:
   move buffer; pair finding for them runs on the device at the start of the
   next step, as the reference's ``find_new_contacts`` would before it.
 
+Joints (revolute, prismatic, distance, weld: ``joints.py``) are records of
+the world solved by the same step; creating or destroying one is a
+structural change, and a joint setter edits the record and re-uploads the
+joints before the next step (``gb_batch_set_joints``).
+
 What the GPU step does not support raises instead of running elsewhere:
-loop shapes, joints, sub-stepping, custom contact filters and
-``pre_solve`` callbacks that run mid-step.
+loop shapes, the friction, gear, mouse, pulley, rope and wheel joints,
+controllers, sub-stepping, custom contact filters and ``pre_solve``
+callbacks that run mid-step.
 """
 from __future__ import annotations
 
@@ -34,6 +40,8 @@ import math
 import numpy as np
 
 from . import abi
+from . import joints as _joints
+from .joints import DistanceJoint, Joint, PrismaticJoint, RevoluteJoint, WeldJoint  # noqa: F401
 from .scenes import AABB_EXTENSION, SceneBuilder, _Body
 from .shapes import Circle, Edge, Loop, MassData, Polygon, Shape
 
@@ -410,6 +418,13 @@ class Body:
         return bool(self._rec()["flags"] & abi.BODY_ACTIVE)
 
     @property
+    def joints(self):
+        """Body.joints: the joints attached to this body, in creation order."""
+        if self._world is None:
+            return []
+        return [j for j in self._world._joints if j._body_a is self or j._body_b is self]
+
+    @property
     def fixed_rotation(self):
         return bool(self._rec()["flags"] & abi.BODY_FIXED_ROTATION)
 
@@ -780,8 +795,8 @@ class World:
     arithmetic for new bodies and fixtures."""
 
     def __init__(self, gravity=(0, -10), do_sleep=True, warm_starting=True, continuous_physics=True,
-                 sub_stepping=False, auto_clear_forces=True, contact_filter=None, precision="f64",
-                 contact_capacity=0):
+                 sub_stepping=False, auto_clear_forces=True, joint_destruction_listener=None,
+                 fixture_destruction_listener=None, contact_filter=None, precision="f64", contact_capacity=0):
         """world.py:64-91.  Beyond the reference: ``precision`` ("f64" or
         "f32") and ``contact_capacity``, the device contact slots of the
         world (0: 6 per fixture); a step that needs more raises
@@ -807,6 +822,11 @@ class World:
         self._locked = False
         self._inv_dt0 = 0.0
         self.contact_manager = ContactManager()
+        self._J = np.zeros(0, dtype=abi.JOINT)   # World.joints records (world field 0)
+        self._joints: list[Joint] = []
+        self._upload_joints = False
+        self.joint_destruction_listener = joint_destruction_listener
+        self.fixture_destruction_listener = fixture_destruction_listener
 
     # -- properties
     @property
@@ -956,9 +976,16 @@ class World:
         return self.create_body(body, type=Body.KINEMATIC, **kwargs)
 
     def destroy_body(self, body):
-        """world.py:235-270: the body, its fixtures and their contacts leave the world
-        (touching ones reported to end_contact, contact_manager.py:167-168)."""
+        """world.py:235-270: the body, its joints (body.py:313-320, each reported
+        to joint_destruction_listener), its contacts (touching ones reported to
+        end_contact, contact_manager.py:167-168) and its fixtures (each
+        reported to fixture_destruction_listener, body.py:330-333) leave the
+        world."""
         self._check_unlocked()
+        for j in list(body.joints):
+            if self.joint_destruction_listener is not None:
+                self.joint_destruction_listener(j)
+            self.destroy_joint(j)
         self._structural()
         bi = body._index
         B, F, C, M = self._B, self._F, self._C, self._M
@@ -969,6 +996,9 @@ class World:
                 if int(c["flags"]) & abi.C_TOUCHING:
                     self.contact_manager.end_contact(EventContact(self._fixture_at(int(c["fixture_a"])),
                                                                   self._fixture_at(int(c["fixture_b"])), False))
+        if self.fixture_destruction_listener is not None:
+            for f in list(body.fixtures):
+                self.fixture_destruction_listener(f)
         C = C[~(gone(C["fixture_a"]) | gone(C["fixture_b"]))].copy()
         for key in ("fixture_a", "fixture_b"):
             C[key] = np.where(C[key] >= f0 + nfix, C[key] - nfix, C[key])
@@ -979,6 +1009,8 @@ class World:
         B = np.delete(B, bi)
         B["fixture_start"] = np.where(B["fixture_start"] > f0, B["fixture_start"] - nfix, B["fixture_start"])
         self._B, self._F, self._C, self._M = B, F, C, M
+        for key in ("body_a", "body_b"):
+            self._J[key] = np.where(self._J[key] > bi, self._J[key] - 1, self._J[key])
         self._sb.bodies.pop(bi)
         self._sb.moves = [(b if b < bi else b - 1, k) for (b, k) in self._sb.moves if b != bi]
         self._bodies.pop(bi)
@@ -1026,13 +1058,78 @@ class World:
         made by create_*_body only."""
         raise NotImplementedError("add_body: create bodies with World.create_*_body")
 
-    def _unsupported(self, *args, **kwargs):
-        raise NotImplementedError("joints and controllers are not part of the GPU world step")
+    # -- joints (world.py:252-306, 823-902)
+    @property
+    def joints(self):
+        return list(self._joints)
 
-    add_joint = destroy_joint = _unsupported
-    create_distance_joint = create_friction_joint = create_gear_joint = _unsupported
-    create_mouse_joint = create_prismatic_joint = create_pulley_joint = _unsupported
-    create_revolute_joint = create_rope_joint = create_weld_joint = create_wheel_joint = _unsupported
+    @property
+    def joint_count(self):
+        return len(self._joints)
+
+    def add_joint(self, joint, duplicate=False):
+        """world.py:252-283.  Creating a joint does not wake its bodies; when
+        it turns collision off, the contacts between its bodies are flagged
+        for filtering."""
+        self._check_unlocked()
+        if duplicate:
+            raise NotImplementedError("add_joint(duplicate=True): create a second joint with the same arguments")
+        if not isinstance(joint, Joint) or type(joint) not in _joints.KINDS.values():
+            raise NotImplementedError(f"{type(joint).__name__} is not solved by the GPU world step")
+        if joint._world is not None:
+            raise ValueError("the joint already belongs to a world")
+        for b in joint.bodies:
+            if b is None or b._world is not self:
+                raise ValueError("Both bodies must be in the same world.")
+        self._structural()
+        r = joint._pending.copy()
+        r["world"] = 0
+        r["body_a"], r["body_b"] = joint._body_a._index, joint._body_b._index
+        self._J = np.concatenate([self._J, np.array([r], dtype=abi.JOINT)])
+        joint._world, joint._index = self, len(self._joints)
+        self._joints.append(joint)
+        if not int(r["flags"]) & abi.J_COLLIDE_CONNECTED:
+            self._flag_contacts_between(int(r["body_a"]), int(r["body_b"]))
+        return joint
+
+    def destroy_joint(self, joint):
+        """world.py:285-305: the bodies are woken; contacts between them are
+        flagged for filtering when the joint turned collision off."""
+        self._check_unlocked()
+        if joint._world is not self:
+            raise ValueError("Joint not in world")
+        self._structural()
+        for b in joint.bodies:
+            b.awake = True
+        i = joint._index
+        r = self._J[i].copy()
+        self._J = np.delete(self._J, i)
+        self._joints.pop(i)
+        for k, j in enumerate(self._joints):
+            j._index = k
+        joint._pending = r
+        joint._world, joint._index = None, -1
+        if not int(r["flags"]) & abi.J_COLLIDE_CONNECTED:
+            self._flag_contacts_between(int(r["body_a"]), int(r["body_b"]))
+
+    def create_revolute_joint(self, *args, **kwargs):
+        return self.add_joint(RevoluteJoint(*args, **kwargs))
+
+    def create_prismatic_joint(self, *args, **kwargs):
+        return self.add_joint(PrismaticJoint(*args, **kwargs))
+
+    def create_distance_joint(self, *args, **kwargs):
+        return self.add_joint(DistanceJoint(*args, **kwargs))
+
+    def create_weld_joint(self, *args, **kwargs):
+        return self.add_joint(WeldJoint(*args, **kwargs))
+
+    def _unsupported(self, *args, **kwargs):
+        raise NotImplementedError("friction, gear, mouse, pulley, rope and wheel joints and controllers are not "
+                                  "part of the GPU world step")
+
+    create_friction_joint = create_gear_joint = create_mouse_joint = _unsupported
+    create_pulley_joint = create_rope_joint = create_wheel_joint = _unsupported
     add_controller = destroy_controller = create_buoyancy_controller = create_gravity_controller = _unsupported
 
     # -- queries
@@ -1173,6 +1270,8 @@ class World:
         self._F["aabb"] = self._gpu.proxies()
         self._C = self._gpu.contacts(0)
         self._M = np.zeros(0, np.int32)
+        if len(self._J):
+            self._J = self._gpu.joints()
         self._host_fresh = True
 
     def _structural(self):
@@ -1196,6 +1295,21 @@ class World:
         if self._gpu is not None or self._owner is not None:
             self._upload_bodies = True
 
+    def _joint_record(self, i, write=False):
+        self._materialise()
+        if write and (self._gpu is not None or self._owner is not None):
+            self._upload_joints = True
+        return self._J[i]
+
+    def _flag_contacts_between(self, ba, bb):
+        """contact._flag_for_filtering of every contact between bodies ba and bb"""
+        if not len(self._C):
+            return
+        fb = self._F["body"]
+        a, b = fb[self._C["fixture_a"]], fb[self._C["fixture_b"]]
+        hit = ((a == ba) & (b == bb)) | ((a == bb) & (b == ba))
+        self._C["flags"] = np.where(hit, self._C["flags"] | abi.C_FILTER, self._C["flags"])
+
     def _query_gpu(self):
         """The device batch holding this world's current state, and the
         world's index in it."""
@@ -1214,17 +1328,23 @@ class World:
             W["contact_count"] = len(self._C)
             W["contact_capacity"] = self._contact_capacity
             W["inv_dt0"] = self._inv_dt0
-            self._gpu = self._make_batch(W, self._B, self._F, self._C, self._M)
+            self._gpu = self._make_batch(W, self._B, self._F, self._C, self._M, self._J)
             self._host_fresh = True
             self._upload_bodies = False
-        elif self._upload_bodies:
+            self._upload_joints = False
+            return
+        if self._upload_bodies:
             self._gpu.set_bodies(self._B)
             self._upload_bodies = False
+        if self._upload_joints:
+            self._gpu.set_joints(self._J)
+            self._upload_joints = False
 
-    def _make_batch(self, W, B, F, C, M):
+    def _make_batch(self, W, B, F, C, M, J=None):
         """The device batch holding this world (gb_batch_create)."""
         from .gpu import GpuBatch
-        return GpuBatch(W, B, F, contacts=C if len(C) else None, precision=self._precision, moves=M)
+        return GpuBatch(W, B, F, contacts=C if len(C) else None, precision=self._precision, moves=M,
+                        joints=J if J is not None and len(J) else None)
 
     def _add_fixture(self, body, fixture):
         """body.py:185-214: the fixture joins the body, its proxy the move
@@ -1494,18 +1614,22 @@ class WorldBatch:
             w._check_unlocked()
             if w._owner is not None:
                 raise ValueError("a world can belong to one WorldBatch at a time")
-        recs = []
-        for w in worlds:
+        recs, Js = [], []
+        for i, w in enumerate(worlds):
             w._materialise()
             W = w._sb.world_record(len(w._B), len(w._F), len(w._M))
             W["contact_count"] = len(w._C)
             W["contact_capacity"] = w._contact_capacity
             W["inv_dt0"] = w._inv_dt0
             recs.append((W, w._B, w._F, w._C, w._M))
+            J = w._J.copy()
+            J["world"] = i
+            Js.append(J)
         W, B, F, C, M = _concat_worlds(recs)
+        J = np.concatenate(Js)
         from .gpu import GpuBatch
         self._gpu = GpuBatch(W, B, F, contacts=C if len(C) else None, precision=precision or worlds[0]._precision,
-                             moves=M)
+                             moves=M, joints=J if len(J) else None)
         self._worlds = worlds
         self._index = {id(w): i for i, w in enumerate(worlds)}
         self._ranges = [(int(r["body_start"]), int(r["body_count"]), int(r["fixture_start"]), int(r["fixture_count"]))
@@ -1519,6 +1643,7 @@ class WorldBatch:
             w._owner = self
             w._host_fresh = True
             w._upload_bodies = False
+            w._upload_joints = False
 
     @property
     def worlds(self):
@@ -1607,20 +1732,35 @@ class WorldBatch:
         w._F["aabb"] = A[f0:f0 + nf]
         w._C = self._gpu.contacts(i)
         w._M = np.zeros(0, np.int32)
+        if len(w._J):
+            J = self._gpu.joints(i).copy()
+            J["world"] = 0
+            w._J = J
         w._host_fresh = True
 
     def _push_edits(self):
-        """Upload the bodies of the whole batch when a world's bodies were
-        edited on the host (velocities, forces, awake flags)."""
-        if not any(w._upload_bodies for w in self._worlds):
+        """Upload the bodies (joints) of the whole batch when a world's bodies
+        (joints) were edited on the host: velocities, forces, awake flags
+        (motor, limit and spring settings)."""
+        bodies = any(w._upload_bodies for w in self._worlds)
+        joints = any(w._upload_joints for w in self._worlds)
+        if not (bodies or joints):
             return
         for w in self._worlds:
             w._materialise()
-        B = np.concatenate([w._B for w in self._worlds])
-        self._gpu.set_bodies(B)
-        self._all = None
+        if bodies:
+            self._gpu.set_bodies(np.concatenate([w._B for w in self._worlds]))
+            self._all = None
+        if joints:
+            Js = []
+            for i, w in enumerate(self._worlds):
+                J = w._J.copy()
+                J["world"] = i
+                Js.append(J)
+            self._gpu.set_joints(np.concatenate(Js))
         for w in self._worlds:
             w._upload_bodies = False
+            w._upload_joints = False
 
     def _device_for(self, w):
         self._push_edits()

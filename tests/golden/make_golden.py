@@ -62,6 +62,15 @@ def fixture_index(world):
     return idx
 
 
+class OrderLog(list):
+    """Contact-list positions of the island contacts in solver order, and
+    (.joints) the World.joints positions of the island joints."""
+
+    def __init__(self):
+        super().__init__()
+        self.joints: list[int] = []
+
+
 def install_hooks(world, b2, order_log):
     fidx = fixture_index(world)
     bp = world.contact_manager.broadphase
@@ -92,6 +101,8 @@ def install_hooks(world, b2, order_log):
     def solve(self, step, gravity, allow_sleep):
         pos = {id(c): i for i, c in enumerate(world.contact_manager.contacts)}
         order_log.extend(pos[id(c)] for c in self.contacts)
+        jpos = {id(j): i for i, j in enumerate(world.joints)}
+        order_log.joints.extend(jpos[id(j)] for j in self.joints)
         return orig_solve(self, step, gravity, allow_sleep)
 
     island_mod.Island.solve = solve
@@ -214,6 +225,47 @@ def export_world(world, b2, contacts=True):
         wf |= abi.W_STEP_COMPLETE
     W[0] = (0, nb, 0, nf, 0, len(C), max(64, 8 * nf), wf, 0, 0, world._gravity.x, world._gravity.y, world._inv_dt0)
     return W, B, F, C
+
+
+def export_joints(world, b2):
+    """Reference World.joints -> gb_joint records (definition and carried state)."""
+    from pypybox2d import joints as jm
+    bidx = {id(b): i for i, b in enumerate(world.bodies)}
+    J = np.zeros(len(world.joints), dtype=abi.JOINT)
+    kinds = ((jm.RevoluteJoint, abi.JOINT_REVOLUTE), (jm.PrismaticJoint, abi.JOINT_PRISMATIC),
+             (jm.DistanceJoint, abi.JOINT_DISTANCE), (jm.WeldJoint, abi.JOINT_WELD))
+    for i, j in enumerate(world.joints):
+        r = J[i]
+        r["type"] = next(t for cls, t in kinds if type(j) is cls)
+        r["body_a"], r["body_b"] = bidx[id(j._body_a)], bidx[id(j._body_b)]
+        fl = abi.J_COLLIDE_CONNECTED if j._collide_connected else 0
+        if getattr(j, "_limit_enabled", False):
+            fl |= abi.J_LIMIT
+        if getattr(j, "_motor_enabled", False):
+            fl |= abi.J_MOTOR
+        r["flags"] = fl
+        r["la_x"], r["la_y"] = j._local_anchor_a.x, j._local_anchor_a.y
+        r["lb_x"], r["lb_y"] = j._local_anchor_b.x, j._local_anchor_b.y
+        if r["type"] == abi.JOINT_DISTANCE:
+            r["length"], r["frequency"], r["damping_ratio"] = j._length, j._frequency, j._damping_ratio
+            r["impulse"][0] = j._impulse
+            r["gamma"], r["bias"] = j._gamma, j._bias
+            r["ux"], r["uy"] = j._u.x, j._u.y
+            continue
+        r["ref_angle"] = j._reference_angle
+        r["impulse"][:] = (j._impulse.x, j._impulse.y, j._impulse.z)
+        if r["type"] == abi.JOINT_REVOLUTE:
+            r["lower"], r["upper"] = j._lower_angle, j._upper_angle
+            r["max_motor"], r["motor_speed"] = j._max_motor_torque, j._motor_speed
+            r["motor_impulse"], r["limit_state"] = j._motor_impulse, j._limit_state
+        elif r["type"] == abi.JOINT_PRISMATIC:
+            r["ax_x"], r["ax_y"] = j._local_x_axis.x, j._local_x_axis.y
+            r["lower"], r["upper"] = j._lower_limit, j._upper_limit
+            r["max_motor"], r["motor_speed"] = j._max_motor_force, j._motor_speed
+            r["motor_impulse"], r["limit_state"] = j._motor_impulse, j._limit_state
+            r["ux"], r["uy"] = j._axis.x, j._axis.y
+            r["perp_x"], r["perp_y"] = j._perp.x, j._perp.y
+    return J
 
 
 # ---------------------------------------------------------------- scenes
@@ -396,6 +448,99 @@ def scene_sensor_filter(b2, seed=13):
     return world
 
 
+def scene_joints(b2, seed=17):
+    """The four joint kinds of the island solver (island.py:107-148): a
+    revolute chain hanging from a static anchor (links collide with nothing
+    they are jointed to, body.py:912-927); a motorised revolute arm with an
+    angle limit and a revolute with equal limits; a prismatic lift with
+    limits and a motor, and a prismatic slider on a tilted unit axis (the
+    reference does not normalise the axis; a longer one makes its position
+    correction diverge); a rigid and a soft distance joint; a
+    cantilever of welded boxes; boxes and circles dropped onto all of it."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    ground = world.create_static_body(position=(0, -0.5), shapes=b2.Polygon(box=(30, 0.5)))
+    # revolute chain
+    anchor = world.create_static_body(position=(-12.0, 12.0), shapes=b2.Polygon(box=(0.3, 0.3)))
+    prev = anchor
+    for k in range(10):
+        link = world.create_dynamic_body(position=(-11.5 + 1.0 * k, 12.0))
+        link.create_polygon_fixture(box=(0.5, 0.125), density=20.0, friction=0.2)
+        world.create_revolute_joint(prev, link, anchor=(-12.0 + 1.0 * k, 12.0))
+        prev = link
+    # motorised arm with a limit, and an arm whose limits are equal
+    hub = world.create_static_body(position=(-4.0, 4.0), shapes=b2.Circle(radius=0.3))
+    arm = world.create_dynamic_body(position=(-2.5, 4.0))
+    arm.create_polygon_fixture(box=(1.5, 0.2), density=2.0, friction=0.5)
+    world.create_revolute_joint(hub, arm, anchor=(-4.0, 4.0), lower_angle=-0.6, upper_angle=0.9, limit_enabled=True,
+                                motor_speed=1.5, max_motor_torque=400.0, motor_enabled=True)
+    stiff = world.create_dynamic_body(position=(-4.0, 7.5), angle=0.3)
+    stiff.create_polygon_fixture(box=(1.0, 0.15), density=1.0, friction=0.5)
+    world.create_revolute_joint(hub, stiff, anchor=(-4.0, 7.0), lower_angle=0.3, upper_angle=0.3, limit_enabled=True)
+    # prismatic lift (vertical, limits and motor) carrying a box, and a slider
+    lift = world.create_dynamic_body(position=(2.0, 1.0))
+    lift.create_polygon_fixture(box=(1.0, 0.2), density=3.0, friction=0.7)
+    world.create_prismatic_joint(ground, lift, anchor=(2.0, 1.0), axis=(0.0, 1.0), lower_limit=0.0, upper_limit=3.0,
+                                 limit_enabled=True, motor_speed=1.0, max_motor_force=500.0, motor_enabled=True)
+    cargo = world.create_dynamic_body(position=(2.0, 1.8))
+    cargo.create_polygon_fixture(box=(0.4, 0.4), density=1.0, friction=0.7)
+    slider = world.create_dynamic_body(position=(6.0, 2.0), angle=0.1)
+    slider.create_polygon_fixture(box=(0.5, 0.3), density=1.0, friction=0.3)
+    world.create_prismatic_joint(ground, slider, anchor=(6.0, 2.0), axis=(0.8, 0.6), lower_limit=-1.0, upper_limit=1.5,
+                                 limit_enabled=True)
+    # distance joints: rigid pair and a soft spring to a static post
+    c1 = world.create_dynamic_body(position=(9.0, 5.0))
+    c1.create_circle_fixture(radius=0.4, density=1.0, friction=0.4)
+    c2 = world.create_dynamic_body(position=(10.5, 5.5))
+    c2.create_circle_fixture(radius=0.3, density=1.0, friction=0.4)
+    world.create_distance_joint(c1, c2, anchor_a=(9.0, 5.0), anchor_b=(10.5, 5.5))
+    post = world.create_static_body(position=(13.0, 8.0), shapes=b2.Polygon(box=(0.2, 0.2)))
+    bob = world.create_dynamic_body(position=(13.5, 5.0))
+    bob.create_polygon_fixture(box=(0.3, 0.3), density=2.0, friction=0.4)
+    world.create_distance_joint(post, bob, anchor_a=(13.0, 8.0), anchor_b=(13.5, 5.3), frequency=2.0, damping_ratio=0.3)
+    # welded cantilever
+    wall = world.create_static_body(position=(17.0, 3.0), shapes=b2.Polygon(box=(0.3, 3.0)))
+    prev = wall
+    for k in range(4):
+        seg = world.create_dynamic_body(position=(17.8 + 1.0 * k, 5.0))
+        seg.create_polygon_fixture(box=(0.5, 0.15), density=1.0, friction=0.6)
+        world.create_weld_joint(prev, seg, anchor=(17.3 + 1.0 * k, 5.0))
+        prev = seg
+    # things falling onto the joints
+    for k in range(8):
+        x = rng.uniform(-10.0, 20.0)
+        b = world.create_dynamic_body(position=(x, 9.0 + 1.5 * k), angle=rng.uniform(-1.0, 1.0))
+        if k % 2:
+            b.create_circle_fixture(radius=rng.uniform(0.25, 0.5), density=1.0, friction=0.5)
+        else:
+            b.create_polygon_fixture(box=(rng.uniform(0.2, 0.5), rng.uniform(0.2, 0.5)), density=1.0, friction=0.5)
+    return world
+
+
+def scene_bridge(b2, planks=30, seed=19):
+    """A suspension bridge: planks joined end to end by revolute joints and
+    pinned to the ground at both ends, with boxes and circles dropped on it
+    (the chains of joints stress the joint colouring)."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    ground = world.create_static_body(position=(0, 0), shapes=b2.Polygon(box=(40, 0.5)))
+    prev = ground
+    x0, y = -15.0, 5.0
+    for k in range(planks):
+        p = world.create_dynamic_body(position=(x0 + 0.5 + 1.0 * k, y))
+        p.create_polygon_fixture(box=(0.5, 0.125), density=20.0, friction=0.2)
+        world.create_revolute_joint(prev, p, anchor=(x0 + 1.0 * k, y))
+        prev = p
+    world.create_revolute_joint(prev, ground, anchor=(x0 + 1.0 * planks, y))
+    for k in range(12):
+        b = world.create_dynamic_body(position=(x0 + 2.0 + 2.2 * k, 8.0 + 0.5 * (k % 3)), angle=rng.uniform(-0.5, 0.5))
+        if k % 3 == 1:
+            b.create_circle_fixture(radius=0.45, density=1.0, friction=0.5)
+        else:
+            b.create_polygon_fixture(box=(0.4, 0.4), density=1.0, friction=0.5)
+    return world
+
+
 SCENES = {
     "pyramid": (scene_pyramid, 300, (1, 2, 3, 5, 10, 30, 31, 100, 101, 200, 201, 300)),
     "pyramid5": (lambda b2: scene_pyramid(b2, rows=5), 150, (1, 2, 5, 20, 21, 60, 61, 150)),
@@ -405,21 +550,26 @@ SCENES = {
     "uneven": (scene_uneven, 240, (1, 2, 5, 30, 31, 60, 61, 120, 121, 180, 240)),
     "kinematic": (scene_kinematic, 180, (1, 2, 5, 20, 21, 60, 61, 120, 121, 180)),
     "sensor_filter": (scene_sensor_filter, 150, (1, 2, 5, 20, 21, 40, 60, 61, 90, 120, 121, 150)),
+    "joints": (scene_joints, 300, (1, 2, 5, 20, 21, 60, 61, 120, 121, 200, 201, 300)),
+    "bridge": (scene_bridge, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
 }
 
 
 def run_scene(b2, name, builder, n_steps, snaps, vel_iters=8, pos_iters=3, dt=1.0 / 60):
     from pypybox2d import island as island_mod
     world = builder(b2)
-    order_log: list[int] = []
+    order_log = OrderLog()
     orig = install_hooks(world, b2, order_log)
     out = {}
     W, B, F, C = export_world(world, b2)
     out["init_world"], out["init_bodies"], out["init_fixtures"] = W, B, F
+    if world.joints:
+        out["init_joints"] = export_joints(world, b2)
     out["iters"] = np.array([vel_iters, pos_iters])
     try:
         for s in range(1, n_steps + 1):
             order_log.clear()
+            order_log.joints.clear()
             world.step(dt, vel_iters, pos_iters)
             if s in snaps:
                 W2, B2, F2, C2 = export_world(world, b2)
@@ -428,6 +578,9 @@ def run_scene(b2, name, builder, n_steps, snaps, vel_iters=8, pos_iters=3, dt=1.
                 out[f"s{s}_contacts"] = C2
                 out[f"s{s}_world"] = W2
                 out[f"s{s}_order"] = np.array(order_log, dtype=np.int32)
+                if world.joints:
+                    out[f"s{s}_joints"] = export_joints(world, b2)
+                    out[f"s{s}_jorder"] = np.array(order_log.joints, dtype=np.int32)
     finally:
         island_mod.Island.solve = orig
     out["snaps"] = np.array(sorted(snaps), dtype=np.int32)

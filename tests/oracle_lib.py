@@ -69,6 +69,18 @@ def load(libm: bool = False) -> ctypes.CDLL:
     lib.or_batch_step.restype = dbl
     lib.or_batch_get_bodies.argtypes = [vp, i32, vp]
     lib.or_batch_get_bodies.restype = i32
+    lib.or_set_joints.argtypes = [vp, vp, i32]
+    lib.or_set_joints.restype = i32
+    lib.or_flag_joint_contacts.argtypes = [vp, i32]
+    lib.or_flag_joint_contacts.restype = None
+    lib.or_joint_count.argtypes = [vp]
+    lib.or_joint_count.restype = i32
+    lib.or_get_joints.argtypes = [vp, vp]
+    lib.or_get_joints.restype = None
+    lib.or_set_joint_order.argtypes = [vp, vp, i32]
+    lib.or_set_joint_order.restype = None
+    lib.or_get_joint_order.argtypes = [vp, vp, i32]
+    lib.or_get_joint_order.restype = i32
     _libs[libm] = lib
     return lib
 
@@ -76,7 +88,7 @@ def load(libm: bool = False) -> ctypes.CDLL:
 class OracleWorld:
     """One world of the restatement, built from gb2d record arrays."""
 
-    def __init__(self, world, bodies, fixtures, contacts=None, libm=False, index=0, moves=None):
+    def __init__(self, world, bodies, fixtures, contacts=None, libm=False, index=0, moves=None, joints=None):
         self.lib = load(libm)
         self._keep = [np.ascontiguousarray(world, dtype=abi.WORLD),
                       np.ascontiguousarray(bodies, dtype=abi.BODY),
@@ -91,17 +103,38 @@ class OracleWorld:
                                     c.ctypes.data if len(c) else None, mv.ctypes.data if len(mv) else None)
         self.nb = int(wd["body_count"][0])
         self.nf = int(wd["fixture_count"][0])
+        if joints is not None and len(joints):
+            J = np.ascontiguousarray(joints, dtype=abi.JOINT)
+            J = np.ascontiguousarray(J[J["world"] == index])
+            if len(J):
+                assert self.lib.or_set_joints(self.h, J.ctypes.data, len(J)) == 0, "bad joint records"
 
     def __del__(self):
         if getattr(self, "h", None):
             self.lib.or_destroy(self.h)
             self.h = None
 
-    def step(self, dt, vel_iters=8, pos_iters=3, order=None):
+    def step(self, dt, vel_iters=8, pos_iters=3, order=None, joint_order=None):
         if order is not None:
             o = np.ascontiguousarray(order, dtype=np.int32)
             self.lib.or_set_solver_order(self.h, o.ctypes.data, len(o))
+        if joint_order is not None:
+            jo = np.ascontiguousarray(joint_order, dtype=np.int32)
+            self.lib.or_set_joint_order(self.h, jo.ctypes.data, len(jo))
         self.lib.or_step(self.h, dt, vel_iters, pos_iters)
+
+    def joints(self):
+        n = self.lib.or_joint_count(self.h)
+        out = np.zeros(n, dtype=abi.JOINT)
+        if n:
+            self.lib.or_get_joints(self.h, out.ctypes.data)
+        return out
+
+    def joint_order(self):
+        cap = self.lib.or_joint_count(self.h) + 1
+        out = np.zeros(cap, dtype=np.int32)
+        n = self.lib.or_get_joint_order(self.h, out.ctypes.data, cap)
+        return out[:n].copy()
 
     def bodies(self):
         out = np.zeros(self.nb, dtype=abi.BODY)
@@ -144,8 +177,8 @@ class OracleBatch:
     (step / bodies / set_bodies / proxies / contacts / status), so the
     World's host logic can be checked on the CPU.  Test infrastructure."""
 
-    def __init__(self, W, B, F, C, M, libm=False):
-        self.o = OracleWorld(W, B, F, C if len(C) else None, libm=libm, moves=M)
+    def __init__(self, W, B, F, C, M, libm=False, joints=None):
+        self.o = OracleWorld(W, B, F, C if len(C) else None, libm=libm, moves=M, joints=joints)
 
     def step(self, dt, vel_iters, pos_iters, n_steps=1, **_):
         for _ in range(n_steps):
@@ -171,6 +204,13 @@ class OracleBatch:
 
     def clear_status(self):
         self.o.lib.or_clear_status(self.o.h)
+
+    def joints(self, world=None):
+        return self.o.joints()
+
+    def set_joints(self, J):
+        J = np.ascontiguousarray(J, dtype=abi.JOINT)
+        assert self.o.lib.or_set_joints(self.o.h, J.ctypes.data, len(J)) == 0
 
     def close(self):
         pass

@@ -8,8 +8,12 @@ solver set-up decisions of each body) -- step after step, with the
 oracle solving each island in the GPU's graph-coloured constraint order
 (the solver-order hook).  The scenes are the reference-exported initial
 states of the golden vectors (pyramid, mixed edge/circle/polygon box,
-bullets with time-of-impact events, sleeping bodies, kinematic bodies, and
-sensors with group and category/mask filtering).
+bullets with time-of-impact events, sleeping bodies, kinematic bodies,
+sensors with group and category/mask filtering, and the four joint kinds:
+a scene of revolute, prismatic, distance and weld joints with limits and
+motors, and a 30-plank revolute bridge).  Joints are compared record for
+record (impulses, motor impulse, limit state, soft-constraint terms) with
+the oracle solving them in the GPU's joint colour order.
 """
 import os
 
@@ -23,7 +27,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 STEPS = {"pyramid": 40, "pyramid5": 150, "mixed": 120, "bullets": 60, "sleep": 90, "uneven": 240, "kinematic": 180,
-         "sensor_filter": 150}
+         "sensor_filter": 150, "joints": 300, "bridge": 240}
 
 
 def _gpu():
@@ -59,12 +63,15 @@ def run_lockstep(scene, steps, launch_mode=1, block_threads=0):
     dt = float(d["dt"][0])
     vi, pi = (int(x) for x in d["iters"])
     W, B, F = d["init_world"], d["init_bodies"], d["init_fixtures"]
-    gpu = GpuBatch(W, B, F, precision="f64")
-    orc = oracle_lib.OracleWorld(W, B, F, libm=False)
+    J = d["init_joints"] if "init_joints" in d.files else None
+    gpu = GpuBatch(W, B, F, precision="f64", joints=J)
+    orc = oracle_lib.OracleWorld(W, B, F, libm=False, joints=J)
     for s in range(1, steps + 1):
         gpu.step(dt, vi, pi, 1, launch_mode=launch_mode, block_threads=block_threads, record_order=True)
         order = gpu.solver_order(0)
-        orc.step(dt, vi, pi, order=order)
+        orc.step(dt, vi, pi, order=order, joint_order=gpu.joint_order(0) if J is not None else None)
+        if J is not None:
+            assert_same(gpu.joints(), orc.joints(), f"{scene} step {s} joints")
         assert_same(gpu.bodies(), orc.bodies(), f"{scene} step {s} bodies")
         assert np.array_equal(gpu.proxies(), orc.fixtures()["aabb"]), f"{scene} step {s} fat AABBs"
         assert_same(used_contact_view(gpu.contacts(0)), used_contact_view(orc.contacts()), f"{scene} step {s} contacts")

@@ -17,10 +17,14 @@ point of the same iteration, a difference of the solver's own residual.
    flags, manifold types, point counts, feature ids and awake flags too,
    except for DISCRETE_ONE_STEP contacts (one manifold type of the 20-row
    pyramid at step 100, a face pair on the knife edge of the reference's
-   face choice, collision.py); positions within ONE_STEP_TOL_M.  Measured:
-   at most 1.0e-2 m (that pyramid step: 590 contacts, 8 velocity
+   face choice, collision.py); positions within ONE_STEP_TOL_M, or
+   JOINT_ONE_STEP_TOL_M in the joint scenes.  Measured: at most 1.0e-2 m
+   among the contact scenes (that pyramid step: 590 contacts, 8 velocity
    iterations far from converged, so the order moves the result most),
-   below 2.5e-3 m in every other scene.
+   below 2.5e-3 m in every other one; 3.7e-2 m on the 30-plank bridge,
+   whose chain of revolute joints the GPU solves in colour order (every
+   other joint, then the rest) where the reference walks the chain, so
+   eight iterations carry an impulse along it differently.
 2. Free run from the initial state: the discrete state equal and positions
    within FREE_TOL_M at every snapshot up to the scene's FREE_HELD step
    (measured at most 3.1e-2 m, bullets at step 41).  After that the chaotic
@@ -37,12 +41,13 @@ from pypybox2d_gb300 import abi
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-SCENES = ("bullets", "kinematic", "mixed", "pyramid", "pyramid5", "sensor_filter", "sleep", "uneven")
+SCENES = ("bridge", "bullets", "joints", "kinematic", "mixed", "pyramid", "pyramid5", "sensor_filter", "sleep", "uneven")
 ONE_STEP_TOL_M = 2e-2
+JOINT_ONE_STEP_TOL_M = 5e-2
 FREE_TOL_M = 5e-2
 # scene -> last snapshot step at which the free run is held to the reference
 FREE_HELD = {"bullets": 41, "kinematic": 61, "mixed": 21, "pyramid": 10, "pyramid5": 5, "sensor_filter": 150,
-             "sleep": 90, "uneven": 61}
+             "sleep": 90, "uneven": 61, "joints": 21, "bridge": 21}
 # scene -> contacts allowed to differ in discrete fields after one step, over all its one-step states
 DISCRETE_ONE_STEP = {"pyramid": 1}
 
@@ -77,7 +82,8 @@ def _snapshot_batch(d, s):
     W["flags"] = W["flags"] & np.uint32(0xFFFFFFFF ^ abi.W_NEW_FIXTURE)
     F = d["init_fixtures"].copy()
     F["aabb"] = d[f"s{s}_aabb"]
-    return GpuBatch(W, d[f"s{s}_bodies"], F, contacts=C if len(C) else None, precision="f64")
+    J = d[f"s{s}_joints"] if f"s{s}_joints" in d.files else None
+    return GpuBatch(W, d[f"s{s}_bodies"], F, contacts=C if len(C) else None, precision="f64", joints=J)
 
 
 @pytest.mark.parametrize("scene", SCENES)
@@ -101,7 +107,8 @@ def test_one_step_from_reference_states(scene):
         apart += max(diffs.values(), default=0)
         worst = max(worst, dp)
     print(f"\n{scene} one step from the reference's states:\n  " + "\n  ".join(lines))
-    assert worst <= ONE_STEP_TOL_M, f"{scene}: {worst:.2e} m"
+    tol = JOINT_ONE_STEP_TOL_M if "init_joints" in d.files else ONE_STEP_TOL_M
+    assert worst <= tol, f"{scene}: {worst:.2e} m"
     assert apart <= DISCRETE_ONE_STEP.get(scene, 0), f"{scene}: {apart} contacts or bodies decided apart"
 
 
@@ -110,7 +117,8 @@ def test_free_run_against_the_reference(scene):
     from pypybox2d_gb300.gpu import GpuBatch
     d = np.load(os.path.join(GOLDEN, scene + ".npz"))
     dt, (vi, pi) = float(d["dt"][0]), (int(x) for x in d["iters"])
-    g = GpuBatch(d["init_world"], d["init_bodies"], d["init_fixtures"], precision="f64")
+    J = d["init_joints"] if "init_joints" in d.files else None
+    g = GpuBatch(d["init_world"], d["init_bodies"], d["init_fixtures"], precision="f64", joints=J)
     done, lines = 0, []
     for s in (int(x) for x in d["snaps"]):
         g.step(dt, vi, pi, s - done, launch_mode=3)

@@ -41,7 +41,8 @@ def test_oracle_matches_reference_bitwise(scene):
     d = np.load(os.path.join(GOLDEN, scene + ".npz"))
     dt = float(d["dt"][0])
     vi, pi = (int(x) for x in d["iters"])
-    w = oracle_lib.OracleWorld(d["init_world"], d["init_bodies"], d["init_fixtures"], libm=True)
+    joints = d["init_joints"] if "init_joints" in d.files else None
+    w = oracle_lib.OracleWorld(d["init_world"], d["init_bodies"], d["init_fixtures"], libm=True, joints=joints)
     snaps = [int(s) for s in d["snaps"]]
     for s in range(1, max(snaps) + 1):
         w.step(dt, vi, pi)
@@ -51,8 +52,11 @@ def test_oracle_matches_reference_bitwise(scene):
             assert_records_equal(w.contacts(), d[f"s{s}_contacts"], f"{scene} step {s} contacts")
             assert np.array_equal(w.solver_order(), d[f"s{s}_order"]), f"{scene} step {s} solver order"
             assert (w.lib.or_world_flags(w.h) & 0x3F) == (int(d[f"s{s}_world"]["flags"][0]) & 0x3F)
+            if joints is not None:
+                assert_records_equal(w.joints(), d[f"s{s}_joints"], f"{scene} step {s} joints")
+                assert np.array_equal(w.joint_order(), d[f"s{s}_jorder"]), f"{scene} step {s} joint order"
     assert w.status() == 0
 
 
 def test_golden_vectors_present():
-    assert {"pyramid", "mixed", "bullets", "sleep"} <= set(SCENES)
+    assert {"pyramid", "mixed", "bullets", "sleep", "joints", "bridge"} <= set(SCENES)
