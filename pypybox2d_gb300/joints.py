@@ -172,8 +172,8 @@ class RevoluteJoint(Joint):
 
     @property
     def joint_angle(self):
-        """body_b angle - body_a angle - reference angle"""
-        return self._body_b.angle - self._body_a.angle - self.reference_angle
+        """revolute.py:119-122: the sweep angles (not Body.angle)"""
+        return self._body_b._rec()["a"] - self._body_a._rec()["a"] - self.reference_angle
 
     @property
     def joint_speed(self):
@@ -244,6 +244,12 @@ class RevoluteJoint(Joint):
 
     def get_motor_torque(self, inv_dt):
         return inv_dt * float(self._rec()["motor_impulse"])
+
+    def get_reaction_force(self, inv_dt):
+        """revolute.py:206-208 slices the Vec3 impulse (`_impulse[:2]`), which
+        Vec3.__getitem__ refuses (common.py:303-311): the reference raises
+        IndexError here, and so does this getter."""
+        raise IndexError("Index must be in (0,1,2)")
 
 
 class PrismaticJoint(Joint):

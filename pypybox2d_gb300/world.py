@@ -256,11 +256,16 @@ class Body:
 
     @position.setter
     def position(self, pos):
-        self.transform = (pos, self.angle)
+        """body.py:420-423: a new origin, the rotation kept"""
+        self._world._check_unlocked()
+        self._world._set_transform(self._index, (float(pos[0]), float(pos[1])), None)
 
     @property
     def angle(self):
-        return float(self._rec()["a"])
+        """body.py:426-428: the transform's angle, atan2 of its rotation
+        (transform.c Transform_get_angle), not the sweep angle"""
+        r = self._rec()
+        return math.atan2(float(r["qs"]), float(r["qc"]))
 
     @angle.setter
     def angle(self, angle):
@@ -1467,12 +1472,15 @@ class World:
             f._slot = j
 
     def _set_transform(self, bi, pos, angle):
-        """body.py:_transform_updated: new transform and sweep; the fixtures
-        are synchronised with zero displacement (fixture.py:287-298,
-        dynamictree.py:152-188) and re-fattened ones enter the move buffer."""
+        """body.py:404-413 _transform_updated: new transform (angle None: the
+        rotation kept) and sweep, whose angle is the transform's atan2
+        (transform.c Transform_get_angle); the fixtures are synchronised with
+        zero displacement (fixture.py:287-298, dynamictree.py:152-188) and
+        re-fattened ones enter the move buffer."""
         self._structural()
         r = self._B[bi]
-        q = (math.cos(angle), math.sin(angle))
+        q = (math.cos(angle), math.sin(angle)) if angle is not None else (float(r["qc"]), float(r["qs"]))
+        angle = math.atan2(q[1], q[0])
         r["px"], r["py"], r["qc"], r["qs"] = pos[0], pos[1], q[0], q[1]
         lcx, lcy = float(r["lcx"]), float(r["lcy"])
         cx = pos[0] + q[0] * lcx + (-q[1]) * lcy

@@ -649,6 +649,27 @@ def run_api_script(b2):
     print(f"api_script: {(len(out) - 1) // 3} snapshots, {len(out['events'])} events -> {os.path.getsize(path)} bytes")
 
 
+def run_api_joints(b2):
+    """tests/golden/api_joints.py on the reference -> api_joints.npz."""
+    sys.path.insert(0, HERE)
+    import api_joints
+    out = {}
+
+    def snap(label, world):
+        W, B, F, C = export_world(world, b2)
+        out[f"{label}_bodies"], out[f"{label}_aabb"], out[f"{label}_contacts"] = B, F["aabb"].copy(), C
+        out[f"{label}_joints"] = export_joints(world, b2)
+        out[f"{label}_getters"] = np.array([api_joints.getter_row(j) for j in world.joints], dtype=np.float64)
+
+    log = []
+    api_joints.script(b2, snap, on_world=pair_order_hook, log=log)
+    out["destroyed"] = np.array(log)
+    path = os.path.join(HERE, "api_joints.npz")
+    np.savez_compressed(path, **out)
+    print(f"api_joints: {len(api_joints.SNAPS)} snapshots, joints destroyed with bodies: {log} -> "
+          f"{os.path.getsize(path)} bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("GB2D_REFERENCE"), required="GB2D_REFERENCE" not in os.environ,
@@ -662,6 +683,8 @@ def main():
         run_scene(b2, name, builder, n, snaps)
     if not args.only or args.only == "api_script":
         run_api_script(b2)
+    if not args.only or args.only == "api_joints":
+        run_api_joints(b2)
 
 
 if __name__ == "__main__":
