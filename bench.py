@@ -228,12 +228,36 @@ def pairs_bytes_per_step(fixtures, n_bodies, n_contacts):
     return 64.0 * n_bodies + float(np.sum(shape + 32 + 32 + 8)) + 8.0 * n_contacts
 
 
-def launches_per_step(W, big_bodies: int = 512):
-    """Kernel launches of one phased step: 12, plus a second solver launch
-    when the batch mixes worlds below and above the wide launch's threshold
-    (big_bodies)."""
-    nbig = int(np.count_nonzero(W["body_count"] >= big_bodies))
-    return 12 + (1 if 0 < nbig < len(W) else 0)
+def group_ranges(counts, n: int):
+    """The library's world groups (gb_launch_config.groups): n runs of
+    consecutive worlds of about equal body counts, as [w0, w1) ranges."""
+    nw = len(counts)
+    n = min(n, nw)
+    if n < 2:
+        return [(0, nw)]
+    total, w, acc, out = int(np.sum(counts)), 0, 0, []
+    for k in range(n):
+        w0, target, last = w, total * (k + 1) // n, nw - (n - 1 - k)
+        while True:
+            acc += int(counts[w])
+            w += 1
+            if not (w < last and acc < target):
+                break
+        if k == n - 1:
+            w = nw
+        out.append((w0, w))
+    return out
+
+
+def launches_per_step(W, big_bodies: int = 512, groups: int = 1):
+    """Kernel launches of one phased step: 12 per world group, plus a second
+    solver launch in each group that mixes worlds below and above the wide
+    launch's threshold (big_bodies)."""
+    n = 0
+    for w0, w1 in group_ranges(W["body_count"], groups):
+        nbig = int(np.count_nonzero(W["body_count"][w0:w1] >= big_bodies))
+        n += 12 + (1 if 0 < nbig < w1 - w0 else 0)
+    return n
 
 
 def cpu_oracle_rate(W, B, F, C, dyn, steps, threads, target_s=8.0):
@@ -384,8 +408,8 @@ def main():
     ap.add_argument("--drift-steps", type=int, default=-1, help="steps of the drift leg (-1: 1000, pyramid 2000; 0: skip)")
     ap.add_argument("--no-tune", action="store_true", help="skip the launch autotuner (use --mode / --threads)")
     ap.add_argument("--tune-steps", type=int, default=3, help="timed steps per autotuner trial")
-    ap.add_argument("--launch-config", default="", help="mode,threads,pipe_bufs,big_bodies: pin this launch "
-                                                         "configuration instead of tuning")
+    ap.add_argument("--launch-config", default="", help="mode,threads,pipe_bufs,big_bodies[,groups]: pin this "
+                                                         "launch configuration instead of tuning")
     ap.add_argument("--graph-steps", type=int, default=50, help="steps per captured CUDA graph in the timed region "
                                                                 "(0 = one gb_batch_step call)")
     args = ap.parse_args()
@@ -444,13 +468,13 @@ def main():
             mode, threads = 0, 0          # steps take the tuned launch configuration
             tune = {"best": best, "trials": len(trials), "steps_per_trial": args.tune_steps,
                     "seconds": round(time.time() - t0, 2),
-                    "table": [[t["launch_mode"], t["block_threads"], t["pipe_bufs"], t["big_bodies"],
+                    "table": [[t["launch_mode"], t["block_threads"], t["pipe_bufs"], t["big_bodies"], t["groups"],
                                round(t["ms_per_step"], 3)] for t in trials],
-                    "columns": ["launch_mode", "block_threads", "pipe_bufs", "big_bodies", "ms_per_step"]}
+                    "columns": ["launch_mode", "block_threads", "pipe_bufs", "big_bodies", "groups", "ms_per_step"]}
     tuned = tune is not None and "best" in tune
     cfg = batch.launch_config() if (tuned or args.launch_config) else {"launch_mode": args.mode,
                                                                       "block_threads": args.threads,
-                                                                      "pipe_bufs": 2, "big_bodies": 512}
+                                                                      "pipe_bufs": 2, "big_bodies": 512, "groups": 1}
     eff_mode = cfg["launch_mode"]
 
     # the timed steps: captured rollouts of graph_steps phased steps replayed
@@ -580,13 +604,15 @@ def main():
         "launch": {"launch_config": cfg,
                    "form": {1: "one persistent launch per timed region, one CTA per world",
                             2: "one persistent launch per timed region, one warp per world",
-                            3: f"{launches_per_step(W, cfg['big_bodies'])} launches per step (batch-wide + per-world)"
+                            3: f"{launches_per_step(W, cfg['big_bodies'], cfg['groups'])} launches per step (batch-wide + "
+                               f"per-world" + (f"; {cfg['groups']} world groups on streams of their own" if cfg['groups'] > 1
+                                                else "") + ")"
                             + (f", captured as CUDA graphs of {graph.n_steps} steps" if graph else "")}[eff_mode],
                    "arena_gib": round(batch.arena_bytes() / 2**30, 2),
                    "mean_contacts_per_world": float(np.mean(counts))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_kind": peak_kind,
-                     "kernel": f"whole step ({launches_per_step(W, cfg['big_bodies'])} launches)",
+                     "kernel": f"whole step ({launches_per_step(W, cfg['big_bodies'], cfg['groups'])} launches)",
                      "algorithmic_bytes_per_step": bytes_step,
                      "traffic_note": "DRAM bytes are measured by ncu on a smaller case and kept in profiles/, "
                                      "not read into this line"},
@@ -594,7 +620,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY.itemsize,
                 "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": e2e_steps,
                 "window": "the first steps of the timed window, restored from its snapshot"},
-        "gpu_launches": launches_per_step(W, cfg["big_bodies"]) * steps if eff_mode == 3 else 1,
+        "gpu_launches": launches_per_step(W, cfg["big_bodies"], cfg["groups"]) * steps if eff_mode == 3 else 1,
         "autotune": tune,
         "graph": graph_info,
         "clocks": clocks.summary(),

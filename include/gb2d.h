@@ -371,8 +371,8 @@ int gb_batch_get_events(gb_batch *batch, int32_t world, gb_event *out, int32_t c
  * the same results as long as each world's solver keeps its shared-memory
  * body cache (worlds of up to 2048 bodies); launch modes 1 and 2 and uncached
  * worlds round differently, within the float32 step error.  A batch starts
- * with {3, 128, 2, 512}.  No counterpart in the reference (one CPython world
- * has no launch geometry). */
+ * with {3, 128, 2, 512, 1}.  No counterpart in the reference (one CPython
+ * world has no launch geometry). */
 typedef struct gb_launch_config {
     int32_t launch_mode;    /* 1 = one CTA per world, 2 = one warp per world, 3 = phased */
     int32_t block_threads;  /* CTA width: mode 1 the world's CTA, mode 2 warps per CTA x 32, mode 3 the
@@ -380,9 +380,14 @@ typedef struct gb_launch_config {
     int32_t pipe_bufs;      /* mode 3 solver: constraint-chunk buffers in shared memory, 0..4
                                (0: records read from global memory) */
     int32_t big_bodies;     /* mode 3 solver: worlds of this many bodies or more get the wide launch */
+    int32_t groups;         /* mode 3: world groups, 1..8 -- runs of consecutive worlds of about equal body
+                               counts, each stepped on a stream of its own so one group's latency-bound
+                               phases (the TOI event loop of its largest worlds) overlap the others' work;
+                               1 for batches with worlds of 16384 bodies or more */
+    int32_t _pad0;
     double ms_per_step;     /* autotune output (device ms per step); ignored on input */
 } gb_launch_config;
-#define GB_LAUNCH_CONFIG_BYTES 24
+#define GB_LAUNCH_CONFIG_BYTES 32
 /* Set the configuration that steps with launch_mode 0 use (and pipe_bufs /
  * big_bodies for every phased step).  The batch state is not touched. */
 int gb_batch_set_launch_config(gb_batch *batch, const gb_launch_config *cfg);
@@ -395,7 +400,8 @@ int gb_batch_get_launch_config(gb_batch *batch, gb_launch_config *cfg);
  * (1) mapping: phased with 32/64/128 threads, one CTA per world with 128/256
  * threads, one warp per world with 2/4 warps per CTA (phased only for
  * batches with cooperative-grid worlds); (2) big_bodies 256/512/1024/2048/
- * none; (3) pipe_bufs 0-4.  Each trial's steps are timed with CUDA events on
+ * none; (3) pipe_bufs 0-4; (4) world groups 1/2/3/4 (phased, without
+ * cooperative-grid worlds).  Each trial's steps are timed with CUDA events on
  * `cuda_stream`.  trials[] receives every trial in order (ms_per_step -1:
  * not runnable, e.g. too much shared memory; -2: its steps raised a status
  * bit, e.g. a copy wait that gave up, and it is not a candidate); the best

@@ -132,11 +132,13 @@ class LaunchConfig(ctypes.Structure):
     _fields_ = [
         ("launch_mode", ctypes.c_int32), ("block_threads", ctypes.c_int32),
         ("pipe_bufs", ctypes.c_int32), ("big_bodies", ctypes.c_int32),
+        ("groups", ctypes.c_int32), ("_pad0", ctypes.c_int32),
         ("ms_per_step", ctypes.c_double),
     ]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if not k.startswith("_")}
+
 
 
 #: gb_ray, gb_ray_hit, gb_aabb_query (world queries)
@@ -148,7 +150,7 @@ AABB_QUERY = np.dtype([("world", "<i4"), ("_pad0", "<i4"), ("lx", "<f8"), ("ly",
                       align=True)
 
 #: sizeof(gb_launch_config) (GB_LAUNCH_CONFIG_BYTES)
-LAUNCH_CONFIG_BYTES = 24
+LAUNCH_CONFIG_BYTES = 32
 
 
 def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,

@@ -90,7 +90,7 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.prof = a.take<long long>((size_t)nw * GB_NPROF);
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
-    B.toi_n = a.take<int>(1);
+    B.toi_n = a.take<int>(GB_MAX_GROUPS);
     B.g_scr = a.take<long long>(4 * (size_t)GB_GRID_MAX_CTAS + 8);
     B.g_sh = a.take<unsigned char>(GB_GRID_SHARED_BYTES);
     B.n_joints = nj;
@@ -130,7 +130,7 @@ template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb
     B.s_hash = a.take<unsigned long long>(4 * (size_t)ncap);
     B.s_plan = a.take<TPlan>((size_t)nw * GB_TOI_PLAN_CAP);
     B.toi_list = a.take<int>(ncap);
-    B.toi_n = a.take<int>(1);
+    B.toi_n = a.take<int>(GB_MAX_GROUPS);
     B.s_jc = a.take<JCons>(nj);
     B.s_jkj = a.take<int>(nj);
     B.s_jkb = a.take<int2>(nj);
@@ -140,6 +140,18 @@ template <class R> void carve_step_scratch(Arena &a, Batch<R> &B, int nw, int nb
     B.s_jvis = a.take<unsigned char>(nj);
 }
 }  // namespace
+
+// A world group: a run of consecutive worlds stepped on a stream of its own
+// (gb_launch_config.groups), so that the latency-bound tail of one group's
+// per-world phases overlaps the other groups' kernels.
+struct WorldGroup {
+    int w0 = 0, w1 = 0;              // worlds [w0, w1)
+    int b0 = 0, nb = 0, s0 = 0, ns = 0;   // their bodies and contact slots
+    int *d_worlds = nullptr;         // their list, largest first (device)
+    int n_list = 0, nbig = 0;        // list length, worlds of the wide solver launch
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
+};
 
 struct gb_batch {
     int prec = GB_PREC_F64;
@@ -161,11 +173,18 @@ struct gb_batch {
     int *d_ev_n = nullptr;
     SideStream side{};               // the solver's second stream (gb_launch.h)
     bool has_side = false;
-    gb_launch_config cfg{3, 128, GB_SOLVE_PIPE_BUFS, GB_SOLVE_BIG_BODIES, 0.0};   // launch_mode 0 steps
+    gb_launch_config cfg{3, 128, GB_SOLVE_PIPE_BUFS, GB_SOLVE_BIG_BODIES, 1, 0, 0.0};   // launch_mode 0 steps
+    std::vector<WorldGroup> groups;  // world groups of cfg.groups > 1
+    cudaEvent_t fork = nullptr;      // the caller's stream -> the groups' streams
     std::vector<gb_graph *> graphs;  // captured rollouts, disarmed when the batch is destroyed
     char *d_query = nullptr;         // staging of query inputs and outputs, grown on demand
     size_t query_bytes = 0;
 };
+
+namespace {
+template <class R> int run_steps(gb_batch *b, const Batch<R> &B, const StepParams &sp, int n_steps, int mode, int threads,
+                                 cudaStream_t st, KernelTimer *kt);
+}
 
 // A captured rollout (gb_graph_capture).  `b` is null once its batch is gone.
 struct gb_graph {
@@ -462,6 +481,12 @@ int gb_batch_destroy(gb_batch *b) {
     cudaFree(b->d_ev);
     cudaFree(b->d_ev_n);
     cudaFree(b->d_query);
+    for (WorldGroup &g : b->groups) {
+        cudaFree(g.d_worlds);
+        if (g.done) cudaEventDestroy(g.done);
+        if (g.st) cudaStreamDestroy(g.st);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->has_side) {
         cudaEventDestroy(b->side.fork);
         cudaEventDestroy(b->side.join);
@@ -502,10 +527,8 @@ int gb_batch_step(gb_batch *b, const gb_step_opts *o, void *stream) {
         }
         kt = b->ktimer;
     }
-    int rc = b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st, kt,
-                                                             b->has_side ? &b->side : nullptr)
-                                    : gb_launch_step<float>(b->bf, sp, o->n_steps, b->d_worlds, b->nw, mode, threads, st, kt,
-                                                            b->has_side ? &b->side : nullptr);
+    int rc = b->prec == GB_PREC_F64 ? run_steps<double>(b, b->bd, sp, o->n_steps, mode, threads, st, kt)
+                                    : run_steps<float>(b, b->bf, sp, o->n_steps, mode, threads, st, kt);
     if (rc) return cuda_fail((cudaError_t)rc, "step launch");
     b->counters[0] += 1;
     b->counters[2] += o->n_steps;
@@ -757,10 +780,77 @@ StepParams params_of(const gb_step_opts *o) {
     return sp;
 }
 
+// n_steps steps of every world on `st`: one launch sequence over the whole
+// batch, or (phased launch, world groups) one per group, each on the group's
+// stream, forked from and joined back into `st` (also under stream capture).
+template <class R> int run_steps(gb_batch *b, const Batch<R> &B, const StepParams &sp, int n_steps, int mode, int threads,
+                                 cudaStream_t st, KernelTimer *kt) {
+    if (mode != 3 || kt || b->groups.size() < 2) {
+        const SideStream *side = b->has_side ? &b->side : nullptr;
+        return gb_launch_step<R>(B, sp, n_steps, b->d_worlds, b->nw, mode, threads, st, kt, side);
+    }
+    cudaError_t e = cudaEventRecord(b->fork, st);
+    for (size_t k = 0; k < b->groups.size() && e == cudaSuccess; ++k) {
+        const WorldGroup &g = b->groups[k];
+        e = cudaStreamWaitEvent(g.st, b->fork, 0);
+        if (e != cudaSuccess) break;
+        Batch<R> G = B;
+        G.n_bodies = g.nb; G.body0 = g.b0;
+        G.n_slots = g.ns; G.slot0 = g.s0;
+        G.toi_n = B.toi_n + k;
+        G.n_big = g.nbig;
+        G.n_huge = 0;
+        const int rc = gb_launch_step<R>(G, sp, n_steps, g.d_worlds, g.n_list, mode, threads, g.st, nullptr, nullptr);
+        if (rc) return rc;
+        e = cudaEventRecord(g.done, g.st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, g.done, 0);
+    }
+    return (int)e;
+}
+
 int launch_steps(gb_batch *b, const StepParams &sp, int n_steps, int mode, int threads, cudaStream_t st) {
-    const SideStream *side = b->has_side ? &b->side : nullptr;
-    return b->prec == GB_PREC_F64 ? gb_launch_step<double>(b->bd, sp, n_steps, b->d_worlds, b->nw, mode, threads, st, nullptr, side)
-                                  : gb_launch_step<float>(b->bf, sp, n_steps, b->d_worlds, b->nw, mode, threads, st, nullptr, side);
+    return b->prec == GB_PREC_F64 ? run_steps<double>(b, b->bd, sp, n_steps, mode, threads, st, nullptr)
+                                  : run_steps<float>(b, b->bf, sp, n_steps, mode, threads, st, nullptr);
+}
+
+// Split the worlds into n runs of about equal body counts (n = 1: none).
+int make_groups(gb_batch *b, int n, int big_from) {
+    for (WorldGroup &g : b->groups) {
+        cudaFree(g.d_worlds);
+        if (g.done) cudaEventDestroy(g.done);
+        if (g.st) cudaStreamDestroy(g.st);
+    }
+    b->groups.clear();
+    n = std::min(n, b->nw);
+    if (n < 2) return 0;
+    if (!b->fork) CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    long long total = 0;
+    for (int i = 0; i < b->nw; ++i) total += b->hdr[i].nb;
+    int w = 0;
+    long long acc = 0;
+    for (int k = 0; k < n; ++k) {
+        WorldGroup g;
+        g.w0 = w;
+        const long long target = total * (k + 1) / n;
+        const int last = b->nw - (n - 1 - k);   // leave a world for each later group
+        do { acc += b->hdr[w].nb; ++w; } while (w < last && acc < target);
+        if (k == n - 1) w = b->nw;
+        g.w1 = w;
+        const WorldHdr &f = b->hdr[g.w0], &l = b->hdr[g.w1 - 1];
+        g.b0 = f.bbase; g.nb = l.bbase + l.nb - f.bbase;
+        g.s0 = f.cbase; g.ns = l.cbase + l.ccap - f.cbase;
+        std::vector<int> list;
+        for (int i : b->launch_order)
+            if (i >= g.w0 && i < g.w1) list.push_back(i);
+        g.n_list = (int)list.size();
+        for (int i : list) g.nbig += b->hdr[i].nb >= big_from ? 1 : 0;
+        CK(cudaMalloc((void **)&g.d_worlds, sizeof(int) * list.size()));
+        CK(cudaMemcpy(g.d_worlds, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
+        CK(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+        b->groups.push_back(g);
+    }
+    return 0;
 }
 
 bool has_grid_worlds(const gb_batch *b) { return (b->prec == GB_PREC_F64 ? b->bd.n_huge : b->bf.n_huge) > 0; }
@@ -775,6 +865,9 @@ int apply_config(gb_batch *b, const gb_launch_config &c, bool apply) {
         return fail(GB_E_ARG, "block_threads must be a multiple of 32 from 32 to 1024");
     if (c.pipe_bufs < 0 || c.pipe_bufs > GB_CFG_MAX_PIPE_BUFS) return fail(GB_E_ARG, "pipe_bufs must be 0 to 4");
     if (c.big_bodies < 1) return fail(GB_E_ARG, "big_bodies must be positive");
+    if (c.groups < 1 || c.groups > GB_MAX_GROUPS) return fail(GB_E_ARG, "groups must be 1 to 8");
+    if (c.groups > 1 && (c.launch_mode != 3 || has_grid_worlds(b)))
+        return fail(GB_E_UNSUPPORTED, "world groups run the phased launch (mode 3) of batches without cooperative-grid worlds");
     if (c.launch_mode != 3 && has_grid_worlds(b))
         return fail(GB_E_UNSUPPORTED, "worlds of 16384 bodies or more run only in the phased launch (mode 3)");
     // worlds run as a cooperative grid (the front of the list) always count
@@ -803,6 +896,8 @@ int apply_config(gb_batch *b, const gb_launch_config &c, bool apply) {
                                       std::to_string(optin));
     }
     if (!apply) return 0;
+    const int grc = make_groups(b, c.groups, big_from);
+    if (grc) return grc;
     for (Batch<double> *B : {&b->bd}) { B->n_big = nbig; B->cache_big = cache_big; B->cache_small = cache_small; B->pipe_bufs = c.pipe_bufs; }
     for (Batch<float> *B : {&b->bf}) { B->n_big = nbig; B->cache_big = cache_big; B->cache_small = cache_small; B->pipe_bufs = c.pipe_bufs; }
     b->cfg = c;
@@ -890,6 +985,7 @@ int gb_batch_autotune(gb_batch *b, const gb_step_opts *o, gb_launch_config *tria
             gb_launch_config c = start;
             c.launch_mode = m.first;
             c.block_threads = m.second;
+            if (c.launch_mode != 3) c.groups = 1;
             trial(c);
         }
     }
@@ -903,6 +999,12 @@ int gb_batch_autotune(gb_batch *b, const gb_step_opts *o, gb_launch_config *tria
         const gb_launch_config base = best_c;
         for (int pb = 0; pb <= GB_CFG_MAX_PIPE_BUFS; ++pb)
             if (pb != base.pipe_bufs) { gb_launch_config c = base; c.pipe_bufs = pb; trial(c); }
+    }
+    // stage 4 (phased launch without cooperative-grid worlds): world groups
+    if (!err && best_c.ms_per_step >= 0.0 && best_c.launch_mode == 3 && !has_grid_worlds(b)) {
+        const gb_launch_config base = best_c;
+        for (int ng : {1, 2, 3, 4})
+            if (ng != base.groups && ng <= b->nw) { gb_launch_config c = base; c.groups = ng; trial(c); }
     }
     // the best configuration stays; the state goes back to the saved one
     const bool found = !err && best_c.ms_per_step >= 0.0;
@@ -1193,8 +1295,8 @@ template <class R> int step_static(gb_batch *b, const Batch<R> &arena_view, cons
     carve_step_scratch(a, B, b->nw, b->nb, b->nf, b->ncap, b->nj);
     // every scratch array is written before it is read inside a step, except
     // the first-pass TOI list counter
-    CK(cudaMemsetAsync(B.toi_n, 0, sizeof(int), st));
-    rc = gb_launch_step<R>(B, sp, n_steps, b->d_worlds, b->nw, mode, threads, st, nullptr, b->has_side ? &b->side : nullptr);
+    CK(cudaMemsetAsync(B.toi_n, 0, sizeof(int) * GB_MAX_GROUPS, st));
+    rc = run_steps<R>(b, B, sp, n_steps, mode, threads, st, nullptr);
     if (rc) return cuda_fail((cudaError_t)rc, "step launch (static scratch)");
     return 0;
 }

@@ -40,6 +40,7 @@ template <class R> __global__ void k_pre(Batch<R> B, int n_bodies, StepParams sp
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b == 0) *B.toi_n = 0;
     if (b >= n_bodies) return;
+    b += B.body0;
     const WorldHdr *H = &B.hdr[B.b_world[b]];
     uint32_t f = B.b_flags[b];
     B.s_wake[b] = ((f & GB_BODY_AWAKE) && B.b_type[b] != GB_BODY_STATIC) ? -1 : GB_INF_IDX;
@@ -51,6 +52,7 @@ template <class R> __global__ void k_pre(Batch<R> B, int n_bodies, StepParams sp
 template <class R, bool EV> __global__ void k_collide(Batch<R> B, int n_slots, StepParams sp) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n_slots) return;
+    s += B.slot0;
     int wi = B.c_world[s];
     WView<R> w = view_global(B, wi);
     int i = s - w.cb;
@@ -73,6 +75,7 @@ template <class R, bool EV> __global__ void k_collide(Batch<R> B, int n_slots, S
 template <class R> __global__ void k_vinit(Batch<R> B, int n_bodies, StepParams sp) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= n_bodies) return;
+    b += B.body0;
     WView<R> w = view_global(B, B.b_world[b]);
     if (!(w.H->pflags & P_SOLVING)) return;
     integrate_velocity_body(w, b - w.bb, sp.dt);
@@ -86,6 +89,7 @@ template <class R> __global__ void k_vinit(Batch<R> B, int n_bodies, StepParams 
 template <class R> __global__ void k_cinit(Batch<R> B, int n_slots, StepParams sp) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n_slots) return;
+    s += B.slot0;
     WView<R> w = view_global(B, B.c_world[s]);
     int k = s - w.cb;
     if (!(w.H->pflags & P_SOLVING) || k >= w.H->last_ncons) return;
@@ -102,6 +106,7 @@ template <class R> __global__ void k_cinit(Batch<R> B, int n_slots, StepParams s
 template <class R> __global__ void k_toi1(Batch<R> B, int n_slots, StepParams sp) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n_slots) return;
+    s += B.slot0;
     WView<R> w = view_global(B, B.c_world[s]);
     int i = s - w.cb;
     if (i >= w.H->nc) return;
@@ -121,7 +126,7 @@ template <class R> __global__ void k_toi1(Batch<R> B, int n_slots, StepParams sp
     toi_reset_contact(w, i);
     int st = toi_status(w, i);
     B.s_proc[s] = st != 0 ? 1 : 0;
-    if (st == 2) B.toi_list[atomicAdd(B.toi_n, 1)] = s;
+    if (st == 2) B.toi_list[B.slot0 + atomicAdd(B.toi_n, 1)] = s;   // the group's part of the list
 }
 
 // First TOI pass, part 2: the float64 times of impact of the listed
@@ -129,7 +134,7 @@ template <class R> __global__ void k_toi1(Batch<R> B, int n_slots, StepParams sp
 template <class R> __global__ void k_toi1b(Batch<R> B) {
     const int n = *B.toi_n;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        int s = B.toi_list[t];
+        int s = B.toi_list[B.slot0 + t];
         WView<R> w = view_global(B, B.c_world[s]);
         int i = s - w.cb;
         const ContactRec<R> &c = w.con(i);

@@ -106,6 +106,10 @@ struct WorldHdr {              // per-world scalars (device)
 
 template <class R> struct Batch {
     int n_worlds, n_bodies, n_slots;
+    // the bodies [body0, body0 + n_bodies) and contact slots [slot0, slot0 +
+    // n_slots) the batch-wide kernels of a launch cover: the whole batch, or
+    // one world group (a run of worlds stepped on a stream of its own)
+    int body0, slot0;
     int cache_bodies;         // worlds of at most this many bodies are solved from shared memory
     int pipe_bufs;            // solver: constraint chunk buffers in shared memory (0: read global memory)
     int n_big;                // worlds solved by the wide launch (the first n_big of the size-sorted list)
@@ -151,7 +155,7 @@ template <class R> struct Batch {
     long long *prof;             // per-world phase clocks (GB_NPROF per world), when profiling
     struct TPlan *s_plan;        // GB_TOI_PLAN_CAP planned TOI sweeps per world
     int *toi_list;               // contact slots needing a first-pass TOI (batch-wide)
-    int *toi_n;                  // their count
+    int *toi_n;                  // their count (one counter per world group)
     int *rec;                    // per body: the step record of the last record_order step
     int *rec_island;             // per body: its island in that step's solve (world-local union-find root, -1: none)
     gb_event *ev;                // contact events: 3 ccap + 64 per world, from 3 cbase + 64 world
@@ -176,6 +180,7 @@ template <class R> struct Batch {
     void *g_sh;                  // their WShared
 };
 #define GB_NPROF 16
+#define GB_MAX_GROUPS 8            // world groups of a batch (streams stepping runs of worlds concurrently)
 #define GB_WAIT_POLLS (1 << 18)    // default poll limit of the solver's waits for its bulk copies
 // finite float64 / float32 value (integer test of the exponent bits)
 static __device__ __forceinline__ bool finite_bits(double x) {

@@ -63,9 +63,9 @@ class GpuBatch:
         return c.as_dict()
 
     def set_launch_config(self, launch_mode: int = 3, block_threads: int = 128, pipe_bufs: int = 2,
-                          big_bodies: int = 512) -> None:
+                          big_bodies: int = 512, groups: int = 1) -> None:
         """Pin a launch configuration (for example one an earlier autotune chose)."""
-        c = abi.LaunchConfig(launch_mode, block_threads, pipe_bufs, big_bodies, 0.0)
+        c = abi.LaunchConfig(launch_mode, block_threads, pipe_bufs, big_bodies, groups, 0, 0.0)
         abi.check(self.lib.gb_batch_set_launch_config(self.h, ctypes.byref(c)))
 
     def autotune(self, dt: float, vel_iters: int = 8, pos_iters: int = 3, steps_per_trial: int = 3,

@@ -102,7 +102,8 @@ def test_graph_capture_rejects_what_it_cannot_capture():
 def test_launch_configs_compute_the_same_step(precision):
     """Phased-launch configurations (CTA widths, chunk buffers 0-4, the wide
     launch's threshold) give bit-identical states."""
-    configs = [(3, 64, 0, 512), (3, 64, 1, 256), (3, 32, 3, 1 << 30), (3, 128, 4, 100), (3, 64, 2, 1024)]
+    configs = [(3, 64, 0, 512), (3, 64, 1, 256), (3, 32, 3, 1 << 30), (3, 128, 4, 100), (3, 64, 2, 1024),
+               (3, 64, 0, 512, 2), (3, 64, 2, 256, 3), (3, 128, 0, 512, 8)]
     recs = scenes.uneven_batch(len(COUNTS), seed=5, counts=COUNTS)
     from pypybox2d_gb300.gpu import GpuBatch
     W, B, F, M = recs
@@ -116,6 +117,27 @@ def test_launch_configs_compute_the_same_step(precision):
         _same_state(g, ref, f"{precision} config {cfg}")
         assert not g.status().any()
         g.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_world_groups_in_graphs_and_static_scratch(precision):
+    """World groups (runs of worlds stepped on streams of their own) inside
+    a captured rollout and through the static-scratch entry point compute
+    the plain single-stream steps."""
+    from pypybox2d_gb300.gpu import GpuBatch
+    W, B, F, M = scenes.uneven_batch(len(COUNTS), seed=11, counts=COUNTS)
+    ref = GpuBatch(W, B, F, precision=precision, moves=M)
+    ref.step(DT, VI, PI, 20, launch_mode=3, block_threads=64)
+    g = GpuBatch(W, B, F, precision=precision, moves=M)
+    g.set_launch_config(3, 64, 0, 512, 3)
+    assert g.launch_config()["groups"] == 3
+    graph = g.capture(DT, VI, PI, n_steps=10, launch_mode=0)
+    graph.launch()
+    g.step_static_scratch(DT, VI, PI, 10, launch_mode=0)
+    _same_state(g, ref, f"{precision} groups in a graph, then static scratch")
+    graph.close()
+    with pytest.raises(abi.GB2DError):
+        g.set_launch_config(1, 128, 0, 512, 2)    # groups run the phased launch only
 
 
 def test_monolithic_mappings_compute_the_same_step_f64():
