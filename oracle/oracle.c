@@ -332,6 +332,8 @@ static void find_new_contacts(or_world *w) {
         int fa = pairs[k].p, fb = pairs[k].q;
         int ba = w->f[fa].body, bb = w->f[fb].body;
         if (ba == bb) continue;
+        /* an inactive body's fixtures have no proxies (body.py:848-872) */
+        if (!(w->b[ba].flags & w->b[bb].flags & GB_BODY_ACTIVE)) continue;
         int exists = 0;
         ivec *lst = &w->bcon[bb];
         for (int i = 0; i < lst->n; ++i) {
@@ -1503,6 +1505,7 @@ static or_seg or_ray_seg(const gb_ray *ray) {
     return s;
 }
 static int or_ray_fixture(const gb_body *bodies, const gb_fixture *f, const or_seg *s, v2 *nrm, double *fr) {
+    if (!(bodies[f->body].flags & GB_BODY_ACTIVE)) return 0;   /* no proxy */
     const double *a = f->aabb;
     if (!or_box_overlap(a, s->slx, s->sly, s->shx, s->shy)) return 0;
     v2 c = V(0.5 * (a[2] + a[0]), 0.5 * (a[3] + a[1]));

@@ -129,6 +129,7 @@ __device__ __forceinline__ RaySeg ray_seg(const gb_ray &ray) {
 template <class R> __device__ bool ray_fixture(const Batch<R> &B, const WorldHdr &H, int k, const RaySeg &s,
                                                vec2<double> *nrm, double *fr) {
     const int f = H.fbase + k;
+    if (!(B.b_flags[H.bbase + B.f_body[f]] & GB_BODY_ACTIVE)) return false;   // an inactive body's fixtures have no proxy
     const dbox a = B.f_aabb[f];
     if (!box_overlap(a, s.slx, s.sly, s.shx, s.shy)) return false;
     const vec2<double> c = mk<double>(0.5 * (a.z + a.x), 0.5 * (a.w + a.y));
@@ -237,7 +238,9 @@ template <class R> __global__ void k_query_aabb(Batch<R> B, const gb_aabb_query 
     for (int k0 = 0; k0 < H.nf; k0 += 32) {
         const int k = k0 + lane;
         bool hit = false;
-        if (k < H.nf) hit = gbq::box_overlap(B.f_aabb[H.fbase + k], box.lx, box.ly, box.ux, box.uy);
+        if (k < H.nf)
+            hit = (B.b_flags[H.bbase + B.f_body[H.fbase + k]] & GB_BODY_ACTIVE) &&
+                  gbq::box_overlap(B.f_aabb[H.fbase + k], box.lx, box.ly, box.ux, box.uy);
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         const int pos = found + __popc(m & ((1u << lane) - 1u));
         if (hit && pos < cap) out[(size_t)q * cap + pos] = k;

@@ -294,6 +294,8 @@ template <class R> __device__ __forceinline__ bool pair_candidate(const WView<R>
     if (!aabb_overlap(w.B.f_aabb[w.fb + q], w.B.f_aabb[w.fb + p])) return false;
     int ba = w.fbody(p), bb = w.fbody(q);
     if (ba == bb) return false;
+    // an inactive body's fixtures have no proxies (body.py:848-872)
+    if (!(w.B.b_flags[w.bb + ba] & w.B.b_flags[w.bb + bb] & GB_BODY_ACTIVE)) return false;
     // does a contact already exist?
     unsigned long long key = ((unsigned long long)(unsigned)min(p, q) << 32) | (unsigned)max(p, q);
     key += 1ull;

@@ -360,6 +360,7 @@ template <class R, class G> __device__ void toi_find_pairs(const G &g, const WVi
         if (!aabb_overlap(w.B.f_aabb[w.fb + q], w.B.f_aabb[w.fb + p])) return false;
         const int ba = w.fbody(p), bb = w.fbody(q);
         if (ba == bb) return false;
+        if (!(w.B.b_flags[w.bb + ba] & w.B.b_flags[w.bb + bb] & GB_BODY_ACTIVE)) return false;   // no proxy
         if (pair_hash_has(hash, hmask, p, q)) return false;
         if (!should_collide(w, bb, ba)) return false;
         if (!default_filter(w, p, q)) return false;

@@ -422,6 +422,17 @@ class Body:
     def active(self):
         return bool(self._rec()["flags"] & abi.BODY_ACTIVE)
 
+    @active.setter
+    def active(self, active):
+        """body.py:846-872: an inactive body keeps its place in the world but
+        its fixtures leave the broad phase and its contacts are destroyed; an
+        active one gets its proxies back (fattened at its transform, in the
+        move buffer, so the next step pairs them)."""
+        self._world._check_unlocked()
+        if bool(active) == self.active:
+            return
+        self._world._set_active(self._index, bool(active))
+
     @property
     def joints(self):
         """Body.joints: the joints attached to this body, in creation order."""
@@ -1470,6 +1481,48 @@ class World:
         fixture._body, fixture._slot = None, -1
         for j, f in enumerate(body.fixtures):
             f._slot = j
+
+    def _set_active(self, bi, active):
+        """Body.active setter (body.py:846-872).  The reference destroys the
+        contacts in a loop over the body's contact list that removes from the
+        same list, so it skips every second one and leaves them in the world;
+        a later step then walks into the inactive body.  Here every contact
+        of the body goes (touching ones reported to end_contact).  Making a
+        body active again after it was made inactive with fixtures raises
+        AssertionError, as in the reference: its Fixture._destroy_proxies
+        leaves the fixture's proxy list non-empty and _create_proxies asserts
+        it is empty (fixture.py:250-267).  Here nothing changes before the
+        exception (the reference has already set the flag, and its next step
+        fails on the dead proxy)."""
+        b = self._sb.bodies[bi]
+        if active and getattr(b, "stale_proxies", False):
+            raise AssertionError("the body's fixtures still hold the proxies destroyed when it was made inactive")
+        self._structural()
+        B, F, C = self._B, self._F, self._C
+        r = B[bi]
+        f0, nfix = int(r["fixture_start"]), int(r["fixture_count"])
+        mine = lambda x: (x >= f0) & (x < f0 + nfix)   # noqa: E731
+        b.active = active
+        if active:
+            r["flags"] |= abi.BODY_ACTIVE
+            pos, q = (float(r["px"]), float(r["py"])), (float(r["qc"]), float(r["qs"]))
+            for k, f in enumerate(b.fixtures):
+                lx, ly, ux, uy = f.shape.compute_aabb(pos, q)
+                F[f0 + k]["aabb"] = (lx - AABB_EXTENSION, ly - AABB_EXTENSION, ux + AABB_EXTENSION, uy + AABB_EXTENSION)
+            self._M = np.concatenate([self._M, np.arange(f0, f0 + nfix, dtype=np.int32)]).astype(np.int32)
+            self._sb.moves.extend((bi, k) for k in range(nfix))
+            return
+        r["flags"] &= np.uint32(0xFFFFFFFF ^ abi.BODY_ACTIVE)
+        b.stale_proxies = nfix > 0
+        hit = mine(C["fixture_a"]) | mine(C["fixture_b"])
+        if self.contact_manager.end_contact is not None:
+            for c in C[hit]:
+                if int(c["flags"]) & abi.C_TOUCHING:
+                    self.contact_manager.end_contact(EventContact(self._fixture_at(int(c["fixture_a"])),
+                                                                  self._fixture_at(int(c["fixture_b"])), False))
+        self._C = C[~hit].copy()
+        self._M = self._M[~mine(self._M)].astype(np.int32)
+        self._sb.moves = [(bb, k) for (bb, k) in self._sb.moves if bb != bi]
 
     def _set_transform(self, bi, pos, angle):
         """body.py:404-413 _transform_updated: new transform (angle None: the

@@ -181,8 +181,11 @@ def export_world(world, b2, contacts=True):
             else:
                 raise NotImplementedError("loop shapes are not exported")
             q["flags"] = fl
-            aabb = f._proxies[0].proxy_ref.aabb
-            q["aabb"][:] = (aabb.lower_bound.x, aabb.lower_bound.y, aabb.upper_bound.x, aabb.upper_bound.y)
+            if f._proxies and f._proxies[0].proxy_ref is not None:
+                aabb = f._proxies[0].proxy_ref.aabb
+                q["aabb"][:] = (aabb.lower_bound.x, aabb.lower_bound.y, aabb.upper_bound.x, aabb.upper_bound.y)
+            else:   # an inactive body's fixture has no proxy (body.py:846-872)
+                q["aabb"][:] = np.nan
             k += 1
     clist = world.contact_manager.contacts if contacts else []
     C = np.zeros(len(clist), dtype=abi.CONTACT)
@@ -670,6 +673,22 @@ def run_api_joints(b2):
           f"{os.path.getsize(path)} bytes")
 
 
+def run_api_active(b2):
+    """tests/golden/api_active.py on the reference -> api_active.npz."""
+    sys.path.insert(0, HERE)
+    import api_active
+    out = {}
+
+    def snap(label, world):
+        W, B, F, C = export_world(world, b2)
+        out[f"{label}_bodies"], out[f"{label}_aabb"], out[f"{label}_contacts"] = B, F["aabb"].copy(), C
+
+    api_active.script(b2, snap, on_world=pair_order_hook)
+    path = os.path.join(HERE, "api_active.npz")
+    np.savez_compressed(path, **out)
+    print(f"api_active: {len(api_active.SNAPS)} snapshots -> {os.path.getsize(path)} bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("GB2D_REFERENCE"), required="GB2D_REFERENCE" not in os.environ,
@@ -685,6 +704,8 @@ def main():
         run_api_script(b2)
     if not args.only or args.only == "api_joints":
         run_api_joints(b2)
+    if not args.only or args.only == "api_active":
+        run_api_active(b2)
 
 
 if __name__ == "__main__":
