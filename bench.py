@@ -250,13 +250,13 @@ def group_ranges(counts, n: int):
 
 
 def launches_per_step(W, big_bodies: int = 512, groups: int = 1):
-    """Kernel launches of one phased step: 12 per world group, plus a second
+    """Kernel launches of one phased step: 13 per world group, plus a second
     solver launch in each group that mixes worlds below and above the wide
     launch's threshold (big_bodies)."""
     n = 0
     for w0, w1 in group_ranges(W["body_count"], groups):
         nbig = int(np.count_nonzero(W["body_count"][w0:w1] >= big_bodies))
-        n += 12 + (1 if 0 < nbig < w1 - w0 else 0)
+        n += 13 + (1 if 0 < nbig < w1 - w0 else 0)
     return n
 
 

@@ -344,20 +344,27 @@ int gb_batch_set_wait_polls(gb_batch *batch, int32_t polls);
 int gb_batch_clear_status(gb_batch *batch, void *cuda_stream);
 /* Per-world status words (GB_ST_* bits), n_worlds uint32. */
 int gb_batch_status(gb_batch *batch, uint32_t *status, void *cuda_stream);
-/* Accumulated SM clock cycles per step phase, 16 int64 per world
+/* Accumulated SM clock cycles per step phase, 24 int64 per world
  * (0 pairing of new fixtures, 1 contact update, 2 islands, 3 colouring,
  * 4 velocity set-up, 5 velocity iterations, 6 position iterations, 7 sleep,
- * 8 fixture sync + pair finding, 9 continuous collision, 10 force clear). */
+ * 8 fixture sync + pair finding, 9 continuous collision, 10 force clear;
+ * continuous-collision loop: 11 passes, 12 finding the earliest event,
+ * 13 events, 14 invalidation and pair search, 15 the number of events,
+ * 16 pass statuses, 17 pass sweep alignment, 18 pass times of impact,
+ * 19 event contact updates, 20 event position passes, 21 event velocity
+ * passes and integration, 22 event fixture sync, 23 the number of fresh
+ * times of impact; 11-14 hold what the finer slots do not). */
 int gb_batch_phase_clocks(gb_batch *batch, int64_t *clocks, void *cuda_stream);
 /* Counters: step launches so far, bytes of device memory held by the
  * batch, world-steps requested so far (3 int64). */
 int gb_batch_counters(gb_batch *batch, int64_t *counters);
 /* Device time of each launch of the phased step (launch_mode 3), summed over
- * the steps run with GB_OPT_KERNEL_TIMES set: 12 slots, in launch order
+ * the steps run with GB_OPT_KERNEL_TIMES set: 13 slots, in launch order
  * (new-fixture pairs, body prologue, contact update, contact update of
  * sleeping pairs, islands and colouring, velocity integration, solver
  * set-up, solver, fixture sync and pairs, TOI candidates, first-pass TOI,
- * TOI event loop).  Measurement only: a timed step waits for its events. */
+ * TOI loop set-up, TOI event loop).  Measurement only: a timed step waits
+ * for its events. */
 int gb_batch_kernel_times(gb_batch *batch, double *total_ms, int32_t capacity, int32_t *n_slots, int64_t *n_steps);
 /* Contact events of one world recorded by the last gb_batch_step call made
  * with GB_OPT_EVENTS (unsorted; order by `key`).  *n_out = number of events;
@@ -409,7 +416,7 @@ int gb_batch_get_launch_config(gb_batch *batch, gb_launch_config *cfg);
 int gb_batch_autotune(gb_batch *batch, const gb_step_opts *opts, gb_launch_config *trials, int32_t capacity,
                       int32_t *n_out, gb_launch_config *best, void *cuda_stream);
 
-/* A multi-step rollout captured as one CUDA graph (the 12-13 launches of
+/* A multi-step rollout captured as one CUDA graph (the 13-14 launches of
  * each of opts->n_steps phased steps), replayed by gb_graph_launch with no
  * host work per step.  Replaces calling World.step n_steps times
  * (world.py:307-354).  The graph keeps the options, launch configuration and

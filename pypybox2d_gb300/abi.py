@@ -215,7 +215,7 @@ EVENT = np.dtype([
 #: gb_step_opts.record_order bit that times each launch of the phased step
 OPT_KERNEL_TIMES = 4
 KERNEL_SLOTS = ("pairs_new", "pre", "collide", "collide_sleeping", "islands", "vinit", "cinit", "solve",
-                "sync_pairs", "toi_candidates", "toi_first_pass", "toi_events")
+                "sync_pairs", "toi_candidates", "toi_first_pass", "toi_setup", "toi_events")
 
 #: bytes of the static device scratch behind gb_batch_step_static_scratch
 STATIC_SCRATCH_BYTES = 32 << 20

@@ -135,6 +135,8 @@ GB_DECL_PHASE_LAUNCHERS(PH_SOLVE)
 GB_DECL_PHASE_LAUNCHERS(PH_PAIRS)
 GB_DECL_PHASE_LAUNCHERS(PH_TOI2)
 #undef GB_DECL_PHASE_LAUNCHERS
+template <> cudaError_t gb_world_launch<PH_TOI1>(int, int, size_t, cudaStream_t, const Batch<GB_REAL> &, const StepParams &,
+                                                 const int *);
 cudaError_t gb_cta_step_launch(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *worlds, int n_list,
                                int threads, cudaStream_t st);
 cudaError_t gb_warp_step_launch(const Batch<GB_REAL> &B, const StepParams &sp, int n_steps, const int *worlds, int n_list,
@@ -214,6 +216,7 @@ GB_DEF_WORLD_LAUNCH(PH_SOLVE)
 #endif
 #if GB_IN_PART(5)
 GB_DEF_WORLD_LAUNCH(PH_TOI2)
+GB_DEF_WORLD_LAUNCH(PH_TOI1)
 #endif
 #if GB_IN_PART(6)
 GB_DEF_GRID_LAUNCH(PH_PAIRS0)
@@ -315,9 +318,11 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
         if (ns) k_toi1b<GB_REAL><<<152 * 4, 128, 0, st>>>(B);
         GB_CK(cudaGetLastError());
         mark(11);
+        GB_CK(gb_world_launch<PH_TOI1>(n_norm, t_isl, 0, st, B, sp, w_norm));
+        mark(12);
         GB_GRID(PH_TOI2);
         GB_CK(gb_world_launch<PH_TOI2>(n_norm, 32, 0, st, B, sp, w_norm));
-        mark(12);
+        mark(13);
         if (kt) {
             GB_CK(cudaEventSynchronize(kt->ev[GB_NKTIME]));
             for (int k = 0; k < GB_NKTIME; ++k) {

@@ -5,7 +5,7 @@
 #include "gb_world.cuh"
 
 // Phased-step kernel timing: GB_NKTIME launch slots, GB_NKTIME + 1 events.
-#define GB_NKTIME 12
+#define GB_NKTIME 13
 struct KernelTimer {
     cudaEvent_t ev[GB_NKTIME + 1];
     double total_ms[GB_NKTIME];

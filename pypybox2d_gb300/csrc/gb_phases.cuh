@@ -1,7 +1,8 @@
 // gb_phases.cuh -- the batched step as a sequence of phase kernels.
 //
-// One World.step of every world of the batch is 11 launches (captured once
-// into a CUDA graph and replayed per step):
+// One World.step of every world of the batch is 13 launches (14 with a
+// second solver launch; captured once into a CUDA graph and replayed per
+// step):
 //
 //   k_pairs0    per world   pair finding over the pending move buffer (new fixtures)
 //   k_pre       per body    collide wake marks, TOI state reset
@@ -15,8 +16,10 @@
 //   k_cinit     per constraint  solver set-up (contact.py:375-496)
 //   k_solve     per world   warm start, velocity and position iterations, sleep
 //   k_pairs     per world   fixture sync and pair finding (world.py:582-592)
-//   k_toi1      per contact first pass of the time-of-impact loop (float64)
-//   k_toi2      per world   the rest of the event loop, force clear
+//   k_toi1      per contact TOI state reset, candidates of the first pass
+//   k_toi1b     per candidate  the first pass's float64 times of impact
+//   k_toi_setup per world   the event loop's adjacency, pair hash and candidate list
+//   k_toi2      per world   the rest of the event loop (one warp), force clear
 //
 // "per body / contact / constraint" kernels run one thread per element of
 // every world (the 4096-world batch gives ~2.4 M contact threads), "per
@@ -152,6 +155,7 @@ template <class R> __global__ void k_toi1b(Batch<R> B) {
 #define PH_SOLVE 3
 #define PH_PAIRS 4
 #define PH_TOI2 5
+#define PH_TOI1 6   // the event loop's set-up, a CTA per world ahead of the one-warp loop
 
 template <class R, int PH> __device__ __forceinline__ void world_phase(const Batch<R> &B, const StepParams &sp, const int wi);
 
@@ -244,6 +248,15 @@ template <class R, int PH, class G> __device__ __forceinline__ void phase_body(c
     } else if (PH == PH_PAIRS) {
         if (g.rank() == 0) H.toimin = ~0ull;   // k_toi1b lowers it
         if (H.pflags & P_SOLVING) sync_pairs_group(g, w, sp, &sh);
+    } else if (PH == PH_TOI1) {
+        // the loop's adjacency, pair hash and candidate list with the whole
+        // CTA, for the worlds whose loop will run (the test of PH_TOI2)
+        const bool par_first = (H.flags & GB_W_STEP_COMPLETE) != 0;
+        const bool none = par_first && (H.toimin == ~0ull || (1.0 - (10.0 * GB_EPSILON)) < dkey_inv(H.toimin));
+        if ((H.flags & GB_W_CONTINUOUS) && sp.dt > 0.0 && par_first && !none) {
+            const int ncand = toi_setup(g, w, &sh);
+            if (g.rank() == 0) { H.toi_ncand = ncand; H.toi_hcap = sh.lhcap; H.toi_ready = 1; }
+        }
     } else if (PH == PH_TOI2) {
         if ((H.flags & GB_W_CONTINUOUS) && sp.dt > 0.0) {
             const bool par_first = (H.flags & GB_W_STEP_COMPLETE) != 0;
@@ -260,6 +273,7 @@ template <class R, int PH, class G> __device__ __forceinline__ void phase_body(c
             }
         }
         g.sync();
+        if (g.rank() == 0) H.toi_ready = 0;
         if (g.rank() == 0 && sp.dt > 0.0) H.inv_dt0 = sp.inv_dt;
         if (H.flags & GB_W_AUTO_CLEAR_FORCES)
             for (int b = g.rank(); b < H.nb; b += g.size()) {

@@ -85,7 +85,8 @@ template <class R> __device__ bool toi_of_contact(const WView<R> &w, int i) {
 // island.py:181-243 Island.solve_toi on rank 0 (island of at most 64
 // bodies and 32 contacts).
 template <class R> __device__ void island_solve_toi(const WView<R> &w, const int *ib, int nbi, const int *ic, int nci,
-                                                    double sub_dt, int vel_iters, int toi_a, int toi_b, const EvCtx *ev = nullptr) {
+                                                    double sub_dt, int vel_iters, int toi_a, int toi_b, const EvCtx *ev = nullptr,
+                                                    PhaseClock *ck = nullptr) {
     vec2<double> pc[2 * GB_MAX_TOI_CONTACTS];
     double pa[2 * GB_MAX_TOI_CONTACTS];
     vec2<R> vv[2 * GB_MAX_TOI_CONTACTS];
@@ -120,6 +121,7 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
         its = it + 1;
         if (minsep >= -1.5 * GB_LINEAR_SLOP) break;
     }
+    if (ck) ck->mark(20);
     if (ev && ev->rec)
         for (int t : {toi_a, toi_b}) {
             rec_add_byte(&ev->rec[ib[t]], GB_REC_TOI_ITERS_SHIFT, its);
@@ -174,6 +176,7 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
                 atomicOr(&w.H->status, GB_ST_NONFINITE);
         }
     }
+    if (ck) ck->mark(21);
 }
 
 // One TOI event (world.py:693-817) on rank 0.  Appends the re-fattened
@@ -182,7 +185,8 @@ template <class R> __device__ void island_solve_toi(const WView<R> &w, const int
 // (Body._contacts).  The island bodies are left in s_stack[0..sh->nisland)
 // with their s_bvis marks set; the caller invalidates and clears them.
 template <class R> __device__ void toi_event(const WView<R> &w, int mi, double min_alpha, double dt, int vel_iters, WShared *sh,
-                                             const int *la, int na, const int *lb, int nlb, const EvCtx *ev = nullptr) {
+                                             const int *la, int na, const int *lb, int nlb, const EvCtx *ev = nullptr,
+                                             PhaseClock *ck = nullptr) {
     ContactRec<R> &mc = w.con(mi);
     unsigned char *bflag = w.B.s_bvis + w.bb;
     int bia = w.fbody(mc.fa), bib = w.fbody(mc.fb);
@@ -240,7 +244,8 @@ template <class R> __device__ void toi_event(const WView<R> &w, int mi, double m
         }
     }
     double sub_dt = (1.0 - min_alpha) * dt;
-    island_solve_toi(w, ib, nbi, ic, nci, sub_dt, vel_iters, 0, 1, ev);
+    if (ck) ck->mark(19);
+    island_solve_toi(w, ib, nbi, ic, nci, sub_dt, vel_iters, 0, 1, ev, ck);
     int *mv = w.B.s_move + w.fb;
     for (int i = 0; i < nbi; ++i) {
         int bi = ib[i];
@@ -256,6 +261,7 @@ template <class R> __device__ void toi_event(const WView<R> &w, int mi, double m
     int *isl = w.B.s_stack + w.bb;
     for (int i = 0; i < nbi; ++i) isl[i] = ib[i];
     sh->nisland = nbi;
+    if (ck) ck->mark(22);
 }
 
 // world.py:599-609 reset of the TOI state of one contact
@@ -431,22 +437,17 @@ template <class R, class G> __device__ void toi_find_pairs(const G &g, const WVi
     g.sync();
 }
 
-// The event loop of world.py:612-821; `first_done` means pass 0 already ran
-// (in the batch-wide kernel).  Passes scan the candidate list only, and the
-// contact lists of the event bodies come from a per-body adjacency built
-// once per step.
-template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh,
-                                                     bool par_first, bool first_done, PhaseClock *pc = nullptr) {
-    PhaseClock dummy;
-    dummy.acc = nullptr;
-    PhaseClock &ck = pc ? *pc : dummy;
-    int *proc = w.B.s_proc + w.cb;
+// Set-up of the event loop: the per-body adjacency of the dynamic bodies
+// (Body._contacts in list order), the loop's pair hash over every contact
+// and the candidate list in list order.  Returns the number of candidates;
+// the hash's slot count is left in sh->lhcap.  Run by the loop itself, or
+// ahead of it by a wider group (the set-up kernel), whose results the loop
+// then reads (WorldHdr::toi_ready).
+template <class R, class G> __device__ int toi_setup(const G &g, const WView<R> &w, WShared *sh) {
     int *ids = w.B.s_pref + w.cb;
-    TPlan *plan = w.B.s_plan + (size_t)w.wi * GB_TOI_PLAN_CAP;
-    unsigned char *bflag = w.B.s_bvis + w.bb;
-    int *cand = w.B.s_cons_of + w.cb;                          // candidate contacts, list order
-    int *off = w.B.s_adjoff + w.bb + w.wi;                     // adjacency of dynamic bodies (nb + 1)
-    int *adj = reinterpret_cast<int *>(w.B.s_kb + w.cb);       // 2 ccap entries
+    int *cand = w.B.s_cons_of + w.cb;
+    int *off = w.B.s_adjoff + w.bb + w.wi;
+    int *adj = reinterpret_cast<int *>(w.B.s_kb + w.cb);
     int *cursor = w.B.s_seed + w.bb;
     const int nb = w.H->nb;
     const int nc0 = w.H->nc;
@@ -487,6 +488,36 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
     for (int i = g.rank(); i < nc0; i += g.size())
         if (w.con(i).flags & GB_C_TOI_CAND) cand[ids[i]] = i;
     g.sync();
+    return ncand;
+}
+
+// The event loop of world.py:612-821; `first_done` means pass 0 already ran
+// (in the batch-wide kernel).  Passes scan the candidate list only, and the
+// contact lists of the event bodies come from a per-body adjacency built
+// once per step.
+template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh,
+                                                     bool par_first, bool first_done, PhaseClock *pc = nullptr) {
+    PhaseClock dummy;
+    dummy.acc = nullptr;
+    PhaseClock &ck = pc ? *pc : dummy;
+    int *proc = w.B.s_proc + w.cb;
+    int *ids = w.B.s_pref + w.cb;
+    TPlan *plan = w.B.s_plan + (size_t)w.wi * GB_TOI_PLAN_CAP;
+    unsigned char *bflag = w.B.s_bvis + w.bb;
+    int *cand = w.B.s_cons_of + w.cb;                          // candidate contacts, list order
+    int *off = w.B.s_adjoff + w.bb + w.wi;                     // adjacency of dynamic bodies (nb + 1)
+    int *adj = reinterpret_cast<int *>(w.B.s_kb + w.cb);       // 2 ccap entries
+    const int nc0 = w.H->nc;
+    unsigned long long *lhash = w.B.s_hash + 4 * (size_t)w.cb;
+    int ncand;
+    if (w.H->toi_ready) {   // made by the set-up kernel
+        ncand = w.H->toi_ncand;
+        if (g.rank() == 0) sh->lhcap = w.H->toi_hcap;
+        g.sync();
+    } else {
+        ncand = toi_setup(g, w, sh);
+    }
+    if (g.rank() == 0) ck.mark(11);
     for (int pass = 0; pass < (1 << 20); ++pass) {
         const int nc = w.H->nc;
         if (pass == 0 && first_done) {
@@ -502,6 +533,7 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
                 return st == 2 ? 1 : 0;
             }, ids);
             g.sync();
+            if (g.rank() == 0) { ck.mark(16); if (ck.acc) ck.acc[23] += nfresh; }
             if (nfresh > 0) {
                 int *fresh = w.B.s_adj + 2 * (size_t)w.cb;   // free during the TOI loop
                 for (int k = g.rank(); k < ncand; k += g.size()) {
@@ -515,7 +547,10 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
                     if (g.rank() == 0)
                         for (int k = 0; k < nfresh; ++k) plan[k].alpha0 = toi_align(w, fresh[k], &plan[k].sa, &plan[k].sb);
                     g.sync();
+                    if (g.rank() == 0) ck.mark(17);
                     for (int k = g.rank(); k < nfresh; k += g.size()) toi_compute(w, fresh[k], plan[k].alpha0, plan[k].sa, plan[k].sb);
+                    g.sync();
+                    if (g.rank() == 0) ck.mark(18);
                 } else if (g.rank() == 0) {
                     for (int k = 0; k < nfresh; ++k) {
                         Sweep sa, sb;
@@ -557,7 +592,7 @@ template <class R, class G> __device__ void toi_loop(const G &g, const WView<R> 
             if (w.btype(bib) == GB_BODY_DYNAMIC) body_contacts(w, off, adj, nc0, nc, bib, [&](int i) { lb[nlb++] = i; });
             sh->nmove = 0;
             const EvCtx ev{sp.events, sp.step_index, GB_EV_PHASE_TOI, sp.record_order ? w.B.rec + w.bb : nullptr};
-            toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh, la, na, lb, nlb, &ev);
+            toi_event(w, mi, min_alpha, sp.dt, sp.vel_iters, sh, la, na, lb, nlb, &ev, &ck);
             ck.mark(13);
         }
         g.sync();

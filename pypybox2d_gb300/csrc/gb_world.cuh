@@ -95,6 +95,8 @@ struct WorldHdr {              // per-world scalars (device)
     unsigned long long toimin; // dkey of the earliest first-pass time of impact below 1 (~0: none)
     int jbase;                 // batch index of its first joint
     int last_njcons, last_njcolours;   // joint constraints and their colours in the current step
+    int toi_ncand, toi_hcap;   // TOI loop set-up made by the set-up kernel: candidates, pair-hash slots
+    int toi_ready;             // that set-up is there for this step's loop
     int _pad2;
 };
 
@@ -179,7 +181,7 @@ template <class R> struct Batch {
     long long *g_scr;            // their group scratch (2 x grid + 8)
     void *g_sh;                  // their WShared
 };
-#define GB_NPROF 16
+#define GB_NPROF 24
 #define GB_MAX_GROUPS 8            // world groups of a batch (streams stepping runs of worlds concurrently)
 #define GB_WAIT_POLLS (1 << 18)    // default poll limit of the solver's waits for its bulk copies
 // finite float64 / float32 value (integer test of the exponent bits)

@@ -195,8 +195,8 @@ class GpuBatch:
         return ev[np.argsort(ev["key"], kind="stable")]
 
     def phase_clocks(self) -> np.ndarray:
-        """Accumulated SM clocks per step phase and world (n_worlds x 16)."""
-        out = np.zeros((self.n_worlds, 16), dtype=np.int64)
+        """Accumulated SM clocks per step phase and world (n_worlds x 24)."""
+        out = np.zeros((self.n_worlds, 24), dtype=np.int64)
         abi.check(self.lib.gb_batch_phase_clocks(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), None))
         return out
 
