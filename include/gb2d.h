@@ -57,6 +57,10 @@ extern "C" {
 #define GB_FIX_SENSOR 1u
 #define GB_FIX_EDGE_HAS_V0 2u /* edge vertex0 present (vx[2],vy[2]) */
 #define GB_FIX_EDGE_HAS_V3 4u /* edge vertex3 present (vx[3],vy[3]) */
+#define GB_FIX_LOOP_CHILD 8u  /* an edge that is one child of a loop: its fat box has no radius margin
+                                 (shapes.py:822-837); a loop fixture of n vertices is n consecutive edge
+                                 records, child i from vertex i to i+1 with vertices i-1 and i+2 as
+                                 vertex0/vertex3 (shapes.py:851-863) */
 
 /* gb_contact.flags, as the Contact._*_flag attributes of contact.py:75-87 */
 #define GB_C_TOUCHING 1u
@@ -152,7 +156,7 @@ typedef struct gb_fixture {
  * ContactManager.contacts. */
 typedef struct gb_contact {
     int32_t fixture_a, fixture_b; /* world-local; A is the primary shape of the pair */
-    int32_t child_a, child_b;
+    int32_t child_a, child_b;     /* 0: each child of a loop is a record of its own (GB_FIX_LOOP_CHILD) */
     uint32_t flags;               /* GB_C_* */
     int32_t toi_count;
     double toi;

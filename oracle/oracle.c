@@ -204,6 +204,10 @@ static void shape_aabb(const gb_fixture *f, xform x, double out[4]) {
         v2 v1 = xmul(x, fx_v(f, 0)), v2_ = xmul(x, fx_v(f, 1));
         v2 lower = V(cmin(v1.x, v2_.x), cmin(v1.y, v2_.y));
         v2 upper = V(cmax(v1.x, v2_.x), cmax(v1.y, v2_.y));
+        if (f->flags & GB_FIX_LOOP_CHILD) {   /* Loop.compute_aabb: no radius (shapes.py:822-837) */
+            out[0] = lower.x; out[1] = lower.y; out[2] = upper.x; out[3] = upper.y;
+            return;
+        }
         out[0] = lower.x - f->radius; out[1] = lower.y - f->radius;
         out[2] = upper.x + f->radius; out[3] = upper.y + f->radius;
     }

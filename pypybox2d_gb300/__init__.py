@@ -4,6 +4,6 @@ World.step hot path behind the reference's World/Body/Fixture API."""
 from .shapes import Circle, Edge, Loop, MassData, Polygon, Shape  # noqa: E402,F401
 from .errors import (CapacityError, ContactOverflowError, EmptyFixtureError, LockedError, NonFiniteError,  # noqa: E402,F401
                      PhysicsError, StepError, WaitTimeoutError)
-from .world import Body, Contact, ContactManager, EventContact, Fixture, Vec2, World, WorldBatch  # noqa: E402,F401
+from .world import AABB, Body, Contact, ContactManager, EventContact, Fixture, Vec2, World, WorldBatch  # noqa: E402,F401
 from . import joints  # noqa: E402,F401
 from .joints import DistanceJoint, Joint, PrismaticJoint, RevoluteJoint, WeldJoint  # noqa: E402,F401

@@ -26,6 +26,7 @@ BODY_ACTIVE = 16
 FIX_SENSOR = 1
 FIX_EDGE_HAS_V0 = 2
 FIX_EDGE_HAS_V3 = 4
+FIX_LOOP_CHILD = 8      # one child edge of a loop fixture (no radius margin on its box)
 
 C_TOUCHING = 1
 C_ENABLED = 2

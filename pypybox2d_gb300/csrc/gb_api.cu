@@ -260,7 +260,8 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         for (int k = 0; k < d.fixture_count; ++k) {
             const gb_fixture &f = scene->fixtures[d.fixture_start + k];
             if (f.body < 0 || f.body >= d.body_count || f.vertex_count < 1 || f.vertex_count > GB_MAX_POLY_VERTS ||
-                f.shape_type == GB_SHAPE_LOOP || f.shape_type < 0 || f.shape_type > GB_SHAPE_EDGE) {
+                f.shape_type == GB_SHAPE_LOOP || f.shape_type < 0 || f.shape_type > GB_SHAPE_EDGE ||
+                ((f.flags & GB_FIX_LOOP_CHILD) && f.shape_type != GB_SHAPE_EDGE)) {
                 delete b;
                 return fail(GB_E_UNSUPPORTED, "world " + std::to_string(i) + " fixture " + std::to_string(k) +
                                                   ": unsupported shape or bad body index");

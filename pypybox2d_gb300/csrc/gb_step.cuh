@@ -224,10 +224,12 @@ template <class R> __device__ dbox shape_aabb_f32(const WView<R> &w, int f, vec2
             hi = mk<float>(fmaxf(hi.x, v.x), fmaxf(hi.y, v.y));
         }
     }
+    if (s.flags & GB_FIX_LOOP_CHILD) return mkbox(p.x + (double)lo.x, p.y + (double)lo.y, p.x + (double)hi.x, p.y + (double)hi.y);
     return mkbox(p.x + (double)(lo.x - r), p.y + (double)(lo.y - r), p.x + (double)(hi.x + r), p.y + (double)(hi.y + r));
 }
 
-// shapes.py compute_aabb (child 0), float64
+// shapes.py compute_aabb (child 0), float64; a loop's child edge takes no
+// radius margin (shapes.py:822-837)
 template <class R> __device__ dbox shape_aabb(const WView<R> &w, int f, xform2<double> x) {
     Shape<R> s = w.shape(f);
     double r = (double)s.radius;
@@ -242,6 +244,7 @@ template <class R> __device__ dbox shape_aabb(const WView<R> &w, int f, xform2<d
         lo = mk<double>(cmin(lo.x, v.x), cmin(lo.y, v.y));
         hi = mk<double>(cmax(hi.x, v.x), cmax(hi.y, v.y));
     }
+    if (s.flags & GB_FIX_LOOP_CHILD) return mkbox(lo.x, lo.y, hi.x, hi.y);
     return mkbox(lo.x - r, lo.y - r, hi.x + r, hi.y + r);
 }
 

@@ -20,7 +20,7 @@ import math
 import numpy as np
 
 from . import abi
-from .shapes import FLT_EPSILON, POLYGON_RADIUS, Circle, Edge, Polygon, _xmul
+from .shapes import FLT_EPSILON, POLYGON_RADIUS, Circle, Edge, Loop, Polygon, _xmul
 
 AABB_EXTENSION = 0.1
 
@@ -60,7 +60,15 @@ class _Body:
         self.bullet, self.active = bool(bullet), bool(active)
         self.sleep_time = 0.0
         self.fixtures: list[_Fix] = []
-        self.aabbs: list[tuple] = []
+        self.aabbs: list[tuple] = []      # per record (a loop fixture has one record per child)
+
+    def record_offset(self, k: int) -> int:
+        """The first record of fixture k (loop fixtures take one per child)."""
+        return sum(f.shape.child_count for f in self.fixtures[:k])
+
+    @property
+    def record_count(self) -> int:
+        return sum(f.shape.child_count for f in self.fixtures)
 
     def reset_mass_data(self):
         """body.py:587-641"""
@@ -113,7 +121,7 @@ class SceneBuilder:
                       (abi.W_CONTINUOUS if continuous_physics else 0) | (abi.W_AUTO_CLEAR_FORCES if auto_clear_forces else 0) |
                       abi.W_STEP_COMPLETE)
         self.bodies: list[_Body] = []
-        self.moves: list[tuple[int, int]] = []   # (body, fixture slot) in proxy creation order
+        self.moves: list[tuple[int, int]] = []   # (body, record within the body) in proxy creation order
 
     def create_body(self, type=abi.BODY_STATIC, fixtures=(), **kw) -> int:
         """World.create_body(**kw) with `fixtures` = [(shape, fixture kwargs)] attached
@@ -145,52 +153,66 @@ class SceneBuilder:
             b.reset_mass_data()
 
     def _create_proxy(self, bi, k):
+        """fixture.py:250-261: one proxy per child, fattened (dynamictree.py:115-134)"""
         b = self.bodies[bi]
-        lx, ly, ux, uy = b.fixtures[k].shape.compute_aabb(b.p, b.q)
-        while len(b.aabbs) <= k:
-            b.aabbs.append(None)
-        b.aabbs[k] = (lx - AABB_EXTENSION, ly - AABB_EXTENSION, ux + AABB_EXTENSION, uy + AABB_EXTENSION)
-        self.moves.append((bi, k))
+        sh = b.fixtures[k].shape
+        o = b.record_offset(k)
+        for c in range(sh.child_count):
+            lx, ly, ux, uy = sh.compute_aabb(b.p, b.q, c) if isinstance(sh, Loop) else sh.compute_aabb(b.p, b.q)
+            while len(b.aabbs) <= o + c:
+                b.aabbs.append(None)
+            b.aabbs[o + c] = (lx - AABB_EXTENSION, ly - AABB_EXTENSION, ux + AABB_EXTENSION, uy + AABB_EXTENSION)
+            self.moves.append((bi, o + c))
 
     def body_records(self, bi: int, body_index: int | None = None):
         """Record of body bi and the records of its fixtures (``body`` field =
         body_index, default bi)."""
         b = self.bodies[bi]
         B = np.zeros(1, dtype=abi.BODY)
-        F = np.zeros(len(b.fixtures), dtype=abi.FIXTURE)
+        F = np.zeros(b.record_count, dtype=abi.FIXTURE)
         fl = ((abi.BODY_AWAKE if b.awake else 0) | (abi.BODY_ALLOW_SLEEP if b.allow_sleep else 0) |
               (abi.BODY_BULLET if b.bullet else 0) | (abi.BODY_FIXED_ROTATION if b.fixed_rotation else 0) |
               (abi.BODY_ACTIVE if b.active else 0))
-        B[0] = (b.type, fl, 0, len(b.fixtures), b.p[0], b.p[1], b.q[0], b.q[1], b.lc[0], b.lc[1],
+        B[0] = (b.type, fl, 0, len(F), b.p[0], b.p[1], b.q[0], b.q[1], b.lc[0], b.lc[1],
                 b.c0[0], b.c0[1], b.c[0], b.c[1], b.a0, b.a, b.alpha0, b.v[0], b.v[1], b.w,
                 b.force[0], b.force[1], b.torque, b.mass, b.inv_mass, b.I, b.invI, b.ld, b.ad, b.gs, b.sleep_time)
-        for j, f in enumerate(b.fixtures):
-            r = F[j]
-            sh = f.shape
-            r["body"], r["shape_type"], r["radius"] = bi if body_index is None else body_index, sh.type, sh.radius
-            r["friction"], r["restitution"], r["density"] = f.friction, f.restitution, f.density
-            r["category_bits"], r["mask_bits"], r["group_index"] = f.category, f.mask, f.group
-            ffl = abi.FIX_SENSOR if f.sensor else 0
-            if isinstance(sh, Circle):
-                r["vertex_count"] = 1
-                r["vx"][0], r["vy"][0] = sh.position
-            elif isinstance(sh, Polygon):
-                r["vertex_count"] = len(sh._vertices)
-                for m, ((vx, vy), (nx, ny)) in enumerate(zip(sh._vertices, sh._normals)):
-                    r["vx"][m], r["vy"][m], r["nx"][m], r["ny"][m] = vx, vy, nx, ny
-            elif isinstance(sh, Edge):
-                r["vertex_count"] = 2
-                r["vx"][0], r["vy"][0] = sh.vertex1
-                r["vx"][1], r["vy"][1] = sh.vertex2
-                if sh.vertex0 is not None:
-                    ffl |= abi.FIX_EDGE_HAS_V0
-                    r["vx"][2], r["vy"][2] = sh.vertex0
-                if sh.vertex3 is not None:
-                    ffl |= abi.FIX_EDGE_HAS_V3
-                    r["vx"][3], r["vy"][3] = sh.vertex3
-            r["flags"] = ffl
-            r["aabb"][:] = b.aabbs[j] if j < len(b.aabbs) and b.aabbs[j] is not None else (0, 0, 0, 0)
+        j = 0
+        for f in b.fixtures:
+            # a loop: one edge record per child (shapes.py:851-863), no radius
+            # margin on its fat box
+            children = [(f.shape.child_edge(c), abi.FIX_LOOP_CHILD) for c in range(f.shape.child_count)] \
+                if isinstance(f.shape, Loop) else [(f.shape, 0)]
+            for sh, extra in children:
+                j = self._fixture_record(F, j, b, f, sh, extra, bi if body_index is None else body_index)
         return B[0], F
+
+    def _fixture_record(self, F, j, b, f, sh, extra, body_index):
+        """Fill record j of F from fixture f with shape sh; returns j + 1."""
+        r = F[j]
+        r["body"], r["shape_type"], r["radius"] = body_index, sh.type, sh.radius
+        r["friction"], r["restitution"], r["density"] = f.friction, f.restitution, f.density
+        r["category_bits"], r["mask_bits"], r["group_index"] = f.category, f.mask, f.group
+        ffl = (abi.FIX_SENSOR if f.sensor else 0) | extra
+        if isinstance(sh, Circle):
+            r["vertex_count"] = 1
+            r["vx"][0], r["vy"][0] = sh.position
+        elif isinstance(sh, Polygon):
+            r["vertex_count"] = len(sh._vertices)
+            for m, ((vx, vy), (nx, ny)) in enumerate(zip(sh._vertices, sh._normals)):
+                r["vx"][m], r["vy"][m], r["nx"][m], r["ny"][m] = vx, vy, nx, ny
+        elif isinstance(sh, Edge):
+            r["vertex_count"] = 2
+            r["vx"][0], r["vy"][0] = sh.vertex1
+            r["vx"][1], r["vy"][1] = sh.vertex2
+            if sh.vertex0 is not None:
+                ffl |= abi.FIX_EDGE_HAS_V0
+                r["vx"][2], r["vy"][2] = sh.vertex0
+            if sh.vertex3 is not None:
+                ffl |= abi.FIX_EDGE_HAS_V3
+                r["vx"][3], r["vy"][3] = sh.vertex3
+        r["flags"] = ffl
+        r["aabb"][:] = b.aabbs[j] if j < len(b.aabbs) and b.aabbs[j] is not None else (0, 0, 0, 0)
+        return j + 1
 
     def world_record(self, nb: int, nf: int, n_moves: int):
         W = np.zeros(1, dtype=abi.WORLD)
@@ -201,7 +223,7 @@ class SceneBuilder:
     def records(self):
         """(worlds[1], bodies, fixtures, moves) record arrays of this world."""
         nb = len(self.bodies)
-        nf = sum(len(b.fixtures) for b in self.bodies)
+        nf = sum(b.record_count for b in self.bodies)
         B = np.zeros(nb, dtype=abi.BODY)
         F = np.zeros(nf, dtype=abi.FIXTURE)
         start = []

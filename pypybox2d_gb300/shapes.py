@@ -1,11 +1,12 @@
-"""Shapes of the drop-in API: Circle, Polygon, Edge.
+"""Shapes of the drop-in API: Circle, Polygon, Edge, Loop.
 
 Construction arithmetic (edge normals, mass data, AABBs) repeats the
 reference's float64 operation order -- pypybox2d/shapes.py Circle
-(:128-236), Polygon (:238-616), Edge (:618-778) and the C-extension vector
-operations of pypybox2d/src/vec2module.c -- so a world built here is
-bit-identical to the same world built with pypybox2d.  Loop shapes
-(shapes.py:780-882) are not supported by the GPU step and raise.
+(:128-236), Polygon (:238-616), Edge (:618-778), Loop (:780-882) and the
+C-extension vector operations of pypybox2d/src/vec2module.c -- so a world
+built here is bit-identical to the same world built with pypybox2d.  A loop
+fixture becomes one edge record per child (``child_edge``), flagged
+``FIX_LOOP_CHILD`` for the loop's fat-box rule.
 """
 from __future__ import annotations
 
@@ -222,7 +223,51 @@ class Edge(Shape):
 
 
 class Loop(Shape):
+    """shapes.py:780-882: a closed chain of edges with double-sided
+    collision; child i runs from vertex i to vertex i + 1 (mod n)."""
+
     type = abi.SHAPE_LOOP
 
-    def __init__(self, *args, **kwargs):
-        raise NotImplementedError("Loop shapes are not supported by the GPU world step")
+    def __init__(self, vertices, *args):
+        if len(vertices) == 2 and isinstance(vertices[0], (int, float)):
+            vertices = [vertices, *args]
+        if len(vertices) < 2:
+            raise ValueError("Must be >= 2 vertices")
+        self.radius = POLYGON_RADIUS
+        self._vertices = [(float(v[0]), float(v[1])) for v in vertices]
+
+    def __copy__(self):
+        return Loop(self._vertices)
+
+    def __repr__(self):
+        return f"Loop(vertices={self._vertices})"
+
+    @property
+    def vertices(self):
+        return list(self._vertices)
+
+    @property
+    def child_count(self):
+        return len(self._vertices)
+
+    def child_edge(self, index):
+        """shapes.py:851-863: the edge of child `index` with its neighbours as
+        vertex0 / vertex3"""
+        n = len(self._vertices)
+        i0, i1, i2 = (index - 1) % n, index, (index + 1) % n
+        i3 = index + 2
+        while i3 >= n:
+            i3 -= n
+        v = self._vertices
+        return Edge(v[i1], v[i2], v[i0], v[i3])
+
+    def compute_mass(self, density):
+        """Loops have no mass (shapes.py:845-847)."""
+        return MassData()
+
+    def compute_aabb(self, p, q, child=0):
+        """shapes.py:822-837: the child's two vertices, no radius margin"""
+        n = len(self._vertices)
+        x1, y1 = _xmul(p, q, self._vertices[child])
+        x2, y2 = _xmul(p, q, self._vertices[(child + 1) % n])
+        return min(x1, x2), min(y1, y2), max(x1, x2), max(y1, y2)

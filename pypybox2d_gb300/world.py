@@ -90,13 +90,37 @@ class Vec2(tuple):
         return f"Vec2({self[0]:g}, {self[1]:g})"
 
 
+class AABB:
+    """The query box of World.query_aabb (common AABB, aabbmodule.c): lower
+    and upper bound, each given as a pair."""
+
+    __slots__ = ("lower_bound", "upper_bound")
+
+    def __init__(self, lower_bound=None, upper_bound=None):
+        self.lower_bound = Vec2(*lower_bound) if lower_bound is not None else Vec2()
+        self.upper_bound = Vec2(*upper_bound) if upper_bound is not None else Vec2()
+
+    @property
+    def center(self):
+        return Vec2(0.5 * (self.lower_bound[0] + self.upper_bound[0]), 0.5 * (self.lower_bound[1] + self.upper_bound[1]))
+
+    @property
+    def extents(self):
+        return Vec2(0.5 * (self.upper_bound[0] - self.lower_bound[0]), 0.5 * (self.upper_bound[1] - self.lower_bound[1]))
+
+    @property
+    def perimeter(self):
+        return 2.0 * ((self.upper_bound[0] - self.lower_bound[0]) + (self.upper_bound[1] - self.lower_bound[1]))
+
+    def __repr__(self):
+        return f"AABB(lower_bound={tuple(self.lower_bound)}, upper_bound={tuple(self.upper_bound)})"
+
+
 class Fixture:
     """fixture.py:43-71: a shape with its material and filter data."""
 
     def __init__(self, shape=None, friction=0.2, restitution=0.0, density=0.0, category_bits=0x0001,
                  mask_bits=0xFFFF, group_index=0, sensor=False, user_data=None, body=None):
-        if isinstance(shape, Loop):
-            raise NotImplementedError("Loop shapes are not supported by the GPU world step")
         self._body = None
         self._slot = -1
         self._shape = shape
@@ -627,7 +651,8 @@ class Body:
         return self.create_fixture(Edge(v1, v2, v0, v3), **kwargs)
 
     def create_loop_fixture(self, vertices, *args, **kwargs):
-        raise NotImplementedError("Loop shapes are not supported by the GPU world step")
+        """body.py:231-234; the loop's children become edge records"""
+        return self.create_fixture(Loop(vertices, *args), **kwargs)
 
     def __repr__(self):
         return f"Body(index={self._index}, position={self.position}, angle={self.angle:g})"
@@ -639,11 +664,9 @@ class Contact:
     def __init__(self, world, rec):
         self._world = world
         self._rec = rec
-        self.fixture_a = world._fixture_at(int(rec["fixture_a"]))
-        self.fixture_b = world._fixture_at(int(rec["fixture_b"]))
+        self.fixture_a, self.child_index_a = world._fixture_child_at(int(rec["fixture_a"]))
+        self.fixture_b, self.child_index_b = world._fixture_child_at(int(rec["fixture_b"]))
 
-    child_index_a = property(lambda self: 0)
-    child_index_b = property(lambda self: 0)
     body_a = property(lambda self: self.fixture_a.body)
     body_b = property(lambda self: self.fixture_b.body)
     shape_a = property(lambda self: self.fixture_a.shape)
@@ -1155,7 +1178,9 @@ class World:
         (lower, upper), or (lx, ly, ux, uy)); one gb_batch_query_aabb.  The
         fixtures come in fixture order (the reference's in tree order).
         Without a callback, an iterator; with one, called per fixture until
-        it returns a false value."""
+        it returns a false value, at once, and an empty iterator comes back:
+        the reference's method is a generator, so callers that pass a
+        callback iterate the result to run it."""
         lx, ly, ux, uy = _box_of(aabb)
         gpu, wi = self._query_gpu()
         q = np.zeros(1, dtype=abi.AABB_QUERY)
@@ -1167,7 +1192,7 @@ class World:
         for f in fixtures:
             if not callback(f):
                 break
-        return None
+        return iter(())
 
     def ray_cast_closest(self, point1, point2):
         """The closest fixture on the segment point1 -> point2: what
@@ -1198,11 +1223,13 @@ class World:
         callback therefore ends as with the reference, and an all-hits one
         sees the same hits.  Without a callback, a generator of
         [fixture, point, normal, fraction] lists whose last entry the caller
-        may set to the same answers."""
+        may set to the same answers.  A callback runs at once and an empty
+        iterator comes back (callers of the reference's generator iterate
+        it to run the callback)."""
         hits = self._ray_hits(point1, point2)
         if callback is not None:
             self._ray_walk(hits, lambda entry: callback(*entry))
-            return None
+            return iter(())
         return self._ray_generator(hits)
 
     def _ray_hits(self, point1, point2):
@@ -1334,17 +1361,48 @@ class World:
         self._sync_device()
         return self._gpu, 0
 
+    def _moves(self):
+        """The move buffer with each proxy at its first position: pairs are
+        found once per moved proxy, ordered by that position, so a proxy
+        touched again before the step (a second filter change) adds
+        nothing (broadphase.py:83-109 collects the pairs in a set)."""
+        M = self._M
+        if len(M) == 0:
+            return M
+        return M[np.sort(np.unique(M, return_index=True)[1])].astype(np.int32)
+
     def _fixture_at(self, f):
+        return self._fixture_child_at(f)[0]
+
+    def _fixture_child_at(self, f):
+        """The fixture of record f and the child index of the record (a loop
+        fixture has one record per child, fixture.py:250-261)."""
         bi = int(self._F[f]["body"])
-        return self._bodies[bi].fixtures[f - int(self._B[bi]["fixture_start"])]
+        local = f - int(self._B[bi]["fixture_start"])
+        for fx in self._bodies[bi].fixtures:
+            n = fx.shape.child_count
+            if local < n:
+                return fx, local
+            local -= n
+        raise IndexError(f"fixture record {f} is past its body's fixtures")
+
+    def _records_of(self, body, fixture):
+        """(first record, record count) of a fixture of a body in the world"""
+        o = int(self._B[body._index]["fixture_start"])
+        for fx in body.fixtures:
+            if fx is fixture:
+                return o, fx.shape.child_count
+            o += fx.shape.child_count
+        raise ValueError("This fixture does not belong to this body")
 
     def _sync_device(self):
         if self._gpu is None:
-            W = self._sb.world_record(len(self._B), len(self._F), len(self._M))
+            M = self._moves()
+            W = self._sb.world_record(len(self._B), len(self._F), len(M))
             W["contact_count"] = len(self._C)
             W["contact_capacity"] = self._contact_capacity
             W["inv_dt0"] = self._inv_dt0
-            self._gpu = self._make_batch(W, self._B, self._F, self._C, self._M, self._J)
+            self._gpu = self._make_batch(W, self._B, self._F, self._C, M, self._J)
             self._host_fresh = True
             self._upload_bodies = False
             self._upload_joints = False
@@ -1374,15 +1432,17 @@ class World:
         r = self._B[bi]
         for key in ("lcx", "lcy", "c0x", "c0y", "cx", "cy", "vx", "vy", "mass", "inv_mass", "I", "inv_I"):
             r[key] = rb[key]
-        pos = int(r["fixture_start"]) + len(body.fixtures)
-        self._F = np.insert(self._F, pos, rf[-1])
-        self._B["fixture_count"][bi] += 1
-        self._B["fixture_start"] = np.where(np.arange(len(self._B)) > bi, self._B["fixture_start"] + 1,
+        n = fixture.shape.child_count
+        pos = int(r["fixture_start"]) + int(r["fixture_count"])
+        self._F = np.insert(self._F, pos, rf[-n:])
+        self._B["fixture_count"][bi] += n
+        self._B["fixture_start"] = np.where(np.arange(len(self._B)) > bi, self._B["fixture_start"] + n,
                                             self._B["fixture_start"])
         for key in ("fixture_a", "fixture_b"):
-            self._C[key] = np.where(self._C[key] >= pos, self._C[key] + 1, self._C[key])
-        M = np.where(self._M >= pos, self._M + 1, self._M)
-        self._M = np.concatenate([M, np.array([pos], np.int32)]).astype(np.int32)
+            self._C[key] = np.where(self._C[key] >= pos, self._C[key] + n, self._C[key])
+        M = np.where(self._M >= pos, self._M + n, self._M)
+        new = np.arange(pos, pos + n, dtype=np.int32) if b.active else np.zeros(0, np.int32)
+        self._M = np.concatenate([M, new]).astype(np.int32)
         fixture._body, fixture._slot = body, len(body.fixtures)
         body.fixtures.append(fixture)
 
@@ -1403,19 +1463,22 @@ class World:
         self._structural()
         body = fixture._body
         bi, k = body._index, fixture._slot
-        fi = int(self._B[bi]["fixture_start"]) + k
-        r = self._F[fi]
-        r["friction"], r["restitution"], r["density"] = fixture.friction, fixture.restitution, fixture.density
-        r["category_bits"], r["mask_bits"], r["group_index"] = fixture.category_bits, fixture.mask_bits, fixture.group_index
-        r["flags"] = (int(r["flags"]) | abi.FIX_SENSOR) if fixture.sensor else (int(r["flags"]) & ~abi.FIX_SENSOR)
+        fi, n = self._records_of(body, fixture)
+        for r in self._F[fi:fi + n]:
+            r["friction"], r["restitution"], r["density"] = fixture.friction, fixture.restitution, fixture.density
+            r["category_bits"], r["mask_bits"], r["group_index"] = fixture.category_bits, fixture.mask_bits, fixture.group_index
+            r["flags"] = (int(r["flags"]) | abi.FIX_SENSOR) if fixture.sensor else (int(r["flags"]) & ~abi.FIX_SENSOR)
         sf = self._sb.bodies[bi].fixtures[k]
         sf.friction, sf.restitution, sf.density = fixture.friction, fixture.restitution, fixture.density
         sf.category, sf.mask, sf.group, sf.sensor = fixture.category_bits, fixture.mask_bits, fixture.group_index, fixture.sensor
         if refilter:
             C = self._C
-            C["flags"] = np.where((C["fixture_a"] == fi) | (C["fixture_b"] == fi), C["flags"] | abi.C_FILTER, C["flags"])
-            self._M = np.concatenate([self._M, np.array([fi], np.int32)]).astype(np.int32)
-            self._sb.moves.append((bi, k))
+            mine = lambda x: (x >= fi) & (x < fi + n)   # noqa: E731
+            C["flags"] = np.where(mine(C["fixture_a"]) | mine(C["fixture_b"]), C["flags"] | abi.C_FILTER, C["flags"])
+            if int(self._B[bi]["flags"]) & abi.BODY_ACTIVE:
+                self._M = np.concatenate([self._M, np.arange(fi, fi + n, dtype=np.int32)]).astype(np.int32)
+                o = fi - int(self._B[bi]["fixture_start"])
+                self._sb.moves.extend((bi, o + c) for c in range(n))
 
     def _set_type(self, body, t):
         self._structural()
@@ -1449,8 +1512,10 @@ class World:
         bi = body._index
         k = body.fixtures.index(fixture)
         B, F, C, M = self._B, self._F, self._C, self._M
-        fi = int(B[bi]["fixture_start"]) + k
-        hit = (C["fixture_a"] == fi) | (C["fixture_b"] == fi)
+        fi, n = self._records_of(body, fixture)
+        o = fi - int(B[bi]["fixture_start"])
+        gone = lambda x: (x >= fi) & (x < fi + n)   # noqa: E731
+        hit = gone(C["fixture_a"]) | gone(C["fixture_b"])
         if self.contact_manager.end_contact is not None:
             for c in C[hit]:
                 if int(c["flags"]) & abi.C_TOUCHING:
@@ -1458,20 +1523,19 @@ class World:
                                                                   self._fixture_at(int(c["fixture_b"])), False))
         C = C[~hit].copy()
         for key in ("fixture_a", "fixture_b"):
-            C[key] = np.where(C[key] > fi, C[key] - 1, C[key])
-        M = M[M != fi]
-        M = np.where(M > fi, M - 1, M).astype(np.int32)
-        F = np.delete(F, fi)
-        B["fixture_count"][bi] -= 1
-        B["fixture_start"] = np.where(np.arange(len(B)) > bi, B["fixture_start"] - 1, B["fixture_start"])
+            C[key] = np.where(C[key] >= fi + n, C[key] - n, C[key])
+        M = M[~gone(M)]
+        M = np.where(M >= fi + n, M - n, M).astype(np.int32)
+        F = np.delete(F, np.arange(fi, fi + n))
+        B["fixture_count"][bi] -= n
+        B["fixture_start"] = np.where(np.arange(len(B)) > bi, B["fixture_start"] - n, B["fixture_start"])
         # the construction-time body: current state, fixture gone, mass data reset
         b = self._sb.bodies[bi]
         _load_body_state(b, B[bi])
         b.fixtures.pop(k)
-        if k < len(b.aabbs):
-            b.aabbs.pop(k)
-        self._sb.moves = [(bb, kk - 1 if (bb == bi and kk > k) else kk) for (bb, kk) in self._sb.moves
-                          if not (bb == bi and kk == k)]
+        del b.aabbs[o:o + n]
+        self._sb.moves = [(bb, kk - n if (bb == bi and kk >= o + n) else kk) for (bb, kk) in self._sb.moves
+                          if not (bb == bi and o <= kk < o + n)]
         b.reset_mass_data()
         rb, _ = self._sb.body_records(bi)
         for key in ("lcx", "lcy", "c0x", "c0y", "cx", "cy", "vx", "vy", "mass", "inv_mass", "I", "inv_I"):
@@ -1506,8 +1570,7 @@ class World:
         if active:
             r["flags"] |= abi.BODY_ACTIVE
             pos, q = (float(r["px"]), float(r["py"])), (float(r["qc"]), float(r["qs"]))
-            for k, f in enumerate(b.fixtures):
-                lx, ly, ux, uy = f.shape.compute_aabb(pos, q)
+            for k, (lx, ly, ux, uy) in enumerate(_record_aabbs(b.fixtures, pos, q)):
                 F[f0 + k]["aabb"] = (lx - AABB_EXTENSION, ly - AABB_EXTENSION, ux + AABB_EXTENSION, uy + AABB_EXTENSION)
             self._M = np.concatenate([self._M, np.arange(f0, f0 + nfix, dtype=np.int32)]).astype(np.int32)
             self._sb.moves.extend((bi, k) for k in range(nfix))
@@ -1542,8 +1605,7 @@ class World:
         r["a0"] = r["a"] = angle
         start = int(r["fixture_start"])
         moved = []
-        for k, f in enumerate(self._sb.bodies[bi].fixtures):
-            tight = f.shape.compute_aabb(pos, q)
+        for k, tight in enumerate(_record_aabbs(self._sb.bodies[bi].fixtures, pos, q)):
             fat = tuple(float(x) for x in self._F[start + k]["aabb"])
             if not _contains(fat, tight):
                 self._F[start + k]["aabb"] = (tight[0] - AABB_EXTENSION, tight[1] - AABB_EXTENSION,
@@ -1551,6 +1613,19 @@ class World:
                 moved.append(start + k)
         if moved:
             self._M = np.concatenate([self._M, np.array(moved, np.int32)]).astype(np.int32)
+
+
+def _record_aabbs(fixtures, p, q):
+    """The tight AABB of every fixture record under transform (p, q): one per
+    child of a loop (shapes.py:822-837), one per other shape."""
+    out = []
+    for f in fixtures:
+        sh = f.shape
+        if isinstance(sh, Loop):
+            out.extend(sh.compute_aabb(p, q, c) for c in range(sh.child_count))
+        else:
+            out.append(sh.compute_aabb(p, q))
+    return out
 
 
 _EPSILON_SQR = 2.220446049250313e-16 ** 2       # settings.py EPSILON_SQR
@@ -1678,11 +1753,12 @@ class WorldBatch:
         recs, Js = [], []
         for i, w in enumerate(worlds):
             w._materialise()
-            W = w._sb.world_record(len(w._B), len(w._F), len(w._M))
+            M = w._moves()
+            W = w._sb.world_record(len(w._B), len(w._F), len(M))
             W["contact_count"] = len(w._C)
             W["contact_capacity"] = w._contact_capacity
             W["inv_dt0"] = w._inv_dt0
-            recs.append((W, w._B, w._F, w._C, w._M))
+            recs.append((W, w._B, w._F, w._C, M))
             J = w._J.copy()
             J["world"] = i
             Js.append(J)

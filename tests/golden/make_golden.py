@@ -53,12 +53,15 @@ def load_reference(ref_root: str):
 
 
 def fixture_index(world):
+    """id(fixture) -> its first record; a loop fixture takes one record per
+    child (its proxies, fixture.py:250-261), so proxy (f, child) is record
+    idx[id(f)] + child."""
     idx = {}
     k = 0
     for body in world.bodies:
         for f in body.fixtures:
             idx[id(f)] = k
-            k += 1
+            k += f._shape.child_count
     return idx
 
 
@@ -87,7 +90,7 @@ def install_hooks(world, b2, order_log):
                     continue
                 if res in first and first[res] < pos:
                     continue
-                pairs.append((pos, fidx[id(res.user_data.fixture)], node, res))
+                pairs.append((pos, fidx[id(res.user_data.fixture)] + res.user_data.child_index, node, res))
         self._move_buffer = []
         pairs.sort(key=lambda t: (t[0], t[1]))
         for _, _, a, b in pairs:
@@ -113,7 +116,7 @@ def export_world(world, b2, contacts=True):
     """Reference world -> (worlds, bodies, fixtures, contacts) record arrays."""
     fidx = fixture_index(world)
     nb = len(world.bodies)
-    nf = sum(len(b.fixtures) for b in world.bodies)
+    nf = sum(f._shape.child_count for b in world.bodies for f in b.fixtures)
     B = np.zeros(nb, dtype=abi.BODY)
     F = np.zeros(nf, dtype=abi.FIXTURE)
     k = 0
@@ -133,7 +136,7 @@ def export_world(world, b2, contacts=True):
             fl |= abi.BODY_ACTIVE
         r["flags"] = fl
         r["fixture_start"] = k
-        r["fixture_count"] = len(body.fixtures)
+        r["fixture_count"] = sum(f._shape.child_count for f in body.fixtures)
         xf = body._xf
         r["px"], r["py"] = xf.position.x, xf.position.y
         rot = xf.rotation
@@ -151,15 +154,17 @@ def export_world(world, b2, contacts=True):
         r["linear_damping"], r["angular_damping"] = body._linear_damping, body._angular_damping
         r["gravity_scale"] = body._gravity_scale
         r["sleep_time"] = body._sleep_time
-        for f in body.fixtures:
+        for f, child, sh in ((f, c, f._shape.child_edge(c) if f._shape._type == abi.SHAPE_LOOP else f._shape)
+                             for f in body.fixtures for c in range(f._shape.child_count)):
             q = F[k]
-            sh = f._shape
             q["body"] = i
             q["shape_type"] = sh._type
             q["radius"] = sh.radius
             q["friction"], q["restitution"], q["density"] = f._friction, f._restitution, f._density
             q["category_bits"], q["mask_bits"], q["group_index"] = f._category_bits, f._mask_bits, f._group_index
             fl = abi.FIX_SENSOR if f._sensor else 0
+            if f._shape._type == abi.SHAPE_LOOP:
+                fl |= abi.FIX_LOOP_CHILD
             if sh._type == abi.SHAPE_CIRCLE:
                 q["vertex_count"] = 1
                 q["vx"][0], q["vy"][0] = sh.position.x, sh.position.y
@@ -179,10 +184,10 @@ def export_world(world, b2, contacts=True):
                     fl |= abi.FIX_EDGE_HAS_V3
                     q["vx"][3], q["vy"][3] = sh._vertex3.x, sh._vertex3.y
             else:
-                raise NotImplementedError("loop shapes are not exported")
+                raise NotImplementedError(f"shape type {sh._type} is not exported")
             q["flags"] = fl
-            if f._proxies and f._proxies[0].proxy_ref is not None:
-                aabb = f._proxies[0].proxy_ref.aabb
+            if f._proxies and f._proxies[child].proxy_ref is not None:
+                aabb = f._proxies[child].proxy_ref.aabb
                 q["aabb"][:] = (aabb.lower_bound.x, aabb.lower_bound.y, aabb.upper_bound.x, aabb.upper_bound.y)
             else:   # an inactive body's fixture has no proxy (body.py:846-872)
                 q["aabb"][:] = np.nan
@@ -191,8 +196,9 @@ def export_world(world, b2, contacts=True):
     C = np.zeros(len(clist), dtype=abi.CONTACT)
     for i, c in enumerate(clist):
         r = C[i]
-        r["fixture_a"], r["fixture_b"] = fidx[id(c._fixture_a)], fidx[id(c._fixture_b)]
-        r["child_a"], r["child_b"] = c._index_a, c._index_b
+        # a loop's child is its own record: the child index goes into the
+        # record index, the child fields stay 0
+        r["fixture_a"], r["fixture_b"] = fidx[id(c._fixture_a)] + c._index_a, fidx[id(c._fixture_b)] + c._index_b
         fl = 0
         for bit, name in ((abi.C_TOUCHING, "_touching_flag"), (abi.C_ENABLED, "_enabled_flag"),
                           (abi.C_FILTER, "_filter_flag"), (abi.C_ISLAND, "_island_flag"),
@@ -544,6 +550,40 @@ def scene_bridge(b2, planks=30, seed=19):
     return world
 
 
+def scene_loops(b2, seed=23):
+    """Loop shapes: a static closed terrain loop (a valley with a hill whose
+    top vertex is the body's origin, so its neighbouring child edges lose
+    vertex0 / vertex3), a two-vertex loop as a shelf, a static sensor loop,
+    a dynamic body carrying a triangle loop beside a circle, circles and
+    convex polygons dropped into the valley and a bullet circle fired at
+    the terrain (continuous collision against loop children)."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    terrain = world.create_static_body(position=(0, -2))
+    terrain.create_loop_fixture([(-15, 8), (-15, -2), (-9, -3), (-4, -3), (0, 0), (4, -3), (9, -2.5), (15, -2),
+                                 (15, 8)], friction=0.6)
+    shelf = world.create_static_body(position=(-10, 2))
+    shelf.create_loop_fixture([(-2, 0), (2, 0.5)], friction=0.4)
+    gate = world.create_static_body(position=(6, -1))
+    gate.create_loop_fixture([(-1, -1), (1, -1), (1, 1), (-1, 1)], sensor=True)
+    frame = world.create_dynamic_body(position=(7, 2), angle=0.3)
+    frame.create_loop_fixture([(-0.8, -0.5), (0.8, -0.5), (0, 0.7)], friction=0.5)
+    frame.create_circle_fixture(radius=0.25, density=2.0, friction=0.5)
+    for i in range(22):
+        x, y = rng.uniform(-13, 13), rng.uniform(-1, 4.5)
+        body = world.create_dynamic_body(position=(x, y), angle=rng.uniform(-2, 2),
+                                         linear_velocity=(rng.gauss(0, 1.5), rng.gauss(0, 1.5)))
+        if i % 2 == 0:
+            body.create_circle_fixture(radius=rng.uniform(0.2, 0.5), density=rng.uniform(0.5, 3), friction=0.4,
+                                       restitution=rng.uniform(0, 0.3))
+        else:
+            body.create_polygon_fixture(vertices=random_convex(rng, rng.randint(3, 7), rng.uniform(0.3, 0.6)),
+                                        density=rng.uniform(0.5, 3), friction=0.5)
+    world.create_dynamic_body(position=(-12, 5), bullet=True, linear_velocity=(90.0, -40.0)).create_circle_fixture(
+        radius=0.1, density=50.0)
+    return world
+
+
 SCENES = {
     "pyramid": (scene_pyramid, 300, (1, 2, 3, 5, 10, 30, 31, 100, 101, 200, 201, 300)),
     "pyramid5": (lambda b2: scene_pyramid(b2, rows=5), 150, (1, 2, 5, 20, 21, 60, 61, 150)),
@@ -555,6 +595,7 @@ SCENES = {
     "sensor_filter": (scene_sensor_filter, 150, (1, 2, 5, 20, 21, 40, 60, 61, 90, 120, 121, 150)),
     "joints": (scene_joints, 300, (1, 2, 5, 20, 21, 60, 61, 120, 121, 200, 201, 300)),
     "bridge": (scene_bridge, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
+    "loops": (scene_loops, 180, (1, 2, 5, 20, 21, 60, 61, 120, 121, 180)),
 }
 
 
@@ -611,7 +652,7 @@ def pair_order_hook(world):
                     continue
                 if res in first and first[res] < pos:
                     continue
-                pairs.append((pos, fidx[id(res.user_data.fixture)], node, res))
+                pairs.append((pos, fidx[id(res.user_data.fixture)] + res.user_data.child_index, node, res))
         self._move_buffer = []
         pairs.sort(key=lambda t: (t[0], t[1]))
         for _, _, a, b in pairs:
@@ -689,6 +730,25 @@ def run_api_active(b2):
     print(f"api_active: {len(api_active.SNAPS)} snapshots -> {os.path.getsize(path)} bytes")
 
 
+def run_api_loops(b2):
+    """tests/golden/api_loops.py on the reference -> api_loops.npz."""
+    sys.path.insert(0, HERE)
+    import api_loops
+    out = {}
+
+    def snap(label, world):
+        W, B, F, C = export_world(world, b2)
+        out[f"{label}_bodies"], out[f"{label}_aabb"], out[f"{label}_contacts"] = B, F["aabb"].copy(), C
+        rays, queries = api_loops.probes(b2, world)
+        out[f"{label}_rays"] = np.array(rays, dtype=np.float64)
+        out[f"{label}_queries"] = np.array(queries, dtype=np.float64)
+
+    api_loops.script(b2, snap, on_world=pair_order_hook)
+    path = os.path.join(HERE, "api_loops.npz")
+    np.savez_compressed(path, **out)
+    print(f"api_loops: {len(api_loops.SNAPS)} snapshots -> {os.path.getsize(path)} bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("GB2D_REFERENCE"), required="GB2D_REFERENCE" not in os.environ,
@@ -706,6 +766,8 @@ def main():
         run_api_joints(b2)
     if not args.only or args.only == "api_active":
         run_api_active(b2)
+    if not args.only or args.only == "api_loops":
+        run_api_loops(b2)
 
 
 if __name__ == "__main__":

@@ -179,6 +179,16 @@ class OracleBatch:
 
     def __init__(self, W, B, F, C, M, libm=False, joints=None):
         self.o = OracleWorld(W, B, F, C if len(C) else None, libm=libm, moves=M, joints=joints)
+        self.libm = libm
+
+    def query_aabb(self, q, max_per_query):
+        return query_aabb_records(self.o.fixtures(), q, max_per_query, libm=self.libm)
+
+    def ray_cast(self, r):
+        return ray_cast_records(self.o.bodies(), self.o.fixtures(), r, libm=self.libm)
+
+    def ray_cast_all(self, r, max_per_ray):
+        return ray_cast_all_records(self.o.bodies(), self.o.fixtures(), r, max_per_ray, libm=self.libm)
 
     def step(self, dt, vel_iters, pos_iters, n_steps=1, **_):
         for _ in range(n_steps):

@@ -59,10 +59,6 @@ def test_unsupported_features_raise():
         b2.World(sub_stepping=True)
     with pytest.raises(NotImplementedError):
         b2.World(contact_filter=lambda a, b: True)
-    w = b2.World()
-    body = w.create_dynamic_body()
-    with pytest.raises(NotImplementedError):
-        body.create_loop_fixture([(0, 0), (1, 0), (1, 1)])
 
 
 def test_pre_step_edits_stay_on_the_host():

@@ -198,8 +198,8 @@ def test_manifold_view_decodes_feature_ids():
     c = next(r for r in C if r["m_point_count"] == 2)
 
     class _W:            # the two fixture lookups a Contact makes
-        def _fixture_at(self, f):
-            return f
+        def _fixture_child_at(self, f):
+            return f, 0
     m = Contact(_W(), c).manifold
     assert m.type == int(c["m_type"]) and m.point_count == 2
     for k, p in enumerate(m.points):
