@@ -61,6 +61,8 @@ extern "C" {
                                  (shapes.py:822-837); a loop fixture of n vertices is n consecutive edge
                                  records, child i from vertex i to i+1 with vertices i-1 and i+2 as
                                  vertex0/vertex3 (shapes.py:851-863) */
+#define GB_FIX_LOOP_FIRST 16u /* the first child record of a loop fixture: a buoyancy controller sums a
+                                 loop's children before it adds them to the body (shapes.py:866-882) */
 
 /* gb_contact.flags, as the Contact._*_flag attributes of contact.py:75-87 */
 #define GB_C_TOUCHING 1u
@@ -213,6 +215,37 @@ typedef struct gb_joint {
     double perp_x, perp_y;         /* last set-up: prismatic _perp */
 } gb_joint;
 
+/* controller kinds (pypybox2d/controllers.py) */
+#define GB_CONTROLLER_BUOYANCY 1
+#define GB_CONTROLLER_GRAVITY 2
+
+/* gb_controller.flags */
+#define GB_CTRL_OWN_GRAVITY 1u  /* buoyancy: gravity_x/y given (a gravity of None or (0, 0) takes the world's) */
+#define GB_CTRL_INV_SQR 2u      /* gravity: force falls off as 1/r^2 (else 1/r) */
+
+/* One controller (controllers.py:24-280): a force rule applied to a list of
+ * bodies at the start of the solve of every step (world.py:476-479), before
+ * the islands are built.  Controllers of a batch are sorted by world; within
+ * a world they are in World.controllers order, which is the order they run
+ * in.  The controller's bodies are controller_bodies[body_start ..
+ * body_start + body_count): world-local body indices in the controller's
+ * own body order (Controller.add_body order), which is the order of the
+ * gravity controller's pair loop. */
+typedef struct gb_controller {
+    int32_t world;                 /* world of the batch */
+    int32_t type;                  /* GB_CONTROLLER_* */
+    int32_t body_start, body_count;
+    uint32_t flags;                /* GB_CTRL_* */
+    int32_t _pad0;
+    double normal_x, normal_y;     /* buoyancy: the fluid's outer surface normal (as given, not normalised) */
+    double offset;                 /* buoyancy: height of the surface along the normal */
+    double density;                /* buoyancy: fluid density */
+    double velocity_x, velocity_y; /* buoyancy: fluid velocity (drag) */
+    double linear_drag, angular_drag;
+    double gravity_x, gravity_y;   /* buoyancy: with GB_CTRL_OWN_GRAVITY */
+    double G;                      /* gravity controller: strength */
+} gb_controller;
+
 /* One world of a batch. */
 typedef struct gb_world_desc {
     int32_t body_start, body_count;       /* into the batch body array */
@@ -240,6 +273,9 @@ typedef struct gb_scene {
     const int32_t *moves;                 /* world-local fixture indices (BroadPhase._move_buffer) */
     int32_t n_joints, _pad1;
     const gb_joint *joints;               /* sorted by world (NULL when n_joints is 0) */
+    int32_t n_controllers, n_controller_bodies;
+    const gb_controller *controllers;     /* sorted by world (NULL when n_controllers is 0) */
+    const int32_t *controller_bodies;     /* world-local body indices of the controllers' body lists */
 } gb_scene;
 
 typedef struct gb_batch gb_batch; /* opaque device-resident batch of worlds */
@@ -269,6 +305,8 @@ const char *gb_last_error(void);
 int gb_struct_sizes(int32_t *sizes);
 /* sizeof(gb_joint). */
 int gb_joint_size(void);
+/* sizeof(gb_controller). */
+int gb_controller_size(void);
 
 /* One contact event of a step, replayed to the contact listeners after it.
  * `key` orders a world's events: (step of the call) << 48 | phase << 40 |
@@ -319,6 +357,11 @@ int gb_batch_get_joint_order(gb_batch *batch, int32_t world, int32_t *order, int
  * the ones the batch was made with. */
 int gb_batch_get_joints(gb_batch *batch, gb_joint *joints, int32_t n_joints, void *cuda_stream);
 int gb_batch_set_joints(gb_batch *batch, const gb_joint *joints, int32_t n_joints, void *cuda_stream);
+/* Overwrite the parameters of the batch's controllers (scene order): the
+ * setters of BuoyancyController / GravityController between steps.  The
+ * world, kind and body list range of each controller must be the ones the
+ * batch was made with (a changed body list needs a new batch). */
+int gb_batch_set_controllers(gb_batch *batch, const gb_controller *controllers, int32_t n_controllers, void *cuda_stream);
 /* Step record of one world's bodies (world-local order) from the last step
  * run with record_order bit 0 set: out[0..n) the decisions of each body,
  * out[n..2n) its island in the solve (the smallest world-local index of the

@@ -128,6 +128,10 @@ struct or_world {
     int *jhook_rank;      /* joint solver order hook: rank per joint */
     int jhook_set;
     ivec last_jorder;     /* joints in solver order, last _solve */
+    /* controllers (World.controllers order) and their body lists */
+    gb_controller *ctl;
+    int nctl;
+    int *ctl_bodies;
 };
 
 static void rec_add(int *x, int shift, int v) {
@@ -830,7 +834,10 @@ static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts,
 }
 
 /* world.py:475-592 World._solve */
+#include "oracle_controllers.h"
+
 static void world_solve(or_world *w, double dt, double inv_dt, double dt_ratio, int vel_iters, int pos_iters) {
+    controllers_step(w);   /* world.py:476-479 */
     int nb = w->nb;
     int *bflag = w->island_flag_b;
     for (int i = 0; i < nb; ++i) bflag[i] = 0;
@@ -1183,6 +1190,7 @@ void or_destroy(or_world *w) {
     if (w->bjoint)
         for (int i = 0; i < w->nb; ++i) free(w->bjoint[i].d);
     free(w->bjoint); free(w->j); free(w->jflag); free(w->jhook_rank); free(w->last_jorder.d);
+    free(w->ctl); free(w->ctl_bodies);
     free(w->c); free(w->b); free(w->f);
     free(w);
 }
@@ -1300,6 +1308,45 @@ typedef struct {
     pthread_mutex_t mu;
 } or_job;
 
+/* The controllers of a world (World.controllers order) with their body
+ * lists: controller k's bodies are bodies[ctl[k].body_start ..
+ * + ctl[k].body_count), world-local.  Replaces any controllers given before;
+ * returns -1 (keeping the old ones) for a bad kind or body index. */
+int or_set_controllers(or_world *w, const gb_controller *ctl, int n, const int32_t *bodies, int nbodies) {
+    if (n < 0) return -1;
+    size_t total = 0;
+    for (int k = 0; k < n; ++k) {
+        const gb_controller *C = &ctl[k];
+        if (C->type < GB_CONTROLLER_BUOYANCY || C->type > GB_CONTROLLER_GRAVITY || C->body_count < 0 || C->body_start < 0 ||
+            C->body_start + C->body_count > nbodies)
+            return -1;
+        for (int i = 0; i < C->body_count; ++i)
+            if (bodies[C->body_start + i] < 0 || bodies[C->body_start + i] >= w->nb) return -1;
+        total += (size_t)C->body_count;
+    }
+    w->ctl = (gb_controller *)realloc(w->ctl, sizeof(gb_controller) * (n > 0 ? (size_t)n : 1u));
+    w->ctl_bodies = (int *)realloc(w->ctl_bodies, sizeof(int) * (total ? total : 1));
+    int at = 0;
+    for (int k = 0; k < n; ++k) {
+        w->ctl[k] = ctl[k];
+        for (int i = 0; i < ctl[k].body_count; ++i) w->ctl_bodies[at + i] = bodies[ctl[k].body_start + i];
+        w->ctl[k].body_start = at;
+        at += ctl[k].body_count;
+    }
+    w->nctl = n;
+    return 0;
+}
+
+/* the controllers of world `wi` of a scene (sorted by world) */
+static void scene_controllers(or_world *w, const gb_scene *scene, int wi) {
+    if (scene->n_controllers <= 0 || !scene->controllers) return;
+    int s0 = 0;
+    while (s0 < scene->n_controllers && scene->controllers[s0].world < wi) ++s0;
+    int s1 = s0;
+    while (s1 < scene->n_controllers && scene->controllers[s1].world == wi) ++s1;
+    if (s1 > s0) or_set_controllers(w, scene->controllers + s0, s1 - s0, scene->controller_bodies, scene->n_controller_bodies);
+}
+
 /* the joints of world `wi` of a scene (sorted by world) */
 static void scene_joints(or_world *w, const gb_scene *scene, int wi) {
     if (scene->n_joints <= 0 || !scene->joints) return;
@@ -1320,6 +1367,7 @@ static void *or_worker(void *arg) {
         const gb_world_desc *wd = &j->scene->worlds[wi];
         or_world *w = or_create(wd, j->scene->bodies, j->scene->fixtures, j->scene->contacts, j->scene->moves);
         scene_joints(w, j->scene, wi);
+        scene_controllers(w, j->scene, wi);
         for (int s = 0; s < j->steps; ++s) or_step(w, j->dt, j->vi, j->pi);
         if (j->out) or_get_bodies(w, j->out + wd->body_start);
         or_destroy(w);
@@ -1359,6 +1407,7 @@ or_batch *or_batch_create(const gb_scene *scene) {
     for (int i = 0; i < b->n; ++i) {
         b->w[i] = or_create(&scene->worlds[i], scene->bodies, scene->fixtures, scene->contacts, scene->moves);
         scene_joints(b->w[i], scene, i);
+        scene_controllers(b->w[i], scene, i);
     }
     return b;
 }

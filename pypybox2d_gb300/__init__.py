@@ -6,4 +6,6 @@ from .errors import (CapacityError, ContactOverflowError, EmptyFixtureError, Loc
                      PhysicsError, StepError, WaitTimeoutError)
 from .world import AABB, Body, Contact, ContactManager, EventContact, Fixture, Vec2, World, WorldBatch  # noqa: E402,F401
 from . import joints  # noqa: E402,F401
+from . import controllers  # noqa: E402,F401
+from .controllers import BuoyancyController, Controller, GravityController  # noqa: E402,F401
 from .joints import DistanceJoint, Joint, PrismaticJoint, RevoluteJoint, WeldJoint  # noqa: E402,F401

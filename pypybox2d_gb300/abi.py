@@ -27,6 +27,7 @@ FIX_SENSOR = 1
 FIX_EDGE_HAS_V0 = 2
 FIX_EDGE_HAS_V3 = 4
 FIX_LOOP_CHILD = 8      # one child edge of a loop fixture (no radius margin on its box)
+FIX_LOOP_FIRST = 16     # the first child record of a loop fixture
 
 C_TOUCHING = 1
 C_ENABLED = 2
@@ -99,6 +100,17 @@ JOINT = np.dtype([
     ("ux", "<f8"), ("uy", "<f8"), ("perp_x", "<f8"), ("perp_y", "<f8"),
 ], align=True)
 
+CONTROLLER_BUOYANCY, CONTROLLER_GRAVITY = 1, 2
+CTRL_OWN_GRAVITY, CTRL_INV_SQR = 1, 2
+
+#: ``gb_controller``: one controller (controllers.py) with its body-list range
+CONTROLLER = np.dtype([
+    ("world", "<i4"), ("type", "<i4"), ("body_start", "<i4"), ("body_count", "<i4"), ("flags", "<u4"), ("_pad0", "<i4"),
+    ("normal_x", "<f8"), ("normal_y", "<f8"), ("offset", "<f8"), ("density", "<f8"),
+    ("velocity_x", "<f8"), ("velocity_y", "<f8"), ("linear_drag", "<f8"), ("angular_drag", "<f8"),
+    ("gravity_x", "<f8"), ("gravity_y", "<f8"), ("G", "<f8"),
+], align=True)
+
 WORLD = np.dtype([
     ("body_start", "<i4"), ("body_count", "<i4"), ("fixture_start", "<i4"), ("fixture_count", "<i4"),
     ("contact_start", "<i4"), ("contact_count", "<i4"), ("contact_capacity", "<i4"), ("flags", "<u4"),
@@ -116,6 +128,8 @@ class Scene(ctypes.Structure):
         ("fixtures", ctypes.c_void_p), ("contacts", ctypes.c_void_p),
         ("n_moves", ctypes.c_int32), ("_pad0", ctypes.c_int32), ("moves", ctypes.c_void_p),
         ("n_joints", ctypes.c_int32), ("_pad1", ctypes.c_int32), ("joints", ctypes.c_void_p),
+        ("n_controllers", ctypes.c_int32), ("n_controller_bodies", ctypes.c_int32),
+        ("controllers", ctypes.c_void_p), ("controller_bodies", ctypes.c_void_p),
     ]
 
 
@@ -156,10 +170,13 @@ LAUNCH_CONFIG_BYTES = 32
 
 def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,
                contacts: np.ndarray | None = None, moves: np.ndarray | None = None,
-               joints: np.ndarray | None = None) -> tuple[Scene, tuple]:
+               joints: np.ndarray | None = None, controllers: np.ndarray | None = None,
+               controller_bodies: np.ndarray | None = None) -> tuple[Scene, tuple]:
     """Pack contiguous record arrays into a ``gb_scene``; the returned tuple
     keeps the arrays alive as long as the scene is used.  ``joints`` are
-    sorted by their ``world`` field (stable: each world keeps its order)."""
+    sorted by their ``world`` field (stable: each world keeps its order);
+    ``controllers`` must already be sorted by world, their ``body_start``
+    indexing ``controller_bodies``."""
     worlds = np.ascontiguousarray(worlds, dtype=WORLD)
     bodies = np.ascontiguousarray(bodies, dtype=BODY)
     fixtures = np.ascontiguousarray(fixtures, dtype=FIXTURE)
@@ -183,7 +200,15 @@ def make_scene(worlds: np.ndarray, bodies: np.ndarray, fixtures: np.ndarray,
         joints = joints[np.argsort(joints["world"], kind="stable")]
     s.n_joints = len(joints)
     s.joints = joints.ctypes.data if len(joints) else None
-    return s, (worlds, bodies, fixtures, contacts, moves, joints)
+    controllers = np.ascontiguousarray(controllers if controllers is not None else np.zeros(0, CONTROLLER),
+                                       dtype=CONTROLLER)
+    cbodies = np.ascontiguousarray(controller_bodies if controller_bodies is not None else np.zeros(0, np.int32),
+                                   dtype=np.int32)
+    s.n_controllers = len(controllers)
+    s.controllers = controllers.ctypes.data if len(controllers) else None
+    s.n_controller_bodies = len(cbodies)
+    s.controller_bodies = cbodies.ctypes.data if len(cbodies) else None
+    return s, (worlds, bodies, fixtures, contacts, moves, joints, controllers, cbodies)
 
 
 _PKG_DIR = os.path.dirname(os.path.abspath(__file__))
@@ -202,6 +227,7 @@ EXPORTED = (
     "gb_batch_snapshot_bytes", "gb_batch_snapshot", "gb_batch_restore", "gb_batch_get_step_record",
     "gb_batch_set_wait_polls", "gb_batch_clear_status",
     "gb_joint_size", "gb_batch_get_joint_order", "gb_batch_get_joints", "gb_batch_set_joints",
+    "gb_controller_size", "gb_batch_set_controllers",
 )
 
 #: gb_step_opts.record_order bit that records contact events
@@ -282,6 +308,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_get_joint_order.argtypes = [vp, i32, i32p, i32, i32p, vp]
     lib.gb_batch_get_joints.argtypes = [vp, vp, i32, vp]
     lib.gb_batch_set_joints.argtypes = [vp, vp, i32, vp]
+    lib.gb_controller_size.argtypes = []
+    lib.gb_batch_set_controllers.argtypes = [vp, vp, i32, vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

@@ -45,7 +45,7 @@ struct Arena {
     }
 };
 
-template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap, int nj) {
+template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int ncap, int nj, int nctl, int nctlb) {
     B.n_worlds = nw;
     B.n_bodies = nb;
     B.n_slots = ncap;
@@ -105,6 +105,9 @@ template <class R> void carve(Arena &a, Batch<R> &B, int nw, int nb, int nf, int
     B.s_joff = a.take<int>(nj + nw);
     B.s_jvis = a.take<unsigned char>(nj);
     B.jorder_out = a.take<int>(nj);
+    B.n_ctl = nctl;
+    B.ctl = a.take<gb_controller>(nctl);
+    B.ctl_bodies = a.take<int>(nctlb);
 }
 // Re-points the per-step scratch arrays of a batch into one region laid out
 // by `a` (a.base == nullptr only measures it).  The state that outlives a step
@@ -156,6 +159,8 @@ struct WorldGroup {
 struct gb_batch {
     int prec = GB_PREC_F64;
     int nw = 0, nb = 0, nf = 0, ncap = 0, nj = 0;
+    int nctl = 0, nctlb = 0;       // controllers and the entries of their body lists
+    std::vector<gb_controller> controllers;   // at creation (world, kind and body lists are fixed for the batch)
     std::vector<WorldHdr> hdr;     // host copy of the headers at creation
     std::vector<gb_joint> joints;  // the joints at creation (world, type and bodies are fixed for the batch)
     std::vector<int> launch_order; // worlds sorted by body count, largest first
@@ -218,6 +223,7 @@ extern "C" {
 const char *gb_version(void) { return "gb2d 0.1 sm_103a"; }
 const char *gb_last_error(void) { return g_err.c_str(); }
 int gb_joint_size(void) { return (int)sizeof(gb_joint); }
+int gb_controller_size(void) { return (int)sizeof(gb_controller); }
 
 int gb_struct_sizes(int32_t *sizes) {
     if (!sizes) return fail(GB_E_ARG, "sizes is NULL");
@@ -314,13 +320,40 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         if (b->hdr[J.world].nj == 0) b->hdr[J.world].jbase = i;
         b->hdr[J.world].nj += 1;
     }
+    // controllers: sorted by world, known kinds, body lists inside the scene
+    // array and their bodies inside their world
+    if (scene->n_controllers < 0 || scene->n_controller_bodies < 0 ||
+        (scene->n_controllers > 0 && (!scene->controllers || (scene->n_controller_bodies > 0 && !scene->controller_bodies)))) {
+        delete b;
+        return fail(GB_E_ARG, "bad controller arrays");
+    }
+    b->nctl = scene->n_controllers;
+    b->nctlb = scene->n_controllers > 0 ? scene->n_controller_bodies : 0;
+    b->controllers.assign(scene->controllers, scene->controllers + b->nctl);
+    for (int i = 0; i < b->nctl; ++i) {
+        const gb_controller &C = b->controllers[i];
+        bool ok = C.world >= 0 && C.world < b->nw && (i == 0 || C.world >= b->controllers[i - 1].world) &&
+                  C.type >= GB_CONTROLLER_BUOYANCY && C.type <= GB_CONTROLLER_GRAVITY && C.body_start >= 0 &&
+                  C.body_count >= 0 && C.body_start + C.body_count <= b->nctlb;
+        for (int k = 0; ok && k < C.body_count; ++k) {
+            const int bi = scene->controller_bodies[C.body_start + k];
+            ok = bi >= 0 && bi < b->hdr[C.world].nb;
+        }
+        if (!ok) {
+            delete b;
+            return fail(C.type < GB_CONTROLLER_BUOYANCY || C.type > GB_CONTROLLER_GRAVITY ? GB_E_UNSUPPORTED : GB_E_ARG,
+                        "controller " + std::to_string(i) + ": world out of order, unknown kind or body outside its world");
+        }
+        if (b->hdr[C.world].nctl == 0) b->hdr[C.world].ctlbase = i;
+        b->hdr[C.world].nctl += 1;
+    }
     b->launch_order.resize(b->nw);
     for (int i = 0; i < b->nw; ++i) b->launch_order[i] = i;
     std::stable_sort(b->launch_order.begin(), b->launch_order.end(),
                      [&](int x, int y) { return b->hdr[x].nb > b->hdr[y].nb; });
     Arena a;
-    if (precision == GB_PREC_F64) carve(a, b->bd, b->nw, b->nb, b->nf, b->ncap, b->nj);
-    else carve(a, b->bf, b->nw, b->nb, b->nf, b->ncap, b->nj);
+    if (precision == GB_PREC_F64) carve(a, b->bd, b->nw, b->nb, b->nf, b->ncap, b->nj, b->nctl, b->nctlb);
+    else carve(a, b->bf, b->nw, b->nb, b->nf, b->ncap, b->nj, b->nctl, b->nctlb);
     size_t bytes = a.off + 256;
     cudaError_t e = cudaMalloc((void **)&b->arena, bytes);
     if (e != cudaSuccess) { delete b; return cuda_fail(e, "cudaMalloc(arena)"); }
@@ -328,8 +361,8 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
     CK(cudaMemset(b->arena, 0, bytes));
     Arena a2;
     a2.base = b->arena;
-    if (precision == GB_PREC_F64) carve(a2, b->bd, b->nw, b->nb, b->nf, b->ncap, b->nj);
-    else carve(a2, b->bf, b->nw, b->nb, b->nf, b->ncap, b->nj);
+    if (precision == GB_PREC_F64) carve(a2, b->bd, b->nw, b->nb, b->nf, b->ncap, b->nj, b->nctl, b->nctlb);
+    else carve(a2, b->bf, b->nw, b->nb, b->nf, b->ncap, b->nj, b->nctl, b->nctlb);
     {
         std::vector<int> bw(std::max(1, b->nb), 0), cw(std::max(1, b->ncap), 0);
         for (int i = 0; i < b->nw; ++i) {
@@ -389,6 +422,14 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         CK(cudaMemcpy(f64 ? b->bd.j : b->bf.j, b->joints.data(), sizeof(gb_joint) * b->nj, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(f64 ? b->bd.b_joff : b->bf.b_joff, joff.data(), sizeof(int) * joff.size(), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(f64 ? b->bd.b_jadj : b->bf.b_jadj, jadj.data(), sizeof(int) * jadj.size(), cudaMemcpyHostToDevice));
+    }
+    if (b->nctl > 0) {
+        const bool f64 = precision == GB_PREC_F64;
+        CK(cudaMemcpy(f64 ? b->bd.ctl : b->bf.ctl, b->controllers.data(), sizeof(gb_controller) * b->nctl,
+                      cudaMemcpyHostToDevice));
+        if (b->nctlb > 0)
+            CK(cudaMemcpy(f64 ? b->bd.ctl_bodies : b->bf.ctl_bodies, scene->controller_bodies, sizeof(int) * b->nctlb,
+                          cudaMemcpyHostToDevice));
     }
     CK(cudaMalloc((void **)&b->d_worlds, sizeof(int) * b->nw));
     CK(cudaMemcpy(b->d_worlds, b->launch_order.data(), sizeof(int) * b->nw, cudaMemcpyHostToDevice));
@@ -671,6 +712,23 @@ int gb_batch_set_joints(gb_batch *b, const gb_joint *joints, int32_t n, void *st
     if (n > 0)
         CK(cudaMemcpyAsync(b->prec == GB_PREC_F64 ? b->bd.j : b->bf.j, joints, sizeof(gb_joint) * n, cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+int gb_batch_set_controllers(gb_batch *b, const gb_controller *controllers, int32_t n, void *stream) {
+    if (!b || (!controllers && n > 0)) return fail(GB_E_ARG, "NULL argument");
+    if (n != b->nctl) return fail(GB_E_ARG, "n_controllers must equal the batch's controller count");
+    for (int i = 0; i < n; ++i) {
+        const gb_controller &C = controllers[i], &K = b->controllers[i];
+        if (C.world != K.world || C.type != K.type || C.body_start != K.body_start || C.body_count != K.body_count)
+            return fail(GB_E_ARG, "controller " + std::to_string(i) + ": world, kind and body list are fixed for the batch");
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n > 0)
+        CK(cudaMemcpyAsync(b->prec == GB_PREC_F64 ? b->bd.ctl : b->bf.ctl, controllers, sizeof(gb_controller) * n,
+                           cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    for (int i = 0; i < n; ++i) b->controllers[i] = controllers[i];
     return 0;
 }
 

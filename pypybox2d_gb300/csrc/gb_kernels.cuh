@@ -134,6 +134,7 @@ GB_DECL_PHASE_LAUNCHERS(PH_ISLANDS)
 GB_DECL_PHASE_LAUNCHERS(PH_SOLVE)
 GB_DECL_PHASE_LAUNCHERS(PH_PAIRS)
 GB_DECL_PHASE_LAUNCHERS(PH_TOI2)
+GB_DECL_PHASE_LAUNCHERS(PH_CTL)
 #undef GB_DECL_PHASE_LAUNCHERS
 template <> cudaError_t gb_world_launch<PH_TOI1>(int, int, size_t, cudaStream_t, const Batch<GB_REAL> &, const StepParams &,
                                                  const int *);
@@ -213,6 +214,7 @@ GB_DEF_WORLD_LAUNCH(PH_ISLANDS)
 #endif
 #if GB_IN_PART(4)
 GB_DEF_WORLD_LAUNCH(PH_SOLVE)
+GB_DEF_WORLD_LAUNCH(PH_CTL)
 #endif
 #if GB_IN_PART(5)
 GB_DEF_WORLD_LAUNCH(PH_TOI2)
@@ -224,6 +226,7 @@ GB_DEF_GRID_LAUNCH(PH_PAIRS)
 GB_DEF_GRID_LAUNCH(PH_COLLIDE2)
 #endif
 #if GB_IN_PART(7)
+GB_DEF_GRID_LAUNCH(PH_CTL)
 GB_DEF_GRID_LAUNCH(PH_ISLANDS)
 GB_DEF_GRID_LAUNCH(PH_SOLVE)
 GB_DEF_GRID_LAUNCH(PH_TOI2)
@@ -286,6 +289,10 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
         GB_GRID(PH_COLLIDE2);
         GB_CK(gb_world_launch<PH_COLLIDE2>(n_norm, t_pair, 0, st, B, sp, w_norm));
         mark(4);
+        if (B.n_ctl) {   // controllers (timed with the islands)
+            GB_GRID(PH_CTL);
+            GB_CK(gb_world_launch<PH_CTL>(n_norm, t_isl, 0, st, B, sp, w_norm));
+        }
         GB_GRID(PH_ISLANDS);
         GB_CK(gb_world_launch<PH_ISLANDS>(n_norm, t_isl, 0, st, B, sp, w_norm));
         mark(5);

@@ -156,6 +156,7 @@ template <class R> __global__ void k_toi1b(Batch<R> B) {
 #define PH_PAIRS 4
 #define PH_TOI2 5
 #define PH_TOI1 6   // the event loop's set-up, a CTA per world ahead of the one-warp loop
+#define PH_CTL 7    // controllers, launched ahead of PH_ISLANDS only for batches that have some
 
 template <class R, int PH> __device__ __forceinline__ void world_phase(const Batch<R> &B, const StepParams &sp, const int wi);
 
@@ -235,6 +236,10 @@ template <class R, int PH, class G> __device__ __forceinline__ void phase_body(c
             H.last_ncons = 0;
             H.last_njcons = 0;
         }
+    } else if (PH == PH_CTL) {
+        // the controllers open the solve (world.py:476-479): a kernel of their
+        // own keeps their registers out of the island kernel
+        if (solving && H.nctl) controllers_group(g, w);
     } else if (PH == PH_SOLVE) {
         if (H.pflags & P_SOLVING) {
             PhaseClock pc;

@@ -1060,6 +1060,8 @@ template <class R> __device__ __forceinline__ bool joint_simulated(const WView<R
 // Island search by union-find (world.py:495-573 without the visit order):
 // components over qualifying contacts between non-static bodies, the
 // simulated flag of each component and its depth-first seed.
+#include "gb_controllers.cuh"
+
 template <class R, class G> __device__ void islands_group(const G &g, const WView<R> &w, const StepParams &sp) {
     const int nb = w.H->nb, nc = w.H->nc, nf = w.H->nf;
     int *parent = w.B.s_parent + w.bb;
@@ -2092,6 +2094,7 @@ template <class R, class G> __device__ void sync_pairs_group(const G &g, const W
 
 template <class R, class G> __device__ void world_solve(const G &g, const WView<R> &w, const StepParams &sp, WShared *sh,
                                                         PhaseClock &pc) {
+    if (w.H->nctl) controllers_group(g, w);
     islands_group(g, w, sp);
     if (g.rank() == 0) pc.mark(2);
     constraints_group(g, w, sp);

@@ -97,6 +97,8 @@ struct WorldHdr {              // per-world scalars (device)
     int last_njcons, last_njcolours;   // joint constraints and their colours in the current step
     int toi_ncand, toi_hcap;   // TOI loop set-up made by the set-up kernel: candidates, pair-hash slots
     int toi_ready;             // that set-up is there for this step's loop
+    int nctl;                  // controllers of the world
+    int ctlbase;               // batch index of its first controller
     int _pad2;
 };
 
@@ -174,7 +176,11 @@ template <class R> struct Batch {
     int *s_jpref;                // scan / colour-compaction scratch (per joint slot)
     int *s_joff;                 // colour offsets of the colour-major layout: nj + 1 per world (from jbase + world)
     unsigned char *s_jvis;       // depth-first search marks (Joint._island_flag)
-    int *jorder_out;             // recorded joint order of the last record_order step (per joint slot)
+    int *jorder_out;
+    // controllers (sorted by world) and their body lists (world-local bodies)
+    int n_ctl;
+    gb_controller *ctl;
+    int *ctl_bodies;             // recorded joint order of the last record_order step (per joint slot)
     // worlds advanced by a cooperative grid (the first n_huge of the size-sorted list)
     int n_huge;
     int huge_ids[GB_MAX_HUGE];

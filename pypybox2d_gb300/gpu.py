@@ -17,10 +17,11 @@ from . import abi
 class GpuBatch:
     """A batch of independent worlds resident in device memory."""
 
-    def __init__(self, worlds, bodies, fixtures, contacts=None, precision: str = "f64", moves=None, joints=None):
+    def __init__(self, worlds, bodies, fixtures, contacts=None, precision: str = "f64", moves=None, joints=None,
+                 controllers=None, controller_bodies=None):
         self.lib = abi.load_library()
         self.prec = abi.PREC_F64 if precision in ("f64", "float64", abi.PREC_F64) else abi.PREC_F32
-        scene, keep = abi.make_scene(worlds, bodies, fixtures, contacts, moves, joints)
+        scene, keep = abi.make_scene(worlds, bodies, fixtures, contacts, moves, joints, controllers, controller_bodies)
         self.worlds, self.n_bodies, self.n_fixtures = keep[0], len(keep[1]), len(keep[2])
         self.joint_worlds = keep[5]["world"].copy()
         self.n_joints = len(keep[5])
@@ -177,6 +178,11 @@ class GpuBatch:
         """Overwrite every joint's definition and state (same worlds, kinds and bodies)."""
         j = np.ascontiguousarray(joints, dtype=abi.JOINT)
         abi.check(self.lib.gb_batch_set_joints(self.h, j.ctypes.data, len(j), None))
+
+    def set_controllers(self, controllers: np.ndarray) -> None:
+        """Overwrite every controller's parameters (same worlds, kinds and body lists)."""
+        c = np.ascontiguousarray(controllers, dtype=abi.CONTROLLER)
+        abi.check(self.lib.gb_batch_set_controllers(self.h, c.ctypes.data, len(c), None))
 
     def events(self, world: int = 0) -> np.ndarray:
         """Contact events of one world from the last step call made with

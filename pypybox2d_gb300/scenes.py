@@ -180,8 +180,8 @@ class SceneBuilder:
         for f in b.fixtures:
             # a loop: one edge record per child (shapes.py:851-863), no radius
             # margin on its fat box
-            children = [(f.shape.child_edge(c), abi.FIX_LOOP_CHILD) for c in range(f.shape.child_count)] \
-                if isinstance(f.shape, Loop) else [(f.shape, 0)]
+            children = [(f.shape.child_edge(c), abi.FIX_LOOP_CHILD | (abi.FIX_LOOP_FIRST if c == 0 else 0))
+                        for c in range(f.shape.child_count)] if isinstance(f.shape, Loop) else [(f.shape, 0)]
             for sh, extra in children:
                 j = self._fixture_record(F, j, b, f, sh, extra, bi if body_index is None else body_index)
         return B[0], F

@@ -28,10 +28,15 @@ the world solved by the same step; creating or destroying one is a
 structural change, and a joint setter edits the record and re-uploads the
 joints before the next step (``gb_batch_set_joints``).
 
+Controllers (buoyancy, gravity: ``controllers.py``) run inside the step;
+before each step the World compares ``World.controllers`` with what the
+device holds, uploading new parameters or rebuilding the batch for a new
+controller or body list.
+
 What the GPU step does not support raises instead of running elsewhere:
-loop shapes, the friction, gear, mouse, pulley, rope and wheel joints,
-controllers, sub-stepping, custom contact filters and ``pre_solve``
-callbacks that run mid-step.
+the friction, gear, mouse, pulley, rope and wheel joints, controllers with
+a Python ``step`` of their own, sub-stepping, custom contact filters and
+``pre_solve`` callbacks that run mid-step.
 """
 from __future__ import annotations
 
@@ -41,6 +46,7 @@ import numpy as np
 
 from . import abi
 from . import joints as _joints
+from .controllers import BuoyancyController, Controller, GravityController, controller_records  # noqa: F401
 from .joints import DistanceJoint, Joint, PrismaticJoint, RevoluteJoint, WeldJoint  # noqa: F401
 from .scenes import AABB_EXTENSION, SceneBuilder, _Body
 from .shapes import Circle, Edge, Loop, MassData, Polygon, Shape
@@ -232,6 +238,15 @@ class Body:
         self._index = index
         self.fixtures = fixtures
         self.user_data = user_data
+        self._controllers = []
+
+    def _attached_to_controller(self, controller):
+        """body.py:348-350"""
+        self._controllers.append(controller)
+
+    def _detached_from_controller(self, controller):
+        """body.py:352-353"""
+        self._controllers.remove(controller)
 
     # -- record access
     def _rec(self):
@@ -864,6 +879,9 @@ class World:
         self._J = np.zeros(0, dtype=abi.JOINT)   # World.joints records (world field 0)
         self._joints: list[Joint] = []
         self._upload_joints = False
+        self.controllers: list[Controller] = []   # World.controllers (world.py:73), run in this order
+        self._ctl_key = None                      # controller kinds and body lists the device batch holds
+        self._ctl_params = None                   # and their parameters
         self.joint_destruction_listener = joint_destruction_listener
         self.fixture_destruction_listener = fixture_destruction_listener
 
@@ -1055,6 +1073,11 @@ class World:
         self._bodies.pop(bi)
         for b in self._bodies[bi:]:
             b._index -= 1
+        # body.py:342-344: the loop removes from the list it walks, so a body
+        # in several controllers stays in every second one (as a body of no
+        # world it has no record on the device)
+        for controller in body._controllers:
+            controller.remove_body(body)
         body._world = None
 
     def clear_forces(self):
@@ -1074,6 +1097,7 @@ class World:
         cm = self.contact_manager
         if cm.pre_solve is not None:
             raise NotImplementedError("pre_solve listeners cannot run inside the GPU step")
+        self._sync_controllers()
         self._sync_device()
         events = cm.wants_events
         self._locked = True
@@ -1164,12 +1188,52 @@ class World:
         return self.add_joint(WeldJoint(*args, **kwargs))
 
     def _unsupported(self, *args, **kwargs):
-        raise NotImplementedError("friction, gear, mouse, pulley, rope and wheel joints and controllers are not "
-                                  "part of the GPU world step")
+        raise NotImplementedError("friction, gear, mouse, pulley, rope and wheel joints are not part of the GPU "
+                                  "world step")
 
     create_friction_joint = create_gear_joint = create_mouse_joint = _unsupported
     create_pulley_joint = create_rope_joint = create_wheel_joint = _unsupported
-    add_controller = destroy_controller = create_buoyancy_controller = create_gravity_controller = _unsupported
+
+    # -- controllers (world.py:923-957)
+    def create_gravity_controller(self, *args, **kwargs):
+        """world.py:923-929"""
+        return self.add_controller(GravityController(self, *args, **kwargs))
+
+    def create_buoyancy_controller(self, *args, **kwargs):
+        """world.py:931-937"""
+        return self.add_controller(BuoyancyController(self, *args, **kwargs))
+
+    def add_controller(self, controller):
+        """world.py:939-945"""
+        self.controllers.append(controller)
+        return controller
+
+    def destroy_controller(self, controller):
+        """world.py:947-957: its bodies are detached, it leaves the world"""
+        if controller not in self.controllers:
+            raise ValueError("Controller not in this world")
+        controller.clear()
+        self.controllers.remove(controller)
+
+    def _controller_state(self):
+        """(records, body lists, structure key) of World.controllers"""
+        C, cb = controller_records(self, self.controllers)
+        key = (C[["type", "body_start", "body_count"]].tobytes(), cb.tobytes())
+        return C, cb, key
+
+    def _sync_controllers(self):
+        """Before a step: a new controller or body list rebuilds the device
+        batch, new parameters are uploaded (gb_batch_set_controllers)."""
+        if not self.controllers and self._ctl_key is None:
+            return
+        C, cb, key = self._controller_state()
+        if self._gpu is None:
+            return
+        if key != self._ctl_key:
+            self._structural()
+        elif C.tobytes() != self._ctl_params:
+            self._gpu.set_controllers(C)
+            self._ctl_params = C.tobytes()
 
     # -- queries
     def query_aabb(self, aabb, callback=None):
@@ -1402,7 +1466,9 @@ class World:
             W["contact_count"] = len(self._C)
             W["contact_capacity"] = self._contact_capacity
             W["inv_dt0"] = self._inv_dt0
-            self._gpu = self._make_batch(W, self._B, self._F, self._C, M, self._J)
+            C, cb, key = self._controller_state() if self.controllers else (None, None, None)
+            self._gpu = self._make_batch(W, self._B, self._F, self._C, M, self._J, C, cb)
+            self._ctl_key, self._ctl_params = key, (C.tobytes() if C is not None else None)
             self._host_fresh = True
             self._upload_bodies = False
             self._upload_joints = False
@@ -1414,11 +1480,11 @@ class World:
             self._gpu.set_joints(self._J)
             self._upload_joints = False
 
-    def _make_batch(self, W, B, F, C, M, J=None):
+    def _make_batch(self, W, B, F, C, M, J=None, CT=None, CB=None):
         """The device batch holding this world (gb_batch_create)."""
         from .gpu import GpuBatch
         return GpuBatch(W, B, F, contacts=C if len(C) else None, precision=self._precision, moves=M,
-                        joints=J if J is not None and len(J) else None)
+                        joints=J if J is not None and len(J) else None, controllers=CT, controller_bodies=CB)
 
     def _add_fixture(self, body, fixture):
         """body.py:185-214: the fixture joins the body, its proxy the move
@@ -1764,9 +1830,13 @@ class WorldBatch:
             Js.append(J)
         W, B, F, C, M = _concat_worlds(recs)
         J = np.concatenate(Js)
+        self._ctl_keys = [w._controller_state()[2] if w.controllers else None for w in worlds]
+        CT, CB = self._controller_records(worlds)
+        self._ctl_params = CT.tobytes()
         from .gpu import GpuBatch
         self._gpu = GpuBatch(W, B, F, contacts=C if len(C) else None, precision=precision or worlds[0]._precision,
-                             moves=M, joints=J if len(J) else None)
+                             moves=M, joints=J if len(J) else None, controllers=CT if len(CT) else None,
+                             controller_bodies=CB)
         self._worlds = worlds
         self._index = {id(w): i for i, w in enumerate(worlds)}
         self._ranges = [(int(r["body_start"]), int(r["body_count"]), int(r["fixture_start"]), int(r["fixture_count"]))
@@ -1875,10 +1945,44 @@ class WorldBatch:
             w._J = J
         w._host_fresh = True
 
+    @staticmethod
+    def _controller_records(worlds):
+        """The controllers of every world, world by world (world field = its
+        index in the batch), and their concatenated body lists."""
+        Cs, Bs = [np.zeros(0, abi.CONTROLLER)], [np.zeros(0, np.int32)]
+        nb = 0
+        for i, w in enumerate(worlds):
+            if not w.controllers:
+                continue
+            C, cb, _ = w._controller_state()
+            C["world"] = i
+            C["body_start"] += nb
+            nb += len(cb)
+            Cs.append(C)
+            Bs.append(cb)
+        return np.concatenate(Cs), np.concatenate(Bs).astype(np.int32)
+
+    def _push_controllers(self):
+        """Controller parameters edited since the last step go up
+        (gb_batch_set_controllers); a new controller or body list is a
+        structural change."""
+        if not any(w.controllers for w in self._worlds) and not any(self._ctl_keys):
+            return
+        for w, key in zip(self._worlds, self._ctl_keys):
+            if (w._controller_state()[2] if w.controllers else None) != key:
+                raise NotImplementedError("a controller or controller body list changed in a world inside a "
+                                          "WorldBatch: build a new batch after the change")
+        CT, _ = self._controller_records(self._worlds)
+        if CT.tobytes() != self._ctl_params:
+            self._gpu.set_controllers(CT)
+            self._ctl_params = CT.tobytes()
+
     def _push_edits(self):
-        """Upload the bodies (joints) of the whole batch when a world's bodies
-        (joints) were edited on the host: velocities, forces, awake flags
-        (motor, limit and spring settings)."""
+        """Upload the bodies (joints, controllers) of the whole batch when a
+        world's bodies (joints, controllers) were edited on the host:
+        velocities, forces, awake flags (motor, limit and spring settings;
+        controller parameters)."""
+        self._push_controllers()
         bodies = any(w._upload_bodies for w in self._worlds)
         joints = any(w._upload_joints for w in self._worlds)
         if not (bodies or joints):

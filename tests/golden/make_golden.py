@@ -164,7 +164,7 @@ def export_world(world, b2, contacts=True):
             q["category_bits"], q["mask_bits"], q["group_index"] = f._category_bits, f._mask_bits, f._group_index
             fl = abi.FIX_SENSOR if f._sensor else 0
             if f._shape._type == abi.SHAPE_LOOP:
-                fl |= abi.FIX_LOOP_CHILD
+                fl |= abi.FIX_LOOP_CHILD | (abi.FIX_LOOP_FIRST if child == 0 else 0)
             if sh._type == abi.SHAPE_CIRCLE:
                 q["vertex_count"] = 1
                 q["vx"][0], q["vy"][0] = sh.position.x, sh.position.y
@@ -278,6 +278,36 @@ def export_joints(world, b2):
 
 
 # ---------------------------------------------------------------- scenes
+def export_controllers(world, b2):
+    """Reference World.controllers -> (gb_controller records, body lists)."""
+    from pypybox2d import controllers as cm
+    bidx = {id(b): i for i, b in enumerate(world.bodies)}
+    C = np.zeros(len(world.controllers), dtype=abi.CONTROLLER)
+    bodies = []
+    for k, c in enumerate(world.controllers):
+        r = C[k]
+        if type(c) is cm.BuoyancyController:
+            r["type"] = abi.CONTROLLER_BUOYANCY
+            own = bool(c._gravity)      # None or a zero Vec2 take the world's (controllers.py:177)
+            r["flags"] = abi.CTRL_OWN_GRAVITY if own else 0
+            r["normal_x"], r["normal_y"] = c._normal.x, c._normal.y
+            r["offset"], r["density"] = c._offset, c._density
+            r["velocity_x"], r["velocity_y"] = c._velocity.x, c._velocity.y
+            r["linear_drag"], r["angular_drag"] = c._linear_drag, c._angular_drag
+            if own:
+                r["gravity_x"], r["gravity_y"] = c._gravity.x, c._gravity.y
+        elif type(c) is cm.GravityController:
+            r["type"] = abi.CONTROLLER_GRAVITY
+            r["flags"] = abi.CTRL_INV_SQR if c._inv_sqr else 0
+            r["G"] = c._G
+        else:
+            raise NotImplementedError(type(c).__name__)
+        mine = [bidx[id(b)] for b in c._bodies if id(b) in bidx]
+        r["body_start"], r["body_count"] = len(bodies), len(mine)
+        bodies.extend(mine)
+    return C, np.array(bodies, dtype=np.int32)
+
+
 def scene_pyramid(b2, rows=20):
     """Configuration 1: the pyramid of 20 rows of 0.5 m boxes (210 bodies)."""
     from pypybox2d.common import Vec2
@@ -584,6 +614,82 @@ def scene_loops(b2, seed=23):
     return world
 
 
+def scene_buoyancy(b2, seed=29):
+    """Buoyancy controllers: a pool (offset 6 along (0, 1), density 2, linear
+    drag 2, angular drag 1) holding circles, boxes, triangles, a body whose
+    only fixture is an edge, a body carrying a loop beside a circle and a
+    chain of planks joined by revolute joints; a second controller with its
+    own gravity and a current (fluid velocity) acts on some of them too, so
+    two controllers run one after the other on the same bodies."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    ground = world.create_static_body(shapes=b2.Edge((-20, 0), (20, 0)))
+    pool = world.create_buoyancy_controller(offset=6, normal=(0, 1), density=2, linear_drag=2, angular_drag=1)
+    current = world.create_buoyancy_controller(offset=4.5, normal=(0, 1), density=0.5, velocity=(1.5, 0.0),
+                                               linear_drag=1, angular_drag=0.5, gravity=(0, -9.0))
+    for i in range(6):
+        b = world.create_dynamic_body(position=(-11 + 4.0 * i, 10 + rng.uniform(0, 2)),
+                                      fixtures=b2.Fixture(shape=b2.Circle(radius=0.6 + 0.1 * (i % 3)), density=1.0))
+        pool.add_body(b)
+        if i % 2 == 0:
+            current.add_body(b)
+    prev = ground
+    for k in range(10):
+        p = world.create_dynamic_body(position=(-14.5 + 1.0 * k, 5))
+        p.create_polygon_fixture(box=(0.5, 0.125), density=1.0, friction=0.2)
+        world.create_revolute_joint(prev, p, anchor=(-15.0 + 1.0 * k, 5))
+        pool.add_body(p)
+        prev = p
+    for i in range(4):
+        b = world.create_dynamic_body(position=(-8 + 3.0 * i, 14), angle=rng.uniform(-1, 1),
+                                      fixtures=b2.Fixture(shape=b2.Polygon(vertices=[(-0.5, 0), (0, -0.5), (0.5, 0)]),
+                                                          density=1.0))
+        pool.add_body(b)
+    for i in range(3):
+        b = world.create_dynamic_body(position=(4 + 2.5 * i, 9 + i), angle=0.3 * i)
+        b.create_polygon_fixture(box=(0.5, 0.3), density=0.8 + 0.4 * i, friction=0.4)
+        pool.add_body(b)
+        current.add_body(b)
+    edge = world.create_dynamic_body(fixtures=b2.Fixture(shape=b2.Edge((5, 0), (5, 3)), density=1.0))
+    pool.add_body(edge)
+    raft = world.create_dynamic_body(position=(12, 9), angle=0.2)
+    raft.create_loop_fixture([(-1, -0.4), (1, -0.4), (1, 0.4), (-1, 0.4)], friction=0.4)
+    raft.create_circle_fixture(radius=0.3, density=1.5)
+    pool.add_body(raft)
+    current.add_body(raft)
+    return world
+
+
+def scene_gravity(b2, seed=31):
+    """Gravity controllers in a world without gravity: an inverse-square
+    controller over circles, triangles, boxes (two of them created asleep,
+    woken by the controller's forces) and a static anchor body (zero mass:
+    its pairs give zero forces but still wake their partners), and an
+    inverse-distance controller over a second group."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, 0), do_sleep=True)
+    anchor = world.create_static_body(position=(0, 0), shapes=b2.Circle(radius=0.5))
+    g1 = world.create_gravity_controller(G=0.8, inv_sqr=True)
+    g2 = world.create_gravity_controller(G=0.3, inv_sqr=False)
+    g1.add_body(anchor)
+    for i in range(1, 5):
+        b = world.create_dynamic_body(position=(0.25 * i, 2.0 + 3.5 * i), bullet=(i == 4),
+                                      fixtures=b2.Fixture(shape=b2.Circle(radius=0.25 * i), density=1.0))
+        g1.add_body(b)
+    for i in range(4):
+        b = world.create_dynamic_body(position=(-8 + 4.0 * i, -6 + rng.uniform(-1, 1)), angle=rng.uniform(-1, 1),
+                                      awake=(i % 2 == 0),
+                                      fixtures=b2.Fixture(shape=b2.Polygon(vertices=[(-0.5, 0), (0, -0.5), (0.5, 0)]),
+                                                          density=1.0))
+        g1.add_body(b)
+    for i in range(5):
+        b = world.create_dynamic_body(position=(10 + 1.5 * i, 5 + rng.uniform(-2, 2)),
+                                      linear_velocity=(0, rng.uniform(-1, 1)))
+        b.create_polygon_fixture(box=(0.4, 0.4), density=2.0, friction=0.5)
+        g2.add_body(b)
+    return world
+
+
 SCENES = {
     "pyramid": (scene_pyramid, 300, (1, 2, 3, 5, 10, 30, 31, 100, 101, 200, 201, 300)),
     "pyramid5": (lambda b2: scene_pyramid(b2, rows=5), 150, (1, 2, 5, 20, 21, 60, 61, 150)),
@@ -596,6 +702,8 @@ SCENES = {
     "joints": (scene_joints, 300, (1, 2, 5, 20, 21, 60, 61, 120, 121, 200, 201, 300)),
     "bridge": (scene_bridge, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
     "loops": (scene_loops, 180, (1, 2, 5, 20, 21, 60, 61, 120, 121, 180)),
+    "buoyancy": (scene_buoyancy, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
+    "gravity": (scene_gravity, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
 }
 
 
@@ -609,6 +717,8 @@ def run_scene(b2, name, builder, n_steps, snaps, vel_iters=8, pos_iters=3, dt=1.
     out["init_world"], out["init_bodies"], out["init_fixtures"] = W, B, F
     if world.joints:
         out["init_joints"] = export_joints(world, b2)
+    if world.controllers:
+        out["init_controllers"], out["init_controller_bodies"] = export_controllers(world, b2)
     out["iters"] = np.array([vel_iters, pos_iters])
     try:
         for s in range(1, n_steps + 1):
@@ -749,6 +859,23 @@ def run_api_loops(b2):
     print(f"api_loops: {len(api_loops.SNAPS)} snapshots -> {os.path.getsize(path)} bytes")
 
 
+def run_api_controllers(b2):
+    """tests/golden/api_controllers.py on the reference -> api_controllers.npz."""
+    sys.path.insert(0, HERE)
+    import api_controllers
+    out = {}
+
+    def snap(label, world):
+        W, B, F, C = export_world(world, b2)
+        out[f"{label}_bodies"], out[f"{label}_contacts"] = B, C
+        out[f"{label}_controllers"], out[f"{label}_controller_bodies"] = export_controllers(world, b2)
+
+    api_controllers.script(b2, snap, on_world=pair_order_hook)
+    path = os.path.join(HERE, "api_controllers.npz")
+    np.savez_compressed(path, **out)
+    print(f"api_controllers: {len(api_controllers.SNAPS)} snapshots -> {os.path.getsize(path)} bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("GB2D_REFERENCE"), required="GB2D_REFERENCE" not in os.environ,
@@ -768,6 +895,8 @@ def main():
         run_api_active(b2)
     if not args.only or args.only == "api_loops":
         run_api_loops(b2)
+    if not args.only or args.only == "api_controllers":
+        run_api_controllers(b2)
 
 
 if __name__ == "__main__":

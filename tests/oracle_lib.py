@@ -81,14 +81,26 @@ def load(libm: bool = False) -> ctypes.CDLL:
     lib.or_set_joint_order.restype = None
     lib.or_get_joint_order.argtypes = [vp, vp, i32]
     lib.or_get_joint_order.restype = i32
+    lib.or_set_controllers.argtypes = [vp, vp, i32, vp, i32]
+    lib.or_set_controllers.restype = i32
     _libs[libm] = lib
     return lib
+
+
+def golden_extras(d) -> dict:
+    """The joints and controllers of a golden scene (npz), as keyword
+    arguments of OracleWorld and GpuBatch."""
+    out = {"joints": d["init_joints"] if "init_joints" in d.files else None}
+    if "init_controllers" in d.files:
+        out["controllers"], out["controller_bodies"] = d["init_controllers"], d["init_controller_bodies"]
+    return out
 
 
 class OracleWorld:
     """One world of the restatement, built from gb2d record arrays."""
 
-    def __init__(self, world, bodies, fixtures, contacts=None, libm=False, index=0, moves=None, joints=None):
+    def __init__(self, world, bodies, fixtures, contacts=None, libm=False, index=0, moves=None, joints=None,
+                 controllers=None, controller_bodies=None):
         self.lib = load(libm)
         self._keep = [np.ascontiguousarray(world, dtype=abi.WORLD),
                       np.ascontiguousarray(bodies, dtype=abi.BODY),
@@ -108,6 +120,19 @@ class OracleWorld:
             J = np.ascontiguousarray(J[J["world"] == index])
             if len(J):
                 assert self.lib.or_set_joints(self.h, J.ctypes.data, len(J)) == 0, "bad joint records"
+        if controllers is not None and len(controllers):
+            self.set_controllers(controllers, controller_bodies, index)
+
+    def set_controllers(self, controllers, controller_bodies, index=0):
+        """The controllers of world `index` (records sorted by world, body
+        lists in controller_bodies)."""
+        C = np.ascontiguousarray(controllers, dtype=abi.CONTROLLER)
+        C = np.ascontiguousarray(C[C["world"] == index])
+        cb = np.ascontiguousarray(controller_bodies if controller_bodies is not None else np.zeros(0, np.int32),
+                                  dtype=np.int32)
+        self._ctl = (C, cb)
+        assert self.lib.or_set_controllers(self.h, C.ctypes.data if len(C) else None, len(C),
+                                           cb.ctypes.data if len(cb) else None, len(cb)) == 0, "bad controller records"
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -177,8 +202,9 @@ class OracleBatch:
     (step / bodies / set_bodies / proxies / contacts / status), so the
     World's host logic can be checked on the CPU.  Test infrastructure."""
 
-    def __init__(self, W, B, F, C, M, libm=False, joints=None):
-        self.o = OracleWorld(W, B, F, C if len(C) else None, libm=libm, moves=M, joints=joints)
+    def __init__(self, W, B, F, C, M, libm=False, joints=None, controllers=None, controller_bodies=None):
+        self.o = OracleWorld(W, B, F, C if len(C) else None, libm=libm, moves=M, joints=joints, controllers=controllers,
+                             controller_bodies=controller_bodies)
         self.libm = libm
 
     def query_aabb(self, q, max_per_query):
@@ -217,6 +243,9 @@ class OracleBatch:
 
     def joints(self, world=None):
         return self.o.joints()
+
+    def set_controllers(self, controllers):
+        self.o.set_controllers(controllers, getattr(self.o, "_ctl", (None, None))[1])
 
     def set_joints(self, J):
         J = np.ascontiguousarray(J, dtype=abi.JOINT)

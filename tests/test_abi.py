@@ -42,6 +42,8 @@ def test_record_layouts_match(lib):
     assert sizes[3] == abi.WORLD.itemsize
     assert sizes[4] == ctypes.sizeof(abi.Scene)
     assert sizes[5] == ctypes.sizeof(abi.StepOpts)
+    assert lib.gb_joint_size() == abi.JOINT.itemsize
+    assert lib.gb_controller_size() == abi.CONTROLLER.itemsize
 
 
 def test_errors_are_reported_not_silent(lib):

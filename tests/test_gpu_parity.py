@@ -27,7 +27,7 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 STEPS = {"pyramid": 40, "pyramid5": 150, "mixed": 120, "bullets": 60, "sleep": 90, "uneven": 240, "kinematic": 180,
-         "sensor_filter": 150, "joints": 300, "bridge": 240, "loops": 180}
+         "sensor_filter": 150, "joints": 300, "bridge": 240, "loops": 180, "buoyancy": 240, "gravity": 240}
 
 
 def _gpu():
@@ -63,9 +63,10 @@ def run_lockstep(scene, steps, launch_mode=1, block_threads=0):
     dt = float(d["dt"][0])
     vi, pi = (int(x) for x in d["iters"])
     W, B, F = d["init_world"], d["init_bodies"], d["init_fixtures"]
-    J = d["init_joints"] if "init_joints" in d.files else None
-    gpu = GpuBatch(W, B, F, precision="f64", joints=J)
-    orc = oracle_lib.OracleWorld(W, B, F, libm=False, joints=J)
+    extras = oracle_lib.golden_extras(d)
+    J = extras["joints"]
+    gpu = GpuBatch(W, B, F, precision="f64", **extras)
+    orc = oracle_lib.OracleWorld(W, B, F, libm=False, **extras)
     for s in range(1, steps + 1):
         gpu.step(dt, vi, pi, 1, launch_mode=launch_mode, block_threads=block_threads, record_order=True)
         order = gpu.solver_order(0)

@@ -36,19 +36,20 @@ import os
 import numpy as np
 import pytest
 
+import oracle_lib
 from pypybox2d_gb300 import abi
 
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-SCENES = ("bridge", "bullets", "joints", "kinematic", "loops", "mixed", "pyramid", "pyramid5", "sensor_filter", "sleep",
-          "uneven")
+SCENES = ("bridge", "buoyancy", "bullets", "gravity", "joints", "kinematic", "loops", "mixed", "pyramid", "pyramid5",
+          "sensor_filter", "sleep", "uneven")
 ONE_STEP_TOL_M = 2e-2
 JOINT_ONE_STEP_TOL_M = 5e-2
 FREE_TOL_M = 5e-2
 # scene -> last snapshot step at which the free run is held to the reference
 FREE_HELD = {"bullets": 41, "kinematic": 61, "mixed": 21, "pyramid": 10, "pyramid5": 5, "sensor_filter": 150,
-             "sleep": 90, "uneven": 61, "joints": 21, "bridge": 21, "loops": 21}
+             "sleep": 90, "uneven": 61, "joints": 21, "bridge": 21, "loops": 21, "buoyancy": 61, "gravity": 240}
 # scene -> contacts allowed to differ in discrete fields after one step, over all its one-step states
 DISCRETE_ONE_STEP = {"pyramid": 1}
 
@@ -84,7 +85,8 @@ def _snapshot_batch(d, s):
     F = d["init_fixtures"].copy()
     F["aabb"] = d[f"s{s}_aabb"]
     J = d[f"s{s}_joints"] if f"s{s}_joints" in d.files else None
-    return GpuBatch(W, d[f"s{s}_bodies"], F, contacts=C if len(C) else None, precision="f64", joints=J)
+    ctl = {k: v for k, v in oracle_lib.golden_extras(d).items() if k != "joints"}
+    return GpuBatch(W, d[f"s{s}_bodies"], F, contacts=C if len(C) else None, precision="f64", joints=J, **ctl)
 
 
 @pytest.mark.parametrize("scene", SCENES)
@@ -118,8 +120,7 @@ def test_free_run_against_the_reference(scene):
     from pypybox2d_gb300.gpu import GpuBatch
     d = np.load(os.path.join(GOLDEN, scene + ".npz"))
     dt, (vi, pi) = float(d["dt"][0]), (int(x) for x in d["iters"])
-    J = d["init_joints"] if "init_joints" in d.files else None
-    g = GpuBatch(d["init_world"], d["init_bodies"], d["init_fixtures"], precision="f64", joints=J)
+    g = GpuBatch(d["init_world"], d["init_bodies"], d["init_fixtures"], precision="f64", **oracle_lib.golden_extras(d))
     done, lines = 0, []
     for s in (int(x) for x in d["snaps"]):
         g.step(dt, vi, pi, s - done, launch_mode=3)

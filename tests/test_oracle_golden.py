@@ -17,7 +17,7 @@ from pypybox2d_gb300 import abi
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 SCENES = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                if not p.endswith(("api_script.npz", "api_joints.npz", "api_active.npz", "api_loops.npz",
+                if not p.endswith(("api_script.npz", "api_joints.npz", "api_active.npz", "api_loops.npz", "api_controllers.npz",
                                   "queries.npz")))   # own tests
 
 
@@ -42,8 +42,9 @@ def test_oracle_matches_reference_bitwise(scene):
     d = np.load(os.path.join(GOLDEN, scene + ".npz"))
     dt = float(d["dt"][0])
     vi, pi = (int(x) for x in d["iters"])
-    joints = d["init_joints"] if "init_joints" in d.files else None
-    w = oracle_lib.OracleWorld(d["init_world"], d["init_bodies"], d["init_fixtures"], libm=True, joints=joints)
+    extras = oracle_lib.golden_extras(d)
+    joints = extras["joints"]
+    w = oracle_lib.OracleWorld(d["init_world"], d["init_bodies"], d["init_fixtures"], libm=True, **extras)
     snaps = [int(s) for s in d["snaps"]]
     for s in range(1, max(snaps) + 1):
         w.step(dt, vi, pi)

@@ -80,8 +80,8 @@ def oracle_world_class(libm):
     import oracle_lib
 
     class OracleBackedWorld(b2.World):
-        def _make_batch(self, W, B, F, C, M, J=None):
-            return oracle_lib.OracleBatch(W, B, F, C, M, libm=libm, joints=J)
+        def _make_batch(self, W, B, F, C, M, J=None, CT=None, CB=None):
+            return oracle_lib.OracleBatch(W, B, F, C, M, libm=libm, joints=J, controllers=CT, controller_bodies=CB)
 
     return OracleBackedWorld
 

@@ -221,8 +221,8 @@ def test_host_edits_between_steps_match_reference():
     import oracle_lib
 
     class OracleBackedWorld(b2.World):
-        def _make_batch(self, W, B, F, C, M, J=None):
-            return oracle_lib.OracleBatch(W, B, F, C, M, libm=True, joints=J)
+        def _make_batch(self, W, B, F, C, M, J=None, CT=None, CB=None):
+            return oracle_lib.OracleBatch(W, B, F, C, M, libm=True, joints=J, controllers=CT, controller_bodies=CB)
 
     d = np.load(os.path.join(GOLDEN, "queries.npz"))
     snaps = {}
@@ -247,11 +247,10 @@ def test_host_edits_between_steps_match_reference():
     assert np.array_equal(np.array(log, dtype=np.int32).reshape(-1, 2), d["edits_end_log"])
 
 
-def test_unsupported_joints_and_controllers_raise_clearly():
+def test_unsupported_joints_raise_clearly():
     w = b2.World()
     for name in ("create_friction_joint", "create_gear_joint", "create_mouse_joint", "create_pulley_joint",
-                 "create_rope_joint", "create_wheel_joint", "create_gravity_controller", "create_buoyancy_controller",
-                 "add_controller"):
+                 "create_rope_joint", "create_wheel_joint"):
         with pytest.raises(NotImplementedError):
             getattr(w, name)()
     with pytest.raises(NotImplementedError):

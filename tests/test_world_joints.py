@@ -52,8 +52,8 @@ def oracle_world_class():
     import oracle_lib
 
     class OracleBackedWorld(b2.World):
-        def _make_batch(self, W, B, F, C, M, J=None):
-            return oracle_lib.OracleBatch(W, B, F, C, M, libm=True, joints=J)
+        def _make_batch(self, W, B, F, C, M, J=None, CT=None, CB=None):
+            return oracle_lib.OracleBatch(W, B, F, C, M, libm=True, joints=J, controllers=CT, controller_bodies=CB)
 
     return OracleBackedWorld
 
