@@ -5,10 +5,16 @@
   every world steps bit for bit as the oracle steps it alone, so the
   per-world joint ranges, body joint lists and colour layouts of a batch are
   the ones each world has on its own;
-* the float32 unit on the joint scenes: one step from identical float64
-  state against the float64 step, positions within F32_TOL_M (joints are
-  solved in float64 in both units; the float32 unit rounds the velocities
-  they act on; measured at most 1.2e-7 m at steps 20, 60 and 120);
+* the float32 unit on the joint, loop and controller scenes: one step from
+  identical float64 state against the float64 step, positions within
+  F32_TOL_M (joints and controllers compute in float64 in both units; the
+  float32 unit rounds the velocities and forces they act on; measured at
+  most 1.4e-7 m at steps 20, 60 and 120) over the bodies whose step
+  records agree.  The loops scene's step 60 has a TOI event whose first
+  position pass ends exactly on the -1.5 slop early exit (a ball rolling
+  into the terrain), so rounding decides one more pass there (4.7e-4 m, the
+  threshold case of tests/test_gpu_f32_parity.py); at most one body a state
+  may take a decision apart, and its island is left out of the bound;
 * joint state through the C ABI: gb_batch_get_joints returns what was
   uploaded before any step, and gb_batch_set_joints refuses a record whose
   world, kind or bodies differ from the batch's.
@@ -69,11 +75,13 @@ def test_batch_of_worlds_with_and_without_joints(names):
     assert not g.status().any()
 
 
-@pytest.mark.parametrize("scene", ["joints", "bridge"])
+@pytest.mark.parametrize("scene", ["joints", "bridge", "loops", "buoyancy", "gravity"])
 def test_f32_joint_step_against_f64(scene):
     from pypybox2d_gb300.gpu import GpuBatch
     W, B, F, J = _scene(scene)
-    g64 = GpuBatch(W, B, F, precision="f64", joints=J)
+    ctl = {k: v for k, v in oracle_lib.golden_extras(np.load(os.path.join(GOLDEN, scene + ".npz"))).items()
+           if k != "joints"}
+    g64 = GpuBatch(W, B, F, precision="f64", joints=J, **ctl)
     worst = 0.0
     done = 0
     for s in (20, 60, 120):
@@ -86,14 +94,21 @@ def test_f32_joint_step_against_f64(scene):
         W0["inv_dt0"] = 1.0 / (1 / 60)
         F0 = F.copy()
         F0["aabb"] = P0
-        a = GpuBatch(W0, B0, F0, contacts=C0 if len(C0) else None, precision="f64", joints=J0)
-        b = GpuBatch(W0, B0, F0, contacts=C0 if len(C0) else None, precision="f32", joints=J0)
-        a.step(1 / 60, 8, 3, 1, launch_mode=3)
-        b.step(1 / 60, 8, 3, 1, launch_mode=3)
+        a = GpuBatch(W0, B0, F0, contacts=C0 if len(C0) else None, precision="f64", joints=J0, **ctl)
+        b = GpuBatch(W0, B0, F0, contacts=C0 if len(C0) else None, precision="f32", joints=J0, **ctl)
+        a.step(1 / 60, 8, 3, 1, launch_mode=3, record_order=True)
+        b.step(1 / 60, 8, 3, 1, launch_mode=3, record_order=True)
         ba, bb = a.bodies(), b.bodies()
-        err = float(np.hypot(ba["cx"] - bb["cx"], ba["cy"] - bb["cy"]).max())
+        ra, rb = a.step_record(0), b.step_record(0)
+        apart = ra[0] != rb[0]
+        islands = set(ra[1][apart & (ra[1] >= 0)].tolist()) | set(rb[1][apart & (rb[1] >= 0)].tolist())
+        keep = ~apart & ~np.isin(ra[1], list(islands)) & ~np.isin(rb[1], list(islands))
+        d = np.hypot(ba["cx"] - bb["cx"], ba["cy"] - bb["cy"])
+        err = float(d[keep].max()) if keep.any() else 0.0
         worst = max(worst, err)
-        print(f"\n{scene} step {s}: float32 one-step position error {err:.2e} m")
+        print(f"\n{scene} step {s}: float32 one-step position error {err:.2e} m over {int(keep.sum())} bodies, "
+              f"{int(apart.sum())} body decided apart ({float(d.max()):.2e} m over all)")
+        assert int(apart.sum()) <= 1
         assert not b.status().any()
     assert worst <= F32_TOL_M, f"{scene}: {worst:.2e} m"
 
