@@ -142,7 +142,7 @@ template <class R> __global__ void k_toi1b(Batch<R> B) {
         int i = s - w.cb;
         const ContactRec<R> &c = w.con(i);
         int ba = w.fbody(c.fa), bb = w.fbody(c.fb);
-        toi_compute(w, i, 0.0, w.sweep(ba), w.sweep(bb));
+        toi_compute<R, true>(w, i, 0.0, w.sweep(ba), w.sweep(bb));
         const double toi = c.toi;
         if (toi < 1.0) atomicMin(&B.hdr[w.wi].toimin, dkey(toi));
     }
@@ -166,6 +166,8 @@ template <class R, int PH> __global__ void __launch_bounds__(256) k_world(Batch<
 
 // The TOI event loop is latency bound (float64, mostly one thread): one warp
 // per world with a register cap keeps many worlds in flight per SM.
+// (Measured on the uneven batch: 16 or 12 resident warps, with up to 128
+// and 168 registers, make the slowest world's event chain 10 % longer.)
 template <class R> __global__ void __launch_bounds__(32, 24) k_world_toi2(Batch<R> B, StepParams sp, const int *worlds) {
     world_phase<R, PH_TOI2>(B, sp, worlds[blockIdx.x]);
 }

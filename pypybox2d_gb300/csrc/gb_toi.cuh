@@ -55,14 +55,15 @@ template <class R> __device__ double toi_align(const WView<R> &w, int i, Sweep *
 // stops at -1.5 slop (contact.py:931), which is where the TOI target leaves
 // the separation, so float32 arithmetic here moves the bodies by up to
 // ~1e-3 m against the float64 step.
-template <class R> __device__ void toi_compute(const WView<R> &w, int i, double alpha0, const Sweep &sa, const Sweep &sb) {
+template <class R, bool XF_CACHE = false>
+__device__ void toi_compute(const WView<R> &w, int i, double alpha0, const Sweep &sa, const Sweep &sb) {
     ContactRec<R> &c = w.con(i);
     double beta;
     bool lim = false;
     DProxy pa, pb;
     dproxy_init(pa, w.shape(c.fa));
     dproxy_init(pb, w.shape(c.fb));
-    int state = time_of_impact(pa, pb, sa, sb, 1.0, &beta, &lim);
+    int state = time_of_impact<XF_CACHE>(pa, pb, sa, sb, 1.0, &beta, &lim);
     if (lim) atomicOr(&w.H->status, GB_ST_ITER_LIMIT);
     double alpha = (state == TOI_TOUCHING) ? pymin(alpha0 + (1.0 - alpha0) * beta, 1.0) : 1.0;
     c.toi = alpha;

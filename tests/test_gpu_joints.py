@@ -13,8 +13,9 @@
   records agree.  The loops scene's step 60 has a TOI event whose first
   position pass ends exactly on the -1.5 slop early exit (a ball rolling
   into the terrain), so rounding decides one more pass there (4.7e-4 m, the
-  threshold case of tests/test_gpu_f32_parity.py); at most one body a state
-  may take a decision apart, and its island is left out of the bound;
+  threshold case of tests/test_gpu_f32_parity.py); at most one TOI event (its
+  two bodies) a state may be decided apart, and its islands are left out of
+  the bound;
 * joint state through the C ABI: gb_batch_get_joints returns what was
   uploaded before any step, and gb_batch_set_joints refuses a record whose
   world, kind or bodies differ from the batch's.
@@ -108,7 +109,7 @@ def test_f32_joint_step_against_f64(scene):
         worst = max(worst, err)
         print(f"\n{scene} step {s}: float32 one-step position error {err:.2e} m over {int(keep.sum())} bodies, "
               f"{int(apart.sum())} body decided apart ({float(d.max()):.2e} m over all)")
-        assert int(apart.sum()) <= 1
+        assert int(apart.sum()) <= 2      # one TOI event: its two bodies
         assert not b.status().any()
     assert worst <= F32_TOL_M, f"{scene}: {worst:.2e} m"
 
