@@ -171,16 +171,21 @@ typedef struct gb_contact {
     uint32_t p_id[2];             /* index_a | index_b<<8 | type_a<<16 | type_b<<24 */
 } gb_contact;
 
-/* joint types (pypybox2d/joints/: revolute.py, prismatic.py, distance.py, weld.py) */
+/* joint types (pypybox2d/joints/: revolute.py, prismatic.py, distance.py, weld.py,
+ * friction.py, rope.py, wheel.py, pulley.py) */
 #define GB_JOINT_REVOLUTE 1
 #define GB_JOINT_PRISMATIC 2
 #define GB_JOINT_DISTANCE 3
 #define GB_JOINT_WELD 4
+#define GB_JOINT_FRICTION 5
+#define GB_JOINT_ROPE 6
+#define GB_JOINT_WHEEL 7
+#define GB_JOINT_PULLEY 8
 
 /* gb_joint.flags */
 #define GB_J_COLLIDE_CONNECTED 1u /* Joint._collide_connected */
 #define GB_J_LIMIT 2u             /* _limit_enabled (revolute, prismatic) */
-#define GB_J_MOTOR 4u             /* _motor_enabled (revolute, prismatic) */
+#define GB_J_MOTOR 4u             /* _motor_enabled (revolute, prismatic, wheel) */
 
 /* gb_joint.limit_state, as joints/joint.py:35 */
 #define GB_LIMIT_INACTIVE 0
@@ -211,8 +216,15 @@ typedef struct gb_joint {
     double impulse[3];             /* _impulse (distance: impulse[0]) */
     double motor_impulse;          /* _motor_impulse */
     double gamma, bias;            /* distance: kept from the last set-up with frequency > 0 (distance.py:246-266) */
-    double ux, uy;                 /* last set-up: distance _u, prismatic _axis (for the reaction force) */
-    double perp_x, perp_y;         /* last set-up: prismatic _perp */
+    double ux, uy;                 /* last set-up: distance _u, prismatic _axis (for the reaction force),
+                                      rope _u (the unnormalised anchor difference) */
+    double perp_x, perp_y;         /* last set-up: prismatic _perp, wheel _ay */
+    double max_force, max_torque;  /* friction */
+    double max_length, cur_length; /* rope: _max_length; _length of the last set-up */
+    double spring_impulse;         /* wheel _spring_impulse */
+    double sax_x, sax_y, s_ax, s_bx; /* wheel _ax, _s_ax, _s_bx: set by a set-up with a spring, kept otherwise */
+    double ga_x, ga_y, gb_x, gb_y; /* pulley ground anchors */
+    double ratio, constant;        /* pulley _ratio, _constant */
 } gb_joint;
 
 /* controller kinds (pypybox2d/controllers.py) */

@@ -1249,7 +1249,7 @@ int or_set_joints(or_world *w, const gb_joint *joints, int n) {
     for (int i = 0; i < n; ++i) {
         const gb_joint *J = &joints[i];
         if (J->body_a < 0 || J->body_a >= w->nb || J->body_b < 0 || J->body_b >= w->nb || J->body_a == J->body_b ||
-            J->type < GB_JOINT_REVOLUTE || J->type > GB_JOINT_WELD)
+            J->type < GB_JOINT_REVOLUTE || J->type > GB_JOINT_PULLEY)
             return -1;
     }
     for (int i = 0; i < w->nb; ++i) w->bjoint[i].n = 0;

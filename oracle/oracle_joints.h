@@ -610,6 +610,381 @@ static int weld_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
     return position_error <= OR_LINEAR_SLOP_J && angular_error <= OR_ANGULAR_SLOP;
 }
 
+/* ------------------------------------------------------------ friction
+ * joints/friction.py:107-233.  Its _solve_velocity_constraints writes the
+ * positions back instead of the velocities (friction.py:228-229), so the
+ * passes change only the accumulated impulses; the warm start of the set-up
+ * is the only velocity change the joint makes. */
+static void friction_init(gb_joint *J, or_jcons *k, const double *pa, v2 *vv, double *ww, double dt_ratio, int warm) {
+    double ma = k->ma, mb = k->mb, iA = k->iA, iB = k->iB;
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    rot qa = rot_of(pa[k->ia]), qb = rot_of(pa[k->ib]);
+    v2 ra = k->ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    double a = ma + mb + iA * ra.y * ra.y + iB * rb.y * rb.y;
+    double c = -iA * ra.x * ra.y - iB * rb.x * rb.y;
+    double b = c;
+    double d = ma + mb + iA * ra.x * ra.x + iB * rb.x * rb.x;
+    double det = a * d - b * c;                    /* Mat22.inverse (mat22module.c) */
+    if (det != 0.0) det = 1.0 / det;
+    k->m.c1 = V3(det * d, -det * c, 0.0);
+    k->m.c2 = V3(-det * b, det * a, 0.0);
+    k->motor_mass = iA + iB;
+    if (k->motor_mass > 0.0) k->motor_mass = 1.0 / k->motor_mass;
+    if (warm) {
+        J->impulse[0] = J->impulse[0] * dt_ratio;
+        J->impulse[1] = J->impulse[1] * dt_ratio;
+        J->impulse[2] = J->impulse[2] * dt_ratio;
+        v2 P = V(J->impulse[0], J->impulse[1]);
+        va = vsub(va, vscale(ma, P));
+        wa = wa - iA * (vcross(ra, P) + J->impulse[2]);
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + iB * (vcross(rb, P) + J->impulse[2]);
+    } else {
+        J->impulse[0] = J->impulse[1] = J->impulse[2] = 0.0;
+    }
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void friction_solve_velocity(gb_joint *J, or_jcons *k, const v2 *vv, const double *ww, double dt) {
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    v2 ra = k->ra, rb = k->rb;
+    double iA = k->iA, iB = k->iB;
+    double Cdot = wb - wa;
+    double impulse = -k->motor_mass * Cdot;
+    double old_impulse = J->impulse[2];
+    double max_impulse = dt * J->max_torque;
+    J->impulse[2] = cclamp(J->impulse[2] + impulse, -max_impulse, max_impulse);
+    impulse = J->impulse[2] - old_impulse;
+    wa = wa - iA * impulse;
+    wb = wb + iB * impulse;
+    v2 Cdot2 = vsub(vsub(vadd(vb, vcross_sv(wb, rb)), va), vcross_sv(wa, ra));
+    v2 li = V(-(k->m.c1.x * Cdot2.x + k->m.c2.x * Cdot2.y), -(k->m.c1.y * Cdot2.x + k->m.c2.y * Cdot2.y));
+    v2 acc = V(J->impulse[0] + li.x, J->impulse[1] + li.y);
+    double max_force_impulse = dt * J->max_force;
+    if (acc.x * acc.x + acc.y * acc.y > SQ(max_force_impulse)) acc = vscale(max_force_impulse, vnormalized(acc));
+    J->impulse[0] = acc.x;
+    J->impulse[1] = acc.y;
+}
+
+/* ------------------------------------------------------------ rope
+ * joints/rope.py:106-248.  `u /= length` rebinds the local name only, so the
+ * kept `_u` is the unnormalised anchor difference: the velocity passes and
+ * the warm start project on it (rope.py:140-149, 186-196). */
+static void rope_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt_ratio,
+                      int warm) {
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    rot qa = rot_of(pa[k->ia]), qb = rot_of(pa[k->ib]);
+    v2 ra = k->ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 u = vsub(vsub(vadd(cb, rb), ca), ra);
+    J->ux = u.x; J->uy = u.y;
+    J->cur_length = vlen(u);
+    double C = J->cur_length - J->max_length;
+    J->limit_state = C > 0.0 ? GB_LIMIT_UPPER : GB_LIMIT_INACTIVE;
+    if (J->cur_length > OR_LINEAR_SLOP_J) {
+        u = V(u.x / J->cur_length, u.y / J->cur_length);
+    } else {
+        k->dmass = 0.0;
+        J->impulse[0] = 0.0;
+        return;
+    }
+    double cra = vcross(ra, u), crb = vcross(rb, u);
+    double inv_mass = ma + ia * cra * cra + mb + ib * crb * crb;
+    k->dmass = inv_mass != 0.0 ? 1.0 / inv_mass : 0.0;
+    if (warm) {
+        J->impulse[0] = J->impulse[0] * dt_ratio;
+        v2 P = vscale(J->impulse[0], V(J->ux, J->uy));
+        va = vsub(va, vscale(ma, P));
+        wa = wa - ia * vcross(ra, P);
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + ib * vcross(rb, P);
+    } else {
+        J->impulse[0] = 0.0;
+    }
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void rope_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww, double inv_dt) {
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    v2 ra = k->ra, rb = k->rb;
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 u = V(J->ux, J->uy);
+    v2 vpa = vadd(va, vcross_sv(wa, ra));
+    v2 vpb = vadd(vb, vcross_sv(wb, rb));
+    double C = J->cur_length - J->max_length;
+    double Cdot = vdot(u, vsub(vpb, vpa));
+    if (C < 0.0) Cdot += inv_dt * C;
+    double impulse = -k->dmass * Cdot;
+    double old_impulse = J->impulse[0];
+    J->impulse[0] = pymin(0.0, J->impulse[0] + impulse);
+    impulse = J->impulse[0] - old_impulse;
+    v2 P = vscale(impulse, u);
+    va = vsub(va, vscale(ma, P));
+    wa = wa - ia * vcross(ra, P);
+    vb = vadd(vb, vscale(mb, P));
+    wb = wb + ib * vcross(rb, P);
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static int rope_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 u = vsub(vsub(vadd(cb, rb), ca), ra);
+    double length = vlen(u);
+    u = vnormalized(u);
+    double C = cclamp(length - J->max_length, 0.0, OR_MAX_LINEAR_CORRECTION_J);
+    double impulse = -k->dmass * C;
+    v2 P = vscale(impulse, u);
+    ca = vsub(ca, vscale(ma, P));
+    aa = aa - ia * vcross(ra, P);
+    cb = vadd(cb, vscale(mb, P));
+    ab = ab + ib * vcross(rb, P);
+    pc[k->ia] = ca; pa[k->ia] = aa;
+    pc[k->ib] = cb; pa[k->ib] = ab;
+    return length - J->max_length < OR_LINEAR_SLOP_J;
+}
+
+/* ------------------------------------------------------------ wheel
+ * joints/wheel.py:202-417.  The spring's axis and arms (_ax, _s_ax, _s_bx)
+ * are set only by a set-up with a positive frequency and kept otherwise,
+ * and the velocity passes always run the spring and motor rows
+ * (wheel.py:329-355); the position pass takes its effective mass from the
+ * set-up's arms (wheel.py:397). */
+static void wheel_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt,
+                       double dt_ratio, int warm) {
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    rot qa = rot_of(pa[k->ia]), qb = rot_of(pa[k->ib]);
+    v2 ra = k->ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 d = vsub(vsub(vadd(cb, rb), ca), ra);
+    v2 ay = k->axis = rmul(qa, j_ly(J));
+    J->perp_x = ay.x; J->perp_y = ay.y;            /* _ay, kept for the reaction force */
+    double s_ay = k->s1 = vcross(vadd(d, ra), ay);
+    double s_by = k->s2 = vcross(rb, ay);
+    k->dmass = ma + mb + ia * SQ(s_ay) + ib * SQ(s_by);
+    if (k->dmass > 0.0) k->dmass = 1.0 / k->dmass;
+    k->a1 = 0.0;                                   /* _spring_mass */
+    J->bias = 0.0;
+    J->gamma = 0.0;
+    if (J->frequency > 0.0) {
+        v2 ax = rmul(qa, V(J->ax_x, J->ax_y));
+        J->sax_x = ax.x; J->sax_y = ax.y;
+        J->s_ax = vcross(vadd(d, ra), ax);
+        J->s_bx = vcross(rb, ax);
+        double inv_mass = ma + mb + ia * SQ(J->s_ax) + ib * SQ(J->s_bx);
+        if (inv_mass > 0.0) {
+            k->a1 = 1.0 / inv_mass;
+            double C = vdot(d, ax);
+            double omega = 2.0 * OR_PI * J->frequency;
+            double dd = 2.0 * k->a1 * J->damping_ratio * omega;
+            double kk = k->a1 * SQ(omega);
+            J->gamma = dt * (dd + dt * kk);
+            if (J->gamma > 0.0) J->gamma = 1.0 / J->gamma;
+            J->bias = C * dt * kk * J->gamma;
+            k->a1 = inv_mass + J->gamma;
+            if (k->a1 > 0.0) k->a1 = 1.0 / k->a1;
+        }
+    } else {
+        J->spring_impulse = 0.0;
+    }
+    if (J->flags & GB_J_MOTOR) {
+        k->motor_mass = ia + ib;
+        if (k->motor_mass > 0.0) k->motor_mass = 1.0 / k->motor_mass;
+    } else {
+        k->motor_mass = 0.0;
+        J->motor_impulse = 0.0;
+    }
+    if (warm) {
+        J->impulse[0] = J->impulse[0] * dt_ratio;
+        J->spring_impulse = J->spring_impulse * dt_ratio;
+        J->motor_impulse = J->motor_impulse * dt_ratio;
+        double imp = J->impulse[0], si = J->spring_impulse, mi = J->motor_impulse;
+        v2 P = vadd(vscale(imp, ay), vscale(si, V(J->sax_x, J->sax_y)));
+        double La = imp * s_ay + si * J->s_ax + mi;
+        double Lb = imp * s_by + si * J->s_bx + mi;
+        va = vsub(va, vscale(ma, P));
+        wa = wa - ia * La;
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + ib * Lb;
+    } else {
+        J->impulse[0] = 0.0;
+        J->spring_impulse = 0.0;
+        J->motor_impulse = 0.0;
+    }
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void wheel_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww, double dt) {
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ax = V(J->sax_x, J->sax_y);
+    double Cdot = vdot(ax, vsub(vb, va)) + J->s_bx * wb - J->s_ax * wa;
+    double impulse = -k->a1 * (Cdot + J->bias + J->gamma * J->spring_impulse);
+    J->spring_impulse = J->spring_impulse + impulse;
+    v2 P = vscale(impulse, ax);
+    double La = impulse * J->s_ax, Lb = impulse * J->s_bx;
+    va = vsub(va, vscale(ma, P));
+    wa = wa - ia * La;
+    vb = vadd(vb, vscale(mb, P));
+    wb = wb + ib * Lb;
+    Cdot = wb - wa - J->motor_speed;
+    impulse = -k->motor_mass * Cdot;
+    double old_impulse = J->motor_impulse;
+    double max_impulse = dt * J->max_motor;
+    J->motor_impulse = cclamp(J->motor_impulse + impulse, -max_impulse, max_impulse);
+    impulse = J->motor_impulse - old_impulse;
+    wa = wa - ia * impulse;
+    wb = wb + ib * impulse;
+    Cdot = vdot(k->axis, vsub(vb, va)) + k->s2 * wb - k->s1 * wa;
+    impulse = -k->dmass * Cdot;
+    J->impulse[0] = J->impulse[0] + impulse;
+    P = vscale(impulse, k->axis);
+    La = impulse * k->s1; Lb = impulse * k->s2;
+    va = vsub(va, vscale(ma, P));
+    wa = wa - ia * La;
+    vb = vadd(vb, vscale(mb, P));
+    wb = wb + ib * Lb;
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static int wheel_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 d = vsub(vadd(vsub(cb, ca), rb), ra);
+    double kk = ma + mb + ia * SQ(k->s1) + ib * SQ(k->s2);
+    v2 ay = rmul(qa, j_ly(J));
+    double s_ay = vcross(vadd(d, ra), ay);
+    double s_by = vcross(rb, ay);
+    double C = vdot(d, ay);
+    double impulse = kk != 0.0 ? -C / kk : 0.0;
+    v2 P = vscale(impulse, ay);
+    double La = impulse * s_ay, Lb = impulse * s_by;
+    ca = vsub(ca, vscale(ma, P));
+    aa = aa - ia * La;
+    cb = vadd(cb, vscale(mb, P));
+    ab = ab + ib * Lb;
+    pc[k->ia] = ca; pa[k->ia] = aa;
+    pc[k->ib] = cb; pa[k->ib] = ab;
+    return fabs(C) <= OR_LINEAR_SLOP_J;
+}
+
+/* ------------------------------------------------------------ pulley
+ * joints/pulley.py:156-320.  The set-up's warm start and the position pass
+ * apply the impulses with the effective masses ma + ia * (ra x ua)^2 (the
+ * local names are rebound, pulley.py:190-193, 292-295); the velocity passes
+ * take the inverse masses. */
+static void pulley_arms(const gb_joint *J, v2 ca, v2 ra, v2 cb, v2 rb, v2 *ua, v2 *ub, double *la, double *lb) {
+    v2 a = vsub(vadd(ca, ra), V(J->ga_x, J->ga_y));
+    v2 b = vsub(vadd(cb, rb), V(J->gb_x, J->gb_y));
+    *la = vlen(a);
+    *lb = vlen(b);
+    *ua = *la > 10.0 * OR_LINEAR_SLOP_J ? V(a.x / *la, a.y / *la) : V(0.0, 0.0);
+    *ub = *lb > 10.0 * OR_LINEAR_SLOP_J ? V(b.x / *lb, b.y / *lb) : V(0.0, 0.0);
+}
+
+static void pulley_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt_ratio,
+                        int warm) {
+    double ia = k->iA, ib = k->iB;
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    rot qa = rot_of(pa[k->ia]), qb = rot_of(pa[k->ib]);
+    v2 ra = k->ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    double la, lb;
+    pulley_arms(J, pc[k->ia], ra, pc[k->ib], rb, &k->u, &k->perp, &la, &lb);
+    double rua = vcross(ra, k->u), rub = vcross(rb, k->perp);
+    double ma = k->ma + ia * SQ(rua);
+    double mb = k->mb + ib * SQ(rub);
+    k->dmass = ma + J->ratio * J->ratio * mb;
+    if (k->dmass > 0.0) k->dmass = 1.0 / k->dmass;
+    if (warm) {
+        J->impulse[0] = J->impulse[0] * dt_ratio;
+        v2 Pa = vscale(-J->impulse[0], k->u);
+        v2 Pb = vscale(-J->ratio * J->impulse[0], k->perp);
+        va = vadd(va, vscale(ma, Pa));
+        wa = wa + ia * vcross(ra, Pa);
+        vb = vadd(vb, vscale(mb, Pb));
+        wb = wb + ib * vcross(rb, Pb);
+    } else {
+        J->impulse[0] = 0.0;
+    }
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void pulley_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww) {
+    v2 va = vv[k->ia], vb = vv[k->ib];
+    double wa = ww[k->ia], wb = ww[k->ib];
+    v2 ra = k->ra, rb = k->rb;
+    double ma = k->ma, mb = k->mb, ia = k->iA, ib = k->iB;
+    v2 vpa = vadd(va, vcross_sv(wa, ra));
+    v2 vpb = vadd(vb, vcross_sv(wb, rb));
+    double Cdot = -vdot(k->u, vpa) - J->ratio * vdot(k->perp, vpb);
+    double impulse = -k->dmass * Cdot;
+    J->impulse[0] = J->impulse[0] + impulse;
+    v2 Pa = vscale(-impulse, k->u);
+    v2 Pb = vscale(-J->ratio * impulse, k->perp);
+    va = vadd(va, vscale(ma, Pa));
+    wa = wa + ia * vcross(ra, Pa);
+    vb = vadd(vb, vscale(mb, Pb));
+    wb = wb + ib * vcross(rb, Pb);
+    vv[k->ia] = va; ww[k->ia] = wa;
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static int pulley_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
+    v2 ca = pc[k->ia], cb = pc[k->ib];
+    double aa = pa[k->ia], ab = pa[k->ib];
+    rot qa = rot_of(aa), qb = rot_of(ab);
+    double ia = k->iA, ib = k->iB;
+    v2 ra = rmul(qa, vsub(j_la(J), k->lca));
+    v2 rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    v2 ua, ub;
+    double la, lb;
+    pulley_arms(J, ca, ra, cb, rb, &ua, &ub, &la, &lb);
+    double rua = vcross(ra, ua), rub = vcross(rb, ub);
+    double ma = k->ma + ia * SQ(rua);
+    double mb = k->mb + ib * SQ(rub);
+    double mass = ma + SQ(J->ratio) * mb;
+    if (mass > 0.0) mass = 1.0 / mass;
+    double C = J->constant - la - J->ratio * lb;
+    double linear_error = fabs(C);
+    double impulse = -mass * C;
+    v2 Pa = vscale(-impulse, ua);
+    v2 Pb = vscale(-J->ratio * impulse, ub);
+    ca = vadd(ca, vscale(ma, Pa));
+    aa = aa + ia * vcross(ra, Pa);
+    cb = vadd(cb, vscale(mb, Pb));
+    ab = ab + ib * vcross(rb, Pb);
+    pc[k->ia] = ca; pa[k->ia] = aa;
+    pc[k->ib] = cb; pa[k->ib] = ab;
+    return linear_error < OR_LINEAR_SLOP_J;
+}
+
 /* ------------------------------------------------------------ dispatch */
 static void joint_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt,
                        double dt_ratio, int warm) {
@@ -617,6 +992,10 @@ static void joint_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa,
     case GB_JOINT_REVOLUTE: revolute_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
     case GB_JOINT_PRISMATIC: prismatic_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
     case GB_JOINT_DISTANCE: distance_init(J, k, pc, pa, vv, ww, dt, dt_ratio, warm); break;
+    case GB_JOINT_FRICTION: friction_init(J, k, pa, vv, ww, dt_ratio, warm); break;
+    case GB_JOINT_ROPE: rope_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
+    case GB_JOINT_WHEEL: wheel_init(J, k, pc, pa, vv, ww, dt, dt_ratio, warm); break;
+    case GB_JOINT_PULLEY: pulley_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
     default: weld_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
     }
 }
@@ -625,6 +1004,10 @@ static void joint_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww, d
     case GB_JOINT_REVOLUTE: revolute_solve_velocity(J, k, vv, ww, dt); break;
     case GB_JOINT_PRISMATIC: prismatic_solve_velocity(J, k, vv, ww, dt); break;
     case GB_JOINT_DISTANCE: distance_solve_velocity(J, k, vv, ww); break;
+    case GB_JOINT_FRICTION: friction_solve_velocity(J, k, vv, ww, dt); break;
+    case GB_JOINT_ROPE: rope_solve_velocity(J, k, vv, ww, 1.0 / dt); break;
+    case GB_JOINT_WHEEL: wheel_solve_velocity(J, k, vv, ww, dt); break;
+    case GB_JOINT_PULLEY: pulley_solve_velocity(J, k, vv, ww); break;
     default: weld_solve_velocity(J, k, vv, ww); break;
     }
 }
@@ -633,6 +1016,10 @@ static int joint_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
     case GB_JOINT_REVOLUTE: return revolute_solve_position(J, k, pc, pa);
     case GB_JOINT_PRISMATIC: return prismatic_solve_position(J, k, pc, pa);
     case GB_JOINT_DISTANCE: return distance_solve_position(J, k, pc, pa);
+    case GB_JOINT_FRICTION: return 1;
+    case GB_JOINT_ROPE: return rope_solve_position(J, k, pc, pa);
+    case GB_JOINT_WHEEL: return wheel_solve_position(J, k, pc, pa);
+    case GB_JOINT_PULLEY: return pulley_solve_position(J, k, pc, pa);
     default: return weld_solve_position(J, k, pc, pa);
     }
 }

@@ -311,10 +311,10 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         const gb_joint &J = b->joints[i];
         const bool ok = J.world >= 0 && J.world < b->nw && (i == 0 || J.world >= b->joints[i - 1].world) &&
                         J.body_a >= 0 && J.body_a < b->hdr[J.world].nb && J.body_b >= 0 && J.body_b < b->hdr[J.world].nb &&
-                        J.body_a != J.body_b && J.type >= GB_JOINT_REVOLUTE && J.type <= GB_JOINT_WELD;
+                        J.body_a != J.body_b && J.type >= GB_JOINT_REVOLUTE && J.type <= GB_JOINT_PULLEY;
         if (!ok) {
             delete b;
-            return fail(J.type < GB_JOINT_REVOLUTE || J.type > GB_JOINT_WELD ? GB_E_UNSUPPORTED : GB_E_ARG,
+            return fail(J.type < GB_JOINT_REVOLUTE || J.type > GB_JOINT_PULLEY ? GB_E_UNSUPPORTED : GB_E_ARG,
                         "joint " + std::to_string(i) + ": world out of order, body outside its world or unknown type");
         }
         if (b->hdr[J.world].nj == 0) b->hdr[J.world].jbase = i;

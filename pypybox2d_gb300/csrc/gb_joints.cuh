@@ -1,7 +1,9 @@
 // gb_joints.cuh -- the joint constraints the island solver runs beside the
 // contacts (island.py:107-113, 145-148): revolute (joints/revolute.py:240-453),
-// prismatic (joints/prismatic.py:238-513), distance (joints/distance.py:175-311)
-// and weld (joints/weld.py:118-257).
+// prismatic (joints/prismatic.py:238-513), distance (joints/distance.py:175-311),
+// weld (joints/weld.py:118-257), friction (joints/friction.py:107-233), rope
+// (joints/rope.py:106-248), wheel (joints/wheel.py:202-417) and pulley
+// (joints/pulley.py:156-320).
 //
 // Joints are few next to contacts, so they are solved in float64 in both
 // precision units: the float32 unit widens the bodies' velocities for the
@@ -517,6 +519,337 @@ static __device__ bool weld_position(const gb_joint &J, const JCons &k, vec2<dou
     return position_error <= GB_LINEAR_SLOP_J && angular_error <= GB_ANGULAR_SLOP_J;
 }
 
+// ------------------------------------------------------------ friction
+// Mat22.inverse of the symmetric effective mass (mat22module.c); the velocity
+// passes change only the accumulated impulses: the reference writes the
+// positions back where the velocities belong (friction.py:228-229).
+static __device__ void friction_init(gb_joint &J, JCons &k, double aa, double ab, vec2<double> &va, double &wa,
+                                     vec2<double> &vb, double &wb, double dt_ratio, bool warm) {
+    const double ma = k.ma, mb = k.mb, iA = k.iA, iB = k.iB;
+    const rot2<double> qa = pose_rot(aa), qb = pose_rot(ab);
+    const vec2<double> ra = k.ra = rmul(qa, j_la(J) - k.lca);
+    const vec2<double> rb = k.rb = rmul(qb, j_lb(J) - k.lcb);
+    const double a = ma + mb + iA * ra.y * ra.y + iB * rb.y * rb.y;
+    const double c = -iA * ra.x * ra.y - iB * rb.x * rb.y;
+    const double b = c;
+    const double d = ma + mb + iA * ra.x * ra.x + iB * rb.x * rb.x;
+    double det = a * d - b * c;
+    if (det != 0.0) det = 1.0 / det;
+    k.m.c1 = mk3(det * d, -det * c, 0.0);
+    k.m.c2 = mk3(-det * b, det * a, 0.0);
+    k.motor_mass = iA + iB;
+    if (k.motor_mass > 0.0) k.motor_mass = 1.0 / k.motor_mass;
+    if (warm) {
+        J.impulse[0] = J.impulse[0] * dt_ratio;
+        J.impulse[1] = J.impulse[1] * dt_ratio;
+        J.impulse[2] = J.impulse[2] * dt_ratio;
+        const vec2<double> P = mk<double>(J.impulse[0], J.impulse[1]);
+        va = va - ma * P;
+        wa = wa - iA * (cross(ra, P) + J.impulse[2]);
+        vb = vb + mb * P;
+        wb = wb + iB * (cross(rb, P) + J.impulse[2]);
+    } else {
+        J.impulse[0] = J.impulse[1] = J.impulse[2] = 0.0;
+    }
+}
+
+static __device__ void friction_velocity(gb_joint &J, const JCons &k, vec2<double> va, double wa, vec2<double> vb,
+                                         double wb, double dt) {
+    const double Cdot = wb - wa;
+    double impulse = -k.motor_mass * Cdot;
+    const double old_impulse = J.impulse[2];
+    const double max_impulse = dt * J.max_torque;
+    J.impulse[2] = cclamp(J.impulse[2] + impulse, -max_impulse, max_impulse);
+    impulse = J.impulse[2] - old_impulse;
+    wa = wa - k.iA * impulse;
+    wb = wb + k.iB * impulse;
+    const vec2<double> Cdot2 = vb + cross(wb, k.rb) - va - cross(wa, k.ra);
+    const vec2<double> li = mk<double>(-(k.m.c1.x * Cdot2.x + k.m.c2.x * Cdot2.y), -(k.m.c1.y * Cdot2.x + k.m.c2.y * Cdot2.y));
+    vec2<double> acc = mk<double>(J.impulse[0] + li.x, J.impulse[1] + li.y);
+    const double max_force_impulse = dt * J.max_force;
+    if (acc.x * acc.x + acc.y * acc.y > sq(max_force_impulse)) acc = max_force_impulse * normalized(acc);
+    J.impulse[0] = acc.x;
+    J.impulse[1] = acc.y;
+}
+
+// ------------------------------------------------------------ rope
+// `u /= length` rebinds the local name: the kept _u (ux, uy) is the
+// unnormalised anchor difference, on which the warm start and the velocity
+// passes project (rope.py:140-149, 186-196).
+static __device__ void rope_init(gb_joint &J, JCons &k, vec2<double> ca, double aa, vec2<double> cb, double ab,
+                                 vec2<double> &va, double &wa, vec2<double> &vb, double &wb, double dt_ratio, bool warm) {
+    const double ma = k.ma, mb = k.mb, ia = k.iA, ib = k.iB;
+    const rot2<double> qa = pose_rot(aa), qb = pose_rot(ab);
+    const vec2<double> ra = k.ra = rmul(qa, j_la(J) - k.lca);
+    const vec2<double> rb = k.rb = rmul(qb, j_lb(J) - k.lcb);
+    vec2<double> u = cb + rb - ca - ra;
+    J.ux = u.x; J.uy = u.y;
+    J.cur_length = len(u);
+    const double C = J.cur_length - J.max_length;
+    J.limit_state = C > 0.0 ? GB_LIMIT_UPPER : GB_LIMIT_INACTIVE;
+    if (J.cur_length > GB_LINEAR_SLOP_J) {
+        u = mk<double>(u.x / J.cur_length, u.y / J.cur_length);
+    } else {
+        k.dmass = 0.0;
+        J.impulse[0] = 0.0;
+        return;
+    }
+    const double cra = cross(ra, u), crb = cross(rb, u);
+    const double inv_mass = ma + ia * cra * cra + mb + ib * crb * crb;
+    k.dmass = inv_mass != 0.0 ? 1.0 / inv_mass : 0.0;
+    if (warm) {
+        J.impulse[0] = J.impulse[0] * dt_ratio;
+        const vec2<double> P = J.impulse[0] * mk<double>(J.ux, J.uy);
+        va = va - ma * P;
+        wa = wa - ia * cross(ra, P);
+        vb = vb + mb * P;
+        wb = wb + ib * cross(rb, P);
+    } else {
+        J.impulse[0] = 0.0;
+    }
+}
+
+static __device__ void rope_velocity(gb_joint &J, const JCons &k, vec2<double> &va, double &wa, vec2<double> &vb,
+                                     double &wb, double inv_dt) {
+    const vec2<double> u = mk<double>(J.ux, J.uy);
+    const vec2<double> vpa = va + cross(wa, k.ra);
+    const vec2<double> vpb = vb + cross(wb, k.rb);
+    const double C = J.cur_length - J.max_length;
+    double Cdot = dot(u, vpb - vpa);
+    if (C < 0.0) Cdot += inv_dt * C;
+    double impulse = -k.dmass * Cdot;
+    const double old_impulse = J.impulse[0];
+    J.impulse[0] = pymin(0.0, J.impulse[0] + impulse);
+    impulse = J.impulse[0] - old_impulse;
+    const vec2<double> P = impulse * u;
+    va = va - k.ma * P;
+    wa = wa - k.iA * cross(k.ra, P);
+    vb = vb + k.mb * P;
+    wb = wb + k.iB * cross(k.rb, P);
+}
+
+static __device__ bool rope_position(const gb_joint &J, const JCons &k, vec2<double> &ca, double &aa, vec2<double> &cb,
+                                     double &ab) {
+    const rot2<double> qa = pose_rot(aa), qb = pose_rot(ab);
+    const vec2<double> ra = rmul(qa, j_la(J) - k.lca);
+    const vec2<double> rb = rmul(qb, j_lb(J) - k.lcb);
+    vec2<double> u = cb + rb - ca - ra;
+    const double length = len(u);
+    u = normalized(u);
+    const double C = cclamp(length - J.max_length, 0.0, GB_MAX_LINEAR_CORRECTION_J);
+    const double impulse = -k.dmass * C;
+    const vec2<double> P = impulse * u;
+    ca = ca - k.ma * P;
+    aa = aa - k.iA * cross(ra, P);
+    cb = cb + k.mb * P;
+    ab = ab + k.iB * cross(rb, P);
+    return length - J.max_length < GB_LINEAR_SLOP_J;
+}
+
+// ------------------------------------------------------------ wheel
+// The spring's axis and arms (sax, s_ax, s_bx) are set only by a set-up with
+// a positive frequency and kept otherwise; the velocity passes always run the
+// spring and motor rows (wheel.py:329-355); the position pass takes its
+// effective mass from the set-up's arms (wheel.py:397).
+static __device__ void wheel_init(gb_joint &J, JCons &k, vec2<double> ca, double aa, vec2<double> cb, double ab,
+                                  vec2<double> &va, double &wa, vec2<double> &vb, double &wb, double dt, double dt_ratio,
+                                  bool warm) {
+    const double ma = k.ma, mb = k.mb, ia = k.iA, ib = k.iB;
+    const rot2<double> qa = pose_rot(aa), qb = pose_rot(ab);
+    const vec2<double> ra = k.ra = rmul(qa, j_la(J) - k.lca);
+    const vec2<double> rb = k.rb = rmul(qb, j_lb(J) - k.lcb);
+    const vec2<double> d = cb + rb - ca - ra;
+    const vec2<double> ay = k.axis = rmul(qa, j_ly(J));
+    J.perp_x = ay.x; J.perp_y = ay.y;   // _ay, kept for the reaction force
+    const double s_ay = k.s1 = cross(d + ra, ay);
+    const double s_by = k.s2 = cross(rb, ay);
+    k.dmass = ma + mb + ia * sq(s_ay) + ib * sq(s_by);
+    if (k.dmass > 0.0) k.dmass = 1.0 / k.dmass;
+    k.a1 = 0.0;   // _spring_mass
+    J.bias = 0.0;
+    J.gamma = 0.0;
+    if (J.frequency > 0.0) {
+        const vec2<double> ax = rmul(qa, mk<double>(J.ax_x, J.ax_y));
+        J.sax_x = ax.x; J.sax_y = ax.y;
+        J.s_ax = cross(d + ra, ax);
+        J.s_bx = cross(rb, ax);
+        const double inv_mass = ma + mb + ia * sq(J.s_ax) + ib * sq(J.s_bx);
+        if (inv_mass > 0.0) {
+            k.a1 = 1.0 / inv_mass;
+            const double C = dot(d, ax);
+            const double omega = 2.0 * 3.141592653589793 * J.frequency;
+            const double dd = 2.0 * k.a1 * J.damping_ratio * omega;
+            const double kk = k.a1 * sq(omega);
+            J.gamma = dt * (dd + dt * kk);
+            if (J.gamma > 0.0) J.gamma = 1.0 / J.gamma;
+            J.bias = C * dt * kk * J.gamma;
+            k.a1 = inv_mass + J.gamma;
+            if (k.a1 > 0.0) k.a1 = 1.0 / k.a1;
+        }
+    } else {
+        J.spring_impulse = 0.0;
+    }
+    if (J.flags & GB_J_MOTOR) {
+        k.motor_mass = ia + ib;
+        if (k.motor_mass > 0.0) k.motor_mass = 1.0 / k.motor_mass;
+    } else {
+        k.motor_mass = 0.0;
+        J.motor_impulse = 0.0;
+    }
+    if (warm) {
+        J.impulse[0] = J.impulse[0] * dt_ratio;
+        J.spring_impulse = J.spring_impulse * dt_ratio;
+        J.motor_impulse = J.motor_impulse * dt_ratio;
+        const double imp = J.impulse[0], si = J.spring_impulse, mi = J.motor_impulse;
+        const vec2<double> P = imp * ay + si * mk<double>(J.sax_x, J.sax_y);
+        const double La = imp * s_ay + si * J.s_ax + mi;
+        const double Lb = imp * s_by + si * J.s_bx + mi;
+        va = va - ma * P;
+        wa = wa - ia * La;
+        vb = vb + mb * P;
+        wb = wb + ib * Lb;
+    } else {
+        J.impulse[0] = 0.0;
+        J.spring_impulse = 0.0;
+        J.motor_impulse = 0.0;
+    }
+}
+
+static __device__ void wheel_velocity(gb_joint &J, const JCons &k, vec2<double> &va, double &wa, vec2<double> &vb,
+                                      double &wb, double dt) {
+    const double ma = k.ma, mb = k.mb, ia = k.iA, ib = k.iB;
+    const vec2<double> ax = mk<double>(J.sax_x, J.sax_y);
+    double Cdot = dot(ax, vb - va) + J.s_bx * wb - J.s_ax * wa;
+    double impulse = -k.a1 * (Cdot + J.bias + J.gamma * J.spring_impulse);
+    J.spring_impulse = J.spring_impulse + impulse;
+    vec2<double> P = impulse * ax;
+    double La = impulse * J.s_ax, Lb = impulse * J.s_bx;
+    va = va - ma * P;
+    wa = wa - ia * La;
+    vb = vb + mb * P;
+    wb = wb + ib * Lb;
+    Cdot = wb - wa - J.motor_speed;
+    impulse = -k.motor_mass * Cdot;
+    const double old_impulse = J.motor_impulse;
+    const double max_impulse = dt * J.max_motor;
+    J.motor_impulse = cclamp(J.motor_impulse + impulse, -max_impulse, max_impulse);
+    impulse = J.motor_impulse - old_impulse;
+    wa = wa - ia * impulse;
+    wb = wb + ib * impulse;
+    Cdot = dot(k.axis, vb - va) + k.s2 * wb - k.s1 * wa;
+    impulse = -k.dmass * Cdot;
+    J.impulse[0] = J.impulse[0] + impulse;
+    P = impulse * k.axis;
+    La = impulse * k.s1; Lb = impulse * k.s2;
+    va = va - ma * P;
+    wa = wa - ia * La;
+    vb = vb + mb * P;
+    wb = wb + ib * Lb;
+}
+
+static __device__ bool wheel_position(const gb_joint &J, const JCons &k, vec2<double> &ca, double &aa, vec2<double> &cb,
+                                      double &ab) {
+    const double ma = k.ma, mb = k.mb, ia = k.iA, ib = k.iB;
+    const rot2<double> qa = pose_rot(aa), qb = pose_rot(ab);
+    const vec2<double> ra = rmul(qa, j_la(J) - k.lca);
+    const vec2<double> rb = rmul(qb, j_lb(J) - k.lcb);
+    const vec2<double> d = (cb - ca) + rb - ra;
+    const double kk = ma + mb + ia * sq(k.s1) + ib * sq(k.s2);
+    const vec2<double> ay = rmul(qa, j_ly(J));
+    const double s_ay = cross(d + ra, ay);
+    const double s_by = cross(rb, ay);
+    const double C = dot(d, ay);
+    const double impulse = kk != 0.0 ? -C / kk : 0.0;
+    const vec2<double> P = impulse * ay;
+    const double La = impulse * s_ay, Lb = impulse * s_by;
+    ca = ca - ma * P;
+    aa = aa - ia * La;
+    cb = cb + mb * P;
+    ab = ab + ib * Lb;
+    return fabs(C) <= GB_LINEAR_SLOP_J;
+}
+
+// ------------------------------------------------------------ pulley
+// The warm start and the position pass apply the impulses with the effective
+// masses ma + ia * (ra x ua)^2 (the local names are rebound, pulley.py:190-193,
+// 292-295); the velocity passes take the inverse masses.
+static __device__ void pulley_arms(const gb_joint &J, vec2<double> ca, vec2<double> ra, vec2<double> cb, vec2<double> rb,
+                                   vec2<double> &ua, vec2<double> &ub, double &la, double &lb) {
+    const vec2<double> a = ca + ra - mk<double>(J.ga_x, J.ga_y);
+    const vec2<double> b = cb + rb - mk<double>(J.gb_x, J.gb_y);
+    la = len(a);
+    lb = len(b);
+    ua = la > 10.0 * GB_LINEAR_SLOP_J ? mk<double>(a.x / la, a.y / la) : mk<double>(0.0, 0.0);
+    ub = lb > 10.0 * GB_LINEAR_SLOP_J ? mk<double>(b.x / lb, b.y / lb) : mk<double>(0.0, 0.0);
+}
+
+static __device__ void pulley_init(gb_joint &J, JCons &k, vec2<double> ca, double aa, vec2<double> cb, double ab,
+                                   vec2<double> &va, double &wa, vec2<double> &vb, double &wb, double dt_ratio, bool warm) {
+    const double ia = k.iA, ib = k.iB;
+    const rot2<double> qa = pose_rot(aa), qb = pose_rot(ab);
+    const vec2<double> ra = k.ra = rmul(qa, j_la(J) - k.lca);
+    const vec2<double> rb = k.rb = rmul(qb, j_lb(J) - k.lcb);
+    double la, lb;
+    pulley_arms(J, ca, ra, cb, rb, k.u, k.perp, la, lb);
+    const double rua = cross(ra, k.u), rub = cross(rb, k.perp);
+    const double ma = k.ma + ia * sq(rua);
+    const double mb = k.mb + ib * sq(rub);
+    k.dmass = ma + J.ratio * J.ratio * mb;
+    if (k.dmass > 0.0) k.dmass = 1.0 / k.dmass;
+    if (warm) {
+        J.impulse[0] = J.impulse[0] * dt_ratio;
+        const vec2<double> Pa = (-J.impulse[0]) * k.u;
+        const vec2<double> Pb = (-J.ratio * J.impulse[0]) * k.perp;
+        va = va + ma * Pa;
+        wa = wa + ia * cross(ra, Pa);
+        vb = vb + mb * Pb;
+        wb = wb + ib * cross(rb, Pb);
+    } else {
+        J.impulse[0] = 0.0;
+    }
+}
+
+static __device__ void pulley_velocity(gb_joint &J, const JCons &k, vec2<double> &va, double &wa, vec2<double> &vb,
+                                       double &wb) {
+    const vec2<double> vpa = va + cross(wa, k.ra);
+    const vec2<double> vpb = vb + cross(wb, k.rb);
+    const double Cdot = -dot(k.u, vpa) - J.ratio * dot(k.perp, vpb);
+    const double impulse = -k.dmass * Cdot;
+    J.impulse[0] = J.impulse[0] + impulse;
+    const vec2<double> Pa = (-impulse) * k.u;
+    const vec2<double> Pb = (-J.ratio * impulse) * k.perp;
+    va = va + k.ma * Pa;
+    wa = wa + k.iA * cross(k.ra, Pa);
+    vb = vb + k.mb * Pb;
+    wb = wb + k.iB * cross(k.rb, Pb);
+}
+
+static __device__ bool pulley_position(const gb_joint &J, const JCons &k, vec2<double> &ca, double &aa, vec2<double> &cb,
+                                       double &ab) {
+    const double ia = k.iA, ib = k.iB;
+    const rot2<double> qa = pose_rot(aa), qb = pose_rot(ab);
+    const vec2<double> ra = rmul(qa, j_la(J) - k.lca);
+    const vec2<double> rb = rmul(qb, j_lb(J) - k.lcb);
+    vec2<double> ua, ub;
+    double la, lb;
+    pulley_arms(J, ca, ra, cb, rb, ua, ub, la, lb);
+    const double rua = cross(ra, ua), rub = cross(rb, ub);
+    const double ma = k.ma + ia * sq(rua);
+    const double mb = k.mb + ib * sq(rub);
+    double mass = ma + sq(J.ratio) * mb;
+    if (mass > 0.0) mass = 1.0 / mass;
+    const double C = J.constant - la - J.ratio * lb;
+    const double linear_error = fabs(C);
+    const double impulse = -mass * C;
+    const vec2<double> Pa = (-impulse) * ua;
+    const vec2<double> Pb = (-J.ratio * impulse) * ub;
+    ca = ca + ma * Pa;
+    aa = aa + ia * cross(ra, Pa);
+    cb = cb + mb * Pb;
+    ab = ab + ib * cross(rb, Pb);
+    return linear_error < GB_LINEAR_SLOP_J;
+}
+
 // ------------------------------------------------------------ dispatch
 static __device__ void joint_init(gb_joint &J, JCons &k, vec2<double> ca, double aa, vec2<double> cb, double ab,
                                   vec2<double> &va, double &wa, vec2<double> &vb, double &wb, double dt, double dt_ratio,
@@ -525,6 +858,10 @@ static __device__ void joint_init(gb_joint &J, JCons &k, vec2<double> ca, double
     case GB_JOINT_REVOLUTE: revolute_init(J, k, aa, ab, va, wa, vb, wb, dt_ratio, warm); break;
     case GB_JOINT_PRISMATIC: prismatic_init(J, k, ca, aa, cb, ab, va, wa, vb, wb, dt_ratio, warm); break;
     case GB_JOINT_DISTANCE: distance_init(J, k, ca, aa, cb, ab, va, wa, vb, wb, dt, dt_ratio, warm); break;
+    case GB_JOINT_FRICTION: friction_init(J, k, aa, ab, va, wa, vb, wb, dt_ratio, warm); break;
+    case GB_JOINT_ROPE: rope_init(J, k, ca, aa, cb, ab, va, wa, vb, wb, dt_ratio, warm); break;
+    case GB_JOINT_WHEEL: wheel_init(J, k, ca, aa, cb, ab, va, wa, vb, wb, dt, dt_ratio, warm); break;
+    case GB_JOINT_PULLEY: pulley_init(J, k, ca, aa, cb, ab, va, wa, vb, wb, dt_ratio, warm); break;
     default: weld_init(J, k, aa, ab, va, wa, vb, wb, dt_ratio, warm); break;
     }
 }
@@ -534,6 +871,10 @@ static __device__ void joint_velocity(gb_joint &J, const JCons &k, vec2<double> 
     case GB_JOINT_REVOLUTE: revolute_velocity(J, k, va, wa, vb, wb, dt); break;
     case GB_JOINT_PRISMATIC: prismatic_velocity(J, k, va, wa, vb, wb, dt); break;
     case GB_JOINT_DISTANCE: distance_velocity(J, k, va, wa, vb, wb); break;
+    case GB_JOINT_FRICTION: friction_velocity(J, k, va, wa, vb, wb, dt); break;
+    case GB_JOINT_ROPE: rope_velocity(J, k, va, wa, vb, wb, 1.0 / dt); break;
+    case GB_JOINT_WHEEL: wheel_velocity(J, k, va, wa, vb, wb, dt); break;
+    case GB_JOINT_PULLEY: pulley_velocity(J, k, va, wa, vb, wb); break;
     default: weld_velocity(J, k, va, wa, vb, wb); break;
     }
 }
@@ -543,6 +884,10 @@ static __device__ bool joint_position(const gb_joint &J, const JCons &k, vec2<do
     case GB_JOINT_REVOLUTE: return revolute_position(J, k, ca, aa, cb, ab);
     case GB_JOINT_PRISMATIC: return prismatic_position(J, k, ca, aa, cb, ab);
     case GB_JOINT_DISTANCE: return distance_position(J, k, ca, aa, cb, ab);
+    case GB_JOINT_FRICTION: return true;
+    case GB_JOINT_ROPE: return rope_position(J, k, ca, aa, cb, ab);
+    case GB_JOINT_WHEEL: return wheel_position(J, k, ca, aa, cb, ab);
+    case GB_JOINT_PULLEY: return pulley_position(J, k, ca, aa, cb, ab);
     default: return weld_position(J, k, ca, aa, cb, ab);
     }
 }

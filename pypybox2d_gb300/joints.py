@@ -1,6 +1,6 @@
 """The joint classes of the reference (pypybox2d/joints/): revolute,
-prismatic, distance and weld, with their constructors, properties, setters
-and reaction getters.
+prismatic, distance, weld, friction, rope, wheel and pulley, with their
+constructors, properties, setters and reaction getters.
 
 A joint is a view of one ``abi.JOINT`` record of its world (definition and
 carried state: impulses, motor impulse, limit state); the GPU step solves
@@ -465,5 +465,259 @@ class WeldJoint(Joint):
         return float(self._rec()["ref_angle"])
 
 
+def _valid_float(v):
+    """common.py is_valid_float: a finite number"""
+    return isinstance(v, (int, float)) and math.isfinite(v)
+
+
+class FrictionJoint(Joint):
+    """joints/friction.py:30-233: translational and angular friction between
+    two bodies.  The reference's velocity passes write the positions back
+    where the velocities belong (friction.py:228-229), so the joint acts on
+    the bodies only through the warm start of each set-up; the passes update
+    the accumulated impulses."""
+
+    _type = abi.JOINT_FRICTION
+
+    def __init__(self, body_a, body_b, local_anchor_a=(0, 0), local_anchor_b=(0, 0), max_force=0.0, max_torque=0.0,
+                 collide_connected=False):
+        if body_a is None or body_b is None:
+            raise ValueError("body_a and body_b must be set")
+        Joint.__init__(self, body_a, body_b, collide_connected)
+        self._set_anchors(None, None, local_anchor_a, local_anchor_b)
+        r = self._pending
+        r["max_force"], r["max_torque"] = max_force, max_torque
+
+    def get_reaction_force(self, inv_dt):
+        r = self._rec()
+        return _V(inv_dt * float(r["impulse"][0]), inv_dt * float(r["impulse"][1]))
+
+    def get_reaction_torque(self, inv_dt):
+        return inv_dt * float(self._rec()["impulse"][2])
+
+    @property
+    def max_force(self):
+        return float(self._rec()["max_force"])
+
+    @max_force.setter
+    def max_force(self, value):
+        if not _valid_float(value) or value < 0.0:
+            raise ValueError("Max force must be >= 0.0")
+        self._edit()["max_force"] = value
+
+    @property
+    def max_torque(self):
+        return float(self._rec()["max_torque"])
+
+    @max_torque.setter
+    def max_torque(self, value):
+        if not _valid_float(value) or value < 0.0:
+            raise ValueError("Max torque must be >= 0.0")
+        self._edit()["max_torque"] = value
+
+
+class RopeJoint(Joint):
+    """joints/rope.py:32-248: a maximum distance between two anchors.  The
+    reference's limit_state property reads an attribute it never sets
+    (rope.py:93-95; the state is kept as _state) and raises AttributeError,
+    as here."""
+
+    _type = abi.JOINT_ROPE
+
+    def __init__(self, body_a, body_b, local_anchor_a=(0, 0), local_anchor_b=(0, 0), max_length=0.0,
+                 collide_connected=False):
+        if body_a is None or body_b is None:
+            raise ValueError("body_a and body_b must be set")
+        Joint.__init__(self, body_a, body_b, collide_connected)
+        self._set_anchors(None, None, local_anchor_a, local_anchor_b)
+        self._pending["max_length"] = max_length
+
+    def get_reaction_force(self, inv_dt):
+        """(inv_dt * impulse) * _u, _u the unnormalised anchor difference of
+        the last set-up (rope.py:140, 84-86)"""
+        r = self._rec()
+        s = inv_dt * float(r["impulse"][0])
+        return _V(s * float(r["ux"]), s * float(r["uy"]))
+
+    def get_reaction_torque(self, inv_dt):
+        return 0.0
+
+    @property
+    def limit_state(self):
+        raise AttributeError("'RopeJoint' object has no attribute '_limit_state'")
+
+    @property
+    def max_length(self):
+        return float(self._rec()["max_length"])
+
+
+class WheelJoint(Joint):
+    """joints/wheel.py:32-417: translation along an axis fixed in body_a
+    with a spring, rotation with a motor.  As in the reference, the
+    spring_frequency and spring_damping_ratio properties read attributes the
+    constructor never sets (wheel.py:184-199): reading one before setting it
+    raises AttributeError, and setting one does not reach the solver, which
+    runs the constructor's frequency and damping ratio."""
+
+    _type = abi.JOINT_WHEEL
+
+    def __init__(self, body_a, body_b, anchor=None, axis=None, frequency=2.0, damping_ratio=0.7, motor_enabled=False,
+                 motor_speed=0.0, max_motor_torque=0.0, local_anchor_a=None, local_anchor_b=None, local_x_axis=None,
+                 collide_connected=False):
+        if body_a is None or body_b is None:
+            raise ValueError("body_a and body_b must be set")
+        Joint.__init__(self, body_a, body_b, collide_connected)
+        self._set_anchors(anchor, anchor, local_anchor_a, local_anchor_b)
+        r = self._pending
+        ax = local_x_axis if local_x_axis is not None else body_a.get_local_vector(axis)
+        r["ax_x"], r["ax_y"] = float(ax[0]), float(ax[1])
+        r["frequency"], r["damping_ratio"] = float(frequency), float(damping_ratio)
+        r["max_motor"], r["motor_speed"] = float(max_motor_torque), float(motor_speed)
+        if motor_enabled:
+            r["flags"] = int(r["flags"]) | abi.J_MOTOR
+
+    def get_reaction_force(self, inv_dt):
+        """inv_dt * (impulse * _ay + spring_impulse * _ax) of the last set-up"""
+        r = self._rec()
+        imp, si = float(r["impulse"][0]), float(r["spring_impulse"])
+        return _V(inv_dt * (imp * float(r["perp_x"]) + si * float(r["sax_x"])),
+                  inv_dt * (imp * float(r["perp_y"]) + si * float(r["sax_y"])))
+
+    def get_reaction_torque(self, inv_dt):
+        return inv_dt * float(self._rec()["motor_impulse"])
+
+    @property
+    def local_x_axis(self):
+        r = self._rec()
+        return _V(r["ax_x"], r["ax_y"])
+
+    @property
+    def joint_translation(self):
+        d = _sub(self.anchor_b, self.anchor_a)
+        axis = self._body_a.get_world_vector(self.local_x_axis)
+        return d[0] * axis[0] + d[1] * axis[1]
+
+    @property
+    def joint_speed(self):
+        """wheel.py:127-130: the bodies' angular velocity difference"""
+        return self._body_b.angular_velocity - self._body_a.angular_velocity
+
+    @property
+    def motor_enabled(self):
+        return self._flag(abi.J_MOTOR)
+
+    @motor_enabled.setter
+    def motor_enabled(self, on):
+        if bool(on) != self.motor_enabled:
+            self._wake()
+            self._set_flag(abi.J_MOTOR, bool(on))
+
+    @property
+    def motor_speed(self):
+        return float(self._rec()["motor_speed"])
+
+    @motor_speed.setter
+    def motor_speed(self, speed):
+        self._wake()
+        self._edit()["motor_speed"] = speed
+
+    @property
+    def max_motor_torque(self):
+        return float(self._rec()["max_motor"])
+
+    @max_motor_torque.setter
+    def max_motor_torque(self, torque):
+        self._wake()
+        self._edit()["max_motor"] = torque
+
+    def motor_torque(self, inv_dt):
+        return inv_dt * float(self._rec()["motor_impulse"])
+
+    @property
+    def spring_frequency(self):
+        try:
+            return self.__dict__["_spring_frequency"]
+        except KeyError:
+            raise AttributeError("'WheelJoint' object has no attribute '_spring_frequency'") from None
+
+    @spring_frequency.setter
+    def spring_frequency(self, value):
+        self.__dict__["_spring_frequency"] = value
+
+    @property
+    def spring_damping_ratio(self):
+        try:
+            return self.__dict__["_spring_damping_ratio"]
+        except KeyError:
+            raise AttributeError("'WheelJoint' object has no attribute '_spring_damping_ratio'") from None
+
+    @spring_damping_ratio.setter
+    def spring_damping_ratio(self, value):
+        self.__dict__["_spring_damping_ratio"] = value
+
+
+class PulleyJoint(Joint):
+    """joints/pulley.py:32-320: two bodies hung from two ground anchors with
+    length_a + ratio * length_b held at its initial value.  The reference's
+    reaction force reads a direction it never sets (pulley.py:103-105, _u2
+    stays the zero vector), so it is zero, as here."""
+
+    _type = abi.JOINT_PULLEY
+
+    def __init__(self, body_a, body_b, ground_anchor_a=(0, 0), ground_anchor_b=(0, 0), anchor_a=(0, 0),
+                 anchor_b=(0, 0), ratio=1.0, length_a=None, length_b=None, collide_connected=False,
+                 local_anchor_a=None, local_anchor_b=None):
+        if body_a is None or body_b is None:
+            raise ValueError("body_a and body_b must be set")
+        Joint.__init__(self, body_a, body_b, collide_connected)
+        if ratio == 0.0 or ratio < 2.220446049250313e-16:
+            raise ValueError("Ratio must be positive, non-zero and not too small")
+        self._set_anchors(anchor_a, anchor_b, local_anchor_a, local_anchor_b)
+        r = self._pending
+        r["ga_x"], r["ga_y"] = float(ground_anchor_a[0]), float(ground_anchor_a[1])
+        r["gb_x"], r["gb_y"] = float(ground_anchor_b[0]), float(ground_anchor_b[1])
+        if length_a is None:   # from the world anchor arguments (pulley.py:80-83)
+            dx, dy = anchor_a[0] - r["ga_x"], anchor_a[1] - r["ga_y"]
+            length_a = math.sqrt(dx * dx + dy * dy)
+        if length_b is None:
+            dx, dy = anchor_b[0] - r["gb_x"], anchor_b[1] - r["gb_y"]
+            length_b = math.sqrt(dx * dx + dy * dy)
+        self._length_a, self._length_b = length_a, length_b
+        r["constant"] = length_a + ratio * length_b
+        r["ratio"] = ratio
+
+    def get_reaction_force(self, inv_dt):
+        s = inv_dt * float(self._rec()["impulse"][0])
+        return _V(s * 0.0, s * 0.0)
+
+    def get_reaction_torque(self, inv_dt):
+        return 0.0
+
+    @property
+    def ground_anchor_a(self):
+        r = self._rec()
+        return _V(r["ga_x"], r["ga_y"])
+
+    @property
+    def ground_anchor_b(self):
+        r = self._rec()
+        return _V(r["gb_x"], r["gb_y"])
+
+    @property
+    def length_a(self):
+        d = _sub(self.anchor_a, self.ground_anchor_a)
+        return math.sqrt(d[0] * d[0] + d[1] * d[1])
+
+    @property
+    def length_b(self):
+        d = _sub(self.anchor_b, self.ground_anchor_b)
+        return math.sqrt(d[0] * d[0] + d[1] * d[1])
+
+    @property
+    def ratio(self):
+        return float(self._rec()["ratio"])
+
+
 KINDS = {abi.JOINT_REVOLUTE: RevoluteJoint, abi.JOINT_PRISMATIC: PrismaticJoint, abi.JOINT_DISTANCE: DistanceJoint,
-         abi.JOINT_WELD: WeldJoint}
+         abi.JOINT_WELD: WeldJoint, abi.JOINT_FRICTION: FrictionJoint, abi.JOINT_ROPE: RopeJoint,
+         abi.JOINT_WHEEL: WheelJoint, abi.JOINT_PULLEY: PulleyJoint}

@@ -1187,12 +1187,22 @@ class World:
     def create_weld_joint(self, *args, **kwargs):
         return self.add_joint(WeldJoint(*args, **kwargs))
 
-    def _unsupported(self, *args, **kwargs):
-        raise NotImplementedError("friction, gear, mouse, pulley, rope and wheel joints are not part of the GPU "
-                                  "world step")
+    def create_friction_joint(self, *args, **kwargs):
+        return self.add_joint(_joints.FrictionJoint(*args, **kwargs))
 
-    create_friction_joint = create_gear_joint = create_mouse_joint = _unsupported
-    create_pulley_joint = create_rope_joint = create_wheel_joint = _unsupported
+    def create_rope_joint(self, *args, **kwargs):
+        return self.add_joint(_joints.RopeJoint(*args, **kwargs))
+
+    def create_wheel_joint(self, *args, **kwargs):
+        return self.add_joint(_joints.WheelJoint(*args, **kwargs))
+
+    def create_pulley_joint(self, *args, **kwargs):
+        return self.add_joint(_joints.PulleyJoint(*args, **kwargs))
+
+    def _unsupported(self, *args, **kwargs):
+        raise NotImplementedError("gear and mouse joints are not part of the GPU world step")
+
+    create_gear_joint = create_mouse_joint = _unsupported
 
     # -- controllers (world.py:923-957)
     def create_gravity_controller(self, *args, **kwargs):

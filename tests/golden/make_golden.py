@@ -242,7 +242,9 @@ def export_joints(world, b2):
     bidx = {id(b): i for i, b in enumerate(world.bodies)}
     J = np.zeros(len(world.joints), dtype=abi.JOINT)
     kinds = ((jm.RevoluteJoint, abi.JOINT_REVOLUTE), (jm.PrismaticJoint, abi.JOINT_PRISMATIC),
-             (jm.DistanceJoint, abi.JOINT_DISTANCE), (jm.WeldJoint, abi.JOINT_WELD))
+             (jm.DistanceJoint, abi.JOINT_DISTANCE), (jm.WeldJoint, abi.JOINT_WELD),
+             (jm.FrictionJoint, abi.JOINT_FRICTION), (jm.RopeJoint, abi.JOINT_ROPE), (jm.WheelJoint, abi.JOINT_WHEEL),
+             (jm.PulleyJoint, abi.JOINT_PULLEY))
     for i, j in enumerate(world.joints):
         r = J[i]
         r["type"] = next(t for cls, t in kinds if type(j) is cls)
@@ -255,6 +257,32 @@ def export_joints(world, b2):
         r["flags"] = fl
         r["la_x"], r["la_y"] = j._local_anchor_a.x, j._local_anchor_a.y
         r["lb_x"], r["lb_y"] = j._local_anchor_b.x, j._local_anchor_b.y
+        if r["type"] == abi.JOINT_FRICTION:
+            r["max_force"], r["max_torque"] = j._max_force, j._max_torque
+            r["impulse"][:] = (j._linear_impulse.x, j._linear_impulse.y, j._angular_impulse)
+            continue
+        if r["type"] == abi.JOINT_ROPE:
+            r["max_length"], r["cur_length"] = j._max_length, j._length
+            r["impulse"][0] = j._impulse
+            r["limit_state"] = j._state
+            r["ux"], r["uy"] = j._u.x, j._u.y
+            continue
+        if r["type"] == abi.JOINT_WHEEL:
+            r["ax_x"], r["ax_y"] = j._local_x_axis.x, j._local_x_axis.y
+            r["frequency"], r["damping_ratio"] = j._frequency, j._damping_ratio
+            r["max_motor"], r["motor_speed"] = j._max_motor_torque, j._motor_speed
+            r["impulse"][0] = j._impulse
+            r["motor_impulse"], r["spring_impulse"] = j._motor_impulse, j._spring_impulse
+            r["sax_x"], r["sax_y"], r["s_ax"], r["s_bx"] = j._ax.x, j._ax.y, j._s_ax, j._s_bx
+            r["perp_x"], r["perp_y"] = j._ay.x, j._ay.y
+            r["bias"], r["gamma"] = j._bias, j._gamma
+            continue
+        if r["type"] == abi.JOINT_PULLEY:
+            r["ga_x"], r["ga_y"] = j._ground_anchor_a.x, j._ground_anchor_a.y
+            r["gb_x"], r["gb_y"] = j._ground_anchor_b.x, j._ground_anchor_b.y
+            r["ratio"], r["constant"] = j._ratio, j._constant
+            r["impulse"][0] = j._impulse
+            continue
         if r["type"] == abi.JOINT_DISTANCE:
             r["length"], r["frequency"], r["damping_ratio"] = j._length, j._frequency, j._damping_ratio
             r["impulse"][0] = j._impulse
@@ -580,6 +608,58 @@ def scene_bridge(b2, planks=30, seed=19):
     return world
 
 
+def scene_joints2(b2, seed=37):
+    """The friction, rope, wheel and pulley joints: a box sliding on the
+    ground held back by a friction joint, a ball on a slack rope that pulls
+    taut, a two-wheeled cart on sprung wheel joints with a motor on the rear
+    wheel, a wheel without a spring (frequency 0, whose spring axis keeps
+    its initial zero), and two boxes on a pulley with ratio 1.5, plus a few
+    boxes dropped among them."""
+    rng = random.Random(seed)
+    world = b2.World(gravity=(0, -10), do_sleep=True)
+    ground = world.create_static_body(position=(0, -0.5), shapes=b2.Polygon(box=(40, 0.5)))
+    # friction: a box sliding right, held back by a friction joint to the ground
+    slider = world.create_dynamic_body(position=(-20, 0.5), linear_velocity=(6, 0), angular_velocity=1.0)
+    slider.create_polygon_fixture(box=(0.5, 0.5), density=1.0, friction=0.1)
+    world.create_friction_joint(ground, slider, local_anchor_a=(-20, 0.5), local_anchor_b=(0, 0), max_force=4.0,
+                                max_torque=1.5)
+    # rope: a pendulum on a rope longer than its initial distance
+    hook = world.create_static_body(position=(-10, 10))
+    hook.create_circle_fixture(0.2)
+    ball = world.create_dynamic_body(position=(-8, 9))
+    ball.create_circle_fixture(0.4, density=2.0)
+    world.create_rope_joint(hook, ball, local_anchor_a=(0, 0), local_anchor_b=(0, 0), max_length=4.0)
+    # wheel: a cart, rear wheel driven
+    cart = world.create_dynamic_body(position=(0, 1.6))
+    cart.create_polygon_fixture(box=(1.5, 0.3), density=1.0, friction=0.4)
+    rear = world.create_dynamic_body(position=(-1.0, 0.9))
+    rear.create_circle_fixture(0.4, density=1.0, friction=0.9)
+    front = world.create_dynamic_body(position=(1.0, 0.9))
+    front.create_circle_fixture(0.4, density=1.0, friction=0.9)
+    world.create_wheel_joint(cart, rear, anchor=(-1.0, 0.9), axis=(0, 1), frequency=4.0, damping_ratio=0.7,
+                             motor_enabled=True, motor_speed=-8.0, max_motor_torque=15.0)
+    world.create_wheel_joint(cart, front, anchor=(1.0, 0.9), axis=(0, 1), frequency=4.0, damping_ratio=0.7)
+    # a wheel joint without a spring on a separate body pair
+    axle = world.create_dynamic_body(position=(8, 2.5))
+    axle.create_polygon_fixture(box=(0.8, 0.2), density=1.0)
+    hub = world.create_dynamic_body(position=(8, 1.8))
+    hub.create_circle_fixture(0.35, density=1.0, friction=0.8)
+    world.create_wheel_joint(axle, hub, anchor=(8, 1.8), axis=(0.2, 1.0), frequency=0.0, motor_enabled=True,
+                             motor_speed=3.0, max_motor_torque=5.0)
+    # pulley: two boxes hung from ground anchors, ratio 1.5
+    pa = world.create_dynamic_body(position=(14, 6))
+    pa.create_polygon_fixture(box=(0.4, 0.4), density=1.0)
+    pb = world.create_dynamic_body(position=(18, 5))
+    pb.create_polygon_fixture(box=(0.5, 0.5), density=1.0)
+    world.create_pulley_joint(pa, pb, ground_anchor_a=(14, 12), ground_anchor_b=(18, 12), anchor_a=(14, 6.4),
+                              anchor_b=(18, 5.5), ratio=1.5)
+    for i in range(6):
+        b = world.create_dynamic_body(position=(-14 + 5.5 * i + rng.uniform(-0.5, 0.5), 7 + rng.uniform(0, 3)),
+                                      angle=rng.uniform(-1, 1))
+        b.create_polygon_fixture(box=(0.35, 0.35), density=1.0, friction=0.5)
+    return world
+
+
 def scene_loops(b2, seed=23):
     """Loop shapes: a static closed terrain loop (a valley with a hill whose
     top vertex is the body's origin, so its neighbouring child edges lose
@@ -703,6 +783,7 @@ SCENES = {
     "bridge": (scene_bridge, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
     "loops": (scene_loops, 180, (1, 2, 5, 20, 21, 60, 61, 120, 121, 180)),
     "buoyancy": (scene_buoyancy, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
+    "joints2": (scene_joints2, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
     "gravity": (scene_gravity, 240, (1, 2, 5, 20, 21, 60, 61, 120, 121, 240)),
 }
 
@@ -824,6 +905,24 @@ def run_api_joints(b2):
           f"{os.path.getsize(path)} bytes")
 
 
+def run_api_joints2(b2):
+    """tests/golden/api_joints2.py on the reference -> api_joints2.npz."""
+    sys.path.insert(0, HERE)
+    import api_joints2
+    out = {}
+
+    def snap(label, world):
+        W, B, F, C = export_world(world, b2)
+        out[f"{label}_bodies"], out[f"{label}_contacts"] = B, C
+        out[f"{label}_joints"] = export_joints(world, b2)
+        out[f"{label}_getters"] = np.array([api_joints2.getter_row(j) for j in world.joints], dtype=np.float64)
+
+    api_joints2.script(b2, snap, on_world=pair_order_hook)
+    path = os.path.join(HERE, "api_joints2.npz")
+    np.savez_compressed(path, **out)
+    print(f"api_joints2: {len(api_joints2.SNAPS)} snapshots -> {os.path.getsize(path)} bytes")
+
+
 def run_api_active(b2):
     """tests/golden/api_active.py on the reference -> api_active.npz."""
     sys.path.insert(0, HERE)
@@ -893,6 +992,8 @@ def main():
         run_api_joints(b2)
     if not args.only or args.only == "api_active":
         run_api_active(b2)
+    if not args.only or args.only == "api_joints2":
+        run_api_joints2(b2)
     if not args.only or args.only == "api_loops":
         run_api_loops(b2)
     if not args.only or args.only == "api_controllers":

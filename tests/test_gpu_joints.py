@@ -57,7 +57,8 @@ def _batch(names):
     return cat(Ws), cat(Bs), cat(Fs), cat(Js)
 
 
-@pytest.mark.parametrize("names", [("joints", "mixed", "bridge", "joints"), ("bridge", "bridge", "pyramid5", "joints")])
+@pytest.mark.parametrize("names", [("joints", "mixed", "bridge", "joints"), ("bridge", "bridge", "pyramid5", "joints"),
+                                   ("joints2", "joints", "mixed", "joints2")])
 def test_batch_of_worlds_with_and_without_joints(names):
     from pypybox2d_gb300.gpu import GpuBatch
     W, B, F, J = _batch(names)
@@ -76,7 +77,7 @@ def test_batch_of_worlds_with_and_without_joints(names):
     assert not g.status().any()
 
 
-@pytest.mark.parametrize("scene", ["joints", "bridge", "loops", "buoyancy", "gravity"])
+@pytest.mark.parametrize("scene", ["joints", "bridge", "joints2", "loops", "buoyancy", "gravity"])
 def test_f32_joint_step_against_f64(scene):
     from pypybox2d_gb300.gpu import GpuBatch
     W, B, F, J = _scene(scene)

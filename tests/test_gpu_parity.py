@@ -27,7 +27,8 @@ pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 STEPS = {"pyramid": 40, "pyramid5": 150, "mixed": 120, "bullets": 60, "sleep": 90, "uneven": 240, "kinematic": 180,
-         "sensor_filter": 150, "joints": 300, "bridge": 240, "loops": 180, "buoyancy": 240, "gravity": 240}
+         "sensor_filter": 150, "joints": 300, "bridge": 240, "loops": 180, "buoyancy": 240, "gravity": 240,
+         "joints2": 240}
 
 
 def _gpu():

@@ -42,14 +42,15 @@ from pypybox2d_gb300 import abi
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-SCENES = ("bridge", "buoyancy", "bullets", "gravity", "joints", "kinematic", "loops", "mixed", "pyramid", "pyramid5",
-          "sensor_filter", "sleep", "uneven")
+SCENES = ("bridge", "buoyancy", "bullets", "gravity", "joints", "joints2", "kinematic", "loops", "mixed", "pyramid",
+          "pyramid5", "sensor_filter", "sleep", "uneven")
 ONE_STEP_TOL_M = 2e-2
 JOINT_ONE_STEP_TOL_M = 5e-2
 FREE_TOL_M = 5e-2
 # scene -> last snapshot step at which the free run is held to the reference
 FREE_HELD = {"bullets": 41, "kinematic": 61, "mixed": 21, "pyramid": 10, "pyramid5": 5, "sensor_filter": 150,
-             "sleep": 90, "uneven": 61, "joints": 21, "bridge": 21, "loops": 21, "buoyancy": 61, "gravity": 240}
+             "sleep": 90, "uneven": 61, "joints": 21, "bridge": 21, "loops": 21, "buoyancy": 61, "gravity": 240,
+             "joints2": 61}
 # scene -> contacts allowed to differ in discrete fields after one step, over all its one-step states
 DISCRETE_ONE_STEP = {"pyramid": 1}
 

@@ -58,7 +58,7 @@ def oracle_world_class():
     return OracleBackedWorld
 
 
-@pytest.mark.parametrize("scene", ["joints", "bridge"])
+@pytest.mark.parametrize("scene", ["joints", "bridge", "joints2"])
 def test_joint_scene_construction_matches_reference(scene):
     d = np.load(os.path.join(GOLDEN, scene + ".npz"))
     w = getattr(make_golden, "scene_" + scene)(b2)
@@ -100,6 +100,72 @@ def test_joint_session_matches_reference_bitwise():
         same(J, d[f"{label}_joints"], f"{label} joints")
         want = d[f"{label}_getters"]
         assert G.shape == want.shape and np.array_equal(G, want, equal_nan=True), f"{label} joint getters"
+
+
+def _run_script2(world_class):
+    import api_joints2
+    snaps = {}
+
+    class Recorder(world_class):
+        pass
+
+    def snap(label, world):
+        world._materialise()
+        getters = np.array([api_joints2.getter_row(j) for j in world.joints], dtype=np.float64)
+        snaps[label] = (world._B.copy(), world._C.copy(), world._J.copy(), getters)
+
+    orig = b2.World
+    b2.World = Recorder
+    try:
+        api_joints2.script(b2, snap)
+    finally:
+        b2.World = orig
+    return snaps
+
+
+def test_friction_rope_wheel_pulley_session_matches_reference_bitwise():
+    """tests/golden/api_joints2.py: the friction, rope, wheel and pulley
+    joints created, stepped, edited through their setters and destroyed;
+    bodies, contacts, joint records and getters bit for bit on the CPU
+    restatement."""
+    import api_joints2
+    d = np.load(os.path.join(GOLDEN, "api_joints2.npz"))
+    snaps = _run_script2(oracle_world_class())
+    for label in api_joints2.SNAPS:
+        B, C, J, G = snaps[label]
+        same(B, d[f"{label}_bodies"], f"{label} bodies")
+        same(used(C), used(d[f"{label}_contacts"]), f"{label} contacts")
+        same(J, d[f"{label}_joints"], f"{label} joints")
+        want = d[f"{label}_getters"]
+        assert G.shape == want.shape and np.array_equal(G, want, equal_nan=True), f"{label} joint getters"
+
+
+def test_new_joint_kinds_api():
+    w = b2.World()
+    a = w.create_dynamic_body(position=(0, 0))
+    a.create_circle_fixture(0.5, density=1.0)
+    c = w.create_dynamic_body(position=(2, 0))
+    c.create_circle_fixture(0.5, density=1.0)
+    fr = w.create_friction_joint(a, c, max_force=1.0)
+    with pytest.raises(ValueError):                 # friction.py:84-86
+        fr.max_force = -1.0
+    rope = w.create_rope_joint(a, c, max_length=3.0)
+    with pytest.raises(AttributeError):             # rope.py:93-95 reads an attribute it never sets
+        rope.limit_state
+    wheel = w.create_wheel_joint(a, c, anchor=(2, 0), axis=(0, 1))
+    with pytest.raises(AttributeError):             # wheel.py:184-188
+        wheel.spring_frequency
+    wheel.spring_frequency = 3.0
+    assert wheel.spring_frequency == 3.0 and float(wheel._rec()["frequency"]) == 2.0
+    with pytest.raises(ValueError):                 # pulley.py:62-63
+        w.create_pulley_joint(a, c, ratio=0.0)
+    p = w.create_pulley_joint(a, c, ground_anchor_a=(0, 5), ground_anchor_b=(2, 5), anchor_a=(0, 0),
+                              anchor_b=(2, 0), ratio=2.0)
+    assert p.ratio == 2.0 and tuple(p.get_reaction_force(60.0)) == (0.0, 0.0)
+    assert float(p._rec()["constant"]) == 5.0 + 2.0 * 5.0
+    assert w.joints == [fr, rope, wheel, p]
+    with pytest.raises(NotImplementedError):
+        w.create_gear_joint(wheel, wheel)
 
 
 def test_joint_api_errors():
