@@ -172,7 +172,7 @@ typedef struct gb_contact {
 } gb_contact;
 
 /* joint types (pypybox2d/joints/: revolute.py, prismatic.py, distance.py, weld.py,
- * friction.py, rope.py, wheel.py, pulley.py) */
+ * friction.py, rope.py, wheel.py, pulley.py, mouse.py) */
 #define GB_JOINT_REVOLUTE 1
 #define GB_JOINT_PRISMATIC 2
 #define GB_JOINT_DISTANCE 3
@@ -181,6 +181,7 @@ typedef struct gb_contact {
 #define GB_JOINT_ROPE 6
 #define GB_JOINT_WHEEL 7
 #define GB_JOINT_PULLEY 8
+#define GB_JOINT_MOUSE 9   /* one body: the reference's body_a is None; the record gives body_a = body_b */
 
 /* gb_joint.flags */
 #define GB_J_COLLIDE_CONNECTED 1u /* Joint._collide_connected */
@@ -225,6 +226,7 @@ typedef struct gb_joint {
     double sax_x, sax_y, s_ax, s_bx; /* wheel _ax, _s_ax, _s_bx: set by a set-up with a spring, kept otherwise */
     double ga_x, ga_y, gb_x, gb_y; /* pulley ground anchors */
     double ratio, constant;        /* pulley _ratio, _constant */
+    double target_x, target_y;     /* mouse _target (max_force: _max_force; bias: _beta; gamma: _gamma) */
 } gb_joint;
 
 /* controller kinds (pypybox2d/controllers.py) */

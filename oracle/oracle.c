@@ -752,7 +752,7 @@ static void island_solve(or_world *w, const int *bodies, int nbi, int *contacts,
         k->lcb = V(bb->lcx, bb->lcy);
         k->ma = ba->inv_mass; k->mb = bb->inv_mass;
         k->iA = ba->inv_I; k->iB = bb->inv_I;
-        joint_init(J, k, pc, pa, vv, ww, dt, dt_ratio, warm);
+        joint_init(J, k, pc, pa, vv, ww, dt, dt_ratio, bb->mass, warm);
     }
     /* velocity iterations: the joints, then the contacts (island.py:110-113) */
     for (int it = 0; it < vel_iters; ++it) {
@@ -1248,8 +1248,9 @@ void or_clear_status(or_world *w) { w->status = 0; }
 int or_set_joints(or_world *w, const gb_joint *joints, int n) {
     for (int i = 0; i < n; ++i) {
         const gb_joint *J = &joints[i];
-        if (J->body_a < 0 || J->body_a >= w->nb || J->body_b < 0 || J->body_b >= w->nb || J->body_a == J->body_b ||
-            J->type < GB_JOINT_REVOLUTE || J->type > GB_JOINT_PULLEY)
+        if (J->body_a < 0 || J->body_a >= w->nb || J->body_b < 0 || J->body_b >= w->nb ||
+            (J->type == GB_JOINT_MOUSE ? J->body_a != J->body_b : J->body_a == J->body_b) ||
+            J->type < GB_JOINT_REVOLUTE || J->type > GB_JOINT_MOUSE)
             return -1;
     }
     for (int i = 0; i < w->nb; ++i) w->bjoint[i].n = 0;
@@ -1260,7 +1261,7 @@ int or_set_joints(or_world *w, const gb_joint *joints, int n) {
     w->nj = n;
     for (int i = 0; i < n; ++i) {
         iv_push(&w->bjoint[w->j[i].body_a], i);
-        iv_push(&w->bjoint[w->j[i].body_b], i);
+        if (w->j[i].body_b != w->j[i].body_a) iv_push(&w->bjoint[w->j[i].body_b], i);   /* mouse: one body */
     }
     return 0;
 }

@@ -985,10 +985,76 @@ static int pulley_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
     return linear_error < OR_LINEAR_SLOP_J;
 }
 
+/* ------------------------------------------------------------ mouse
+ * joints/mouse.py:138-229: body B pulled towards a target by a soft
+ * constraint with a force limit; the record's body_a is body B (the
+ * reference's is None), so the island indices coincide and only B's slots
+ * are written.  The set-up damps B's angular velocity by 0.98
+ * (mouse.py:183). */
+static void mouse_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt,
+                       double dt_ratio, double body_mass, int warm) {
+    double mb = k->mb, ib = k->iB;
+    v2 cb = pc[k->ib];
+    v2 vb = vv[k->ib];
+    double wb = ww[k->ib];
+    rot qb = rot_of(pa[k->ib]);
+    double mass = body_mass;
+    double omega = 2.0 * OR_PI * J->frequency;
+    double d = 2.0 * mass * J->damping_ratio * omega;
+    double kk = mass * SQ(omega);
+    J->gamma = dt * (d + dt * kk);
+    if (J->gamma != 0.0) J->gamma = 1.0 / J->gamma;
+    J->bias = dt * kk * J->gamma;                 /* _beta */
+    v2 rb = k->rb = rmul(qb, vsub(j_lb(J), k->lcb));
+    double a = mb + ib * SQ(rb.y) + J->gamma;
+    double c = -ib * rb.x * rb.y;
+    double b = c;
+    double dd = mb + ib * SQ(rb.x) + J->gamma;
+    double det = a * dd - b * c;                  /* Mat22.inverse */
+    if (det != 0.0) det = 1.0 / det;
+    k->m.c1 = V3(det * dd, -det * c, 0.0);
+    k->m.c2 = V3(-det * b, det * a, 0.0);
+    k->u = vscale(J->bias, vsub(vadd(cb, rb), V(J->target_x, J->target_y)));   /* _c */
+    wb = wb * 0.98;
+    if (warm) {
+        J->impulse[0] = J->impulse[0] * dt_ratio;
+        J->impulse[1] = J->impulse[1] * dt_ratio;
+        v2 P = V(J->impulse[0], J->impulse[1]);
+        vb = vadd(vb, vscale(mb, P));
+        wb = wb + ib * vcross(rb, P);
+    } else {
+        J->impulse[0] = J->impulse[1] = 0.0;
+    }
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
+static void mouse_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww, double dt) {
+    v2 vb = vv[k->ib];
+    double wb = ww[k->ib];
+    v2 rb = k->rb;
+    v2 Cdot = vadd(vb, vcross_sv(wb, rb));
+    v2 acc = V(J->impulse[0], J->impulse[1]);
+    v2 e = vneg(vadd(vadd(Cdot, k->u), vscale(J->gamma, acc)));
+    v2 impulse = V(k->m.c1.x * e.x + k->m.c2.x * e.y, k->m.c1.y * e.x + k->m.c2.y * e.y);
+    v2 old_impulse = acc;
+    acc = vadd(acc, impulse);
+    double max_impulse = dt * J->max_force;
+    if (acc.x * acc.x + acc.y * acc.y > SQ(max_impulse)) {
+        double s = max_impulse / sqrt(acc.x * acc.x + acc.y * acc.y);
+        acc = V(acc.x * s, acc.y * s);
+    }
+    J->impulse[0] = acc.x; J->impulse[1] = acc.y;
+    impulse = vsub(acc, old_impulse);
+    vb = vadd(vb, vscale(k->mb, impulse));
+    wb = wb + k->iB * vcross(rb, impulse);
+    vv[k->ib] = vb; ww[k->ib] = wb;
+}
+
 /* ------------------------------------------------------------ dispatch */
 static void joint_init(gb_joint *J, or_jcons *k, const v2 *pc, const double *pa, v2 *vv, double *ww, double dt,
-                       double dt_ratio, int warm) {
+                       double dt_ratio, double body_b_mass, int warm) {
     switch (J->type) {
+    case GB_JOINT_MOUSE: mouse_init(J, k, pc, pa, vv, ww, dt, dt_ratio, body_b_mass, warm); break;
     case GB_JOINT_REVOLUTE: revolute_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
     case GB_JOINT_PRISMATIC: prismatic_init(J, k, pc, pa, vv, ww, dt_ratio, warm); break;
     case GB_JOINT_DISTANCE: distance_init(J, k, pc, pa, vv, ww, dt, dt_ratio, warm); break;
@@ -1008,6 +1074,7 @@ static void joint_solve_velocity(gb_joint *J, or_jcons *k, v2 *vv, double *ww, d
     case GB_JOINT_ROPE: rope_solve_velocity(J, k, vv, ww, 1.0 / dt); break;
     case GB_JOINT_WHEEL: wheel_solve_velocity(J, k, vv, ww, dt); break;
     case GB_JOINT_PULLEY: pulley_solve_velocity(J, k, vv, ww); break;
+    case GB_JOINT_MOUSE: mouse_solve_velocity(J, k, vv, ww, dt); break;
     default: weld_solve_velocity(J, k, vv, ww); break;
     }
 }
@@ -1020,6 +1087,7 @@ static int joint_solve_position(gb_joint *J, or_jcons *k, v2 *pc, double *pa) {
     case GB_JOINT_ROPE: return rope_solve_position(J, k, pc, pa);
     case GB_JOINT_WHEEL: return wheel_solve_position(J, k, pc, pa);
     case GB_JOINT_PULLEY: return pulley_solve_position(J, k, pc, pa);
+    case GB_JOINT_MOUSE: return 1;
     default: return weld_solve_position(J, k, pc, pa);
     }
 }

@@ -8,5 +8,5 @@ from .world import AABB, Body, Contact, ContactManager, EventContact, Fixture, V
 from . import joints  # noqa: E402,F401
 from . import controllers  # noqa: E402,F401
 from .controllers import BuoyancyController, Controller, GravityController  # noqa: E402,F401
-from .joints import (DistanceJoint, FrictionJoint, Joint, PrismaticJoint, PulleyJoint, RevoluteJoint,  # noqa: E402,F401
-                     RopeJoint, WeldJoint, WheelJoint)
+from .joints import (DistanceJoint, FrictionJoint, Joint, MouseJoint, PrismaticJoint, PulleyJoint,  # noqa: E402,F401
+                     RevoluteJoint, RopeJoint, WeldJoint, WheelJoint)

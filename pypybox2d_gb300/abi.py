@@ -87,7 +87,7 @@ CONTACT = np.dtype([
 ], align=True)
 
 JOINT_REVOLUTE, JOINT_PRISMATIC, JOINT_DISTANCE, JOINT_WELD = 1, 2, 3, 4
-JOINT_FRICTION, JOINT_ROPE, JOINT_WHEEL, JOINT_PULLEY = 5, 6, 7, 8
+JOINT_FRICTION, JOINT_ROPE, JOINT_WHEEL, JOINT_PULLEY, JOINT_MOUSE = 5, 6, 7, 8, 9
 J_COLLIDE_CONNECTED, J_LIMIT, J_MOTOR = 1, 2, 4
 LIMIT_INACTIVE, LIMIT_LOWER, LIMIT_UPPER, LIMIT_EQUAL = 0, 1, 2, 3
 
@@ -102,6 +102,7 @@ JOINT = np.dtype([
     ("max_force", "<f8"), ("max_torque", "<f8"), ("max_length", "<f8"), ("cur_length", "<f8"),
     ("spring_impulse", "<f8"), ("sax_x", "<f8"), ("sax_y", "<f8"), ("s_ax", "<f8"), ("s_bx", "<f8"),
     ("ga_x", "<f8"), ("ga_y", "<f8"), ("gb_x", "<f8"), ("gb_y", "<f8"), ("ratio", "<f8"), ("constant", "<f8"),
+    ("target_x", "<f8"), ("target_y", "<f8"),
 ], align=True)
 
 CONTROLLER_BUOYANCY, CONTROLLER_GRAVITY = 1, 2

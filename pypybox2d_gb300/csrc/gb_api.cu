@@ -311,10 +311,11 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
         const gb_joint &J = b->joints[i];
         const bool ok = J.world >= 0 && J.world < b->nw && (i == 0 || J.world >= b->joints[i - 1].world) &&
                         J.body_a >= 0 && J.body_a < b->hdr[J.world].nb && J.body_b >= 0 && J.body_b < b->hdr[J.world].nb &&
-                        J.body_a != J.body_b && J.type >= GB_JOINT_REVOLUTE && J.type <= GB_JOINT_PULLEY;
+                        (J.type == GB_JOINT_MOUSE ? J.body_a == J.body_b : J.body_a != J.body_b) &&
+                        J.type >= GB_JOINT_REVOLUTE && J.type <= GB_JOINT_MOUSE;
         if (!ok) {
             delete b;
-            return fail(J.type < GB_JOINT_REVOLUTE || J.type > GB_JOINT_PULLEY ? GB_E_UNSUPPORTED : GB_E_ARG,
+            return fail(J.type < GB_JOINT_REVOLUTE || J.type > GB_JOINT_MOUSE ? GB_E_UNSUPPORTED : GB_E_ARG,
                         "joint " + std::to_string(i) + ": world out of order, body outside its world or unknown type");
         }
         if (b->hdr[J.world].nj == 0) b->hdr[J.world].jbase = i;
@@ -407,7 +408,7 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
             for (int k = 0; k < h.nj; ++k) {
                 const gb_joint &J = b->joints[h.jbase + k];
                 off[J.body_a + 1] += 1;
-                off[J.body_b + 1] += 1;
+                if (J.body_b != J.body_a) off[J.body_b + 1] += 1;   // a mouse joint's one body lists it once
             }
             for (int k = 0; k < h.nb; ++k) off[k + 1] += off[k];
             std::vector<int> cur(off, off + h.nb);
@@ -415,7 +416,7 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
             for (int k = 0; k < h.nj; ++k) {
                 const gb_joint &J = b->joints[h.jbase + k];
                 adj[cur[J.body_a]++] = k;
-                adj[cur[J.body_b]++] = k;
+                if (J.body_b != J.body_a) adj[cur[J.body_b]++] = k;
             }
         }
         const bool f64 = precision == GB_PREC_F64;

@@ -2,8 +2,8 @@
 // contacts (island.py:107-113, 145-148): revolute (joints/revolute.py:240-453),
 // prismatic (joints/prismatic.py:238-513), distance (joints/distance.py:175-311),
 // weld (joints/weld.py:118-257), friction (joints/friction.py:107-233), rope
-// (joints/rope.py:106-248), wheel (joints/wheel.py:202-417) and pulley
-// (joints/pulley.py:156-320).
+// (joints/rope.py:106-248), wheel (joints/wheel.py:202-417), pulley
+// (joints/pulley.py:156-320) and mouse (joints/mouse.py:138-229).
 //
 // Joints are few next to contacts, so they are solved in float64 in both
 // precision units: the float32 unit widens the bodies' velocities for the
@@ -850,11 +850,68 @@ static __device__ bool pulley_position(const gb_joint &J, const JCons &k, vec2<d
     return linear_error < GB_LINEAR_SLOP_J;
 }
 
+// ------------------------------------------------------------ mouse
+// Body B pulled towards a target by a soft constraint with a force limit.
+// The record's body_a is body B (the reference's is None), so the caller's
+// A and B values are the same body's and only B's are changed; the set-up
+// damps B's angular velocity by 0.98 (mouse.py:183).
+static __device__ void mouse_init(gb_joint &J, JCons &k, vec2<double> cb, double ab, vec2<double> &vb, double &wb,
+                                  double dt, double dt_ratio, double body_mass, bool warm) {
+    const double mb = k.mb, ib = k.iB;
+    const rot2<double> qb = pose_rot(ab);
+    const double mass = body_mass;
+    const double omega = 2.0 * 3.141592653589793 * J.frequency;
+    const double d = 2.0 * mass * J.damping_ratio * omega;
+    const double kk = mass * sq(omega);
+    J.gamma = dt * (d + dt * kk);
+    if (J.gamma != 0.0) J.gamma = 1.0 / J.gamma;
+    J.bias = dt * kk * J.gamma;   // _beta
+    const vec2<double> rb = k.rb = rmul(qb, j_lb(J) - k.lcb);
+    const double a = mb + ib * sq(rb.y) + J.gamma;
+    const double c = -ib * rb.x * rb.y;
+    const double b = c;
+    const double dd = mb + ib * sq(rb.x) + J.gamma;
+    double det = a * dd - b * c;
+    if (det != 0.0) det = 1.0 / det;
+    k.m.c1 = mk3(det * dd, -det * c, 0.0);
+    k.m.c2 = mk3(-det * b, det * a, 0.0);
+    k.u = J.bias * (cb + rb - mk<double>(J.target_x, J.target_y));   // _c
+    wb = wb * 0.98;
+    if (warm) {
+        J.impulse[0] = J.impulse[0] * dt_ratio;
+        J.impulse[1] = J.impulse[1] * dt_ratio;
+        const vec2<double> P = mk<double>(J.impulse[0], J.impulse[1]);
+        vb = vb + mb * P;
+        wb = wb + ib * cross(rb, P);
+    } else {
+        J.impulse[0] = J.impulse[1] = 0.0;
+    }
+}
+
+static __device__ void mouse_velocity(gb_joint &J, const JCons &k, vec2<double> &vb, double &wb, double dt) {
+    const vec2<double> Cdot = vb + cross(wb, k.rb);
+    vec2<double> acc = mk<double>(J.impulse[0], J.impulse[1]);
+    const vec2<double> e = -(Cdot + k.u + J.gamma * acc);
+    vec2<double> impulse = mk<double>(k.m.c1.x * e.x + k.m.c2.x * e.y, k.m.c1.y * e.x + k.m.c2.y * e.y);
+    const vec2<double> old_impulse = acc;
+    acc = acc + impulse;
+    const double max_impulse = dt * J.max_force;
+    if (acc.x * acc.x + acc.y * acc.y > sq(max_impulse)) {
+        const double s = max_impulse / sqrt(acc.x * acc.x + acc.y * acc.y);
+        acc = mk<double>(acc.x * s, acc.y * s);
+    }
+    J.impulse[0] = acc.x; J.impulse[1] = acc.y;
+    impulse = acc - old_impulse;
+    vb = vb + k.mb * impulse;
+    wb = wb + k.iB * cross(k.rb, impulse);
+}
+
 // ------------------------------------------------------------ dispatch
 static __device__ void joint_init(gb_joint &J, JCons &k, vec2<double> ca, double aa, vec2<double> cb, double ab,
                                   vec2<double> &va, double &wa, vec2<double> &vb, double &wb, double dt, double dt_ratio,
-                                  bool warm) {
+                                  double body_b_mass, bool warm) {
     switch (J.type) {
+    case GB_JOINT_MOUSE: mouse_init(J, k, cb, ab, vb, wb, dt, dt_ratio, body_b_mass, warm); break;
     case GB_JOINT_REVOLUTE: revolute_init(J, k, aa, ab, va, wa, vb, wb, dt_ratio, warm); break;
     case GB_JOINT_PRISMATIC: prismatic_init(J, k, ca, aa, cb, ab, va, wa, vb, wb, dt_ratio, warm); break;
     case GB_JOINT_DISTANCE: distance_init(J, k, ca, aa, cb, ab, va, wa, vb, wb, dt, dt_ratio, warm); break;
@@ -875,6 +932,7 @@ static __device__ void joint_velocity(gb_joint &J, const JCons &k, vec2<double> 
     case GB_JOINT_ROPE: rope_velocity(J, k, va, wa, vb, wb, 1.0 / dt); break;
     case GB_JOINT_WHEEL: wheel_velocity(J, k, va, wa, vb, wb, dt); break;
     case GB_JOINT_PULLEY: pulley_velocity(J, k, va, wa, vb, wb); break;
+    case GB_JOINT_MOUSE: mouse_velocity(J, k, vb, wb, dt); break;
     default: weld_velocity(J, k, va, wa, vb, wb); break;
     }
 }
@@ -888,6 +946,7 @@ static __device__ bool joint_position(const gb_joint &J, const JCons &k, vec2<do
     case GB_JOINT_ROPE: return rope_position(J, k, ca, aa, cb, ab);
     case GB_JOINT_WHEEL: return wheel_position(J, k, ca, aa, cb, ab);
     case GB_JOINT_PULLEY: return pulley_position(J, k, ca, aa, cb, ab);
+    case GB_JOINT_MOUSE: return true;
     default: return weld_position(J, k, ca, aa, cb, ab);
     }
 }

@@ -1682,7 +1682,7 @@ template <class R, class G> __device__ void solve_group(const G &g, const WView<
                         q.ma = (double)w.B.b_inv_mass[ga]; q.mb = (double)w.B.b_inv_mass[gbb];
                         q.iA = (double)w.B.b_inv_I[ga]; q.iB = (double)w.B.b_inv_I[gbb];
                         joint_init(J, q, w.B.b_c[ga], w.B.b_a[ga], w.B.b_c[gbb], w.B.b_a[gbb], va, wa, vb, wb, dt, dt_ratio,
-                                   warm);
+                                   w.B.b_mass[gbb], warm);
                     } else {
                         joint_velocity(J, q, va, wa, vb, wb, dt);
                     }

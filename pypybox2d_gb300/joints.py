@@ -1,5 +1,5 @@
 """The joint classes of the reference (pypybox2d/joints/): revolute,
-prismatic, distance, weld, friction, rope, wheel and pulley, with their
+prismatic, distance, weld, friction, rope, wheel, pulley and mouse, with their
 constructors, properties, setters and reaction getters.
 
 A joint is a view of one ``abi.JOINT`` record of its world (definition and
@@ -74,7 +74,8 @@ class Joint:
 
     def _wake(self):
         for b in self.bodies:
-            b.awake = True
+            if b is not None:
+                b.awake = True
 
     def _flag(self, bit):
         return bool(int(self._rec()["flags"]) & bit)
@@ -718,6 +719,75 @@ class PulleyJoint(Joint):
         return float(self._rec()["ratio"])
 
 
+class MouseJoint(Joint):
+    """joints/mouse.py:30-229: a point of one body pulled towards a world
+    target by a soft constraint with a force limit.  The body is body_b;
+    body_a is None, as in the reference (its record repeats body_b)."""
+
+    _type = abi.JOINT_MOUSE
+
+    def __init__(self, body, target=(0, 0), max_force=0.0, frequency=5.0, damping_ratio=0.7):
+        if body is None:
+            raise ValueError("body must be set")
+        if not (_valid_float(target[0]) and _valid_float(target[1])):
+            raise ValueError("Invalid target")
+        if not _valid_float(max_force) or max_force < 0.0:
+            raise ValueError("Invalid maximum force")
+        if not _valid_float(frequency) or frequency < 0.0:
+            raise ValueError("Invalid frequency")
+        if not _valid_float(damping_ratio) or damping_ratio < 0.0:
+            raise ValueError("Invalid damping ratio")
+        Joint.__init__(self, None, body, False)
+        r = self._pending
+        r["target_x"], r["target_y"] = float(target[0]), float(target[1])
+        lb = body.get_local_point(target)
+        r["lb_x"], r["lb_y"] = float(lb[0]), float(lb[1])
+        r["max_force"], r["frequency"], r["damping_ratio"] = max_force, frequency, damping_ratio
+
+    def get_reaction_force(self, inv_dt):
+        r = self._rec()
+        return _V(inv_dt * float(r["impulse"][0]), inv_dt * float(r["impulse"][1]))
+
+    def get_reaction_torque(self, inv_dt):
+        return 0.0
+
+    @property
+    def target(self):
+        r = self._rec()
+        return _V(r["target_x"], r["target_y"])
+
+    @target.setter
+    def target(self, target):
+        if not self._body_b.awake:
+            self._body_b.awake = True
+        r = self._edit()
+        r["target_x"], r["target_y"] = float(target[0]), float(target[1])
+
+    @property
+    def max_force(self):
+        return float(self._rec()["max_force"])
+
+    @max_force.setter
+    def max_force(self, value):
+        self._edit()["max_force"] = value
+
+    @property
+    def frequency(self):
+        return float(self._rec()["frequency"])
+
+    @frequency.setter
+    def frequency(self, value):
+        self._edit()["frequency"] = value
+
+    @property
+    def damping_ratio(self):
+        return float(self._rec()["damping_ratio"])
+
+    @damping_ratio.setter
+    def damping_ratio(self, value):
+        self._edit()["damping_ratio"] = value
+
+
 KINDS = {abi.JOINT_REVOLUTE: RevoluteJoint, abi.JOINT_PRISMATIC: PrismaticJoint, abi.JOINT_DISTANCE: DistanceJoint,
          abi.JOINT_WELD: WeldJoint, abi.JOINT_FRICTION: FrictionJoint, abi.JOINT_ROPE: RopeJoint,
-         abi.JOINT_WHEEL: WheelJoint, abi.JOINT_PULLEY: PulleyJoint}
+         abi.JOINT_WHEEL: WheelJoint, abi.JOINT_PULLEY: PulleyJoint, abi.JOINT_MOUSE: MouseJoint}

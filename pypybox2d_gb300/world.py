@@ -1097,6 +1097,7 @@ class World:
         cm = self.contact_manager
         if cm.pre_solve is not None:
             raise NotImplementedError("pre_solve listeners cannot run inside the GPU step")
+        self._check_mouse_joints(dt)
         self._sync_controllers()
         self._sync_device()
         events = cm.wants_events
@@ -1142,12 +1143,16 @@ class World:
         if joint._world is not None:
             raise ValueError("the joint already belongs to a world")
         for b in joint.bodies:
+            if b is None and type(joint) is _joints.MouseJoint:
+                continue   # the mouse joint's body_a is None (mouse.py:67)
             if b is None or b._world is not self:
                 raise ValueError("Both bodies must be in the same world.")
         self._structural()
         r = joint._pending.copy()
         r["world"] = 0
-        r["body_a"], r["body_b"] = joint._body_a._index, joint._body_b._index
+        # a mouse joint's record repeats its one body (gb_joint, GB_JOINT_MOUSE)
+        r["body_a"] = (joint._body_a if joint._body_a is not None else joint._body_b)._index
+        r["body_b"] = joint._body_b._index
         self._J = np.concatenate([self._J, np.array([r], dtype=abi.JOINT)])
         joint._world, joint._index = self, len(self._joints)
         self._joints.append(joint)
@@ -1163,7 +1168,8 @@ class World:
             raise ValueError("Joint not in world")
         self._structural()
         for b in joint.bodies:
-            b.awake = True
+            if b is not None:
+                b.awake = True
         i = joint._index
         r = self._J[i].copy()
         self._J = np.delete(self._J, i)
@@ -1199,10 +1205,34 @@ class World:
     def create_pulley_joint(self, *args, **kwargs):
         return self.add_joint(_joints.PulleyJoint(*args, **kwargs))
 
-    def _unsupported(self, *args, **kwargs):
-        raise NotImplementedError("gear and mouse joints are not part of the GPU world step")
+    def create_mouse_joint(self, *args, **kwargs):
+        return self.add_joint(_joints.MouseJoint(*args, **kwargs))
 
-    create_gear_joint = create_mouse_joint = _unsupported
+    def _check_mouse_joints(self, dt):
+        """mouse.py:161: the set-up asserts d + dt * k > EPSILON (a zero
+        frequency fails it); the reference raises AssertionError from inside
+        the step, here before it, for a mouse joint whose awake dynamic body
+        the step solves."""
+        if dt <= 0.0 or not any(type(j) is _joints.MouseJoint for j in self._joints):
+            return
+        for j in self._joints:
+            if type(j) is not _joints.MouseJoint:
+                continue
+            b = j._body_b
+            r = self._body_record(b._index)
+            if r["type"] != Body.DYNAMIC or not (int(r["flags"]) & abi.BODY_AWAKE) or not (int(r["flags"]) & abi.BODY_ACTIVE):
+                continue
+            mass = float(r["mass"])
+            omega = 2.0 * math.pi * j.frequency
+            d = 2.0 * mass * j.damping_ratio * omega
+            k = mass * omega ** 2
+            if not d + dt * k > 2.220446049250313e-16:
+                raise AssertionError("mouse joint: d + dt * k <= EPSILON (mouse.py:161)")
+
+    def _unsupported(self, *args, **kwargs):
+        raise NotImplementedError("gear joints are not part of the GPU world step")
+
+    create_gear_joint = _unsupported
 
     # -- controllers (world.py:923-957)
     def create_gravity_controller(self, *args, **kwargs):
@@ -1887,6 +1917,7 @@ class WorldBatch:
             w._check_unlocked()
             if w.contact_manager.pre_solve is not None:
                 raise NotImplementedError("pre_solve listeners cannot run inside the GPU step")
+            w._check_mouse_joints(dt)
         self._push_edits()
         events = any(w.contact_manager.wants_events for w in self._worlds)
         for w in self._worlds:

@@ -1,4 +1,4 @@
-"""A scripted session of the friction, rope, wheel and pulley joints through
+"""A scripted session of the friction, rope, wheel, pulley and mouse joints through
 the World API, run on the reference by make_golden.py (api_joints2.npz) and
 on pypybox2d_gb300 by tests/test_world_joints.py.
 
@@ -18,9 +18,9 @@ GETTERS = 12   # floats per joint in a getter row
 
 def getter_row(j, inv_dt=60.0):
     """The getters of one joint, padded to GETTERS floats (the reference's
-    rope joint has no anchor properties: zeros there)."""
+    rope and mouse joints have no anchor properties: zeros there)."""
     name = type(j).__name__
-    anchors = [0.0] * 4 if name == "RopeJoint" else [*j.anchor_a, *j.anchor_b]
+    anchors = [0.0] * 4 if name in ("RopeJoint", "MouseJoint") else [*j.anchor_a, *j.anchor_b]
     row = [*anchors, *j.get_reaction_force(inv_dt), j.get_reaction_torque(inv_dt)]
     if name == "FrictionJoint":
         row += [j.max_force, j.max_torque]
@@ -30,6 +30,8 @@ def getter_row(j, inv_dt=60.0):
         row += [j.joint_translation, j.joint_speed, j.motor_torque(inv_dt), j.motor_speed, j.max_motor_torque]
     elif name == "PulleyJoint":
         row += [j.length_a, j.length_b, j.ratio]
+    elif name == "MouseJoint":
+        row += [*j.target, j.max_force, j.frequency, j.damping_ratio]
     return [float(x) for x in row] + [0.0] * (GETTERS - len(row))
 
 
@@ -59,6 +61,9 @@ def script(b2, snap, on_world=lambda world: None):
     right.create_polygon_fixture(box=(0.3, 0.3), density=2.0)
     world.create_pulley_joint(left, right, ground_anchor_a=(10, 9), ground_anchor_b=(13, 9), anchor_a=(10, 4.3),
                               anchor_b=(13, 3.3), ratio=1.0)
+    crate = world.create_dynamic_body(position=(18, 0.3))
+    crate.create_polygon_fixture(box=(0.4, 0.3), density=1.0, friction=0.6)
+    mouse = world.create_mouse_joint(crate, target=(18.2, 0.4), max_force=30.0, frequency=4.0, damping_ratio=0.7)
 
     def run(n):
         for _ in range(n):
@@ -73,9 +78,12 @@ def script(b2, snap, on_world=lambda world: None):
     fr.max_torque = 0.0
     wj.motor_enabled = True
     wj.motor_speed = -5.0
+    mouse.target = (20, 2.5)
     run(30)
     snap("s60", world)
     wj.max_motor_torque = 2.0
+    mouse.max_force = 5.0
+    mouse.frequency = 2.0
     world.destroy_joint(rope)
     run(30)
     snap("s90", world)

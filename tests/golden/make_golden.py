@@ -244,18 +244,21 @@ def export_joints(world, b2):
     kinds = ((jm.RevoluteJoint, abi.JOINT_REVOLUTE), (jm.PrismaticJoint, abi.JOINT_PRISMATIC),
              (jm.DistanceJoint, abi.JOINT_DISTANCE), (jm.WeldJoint, abi.JOINT_WELD),
              (jm.FrictionJoint, abi.JOINT_FRICTION), (jm.RopeJoint, abi.JOINT_ROPE), (jm.WheelJoint, abi.JOINT_WHEEL),
-             (jm.PulleyJoint, abi.JOINT_PULLEY))
+             (jm.PulleyJoint, abi.JOINT_PULLEY), (jm.MouseJoint, abi.JOINT_MOUSE))
     for i, j in enumerate(world.joints):
         r = J[i]
         r["type"] = next(t for cls, t in kinds if type(j) is cls)
-        r["body_a"], r["body_b"] = bidx[id(j._body_a)], bidx[id(j._body_b)]
+        # a mouse joint has no body_a (mouse.py:67): its record repeats body_b
+        r["body_a"] = bidx[id(j._body_a if j._body_a is not None else j._body_b)]
+        r["body_b"] = bidx[id(j._body_b)]
         fl = abi.J_COLLIDE_CONNECTED if j._collide_connected else 0
         if getattr(j, "_limit_enabled", False):
             fl |= abi.J_LIMIT
         if getattr(j, "_motor_enabled", False):
             fl |= abi.J_MOTOR
         r["flags"] = fl
-        r["la_x"], r["la_y"] = j._local_anchor_a.x, j._local_anchor_a.y
+        if r["type"] != abi.JOINT_MOUSE:   # mouse.py keeps a local anchor on body_b only
+            r["la_x"], r["la_y"] = j._local_anchor_a.x, j._local_anchor_a.y
         r["lb_x"], r["lb_y"] = j._local_anchor_b.x, j._local_anchor_b.y
         if r["type"] == abi.JOINT_FRICTION:
             r["max_force"], r["max_torque"] = j._max_force, j._max_torque
@@ -276,6 +279,13 @@ def export_joints(world, b2):
             r["sax_x"], r["sax_y"], r["s_ax"], r["s_bx"] = j._ax.x, j._ax.y, j._s_ax, j._s_bx
             r["perp_x"], r["perp_y"] = j._ay.x, j._ay.y
             r["bias"], r["gamma"] = j._bias, j._gamma
+            continue
+        if r["type"] == abi.JOINT_MOUSE:
+            r["lb_x"], r["lb_y"] = j._local_anchor_b.x, j._local_anchor_b.y
+            r["target_x"], r["target_y"] = j._target.x, j._target.y
+            r["max_force"], r["frequency"], r["damping_ratio"] = j._max_force, j._frequency, j._damping_ratio
+            r["impulse"][:2] = (j._impulse.x, j._impulse.y)
+            r["gamma"], r["bias"] = j._gamma, j._beta
             continue
         if r["type"] == abi.JOINT_PULLEY:
             r["ga_x"], r["ga_y"] = j._ground_anchor_a.x, j._ground_anchor_a.y
@@ -609,12 +619,12 @@ def scene_bridge(b2, planks=30, seed=19):
 
 
 def scene_joints2(b2, seed=37):
-    """The friction, rope, wheel and pulley joints: a box sliding on the
-    ground held back by a friction joint, a ball on a slack rope that pulls
-    taut, a two-wheeled cart on sprung wheel joints with a motor on the rear
-    wheel, a wheel without a spring (frequency 0, whose spring axis keeps
-    its initial zero), and two boxes on a pulley with ratio 1.5, plus a few
-    boxes dropped among them."""
+    """The friction, rope, wheel, pulley and mouse joints: a box sliding on
+    the ground held back by a friction joint, a ball on a slack rope that
+    pulls taut, a two-wheeled cart on sprung wheel joints with a motor on the
+    rear wheel, a wheel without a spring (frequency 0, whose spring axis
+    keeps its initial zero), two boxes on a pulley with ratio 1.5 and a box
+    dragged by a mouse joint, plus a few boxes dropped among them."""
     rng = random.Random(seed)
     world = b2.World(gravity=(0, -10), do_sleep=True)
     ground = world.create_static_body(position=(0, -0.5), shapes=b2.Polygon(box=(40, 0.5)))
@@ -653,6 +663,10 @@ def scene_joints2(b2, seed=37):
     pb.create_polygon_fixture(box=(0.5, 0.5), density=1.0)
     world.create_pulley_joint(pa, pb, ground_anchor_a=(14, 12), ground_anchor_b=(18, 12), anchor_a=(14, 6.4),
                               anchor_b=(18, 5.5), ratio=1.5)
+    # mouse: a box dragged towards a point above the ground
+    dragged = world.create_dynamic_body(position=(24, 0.5), angle=0.3)
+    dragged.create_polygon_fixture(box=(0.5, 0.3), density=1.0, friction=0.5)
+    world.create_mouse_joint(dragged, target=(24.3, 0.6), max_force=40.0, frequency=3.0, damping_ratio=0.6)
     for i in range(6):
         b = world.create_dynamic_body(position=(-14 + 5.5 * i + rng.uniform(-0.5, 0.5), 7 + rng.uniform(0, 3)),
                                       angle=rng.uniform(-1, 1))
