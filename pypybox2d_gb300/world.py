@@ -1258,7 +1258,7 @@ class World:
     def _controller_state(self):
         """(records, body lists, structure key) of World.controllers"""
         C, cb = controller_records(self, self.controllers)
-        key = (C[["type", "body_start", "body_count"]].tobytes(), cb.tobytes())
+        key = (tuple(int(x) for x in C["type"]), tuple(int(x) for x in C["body_count"]), tuple(int(x) for x in cb))
         return C, cb, key
 
     def _sync_controllers(self):

@@ -119,3 +119,37 @@ def test_listeners_run_with_the_world_locked():
     with pytest.raises(b2.LockedError):
         w._replay(ev)
     assert seen == [True] and not w.locked and w.body_count == 1 + 6
+
+
+@pytest.mark.gpu
+def test_world_batch_with_joints_loops_and_controllers():
+    """Worlds with joints of every kind, loop shapes and controllers in one
+    batch follow the lone worlds bit for bit (the batch's joint ranges,
+    controller records and their body lists are offset per world), also
+    after a controller parameter edit (gb_batch_set_controllers); a new
+    controller body list inside the batch is refused."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+    scenes = (make_golden.scene_joints2, make_golden.scene_buoyancy, make_golden.scene_loops, make_golden.scene_gravity)
+    A = [s(b2) for s in scenes]
+    S = [s(b2) for s in scenes]
+    batch = b2.WorldBatch(A)
+    for k in range(3):
+        batch.step(1 / 60, 8, 3, n_steps=10)
+        for w in S:
+            for _ in range(10):
+                w.step(1 / 60, 8, 3)
+        for i in range(len(A)):
+            _same_worlds(A[i], S[i], f"round {k} world {i}")
+        if k == 0:
+            for w in (A[1], S[1]):
+                w.controllers[0].density = 3.0
+                w.controllers[1].velocity = (-1.0, 0.0)
+            for w in (A[3], S[3]):
+                w.controllers[0].G = 2.0
+    with pytest.raises(NotImplementedError):
+        A[3].controllers[1].add_body(A[3].bodies[1])
+        batch.step(1 / 60, 8, 3)
+    batch.close()
