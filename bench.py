@@ -27,8 +27,11 @@ Reported (one JSON line on rank 0):
   value    dynamic body-steps/s with the batch resident in HBM (device time,
            CUDA events on the launching stream, max over ranks)
   e2e      the same metric through the C ABI with host buffers: every step
-           uploads the body records from pinned host memory
-           (gb_batch_set_bodies), steps, and reads them back (gb_batch_get_bodies)
+           uploads the body records from pinned host memory, steps, and reads
+           them back, in one gb_batch_step_host call (chunks of worlds whose
+           copies overlap the other chunks' kernels); ``three_calls_value``
+           is the same round trip as gb_batch_set_bodies, gb_batch_step and
+           gb_batch_get_bodies one after the other
   roofline HBM roofline of the whole step from the algorithmic bytes per
            world-step (152 B per body + shape bytes + 32 B per fixture + 128 B
            per contact, from live counts) over the event-timed step; the
@@ -579,21 +582,33 @@ def main():
     lib = batch.lib
     host[:] = batch.bodies(stream=sh)
     ptr = pinned.data_ptr()
-    e2 = torch.cuda.Event(enable_timing=True)
-    e3 = torch.cuda.Event(enable_timing=True)
     opts = abi.StepOpts(DT, VI, PI, 1, mode, threads, 0)
-    barrier()
-    torch.cuda.synchronize()
-    e2.record(stream)
-    for _ in range(e2e_steps):
+
+    def e2e_leg(one_step):
+        e2 = torch.cuda.Event(enable_timing=True)
+        e3 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        e2.record(stream)
+        for _ in range(e2e_steps):
+            one_step()
+        e3.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return total_dyn * e2e_steps / (e2.elapsed_time(e3) / 1e3)
+
+    def chunked():      # gb_batch_step_host: chunks of worlds upload, step and download on streams of their own
+        abi.check(lib.gb_batch_step_host(batch.h, ptr, ptr, n_b, ctypes.byref(opts), ctypes.c_void_p(sh)))
+
+    def three_calls():  # the same round trip as three calls on one stream
         abi.check(lib.gb_batch_set_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh)))
         abi.check(lib.gb_batch_step(batch.h, ctypes.byref(opts), ctypes.c_void_p(sh)))
         abi.check(lib.gb_batch_get_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh)))
-    e3.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    te = e2.elapsed_time(e3) / 1e3
-    e2e_value = total_dyn * e2e_steps / te
+
+    e2e_value = e2e_leg(chunked)
+    restore()
+    host[:] = batch.bodies(stream=sh)
+    e2e_three = e2e_leg(three_calls)
 
     out = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": steps,
@@ -619,7 +634,9 @@ def main():
         "kernels": kernels,
         "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY.itemsize,
                 "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": e2e_steps,
-                "window": "the first steps of the timed window, restored from its snapshot"},
+                "window": "the first steps of the timed window, restored from its snapshot",
+                "entry": "gb_batch_step_host (pinned host buffer in and out, chunks of worlds on streams of their own)",
+                "three_calls_value": e2e_three},
         "gpu_launches": launches_per_step(W, cfg["big_bodies"], cfg["groups"]) * steps if eff_mode == 3 else 1,
         "autotune": tune,
         "graph": graph_info,

@@ -347,6 +347,20 @@ int gb_batch_step(gb_batch *batch, const gb_step_opts *opts, void *cuda_stream);
 int gb_batch_set_bodies(gb_batch *batch, const gb_body *bodies, int32_t n_bodies, void *cuda_stream);
 /* Copy the device body state of the whole batch to host memory. */
 int gb_batch_get_bodies(gb_batch *batch, gb_body *bodies, int32_t n_bodies, void *cuda_stream);
+/* One host-buffer round trip of World.step (world.py:307-354) with the
+ * body state read and written through host memory: the same results as
+ * gb_batch_set_bodies(bodies_in), gb_batch_step(opts) and
+ * gb_batch_get_bodies(bodies_out) in a row, bit for bit.  Under the phased
+ * launch the worlds go in chunks (the batch's world groups, or four runs of
+ * about equal body counts when the launch configuration has one group), each
+ * chunk's upload, steps and download on a stream of its own, so the copies
+ * of one chunk overlap the kernels of the others.  bodies_in and bodies_out
+ * may be the same buffer; pinned host memory lets the copies run
+ * asynchronously.  The call returns once bodies_out is written.  Other
+ * mappings, contact events and launch timing take the three calls in a
+ * row. */
+int gb_batch_step_host(gb_batch *batch, const gb_body *bodies_in, gb_body *bodies_out, int32_t n_bodies,
+                       const gb_step_opts *opts, void *cuda_stream);
 /* Copy the fat AABBs (4 doubles per fixture) to host memory. */
 int gb_batch_get_proxies(gb_batch *batch, double *aabbs, int32_t n_fixtures, void *cuda_stream);
 /* Number of live contacts of every world (n_worlds ints). */

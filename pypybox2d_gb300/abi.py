@@ -222,7 +222,7 @@ LIB_PATH = os.path.join(_PKG_DIR, "_build", "libgb2d.so")
 EXPORTED = (
     "gb_version", "gb_last_error", "gb_struct_sizes",
     "gb_batch_create", "gb_batch_destroy", "gb_batch_step",
-    "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_get_proxies",
+    "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_step_host", "gb_batch_get_proxies",
     "gb_batch_get_contact_counts", "gb_batch_get_contacts", "gb_batch_get_solver_order",
     "gb_batch_status", "gb_batch_counters", "gb_batch_phase_clocks",
     "gb_batch_step_static_scratch", "gb_batch_kernel_times", "gb_batch_get_events",
@@ -283,6 +283,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_step.argtypes = [vp, ctypes.POINTER(StepOpts), vp]
     lib.gb_batch_set_bodies.argtypes = [vp, vp, i32, vp]
     lib.gb_batch_get_bodies.argtypes = [vp, vp, i32, vp]
+    lib.gb_batch_step_host.argtypes = [vp, vp, vp, i32, ctypes.POINTER(StepOpts), vp]
     lib.gb_batch_get_proxies.argtypes = [vp, vp, i32, vp]
     lib.gb_batch_get_contact_counts.argtypes = [vp, i32p, vp]
     lib.gb_batch_get_contacts.argtypes = [vp, i32, vp, i32, i32p, vp]

@@ -180,6 +180,8 @@ struct gb_batch {
     bool has_side = false;
     gb_launch_config cfg{3, 128, GB_SOLVE_PIPE_BUFS, GB_SOLVE_BIG_BODIES, 1, 0, 0.0};   // launch_mode 0 steps
     std::vector<WorldGroup> groups;  // world groups of cfg.groups > 1
+    std::vector<WorldGroup> chunks;  // gb_batch_step_host's chunks while cfg.groups is 1
+    int chunks_big = -1;             // the wide-launch threshold the chunks were made with
     cudaEvent_t fork = nullptr;      // the caller's stream -> the groups' streams
     std::vector<gb_graph *> graphs;  // captured rollouts, disarmed when the batch is destroyed
     char *d_query = nullptr;         // staging of query inputs and outputs, grown on demand
@@ -189,6 +191,7 @@ struct gb_batch {
 namespace {
 template <class R> int run_steps(gb_batch *b, const Batch<R> &B, const StepParams &sp, int n_steps, int mode, int threads,
                                  cudaStream_t st, KernelTimer *kt);
+void free_groups(std::vector<WorldGroup> &groups);
 }
 
 // A captured rollout (gb_graph_capture).  `b` is null once its batch is gone.
@@ -442,10 +445,10 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
     CK(cudaMalloc((void **)&d_fst, sizeof(gb_fixture) * std::max(1, b->nf)));
     if (b->nf > 0) CK(cudaMemcpy(d_fst, scene->fixtures, sizeof(gb_fixture) * b->nf, cudaMemcpyHostToDevice));
     if (precision == GB_PREC_F64) {
-        gb_launch_unpack_bodies<double>(b->bd, b->d_bstage, b->nb, 0);
+        gb_launch_unpack_bodies<double>(b->bd, b->d_bstage, 0, b->nb, 0);
         gb_launch_unpack_fixtures<double>(b->bd, d_fst, b->nf, 0);
     } else {
-        gb_launch_unpack_bodies<float>(b->bf, b->d_bstage, b->nb, 0);
+        gb_launch_unpack_bodies<float>(b->bf, b->d_bstage, 0, b->nb, 0);
         gb_launch_unpack_fixtures<float>(b->bf, d_fst, b->nf, 0);
     }
     {
@@ -478,10 +481,10 @@ int gb_batch_create(const gb_scene *scene, int32_t precision, gb_batch **out) {
             CK(cudaMemcpy(d_s, slots.data(), sizeof(int) * slots.size(), cudaMemcpyHostToDevice));
             if (precision == GB_PREC_F64) {
                 gb_launch_unpack_contacts<double>(b->bd, d_c, d_s, (int)hc.size(), 0);
-                gb_launch_refresh_toi_cand<double>(b->bd, 0);
+                gb_launch_refresh_toi_cand<double>(b->bd, 0, b->bd.n_slots, 0);
             } else {
                 gb_launch_unpack_contacts<float>(b->bf, d_c, d_s, (int)hc.size(), 0);
-                gb_launch_refresh_toi_cand<float>(b->bf, 0);
+                gb_launch_refresh_toi_cand<float>(b->bf, 0, b->bf.n_slots, 0);
             }
             CK(cudaDeviceSynchronize());
             cudaFree(d_c);
@@ -524,11 +527,8 @@ int gb_batch_destroy(gb_batch *b) {
     cudaFree(b->d_ev);
     cudaFree(b->d_ev_n);
     cudaFree(b->d_query);
-    for (WorldGroup &g : b->groups) {
-        cudaFree(g.d_worlds);
-        if (g.done) cudaEventDestroy(g.done);
-        if (g.st) cudaStreamDestroy(g.st);
-    }
+    free_groups(b->groups);
+    free_groups(b->chunks);
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->has_side) {
         cudaEventDestroy(b->side.fork);
@@ -585,11 +585,11 @@ int gb_batch_set_bodies(gb_batch *b, const gb_body *bodies, int32_t n, void *str
     CK(cudaMemcpyAsync(b->d_bstage, bodies, sizeof(gb_body) * n, cudaMemcpyHostToDevice, st));
     // body types and bullet flags decide which contacts can take part in the TOI loop
     if (b->prec == GB_PREC_F64) {
-        gb_launch_unpack_bodies<double>(b->bd, b->d_bstage, n, st);
-        gb_launch_refresh_toi_cand<double>(b->bd, st);
+        gb_launch_unpack_bodies<double>(b->bd, b->d_bstage, 0, n, st);
+        gb_launch_refresh_toi_cand<double>(b->bd, 0, b->bd.n_slots, st);
     } else {
-        gb_launch_unpack_bodies<float>(b->bf, b->d_bstage, n, st);
-        gb_launch_refresh_toi_cand<float>(b->bf, st);
+        gb_launch_unpack_bodies<float>(b->bf, b->d_bstage, 0, n, st);
+        gb_launch_refresh_toi_cand<float>(b->bf, 0, b->bf.n_slots, st);
     }
     CK(cudaGetLastError());
     return 0;
@@ -599,8 +599,8 @@ int gb_batch_get_bodies(gb_batch *b, gb_body *bodies, int32_t n, void *stream) {
     if (!b || !bodies) return fail(GB_E_ARG, "batch or bodies is NULL");
     if (n != b->nb) return fail(GB_E_ARG, "body count mismatch");
     cudaStream_t st = (cudaStream_t)stream;
-    if (b->prec == GB_PREC_F64) gb_launch_pack_bodies<double>(b->bd, b->d_bstage, n, st);
-    else gb_launch_pack_bodies<float>(b->bf, b->d_bstage, n, st);
+    if (b->prec == GB_PREC_F64) gb_launch_pack_bodies<double>(b->bd, b->d_bstage, 0, n, st);
+    else gb_launch_pack_bodies<float>(b->bf, b->d_bstage, 0, n, st);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(bodies, b->d_bstage, sizeof(gb_body) * n, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -840,6 +840,18 @@ StepParams params_of(const gb_step_opts *o) {
     return sp;
 }
 
+// The batch as group k's launch sequence sees it: its bodies and contact
+// slots, its first-pass TOI list counter, its wide-launch worlds.
+template <class R> Batch<R> group_view(const Batch<R> &B, const WorldGroup &g, int k) {
+    Batch<R> G = B;
+    G.n_bodies = g.nb; G.body0 = g.b0;
+    G.n_slots = g.ns; G.slot0 = g.s0;
+    G.toi_n = B.toi_n + k;
+    G.n_big = g.nbig;
+    G.n_huge = 0;
+    return G;
+}
+
 // n_steps steps of every world on `st`: one launch sequence over the whole
 // batch, or (phased launch, world groups) one per group, each on the group's
 // stream, forked from and joined back into `st` (also under stream capture).
@@ -854,13 +866,8 @@ template <class R> int run_steps(gb_batch *b, const Batch<R> &B, const StepParam
         const WorldGroup &g = b->groups[k];
         e = cudaStreamWaitEvent(g.st, b->fork, 0);
         if (e != cudaSuccess) break;
-        Batch<R> G = B;
-        G.n_bodies = g.nb; G.body0 = g.b0;
-        G.n_slots = g.ns; G.slot0 = g.s0;
-        G.toi_n = B.toi_n + k;
-        G.n_big = g.nbig;
-        G.n_huge = 0;
-        const int rc = gb_launch_step<R>(G, sp, n_steps, g.d_worlds, g.n_list, mode, threads, g.st, nullptr, nullptr);
+        const int rc = gb_launch_step<R>(group_view(B, g, (int)k), sp, n_steps, g.d_worlds, g.n_list, mode, threads, g.st,
+                                         nullptr, nullptr);
         if (rc) return rc;
         e = cudaEventRecord(g.done, g.st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(st, g.done, 0);
@@ -873,14 +880,18 @@ int launch_steps(gb_batch *b, const StepParams &sp, int n_steps, int mode, int t
                                   : run_steps<float>(b, b->bf, sp, n_steps, mode, threads, st, nullptr);
 }
 
-// Split the worlds into n runs of about equal body counts (n = 1: none).
-int make_groups(gb_batch *b, int n, int big_from) {
-    for (WorldGroup &g : b->groups) {
+void free_groups(std::vector<WorldGroup> &groups) {
+    for (WorldGroup &g : groups) {
         cudaFree(g.d_worlds);
         if (g.done) cudaEventDestroy(g.done);
         if (g.st) cudaStreamDestroy(g.st);
     }
-    b->groups.clear();
+    groups.clear();
+}
+
+// Split the worlds into n runs of about equal body counts (n = 1: none).
+int build_groups(gb_batch *b, int n, int big_from, std::vector<WorldGroup> &groups) {
+    free_groups(groups);
     n = std::min(n, b->nw);
     if (n < 2) return 0;
     if (!b->fork) CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
@@ -908,10 +919,12 @@ int make_groups(gb_batch *b, int n, int big_from) {
         CK(cudaMemcpy(g.d_worlds, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
         CK(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
-        b->groups.push_back(g);
+        groups.push_back(g);
     }
     return 0;
 }
+
+int make_groups(gb_batch *b, int n, int big_from) { return build_groups(b, n, big_from, b->groups); }
 
 bool has_grid_worlds(const gb_batch *b) { return (b->prec == GB_PREC_F64 ? b->bd.n_huge : b->bf.n_huge) > 0; }
 
@@ -1378,6 +1391,77 @@ extern "C" int gb_batch_step_static_scratch(gb_batch *b, const gb_step_opts *o, 
     int rc = b->prec == GB_PREC_F64 ? step_static<double>(b, b->bd, sp, o->n_steps, mode, threads, st)
                                     : step_static<float>(b, b->bf, sp, o->n_steps, mode, threads, st);
     if (rc) return rc;
+    b->counters[0] += 1;
+    b->counters[2] += o->n_steps;
+    return 0;
+}
+
+// Chunks of gb_batch_step_host when the launch configuration has one world
+// group: enough that the first chunk's upload and the last one's download
+// are short, few enough that each chunk's launches still fill the GPU.
+static constexpr int kHostChunks = 4;
+
+namespace {
+// Each chunk on its own stream: upload of its bodies, the refresh of its
+// contacts' TOI candidate flags, its steps, download.  Chunk k's copies
+// overlap the other chunks' kernels (the copy engines run beside the SMs).
+template <class R> int step_host_chunks(gb_batch *b, const Batch<R> &B, const std::vector<WorldGroup> &chunks,
+                                        const gb_body *in, gb_body *out, const StepParams &sp, int n_steps, int mode,
+                                        int threads, cudaStream_t st) {
+    cudaError_t e = cudaEventRecord(b->fork, st);
+    for (size_t k = 0; k < chunks.size() && e == cudaSuccess; ++k) {
+        const WorldGroup &g = chunks[k];
+        e = cudaStreamWaitEvent(g.st, b->fork, 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(b->d_bstage + g.b0, in + g.b0, sizeof(gb_body) * g.nb, cudaMemcpyHostToDevice, g.st);
+        if (e != cudaSuccess) break;
+        gb_launch_unpack_bodies<R>(B, b->d_bstage, g.b0, g.nb, g.st);
+        gb_launch_refresh_toi_cand<R>(B, g.s0, g.ns, g.st);
+        const int rc = gb_launch_step<R>(group_view(B, g, (int)k), sp, n_steps, g.d_worlds, g.n_list, mode, threads, g.st,
+                                         nullptr, nullptr);
+        if (rc) return rc;
+        gb_launch_pack_bodies<R>(B, b->d_bstage, g.b0, g.nb, g.st);
+        e = cudaMemcpyAsync(out + g.b0, b->d_bstage + g.b0, sizeof(gb_body) * g.nb, cudaMemcpyDeviceToHost, g.st);
+        if (e == cudaSuccess) e = cudaEventRecord(g.done, g.st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, g.done, 0);
+    }
+    return (int)e;
+}
+}  // namespace
+
+extern "C" int gb_batch_step_host(gb_batch *b, const gb_body *in, gb_body *out, int32_t n, const gb_step_opts *o,
+                                  void *stream) {
+    if (!b || !o || !in || !out) return fail(GB_E_ARG, "batch, bodies or opts is NULL");
+    if (n != b->nb) return fail(GB_E_ARG, "body count mismatch");
+    if (o->n_steps < 0 || o->vel_iters < 0 || o->pos_iters < 0) return fail(GB_E_ARG, "negative step count or iterations");
+    int mode = 0, threads = 0;
+    resolve_mapping(b, o, &mode, &threads);
+    if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
+    const std::vector<WorldGroup> *chunks = &b->groups;
+    if (mode == 3 && !has_grid_worlds(b) && !(o->record_order & (GB_OPT_EVENTS | GB_OPT_KERNEL_TIMES)) &&
+        b->groups.size() < 2) {
+        const int big_from = std::min(b->cfg.big_bodies, (int)GB_HUGE_BODIES);
+        if (b->chunks_big != big_from) {
+            const int rc = build_groups(b, kHostChunks, big_from, b->chunks);
+            if (rc) return rc;
+            b->chunks_big = big_from;
+        }
+        chunks = &b->chunks;
+    }
+    // other mappings, contact events, launch timing, batches of one world:
+    // the three calls one after the other
+    if (mode != 3 || has_grid_worlds(b) || (o->record_order & (GB_OPT_EVENTS | GB_OPT_KERNEL_TIMES)) || chunks->size() < 2) {
+        int rc = gb_batch_set_bodies(b, in, n, stream);
+        if (!rc) rc = gb_batch_step(b, o, stream);
+        if (!rc) rc = gb_batch_get_bodies(b, out, n, stream);
+        return rc;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const StepParams sp = params_of(o);
+    const int rc = b->prec == GB_PREC_F64 ? step_host_chunks<double>(b, b->bd, *chunks, in, out, sp, o->n_steps, mode, threads, st)
+                                          : step_host_chunks<float>(b, b->bf, *chunks, in, out, sp, o->n_steps, mode, threads, st);
+    if (rc) return cuda_fail((cudaError_t)rc, "chunked host step");
+    CK(cudaStreamSynchronize(st));
     b->counters[0] += 1;
     b->counters[2] += o->n_steps;
     return 0;

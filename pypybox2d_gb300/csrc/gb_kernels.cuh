@@ -23,9 +23,10 @@
 #if GB_IN_PART(0)
 namespace {
 
-__global__ void k_unpack_bodies(Batch<GB_REAL> B, const gb_body *src, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__global__ void k_unpack_bodies(Batch<GB_REAL> B, const gb_body *src, int b0, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = b0 + k;
     const gb_body &s = src[i];
     B.b_type[i] = s.type; B.b_flags[i] = s.flags; B.b_fstart[i] = s.fixture_start; B.b_fcount[i] = s.fixture_count;
     B.b_xp[i] = mk<double>(s.px, s.py);
@@ -40,9 +41,10 @@ __global__ void k_unpack_bodies(Batch<GB_REAL> B, const gb_body *src, int n) {
     B.b_mass[i] = s.mass; B.b_I[i] = s.I; B.b_sleep[i] = s.sleep_time;
 }
 
-__global__ void k_pack_bodies(Batch<GB_REAL> B, gb_body *dst, int n) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__global__ void k_pack_bodies(Batch<GB_REAL> B, gb_body *dst, int b0, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = b0 + k;
     gb_body s;
     s.type = B.b_type[i]; s.flags = B.b_flags[i]; s.fixture_start = B.b_fstart[i]; s.fixture_count = B.b_fcount[i];
     s.px = B.b_xp[i].x; s.py = B.b_xp[i].y; s.qc = B.b_xq[i].c; s.qs = B.b_xq[i].s;
@@ -106,9 +108,10 @@ __global__ void k_pack_contacts(Batch<GB_REAL> B, gb_contact *dst, int base, int
     dst[i] = g;
 }
 
-__global__ void k_refresh_toi_cand(Batch<GB_REAL> B, int n_slots) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n_slots) return;
+__global__ void k_refresh_toi_cand(Batch<GB_REAL> B, int s0, int n_slots) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_slots) return;
+    const int s = s0 + k;
     WView<GB_REAL> w = view_global(B, B.c_world[s]);
     int i = s - w.cb;
     if (i >= w.H->nc) return;
@@ -345,11 +348,11 @@ template <> int gb_launch_step<GB_REAL>(const Batch<GB_REAL> &B, const StepParam
     return (int)cudaGetLastError();
 }
 
-template <> void gb_launch_unpack_bodies<GB_REAL>(const Batch<GB_REAL> &B, const gb_body *d, int n, cudaStream_t st) {
-    if (n > 0) k_unpack_bodies<<<(n + 255) / 256, 256, 0, st>>>(B, d, n);
+template <> void gb_launch_unpack_bodies<GB_REAL>(const Batch<GB_REAL> &B, const gb_body *d, int b0, int n, cudaStream_t st) {
+    if (n > 0) k_unpack_bodies<<<(n + 255) / 256, 256, 0, st>>>(B, d, b0, n);
 }
-template <> void gb_launch_pack_bodies<GB_REAL>(const Batch<GB_REAL> &B, gb_body *d, int n, cudaStream_t st) {
-    if (n > 0) k_pack_bodies<<<(n + 255) / 256, 256, 0, st>>>(B, d, n);
+template <> void gb_launch_pack_bodies<GB_REAL>(const Batch<GB_REAL> &B, gb_body *d, int b0, int n, cudaStream_t st) {
+    if (n > 0) k_pack_bodies<<<(n + 255) / 256, 256, 0, st>>>(B, d, b0, n);
 }
 template <> void gb_launch_unpack_fixtures<GB_REAL>(const Batch<GB_REAL> &B, const gb_fixture *d, int n, cudaStream_t st) {
     if (n > 0) k_unpack_fixtures<<<(n + 255) / 256, 256, 0, st>>>(B, d, n);
@@ -360,9 +363,8 @@ template <> void gb_launch_unpack_contacts<GB_REAL>(const Batch<GB_REAL> &B, con
 template <> void gb_launch_pack_contacts<GB_REAL>(const Batch<GB_REAL> &B, gb_contact *d, int base, int n, cudaStream_t st) {
     if (n > 0) k_pack_contacts<<<(n + 255) / 256, 256, 0, st>>>(B, d, base, n);
 }
-template <> void gb_launch_refresh_toi_cand<GB_REAL>(const Batch<GB_REAL> &B, cudaStream_t st) {
-    const int n = B.n_slots;
-    if (n > 0) k_refresh_toi_cand<<<(n + 255) / 256, 256, 0, st>>>(B, n);
+template <> void gb_launch_refresh_toi_cand<GB_REAL>(const Batch<GB_REAL> &B, int s0, int n, cudaStream_t st) {
+    if (n > 0) k_refresh_toi_cand<<<(n + 255) / 256, 256, 0, st>>>(B, s0, n);
 }
 static_assert(GB_CFG_MAX_PIPE_BUFS <= GB_MAX_PIPE_BUFS, "launch configurations may ask for more chunk buffers than the solver has barriers");
 template <> size_t gb_solve_smem<GB_REAL>(int cache_bodies, int threads, int nbuf) {

@@ -133,6 +133,24 @@ class GpuBatch:
         b = np.ascontiguousarray(bodies, dtype=abi.BODY)
         abi.check(self.lib.gb_batch_set_bodies(self.h, b.ctypes.data, len(b), ctypes.c_void_p(stream or 0)))
 
+    def step_host(self, bodies: np.ndarray, dt: float, vel_iters: int = 8, pos_iters: int = 3, n_steps: int = 1,
+                  launch_mode: int = 0, block_threads: int = 0, out: np.ndarray | None = None,
+                  stream: int | None = None) -> np.ndarray:
+        """set_bodies(bodies), step and bodies() in one call through host
+        buffers (gb_batch_step_host): chunks of worlds upload, step and
+        download on streams of their own.  ``out`` may be ``bodies``."""
+        b = np.ascontiguousarray(bodies, dtype=abi.BODY)
+        if len(b) != self.n_bodies:
+            raise ValueError("body count mismatch")
+        if out is None:
+            out = np.zeros(self.n_bodies, dtype=abi.BODY)
+        if out.dtype != abi.BODY or len(out) != self.n_bodies or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous body record array of the batch's length")
+        o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, 0)
+        abi.check(self.lib.gb_batch_step_host(self.h, b.ctypes.data, out.ctypes.data, self.n_bodies, ctypes.byref(o),
+                                              ctypes.c_void_p(stream or 0)))
+        return out
+
     def proxies(self) -> np.ndarray:
         out = np.zeros((self.n_fixtures, 4), dtype=np.float64)
         abi.check(self.lib.gb_batch_get_proxies(self.h, out.ctypes.data, self.n_fixtures, None))

@@ -188,3 +188,55 @@ def test_wide_launch_threshold_never_takes_grid_worlds_f64():
     ref.step(DT, VI, PI, 3, launch_mode=3, block_threads=64)
     g.step(DT, VI, PI, 3, launch_mode=0)
     _same_state(g, ref, "grid world, no wide launch")
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_host_step_in_chunks_matches_upload_step_download(precision):
+    """gb_batch_step_host (chunks of worlds uploading, stepping and
+    downloading on streams of their own) computes what gb_batch_set_bodies,
+    gb_batch_step and gb_batch_get_bodies compute one after the other: with a
+    one-group configuration (four chunks) from pageable and from pinned host
+    memory, in place (one buffer in and out), with three world groups as the
+    chunks, and in a monolithic mapping (the three calls)."""
+    import torch
+    from pypybox2d_gb300.gpu import GpuBatch
+    W, B, F, M = scenes.uneven_batch(len(COUNTS), seed=13, counts=COUNTS)
+    ref = GpuBatch(W, B, F, precision=precision, moves=M)
+    g = GpuBatch(W, B, F, precision=precision, moves=M)
+    for b in (ref, g):
+        b.set_launch_config(3, 64, 0, 512, 1)
+        b.step(DT, VI, PI, 20, launch_mode=0)          # live contacts, bodies asleep and awake
+
+    def three_calls(host, n, mode=0):
+        ref.set_bodies(host)
+        ref.step(DT, VI, PI, n, launch_mode=mode)
+        return ref.bodies()
+
+    host = g.bodies()
+    host["vx"][host["type"] == abi.BODY_DYNAMIC] += 0.25             # an edit on the host between steps
+    out = g.step_host(host, DT, VI, PI, 5)
+    _same(out, three_calls(host, 5), f"{precision} four chunks, pageable")
+    _same_state(g, ref, f"{precision} four chunks, device state")
+
+    pinned = torch.empty(len(out) * abi.BODY.itemsize, dtype=torch.uint8, pin_memory=True)
+    buf = np.frombuffer(pinned.numpy(), dtype=abi.BODY)
+    buf[:] = out
+    buf["w"][buf["type"] == abi.BODY_DYNAMIC] *= 0.5
+    expect = three_calls(buf.copy(), 3)
+    g.step_host(buf, DT, VI, PI, 3, out=buf)
+    _same(buf, expect, f"{precision} four chunks, pinned, in place")
+
+    g.set_launch_config(3, 64, 0, 512, 3)
+    expect = three_calls(buf.copy(), 4)
+    g.step_host(buf, DT, VI, PI, 4, out=buf)
+    _same(buf, expect, f"{precision} three world groups")
+    _same_state(g, ref, f"{precision} three world groups, device state")
+
+    expect = three_calls(buf.copy(), 2, mode=1)
+    g.step_host(buf, DT, VI, PI, 2, launch_mode=1, out=buf)
+    _same(buf, expect, f"{precision} CTA per world")
+    assert not g.status().any() and not ref.status().any()
+    with pytest.raises(ValueError):
+        g.step_host(buf[:-1], DT, VI, PI, 1)
+    g.close()
+    ref.close()
