@@ -27,11 +27,13 @@ Reported (one JSON line on rank 0):
   value    dynamic body-steps/s with the batch resident in HBM (device time,
            CUDA events on the launching stream, max over ranks)
   e2e      the same metric through the C ABI with host buffers: every step
-           uploads the body records from pinned host memory, steps, and reads
-           them back, in one gb_batch_step_host call (chunks of worlds whose
-           copies overlap the other chunks' kernels); ``three_calls_value``
-           is the same round trip as gb_batch_set_bodies, gb_batch_step and
-           gb_batch_get_bodies one after the other
+           uploads the bodies' state records (the fields a step reads and
+           writes) from pinned host memory, steps, and reads them back, in one
+           gb_batch_step_host_state call (chunks of worlds whose copies
+           overlap the other chunks' kernels); ``full_records_value``: the
+           same with whole body records (gb_batch_step_host);
+           ``three_calls_value``: whole records through gb_batch_set_bodies,
+           gb_batch_step and gb_batch_get_bodies one after the other
   roofline HBM roofline of the whole step from the algorithmic bytes per
            world-step (152 B per body + shape bytes + 32 B per fixture + 128 B
            per contact, from live counts) over the event-timed step; the
@@ -605,10 +607,48 @@ def main():
         abi.check(lib.gb_batch_step(batch.h, ctypes.byref(opts), ctypes.c_void_p(sh)))
         abi.check(lib.gb_batch_get_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh)))
 
-    e2e_value = e2e_leg(chunked)
+    pinned_s = torch.empty(n_b * abi.BODY_STATE.itemsize, dtype=torch.uint8, pin_memory=True)
+    host_s = np.frombuffer(pinned_s.numpy(), dtype=abi.BODY_STATE)
+    for name in abi.BODY_STATE.names:
+        if not name.startswith("_pad"):
+            host_s[name] = host[name]
+    ptr_s = pinned_s.data_ptr()
+
+    def chunked_state():  # gb_batch_step_host_state: the fields a step changes, same chunks
+        abi.check(lib.gb_batch_step_host_state(batch.h, ptr_s, ptr_s, n_b, ctypes.byref(opts), ctypes.c_void_p(sh)))
+
+    e2e_value = e2e_leg(chunked_state)
+    restore()
+    e2e_full = e2e_leg(chunked)
     restore()
     host[:] = batch.bodies(stream=sh)
     e2e_three = e2e_leg(three_calls)
+
+    def ms_of(fn, reps=3):
+        ea = torch.cuda.Event(enable_timing=True)
+        eb = torch.cuda.Event(enable_timing=True)
+        fn()                    # untimed: a first copy into a new buffer maps its pages
+        torch.cuda.synchronize()
+        ea.record(stream)
+        for _ in range(reps):
+            fn()
+        eb.record(stream)
+        torch.cuda.synchronize()
+        return ea.elapsed_time(eb) / reps
+
+    # where the round trip's time goes: the bare copies of the records, and
+    # each half of the three-call form (copy plus unpack and candidate-flag
+    # refresh; pack plus copy)
+    restore()
+    dbuf = torch.empty(n_b * abi.BODY.itemsize, dtype=torch.uint8, device=local)
+    h2d_ms = ms_of(lambda: dbuf.copy_(pinned, non_blocking=True))    # torch's current stream is `stream`
+    d2h_ms = ms_of(lambda: pinned.copy_(dbuf, non_blocking=True))
+    host[:] = batch.bodies(stream=sh)
+    set_ms = ms_of(lambda: abi.check(lib.gb_batch_set_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh))))
+    get_ms = ms_of(lambda: abi.check(lib.gb_batch_get_bodies(batch.h, ptr, n_b, ctypes.c_void_p(sh))))
+    del dbuf
+    e2e_breakdown = {"h2d_copy_ms": h2d_ms, "d2h_copy_ms": d2h_ms, "set_bodies_ms": set_ms, "get_bodies_ms": get_ms,
+                     "h2d_gbs": n_b * abi.BODY.itemsize / h2d_ms / 1e6, "d2h_gbs": n_b * abi.BODY.itemsize / d2h_ms / 1e6}
 
     out = {
         "metric": METRIC, "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": steps,
@@ -632,11 +672,13 @@ def main():
                      "traffic_note": "DRAM bytes are measured by ncu on a smaller case and kept in profiles/, "
                                      "not read into this line"},
         "kernels": kernels,
-        "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY.itemsize,
-                "d2h_bytes_per_step": n_b * abi.BODY.itemsize, "steps": e2e_steps,
+        "e2e": {"value": e2e_value, "unit": "body-steps/s", "h2d_bytes_per_step": n_b * abi.BODY_STATE.itemsize,
+                "d2h_bytes_per_step": n_b * abi.BODY_STATE.itemsize, "steps": e2e_steps,
                 "window": "the first steps of the timed window, restored from its snapshot",
-                "entry": "gb_batch_step_host (pinned host buffer in and out, chunks of worlds on streams of their own)",
-                "three_calls_value": e2e_three},
+                "entry": "gb_batch_step_host_state (gb_body_state records, the fields a step reads and writes, from "
+                         "and to one pinned host buffer; chunks of worlds on streams of their own)",
+                "full_records_value": e2e_full, "full_records_bytes_per_step": n_b * abi.BODY.itemsize,
+                "three_calls_value": e2e_three, "breakdown": e2e_breakdown},
         "gpu_launches": launches_per_step(W, cfg["big_bodies"], cfg["groups"]) * steps if eff_mode == 3 else 1,
         "autotune": tune,
         "graph": graph_info,

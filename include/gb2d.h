@@ -134,6 +134,23 @@ typedef struct gb_body {
     double sleep_time;
 } gb_body;
 
+/* The fields of a gb_body that World.step (world.py:307-354) reads and
+ * writes: transform, sweep, velocity, accumulated force and torque, sleep
+ * time and flags.  The others (type, fixtures, local centre, mass and
+ * inertia, damping, gravity scale) are inputs the step only reads; they stay
+ * as gb_batch_create or the last gb_batch_set_bodies left them.  152 bytes
+ * against gb_body's 232. */
+typedef struct gb_body_state {
+    uint32_t flags;          /* GB_BODY_* flags */
+    uint32_t _pad0;
+    double px, py, qc, qs;   /* _xf */
+    double c0x, c0y, cx, cy; /* _sweep.c0, _sweep.c */
+    double a0, a, alpha0;    /* _sweep.a0, _sweep.a, _sweep.alpha0 */
+    double vx, vy, w;        /* _linear_velocity, _angular_velocity */
+    double fx, fy, torque;   /* _force, _torque */
+    double sleep_time;
+} gb_body_state;
+
 /* One fixture with its shape and its single broad-phase proxy
  * (fixture.py:42-71, shapes.py).  Polygons store vertices and the unit edge
  * normals computed by the Polygon vertex setter (shapes.py:442-482); a circle
@@ -321,6 +338,8 @@ int gb_struct_sizes(int32_t *sizes);
 int gb_joint_size(void);
 /* sizeof(gb_controller). */
 int gb_controller_size(void);
+/* sizeof(gb_body_state), for binding checks. */
+int gb_body_state_size(void);
 
 /* One contact event of a step, replayed to the contact listeners after it.
  * `key` orders a world's events: (step of the call) << 48 | phase << 40 |
@@ -361,6 +380,11 @@ int gb_batch_get_bodies(gb_batch *batch, gb_body *bodies, int32_t n_bodies, void
  * row. */
 int gb_batch_step_host(gb_batch *batch, const gb_body *bodies_in, gb_body *bodies_out, int32_t n_bodies,
                        const gb_step_opts *opts, void *cuda_stream);
+/* gb_batch_step_host with gb_body_state records: the same chunks, streams
+ * and results, with the step-invariant body fields left on the device (the
+ * call neither reads nor writes them). */
+int gb_batch_step_host_state(gb_batch *batch, const gb_body_state *states_in, gb_body_state *states_out,
+                             int32_t n_bodies, const gb_step_opts *opts, void *cuda_stream);
 /* Copy the fat AABBs (4 doubles per fixture) to host memory. */
 int gb_batch_get_proxies(gb_batch *batch, double *aabbs, int32_t n_fixtures, void *cuda_stream);
 /* Number of live contacts of every world (n_worlds ints). */

@@ -67,6 +67,17 @@ _BODY_FIELDS = [
 ]
 BODY = np.dtype(_BODY_FIELDS, align=True)
 
+#: gb_body_state: the body fields a step reads and writes (gb_batch_step_host_state)
+BODY_STATE = np.dtype([
+    ("flags", "<u4"), ("_pad0", "<u4"),
+    ("px", "<f8"), ("py", "<f8"), ("qc", "<f8"), ("qs", "<f8"),
+    ("c0x", "<f8"), ("c0y", "<f8"), ("cx", "<f8"), ("cy", "<f8"),
+    ("a0", "<f8"), ("a", "<f8"), ("alpha0", "<f8"),
+    ("vx", "<f8"), ("vy", "<f8"), ("w", "<f8"),
+    ("fx", "<f8"), ("fy", "<f8"), ("torque", "<f8"),
+    ("sleep_time", "<f8"),
+], align=True)
+
 FIXTURE = np.dtype([
     ("body", "<i4"), ("shape_type", "<i4"), ("vertex_count", "<i4"), ("flags", "<u4"),
     ("radius", "<f8"), ("friction", "<f8"), ("restitution", "<f8"), ("density", "<f8"),
@@ -222,7 +233,7 @@ LIB_PATH = os.path.join(_PKG_DIR, "_build", "libgb2d.so")
 EXPORTED = (
     "gb_version", "gb_last_error", "gb_struct_sizes",
     "gb_batch_create", "gb_batch_destroy", "gb_batch_step",
-    "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_step_host", "gb_batch_get_proxies",
+    "gb_batch_set_bodies", "gb_batch_get_bodies", "gb_batch_step_host", "gb_batch_step_host_state", "gb_body_state_size", "gb_batch_get_proxies",
     "gb_batch_get_contact_counts", "gb_batch_get_contacts", "gb_batch_get_solver_order",
     "gb_batch_status", "gb_batch_counters", "gb_batch_phase_clocks",
     "gb_batch_step_static_scratch", "gb_batch_kernel_times", "gb_batch_get_events",
@@ -284,6 +295,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_set_bodies.argtypes = [vp, vp, i32, vp]
     lib.gb_batch_get_bodies.argtypes = [vp, vp, i32, vp]
     lib.gb_batch_step_host.argtypes = [vp, vp, vp, i32, ctypes.POINTER(StepOpts), vp]
+    lib.gb_batch_step_host_state.argtypes = [vp, vp, vp, i32, ctypes.POINTER(StepOpts), vp]
+    lib.gb_body_state_size.argtypes = []
     lib.gb_batch_get_proxies.argtypes = [vp, vp, i32, vp]
     lib.gb_batch_get_contact_counts.argtypes = [vp, i32p, vp]
     lib.gb_batch_get_contacts.argtypes = [vp, i32, vp, i32, i32p, vp]

@@ -227,6 +227,7 @@ const char *gb_version(void) { return "gb2d 0.1 sm_103a"; }
 const char *gb_last_error(void) { return g_err.c_str(); }
 int gb_joint_size(void) { return (int)sizeof(gb_joint); }
 int gb_controller_size(void) { return (int)sizeof(gb_controller); }
+int gb_body_state_size(void) { return (int)sizeof(gb_body_state); }
 
 int gb_struct_sizes(int32_t *sizes) {
     if (!sizes) return fail(GB_E_ARG, "sizes is NULL");
@@ -1397,49 +1398,78 @@ extern "C" int gb_batch_step_static_scratch(gb_batch *b, const gb_step_opts *o, 
 }
 
 // Chunks of gb_batch_step_host when the launch configuration has one world
-// group: enough that the first chunk's upload and the last one's download
-// are short, few enough that each chunk's launches still fill the GPU.
+// group: enough that the last chunk's download is short, few enough that
+// each chunk's launches still fill the GPU.
 static constexpr int kHostChunks = 4;
 
 namespace {
+template <class R> void unpack_range(const Batch<R> &B, const gb_body *d, int b0, int n, cudaStream_t st) {
+    gb_launch_unpack_bodies<R>(B, d, b0, n, st);
+}
+template <class R> void unpack_range(const Batch<R> &B, const gb_body_state *d, int b0, int n, cudaStream_t st) {
+    gb_launch_unpack_states<R>(B, d, b0, n, st);
+}
+template <class R> void pack_range(const Batch<R> &B, gb_body *d, int b0, int n, cudaStream_t st) {
+    gb_launch_pack_bodies<R>(B, d, b0, n, st);
+}
+template <class R> void pack_range(const Batch<R> &B, gb_body_state *d, int b0, int n, cudaStream_t st) {
+    gb_launch_pack_states<R>(B, d, b0, n, st);
+}
+
+// Bodies [b0, b0 + nb) up from the host and into the batch, with the TOI
+// candidate flags of contact slots [s0, s0 + ns) (body types and bullet
+// flags decide them); the stage holds either record kind.
+template <class R, class Rec> cudaError_t upload_range(gb_batch *b, const Batch<R> &B, const Rec *in, int b0, int nb, int s0,
+                                                       int ns, cudaStream_t st) {
+    Rec *stage = reinterpret_cast<Rec *>(b->d_bstage);
+    cudaError_t e = cudaMemcpyAsync(stage + b0, in + b0, sizeof(Rec) * nb, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    unpack_range<R>(B, stage, b0, nb, st);
+    gb_launch_refresh_toi_cand<R>(B, s0, ns, st);
+    return cudaGetLastError();
+}
+
+template <class R, class Rec> cudaError_t download_range(gb_batch *b, const Batch<R> &B, Rec *out, int b0, int nb, cudaStream_t st) {
+    Rec *stage = reinterpret_cast<Rec *>(b->d_bstage);
+    pack_range<R>(B, stage, b0, nb, st);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out + b0, stage + b0, sizeof(Rec) * nb, cudaMemcpyDeviceToHost, st);
+    return e;
+}
+
 // Each chunk on its own stream: upload of its bodies, the refresh of its
 // contacts' TOI candidate flags, its steps, download.  Chunk k's copies
 // overlap the other chunks' kernels (the copy engines run beside the SMs).
-template <class R> int step_host_chunks(gb_batch *b, const Batch<R> &B, const std::vector<WorldGroup> &chunks,
-                                        const gb_body *in, gb_body *out, const StepParams &sp, int n_steps, int mode,
-                                        int threads, cudaStream_t st) {
+template <class R, class Rec> int step_host_chunks(gb_batch *b, const Batch<R> &B, const std::vector<WorldGroup> &chunks,
+                                                   const Rec *in, Rec *out, const StepParams &sp, int n_steps, int mode,
+                                                   int threads, cudaStream_t st) {
     cudaError_t e = cudaEventRecord(b->fork, st);
     for (size_t k = 0; k < chunks.size() && e == cudaSuccess; ++k) {
         const WorldGroup &g = chunks[k];
         e = cudaStreamWaitEvent(g.st, b->fork, 0);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(b->d_bstage + g.b0, in + g.b0, sizeof(gb_body) * g.nb, cudaMemcpyHostToDevice, g.st);
+        if (e == cudaSuccess) e = upload_range<R>(b, B, in, g.b0, g.nb, g.s0, g.ns, g.st);
         if (e != cudaSuccess) break;
-        gb_launch_unpack_bodies<R>(B, b->d_bstage, g.b0, g.nb, g.st);
-        gb_launch_refresh_toi_cand<R>(B, g.s0, g.ns, g.st);
         const int rc = gb_launch_step<R>(group_view(B, g, (int)k), sp, n_steps, g.d_worlds, g.n_list, mode, threads, g.st,
                                          nullptr, nullptr);
         if (rc) return rc;
-        gb_launch_pack_bodies<R>(B, b->d_bstage, g.b0, g.nb, g.st);
-        e = cudaMemcpyAsync(out + g.b0, b->d_bstage + g.b0, sizeof(gb_body) * g.nb, cudaMemcpyDeviceToHost, g.st);
+        e = download_range<R>(b, B, out, g.b0, g.nb, g.st);
         if (e == cudaSuccess) e = cudaEventRecord(g.done, g.st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(st, g.done, 0);
     }
     return (int)e;
 }
-}  // namespace
 
-extern "C" int gb_batch_step_host(gb_batch *b, const gb_body *in, gb_body *out, int32_t n, const gb_step_opts *o,
-                                  void *stream) {
+template <class Rec> int step_host(gb_batch *b, const Rec *in, Rec *out, int32_t n, const gb_step_opts *o, void *stream) {
     if (!b || !o || !in || !out) return fail(GB_E_ARG, "batch, bodies or opts is NULL");
     if (n != b->nb) return fail(GB_E_ARG, "body count mismatch");
     if (o->n_steps < 0 || o->vel_iters < 0 || o->pos_iters < 0) return fail(GB_E_ARG, "negative step count or iterations");
     int mode = 0, threads = 0;
     resolve_mapping(b, o, &mode, &threads);
     if (threads % 32 || threads > 1024) return fail(GB_E_ARG, "block_threads must be a multiple of 32 up to 1024");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool chunked = mode == 3 && !has_grid_worlds(b) && !(o->record_order & (GB_OPT_EVENTS | GB_OPT_KERNEL_TIMES));
     const std::vector<WorldGroup> *chunks = &b->groups;
-    if (mode == 3 && !has_grid_worlds(b) && !(o->record_order & (GB_OPT_EVENTS | GB_OPT_KERNEL_TIMES)) &&
-        b->groups.size() < 2) {
+    if (chunked && b->groups.size() < 2) {
         const int big_from = std::min(b->cfg.big_bodies, (int)GB_HUGE_BODIES);
         if (b->chunks_big != big_from) {
             const int rc = build_groups(b, kHostChunks, big_from, b->chunks);
@@ -1448,15 +1478,20 @@ extern "C" int gb_batch_step_host(gb_batch *b, const gb_body *in, gb_body *out, 
         }
         chunks = &b->chunks;
     }
-    // other mappings, contact events, launch timing, batches of one world:
-    // the three calls one after the other
-    if (mode != 3 || has_grid_worlds(b) || (o->record_order & (GB_OPT_EVENTS | GB_OPT_KERNEL_TIMES)) || chunks->size() < 2) {
-        int rc = gb_batch_set_bodies(b, in, n, stream);
-        if (!rc) rc = gb_batch_step(b, o, stream);
-        if (!rc) rc = gb_batch_get_bodies(b, out, n, stream);
-        return rc;
+    if (!chunked || chunks->size() < 2) {
+        // other mappings, contact events, launch timing, batches of one
+        // world: upload, gb_batch_step and download on the caller's stream
+        cudaError_t e = b->prec == GB_PREC_F64 ? upload_range<double>(b, b->bd, in, 0, b->nb, 0, b->bd.n_slots, st)
+                                               : upload_range<float>(b, b->bf, in, 0, b->nb, 0, b->bf.n_slots, st);
+        if (e != cudaSuccess) return cuda_fail(e, "body upload");
+        const int rc = gb_batch_step(b, o, stream);
+        if (rc) return rc;
+        e = b->prec == GB_PREC_F64 ? download_range<double>(b, b->bd, out, 0, b->nb, st)
+                                   : download_range<float>(b, b->bf, out, 0, b->nb, st);
+        if (e != cudaSuccess) return cuda_fail(e, "body download");
+        CK(cudaStreamSynchronize(st));
+        return 0;
     }
-    cudaStream_t st = (cudaStream_t)stream;
     const StepParams sp = params_of(o);
     const int rc = b->prec == GB_PREC_F64 ? step_host_chunks<double>(b, b->bd, *chunks, in, out, sp, o->n_steps, mode, threads, st)
                                           : step_host_chunks<float>(b, b->bf, *chunks, in, out, sp, o->n_steps, mode, threads, st);
@@ -1465,4 +1500,15 @@ extern "C" int gb_batch_step_host(gb_batch *b, const gb_body *in, gb_body *out, 
     b->counters[0] += 1;
     b->counters[2] += o->n_steps;
     return 0;
+}
+}  // namespace
+
+extern "C" int gb_batch_step_host(gb_batch *b, const gb_body *in, gb_body *out, int32_t n, const gb_step_opts *o,
+                                  void *stream) {
+    return step_host<gb_body>(b, in, out, n, o, stream);
+}
+
+extern "C" int gb_batch_step_host_state(gb_batch *b, const gb_body_state *in, gb_body_state *out, int32_t n,
+                                        const gb_step_opts *o, void *stream) {
+    return step_host<gb_body_state>(b, in, out, n, o, stream);
 }

@@ -58,6 +58,36 @@ __global__ void k_pack_bodies(Batch<GB_REAL> B, gb_body *dst, int b0, int n) {
     dst[i] = s;
 }
 
+__global__ void k_unpack_states(Batch<GB_REAL> B, const gb_body_state *src, int b0, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = b0 + k;
+    const gb_body_state &s = src[i];
+    B.b_flags[i] = s.flags;
+    B.b_xp[i] = mk<double>(s.px, s.py);
+    rot2<double> q; q.c = s.qc; q.s = s.qs; B.b_xq[i] = q;
+    B.b_c[i] = mk<double>(s.cx, s.cy); B.b_c0[i] = mk<double>(s.c0x, s.c0y);
+    B.b_a[i] = s.a; B.b_a0[i] = s.a0; B.b_alpha0[i] = s.alpha0;
+    B.b_v[i] = mk<GB_REAL>((GB_REAL)s.vx, (GB_REAL)s.vy); B.b_w[i] = (GB_REAL)s.w;
+    B.b_f[i] = mk<GB_REAL>((GB_REAL)s.fx, (GB_REAL)s.fy); B.b_torque[i] = (GB_REAL)s.torque;
+    B.b_sleep[i] = s.sleep_time;
+}
+
+__global__ void k_pack_states(Batch<GB_REAL> B, gb_body_state *dst, int b0, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = b0 + k;
+    gb_body_state s;
+    s.flags = B.b_flags[i]; s._pad0 = 0;
+    s.px = B.b_xp[i].x; s.py = B.b_xp[i].y; s.qc = B.b_xq[i].c; s.qs = B.b_xq[i].s;
+    s.c0x = B.b_c0[i].x; s.c0y = B.b_c0[i].y; s.cx = B.b_c[i].x; s.cy = B.b_c[i].y;
+    s.a0 = B.b_a0[i]; s.a = B.b_a[i]; s.alpha0 = B.b_alpha0[i];
+    s.vx = (double)B.b_v[i].x; s.vy = (double)B.b_v[i].y; s.w = (double)B.b_w[i];
+    s.fx = (double)B.b_f[i].x; s.fy = (double)B.b_f[i].y; s.torque = (double)B.b_torque[i];
+    s.sleep_time = B.b_sleep[i];
+    dst[i] = s;
+}
+
 __global__ void k_unpack_fixtures(Batch<GB_REAL> B, const gb_fixture *src, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -353,6 +383,12 @@ template <> void gb_launch_unpack_bodies<GB_REAL>(const Batch<GB_REAL> &B, const
 }
 template <> void gb_launch_pack_bodies<GB_REAL>(const Batch<GB_REAL> &B, gb_body *d, int b0, int n, cudaStream_t st) {
     if (n > 0) k_pack_bodies<<<(n + 255) / 256, 256, 0, st>>>(B, d, b0, n);
+}
+template <> void gb_launch_unpack_states<GB_REAL>(const Batch<GB_REAL> &B, const gb_body_state *d, int b0, int n, cudaStream_t st) {
+    if (n > 0) k_unpack_states<<<(n + 255) / 256, 256, 0, st>>>(B, d, b0, n);
+}
+template <> void gb_launch_pack_states<GB_REAL>(const Batch<GB_REAL> &B, gb_body_state *d, int b0, int n, cudaStream_t st) {
+    if (n > 0) k_pack_states<<<(n + 255) / 256, 256, 0, st>>>(B, d, b0, n);
 }
 template <> void gb_launch_unpack_fixtures<GB_REAL>(const Batch<GB_REAL> &B, const gb_fixture *d, int n, cudaStream_t st) {
     if (n > 0) k_unpack_fixtures<<<(n + 255) / 256, 256, 0, st>>>(B, d, n);

@@ -23,6 +23,8 @@ template <class R> int gb_launch_step(const Batch<R> &B, const StepParams &sp, i
                                       const SideStream *side = nullptr);
 template <class R> void gb_launch_unpack_bodies(const Batch<R> &B, const gb_body *d, int b0, int n, cudaStream_t st);
 template <class R> void gb_launch_pack_bodies(const Batch<R> &B, gb_body *d, int b0, int n, cudaStream_t st);
+template <class R> void gb_launch_unpack_states(const Batch<R> &B, const gb_body_state *d, int b0, int n, cudaStream_t st);
+template <class R> void gb_launch_pack_states(const Batch<R> &B, gb_body_state *d, int b0, int n, cudaStream_t st);
 template <class R> void gb_launch_unpack_fixtures(const Batch<R> &B, const gb_fixture *d, int n, cudaStream_t st);
 template <class R> void gb_launch_unpack_contacts(const Batch<R> &B, const gb_contact *d, const int *slots, int n, cudaStream_t st);
 template <class R> void gb_launch_pack_contacts(const Batch<R> &B, gb_contact *d, int base, int n, cudaStream_t st);
@@ -46,7 +48,11 @@ template <> int gb_launch_step<float>(const Batch<float> &, const StepParams &, 
 template <> void gb_launch_unpack_bodies<double>(const Batch<double> &, const gb_body *, int, int, cudaStream_t);
 template <> void gb_launch_unpack_bodies<float>(const Batch<float> &, const gb_body *, int, int, cudaStream_t);
 template <> void gb_launch_pack_bodies<double>(const Batch<double> &, gb_body *, int, int, cudaStream_t);
+template <> void gb_launch_unpack_states<double>(const Batch<double> &, const gb_body_state *, int, int, cudaStream_t);
+template <> void gb_launch_pack_states<double>(const Batch<double> &, gb_body_state *, int, int, cudaStream_t);
 template <> void gb_launch_pack_bodies<float>(const Batch<float> &, gb_body *, int, int, cudaStream_t);
+template <> void gb_launch_unpack_states<float>(const Batch<float> &, const gb_body_state *, int, int, cudaStream_t);
+template <> void gb_launch_pack_states<float>(const Batch<float> &, gb_body_state *, int, int, cudaStream_t);
 template <> void gb_launch_unpack_fixtures<double>(const Batch<double> &, const gb_fixture *, int, cudaStream_t);
 template <> void gb_launch_unpack_fixtures<float>(const Batch<float> &, const gb_fixture *, int, cudaStream_t);
 template <> void gb_launch_unpack_contacts<double>(const Batch<double> &, const gb_contact *, const int *, int, cudaStream_t);

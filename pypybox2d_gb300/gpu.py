@@ -138,17 +138,21 @@ class GpuBatch:
                   stream: int | None = None) -> np.ndarray:
         """set_bodies(bodies), step and bodies() in one call through host
         buffers (gb_batch_step_host): chunks of worlds upload, step and
-        download on streams of their own.  ``out`` may be ``bodies``."""
-        b = np.ascontiguousarray(bodies, dtype=abi.BODY)
+        download on streams of their own.  ``bodies`` holds abi.BODY records,
+        or abi.BODY_STATE records (gb_batch_step_host_state: the fields a
+        step changes; the others stay on the device).  ``out`` (same record
+        kind) may be ``bodies``."""
+        kind = abi.BODY_STATE if bodies.dtype == abi.BODY_STATE else abi.BODY
+        b = np.ascontiguousarray(bodies, dtype=kind)
         if len(b) != self.n_bodies:
             raise ValueError("body count mismatch")
         if out is None:
-            out = np.zeros(self.n_bodies, dtype=abi.BODY)
-        if out.dtype != abi.BODY or len(out) != self.n_bodies or not out.flags.c_contiguous:
-            raise ValueError("out must be a contiguous body record array of the batch's length")
+            out = np.zeros(self.n_bodies, dtype=kind)
+        if out.dtype != kind or len(out) != self.n_bodies or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous array of the input's record kind and the batch's length")
         o = abi.StepOpts(dt, vel_iters, pos_iters, n_steps, launch_mode, block_threads, 0)
-        abi.check(self.lib.gb_batch_step_host(self.h, b.ctypes.data, out.ctypes.data, self.n_bodies, ctypes.byref(o),
-                                              ctypes.c_void_p(stream or 0)))
+        fn = self.lib.gb_batch_step_host_state if kind is abi.BODY_STATE else self.lib.gb_batch_step_host
+        abi.check(fn(self.h, b.ctypes.data, out.ctypes.data, self.n_bodies, ctypes.byref(o), ctypes.c_void_p(stream or 0)))
         return out
 
     def proxies(self) -> np.ndarray:

@@ -44,6 +44,7 @@ def test_record_layouts_match(lib):
     assert sizes[5] == ctypes.sizeof(abi.StepOpts)
     assert lib.gb_joint_size() == abi.JOINT.itemsize
     assert lib.gb_controller_size() == abi.CONTROLLER.itemsize
+    assert lib.gb_body_state_size() == abi.BODY_STATE.itemsize == 152
 
 
 def test_errors_are_reported_not_silent(lib):

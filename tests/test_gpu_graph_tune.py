@@ -197,7 +197,8 @@ def test_host_step_in_chunks_matches_upload_step_download(precision):
     gb_batch_step and gb_batch_get_bodies compute one after the other: with a
     one-group configuration (four chunks) from pageable and from pinned host
     memory, in place (one buffer in and out), with three world groups as the
-    chunks, and in a monolithic mapping (the three calls)."""
+    chunks, and in a monolithic mapping (the three calls); body state records
+    (gb_batch_step_host_state) give the same fields."""
     import torch
     from pypybox2d_gb300.gpu import GpuBatch
     W, B, F, M = scenes.uneven_batch(len(COUNTS), seed=13, counts=COUNTS)
@@ -232,9 +233,29 @@ def test_host_step_in_chunks_matches_upload_step_download(precision):
     _same(buf, expect, f"{precision} three world groups")
     _same_state(g, ref, f"{precision} three world groups, device state")
 
+    # body state records (gb_batch_step_host_state): the step-invariant
+    # fields stay on the device, the rest goes up and comes back
+    def states(full):
+        st = np.zeros(len(full), abi.BODY_STATE)
+        for name in abi.BODY_STATE.names:
+            if not name.startswith("_pad"):
+                st[name] = full[name]
+        return st
+
+    buf["vy"][buf["type"] == abi.BODY_DYNAMIC] -= 0.125
+    st = states(buf)
+    expect = three_calls(buf.copy(), 3)
+    g.step_host(st, DT, VI, PI, 3, out=st)
+    _same(st, states(expect), f"{precision} state records, three world groups")
+    buf[:] = expect
+
     expect = three_calls(buf.copy(), 2, mode=1)
     g.step_host(buf, DT, VI, PI, 2, launch_mode=1, out=buf)
     _same(buf, expect, f"{precision} CTA per world")
+    st = states(buf)
+    expect = three_calls(buf.copy(), 1, mode=1)
+    g.step_host(st, DT, VI, PI, 1, launch_mode=1, out=st)
+    _same(st, states(expect), f"{precision} state records, CTA per world")
     assert not g.status().any() and not ref.status().any()
     with pytest.raises(ValueError):
         g.step_host(buf[:-1], DT, VI, PI, 1)
