@@ -414,6 +414,17 @@ int gb_batch_set_joints(gb_batch *batch, const gb_joint *joints, int32_t n_joint
  * world, kind and body list range of each controller must be the ones the
  * batch was made with (a changed body list needs a new batch). */
 int gb_batch_set_controllers(gb_batch *batch, const gb_controller *controllers, int32_t n_controllers, void *cuda_stream);
+/* A world's custom contact filter (world.py:123-136: World.contact_filter,
+ * called by contact_manager.py:145 for a new pair and :202 for a contact
+ * flagged for filtering) as its answers: accept[a * n_fixtures + b] != 0
+ * when fixture records a and b (world-local) may collide, for every ordered
+ * pair.  It replaces the default category/mask/group rule for that world;
+ * accept = NULL restores the default.  n_fixtures must be the world's
+ * fixture record count, at most GB_PAIR_FILTER_MAX_FIXTURES.  Refused
+ * (GB_E_UNSUPPORTED) while captured rollouts of the batch exist.  The call
+ * waits for the device's earlier work, then replaces the tables. */
+#define GB_PAIR_FILTER_MAX_FIXTURES 16384
+int gb_batch_set_pair_filter(gb_batch *batch, int32_t world, const uint8_t *accept, int32_t n_fixtures, void *cuda_stream);
 /* Step record of one world's bodies (world-local order) from the last step
  * run with record_order bit 0 set: out[0..n) the decisions of each body,
  * out[n..2n) its island in the solve (the smallest world-local index of the

@@ -132,6 +132,11 @@ struct or_world {
     gb_controller *ctl;
     int nctl;
     int *ctl_bodies;
+    /* a custom contact filter (world.py:123-136) as its answers for every
+     * ordered pair of fixture records: accept[a * accept_n + b], or NULL for
+     * the default rule */
+    unsigned char *accept;
+    int accept_n;
 };
 
 static void rec_add(int *x, int shift, int v) {
@@ -262,6 +267,13 @@ static int default_filter(const gb_fixture *a, const gb_fixture *b) {
     return ((a->mask_bits & b->category_bits) != 0) && ((a->category_bits & b->mask_bits) != 0);
 }
 
+/* contact_manager.py:145,202: the world's contact filter, the default rule
+ * (world.py:958-970) unless a custom filter's answers were given */
+static int pair_filter(const or_world *w, int fa, int fb) {
+    if (w->accept && fa < w->accept_n && fb < w->accept_n) return w->accept[(size_t)fa * w->accept_n + fb] != 0;
+    return default_filter(&w->f[fa], &w->f[fb]);
+}
+
 /* body.py:912-927 _should_collide of body `a` with body `b`: one of them
  * dynamic, and no joint between them that turns collision off */
 static int should_collide(const or_world *w, int a, int b) {
@@ -353,7 +365,7 @@ static void find_new_contacts(or_world *w) {
         }
         if (exists) continue;
         if (!should_collide(w, bb, ba)) continue;
-        if (!default_filter(&w->f[fa], &w->f[fb])) continue;
+        if (!pair_filter(w, fa, fb)) continue;
         create_contact(w, fa, 0, fb, 0);
     }
     free(pairs);
@@ -416,7 +428,7 @@ static void collide(or_world *w) {
         int act_b = body_awake(bb) && bb->type != GB_BODY_STATIC;
         if (!act_a && !act_b) continue;
         if (c->flags & GB_C_FILTER) {
-            if (!should_collide(w, w->f[c->fb].body, w->f[c->fa].body) || !default_filter(&w->f[c->fa], &w->f[c->fb])) {
+            if (!should_collide(w, w->f[c->fb].body, w->f[c->fa].body) || !pair_filter(w, c->fa, c->fb)) {
                 rm[nrm++] = id;
                 continue;
             }
@@ -1190,7 +1202,7 @@ void or_destroy(or_world *w) {
     if (w->bjoint)
         for (int i = 0; i < w->nb; ++i) free(w->bjoint[i].d);
     free(w->bjoint); free(w->j); free(w->jflag); free(w->jhook_rank); free(w->last_jorder.d);
-    free(w->ctl); free(w->ctl_bodies);
+    free(w->ctl); free(w->ctl_bodies); free(w->accept);
     free(w->c); free(w->b); free(w->f);
     free(w);
 }
@@ -1308,6 +1320,21 @@ typedef struct {
     int next;
     pthread_mutex_t mu;
 } or_job;
+
+/* A custom contact filter's answers for every ordered pair of the world's
+ * fixture records (n must be the record count), or accept = NULL for the
+ * default rule again; returns -1 for a wrong count. */
+int or_set_pair_filter(or_world *w, const unsigned char *accept, int n) {
+    if (!accept) { free(w->accept); w->accept = NULL; w->accept_n = 0; return 0; }
+    if (n != w->nf) return -1;
+    unsigned char *m = (unsigned char *)malloc((size_t)n * (size_t)n + 1u);
+    if (!m) return -1;
+    memcpy(m, accept, (size_t)n * (size_t)n);
+    free(w->accept);
+    w->accept = m;
+    w->accept_n = n;
+    return 0;
+}
 
 /* The controllers of a world (World.controllers order) with their body
  * lists: controller k's bodies are bodies[ctl[k].body_start ..

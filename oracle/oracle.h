@@ -48,6 +48,7 @@ void or_clear_status(or_world *w);
  * -1 for a bad body index or type. */
 int or_set_joints(or_world *w, const gb_joint *joints, int n);
 int or_set_controllers(or_world *w, const gb_controller *ctl, int n, const int32_t *bodies, int nbodies);
+int or_set_pair_filter(or_world *w, const unsigned char *accept, int n);
 /* World.add_joint's filter flag on the contacts between joint j's bodies
  * (world.py:275-281; nothing for a joint with collide_connected). */
 void or_flag_joint_contacts(or_world *w, int j);

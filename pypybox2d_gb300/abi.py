@@ -243,7 +243,7 @@ EXPORTED = (
     "gb_batch_snapshot_bytes", "gb_batch_snapshot", "gb_batch_restore", "gb_batch_get_step_record",
     "gb_batch_set_wait_polls", "gb_batch_clear_status",
     "gb_joint_size", "gb_batch_get_joint_order", "gb_batch_get_joints", "gb_batch_set_joints",
-    "gb_controller_size", "gb_batch_set_controllers",
+    "gb_controller_size", "gb_batch_set_controllers", "gb_batch_set_pair_filter",
 )
 
 #: gb_step_opts.record_order bit that records contact events
@@ -329,6 +329,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     lib.gb_batch_set_joints.argtypes = [vp, vp, i32, vp]
     lib.gb_controller_size.argtypes = []
     lib.gb_batch_set_controllers.argtypes = [vp, vp, i32, vp]
+    lib.gb_batch_set_pair_filter.argtypes = [vp, i32, vp, i32, vp]
     for name in EXPORTED:
         if name not in ("gb_version", "gb_last_error"):
             getattr(lib, name).restype = ctypes.c_int

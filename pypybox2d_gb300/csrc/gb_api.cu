@@ -186,6 +186,9 @@ struct gb_batch {
     std::vector<gb_graph *> graphs;  // captured rollouts, disarmed when the batch is destroyed
     char *d_query = nullptr;         // staging of query inputs and outputs, grown on demand
     size_t query_bytes = 0;
+    std::vector<std::vector<unsigned char>> pf;   // custom contact filters' accept tables per world (empty: default)
+    long long *d_pf_off = nullptr;   // their offsets on the device (-1: default rule)
+    unsigned char *d_pf = nullptr;   // the tables
 };
 
 namespace {
@@ -528,6 +531,8 @@ int gb_batch_destroy(gb_batch *b) {
     cudaFree(b->d_ev);
     cudaFree(b->d_ev_n);
     cudaFree(b->d_query);
+    cudaFree(b->d_pf_off);
+    cudaFree(b->d_pf);
     free_groups(b->groups);
     free_groups(b->chunks);
     if (b->fork) cudaEventDestroy(b->fork);
@@ -731,6 +736,40 @@ int gb_batch_set_controllers(gb_batch *b, const gb_controller *controllers, int3
                            cudaMemcpyHostToDevice, st));
     CK(cudaStreamSynchronize(st));
     for (int i = 0; i < n; ++i) b->controllers[i] = controllers[i];
+    return 0;
+}
+
+int gb_batch_set_pair_filter(gb_batch *b, int32_t world, const uint8_t *accept, int32_t n_fixtures, void *stream) {
+    if (!b) return fail(GB_E_ARG, "batch is NULL");
+    if (world < 0 || world >= b->nw) return fail(GB_E_ARG, "world index out of range");
+    if (accept && n_fixtures != b->hdr[world].nf)
+        return fail(GB_E_ARG, "n_fixtures must equal the world's fixture record count");
+    if (accept && n_fixtures > GB_PAIR_FILTER_MAX_FIXTURES)
+        return fail(GB_E_ARG, "a contact filter table holds at most GB_PAIR_FILTER_MAX_FIXTURES fixture records");
+    if (!b->graphs.empty())
+        return fail(GB_E_UNSUPPORTED, "captured rollouts keep the batch's contact filter tables: destroy them first");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (b->pf.empty()) b->pf.resize(b->nw);
+    if (accept) b->pf[world].assign(accept, accept + (size_t)n_fixtures * (size_t)n_fixtures);
+    else b->pf[world].clear();
+    std::vector<long long> off(b->nw, -1);
+    size_t total = 0;
+    for (int i = 0; i < b->nw; ++i)
+        if (!b->pf[i].empty()) { off[i] = (long long)total; total += b->pf[i].size(); }
+    CK(cudaStreamSynchronize(st));
+    CK(cudaDeviceSynchronize());   // steps on other streams may still read the old tables
+    cudaFree(b->d_pf);
+    b->d_pf = nullptr;
+    if (!b->d_pf_off) CK(cudaMalloc((void **)&b->d_pf_off, sizeof(long long) * b->nw));
+    if (total) {
+        CK(cudaMalloc((void **)&b->d_pf, total));
+        for (int i = 0; i < b->nw; ++i)
+            if (!b->pf[i].empty()) CK(cudaMemcpy(b->d_pf + off[i], b->pf[i].data(), b->pf[i].size(), cudaMemcpyHostToDevice));
+    }
+    CK(cudaMemcpy(b->d_pf_off, off.data(), sizeof(long long) * b->nw, cudaMemcpyHostToDevice));
+    const long long *po = total ? b->d_pf_off : nullptr;
+    b->bd.pf_off = b->bf.pf_off = po;
+    b->bd.pf_accept = b->bf.pf_accept = b->d_pf;
     return 0;
 }
 

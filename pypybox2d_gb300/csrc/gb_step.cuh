@@ -111,6 +111,17 @@ template <class R> __device__ __forceinline__ bool default_filter(const WView<R>
     if (ga == gb && ga != 0) return ga > 0;
     return ((w.B.f_mask[w.fb + fa] & w.B.f_cat[w.fb + fb]) != 0) && ((w.B.f_cat[w.fb + fa] & w.B.f_mask[w.fb + fb]) != 0);
 }
+// contact_manager.py:145,202: the world's contact filter.  A custom filter
+// (world.py:123-136) reaches the device as its answers for every ordered
+// pair of the world's fixture records; without one the default rule.
+template <class R> __device__ __forceinline__ bool pair_filter(const WView<R> &w, int fa, int fb) {
+    if (w.B.pf_off) {
+        const long long o = w.B.pf_off[w.wi];
+        if (o >= 0) return w.B.pf_accept[o + (long long)fa * w.H->nf + fb] != 0;
+    }
+    return default_filter(w, fa, fb);
+}
+
 // body.py:912-927 _should_collide: one body dynamic, and no joint between
 // the two that turns collision off (the joint list of body ba)
 template <class R> __device__ __forceinline__ bool should_collide(const WView<R> &w, int ba, int bb) {
@@ -310,7 +321,7 @@ template <class R> __device__ __forceinline__ bool pair_candidate(const WView<R>
         h = (h + 1) & hmask;
     }
     if (!should_collide(w, bb, ba)) return false;
-    if (!default_filter(w, p, q)) return false;
+    if (!pair_filter(w, p, q)) return false;
     bool prim;
     if (!pair_registered(w.B.f_type[w.fb + p], w.B.f_type[w.fb + q], &prim)) return false;
     return true;
@@ -607,7 +618,7 @@ template <class R, bool EV = true> __device__ int collide_one(const WView<R> &w,
     if (!act_a && !act_b) return 0;
     bool destroy = false;
     if (c.flags & GB_C_FILTER) {
-        if (!should_collide(w, bb, ba) || !default_filter(w, c.fa, c.fb)) destroy = true;
+        if (!should_collide(w, bb, ba) || !pair_filter(w, c.fa, c.fb)) destroy = true;
         else c.flags &= ~GB_C_FILTER;
     }
     if (!destroy && !aabb_overlap(w.B.f_aabb[w.fb + c.fa], w.B.f_aabb[w.fb + c.fb])) destroy = true;

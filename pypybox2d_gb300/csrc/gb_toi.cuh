@@ -370,7 +370,7 @@ template <class R, class G> __device__ void toi_find_pairs(const G &g, const WVi
         if (!(w.B.b_flags[w.bb + ba] & w.B.b_flags[w.bb + bb] & GB_BODY_ACTIVE)) return false;   // no proxy
         if (pair_hash_has(hash, hmask, p, q)) return false;
         if (!should_collide(w, bb, ba)) return false;
-        if (!default_filter(w, p, q)) return false;
+        if (!pair_filter(w, p, q)) return false;
         bool prim;
         return pair_registered(w.B.f_type[w.fb + p], w.B.f_type[w.fb + q], &prim);
     };

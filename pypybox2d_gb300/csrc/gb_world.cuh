@@ -181,6 +181,10 @@ template <class R> struct Batch {
     int n_ctl;
     gb_controller *ctl;
     int *ctl_bodies;             // recorded joint order of the last record_order step (per joint slot)
+    // custom contact filters (gb_batch_set_pair_filter): per world the offset
+    // of its accept table in pf_accept (nf x nf bytes), -1 for the default rule
+    const long long *pf_off;
+    const unsigned char *pf_accept;
     // worlds advanced by a cooperative grid (the first n_huge of the size-sorted list)
     int n_huge;
     int huge_ids[GB_MAX_HUGE];

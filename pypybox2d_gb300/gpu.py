@@ -206,6 +206,18 @@ class GpuBatch:
         c = np.ascontiguousarray(controllers, dtype=abi.CONTROLLER)
         abi.check(self.lib.gb_batch_set_controllers(self.h, c.ctypes.data, len(c), None))
 
+    def set_pair_filter(self, world: int, accept: np.ndarray | None) -> None:
+        """A world's custom contact filter as its answers for every ordered
+        pair of its fixture records (an n x n array, nonzero = may collide),
+        or None for the default rule (gb_batch_set_pair_filter)."""
+        if accept is None:
+            abi.check(self.lib.gb_batch_set_pair_filter(self.h, world, None, 0, None))
+            return
+        m = np.ascontiguousarray(accept, dtype=np.uint8)
+        if m.ndim != 2 or m.shape[0] != m.shape[1]:
+            raise ValueError("accept must be a square array over the world's fixture records")
+        abi.check(self.lib.gb_batch_set_pair_filter(self.h, world, m.ctypes.data, m.shape[0], None))
+
     def events(self, world: int = 0) -> np.ndarray:
         """Contact events of one world from the last step call made with
         events=True, in replay order (sorted by key)."""

@@ -840,6 +840,11 @@ def _check_body_args(btype, kw):
         raise ValueError("Invalid body type")
 
 
+
+# World._contact_filter before any filter is set: the reference's default rule
+# (world.py:88-89), applied on the device without a table.
+_DEFAULT_FILTER = object()
+
 class World:
     """world.py:64-473 for the step path, advanced by the GPU library.
 
@@ -857,8 +862,6 @@ class World:
         ContactOverflowError."""
         if sub_stepping:
             raise NotImplementedError("sub_stepping is not supported by the GPU world step")
-        if contact_filter is not None:
-            raise NotImplementedError("a custom contact filter cannot run inside the GPU step")
         self._sb = SceneBuilder(gravity=gravity, do_sleep=do_sleep, warm_starting=warm_starting,
                                 continuous_physics=continuous_physics, auto_clear_forces=auto_clear_forces)
         self._precision = precision
@@ -881,6 +884,10 @@ class World:
         self._upload_joints = False
         self.controllers: list[Controller] = []   # World.controllers (world.py:73), run in this order
         self._ctl_key = None                      # controller kinds and body lists the device batch holds
+        self._contact_filter = _DEFAULT_FILTER    # the contact filter (world.py:88-91, 123-136)
+        self._pf_key = None                       # what the device batch's filter table was made from
+        if contact_filter is not None:
+            self.contact_filter = contact_filter
         self._ctl_params = None                   # and their parameters
         self.joint_destruction_listener = joint_destruction_listener
         self.fixture_destruction_listener = fixture_destruction_listener
@@ -952,13 +959,74 @@ class World:
 
     @property
     def contact_filter(self):
-        """world.py:123-136; only the default filter runs inside the GPU step."""
-        return None
+        """world.py:123-136: called as contact_filter(fixture_a, fixture_b)
+        for a new pair (contact_manager.py:145) and for a contact flagged for
+        filtering (contact_manager.py:202).  A custom filter reaches the GPU
+        step as its answers for every pair of the world's fixtures, asked
+        before the next step and again whenever the filter, the fixtures or
+        their filter data change.  So the filter must answer alike for both
+        orders of a pair and must not depend on other state that changes
+        between steps (set it again after such a change).  None, as in the
+        reference, turns filtering off: every pair may collide."""
+        if self._contact_filter is _DEFAULT_FILTER:
+            return self.default_contact_filter
+        return self._contact_filter
 
     @contact_filter.setter
     def contact_filter(self, fcn):
-        if fcn is not None:
-            raise NotImplementedError("a custom contact filter cannot run inside the GPU step")
+        if fcn is not None and not callable(fcn):
+            raise TypeError("contact_filter must be callable")
+        default = fcn is not None and getattr(fcn, "__func__", fcn) is World.default_contact_filter
+        self._contact_filter = _DEFAULT_FILTER if default else fcn
+        self._pf_key = None if self._gpu is None else ("stale",)
+
+    def _pair_filter_table(self):
+        """The filter's answers for every ordered pair of fixture records
+        (loop children share their fixture's answers; no filter accepts
+        every pair), or None for the default rule."""
+        fn = self._contact_filter
+        if fn is _DEFAULT_FILTER:
+            return None
+        n = len(self._F)
+        if fn is None:
+            return np.ones((n, n), dtype=np.uint8)
+        owners = [self._fixture_at(r) for r in range(n)]
+        uniq, idx = [], []
+        pos = {}
+        for fx in owners:
+            k = id(fx)
+            if k not in pos:
+                pos[k] = len(uniq)
+                uniq.append(fx)
+            idx.append(pos[k])
+        m = len(uniq)
+        T = np.zeros((m, m), dtype=np.uint8)
+        for a in range(m):
+            for b in range(m):
+                T[a, b] = 1 if fn(uniq[a], uniq[b]) else 0
+        ix = np.asarray(idx, dtype=np.int64)
+        return np.ascontiguousarray(T[np.ix_(ix, ix)])
+
+    def _pair_filter_key(self):
+        """What the filter table depends on: the filter, the fixtures in
+        record order and their filter data."""
+        if self._contact_filter is _DEFAULT_FILTER:
+            return None
+        self._materialise()
+        if self._contact_filter is None:
+            return ("off", len(self._F))
+        owners = tuple(id(self._fixture_at(r)) for r in range(len(self._F)))
+        data = self._F[["category_bits", "mask_bits", "group_index"]]
+        return (id(self._contact_filter), owners, tuple(map(tuple, data.tolist())))
+
+    def _sync_pair_filter(self, gpu, world_index=0):
+        """Before a step: the custom filter's table reaches the device batch
+        when it changed (gb_batch_set_pair_filter)."""
+        key = self._pair_filter_key()
+        if key == self._pf_key:
+            return
+        gpu.set_pair_filter(world_index, self._pair_filter_table())
+        self._pf_key = key
 
     @property
     def sub_stepping(self):
@@ -1100,6 +1168,7 @@ class World:
         self._check_mouse_joints(dt)
         self._sync_controllers()
         self._sync_device()
+        self._sync_pair_filter(self._gpu)
         events = cm.wants_events
         self._locked = True
         try:
@@ -1509,6 +1578,7 @@ class World:
             C, cb, key = self._controller_state() if self.controllers else (None, None, None)
             self._gpu = self._make_batch(W, self._B, self._F, self._C, M, self._J, C, cb)
             self._ctl_key, self._ctl_params = key, (C.tobytes() if C is not None else None)
+            self._pf_key = None
             self._host_fresh = True
             self._upload_bodies = False
             self._upload_joints = False
@@ -1879,6 +1949,9 @@ class WorldBatch:
                              controller_bodies=CB)
         self._worlds = worlds
         self._index = {id(w): i for i, w in enumerate(worlds)}
+        for i, w in enumerate(worlds):
+            w._pf_key = None
+            w._sync_pair_filter(self._gpu, i)
         self._ranges = [(int(r["body_start"]), int(r["body_count"]), int(r["fixture_start"]), int(r["fixture_count"]))
                         for r in W]
         self._all = None        # (bodies, fat AABBs) of the whole batch, downloaded once after a step
@@ -2024,6 +2097,9 @@ class WorldBatch:
         velocities, forces, awake flags (motor, limit and spring settings;
         controller parameters)."""
         self._push_controllers()
+        for i, w in enumerate(self._worlds):
+            if w._contact_filter is not _DEFAULT_FILTER or w._pf_key is not None:
+                w._sync_pair_filter(self._gpu, i)
         bodies = any(w._upload_bodies for w in self._worlds)
         joints = any(w._upload_joints for w in self._worlds)
         if not (bodies or joints):

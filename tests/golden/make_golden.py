@@ -989,6 +989,22 @@ def run_api_controllers(b2):
     print(f"api_controllers: {len(api_controllers.SNAPS)} snapshots -> {os.path.getsize(path)} bytes")
 
 
+def run_api_filter(b2):
+    """tests/golden/api_filter.py on the reference -> api_filter.npz."""
+    sys.path.insert(0, HERE)
+    import api_filter
+    out = {}
+
+    def snap(label, world):
+        W, B, F, C = export_world(world, b2)
+        out[f"{label}_bodies"], out[f"{label}_contacts"] = B, C
+
+    api_filter.script(b2, snap, on_world=pair_order_hook)
+    path = os.path.join(HERE, "api_filter.npz")
+    np.savez_compressed(path, **out)
+    print(f"api_filter: {len(api_filter.SNAPS)} snapshots -> {os.path.getsize(path)} bytes")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("GB2D_REFERENCE"), required="GB2D_REFERENCE" not in os.environ,
@@ -1012,6 +1028,8 @@ def main():
         run_api_loops(b2)
     if not args.only or args.only == "api_controllers":
         run_api_controllers(b2)
+    if not args.only or args.only == "api_filter":
+        run_api_filter(b2)
 
 
 if __name__ == "__main__":

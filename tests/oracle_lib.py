@@ -83,6 +83,8 @@ def load(libm: bool = False) -> ctypes.CDLL:
     lib.or_get_joint_order.restype = i32
     lib.or_set_controllers.argtypes = [vp, vp, i32, vp, i32]
     lib.or_set_controllers.restype = i32
+    lib.or_set_pair_filter.argtypes = [vp, vp, i32]
+    lib.or_set_pair_filter.restype = i32
     _libs[libm] = lib
     return lib
 
@@ -133,6 +135,16 @@ class OracleWorld:
         self._ctl = (C, cb)
         assert self.lib.or_set_controllers(self.h, C.ctypes.data if len(C) else None, len(C),
                                            cb.ctypes.data if len(cb) else None, len(cb)) == 0, "bad controller records"
+
+    def set_pair_filter(self, accept):
+        """A custom contact filter's answers over the fixture records (n x n),
+        or None for the default rule (or_set_pair_filter)."""
+        if accept is None:
+            self._pf = None
+            assert self.lib.or_set_pair_filter(self.h, None, 0) == 0
+            return
+        self._pf = np.ascontiguousarray(accept, dtype=np.uint8)
+        assert self.lib.or_set_pair_filter(self.h, self._pf.ctypes.data, self._pf.shape[0]) == 0, "bad filter table"
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -209,6 +221,9 @@ class OracleBatch:
 
     def query_aabb(self, q, max_per_query):
         return query_aabb_records(self.o.fixtures(), q, max_per_query, libm=self.libm)
+
+    def set_pair_filter(self, world, accept):
+        self.o.set_pair_filter(accept)
 
     def ray_cast(self, r):
         return ray_cast_records(self.o.bodies(), self.o.fixtures(), r, libm=self.libm)

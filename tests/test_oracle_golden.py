@@ -17,7 +17,7 @@ from pypybox2d_gb300 import abi
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 SCENES = sorted(os.path.splitext(os.path.basename(p))[0] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
-                if not p.endswith(("api_script.npz", "api_joints.npz", "api_active.npz", "api_loops.npz", "api_controllers.npz", "api_joints2.npz",
+                if not p.endswith(("api_script.npz", "api_joints.npz", "api_active.npz", "api_loops.npz", "api_controllers.npz", "api_joints2.npz", "api_filter.npz",
                                   "queries.npz")))   # own tests
 
 

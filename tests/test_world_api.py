@@ -57,8 +57,11 @@ def test_construction_matches_reference():
 def test_unsupported_features_raise():
     with pytest.raises(NotImplementedError):
         b2.World(sub_stepping=True)
-    with pytest.raises(NotImplementedError):
-        b2.World(contact_filter=lambda a, b: True)
+    w = b2.World((0, -10), True)
+    w.contact_manager.pre_solve = lambda contact, old_manifold: None
+    w.create_dynamic_body(position=(0, 1)).create_circle_fixture(0.5, density=1.0)
+    with pytest.raises(NotImplementedError):      # pre_solve would run inside the step
+        w.step(1 / 60, 8, 3)
 
 
 def test_pre_step_edits_stay_on_the_host():

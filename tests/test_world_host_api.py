@@ -55,10 +55,9 @@ def test_default_contact_filter():
     for a, b, want in cases:
         assert b2.World.default_contact_filter(a, b) is want
     w = b2.World()
+    assert w.contact_filter is b2.World.default_contact_filter   # world.py:88-89
+    w.contact_filter = None                                      # no filtering (contact_manager.py:145)
     assert w.contact_filter is None
-    w.contact_filter = None
-    with pytest.raises(NotImplementedError):
-        w.contact_filter = lambda a, b: True
 
 
 def test_create_fixtures_and_destroy_fixture_match_reference():
